@@ -1,0 +1,165 @@
+/*
+ * qhg_gpu.h - C ABI of the GB300 implementation of QHG4's per-step agent
+ * hot path (libqhg_gpu.so).
+ *
+ * One handle (qhg_run) holds one simulation: the cell grid and the agents
+ * live in device memory (HBM) between calls.  A step is the reference's
+ * PopLooper::doStep (core/PopLooper.cpp:166-200) for one population:
+ * initializeStep (rates, pairing), doActions over all priority levels,
+ * finalizeStep (births, deaths, moves, per-cell counts).
+ *
+ * The entry points replace, in the reference:
+ *   qhg_gpu_create         SPopulation<T>::SPopulation + the action objects and
+ *                          Prioritizer set-up (core/SPopulation.cpp:44-84,
+ *                          core/SPopulation.cpp:247-261 setPrioList,
+ *                          populations/tut_SexualPop.cpp:24-43)
+ *   qhg_gpu_upload_grid    SCellGrid neighbour table (core/SCellGrid.h:45-57,
+ *                          core/SCell.h:4-12) and the K / weight arrays
+ *                          (actions/VerhulstVarK.cpp:29, actions/SingleEvaluator.cpp:174-241)
+ *   qhg_gpu_upload_agents  SPopulation<T>::addAgent / setAgentBasic
+ *                          (core/SPopulation.cpp:1149, 1254) for a whole table
+ *   qhg_gpu_step           PopLooper::doStep (core/PopLooper.cpp:166-200):
+ *                          SPopulation<T>::initializeStep (core/SPopulation.cpp:394),
+ *                          doActions (:554), finalizeStep (:439) with
+ *                          recycleDeadSpaceNew (:596), performMoves (:1058),
+ *                          updateNumAgentsPerCell (:509)
+ *   qhg_gpu_download       the agent table as SPopulation<T>::writeAgentDataQDFSafe
+ *                          (core/SPopulation.cpp:1465) collects it
+ *   qhg_gpu_counts         SPopulation<T>::getNumAgentsArray (core/SPopulation.h:142)
+ *   qhg_gpu_destroy        SPopulation<T>::~SPopulation (core/SPopulation.cpp:94)
+ *
+ * Rules: every call returns an int status (QHG_OK = 0, negative = error;
+ * qhg_gpu_last_error() describes the last error of the calling thread).
+ * Buffers passed in are host memory owned by the caller and are not kept.
+ * A handle is used by one host thread at a time.  Nothing throws across the
+ * ABI.  Random draws are Philox4x32-10 keyed by (seed, step, agent ID,
+ * action), so results do not depend on launch shapes or memory layout.
+ */
+#ifndef QHG_GPU_H
+#define QHG_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define QHG_OK                  0
+#define QHG_ERR_ARG            -1   /* invalid argument */
+#define QHG_ERR_CUDA           -2   /* CUDA runtime error */
+#define QHG_ERR_NOMEM          -3   /* device or host allocation failed */
+#define QHG_ERR_STATE          -4   /* call out of order (e.g. step before upload) */
+#define QHG_ERR_CELL_TOO_LARGE -5   /* a cell holds more agents than QHG_MAX_CELL_AGENTS */
+#define QHG_ERR_TIMEOUT        -6   /* a device-side wait gave up (bounded spin) */
+#define QHG_ERR_CAPACITY       -7   /* agent or genome capacity exhausted */
+#define QHG_ERR_DEVICE         -8   /* a kernel reported an inconsistency */
+
+/* action type codes (reference class names in parentheses) */
+#define QHG_ACT_GETOLD        0  /* GetOld        actions/GetOld.cpp:37-48 */
+#define QHG_ACT_FERTILITY     1  /* Fertility     actions/Fertility.cpp:49-73 */
+#define QHG_ACT_RANDOMPAIR    2  /* RandomPair    actions/RandomPair.cpp:107-270 */
+#define QHG_ACT_VERHULST      3  /* Verhulst      actions/Verhulst.cpp:70-121 */
+#define QHG_ACT_VERHULSTVARK  4  /* VerhulstVarK  actions/VerhulstVarK.cpp:69-111 */
+#define QHG_ACT_OLDAGEDEATH   5  /* OldAgeDeath   actions/OldAgeDeath.cpp:48-67 */
+#define QHG_ACT_RANDOMMOVE    6  /* RandomMove    actions/RandomMove.cpp:65-100 */
+#define QHG_ACT_WEIGHTEDMOVE  7  /* WeightedMove  actions/WeightedMove.cpp:45-106 */
+
+#define QHG_MAX_ACTIONS       16
+#define QHG_MAX_CELL_AGENTS   1024   /* agents one cell may hold */
+#define QHG_CROSSOVER_POISSON1 (-100) /* Poisson(1) breakpoints per parent */
+
+/* life states stored in the agent table (core/SPopulation.h:69-73) */
+#define QHG_LS_ALIVE          1
+#define QHG_LS_FERTILE        5
+
+/* flags of qhg_run_desc */
+#define QHG_FLAG_LOG_BIRTHS   1u   /* keep a (baby, mother, father) ID log */
+
+typedef struct qhg_run qhg_run;
+
+/*
+ * Description of one population.  Actions are given in execution order:
+ * ascending priority, ties in alphabetical order of the reference class
+ * name (the order SPopulation::setPrioList produces).  Parameter slots:
+ *   FERTILITY     {min_age, max_age, interbirth}
+ *   VERHULST      {b0, d0, theta, K}
+ *   VERHULSTVARK  {b0, d0, theta}            (K per cell from the grid)
+ *   OLDAGEDEATH   {max_age, uncertainty}
+ *   RANDOMMOVE    {prob}
+ *   WEIGHTEDMOVE  {prob}                     (weights: the grid's K, cumulated)
+ */
+typedef struct {
+    uint64_t seed;
+    int32_t  n_actions;
+    int32_t  action_type[QHG_MAX_ACTIONS];
+    double   action_param[QHG_MAX_ACTIONS][4];
+    int32_t  genome_size;      /* loci per strand, 0 = no genetics */
+    int32_t  num_crossover;    /* > 0 fixed count, 0 none, QHG_CROSSOVER_POISSON1 */
+    double   mutation_rate;    /* per locus */
+    int64_t  agent_capacity;   /* agent slots to allocate (0: 4 x initial + 65536) */
+    uint32_t flags;            /* QHG_FLAG_* */
+    int32_t  device;           /* CUDA device ordinal */
+} qhg_run_desc;
+
+/* agent table, structure of arrays; genome is n x (2 * ceil(genome_size/64))
+ * words, strand 0 then strand 1 (actions/Genetics.h m_aGenome layout) */
+typedef struct {
+    int64_t  *id;
+    int32_t  *cell;
+    float    *birth;
+    float    *age;
+    float    *last_birth;
+    uint8_t  *gender;
+    uint8_t  *state;
+    uint64_t *genome;
+} qhg_agents_soa;
+
+/* per-step statistics */
+typedef struct {
+    uint64_t live;     /* agents alive after the step */
+    uint64_t births;
+    uint64_t deaths;
+    uint64_t moves;    /* registered moves */
+} qhg_step_stats;
+
+const char *qhg_gpu_last_error(void);
+const char *qhg_gpu_version(void);
+
+int qhg_gpu_create(const qhg_run_desc *desc, qhg_run **out);
+int qhg_gpu_upload_grid(qhg_run *run, const int32_t *nbr6, const uint8_t *nnbr, const double *K,
+                        int32_t num_cells);
+/* agents in any order; dead rows (state 0) are dropped */
+int qhg_gpu_upload_agents(qhg_run *run, const qhg_agents_soa *agents, int64_t n, int32_t first_step);
+/* runs nsteps steps asynchronously on the run's stream */
+int qhg_gpu_step(qhg_run *run, int32_t nsteps);
+/* waits for the run's stream and reports device-side errors */
+int qhg_gpu_sync(qhg_run *run);
+int qhg_gpu_num_agents(qhg_run *run, int64_t *n);
+int qhg_gpu_current_step(qhg_run *run, int32_t *step);
+/* agents ordered by cell (device order); cap = room in the caller's arrays */
+int qhg_gpu_download(qhg_run *run, qhg_agents_soa *out, int64_t cap, int64_t *n);
+int qhg_gpu_counts(qhg_run *run, uint32_t *cell_counts);
+/* statistics of the last `nsteps` steps (nsteps <= 1024) */
+int qhg_gpu_stats(qhg_run *run, int32_t nsteps, qhg_step_stats *out);
+/* birth log (QHG_FLAG_LOG_BIRTHS): rows (baby, mother, father) */
+int qhg_gpu_birth_log(qhg_run *run, int64_t *baby, int64_t *mother, int64_t *father, int64_t cap,
+                      int64_t *n);
+/* the run's CUDA stream (cudaStream_t) */
+int qhg_gpu_stream(qhg_run *run, void **stream);
+int qhg_gpu_destroy(qhg_run *run);
+
+/*
+ * Timing helpers for the benchmark: the duration, measured with CUDA events
+ * on the run's stream, of the kernels of the last qhg_gpu_step call, summed
+ * per kernel kind (0 actions, 1 cell scan, 2 scatter, 3 genomes), in ms.
+ * Only filled when the run was created with QHG_FLAG_KERNEL_TIMING.
+ */
+#define QHG_FLAG_KERNEL_TIMING 2u
+int qhg_gpu_kernel_times(qhg_run *run, float *ms4);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

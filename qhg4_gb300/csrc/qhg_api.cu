@@ -1,0 +1,660 @@
+// Host side of the C ABI declared in include/qhg_gpu.h.
+//
+// Compiled with -ffp-contract=off: the per-action constants below (the
+// OldAgeDeath window, the move-probability thresholds, the WeightedMove
+// weight thresholds) must round exactly like the reference's expressions.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "qhg_device.cuh"
+#include "../../include/qhg_gpu.h"
+
+extern "C" int qhg_launch_step(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
+                               int cell_grid, cudaStream_t stream);
+extern "C" int qhg_launch_step_timed(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
+                                     int cell_grid, cudaStream_t stream, cudaEvent_t *ev);
+
+using namespace qhg;
+
+static thread_local std::string g_last_error;
+
+static int fail(int code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define CUDA_TRY(expr)                                                                  \
+    do {                                                                                \
+        cudaError_t e_ = (expr);                                                        \
+        if (e_ != cudaSuccess) {                                                        \
+            return fail(e_ == cudaErrorMemoryAllocation ? QHG_ERR_NOMEM : QHG_ERR_CUDA, \
+                        std::string(#expr) + ": " + cudaGetErrorString(e_));           \
+        }                                                                               \
+    } while (0)
+
+struct qhg_run {
+    qhg_run_desc desc;
+    cudaStream_t stream = nullptr;
+    StepConst P;
+    // grid
+    int C = 0;
+    int32_t *d_nbr = nullptr;
+    uint8_t *d_nnbr = nullptr;
+    int32_t *d_rev = nullptr;
+    double *d_K = nullptr;
+    uint64_t *d_wthr = nullptr;
+    uint8_t *d_wflag = nullptr;
+    std::vector<int32_t> h_nbr;
+    // agents (ping-pong)
+    uint32_t cap = 0;
+    int64_t *d_id[2] = {nullptr, nullptr};
+    float *d_birth[2] = {nullptr, nullptr};
+    float *d_age[2] = {nullptr, nullptr};
+    float *d_lastb[2] = {nullptr, nullptr};
+    uint8_t *d_meta[2] = {nullptr, nullptr};
+    uint32_t *d_cs[2] = {nullptr, nullptr};
+    uint32_t *d_ne[2] = {nullptr, nullptr};
+    // scratch
+    uint8_t *d_outc = nullptr;
+    int32_t *d_father = nullptr;
+    uint16_t *d_brank = nullptr;
+    uint32_t *d_clsc = nullptr, *d_sbase = nullptr, *d_bbase = nullptr, *d_bidb = nullptr, *d_obase = nullptr;
+    uint32_t *d_tflag = nullptr;
+    uint4 *d_tagg = nullptr, *d_tincl = nullptr;
+    int64_t *d_blog = nullptr;
+    uint64_t blog_cap = 0;
+    RunState *d_rs = nullptr;
+    RunState *h_rs = nullptr;   // pinned
+    // step state
+    int cur = 0;                 // table holding the current step
+    int32_t upload_step = 0;
+    bool grid_ok = false, agents_ok = false;
+    int cell_grid = 0;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    cudaEvent_t ev[8];
+    bool events = false;
+    float ktimes[4] = {0, 0, 0, 0};
+};
+
+static void free_agents(qhg_run *r) {
+    for (int p = 0; p < 2; p++) {
+        cudaFree(r->d_id[p]); cudaFree(r->d_birth[p]); cudaFree(r->d_age[p]); cudaFree(r->d_lastb[p]);
+        cudaFree(r->d_meta[p]); cudaFree(r->d_cs[p]); cudaFree(r->d_ne[p]);
+        r->d_id[p] = nullptr; r->d_birth[p] = r->d_age[p] = r->d_lastb[p] = nullptr;
+        r->d_meta[p] = nullptr; r->d_cs[p] = r->d_ne[p] = nullptr;
+    }
+    cudaFree(r->d_outc); cudaFree(r->d_father); cudaFree(r->d_brank); cudaFree(r->d_blog);
+    r->d_outc = nullptr; r->d_father = nullptr; r->d_brank = nullptr; r->d_blog = nullptr;
+    r->cap = 0;
+}
+
+static void drop_graphs(qhg_run *r) {
+    for (int p = 0; p < 2; p++) {
+        if (r->graph[p]) cudaGraphExecDestroy(r->graph[p]);
+        r->graph[p] = nullptr;
+    }
+}
+
+// u < thr  <=>  u / 2^32 < x   (exact: u / 2^32 is exact in double)
+static uint64_t host_prob_threshold(double x) {
+    if (!(x > 0.0)) return 0ull;
+    double y = x * 4294967296.0;
+    if (y >= 4294967296.0) return 4294967296ull;
+    return (uint64_t)std::ceil(y);
+}
+
+// largest float f with (double)f <= x
+static float float_floor_of(double x) {
+    float f = (float)x;
+    if ((double)f > x) f = std::nextafter(f, -INFINITY);
+    return f;
+}
+
+extern "C" const char *qhg_gpu_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" const char *qhg_gpu_version(void) { return "qhg_gpu 0.1 (sm_103a)"; }
+
+extern "C" int qhg_gpu_create(const qhg_run_desc *desc, qhg_run **out) {
+    if (desc == nullptr || out == nullptr) return fail(QHG_ERR_ARG, "null argument");
+    if (desc->n_actions < 0 || desc->n_actions > QHG_MAX_ACTIONS) return fail(QHG_ERR_ARG, "bad n_actions");
+    if (desc->genome_size < 0) return fail(QHG_ERR_ARG, "bad genome_size");
+    if (desc->genome_size > 0) return fail(QHG_ERR_ARG, "genetics is not supported by this build");
+    int ndev = 0;
+    CUDA_TRY(cudaGetDeviceCount(&ndev));
+    if (desc->device < 0 || desc->device >= ndev) return fail(QHG_ERR_ARG, "bad device ordinal");
+    CUDA_TRY(cudaSetDevice(desc->device));
+    qhg_run *r = new qhg_run();
+    r->desc = *desc;
+    StepConst &P = r->P;
+    memset(&P, 0, sizeof(P));
+    P.seed = desc->seed;
+    P.n_act = desc->n_actions;
+    P.log_births = (desc->flags & QHG_FLAG_LOG_BIRTHS) ? 1 : 0;
+    uint32_t w = 0;
+    for (int a = 0; a < desc->n_actions; a++) {
+        ActionConst &A = P.act[a];
+        const double *p = desc->action_param[a];
+        A.type = desc->action_type[a];
+        A.window = w;
+        switch (A.type) {
+        case kGetOld:
+            P.age_from_birth = 1;
+            break;
+        case kFertility:
+            A.f0 = (float)p[0]; A.f1 = (float)p[1]; A.f2 = (float)p[2];
+            break;
+        case kRandomPair:
+            P.has_pair = 1;
+            break;
+        case kVerhulst:
+        case kVerhulstVarK:
+            A.b0 = p[0]; A.d0 = p[1]; A.th = p[2];
+            A.th_b0 = p[2] - p[0];
+            A.th_d0 = p[2] - p[1];
+            A.K = p[3];
+            w += 2;
+            break;
+        case kOldAgeDeath: {
+            // OldAgeDeath::execute (actions/OldAgeDeath.cpp:57-60):
+            // age > M + wrandr(1 - U*M, 1 + U*M)
+            const double M = p[0], U = p[1];
+            const double a = 1 - U * M;
+            const double b = 1 + U * M;
+            const double wd = b - a;
+            A.oad_M = M; A.oad_a = a; A.oad_w = wd;
+            const double g0 = M + (a + (wd * 0.0) / 4294967296.0);
+            const double g1 = M + (a + (wd * 4294967295.0) / 4294967296.0);
+            A.age_lo = float_floor_of(g0);
+            A.age_hi = float_floor_of(g1);
+            P.age_from_birth = 1;
+            w += 1;
+            break;
+        }
+        case kRandomMove:
+        case kWeightedMove:
+            A.pthr = host_prob_threshold(p[0]);
+            w += 2;
+            break;
+        default:
+            delete r;
+            return fail(QHG_ERR_ARG, "unknown action type");
+        }
+    }
+    if (w > 4 * 64) {
+        delete r;
+        return fail(QHG_ERR_ARG, "too many draws per agent");
+    }
+    cudaError_t e = cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&r->d_rs, sizeof(RunState));
+    if (e == cudaSuccess) e = cudaMallocHost(&r->h_rs, sizeof(RunState));
+    if (e != cudaSuccess) {
+        if (r->stream) cudaStreamDestroy(r->stream);
+        cudaFree(r->d_rs);
+        delete r;
+        return fail(QHG_ERR_CUDA, std::string("create: ") + cudaGetErrorString(e));
+    }
+    memset(r->h_rs, 0, sizeof(RunState));
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, desc->device);
+    r->cell_grid = std::max(1, nsm) * 8;
+    if (desc->flags & QHG_FLAG_KERNEL_TIMING) {
+        for (int i = 0; i < 8; i++) cudaEventCreate(&r->ev[i]);
+        r->events = true;
+    }
+    *out = r;
+    return QHG_OK;
+}
+
+extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_t *nnbr, const double *K,
+                                   int32_t num_cells) {
+    if (r == nullptr || nbr6 == nullptr || nnbr == nullptr || K == nullptr || num_cells <= 0) {
+        return fail(QHG_ERR_ARG, "bad grid arguments");
+    }
+    CUDA_TRY(cudaSetDevice(r->desc.device));
+    const int C = num_cells;
+    std::vector<int32_t> rev((size_t)C * 6, 0);
+    for (int c = 0; c < C; c++) {
+        if (nnbr[c] > 6) return fail(QHG_ERR_ARG, "more than 6 neighbours");
+        for (int j = 0; j < 6; j++) {
+            const int d = nbr6[(size_t)c * 6 + j];
+            if (d >= C || d < -1) return fail(QHG_ERR_ARG, "neighbour index out of range");
+            if (j >= nnbr[c] || d < 0) continue;
+            int k = -1;
+            for (int q = 0; q < nnbr[d]; q++) {
+                if (nbr6[(size_t)d * 6 + q] == c) { k = q; break; }
+            }
+            if (k < 0) return fail(QHG_ERR_ARG, "neighbour table is not symmetric");
+            rev[(size_t)c * 6 + j] = k;
+        }
+    }
+    // WeightedMove: cumulated weights (SingleEvaluator, actions/SingleEvaluator.cpp:174-241)
+    // turned into integer thresholds: dR2 = wrandd()*W[n] < W[j]  <=>  u < T_j
+    std::vector<uint64_t> wthr((size_t)C * 6, 0);
+    std::vector<uint8_t> wflag(C, 0);
+    bool has_wm = false;
+    for (int a = 0; a < r->P.n_act; a++) has_wm |= (r->P.act[a].type == kWeightedMove);
+    if (has_wm) {
+        std::vector<double> W((size_t)C * 7);
+        for (int c = 0; c < C; c++) {
+            const double dV = K[c];
+            W[(size_t)c * 7] = (dV > 0) ? dV : 0;
+        }
+        for (int c = 0; c < C; c++) {
+            double dW = W[(size_t)c * 7];
+            for (int i = 0; i < 6; i++) {
+                double dCW = 0;
+                const int ni = nbr6[(size_t)c * 6 + i];
+                if (ni >= 0) dCW = W[(size_t)ni * 7];
+                dCW = (dCW > 0) ? dCW : 0;
+                dW = dW + dCW;
+                W[(size_t)c * 7 + i + 1] = dW;
+            }
+        }
+        for (int c = 0; c < C; c++) {
+            const int nn = nnbr[c];
+            const double *Wc = &W[(size_t)c * 7];
+            const double Wn = Wc[nn];
+            if (Wc[0] == Wn) {
+                wflag[c] = 1;
+                continue;
+            }
+            auto f = [&](uint64_t u) { return ((1.0 * (double)u) / 4294967296.0) * Wn; };
+            for (int j = 0; j < nn; j++) {
+                const double x = Wc[j];
+                // smallest u in [0, 2^32] with f(u) >= x  (f(2^32) counts as +inf)
+                double g = std::floor(x / Wn * 4294967296.0);
+                uint64_t u = (g <= 0) ? 0ull : (g >= 4294967296.0 ? 4294967296ull : (uint64_t)g);
+                while (u > 0 && f(u - 1) >= x) u--;
+                while (u < 4294967296ull && f(u) < x) u++;
+                wthr[(size_t)c * 6 + j] = u;
+            }
+        }
+    }
+    cudaFree(r->d_nbr); cudaFree(r->d_nnbr); cudaFree(r->d_rev); cudaFree(r->d_K);
+    cudaFree(r->d_wthr); cudaFree(r->d_wflag);
+    cudaFree(r->d_clsc); cudaFree(r->d_sbase); cudaFree(r->d_bbase); cudaFree(r->d_bidb);
+    cudaFree(r->d_obase); cudaFree(r->d_tflag); cudaFree(r->d_tagg); cudaFree(r->d_tincl);
+    r->grid_ok = false;
+    r->agents_ok = false;
+    drop_graphs(r);
+    const int ntiles = (C + kScanTile - 1) / kScanTile;
+    CUDA_TRY(cudaMalloc(&r->d_nbr, (size_t)C * 6 * sizeof(int32_t)));
+    CUDA_TRY(cudaMalloc(&r->d_nnbr, (size_t)C));
+    CUDA_TRY(cudaMalloc(&r->d_rev, (size_t)C * 6 * sizeof(int32_t)));
+    CUDA_TRY(cudaMalloc(&r->d_K, (size_t)C * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&r->d_wthr, (size_t)C * 6 * sizeof(uint64_t)));
+    CUDA_TRY(cudaMalloc(&r->d_wflag, (size_t)C));
+    CUDA_TRY(cudaMalloc(&r->d_clsc, (size_t)C * kCls * sizeof(uint32_t)));
+    CUDA_TRY(cudaMalloc(&r->d_sbase, (size_t)C * sizeof(uint32_t)));
+    CUDA_TRY(cudaMalloc(&r->d_bbase, (size_t)C * sizeof(uint32_t)));
+    CUDA_TRY(cudaMalloc(&r->d_bidb, (size_t)C * sizeof(uint32_t)));
+    CUDA_TRY(cudaMalloc(&r->d_obase, (size_t)C * 6 * sizeof(uint32_t)));
+    CUDA_TRY(cudaMalloc(&r->d_tflag, (size_t)ntiles * sizeof(uint32_t)));
+    CUDA_TRY(cudaMalloc(&r->d_tagg, (size_t)ntiles * sizeof(uint4)));
+    CUDA_TRY(cudaMalloc(&r->d_tincl, (size_t)ntiles * sizeof(uint4)));
+    CUDA_TRY(cudaMemcpyAsync(r->d_nbr, nbr6, (size_t)C * 6 * sizeof(int32_t), cudaMemcpyHostToDevice, r->stream));
+    CUDA_TRY(cudaMemcpyAsync(r->d_nnbr, nnbr, (size_t)C, cudaMemcpyHostToDevice, r->stream));
+    CUDA_TRY(cudaMemcpyAsync(r->d_rev, rev.data(), (size_t)C * 6 * sizeof(int32_t), cudaMemcpyHostToDevice, r->stream));
+    CUDA_TRY(cudaMemcpyAsync(r->d_K, K, (size_t)C * sizeof(double), cudaMemcpyHostToDevice, r->stream));
+    CUDA_TRY(cudaMemcpyAsync(r->d_wthr, wthr.data(), (size_t)C * 6 * sizeof(uint64_t), cudaMemcpyHostToDevice, r->stream));
+    CUDA_TRY(cudaMemcpyAsync(r->d_wflag, wflag.data(), (size_t)C, cudaMemcpyHostToDevice, r->stream));
+    CUDA_TRY(cudaMemsetAsync(r->d_tflag, 0, (size_t)ntiles * sizeof(uint32_t), r->stream));
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    r->h_nbr.assign(nbr6, nbr6 + (size_t)C * 6);
+    r->C = C;
+    r->P.num_cells = C;
+    r->grid_ok = true;
+    return QHG_OK;
+}
+
+static int alloc_agents(qhg_run *r, uint32_t cap) {
+    free_agents(r);
+    const int C = r->C;
+    for (int p = 0; p < 2; p++) {
+        CUDA_TRY(cudaMalloc(&r->d_id[p], (size_t)cap * sizeof(int64_t)));
+        CUDA_TRY(cudaMalloc(&r->d_birth[p], (size_t)cap * sizeof(float)));
+        CUDA_TRY(cudaMalloc(&r->d_age[p], (size_t)cap * sizeof(float)));
+        CUDA_TRY(cudaMalloc(&r->d_lastb[p], (size_t)cap * sizeof(float)));
+        CUDA_TRY(cudaMalloc(&r->d_meta[p], (size_t)cap));
+        CUDA_TRY(cudaMalloc(&r->d_cs[p], (size_t)(C + 1) * sizeof(uint32_t)));
+        CUDA_TRY(cudaMalloc(&r->d_ne[p], (size_t)C * sizeof(uint32_t)));
+    }
+    CUDA_TRY(cudaMalloc(&r->d_outc, (size_t)cap));
+    CUDA_TRY(cudaMalloc(&r->d_father, (size_t)cap * sizeof(int32_t)));
+    CUDA_TRY(cudaMalloc(&r->d_brank, (size_t)cap * sizeof(uint16_t)));
+    if (r->P.log_births) {
+        r->blog_cap = std::max<uint64_t>(1u << 20, (uint64_t)cap * 4);
+        CUDA_TRY(cudaMalloc(&r->d_blog, r->blog_cap * 3 * sizeof(int64_t)));
+    } else {
+        r->blog_cap = 0;
+    }
+    r->cap = cap;
+    r->P.capacity = cap;
+    return QHG_OK;
+}
+
+extern "C" int qhg_gpu_upload_agents(qhg_run *r, const qhg_agents_soa *a, int64_t n, int32_t first_step) {
+    if (r == nullptr || a == nullptr || n < 0) return fail(QHG_ERR_ARG, "bad agent arguments");
+    if (!r->grid_ok) return fail(QHG_ERR_STATE, "upload the grid before the agents");
+    if (n > 0 && (a->id == nullptr || a->cell == nullptr || a->birth == nullptr || a->age == nullptr ||
+                  a->last_birth == nullptr || a->gender == nullptr || a->state == nullptr)) {
+        return fail(QHG_ERR_ARG, "null agent column");
+    }
+    if (first_step < 0) return fail(QHG_ERR_ARG, "negative first step");
+    CUDA_TRY(cudaSetDevice(r->desc.device));
+    const int C = r->C;
+    // live rows, ordered by (cell, id)
+    std::vector<uint32_t> cnt((size_t)C + 1, 0);
+    int64_t live = 0;
+    int64_t maxid = -1;
+    for (int64_t i = 0; i < n; i++) {
+        if (a->state[i] == 0) continue;
+        const int32_t c = a->cell[i];
+        if (c < 0 || c >= C) return fail(QHG_ERR_ARG, "agent cell out of range");
+        cnt[(size_t)c + 1]++;
+        live++;
+        maxid = std::max<int64_t>(maxid, a->id[i]);
+    }
+    for (int c = 0; c < C; c++) {
+        if (cnt[(size_t)c + 1] > (uint32_t)kMaxCell) {
+            return fail(QHG_ERR_CELL_TOO_LARGE, "a cell holds more than QHG_MAX_CELL_AGENTS agents");
+        }
+        cnt[(size_t)c + 1] += cnt[(size_t)c];
+    }
+    uint64_t want = r->desc.agent_capacity > 0 ? (uint64_t)r->desc.agent_capacity : (uint64_t)live * 4 + 65536;
+    if (want < (uint64_t)live) want = (uint64_t)live;
+    if (want > 0x7fffffffull) return fail(QHG_ERR_CAPACITY, "agent capacity above 2^31-1");
+    std::vector<int64_t> order((size_t)live);
+    {
+        std::vector<uint32_t> pos(cnt.begin(), cnt.end() - 1);
+        for (int64_t i = 0; i < n; i++) {
+            if (a->state[i] == 0) continue;
+            order[pos[a->cell[i]]++] = i;
+        }
+        for (int c = 0; c < C; c++) {
+            std::sort(order.begin() + cnt[c], order.begin() + cnt[(size_t)c + 1],
+                      [&](int64_t x, int64_t y) { return a->id[x] < a->id[y]; });
+        }
+    }
+    std::vector<int64_t> h_id((size_t)live);
+    std::vector<float> h_birth((size_t)live), h_age((size_t)live), h_lastb((size_t)live);
+    std::vector<uint8_t> h_meta((size_t)live);
+    for (int64_t k = 0; k < live; k++) {
+        const int64_t i = order[(size_t)k];
+        h_id[(size_t)k] = a->id[i];
+        h_birth[(size_t)k] = a->birth[i];
+        h_age[(size_t)k] = a->age[i];
+        h_lastb[(size_t)k] = a->last_birth[i];
+        h_meta[(size_t)k] = (uint8_t)((a->gender[i] & 1u) | (a->state[i] == QHG_LS_FERTILE ? kMetaFertile : 0));
+    }
+    std::vector<uint32_t> ne;
+    for (int c = 0; c < C; c++) {
+        if (cnt[(size_t)c + 1] != cnt[(size_t)c]) ne.push_back((uint32_t)c);
+    }
+    drop_graphs(r);
+    r->agents_ok = false;
+    if (r->cap != (uint32_t)want || r->d_id[0] == nullptr) {
+        int rc = alloc_agents(r, (uint32_t)want);
+        if (rc != QHG_OK) return rc;
+    }
+    r->cur = 0;
+    r->upload_step = first_step;
+    if (live > 0) {
+        CUDA_TRY(cudaMemcpyAsync(r->d_id[0], h_id.data(), live * sizeof(int64_t), cudaMemcpyHostToDevice, r->stream));
+        CUDA_TRY(cudaMemcpyAsync(r->d_birth[0], h_birth.data(), live * sizeof(float), cudaMemcpyHostToDevice, r->stream));
+        CUDA_TRY(cudaMemcpyAsync(r->d_age[0], h_age.data(), live * sizeof(float), cudaMemcpyHostToDevice, r->stream));
+        CUDA_TRY(cudaMemcpyAsync(r->d_lastb[0], h_lastb.data(), live * sizeof(float), cudaMemcpyHostToDevice, r->stream));
+        CUDA_TRY(cudaMemcpyAsync(r->d_meta[0], h_meta.data(), live, cudaMemcpyHostToDevice, r->stream));
+    }
+    CUDA_TRY(cudaMemcpyAsync(r->d_cs[0], cnt.data(), (size_t)(C + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, r->stream));
+    if (!ne.empty()) {
+        CUDA_TRY(cudaMemcpyAsync(r->d_ne[0], ne.data(), ne.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, r->stream));
+    }
+    memset(r->h_rs, 0, sizeof(RunState));
+    r->h_rs->step = first_step;
+    r->h_rs->n_agents = (uint32_t)live;
+    r->h_rs->next_id = maxid + 1;
+    r->h_rs->n_nonempty = (uint32_t)ne.size();
+    CUDA_TRY(cudaMemcpyAsync(r->d_rs, r->h_rs, sizeof(RunState), cudaMemcpyHostToDevice, r->stream));
+    const int ntiles = (C + kScanTile - 1) / kScanTile;
+    CUDA_TRY(cudaMemsetAsync(r->d_tflag, 0, (size_t)ntiles * sizeof(uint32_t), r->stream));
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    r->agents_ok = true;
+    return QHG_OK;
+}
+
+static StepBuffers make_buffers(qhg_run *r, int cur) {
+    const int nx = cur ^ 1;
+    StepBuffers B;
+    B.cell_start = r->d_cs[cur]; B.nonempty = r->d_ne[cur];
+    B.id = r->d_id[cur]; B.birth = r->d_birth[cur]; B.age = r->d_age[cur]; B.lastb = r->d_lastb[cur];
+    B.meta = r->d_meta[cur];
+    B.cell_start2 = r->d_cs[nx]; B.nonempty2 = r->d_ne[nx];
+    B.id2 = r->d_id[nx]; B.birth2 = r->d_birth[nx]; B.age2 = r->d_age[nx]; B.lastb2 = r->d_lastb[nx];
+    B.meta2 = r->d_meta[nx];
+    B.nbr = r->d_nbr; B.nnbr = r->d_nnbr; B.rev = r->d_rev; B.K = r->d_K; B.wthr = r->d_wthr;
+    B.wflag = r->d_wflag;
+    B.outc = r->d_outc; B.father = r->d_father; B.brank = r->d_brank; B.clsc = r->d_clsc;
+    B.sbase = r->d_sbase; B.bbase = r->d_bbase; B.bidbase = r->d_bidb; B.obase = r->d_obase;
+    B.tile_flag = r->d_tflag; B.tile_agg = r->d_tagg; B.tile_incl = r->d_tincl;
+    B.blog = r->d_blog; B.blog_cap = r->blog_cap;
+    return B;
+}
+
+static int build_graph(qhg_run *r, int cur) {
+    StepBuffers B = make_buffers(r, cur);
+    cudaGraph_t g = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal));
+    int le = qhg_launch_step(&r->P, r->d_rs, &B, r->cell_grid, r->stream);
+    cudaError_t ee = cudaStreamEndCapture(r->stream, &g);
+    if (le != 0 || ee != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return fail(QHG_ERR_CUDA, std::string("graph capture failed: ") +
+                                      cudaGetErrorString(le != 0 ? (cudaError_t)le : ee));
+    }
+    cudaError_t ie = cudaGraphInstantiate(&r->graph[cur], g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) return fail(QHG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+    return QHG_OK;
+}
+
+extern "C" int qhg_gpu_step(qhg_run *r, int32_t nsteps) {
+    if (r == nullptr || nsteps < 0) return fail(QHG_ERR_ARG, "bad step arguments");
+    if (!r->grid_ok || !r->agents_ok) return fail(QHG_ERR_STATE, "upload grid and agents first");
+    CUDA_TRY(cudaSetDevice(r->desc.device));
+    for (int i = 0; i < 4; i++) r->ktimes[i] = 0.0f;
+    for (int32_t s = 0; s < nsteps; s++) {
+        if (r->events) {
+            StepBuffers B = make_buffers(r, r->cur);
+            int le = qhg_launch_step_timed(&r->P, r->d_rs, &B, r->cell_grid, r->stream, r->ev);
+            if (le != 0) return fail(QHG_ERR_CUDA, std::string("launch: ") + cudaGetErrorString((cudaError_t)le));
+            CUDA_TRY(cudaEventSynchronize(r->ev[3]));
+            for (int k = 0; k < 3; k++) {
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, r->ev[k], r->ev[k + 1]);
+                r->ktimes[k] += ms;
+            }
+        } else {
+            if (r->graph[r->cur] == nullptr) {
+                int rc = build_graph(r, r->cur);
+                if (rc != QHG_OK) return rc;
+            }
+            CUDA_TRY(cudaGraphLaunch(r->graph[r->cur], r->stream));
+        }
+        r->cur ^= 1;
+    }
+    return QHG_OK;
+}
+
+// reads the run state; on a device-side error the run keeps the last
+// committed step and its counters are reset so that stepping can resume
+static int pull_state(qhg_run *r) {
+    CUDA_TRY(cudaMemcpyAsync(r->h_rs, r->d_rs, sizeof(RunState), cudaMemcpyDeviceToHost, r->stream));
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    r->cur = (int)((uint32_t)(r->h_rs->step - r->upload_step) & 1u);
+    if (r->h_rs->error != 0u) {
+        const uint32_t code = r->h_rs->error, info = r->h_rs->error_info;
+        r->h_rs->error = 0u;
+        r->h_rs->error_info = 0u;
+        r->h_rs->scan_tiles_started = 0u;
+        r->h_rs->scatter_ctas_done = 0u;
+        // the failed step's partial statistics would be counted again on retry
+        unsigned long long *st = r->h_rs->stats[(uint32_t)r->h_rs->step % kStatsRing];
+        st[0] = st[1] = st[2] = st[3] = 0ull;
+        CUDA_TRY(cudaMemcpyAsync(r->d_rs, r->h_rs, sizeof(RunState), cudaMemcpyHostToDevice, r->stream));
+        const int ntiles = (r->C + kScanTile - 1) / kScanTile;
+        CUDA_TRY(cudaMemsetAsync(r->d_tflag, 0, (size_t)ntiles * sizeof(uint32_t), r->stream));
+        CUDA_TRY(cudaStreamSynchronize(r->stream));
+        char buf[160];
+        switch (code) {
+        case kErrCellTooLarge:
+            snprintf(buf, sizeof(buf), "cell %u would hold more than %d agents (step %d kept)", info, kMaxCell, r->h_rs->step);
+            return fail(QHG_ERR_CELL_TOO_LARGE, buf);
+        case kErrCapacity:
+            snprintf(buf, sizeof(buf), "%u agents exceed the capacity %u (step %d kept)", info, r->cap, r->h_rs->step);
+            return fail(QHG_ERR_CAPACITY, buf);
+        case kErrTimeout:
+            snprintf(buf, sizeof(buf), "cell scan look-back gave up at tile %u (step %d kept)", info, r->h_rs->step);
+            return fail(QHG_ERR_TIMEOUT, buf);
+        default:
+            snprintf(buf, sizeof(buf), "device error %u/%u (step %d kept)", code, info, r->h_rs->step);
+            return fail(QHG_ERR_DEVICE, buf);
+        }
+    }
+    return QHG_OK;
+}
+
+extern "C" int qhg_gpu_sync(qhg_run *r) {
+    if (r == nullptr) return fail(QHG_ERR_ARG, "null run");
+    CUDA_TRY(cudaSetDevice(r->desc.device));
+    return pull_state(r);
+}
+
+extern "C" int qhg_gpu_num_agents(qhg_run *r, int64_t *n) {
+    if (r == nullptr || n == nullptr) return fail(QHG_ERR_ARG, "null argument");
+    int rc = qhg_gpu_sync(r);
+    if (rc != QHG_OK) return rc;
+    *n = r->agents_ok ? (int64_t)r->h_rs->n_agents : 0;
+    return QHG_OK;
+}
+
+extern "C" int qhg_gpu_current_step(qhg_run *r, int32_t *step) {
+    if (r == nullptr || step == nullptr) return fail(QHG_ERR_ARG, "null argument");
+    int rc = qhg_gpu_sync(r);
+    if (rc != QHG_OK) return rc;
+    *step = r->h_rs->step;
+    return QHG_OK;
+}
+
+extern "C" int qhg_gpu_download(qhg_run *r, qhg_agents_soa *o, int64_t cap, int64_t *n) {
+    if (r == nullptr || o == nullptr || n == nullptr) return fail(QHG_ERR_ARG, "null argument");
+    if (!r->agents_ok) return fail(QHG_ERR_STATE, "no agents uploaded");
+    int rc = qhg_gpu_sync(r);
+    if (rc != QHG_OK) return rc;
+    const int64_t N = r->h_rs->n_agents;
+    *n = N;
+    if (cap < N) return fail(QHG_ERR_ARG, "output arrays too small");
+    const int cur = r->cur;
+    std::vector<uint32_t> cs((size_t)r->C + 1);
+    std::vector<uint8_t> meta((size_t)N);
+    CUDA_TRY(cudaMemcpy(cs.data(), r->d_cs[cur], cs.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (N > 0) {
+        CUDA_TRY(cudaMemcpy(o->id, r->d_id[cur], N * sizeof(int64_t), cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpy(o->birth, r->d_birth[cur], N * sizeof(float), cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpy(o->age, r->d_age[cur], N * sizeof(float), cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpy(o->last_birth, r->d_lastb[cur], N * sizeof(float), cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpy(meta.data(), r->d_meta[cur], N, cudaMemcpyDeviceToHost));
+    }
+    for (int c = 0; c < r->C; c++) {
+        for (uint32_t i = cs[c]; i < cs[(size_t)c + 1]; i++) o->cell[i] = c;
+    }
+    for (int64_t i = 0; i < N; i++) {
+        o->gender[i] = meta[(size_t)i] & kMetaGender;
+        o->state[i] = (meta[(size_t)i] & kMetaFertile) ? QHG_LS_FERTILE : QHG_LS_ALIVE;
+    }
+    return QHG_OK;
+}
+
+extern "C" int qhg_gpu_counts(qhg_run *r, uint32_t *counts) {
+    if (r == nullptr || counts == nullptr) return fail(QHG_ERR_ARG, "null argument");
+    if (!r->agents_ok) return fail(QHG_ERR_STATE, "no agents uploaded");
+    int rc = qhg_gpu_sync(r);
+    if (rc != QHG_OK) return rc;
+    std::vector<uint32_t> cs((size_t)r->C + 1);
+    CUDA_TRY(cudaMemcpy(cs.data(), r->d_cs[r->cur], cs.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    for (int c = 0; c < r->C; c++) counts[c] = cs[(size_t)c + 1] - cs[c];
+    return QHG_OK;
+}
+
+extern "C" int qhg_gpu_stats(qhg_run *r, int32_t nsteps, qhg_step_stats *out) {
+    if (r == nullptr || out == nullptr || nsteps < 0 || nsteps > kStatsRing) return fail(QHG_ERR_ARG, "bad stats arguments");
+    int rc = qhg_gpu_sync(r);
+    if (rc != QHG_OK) return rc;
+    const int32_t st = r->h_rs->step;
+    for (int32_t k = 0; k < nsteps; k++) {
+        const uint32_t s = (uint32_t)(st - nsteps + k);
+        const unsigned long long *v = r->h_rs->stats[s % kStatsRing];
+        out[k].live = v[0]; out[k].births = v[1]; out[k].deaths = v[2]; out[k].moves = v[3];
+    }
+    return QHG_OK;
+}
+
+extern "C" int qhg_gpu_birth_log(qhg_run *r, int64_t *baby, int64_t *mother, int64_t *father, int64_t cap,
+                                 int64_t *n) {
+    if (r == nullptr || n == nullptr) return fail(QHG_ERR_ARG, "null argument");
+    if (!r->P.log_births) return fail(QHG_ERR_STATE, "run was created without QHG_FLAG_LOG_BIRTHS");
+    int rc = qhg_gpu_sync(r);
+    if (rc != QHG_OK) return rc;
+    const uint64_t total = r->h_rs->birth_log_n;
+    *n = (int64_t)total;
+    if (total > r->blog_cap) return fail(QHG_ERR_CAPACITY, "birth log overflowed");
+    if ((uint64_t)cap < total) return fail(QHG_ERR_ARG, "output arrays too small");
+    std::vector<int64_t> tmp(total * 3);
+    if (total > 0) {
+        CUDA_TRY(cudaMemcpy(tmp.data(), r->d_blog, total * 3 * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    }
+    for (uint64_t i = 0; i < total; i++) {
+        baby[i] = tmp[i * 3]; mother[i] = tmp[i * 3 + 1]; father[i] = tmp[i * 3 + 2];
+    }
+    return QHG_OK;
+}
+
+extern "C" int qhg_gpu_stream(qhg_run *r, void **stream) {
+    if (r == nullptr || stream == nullptr) return fail(QHG_ERR_ARG, "null argument");
+    *stream = (void *)r->stream;
+    return QHG_OK;
+}
+
+extern "C" int qhg_gpu_kernel_times(qhg_run *r, float *ms4) {
+    if (r == nullptr || ms4 == nullptr) return fail(QHG_ERR_ARG, "null argument");
+    if (!r->events) return fail(QHG_ERR_STATE, "run was created without QHG_FLAG_KERNEL_TIMING");
+    for (int i = 0; i < 4; i++) ms4[i] = r->ktimes[i];
+    return QHG_OK;
+}
+
+extern "C" int qhg_gpu_destroy(qhg_run *r) {
+    if (r == nullptr) return QHG_OK;
+    cudaSetDevice(r->desc.device);
+    if (r->stream) cudaStreamSynchronize(r->stream);
+    drop_graphs(r);
+    free_agents(r);
+    cudaFree(r->d_nbr); cudaFree(r->d_nnbr); cudaFree(r->d_rev); cudaFree(r->d_K);
+    cudaFree(r->d_wthr); cudaFree(r->d_wflag);
+    cudaFree(r->d_clsc); cudaFree(r->d_sbase); cudaFree(r->d_bbase); cudaFree(r->d_bidb);
+    cudaFree(r->d_obase); cudaFree(r->d_tflag); cudaFree(r->d_tagg); cudaFree(r->d_tincl);
+    cudaFree(r->d_rs);
+    cudaFreeHost(r->h_rs);
+    if (r->events) {
+        for (int i = 0; i < 8; i++) cudaEventDestroy(r->ev[i]);
+    }
+    if (r->stream) cudaStreamDestroy(r->stream);
+    delete r;
+    return QHG_OK;
+}

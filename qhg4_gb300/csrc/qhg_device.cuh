@@ -1,0 +1,135 @@
+// Device-side definitions shared by the kernels and the host API of
+// libqhg_gpu.so: the Philox4x32-10 generator, the per-run state kept in
+// device memory, and the per-step constants passed to every kernel.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace qhg {
+
+// ---------------------------------------------------------------- layout
+constexpr int kMaxActions = 16;
+constexpr int kMaxCell = 512;            // agents one cell may hold (per-warp shared buffers)
+constexpr int kWarpsPerCta = 4;          // cell kernels: one warp per cell
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;            // cells per thread in the cell scan
+constexpr int kScanTile = kScanThreads * kScanItems;
+constexpr int kStatsRing = 1024;
+constexpr uint32_t kSpinLimit = 1u << 24;  // bounded waits in the look-back
+
+// random stream bases (Philox counter word 0), see oracle/philox4x32.h
+constexpr uint32_t kStreamActions = 0u;
+constexpr uint32_t kStreamPair = 64u;
+constexpr uint32_t kStreamBirth = 128u;
+
+// agent meta byte: bit 0 gender, bit 1 fertile (life state 5, else 1)
+constexpr uint8_t kMetaGender = 1u;
+constexpr uint8_t kMetaFertile = 2u;
+
+// outcome byte of a step: bits 0-2 class (0 dead, 1 stay, 2..7 moved to
+// neighbour slot class-2), bit 3 gives birth, bit 4 fertile, bit 5 gender
+constexpr uint8_t kOutBirth = 8u;
+constexpr uint8_t kOutFertile = 16u;
+constexpr uint8_t kOutGender = 32u;
+
+// per-cell class counts: [0] stay, [1..6] movers per neighbour slot, [7] births
+constexpr int kCls = 8;
+
+enum ActionType : int32_t {
+    kGetOld = 0, kFertility = 1, kRandomPair = 2, kVerhulst = 3, kVerhulstVarK = 4,
+    kOldAgeDeath = 5, kRandomMove = 6, kWeightedMove = 7
+};
+
+enum ErrorCode : uint32_t {
+    kErrNone = 0, kErrCellTooLarge = 1, kErrTimeout = 2, kErrCapacity = 3, kErrInternal = 4
+};
+
+// constants of one action, prepared on the host
+struct ActionConst {
+    int32_t type;
+    uint32_t window;        // first draw of the action in the per-agent stream
+    float f0, f1, f2;       // Fertility: min age, max age, interbirth
+    float age_lo, age_hi;   // OldAgeDeath: float bounds of the uncertain age window
+    double b0, d0, th;      // Verhulst
+    double th_b0, th_d0;    // theta - b0, theta - d0
+    double K;               // Verhulst constant K
+    double oad_M, oad_a, oad_w;  // OldAgeDeath: max age, 1 - U*M, (1+U*M) - (1-U*M)
+    uint64_t pthr;          // RandomMove / WeightedMove: u < pthr  <=>  u/2^32 < p
+};
+
+struct StepConst {
+    uint64_t seed;
+    int32_t n_act;
+    int32_t age_from_birth;  // GetOld or OldAgeDeath runs: a survivor's age is t - birth
+    int32_t has_pair;
+    int32_t num_cells;
+    int32_t log_births;
+    int32_t genome_words;    // 2 * blocks, 0 without genetics
+    uint32_t capacity;
+    ActionConst act[kMaxActions];
+};
+
+// per-run scalars in device memory
+struct RunState {
+    int32_t step;            // time of the next step is (float)step
+    uint32_t n_agents;
+    int64_t next_id;
+    uint32_t n_nonempty;
+    uint32_t error;          // first error (ErrorCode)
+    uint32_t error_info;
+    uint32_t scan_tiles_started;
+    uint32_t scatter_ctas_done;
+    // written by the cell scan, committed when the scatter finishes
+    uint32_t new_n_agents;
+    uint32_t new_n_nonempty;
+    uint32_t births;
+    uint64_t birth_log_n;
+    // statistics ring: [step % kStatsRing][live, births, deaths, moves]
+    unsigned long long stats[kStatsRing][4];
+};
+
+// device pointers of one step: the current table, the next table, the
+// grid and the step's scratch arrays
+struct StepBuffers {
+    const uint32_t *cell_start; const uint32_t *nonempty;
+    const int64_t *id; const float *birth; const float *age; const float *lastb; const uint8_t *meta;
+    uint32_t *cell_start2; uint32_t *nonempty2;
+    int64_t *id2; float *birth2; float *age2; float *lastb2; uint8_t *meta2;
+    const int32_t *nbr; const uint8_t *nnbr; const int32_t *rev; const double *K;
+    const uint64_t *wthr; const uint8_t *wflag;
+    uint8_t *outc; int32_t *father; uint16_t *brank; uint32_t *clsc;
+    uint32_t *sbase; uint32_t *bbase; uint32_t *bidbase; uint32_t *obase;
+    uint32_t *tile_flag; uint4 *tile_agg; uint4 *tile_incl;
+    int64_t *blog; uint64_t blog_cap;
+};
+
+// ------------------------------------------------------------- Philox
+struct Draw4 { uint32_t v[4]; };
+
+__device__ __forceinline__ Draw4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                               uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        uint32_t lo0 = 0xD2511F53u * c0;
+        uint32_t hi0 = __umulhi(0xD2511F53u, c0);
+        uint32_t lo1 = 0xCD9E8D57u * c2;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2);
+        uint32_t n0 = hi1 ^ c1 ^ k0;
+        uint32_t n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    Draw4 d;
+    d.v[0] = c0; d.v[1] = c1; d.v[2] = c2; d.v[3] = c3;
+    return d;
+}
+
+// the block `blk` of the stream (seed, step, id)
+__device__ __forceinline__ Draw4 draw_block(uint64_t seed, uint32_t step, int64_t id, uint32_t blk) {
+    uint64_t u = (uint64_t)id;
+    return philox4x32_10(blk, step, (uint32_t)u, (uint32_t)(u >> 32), (uint32_t)seed, (uint32_t)(seed >> 32));
+}
+
+}  // namespace qhg

@@ -1,0 +1,236 @@
+"""ctypes binding of libqhg_gpu.so (include/qhg_gpu.h).
+
+``GpuRun`` holds one simulation on the GPU.  There is no CPU fallback: if
+the library cannot be loaded or no CUDA device is present, every call
+raises.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import os
+from typing import Sequence
+
+import numpy as np
+
+from .spec import Action, Genetics, MAX_ACTIONS, execution_order
+from .workload import Agents, Grid
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libqhg_gpu.so")
+
+QHG_FLAG_LOG_BIRTHS = 1
+QHG_FLAG_KERNEL_TIMING = 2
+
+ERRORS = {
+    -1: "QHG_ERR_ARG", -2: "QHG_ERR_CUDA", -3: "QHG_ERR_NOMEM", -4: "QHG_ERR_STATE",
+    -5: "QHG_ERR_CELL_TOO_LARGE", -6: "QHG_ERR_TIMEOUT", -7: "QHG_ERR_CAPACITY", -8: "QHG_ERR_DEVICE",
+}
+
+#: every symbol include/qhg_gpu.h declares
+EXPORTS = [
+    "qhg_gpu_last_error", "qhg_gpu_version", "qhg_gpu_create", "qhg_gpu_upload_grid",
+    "qhg_gpu_upload_agents", "qhg_gpu_step", "qhg_gpu_sync", "qhg_gpu_num_agents",
+    "qhg_gpu_current_step", "qhg_gpu_download", "qhg_gpu_counts", "qhg_gpu_stats",
+    "qhg_gpu_birth_log", "qhg_gpu_stream", "qhg_gpu_destroy", "qhg_gpu_kernel_times",
+]
+
+
+class QhgError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class RunDesc(ct.Structure):
+    _fields_ = [
+        ("seed", ct.c_uint64),
+        ("n_actions", ct.c_int32),
+        ("action_type", ct.c_int32 * MAX_ACTIONS),
+        ("action_param", (ct.c_double * 4) * MAX_ACTIONS),
+        ("genome_size", ct.c_int32),
+        ("num_crossover", ct.c_int32),
+        ("mutation_rate", ct.c_double),
+        ("agent_capacity", ct.c_int64),
+        ("flags", ct.c_uint32),
+        ("device", ct.c_int32),
+    ]
+
+
+class AgentsSoA(ct.Structure):
+    _fields_ = [("id", ct.c_void_p), ("cell", ct.c_void_p), ("birth", ct.c_void_p), ("age", ct.c_void_p),
+                ("last_birth", ct.c_void_p), ("gender", ct.c_void_p), ("state", ct.c_void_p),
+                ("genome", ct.c_void_p)]
+
+
+class StepStats(ct.Structure):
+    _fields_ = [("live", ct.c_uint64), ("births", ct.c_uint64), ("deaths", ct.c_uint64), ("moves", ct.c_uint64)]
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Loads libqhg_gpu.so (building it first if it is absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        from .build import build
+        build()
+    lib = ct.CDLL(path)
+    P = ct.c_void_p
+    I = ct.c_int
+    sig = {
+        "qhg_gpu_last_error": (ct.c_char_p, []),
+        "qhg_gpu_version": (ct.c_char_p, []),
+        "qhg_gpu_create": (I, [P, P]),
+        "qhg_gpu_upload_grid": (I, [P, P, P, P, ct.c_int32]),
+        "qhg_gpu_upload_agents": (I, [P, P, ct.c_int64, ct.c_int32]),
+        "qhg_gpu_step": (I, [P, ct.c_int32]),
+        "qhg_gpu_sync": (I, [P]),
+        "qhg_gpu_num_agents": (I, [P, P]),
+        "qhg_gpu_current_step": (I, [P, P]),
+        "qhg_gpu_download": (I, [P, P, ct.c_int64, P]),
+        "qhg_gpu_counts": (I, [P, P]),
+        "qhg_gpu_stats": (I, [P, ct.c_int32, P]),
+        "qhg_gpu_birth_log": (I, [P, P, P, P, ct.c_int64, P]),
+        "qhg_gpu_stream": (I, [P, P]),
+        "qhg_gpu_destroy": (I, [P]),
+        "qhg_gpu_kernel_times": (I, [P, P]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        raise QhgError(rc, _lib.qhg_gpu_last_error().decode())
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(ct.c_void_p)
+
+
+def make_desc(actions: Sequence[Action], seed: int, genetics: Genetics = Genetics(), capacity: int = 0,
+              flags: int = 0, device: int = 0) -> RunDesc:
+    ordered = execution_order(actions)
+    if len(ordered) > MAX_ACTIONS:
+        raise ValueError("too many actions")
+    d = RunDesc()
+    d.seed = int(seed)
+    d.n_actions = len(ordered)
+    for i, a in enumerate(ordered):
+        d.action_type[i] = int(a.type)
+        for k, v in enumerate(a.params4()):
+            d.action_param[i][k] = float(v)
+    d.genome_size = int(genetics.genome_size)
+    d.num_crossover = int(genetics.num_crossover)
+    d.mutation_rate = float(genetics.mutation_rate)
+    d.agent_capacity = int(capacity)
+    d.flags = int(flags)
+    d.device = int(device)
+    return d
+
+
+class GpuRun:
+    """One simulation held by libqhg_gpu.so on a CUDA device."""
+
+    def __init__(self, grid: Grid, actions: Sequence[Action], seed: int, genetics: Genetics = Genetics(),
+                 log_births: bool = False, capacity: int = 0, timing: bool = False, device: int = 0):
+        lib = load_library()
+        flags = (QHG_FLAG_LOG_BIRTHS if log_births else 0) | (QHG_FLAG_KERNEL_TIMING if timing else 0)
+        self._desc = make_desc(actions, seed, genetics, capacity, flags, device)
+        h = ct.c_void_p()
+        _check(lib.qhg_gpu_create(ct.byref(self._desc), ct.byref(h)))
+        self.h = h
+        self.C = grid.num_cells
+        self.genetics = genetics
+        self.grid = grid
+        nbr = np.ascontiguousarray(grid.nbr, dtype=np.int32)
+        nnbr = np.ascontiguousarray(grid.nnbr, dtype=np.uint8)
+        K = np.ascontiguousarray(grid.K, dtype=np.float64)
+        _check(lib.qhg_gpu_upload_grid(self.h, _p(nbr), _p(nnbr), _p(K), self.C))
+
+    def load(self, a: Agents, first_step: int = 0) -> None:
+        cols = dict(id=np.ascontiguousarray(a.id, dtype=np.int64), cell=np.ascontiguousarray(a.cell, dtype=np.int32),
+                    birth=np.ascontiguousarray(a.birth, dtype=np.float32),
+                    age=np.ascontiguousarray(a.age, dtype=np.float32),
+                    last_birth=np.ascontiguousarray(a.lastb, dtype=np.float32),
+                    gender=np.ascontiguousarray(a.gender, dtype=np.uint8),
+                    state=np.ascontiguousarray(a.state, dtype=np.uint8))
+        soa = AgentsSoA(**{k: v.ctypes.data for k, v in cols.items()})
+        if self.genetics.genome_size > 0:
+            g = np.ascontiguousarray(a.genome, dtype=np.uint64)
+            cols["genome"] = g
+            soa.genome = g.ctypes.data
+        _check(_lib.qhg_gpu_upload_agents(self.h, ct.byref(soa), len(a), int(first_step)))
+
+    def step(self, n: int = 1) -> None:
+        _check(_lib.qhg_gpu_step(self.h, int(n)))
+
+    def sync(self) -> None:
+        _check(_lib.qhg_gpu_sync(self.h))
+
+    def num_agents(self) -> int:
+        n = ct.c_int64()
+        _check(_lib.qhg_gpu_num_agents(self.h, ct.byref(n)))
+        return int(n.value)
+
+    def current_step(self) -> int:
+        s = ct.c_int32()
+        _check(_lib.qhg_gpu_current_step(self.h, ct.byref(s)))
+        return int(s.value)
+
+    def agents(self, sort_by_id: bool = True) -> Agents:
+        n = self.num_agents()
+        out = Agents(np.zeros(n, np.int64), np.zeros(n, np.int32), np.zeros(n, np.float32),
+                     np.zeros(n, np.float32), np.zeros(n, np.float32), np.zeros(n, np.uint8),
+                     np.zeros(n, np.uint8))
+        soa = AgentsSoA(out.id.ctypes.data, out.cell.ctypes.data, out.birth.ctypes.data, out.age.ctypes.data,
+                        out.lastb.ctypes.data, out.gender.ctypes.data, out.state.ctypes.data, None)
+        if self.genetics.genome_size > 0:
+            out.genome = np.zeros((n, 2 * self.genetics.num_blocks), dtype=np.uint64)
+            soa.genome = out.genome.ctypes.data
+        got = ct.c_int64()
+        _check(_lib.qhg_gpu_download(self.h, ct.byref(soa), n, ct.byref(got)))
+        return out.sorted_by_id() if sort_by_id else out
+
+    def counts(self) -> np.ndarray:
+        c = np.zeros(self.C, dtype=np.uint32)
+        _check(_lib.qhg_gpu_counts(self.h, _p(c)))
+        return c
+
+    def stats(self, nsteps: int) -> np.ndarray:
+        buf = (StepStats * max(1, nsteps))()
+        _check(_lib.qhg_gpu_stats(self.h, int(nsteps), ct.byref(buf)))
+        return np.array([[s.live, s.births, s.deaths, s.moves] for s in buf[:nsteps]], dtype=np.uint64)
+
+    def birth_log(self) -> np.ndarray:
+        n = ct.c_int64()
+        rc = _lib.qhg_gpu_birth_log(self.h, None, None, None, 0, ct.byref(n))
+        total = int(n.value)
+        b, m, f = np.zeros(total, np.int64), np.zeros(total, np.int64), np.zeros(total, np.int64)
+        if total > 0 or rc != 0:
+            _check(_lib.qhg_gpu_birth_log(self.h, _p(b), _p(m), _p(f), total, ct.byref(n)))
+        o = np.argsort(b, kind="stable")
+        return np.stack([b[o], m[o], f[o]], axis=1)
+
+    def kernel_times(self) -> np.ndarray:
+        t = np.zeros(4, dtype=np.float32)
+        _check(_lib.qhg_gpu_kernel_times(self.h, _p(t)))
+        return t
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            _lib.qhg_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,62 @@
+"""Bit-exact parity of the CUDA path (through the C ABI) with the oracle.
+
+The oracle is the C port in oracle/qhg_oracle.c, itself pinned against the
+reference's own action code (tests/test_oracle_pinning.py).  Every field of
+every agent, sorted by ID, must match bit for bit, as must the per-step
+statistics, the per-cell counts and the (baby, mother, father) birth log.
+"""
+import numpy as np
+import pytest
+
+from oracle import port
+from qhg4_gb300.gpu import GpuRun
+from qhg4_gb300.spec import (ACT_FERTILITY, ACT_GETOLD, ACT_OLDAGEDEATH, ACT_RANDOMMOVE, ACT_RANDOMPAIR,
+                             ACT_VERHULST, ACT_VERHULSTVARK, ACT_WEIGHTEDMOVE, Action)
+from qhg4_gb300.workload import make_agents, terrain_grid, uniform_grid
+
+from helpers import case_config1, case_config2, table_diff
+
+pytestmark = pytest.mark.gpu
+
+
+def run_both(grid, agents, actions, steps, seed, chunks=(None,)):
+    o = port.OracleRun(grid, actions, seed)
+    o.load(agents)
+    g = GpuRun(grid, actions, seed, log_births=True)
+    g.load(agents)
+    done = 0
+    ost = []
+    for ch in chunks:
+        k = steps - done if ch is None else ch
+        ost.append(o.step(k))
+        g.step(k)
+        done += k
+    ost = np.concatenate(ost, axis=0)
+    return o, g, ost
+
+
+def assert_same(o, g, ost, steps):
+    d = table_diff(o.agents(), g.agents())
+    assert d is None, d
+    assert np.array_equal(o.counts(), g.counts())
+    assert np.array_equal(ost[-min(steps, 1024):], g.stats(min(steps, 1024)))
+    ob, gb = o.birth_log(), g.birth_log()
+    assert np.array_equal(ob, gb), f"birth logs differ ({len(ob)} vs {len(gb)})"
+
+
+def test_config1_small(gpu_lib):
+    grid, agents, acts = case_config1()
+    o, g, st = run_both(grid, agents, acts, 60, 42)
+    assert_same(o, g, st, 60)
+
+
+def test_config1_stepwise(gpu_lib):
+    grid, agents, acts = case_config1(n=6, N=6000, seed=5)
+    o, g, st = run_both(grid, agents, acts, 25, 7, chunks=(1, 1, 3, 20))
+    assert_same(o, g, st, 25)
+
+
+def test_config2_small(gpu_lib):
+    grid, agents, acts = case_config2()
+    o, g, st = run_both(grid, agents, acts, 40, 5)
+    assert_same(o, g, st, 40)
