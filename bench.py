@@ -1,0 +1,358 @@
+#!/usr/bin/env python3
+"""Benchmark of the per-step agent hot path on GB300: agent-steps/s.
+
+Workload (default, ``--workload large``): the single large run -- icosahedral
+grid n=256 (655,362 cells), altitude-derived K, 20M agents placed with
+probability proportional to K, ages U[0,60); GetOld, Fertility, RandomPair,
+VerhulstVarK, OldAgeDeath (onset U[60,70)), WeightedMove (p=0.2).  Synthetic,
+seeded inputs of the configuration's shapes and distributions.
+
+One line of JSON on rank 0 (the contract's keys plus ``roofline``,
+``cpu_baseline``, ``e2e``, ``clocks``, ``gpu_launches``).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+``--impl reference`` times the CPU implementation of the path on this host's
+cores: the C port of the reference algorithm (oracle/qhg_oracle.c), because
+the reference itself cannot be compiled on the GPU host (its sources are not
+there).  With several GPUs (torchrun), every rank runs an independent replica
+of the workload on its own GPU (the path has no data exchange between runs);
+``value`` sums the agent-steps of all ranks over the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+from qhg4_gb300.spec import config1_actions, config2_actions  # noqa: E402
+from qhg4_gb300.workload import make_agents, terrain_grid, uniform_grid  # noqa: E402
+
+METRIC = "agent-steps/s"
+
+WORKLOADS = {
+    # name: grid n, agents, age max, K-proportional placement, actions, bytes per cell-step
+    "large": dict(n=256, agents=20_000_000, age_max=60.0, prop=True, actions=config2_actions,
+                  cell_bytes=53 + 56, desc="single large run: grid n=256 (655,362 cells), altitude K, 20M agents, "
+                  "GetOld+Fertility+RandomPair+VerhulstVarK+OldAgeDeath+WeightedMove(p=0.2)", job_steps=200),
+    # a smaller case of the same actions for profiler captures (hot table > L2)
+    "medium": dict(n=192, agents=8_000_000, age_max=60.0, prop=True, actions=config2_actions,
+                   cell_bytes=53 + 56, desc="grid n=192 (368,642 cells), altitude K, 8M agents, "
+                   "actions of the large run", job_steps=200),
+    "plain": dict(n=32, agents=100_000, age_max=50.0, prop=False, actions=config1_actions,
+                  cell_bytes=53, desc="plain method: grid n=32 (10,242 cells), K=30, 100k agents, "
+                  "GetOld+Fertility+RandomPair+Verhulst+RandomMove(p=0.1)", job_steps=1000),
+}
+AGENT_BYTES = 60   # one read and one write of the 30-byte hot record per agent-step
+
+
+def build_workload(name: str, seed: int = 42, grid_seed: int = 2024):
+    w = WORKLOADS[name]
+    if w["prop"]:
+        grid = terrain_grid(w["n"], seed=grid_seed)
+    else:
+        grid = uniform_grid(w["n"], 30.0)
+    agents = make_agents(grid, w["agents"], seed=seed, age_max=w["age_max"], proportional_to_K=w["prop"])
+    return grid, agents, w["actions"]()
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,utilization.gpu")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons, busy = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 10:
+                continue
+            try:
+                s, m = float(f[1]), float(f[2])
+                util = float(f[9])
+            except ValueError:
+                continue
+            sm.append(s)
+            smax.append(m)
+            if util > 0:
+                busy.append(s)
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        load = busy if busy else sm
+        return {"sm_mhz": float(np.median(load)) if load else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm), "samples_busy": len(busy)}
+
+
+def read_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def read_traffic(workload: str):
+    """DRAM bytes per agent-step of one step's kernels, from the committed ncu
+    summary (profiles/step_traffic_<workload>.txt), or None."""
+    p = os.path.join(ROOT, "profiles", f"step_traffic_{workload}.txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for ln in f:
+            m = re.match(r"\s*dram_bytes_per_agent_step\s*[:=]\s*([0-9.eE+]+)", ln)
+            if m:
+                return float(m.group(1))
+    return None
+
+
+def cpu_leg(grid, agents, actions, seed, steps, warmup):
+    """The C port of the reference algorithm on all host threads (OpenMP)."""
+    from oracle import port
+    threads = os.cpu_count() or 1
+    port.set_threads(threads)
+    r = port.OracleRun(grid, actions, seed, log_births=False)
+    r.load(agents)
+    if warmup > 0:
+        r.step(warmup)
+    n0 = r.num_agents()
+    t0 = time.perf_counter()
+    st = r.step(steps)
+    dt = time.perf_counter() - t0
+    agent_steps = n0 + int(st[:-1, 0].sum()) if steps > 0 else 0
+    r.close()
+    return agent_steps, dt, threads
+
+
+def init_dist(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local, dist
+
+
+def gather_max(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def gather_sum(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def run_reference(args, world, rank, dist):
+    if rank != 0:
+        return 0
+    grid, agents, actions = build_workload(args.workload, args.seed)
+    steps = max(1, min(args.steps, args.cpu_steps))
+    warm = min(args.warmup, 1)
+    n_as, dt, thr = cpu_leg(grid, agents, actions, args.seed, steps, warm)
+    v = n_as / dt
+    sample = (f"{steps} step(s) after {warm} warm-up step(s) of the full {args.workload} workload "
+              f"({WORKLOADS[args.workload]['agents']} initial agents)")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "agent-steps/s", "n_gpus": args.gpus,
+        "steps": steps, "warmup": warm, "ms_per_step": 1000.0 * dt / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32/f32/f64", "data": "synthetic",
+        "config": {"workload": args.workload, "detail": WORKLOADS[args.workload]["desc"],
+                   "cpu": "C port of the reference algorithm (oracle/qhg_oracle.c), OpenMP"},
+        "cpu_baseline": {"value": v, "unit": "agent-steps/s", "cores": thr, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "agent-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, world, rank, local, dist):
+    from qhg4_gb300.gpu import GpuRun
+    device = local if world > 1 else args.device
+    grid, agents, actions = build_workload(args.workload, args.seed + rank)
+    N0 = len(agents)
+    C = grid.num_cells
+    wl = WORKLOADS[args.workload]
+    run = GpuRun(grid, actions, args.seed + rank, capacity=int(N0 * 2.5) + 65536, device=device)
+    run.load(agents)
+    if args.warmup > 0:
+        run.step(args.warmup)
+    run.sync()
+    n_start = run.num_agents()
+    sampler = ClockSampler(device)
+    sampler.start()
+    time.sleep(0.3)
+    if dist is not None:
+        dist.barrier()
+    ms = run.step_timed(args.steps)
+    if dist is not None:
+        dist.barrier()
+    st = run.stats(args.steps) if args.steps > 0 else np.zeros((0, 4), np.uint64)
+    agent_steps = n_start + int(st[:-1, 0].sum()) if args.steps > 0 else 0
+    # per-kernel device times (each kernel launched alone between events)
+    prof_steps = max(1, args.profile_steps)
+    kms = run.step_profiled(prof_steps)
+    n_prof_start = int(st[-1, 0]) if args.steps > 0 else n_start
+    pst = run.stats(prof_steps)
+    prof_agents = (n_prof_start + int(pst[:-1, 0].sum())) / prof_steps
+    if os.environ.get("QHG_BENCH_DEBUG"):
+        sys.stderr.write(f"timed stats tail {st[-3:].tolist()} profiled stats {pst.tolist()} kms {kms.tolist()}\n")
+    clocks = sampler.stop()
+    t_max = gather_max(dist, ms / 1000.0)
+    total = gather_sum(dist, float(agent_steps))
+    value = total / t_max if t_max > 0 else 0.0
+
+    kmean = kms.mean(axis=0)
+    step_ms = float(kmean[:3].sum())
+    names = ["k_actions", "k_cell_scan", "k_scatter", "k_genomes"]
+    kshare = {names[i]: {"ms": float(kmean[i]), "share": float(kmean[i] / step_ms) if step_ms > 0 else 0.0}
+              for i in range(3)}
+    dominant = max(range(3), key=lambda i: kmean[i])
+    alg_bytes = AGENT_BYTES * prof_agents + wl["cell_bytes"] * C
+    peak, peak_kind = read_peaks()
+    achieved = alg_bytes / (step_ms / 1000.0) / 1e9 if step_ms > 0 else 0.0
+    tpa = read_traffic(args.workload)
+    roofline = {"bound": "hbm", "kernel": "one step: k_actions + k_cell_scan + k_scatter "
+                f"(dominant: {names[dominant]})",
+                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
+                "traffic": (tpa * prof_agents) if tpa is not None else None,
+                "algorithmic_bytes": alg_bytes, "per_kernel": kshare}
+
+    # end to end through the public API: upload from host, the configured job
+    # length with per-step statistics read back, download of the final table
+    e2e = None
+    if not args.skip_e2e:
+        job_steps = wl["job_steps"] if args.e2e_steps <= 0 else args.e2e_steps
+        run2 = GpuRun(grid, actions, args.seed + rank, capacity=int(N0 * 2.5) + 65536, device=device)
+        run2.sync()
+        t0 = time.perf_counter()
+        run2.load(agents)
+        e_as = 0
+        n_live = N0
+        for _ in range(job_steps):
+            run2.step(1)
+            s1 = run2.stats(1)
+            e_as += n_live
+            n_live = int(s1[0, 0])
+        final = run2.agents(sort_by_id=False)
+        dt = time.perf_counter() - t0
+        run2.close()
+        rec = 8 + 4 + 4 + 4 + 4 + 1 + 1
+        e2e_t = gather_max(dist, dt)
+        e2e_as = gather_sum(dist, float(e_as))
+        e2e = {"value": e2e_as / e2e_t, "unit": "agent-steps/s",
+               "h2d_bytes_per_step": int(N0 * rec / job_steps + (C * 6 * 4 + C + C * 8) / job_steps),
+               "d2h_bytes_per_step": int(32 + len(final) * rec / job_steps),
+               "steps": job_steps, "detail": "qhg_gpu_upload_agents from host arrays + per-step "
+               "qhg_gpu_step(1) and qhg_gpu_stats(1) + final qhg_gpu_download, wall clock"}
+
+    cpu = None
+    if rank == 0 and not args.skip_cpu:
+        cs = max(1, args.cpu_steps)
+        n_as, dt, thr = cpu_leg(grid, agents, actions, args.seed, cs, 0)
+        cpu = {"value": n_as / dt, "unit": "agent-steps/s", "cores": thr, "kind": "port",
+               "sample": f"first {cs} step(s) of the same workload on the C port of the reference algorithm "
+                         f"(oracle/qhg_oracle.c, OpenMP, {thr} threads)"}
+    run.close()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "agent-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / max(1, args.steps),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32/f32/f64",
+            "data": "synthetic (seeded; shapes and distributions of the configuration)",
+            "config": {"workload": args.workload, "detail": wl["desc"], "agents": N0, "cells": C,
+                       "agents_at_timed_start": n_start, "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (hot table ~21 B x agents > 129 MB)"},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "gpu_launches": 3 * args.steps * world,
+        }
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="large")
+    ap.add_argument("--seed", type=int, default=42)
+    ap.add_argument("--device", type=int, default=0)
+    ap.add_argument("--profile-steps", type=int, default=3)
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=0)
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 0 or args.steps < 0:
+        ap.error("steps and warmup must be >= 0")
+    world, rank, local, dist = init_dist(args)
+    try:
+        if args.impl == "reference":
+            return run_reference(args, world, rank, dist)
+        return run_ours(args, world, rank, local, dist)
+    finally:
+        if dist is not None:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

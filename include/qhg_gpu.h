@@ -66,7 +66,7 @@ extern "C" {
 #define QHG_ACT_WEIGHTEDMOVE  7  /* WeightedMove  actions/WeightedMove.cpp:45-106 */
 
 #define QHG_MAX_ACTIONS       16
-#define QHG_MAX_CELL_AGENTS   1024   /* agents one cell may hold */
+#define QHG_MAX_CELL_AGENTS   512    /* agents one cell may hold */
 #define QHG_CROSSOVER_POISSON1 (-100) /* Poisson(1) breakpoints per parent */
 
 /* life states stored in the agent table (core/SPopulation.h:69-73) */
@@ -150,13 +150,17 @@ int qhg_gpu_stream(qhg_run *run, void **stream);
 int qhg_gpu_destroy(qhg_run *run);
 
 /*
- * Timing helpers for the benchmark: the duration, measured with CUDA events
- * on the run's stream, of the kernels of the last qhg_gpu_step call, summed
- * per kernel kind (0 actions, 1 cell scan, 2 scatter, 3 genomes), in ms.
- * Only filled when the run was created with QHG_FLAG_KERNEL_TIMING.
+ * Runs nsteps steps like qhg_gpu_step, but launches each kernel on its own
+ * (no CUDA graph) between CUDA events on the run's stream and waits for
+ * each step.  kernel_ms (nsteps x 4) receives the device time of each
+ * kernel of each step: actions, cell scan, scatter, genomes (0 without
+ * genetics).  For measurement only.
  */
-#define QHG_FLAG_KERNEL_TIMING 2u
-int qhg_gpu_kernel_times(qhg_run *run, float *ms4);
+int qhg_gpu_step_profiled(qhg_run *run, int32_t nsteps, float *kernel_ms);
+
+/* runs nsteps steps like qhg_gpu_step between two CUDA events recorded on
+ * the run's stream, waits, and returns the device time in *elapsed_ms */
+int qhg_gpu_step_timed(qhg_run *run, int32_t nsteps, float *elapsed_ms);
 
 #ifdef __cplusplus
 }

@@ -18,6 +18,7 @@
 
 extern "C" int qhg_launch_step(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
                                int cell_grid, cudaStream_t stream);
+extern "C" int qhg_tile_ctas_per_sm(void);
 extern "C" int qhg_launch_step_timed(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
                                      int cell_grid, cudaStream_t stream, cudaEvent_t *ev);
 
@@ -47,7 +48,7 @@ struct qhg_run {
     int C = 0;
     int32_t *d_nbr = nullptr;
     uint8_t *d_nnbr = nullptr;
-    int32_t *d_rev = nullptr;
+    uint32_t *d_rev = nullptr;
     double *d_K = nullptr;
     uint64_t *d_wthr = nullptr;
     uint8_t *d_wflag = nullptr;
@@ -59,8 +60,9 @@ struct qhg_run {
     float *d_age[2] = {nullptr, nullptr};
     float *d_lastb[2] = {nullptr, nullptr};
     uint8_t *d_meta[2] = {nullptr, nullptr};
-    uint32_t *d_cs[2] = {nullptr, nullptr};
-    uint32_t *d_ne[2] = {nullptr, nullptr};
+    uint32_t *d_ne[2] = {nullptr, nullptr};    // non-empty cells in index order
+    uint32_t *d_nes[2] = {nullptr, nullptr};   // their first rows (+ agent count)
+    uint32_t *d_tf[2] = {nullptr, nullptr};    // first non-empty cell of each tile
     // scratch
     uint8_t *d_outc = nullptr;
     int32_t *d_father = nullptr;
@@ -78,17 +80,17 @@ struct qhg_run {
     bool grid_ok = false, agents_ok = false;
     int cell_grid = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    cudaEvent_t ev[8];
-    bool events = false;
-    float ktimes[4] = {0, 0, 0, 0};
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    std::vector<int64_t> stage;  // host staging for uploads
 };
 
 static void free_agents(qhg_run *r) {
     for (int p = 0; p < 2; p++) {
         cudaFree(r->d_id[p]); cudaFree(r->d_birth[p]); cudaFree(r->d_age[p]); cudaFree(r->d_lastb[p]);
-        cudaFree(r->d_meta[p]); cudaFree(r->d_cs[p]); cudaFree(r->d_ne[p]);
+        cudaFree(r->d_meta[p]); cudaFree(r->d_ne[p]); cudaFree(r->d_nes[p]); cudaFree(r->d_tf[p]);
+        r->d_tf[p] = nullptr;
         r->d_id[p] = nullptr; r->d_birth[p] = r->d_age[p] = r->d_lastb[p] = nullptr;
-        r->d_meta[p] = nullptr; r->d_cs[p] = r->d_ne[p] = nullptr;
+        r->d_meta[p] = nullptr; r->d_ne[p] = r->d_nes[p] = nullptr;
     }
     cudaFree(r->d_outc); cudaFree(r->d_father); cudaFree(r->d_brank); cudaFree(r->d_blog);
     r->d_outc = nullptr; r->d_father = nullptr; r->d_brank = nullptr; r->d_blog = nullptr;
@@ -149,12 +151,19 @@ extern "C" int qhg_gpu_create(const qhg_run_desc *desc, qhg_run **out) {
             break;
         case kFertility:
             A.f0 = (float)p[0]; A.f1 = (float)p[1]; A.f2 = (float)p[2];
+            if (!P.age_from_birth) P.reads_age = 1;   // reads the age before any GetOld sets it
             break;
         case kRandomPair:
             P.has_pair = 1;
             break;
         case kVerhulst:
         case kVerhulstVarK:
+            if (P.n_verhulst >= kMaxVerhulst) {
+                delete r;
+                return fail(QHG_ERR_ARG, "more than 2 Verhulst actions");
+            }
+            A.vslot = P.n_verhulst;
+            P.verhulst_act[P.n_verhulst++] = a;
             A.b0 = p[0]; A.d0 = p[1]; A.th = p[2];
             A.th_b0 = p[2] - p[0];
             A.th_d0 = p[2] - p[1];
@@ -203,11 +212,8 @@ extern "C" int qhg_gpu_create(const qhg_run_desc *desc, qhg_run **out) {
     memset(r->h_rs, 0, sizeof(RunState));
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, desc->device);
-    r->cell_grid = std::max(1, nsm) * 8;
-    if (desc->flags & QHG_FLAG_KERNEL_TIMING) {
-        for (int i = 0; i < 8; i++) cudaEventCreate(&r->ev[i]);
-        r->events = true;
-    }
+    // persistent grid of the tile kernels: as many CTAs as fit at once
+    r->cell_grid = std::max(1, nsm) * std::max(1, qhg_tile_ctas_per_sm());
     *out = r;
     return QHG_OK;
 }
@@ -219,7 +225,7 @@ extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_
     }
     CUDA_TRY(cudaSetDevice(r->desc.device));
     const int C = num_cells;
-    std::vector<int32_t> rev((size_t)C * 6, 0);
+    std::vector<uint32_t> rev((size_t)C, 0u);
     for (int c = 0; c < C; c++) {
         if (nnbr[c] > 6) return fail(QHG_ERR_ARG, "more than 6 neighbours");
         for (int j = 0; j < 6; j++) {
@@ -231,7 +237,7 @@ extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_
                 if (nbr6[(size_t)d * 6 + q] == c) { k = q; break; }
             }
             if (k < 0) return fail(QHG_ERR_ARG, "neighbour table is not symmetric");
-            rev[(size_t)c * 6 + j] = k;
+            rev[(size_t)c] |= (uint32_t)k << (3 * j);
         }
     }
     // WeightedMove: cumulated weights (SingleEvaluator, actions/SingleEvaluator.cpp:174-241)
@@ -287,7 +293,7 @@ extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_
     const int ntiles = (C + kScanTile - 1) / kScanTile;
     CUDA_TRY(cudaMalloc(&r->d_nbr, (size_t)C * 6 * sizeof(int32_t)));
     CUDA_TRY(cudaMalloc(&r->d_nnbr, (size_t)C));
-    CUDA_TRY(cudaMalloc(&r->d_rev, (size_t)C * 6 * sizeof(int32_t)));
+    CUDA_TRY(cudaMalloc(&r->d_rev, (size_t)C * sizeof(uint32_t)));
     CUDA_TRY(cudaMalloc(&r->d_K, (size_t)C * sizeof(double)));
     CUDA_TRY(cudaMalloc(&r->d_wthr, (size_t)C * 6 * sizeof(uint64_t)));
     CUDA_TRY(cudaMalloc(&r->d_wflag, (size_t)C));
@@ -301,7 +307,8 @@ extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_
     CUDA_TRY(cudaMalloc(&r->d_tincl, (size_t)ntiles * sizeof(uint4)));
     CUDA_TRY(cudaMemcpyAsync(r->d_nbr, nbr6, (size_t)C * 6 * sizeof(int32_t), cudaMemcpyHostToDevice, r->stream));
     CUDA_TRY(cudaMemcpyAsync(r->d_nnbr, nnbr, (size_t)C, cudaMemcpyHostToDevice, r->stream));
-    CUDA_TRY(cudaMemcpyAsync(r->d_rev, rev.data(), (size_t)C * 6 * sizeof(int32_t), cudaMemcpyHostToDevice, r->stream));
+    CUDA_TRY(cudaMemcpyAsync(r->d_rev, rev.data(), (size_t)C * sizeof(uint32_t), cudaMemcpyHostToDevice, r->stream));
+    CUDA_TRY(cudaMemsetAsync(r->d_clsc, 0, (size_t)C * kCls * sizeof(uint32_t), r->stream));
     CUDA_TRY(cudaMemcpyAsync(r->d_K, K, (size_t)C * sizeof(double), cudaMemcpyHostToDevice, r->stream));
     CUDA_TRY(cudaMemcpyAsync(r->d_wthr, wthr.data(), (size_t)C * 6 * sizeof(uint64_t), cudaMemcpyHostToDevice, r->stream));
     CUDA_TRY(cudaMemcpyAsync(r->d_wflag, wflag.data(), (size_t)C, cudaMemcpyHostToDevice, r->stream));
@@ -323,8 +330,9 @@ static int alloc_agents(qhg_run *r, uint32_t cap) {
         CUDA_TRY(cudaMalloc(&r->d_age[p], (size_t)cap * sizeof(float)));
         CUDA_TRY(cudaMalloc(&r->d_lastb[p], (size_t)cap * sizeof(float)));
         CUDA_TRY(cudaMalloc(&r->d_meta[p], (size_t)cap));
-        CUDA_TRY(cudaMalloc(&r->d_cs[p], (size_t)(C + 1) * sizeof(uint32_t)));
         CUDA_TRY(cudaMalloc(&r->d_ne[p], (size_t)C * sizeof(uint32_t)));
+        CUDA_TRY(cudaMalloc(&r->d_nes[p], (size_t)(C + 1) * sizeof(uint32_t)));
+        CUDA_TRY(cudaMalloc(&r->d_tf[p], ((size_t)cap / kTileAgents + 2) * sizeof(uint32_t)));
     }
     CUDA_TRY(cudaMalloc(&r->d_outc, (size_t)cap));
     CUDA_TRY(cudaMalloc(&r->d_father, (size_t)cap * sizeof(int32_t)));
@@ -371,16 +379,13 @@ extern "C" int qhg_gpu_upload_agents(qhg_run *r, const qhg_agents_soa *a, int64_
     uint64_t want = r->desc.agent_capacity > 0 ? (uint64_t)r->desc.agent_capacity : (uint64_t)live * 4 + 65536;
     if (want < (uint64_t)live) want = (uint64_t)live;
     if (want > 0x7fffffffull) return fail(QHG_ERR_CAPACITY, "agent capacity above 2^31-1");
+    // rows grouped by cell, input order kept within a cell (counting sort)
     std::vector<int64_t> order((size_t)live);
     {
         std::vector<uint32_t> pos(cnt.begin(), cnt.end() - 1);
         for (int64_t i = 0; i < n; i++) {
             if (a->state[i] == 0) continue;
             order[pos[a->cell[i]]++] = i;
-        }
-        for (int c = 0; c < C; c++) {
-            std::sort(order.begin() + cnt[c], order.begin() + cnt[(size_t)c + 1],
-                      [&](int64_t x, int64_t y) { return a->id[x] < a->id[y]; });
         }
     }
     std::vector<int64_t> h_id((size_t)live);
@@ -394,9 +399,24 @@ extern "C" int qhg_gpu_upload_agents(qhg_run *r, const qhg_agents_soa *a, int64_
         h_lastb[(size_t)k] = a->last_birth[i];
         h_meta[(size_t)k] = (uint8_t)((a->gender[i] & 1u) | (a->state[i] == QHG_LS_FERTILE ? kMetaFertile : 0));
     }
-    std::vector<uint32_t> ne;
+    std::vector<uint32_t> ne, nes;
     for (int c = 0; c < C; c++) {
-        if (cnt[(size_t)c + 1] != cnt[(size_t)c]) ne.push_back((uint32_t)c);
+        if (cnt[(size_t)c + 1] != cnt[(size_t)c]) {
+            ne.push_back((uint32_t)c);
+            nes.push_back(cnt[(size_t)c]);
+        }
+    }
+    nes.push_back((uint32_t)live);
+    // first non-empty cell of each tile (tile t starts at row t * kTileAgents)
+    const uint32_t ntl = (uint32_t)((live + kTileAgents - 1) / kTileAgents);
+    std::vector<uint32_t> tf((size_t)ntl + 1);
+    {
+        uint32_t r = 0;
+        for (uint32_t t = 0; t <= ntl; t++) {
+            const uint64_t row = (uint64_t)t * kTileAgents;
+            while (r < ne.size() && nes[r] < row) r++;
+            tf[t] = r;
+        }
     }
     drop_graphs(r);
     r->agents_ok = false;
@@ -413,10 +433,12 @@ extern "C" int qhg_gpu_upload_agents(qhg_run *r, const qhg_agents_soa *a, int64_
         CUDA_TRY(cudaMemcpyAsync(r->d_lastb[0], h_lastb.data(), live * sizeof(float), cudaMemcpyHostToDevice, r->stream));
         CUDA_TRY(cudaMemcpyAsync(r->d_meta[0], h_meta.data(), live, cudaMemcpyHostToDevice, r->stream));
     }
-    CUDA_TRY(cudaMemcpyAsync(r->d_cs[0], cnt.data(), (size_t)(C + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, r->stream));
     if (!ne.empty()) {
         CUDA_TRY(cudaMemcpyAsync(r->d_ne[0], ne.data(), ne.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, r->stream));
     }
+    CUDA_TRY(cudaMemcpyAsync(r->d_nes[0], nes.data(), nes.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, r->stream));
+    CUDA_TRY(cudaMemcpyAsync(r->d_tf[0], tf.data(), tf.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, r->stream));
+    CUDA_TRY(cudaMemsetAsync(r->d_clsc, 0, (size_t)C * kCls * sizeof(uint32_t), r->stream));
     memset(r->h_rs, 0, sizeof(RunState));
     r->h_rs->step = first_step;
     r->h_rs->n_agents = (uint32_t)live;
@@ -430,13 +452,15 @@ extern "C" int qhg_gpu_upload_agents(qhg_run *r, const qhg_agents_soa *a, int64_
     return QHG_OK;
 }
 
+static int pull_state(qhg_run *r);
+
 static StepBuffers make_buffers(qhg_run *r, int cur) {
     const int nx = cur ^ 1;
     StepBuffers B;
-    B.cell_start = r->d_cs[cur]; B.nonempty = r->d_ne[cur];
+    B.nonempty = r->d_ne[cur]; B.ne_start = r->d_nes[cur]; B.tile_first = r->d_tf[cur];
     B.id = r->d_id[cur]; B.birth = r->d_birth[cur]; B.age = r->d_age[cur]; B.lastb = r->d_lastb[cur];
     B.meta = r->d_meta[cur];
-    B.cell_start2 = r->d_cs[nx]; B.nonempty2 = r->d_ne[nx];
+    B.nonempty2 = r->d_ne[nx]; B.ne_start2 = r->d_nes[nx]; B.tile_first2 = r->d_tf[nx];
     B.id2 = r->d_id[nx]; B.birth2 = r->d_birth[nx]; B.age2 = r->d_age[nx]; B.lastb2 = r->d_lastb[nx];
     B.meta2 = r->d_meta[nx];
     B.nbr = r->d_nbr; B.nnbr = r->d_nnbr; B.rev = r->d_rev; B.K = r->d_K; B.wthr = r->d_wthr;
@@ -469,25 +493,50 @@ extern "C" int qhg_gpu_step(qhg_run *r, int32_t nsteps) {
     if (r == nullptr || nsteps < 0) return fail(QHG_ERR_ARG, "bad step arguments");
     if (!r->grid_ok || !r->agents_ok) return fail(QHG_ERR_STATE, "upload grid and agents first");
     CUDA_TRY(cudaSetDevice(r->desc.device));
-    for (int i = 0; i < 4; i++) r->ktimes[i] = 0.0f;
     for (int32_t s = 0; s < nsteps; s++) {
-        if (r->events) {
-            StepBuffers B = make_buffers(r, r->cur);
-            int le = qhg_launch_step_timed(&r->P, r->d_rs, &B, r->cell_grid, r->stream, r->ev);
-            if (le != 0) return fail(QHG_ERR_CUDA, std::string("launch: ") + cudaGetErrorString((cudaError_t)le));
-            CUDA_TRY(cudaEventSynchronize(r->ev[3]));
-            for (int k = 0; k < 3; k++) {
-                float ms = 0.0f;
-                cudaEventElapsedTime(&ms, r->ev[k], r->ev[k + 1]);
-                r->ktimes[k] += ms;
-            }
-        } else {
-            if (r->graph[r->cur] == nullptr) {
-                int rc = build_graph(r, r->cur);
-                if (rc != QHG_OK) return rc;
-            }
-            CUDA_TRY(cudaGraphLaunch(r->graph[r->cur], r->stream));
+        if (r->graph[r->cur] == nullptr) {
+            int rc = build_graph(r, r->cur);
+            if (rc != QHG_OK) return rc;
         }
+        CUDA_TRY(cudaGraphLaunch(r->graph[r->cur], r->stream));
+        r->cur ^= 1;
+    }
+    return QHG_OK;
+}
+
+extern "C" int qhg_gpu_step_timed(qhg_run *r, int32_t nsteps, float *elapsed_ms) {
+    if (r == nullptr || elapsed_ms == nullptr) return fail(QHG_ERR_ARG, "null argument");
+    CUDA_TRY(cudaSetDevice(r->desc.device));
+    if (r->ev[0] == nullptr) {
+        for (int i = 0; i < 4; i++) CUDA_TRY(cudaEventCreate(&r->ev[i]));
+    }
+    CUDA_TRY(cudaEventRecord(r->ev[0], r->stream));
+    int rc = qhg_gpu_step(r, nsteps);
+    if (rc != QHG_OK) return rc;
+    CUDA_TRY(cudaEventRecord(r->ev[1], r->stream));
+    CUDA_TRY(cudaEventSynchronize(r->ev[1]));
+    CUDA_TRY(cudaEventElapsedTime(elapsed_ms, r->ev[0], r->ev[1]));
+    return pull_state(r);
+}
+
+extern "C" int qhg_gpu_step_profiled(qhg_run *r, int32_t nsteps, float *kernel_ms) {
+    if (r == nullptr || nsteps < 0 || (nsteps > 0 && kernel_ms == nullptr)) return fail(QHG_ERR_ARG, "bad step arguments");
+    if (!r->grid_ok || !r->agents_ok) return fail(QHG_ERR_STATE, "upload grid and agents first");
+    CUDA_TRY(cudaSetDevice(r->desc.device));
+    if (r->ev[0] == nullptr) {
+        for (int i = 0; i < 4; i++) CUDA_TRY(cudaEventCreate(&r->ev[i]));
+    }
+    for (int32_t s = 0; s < nsteps; s++) {
+        StepBuffers B = make_buffers(r, r->cur);
+        int le = qhg_launch_step_timed(&r->P, r->d_rs, &B, r->cell_grid, r->stream, r->ev);
+        if (le != 0) return fail(QHG_ERR_CUDA, std::string("launch: ") + cudaGetErrorString((cudaError_t)le));
+        CUDA_TRY(cudaEventSynchronize(r->ev[3]));
+        for (int k = 0; k < 3; k++) {
+            float ms = 0.0f;
+            CUDA_TRY(cudaEventElapsedTime(&ms, r->ev[k], r->ev[k + 1]));
+            kernel_ms[s * 4 + k] = ms;
+        }
+        kernel_ms[s * 4 + 3] = 0.0f;
         r->cur ^= 1;
     }
     return QHG_OK;
@@ -505,12 +554,15 @@ static int pull_state(qhg_run *r) {
         r->h_rs->error_info = 0u;
         r->h_rs->scan_tiles_started = 0u;
         r->h_rs->scatter_ctas_done = 0u;
+        r->h_rs->action_tiles = 0u;
+        r->h_rs->scatter_tiles = 0u;
         // the failed step's partial statistics would be counted again on retry
         unsigned long long *st = r->h_rs->stats[(uint32_t)r->h_rs->step % kStatsRing];
         st[0] = st[1] = st[2] = st[3] = 0ull;
         CUDA_TRY(cudaMemcpyAsync(r->d_rs, r->h_rs, sizeof(RunState), cudaMemcpyHostToDevice, r->stream));
         const int ntiles = (r->C + kScanTile - 1) / kScanTile;
         CUDA_TRY(cudaMemsetAsync(r->d_tflag, 0, (size_t)ntiles * sizeof(uint32_t), r->stream));
+        CUDA_TRY(cudaMemsetAsync(r->d_clsc, 0, (size_t)r->C * kCls * sizeof(uint32_t), r->stream));
         CUDA_TRY(cudaStreamSynchronize(r->stream));
         char buf[160];
         switch (code) {
@@ -562,9 +614,11 @@ extern "C" int qhg_gpu_download(qhg_run *r, qhg_agents_soa *o, int64_t cap, int6
     *n = N;
     if (cap < N) return fail(QHG_ERR_ARG, "output arrays too small");
     const int cur = r->cur;
-    std::vector<uint32_t> cs((size_t)r->C + 1);
+    const uint32_t nne = r->h_rs->n_nonempty;
+    std::vector<uint32_t> ne(nne), nes((size_t)nne + 1);
     std::vector<uint8_t> meta((size_t)N);
-    CUDA_TRY(cudaMemcpy(cs.data(), r->d_cs[cur], cs.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (nne > 0) CUDA_TRY(cudaMemcpy(ne.data(), r->d_ne[cur], nne * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(nes.data(), r->d_nes[cur], (nne + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost));
     if (N > 0) {
         CUDA_TRY(cudaMemcpy(o->id, r->d_id[cur], N * sizeof(int64_t), cudaMemcpyDeviceToHost));
         CUDA_TRY(cudaMemcpy(o->birth, r->d_birth[cur], N * sizeof(float), cudaMemcpyDeviceToHost));
@@ -572,8 +626,8 @@ extern "C" int qhg_gpu_download(qhg_run *r, qhg_agents_soa *o, int64_t cap, int6
         CUDA_TRY(cudaMemcpy(o->last_birth, r->d_lastb[cur], N * sizeof(float), cudaMemcpyDeviceToHost));
         CUDA_TRY(cudaMemcpy(meta.data(), r->d_meta[cur], N, cudaMemcpyDeviceToHost));
     }
-    for (int c = 0; c < r->C; c++) {
-        for (uint32_t i = cs[c]; i < cs[(size_t)c + 1]; i++) o->cell[i] = c;
+    for (uint32_t k = 0; k < nne; k++) {
+        for (uint32_t i = nes[k]; i < nes[(size_t)k + 1]; i++) o->cell[i] = (int32_t)ne[k];
     }
     for (int64_t i = 0; i < N; i++) {
         o->gender[i] = meta[(size_t)i] & kMetaGender;
@@ -587,9 +641,12 @@ extern "C" int qhg_gpu_counts(qhg_run *r, uint32_t *counts) {
     if (!r->agents_ok) return fail(QHG_ERR_STATE, "no agents uploaded");
     int rc = qhg_gpu_sync(r);
     if (rc != QHG_OK) return rc;
-    std::vector<uint32_t> cs((size_t)r->C + 1);
-    CUDA_TRY(cudaMemcpy(cs.data(), r->d_cs[r->cur], cs.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
-    for (int c = 0; c < r->C; c++) counts[c] = cs[(size_t)c + 1] - cs[c];
+    const uint32_t nne = r->h_rs->n_nonempty;
+    std::vector<uint32_t> ne(nne), nes((size_t)nne + 1);
+    if (nne > 0) CUDA_TRY(cudaMemcpy(ne.data(), r->d_ne[r->cur], nne * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(nes.data(), r->d_nes[r->cur], (nne + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    for (int c = 0; c < r->C; c++) counts[c] = 0u;
+    for (uint32_t k = 0; k < nne; k++) counts[ne[k]] = nes[(size_t)k + 1] - nes[k];
     return QHG_OK;
 }
 
@@ -632,13 +689,6 @@ extern "C" int qhg_gpu_stream(qhg_run *r, void **stream) {
     return QHG_OK;
 }
 
-extern "C" int qhg_gpu_kernel_times(qhg_run *r, float *ms4) {
-    if (r == nullptr || ms4 == nullptr) return fail(QHG_ERR_ARG, "null argument");
-    if (!r->events) return fail(QHG_ERR_STATE, "run was created without QHG_FLAG_KERNEL_TIMING");
-    for (int i = 0; i < 4; i++) ms4[i] = r->ktimes[i];
-    return QHG_OK;
-}
-
 extern "C" int qhg_gpu_destroy(qhg_run *r) {
     if (r == nullptr) return QHG_OK;
     cudaSetDevice(r->desc.device);
@@ -651,8 +701,8 @@ extern "C" int qhg_gpu_destroy(qhg_run *r) {
     cudaFree(r->d_obase); cudaFree(r->d_tflag); cudaFree(r->d_tagg); cudaFree(r->d_tincl);
     cudaFree(r->d_rs);
     cudaFreeHost(r->h_rs);
-    if (r->events) {
-        for (int i = 0; i < 8; i++) cudaEventDestroy(r->ev[i]);
+    for (int i = 0; i < 4; i++) {
+        if (r->ev[i]) cudaEventDestroy(r->ev[i]);
     }
     if (r->stream) cudaStreamDestroy(r->stream);
     delete r;

@@ -10,10 +10,16 @@ namespace qhg {
 
 // ---------------------------------------------------------------- layout
 constexpr int kMaxActions = 16;
-constexpr int kMaxCell = 512;            // agents one cell may hold (per-warp shared buffers)
-constexpr int kWarpsPerCta = 4;          // cell kernels: one warp per cell
+constexpr int kMaxVerhulst = 1;          // Verhulst / VerhulstVarK actions per population
+constexpr int kMaxCell = 512;            // agents one cell may hold
+// agent kernels work on cell-aligned tiles: tile t holds the non-empty cells
+// whose first row lies in [t*kTileAgents, (t+1)*kTileAgents)
+constexpr int kTileAgents = 512;
+constexpr int kTileMax = kTileAgents + kMaxCell;  // rows a tile can hold
+constexpr int kTileCells = kTileAgents;           // cells a tile can hold
+constexpr int kTileThreads = 256;
 constexpr int kScanThreads = 256;
-constexpr int kScanItems = 8;            // cells per thread in the cell scan
+constexpr int kScanItems = 2;            // cells per thread in the cell scan
 constexpr int kScanTile = kScanThreads * kScanItems;
 constexpr int kStatsRing = 1024;
 constexpr uint32_t kSpinLimit = 1u << 24;  // bounded waits in the look-back
@@ -49,6 +55,7 @@ enum ErrorCode : uint32_t {
 struct ActionConst {
     int32_t type;
     uint32_t window;        // first draw of the action in the per-agent stream
+    int32_t vslot;          // Verhulst: index among the population's Verhulst actions
     float f0, f1, f2;       // Fertility: min age, max age, interbirth
     float age_lo, age_hi;   // OldAgeDeath: float bounds of the uncertain age window
     double b0, d0, th;      // Verhulst
@@ -67,6 +74,9 @@ struct StepConst {
     int32_t log_births;
     int32_t genome_words;    // 2 * blocks, 0 without genetics
     uint32_t capacity;
+    int32_t reads_age;       // some action reads the stored age before GetOld/OldAgeDeath sets it
+    int32_t n_verhulst;
+    int32_t verhulst_act[kMaxVerhulst];
     ActionConst act[kMaxActions];
 };
 
@@ -80,6 +90,8 @@ struct RunState {
     uint32_t error_info;
     uint32_t scan_tiles_started;
     uint32_t scatter_ctas_done;
+    uint32_t action_tiles;    // tiles handed out by k_actions
+    uint32_t scatter_tiles;   // tiles handed out by k_scatter
     // written by the cell scan, committed when the scatter finishes
     uint32_t new_n_agents;
     uint32_t new_n_nonempty;
@@ -92,11 +104,16 @@ struct RunState {
 // device pointers of one step: the current table, the next table, the
 // grid and the step's scratch arrays
 struct StepBuffers {
-    const uint32_t *cell_start; const uint32_t *nonempty;
+    // current table: non-empty cells in index order and the first row of each
+    // (ne_start has n_nonempty + 1 entries, the last one the agent count)
+    // tile_first[t]: index of the first non-empty cell of tile t (ceil(N/kTileAgents)+1 entries)
+    const uint32_t *nonempty; const uint32_t *ne_start; const uint32_t *tile_first;
     const int64_t *id; const float *birth; const float *age; const float *lastb; const uint8_t *meta;
-    uint32_t *cell_start2; uint32_t *nonempty2;
+    uint32_t *nonempty2; uint32_t *ne_start2; uint32_t *tile_first2;
     int64_t *id2; float *birth2; float *age2; float *lastb2; uint8_t *meta2;
-    const int32_t *nbr; const uint8_t *nnbr; const int32_t *rev; const double *K;
+    // rev packs, 3 bits per neighbour slot q, the slot of this cell in the
+    // neighbour's own list
+    const int32_t *nbr; const uint8_t *nnbr; const uint32_t *rev; const double *K;
     const uint64_t *wthr; const uint8_t *wflag;
     uint8_t *outc; int32_t *father; uint16_t *brank; uint32_t *clsc;
     uint32_t *sbase; uint32_t *bbase; uint32_t *bidbase; uint32_t *obase;

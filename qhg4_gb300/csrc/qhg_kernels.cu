@@ -1,22 +1,26 @@
 // Step kernels of libqhg_gpu.so (sm_103a).
 //
-// Agents live in device memory as a structure of arrays sorted by cell:
-// cell c owns rows [cell_start[c], cell_start[c+1]).  One step is three
-// kernels (plus the genome kernel with genetics):
+// Agents live in device memory as a structure of arrays sorted by cell.
+// The non-empty cells are listed in index order (nonempty[r]) together with
+// their first row (ne_start[r]).  One step is three kernels (plus the genome
+// kernel with genetics):
 //
-//   k_actions   one warp per non-empty cell.  Computes the cell's Verhulst
-//               thresholds, pairs its FERTILE agents (RandomPair), runs every
-//               action on every agent of the cell and writes one outcome
-//               byte per agent (dead / stays / moves to neighbour slot k,
-//               gives birth, new fertility), per-cell class counts, and for
-//               each mother the father's row and her birth rank by ID.
+//   k_actions   cell-aligned tiles of ~kTileAgents agents, one CTA at a time
+//               per tile, everything staged in shared memory.  Per cell
+//               (one thread each): the Verhulst thresholds.  Per cell, agent
+//               parallel: RandomPair (fertile members ranked by ID, picks
+//               drawn per picking member and decoded independently).  Per
+//               agent: every action in execution order, one outcome byte
+//               (dead / stays / moves to neighbour slot k, gives birth, new
+//               fertility), the father's row of each mother.  Per cell: the
+//               class counts and the mothers' birth ranks by ID.
 //   k_cell_scan one pass over all cells with a decoupled look-back scan:
-//               new per-cell counts (stayers + movers in + births), new
-//               cell_start, output bases of every (cell, class), birth
-//               numbering and the next step's list of non-empty cells.
-//   k_scatter   one warp per old non-empty cell: stable ranks per class by
-//               warp ballots, every survivor and newborn written to its row
-//               of the next table.  The last CTA commits the run state.
+//               new per-cell counts (stayers + movers in + births), output
+//               bases of every (cell, class), birth numbering, and the next
+//               step's non-empty list with first rows.
+//   k_scatter   the same tiles: stable ranks per (cell, class), every
+//               survivor and newborn written to its row of the next table,
+//               the consumed class counts cleared.  The last CTA commits.
 //
 // The reference runs these as SPopulation::initializeStep / doActions /
 // finalizeStep (core/SPopulation.cpp:394-577, 596-724, 1058-1092, 509-536).
@@ -29,15 +33,9 @@ namespace qhg {
 
 #define FULL_MASK 0xffffffffu
 
-__device__ __forceinline__ uint32_t lanemask_lt() {
-    uint32_t m;
-    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
-    return m;
-}
-
 __device__ __forceinline__ uint32_t pick4(const Draw4 &d, uint32_t k) {
-    uint32_t a = (k & 1u) ? d.v[1] : d.v[0];
-    uint32_t b = (k & 1u) ? d.v[3] : d.v[2];
+    const uint32_t a = (k & 1u) ? d.v[1] : d.v[0];
+    const uint32_t b = (k & 1u) ? d.v[3] : d.v[2];
     return (k & 2u) ? b : a;
 }
 
@@ -53,7 +51,7 @@ struct AgentDraws {
         seed = s; step = st; id = i; blk = 0xffffffffu;
     }
     __device__ __forceinline__ uint32_t get(uint32_t k) {
-        uint32_t b = kStreamActions + (k >> 2);
+        const uint32_t b = kStreamActions + (k >> 2);
         if (b != blk) {
             d = draw_block(seed, step, id, b);
             blk = b;
@@ -61,22 +59,6 @@ struct AgentDraws {
         return pick4(d, k & 3u);
     }
 };
-
-// position of the k-th (0-based) set bit of z; the bit must exist
-__device__ __forceinline__ int select_bit(uint32_t z, int k) {
-    int pos = 0;
-    int c = __popc(z & 0xffffu);
-    if (k >= c) { k -= c; pos += 16; z >>= 16; }
-    c = __popc(z & 0xffu);
-    if (k >= c) { k -= c; pos += 8; z >>= 8; }
-    c = __popc(z & 0xfu);
-    if (k >= c) { k -= c; pos += 4; z >>= 4; }
-    c = __popc(z & 0x3u);
-    if (k >= c) { k -= c; pos += 2; z >>= 2; }
-    c = (int)(z & 1u);
-    if (k >= c) { pos += 1; }
-    return pos;
-}
 
 __device__ __forceinline__ void set_error(RunState *rs, uint32_t code, uint32_t info) {
     if (atomicCAS(&rs->error, 0u, code) == 0u) {
@@ -87,27 +69,57 @@ __device__ __forceinline__ void set_error(RunState *rs, uint32_t code, uint32_t 
 // u < thr  <=>  u / 2^32 < x   for a double x (the reference's wrandd() < x)
 __device__ __forceinline__ uint64_t prob_threshold(double x) {
     if (!(x > 0.0)) return 0ull;
-    double y = __dmul_rn(x, 4294967296.0);
+    const double y = __dmul_rn(x, 4294967296.0);
     if (y >= 4294967296.0) return 4294967296ull;
     return (uint64_t)ceil(y);
 }
 
-struct WarpSmem {
-    uint64_t fid[kMaxCell];     // FERTILE ids: females from the front, males from the back
-    uint16_t floc[kMaxCell];    // their rows within the cell
-    uint16_t srt[kMaxCell];     // sorted order (females front, males back)
-    int16_t mate[kMaxCell];     // mate's row within the cell, -1 none
-    uint16_t pick[kMaxCell];    // per pairing: chosen member of the larger side
-    uint8_t bfl[kMaxCell];      // gives birth this step
-    uint32_t taken[kMaxCell / 32];
-    uint64_t thr[kMaxActions][2];  // Verhulst: birth (or birth-death) and death thresholds
-    int32_t thr_kind[kMaxActions]; // 0 none, 1 birth, 2 death by negative birth rate
-};
+// per-cell class counts: slot 0 stay, 1..6 movers to neighbour slot 0..5, 7 births;
+// two 16-bit counters per shared word
+__device__ __forceinline__ void count_slot(uint32_t *cls, int slot) {
+    atomicAdd(&cls[slot >> 1], 1u << (16 * (slot & 1)));
+}
+
+__device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t *red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL_MASK, v, o);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    uint32_t t = 0;
+    if (threadIdx.x == 0) {
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+    }
+    return t;
+}
 
 // ------------------------------------------------------------------ actions
-__global__ void __launch_bounds__(kWarpsPerCta * 32)
+struct ActionsSmem {
+    int64_t id[kTileMax];
+    uint8_t meta[kTileMax];
+    uint8_t bfl[kTileMax];         // gives birth this step
+    uint16_t cell[kTileMax];       // local cell index of each row
+    int16_t mate[kTileMax];        // mate's row within the tile, -1 none
+    uint16_t frank[kTileMax];      // rank of a FERTILE agent among its cell's FERTILE agents of its sex (by ID)
+    uint16_t list[kTileMax];       // at each cell's rows: FERTILE females by ID, then FERTILE males by ID
+    uint16_t pick[kTileMax];       // at each cell's rows: unsorted FERTILE lists, later the pick values
+    uint32_t cstart[kTileCells + 1];  // first row of each cell, relative to the tile
+    int32_t cid[kTileCells];
+    uint32_t nf[kTileCells];
+    uint32_t nm[kTileCells];
+    uint64_t tb[kTileCells];       // Verhulst: birth threshold (kind 1) or birth-rate death threshold (kind 2)
+    uint64_t td[kTileCells];       // LinearDeath threshold
+    uint8_t tk[kTileCells];
+    uint32_t cls[kTileCells][4];
+    uint32_t red[kTileThreads / 32];
+    uint32_t t, r0, r1;
+};
+
+__global__ void __launch_bounds__(kTileThreads)
 k_actions(const StepConst P, RunState *__restrict__ rs,
-          const uint32_t *__restrict__ cell_start, const uint32_t *__restrict__ nonempty,
+          const uint32_t *__restrict__ nonempty, const uint32_t *__restrict__ ne_start,
+          const uint32_t *__restrict__ tile_first,
           const int64_t *__restrict__ id, const float *__restrict__ birth,
           const float *__restrict__ age, const float *__restrict__ lastb,
           const uint8_t *__restrict__ meta,
@@ -116,295 +128,306 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
           const uint8_t *__restrict__ wflag,
           uint8_t *__restrict__ outc, int32_t *__restrict__ father, uint16_t *__restrict__ brank,
           uint32_t *__restrict__ clsc) {
-    __shared__ WarpSmem smem[kWarpsPerCta];
+    __shared__ ActionsSmem S;
     if (rs->error != 0u) return;   // an earlier kernel failed: keep the state
-    const int warp = threadIdx.x >> 5;
-    const int lane = threadIdx.x & 31;
-    WarpSmem &S = smem[warp];
-    const uint32_t lt = lanemask_lt();
+    const int tid = threadIdx.x;
     const int32_t step = rs->step;
     const float fT = (float)step;
-    const uint32_t n_ne = rs->n_nonempty;
+    const uint32_t N = rs->n_agents;
+    const uint32_t ntiles = (N + kTileAgents - 1) / kTileAgents;
     uint32_t cnt_births = 0, cnt_deaths = 0, cnt_moves = 0;
 
-    for (uint32_t w = blockIdx.x * kWarpsPerCta + warp; w < n_ne; w += gridDim.x * kWarpsPerCta) {
-        const int c = (int)nonempty[w];
-        const uint32_t s = cell_start[c];
-        const int n = (int)(cell_start[c + 1] - s);
-        if (n > kMaxCell) {
-            if (lane == 0) set_error(rs, kErrCellTooLarge, (uint32_t)c);
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) {
+            const uint32_t t = atomicAdd(&rs->action_tiles, 1u);
+            S.t = t;
+            if (t < ntiles) {
+                S.r0 = tile_first[t];
+                S.r1 = tile_first[t + 1];
+            }
+        }
+        __syncthreads();
+        if (S.t >= ntiles) break;
+        const uint32_t r0 = S.r0;
+        const int nc = (int)(S.r1 - r0);
+        if (nc == 0) continue;
+        const uint32_t a0 = ne_start[r0];
+        const int na = (int)(ne_start[r0 + nc] - a0);
+        if (na > kTileMax || nc > kTileCells) {
+            if (tid == 0) set_error(rs, kErrCellTooLarge, r0);
             continue;
         }
-        // ---- per-cell rates (LinearBirth/LinearDeath::initialize)
-        if (lane == 0) {
-            for (int a = 0; a < P.n_act; a++) {
-                const ActionConst &A = P.act[a];
-                if (A.type != kVerhulst && A.type != kVerhulstVarK) continue;
+        // ---- cells: ids, rows, Verhulst thresholds (LinearBirth / LinearDeath
+        // ::initialize, actions/LinearBirth.cpp:90-112, actions/LinearDeath.cpp:92-122)
+        for (int lc = tid; lc < nc; lc += kTileThreads) {
+            const int c = (int)nonempty[r0 + lc];
+            const uint32_t cs = ne_start[r0 + lc] - a0;
+            const uint32_t ce = ne_start[r0 + lc + 1] - a0;
+            S.cid[lc] = c;
+            S.cstart[lc] = cs;
+            if (lc == nc - 1) S.cstart[nc] = ce;
+            S.nf[lc] = 0u;
+            S.nm[lc] = 0u;
+            S.cls[lc][0] = S.cls[lc][1] = S.cls[lc][2] = S.cls[lc][3] = 0u;
+            if (P.n_verhulst > 0) {
+                const ActionConst &A = P.act[P.verhulst_act[0]];
                 double B, D;
-                double K = (A.type == kVerhulst) ? A.K : Kc[c];
+                const double K = (A.type == kVerhulst) ? A.K : Kc[c];
                 if (A.type == kVerhulstVarK && K <= 0.0) {
                     B = 0.0;
                     D = 1.0;
                 } else {
-                    double r = __ddiv_rn((double)n, K);
+                    const double r = __ddiv_rn((double)(ce - cs), K);
                     B = __dadd_rn(A.b0, __dmul_rn(A.th_b0, r));
                     D = __dadd_rn(A.d0, __dmul_rn(A.th_d0, r));
                 }
-                int kind = 0;
+                uint8_t kind = 0;
                 uint64_t tb = 0;
                 if (B > 0.0) { kind = 1; tb = prob_threshold(B); }
                 else if (B < 0.0) { kind = 2; tb = prob_threshold(-B); }
-                S.thr_kind[a] = kind;
-                S.thr[a][0] = tb;
-                S.thr[a][1] = prob_threshold(D);
+                S.tk[lc] = kind;
+                S.tb[lc] = tb;
+                S.td[lc] = prob_threshold(D);
             }
         }
-        // ---- pairing (RandomPair::findMates, members in ID order, keyed picks)
-        int nF = 0, nM = 0;
-        for (int b = 0; b < n; b += 32) {
-            const int i = b + lane;
-            const bool in = i < n;
-            const uint8_t m = in ? meta[s + i] : (uint8_t)0;
-            const bool fert = P.has_pair && in && (m & kMetaFertile);
-            const bool fem = fert && !(m & kMetaGender);
-            const bool mal = fert && (m & kMetaGender);
-            const uint32_t bf = __ballot_sync(FULL_MASK, fem);
-            const uint32_t bm = __ballot_sync(FULL_MASK, mal);
-            if (fem) {
-                const int p = nF + __popc(bf & lt);
-                S.fid[p] = id[s + i];
-                S.floc[p] = (uint16_t)i;
-            }
-            if (mal) {
-                const int p = kMaxCell - 1 - (nM + __popc(bm & lt));
-                S.fid[p] = id[s + i];
-                S.floc[p] = (uint16_t)i;
-            }
-            nF += __popc(bf);
-            nM += __popc(bm);
-            if (in) {
-                S.mate[i] = -1;
-                S.bfl[i] = 0;
-            }
+        for (int i = tid; i < na; i += kTileThreads) {
+            S.meta[i] = meta[a0 + i];
+            S.id[i] = id[a0 + i];
+            S.mate[i] = -1;
+            S.bfl[i] = 0;
         }
-        __syncwarp();
-        if (nF > 0 && nM > 0) {
-            // rank sort by ID (IDs are unique)
-            for (int j = lane; j < nF; j += 32) {
-                const uint64_t x = S.fid[j];
-                int r = 0;
-                for (int t = 0; t < nF; t++) r += (S.fid[t] < x) ? 1 : 0;
-                S.srt[r] = (uint16_t)j;
-            }
-            for (int j = lane; j < nM; j += 32) {
-                const uint64_t x = S.fid[kMaxCell - 1 - j];
-                int r = 0;
-                for (int t = 0; t < nM; t++) r += (S.fid[kMaxCell - 1 - t] < x) ? 1 : 0;
-                S.srt[kMaxCell - 1 - r] = (uint16_t)j;
-            }
-            __syncwarp();
-            const bool femSmall = nF <= nM;
-            const int nS = femSmall ? nF : nM;
-            const int nL = femSmall ? nM : nF;
-            // each pick draws from the pairing stream of the picking member
-            for (int r = lane; r < nS; r += 32) {
-                int64_t sid;
-                if (femSmall) sid = (int64_t)S.fid[S.srt[r]];
-                else sid = (int64_t)S.fid[kMaxCell - 1 - S.srt[kMaxCell - 1 - r]];
-                const uint32_t u = draw_block(P.seed, (uint32_t)step, sid, kStreamPair).v[0];
-                const uint32_t nRem = (uint32_t)(nL - r);
-                S.pick[r] = (uint16_t)(((uint64_t)nRem * (uint64_t)u) >> 32);
-            }
-            __syncwarp();
-            if (lane == 0) {
-                const int nw = (nL + 31) >> 5;
-                for (int q = 0; q < nw; q++) S.taken[q] = 0u;
-                for (int r = 0; r < nS; r++) {
-                    int k = S.pick[r];
-                    int p = -1;
-                    for (int q = 0; q < nw; q++) {
-                        uint32_t valid = (q == nw - 1 && (nL & 31)) ? ((1u << (nL & 31)) - 1u) : FULL_MASK;
-                        uint32_t z = ~S.taken[q] & valid;
-                        int pc = __popc(z);
-                        if (k < pc) {
-                            int bit = select_bit(z, k);
-                            S.taken[q] |= 1u << bit;
-                            p = q * 32 + bit;
-                            break;
-                        }
-                        k -= pc;
+        __syncthreads();
+        for (int lc = tid; lc < nc; lc += kTileThreads) {
+            const int ce = (int)S.cstart[lc + 1];
+            for (int i = (int)S.cstart[lc]; i < ce; i++) S.cell[i] = (uint16_t)lc;
+        }
+        __syncthreads();
+        // ---- RandomPair::findMates (actions/RandomPair.cpp:146-270), members in
+        // ID order, each pick drawn from the pairing stream of the picking member
+        if (P.has_pair) {
+            // unsorted FERTILE lists: females from the cell's first row up, males
+            // from its last row down
+            for (int i = tid; i < na; i += kTileThreads) {
+                const uint8_t m = S.meta[i];
+                if (m & kMetaFertile) {
+                    const int lc = S.cell[i];
+                    if (m & kMetaGender) {
+                        const uint32_t q = atomicAdd(&S.nm[lc], 1u);
+                        S.pick[S.cstart[lc + 1] - 1u - q] = (uint16_t)i;
+                    } else {
+                        const uint32_t q = atomicAdd(&S.nf[lc], 1u);
+                        S.pick[S.cstart[lc] + q] = (uint16_t)i;
                     }
-                    S.pick[r] = (uint16_t)p;
                 }
             }
-            __syncwarp();
-            for (int r = lane; r < nS; r += 32) {
-                const int pl = S.pick[r];
-                if (pl >= nL) {   // cannot happen: every pick finds a free member
-                    set_error(rs, kErrInternal, 1u);
-                    continue;
-                }
-                int locS, locL;
-                if (femSmall) {
-                    locS = S.floc[S.srt[r]];
-                    locL = S.floc[kMaxCell - 1 - S.srt[kMaxCell - 1 - pl]];
-                } else {
-                    locS = S.floc[kMaxCell - 1 - S.srt[kMaxCell - 1 - r]];
-                    locL = S.floc[S.srt[pl]];
-                }
-                S.mate[locS] = (int16_t)locL;
-                S.mate[locL] = (int16_t)locS;
-            }
-        }
-        __syncwarp();
-        // ---- actions on every agent (SPopulation::doActions)
-        const int nn = nnbr[c];
-        uint32_t cls_cnt[kCls];
-#pragma unroll
-        for (int k = 0; k < kCls; k++) cls_cnt[k] = 0;
-        for (int b = 0; b < n; b += 32) {
-            const int i = b + lane;
-            const bool in = i < n;
-            int cls = 0;
-            bool bflag = false;
-            if (in) {
-                const uint32_t row = s + (uint32_t)i;
-                const int64_t aid = id[row];
-                const uint8_t m8 = meta[row];
-                const float fb = birth[row];
-                float fa = age[row];
-                const float fl = lastb[row];
-                const bool female = !(m8 & kMetaGender);
-                bool fert = (m8 & kMetaFertile) != 0;
-                bool alive = true;
-                int dir = 0;
-                AgentDraws dr;
-                dr.init(P.seed, (uint32_t)step, aid);
-                for (int a = 0; a < P.n_act && alive; a++) {
-                    const ActionConst &A = P.act[a];
-                    switch (A.type) {
-                    case kGetOld:
-                        fa = __fsub_rn(fT, fb);
-                        break;
-                    case kFertility:
-                        if (female) fert = (fa > A.f0) && (fa < A.f1) && (__fsub_rn(fT, fl) > A.f2);
-                        else fert = fa > A.f0;
-                        break;
-                    case kVerhulst:
-                    case kVerhulstVarK: {
-                        uint32_t k = A.window;
-                        const int kind = S.thr_kind[a];
-                        if (kind == 1) {
-                            if (female && S.mate[i] >= 0) {
-                                if ((uint64_t)dr.get(k++) < S.thr[a][0]) bflag = true;
-                            }
-                        } else if (kind == 2) {
-                            if ((uint64_t)dr.get(k++) < S.thr[a][0]) alive = false;
-                        }
-                        if (alive) {
-                            if ((uint64_t)dr.get(k) < S.thr[a][1]) alive = false;
-                        }
-                        if (!alive) cnt_deaths++;
-                        break;
+            __syncthreads();
+            // rank by ID within the own sex's list (IDs are unique)
+            for (int i = tid; i < na; i += kTileThreads) {
+                const uint8_t m = S.meta[i];
+                if (m & kMetaFertile) {
+                    const int lc = S.cell[i];
+                    const int64_t x = S.id[i];
+                    int r = 0;
+                    if (m & kMetaGender) {
+                        const int e = (int)S.cstart[lc + 1];
+                        const int b = e - (int)S.nm[lc];
+                        for (int q = b; q < e; q++) r += (S.id[S.pick[q]] < x) ? 1 : 0;
+                    } else {
+                        const int b = (int)S.cstart[lc];
+                        const int e = b + (int)S.nf[lc];
+                        for (int q = b; q < e; q++) r += (S.id[S.pick[q]] < x) ? 1 : 0;
                     }
-                    case kOldAgeDeath: {
-                        fa = __fsub_rn(fT, fb);
-                        bool die;
-                        if (fa <= A.age_lo) {
-                            die = false;
-                        } else if (fa > A.age_hi) {
-                            die = true;
+                    S.frank[i] = (uint16_t)r;
+                }
+            }
+            __syncthreads();
+            for (int i = tid; i < na; i += kTileThreads) {
+                const uint8_t m = S.meta[i];
+                if (m & kMetaFertile) {
+                    const int lc = S.cell[i];
+                    const uint32_t off = (m & kMetaGender) ? S.nf[lc] : 0u;
+                    S.list[S.cstart[lc] + off + S.frank[i]] = (uint16_t)i;
+                }
+            }
+            __syncthreads();
+            // pick j takes the pick[j]-th still unpaired member of the larger
+            // side, pick[j] = (int)wrandr(0, nL - j)
+            for (int i = tid; i < na; i += kTileThreads) {
+                const uint8_t m = S.meta[i];
+                if (m & kMetaFertile) {
+                    const int lc = S.cell[i];
+                    const uint32_t nF = S.nf[lc], nM = S.nm[lc];
+                    const bool femSmall = nF <= nM;
+                    if (nF > 0u && nM > 0u && (((m & kMetaGender) == 0) == femSmall)) {
+                        const uint32_t j = S.frank[i];
+                        const uint32_t nL = femSmall ? nM : nF;
+                        const uint32_t u = draw_block(P.seed, (uint32_t)step, S.id[i], kStreamPair).v[0];
+                        S.pick[S.cstart[lc] + j] = (uint16_t)(((uint64_t)(nL - j) * (uint64_t)u) >> 32);
+                    }
+                }
+            }
+            __syncthreads();
+            // the member taken by pick j, decoded on its own: start from pick[j]
+            // and for i = j-1 down to 0 step over the member pick i took when it
+            // lies at or below
+            for (int i = tid; i < na; i += kTileThreads) {
+                const uint8_t m = S.meta[i];
+                if (m & kMetaFertile) {
+                    const int lc = S.cell[i];
+                    const uint32_t nF = S.nf[lc], nM = S.nm[lc];
+                    const bool femSmall = nF <= nM;
+                    if (nF > 0u && nM > 0u && (((m & kMetaGender) == 0) == femSmall)) {
+                        const int cs = (int)S.cstart[lc];
+                        const int j = S.frank[i];
+                        uint32_t p = S.pick[cs + j];
+                        for (int q = j - 1; q >= 0; q--) p += (p >= S.pick[cs + q]) ? 1u : 0u;
+                        const uint32_t nL = femSmall ? nM : nF;
+                        if (p >= nL) {   // cannot happen: every pick finds a free member
+                            set_error(rs, kErrInternal, 1u);
                         } else {
-                            const uint32_t u = dr.get(A.window);
-                            double t = __dmul_rn(__dmul_rn(A.oad_w, (double)u), 2.3283064365386962890625e-10);
-                            double thr = __dadd_rn(A.oad_M, __dadd_rn(A.oad_a, t));
-                            die = (double)fa > thr;
+                            const int partner = S.list[cs + (femSmall ? (int)nF : 0) + (int)p];
+                            S.mate[i] = (int16_t)partner;
+                            S.mate[partner] = (int16_t)i;
                         }
-                        if (die) { alive = false; cnt_deaths++; }
-                        break;
                     }
-                    case kRandomMove: {
-                        if ((uint64_t)dr.get(A.window) < A.pthr) {
-                            const uint32_t u2 = dr.get(A.window + 1);
-                            const int d = (int)(((uint64_t)(nn + 1) * (uint64_t)u2) >> 32);
-                            if (d > 0) {
-                                const int to = nbr[c * 6 + d - 1];
-                                if (to >= 0) { dir = d; cnt_moves++; }
-                            }
-                        }
-                        break;
-                    }
-                    case kWeightedMove: {
-                        if ((uint64_t)dr.get(A.window) < A.pthr) {
-                            const uint32_t u2 = dr.get(A.window + 1);
-                            int d;
-                            if (wflag[c] & 1u) {
-                                d = (int)(((uint64_t)(nn + 1) * (uint64_t)u2) >> 32);
-                            } else {
-                                d = 0;
-                                for (int j = 0; j < nn; j++) d += (wthr[c * 6 + j] <= (uint64_t)u2) ? 1 : 0;
-                            }
-                            if (d > 0) {
-                                const int to = nbr[c * 6 + d - 1];
-                                if (to >= 0) { dir = d; cnt_moves++; }
-                            }
-                        }
-                        break;
-                    }
-                    default:
-                        break;
-                    }
-                }
-                cls = alive ? (1 + dir) : 0;
-                const uint8_t code = (uint8_t)(cls | (bflag ? kOutBirth : 0) | (fert ? kOutFertile : 0) |
-                                               ((m8 & kMetaGender) ? kOutGender : 0));
-                outc[row] = code;
-                if (bflag) {
-                    father[row] = (int32_t)(s + (uint32_t)S.mate[i]);
-                    S.bfl[i] = 1;
-                    cnt_births++;
                 }
             }
-#pragma unroll
-            for (int k = 1; k < kCls; k++) cls_cnt[k - 1] += __popc(__ballot_sync(FULL_MASK, in && cls == k));
-            cls_cnt[kCls - 1] += __popc(__ballot_sync(FULL_MASK, bflag));
+            __syncthreads();
         }
-        __syncwarp();
-        // ---- birth ranks by mother ID (births are numbered in (cell, mother ID) order)
-        if (cls_cnt[kCls - 1] > 0) {
-            int acc = 0;
-            for (int b = 0; b < nF; b += 32) {
-                const int r = b + lane;
-                int loc = 0;
-                bool mom = false;
-                if (r < nF) {
-                    loc = S.floc[S.srt[r]];
-                    mom = S.bfl[loc] != 0;
+        // ---- every action on every agent (SPopulation::doActions)
+        for (int i = tid; i < na; i += kTileThreads) {
+            const uint32_t row = a0 + (uint32_t)i;
+            const int lc = S.cell[i];
+            const int c = S.cid[lc];
+            const uint8_t m8 = S.meta[i];
+            const float fb = birth[row];
+            float fa = P.reads_age ? age[row] : 0.0f;
+            const float fl = lastb[row];
+            const bool female = !(m8 & kMetaGender);
+            bool fert = (m8 & kMetaFertile) != 0;
+            bool alive = true;
+            bool bflag = false;
+            int dir = 0;
+            AgentDraws dr;
+            dr.init(P.seed, (uint32_t)step, S.id[i]);
+            for (int a = 0; a < P.n_act && alive; a++) {
+                const ActionConst &A = P.act[a];
+                switch (A.type) {
+                case kGetOld:
+                    fa = __fsub_rn(fT, fb);
+                    break;
+                case kFertility:
+                    if (female) fert = (fa > A.f0) && (fa < A.f1) && (__fsub_rn(fT, fl) > A.f2);
+                    else fert = fa > A.f0;
+                    break;
+                case kVerhulst:
+                case kVerhulstVarK: {
+                    uint32_t k = A.window;
+                    const int kind = S.tk[lc];
+                    if (kind == 1) {
+                        if (female && S.mate[i] >= 0) {
+                            if ((uint64_t)dr.get(k++) < S.tb[lc]) bflag = true;
+                        }
+                    } else if (kind == 2) {
+                        if ((uint64_t)dr.get(k++) < S.tb[lc]) alive = false;
+                    }
+                    if (alive) {
+                        if ((uint64_t)dr.get(k) < S.td[lc]) alive = false;
+                    }
+                    if (!alive) cnt_deaths++;
+                    break;
                 }
-                const uint32_t mm = __ballot_sync(FULL_MASK, mom);
-                if (mom) brank[s + loc] = (uint16_t)(acc + __popc(mm & lt));
-                acc += __popc(mm);
+                case kOldAgeDeath: {
+                    fa = __fsub_rn(fT, fb);
+                    bool die;
+                    if (fa <= A.age_lo) {
+                        die = false;
+                    } else if (fa > A.age_hi) {
+                        die = true;
+                    } else {
+                        const uint32_t u = dr.get(A.window);
+                        const double t = __dmul_rn(__dmul_rn(A.oad_w, (double)u), 2.3283064365386962890625e-10);
+                        const double thr = __dadd_rn(A.oad_M, __dadd_rn(A.oad_a, t));
+                        die = (double)fa > thr;
+                    }
+                    if (die) { alive = false; cnt_deaths++; }
+                    break;
+                }
+                case kRandomMove: {
+                    if ((uint64_t)dr.get(A.window) < A.pthr) {
+                        const int nn = nnbr[c];
+                        const uint32_t u2 = dr.get(A.window + 1);
+                        const int d = (int)(((uint64_t)(nn + 1) * (uint64_t)u2) >> 32);
+                        if (d > 0) {
+                            const int to = nbr[c * 6 + d - 1];
+                            if (to >= 0) { dir = d; cnt_moves++; }
+                        }
+                    }
+                    break;
+                }
+                case kWeightedMove: {
+                    if ((uint64_t)dr.get(A.window) < A.pthr) {
+                        const int nn = nnbr[c];
+                        const uint32_t u2 = dr.get(A.window + 1);
+                        int d;
+                        if (wflag[c] & 1u) {
+                            d = (int)(((uint64_t)(nn + 1) * (uint64_t)u2) >> 32);
+                        } else {
+                            d = 0;
+                            for (int j = 0; j < nn; j++) d += (wthr[c * 6 + j] <= (uint64_t)u2) ? 1 : 0;
+                        }
+                        if (d > 0) {
+                            const int to = nbr[c * 6 + d - 1];
+                            if (to >= 0) { dir = d; cnt_moves++; }
+                        }
+                    }
+                    break;
+                }
+                default:
+                    break;
+                }
+            }
+            const int cls = alive ? (1 + dir) : 0;
+            outc[row] = (uint8_t)(cls | (bflag ? kOutBirth : 0) | (fert ? kOutFertile : 0) |
+                                  ((m8 & kMetaGender) ? kOutGender : 0));
+            if (cls) count_slot(S.cls[lc], cls - 1);
+            if (bflag) {
+                father[row] = (int32_t)(a0 + (uint32_t)S.mate[i]);
+                S.bfl[i] = 1;
+                count_slot(S.cls[lc], 7);
+                cnt_births++;
             }
         }
-        // ---- per-cell class counts
-        uint32_t myv = 0;
-#pragma unroll
-        for (int k = 0; k < kCls; k++) myv = (lane == k) ? cls_cnt[k] : myv;
-        if (lane < kCls) clsc[c * kCls + lane] = myv;
-        __syncwarp();
+        __syncthreads();
+        // ---- per cell: mothers' birth ranks by ID (births are numbered in
+        // (cell, mother ID) order) and the class counts
+        for (int lc = tid; lc < nc; lc += kTileThreads) {
+            const int cs = (int)S.cstart[lc];
+            const int nF = (int)S.nf[lc];
+            uint32_t r = 0;
+            if (S.cls[lc][3] >> 16) {
+                for (int q = 0; q < nF; q++) {
+                    const int ai = S.list[cs + q];
+                    if (S.bfl[ai]) brank[a0 + ai] = (uint16_t)(r++);
+                }
+            }
+            const uint32_t c = (uint32_t)S.cid[lc];
+            uint4 *dst = reinterpret_cast<uint4 *>(clsc + (size_t)c * kCls);
+            const uint32_t w0 = S.cls[lc][0], w1 = S.cls[lc][1], w2 = S.cls[lc][2], w3 = S.cls[lc][3];
+            dst[0] = make_uint4(w0 & 0xffffu, w0 >> 16, w1 & 0xffffu, w1 >> 16);
+            dst[1] = make_uint4(w2 & 0xffffu, w2 >> 16, w3 & 0xffffu, w3 >> 16);
+        }
     }
     // statistics of the step
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        cnt_births += __shfl_down_sync(FULL_MASK, cnt_births, o);
-        cnt_deaths += __shfl_down_sync(FULL_MASK, cnt_deaths, o);
-        cnt_moves += __shfl_down_sync(FULL_MASK, cnt_moves, o);
-    }
-    if (lane == 0 && (cnt_births | cnt_deaths | cnt_moves)) {
+    const uint32_t tb_ = block_sum(cnt_births, S.red);
+    const uint32_t td_ = block_sum(cnt_deaths, S.red);
+    const uint32_t tm_ = block_sum(cnt_moves, S.red);
+    if (tid == 0 && (tb_ | td_ | tm_)) {
         unsigned long long *st = rs->stats[(uint32_t)step % kStatsRing];
-        atomicAdd(&st[1], (unsigned long long)cnt_births);
-        atomicAdd(&st[2], (unsigned long long)cnt_deaths);
-        atomicAdd(&st[3], (unsigned long long)cnt_moves);
+        atomicAdd(&st[1], (unsigned long long)tb_);
+        atomicAdd(&st[2], (unsigned long long)td_);
+        atomicAdd(&st[3], (unsigned long long)tm_);
     }
 }
 
@@ -427,15 +450,25 @@ __device__ __forceinline__ ScanVal sv_shfl_up(ScanVal v, int o) {
     return r;
 }
 
-// look-back status words: (epoch << 2) | 1 aggregate ready, | 2 inclusive ready
+__device__ __forceinline__ ScanVal sv_shfl_down(ScanVal v, int o) {
+    ScanVal r;
+    r.n = __shfl_down_sync(FULL_MASK, v.n, o);
+    r.b = __shfl_down_sync(FULL_MASK, v.b, o);
+    r.ne = __shfl_down_sync(FULL_MASK, v.ne, o);
+    return r;
+}
+
+// Look-back status words: (epoch << 2) | 1 aggregate ready, | 2 inclusive
+// prefix ready.  The epoch is the step number, so words of earlier steps read
+// as not ready; the host clears them whenever the step counter is reset.
 __global__ void __launch_bounds__(kScanThreads)
 k_cell_scan(const StepConst P, RunState *__restrict__ rs,
-            const uint32_t *__restrict__ cell_start, const int32_t *__restrict__ nbr,
-            const uint8_t *__restrict__ nnbr, const int32_t *__restrict__ rev,
-            const uint32_t *__restrict__ clsc,
-            uint32_t *__restrict__ new_start, uint32_t *__restrict__ sbase, uint32_t *__restrict__ bbase,
+            const int32_t *__restrict__ nbr, const uint8_t *__restrict__ nnbr,
+            const uint32_t *__restrict__ rev, const uint32_t *__restrict__ clsc,
+            uint32_t *__restrict__ sbase, uint32_t *__restrict__ bbase,
             uint32_t *__restrict__ bidbase, uint32_t *__restrict__ obase,
-            uint32_t *__restrict__ new_nonempty,
+            uint32_t *__restrict__ new_nonempty, uint32_t *__restrict__ new_ne_start,
+            uint32_t *__restrict__ new_tile_first,
             uint32_t *__restrict__ tile_flag, uint4 *__restrict__ tile_agg, uint4 *__restrict__ tile_incl) {
     __shared__ uint32_t s_tile;
     __shared__ ScanVal s_warp[kScanThreads / 32];
@@ -443,11 +476,9 @@ k_cell_scan(const StepConst P, RunState *__restrict__ rs,
     if (rs->error != 0u) return;
     const int C = P.num_cells;
     const uint32_t ntiles = (uint32_t)((C + kScanTile - 1) / kScanTile);
-    // flags of earlier steps carry older epochs; the host clears them when
-    // the step counter is reset (upload, error recovery)
     const uint32_t epoch = ((uint32_t)rs->step + 1u) & 0x3fffffffu;
     if (threadIdx.x == 0) {
-        uint32_t t = atomicAdd(&rs->scan_tiles_started, 1u);
+        const uint32_t t = atomicAdd(&rs->scan_tiles_started, 1u);
         if (t == ntiles - 1) rs->scan_tiles_started = 0u;
         s_tile = t;
     }
@@ -468,19 +499,15 @@ k_cell_scan(const StepConst P, RunState *__restrict__ rs,
         const int d = base + j;
         nnew[j] = stay[j] = bth[j] = 0u;
         if (d < C) {
-            const uint32_t nold = cell_start[d + 1] - cell_start[d];
-            uint32_t st = 0, bt = 0;
-            if (nold) {
-                st = clsc[d * kCls + 0];
-                bt = clsc[d * kCls + 7];
-            }
-            uint32_t mvin = 0;
+            // class counts of empty cells are zero (cleared by the scatter)
+            const uint32_t st = clsc[(size_t)d * kCls + 0];
+            const uint32_t bt = clsc[(size_t)d * kCls + 7];
             const int nn = nnbr[d];
+            const uint32_t rv = rev[d];
+            uint32_t mvin = 0;
             for (int q = 0; q < nn; q++) {
                 const int sn = nbr[d * 6 + q];
-                if (sn >= 0 && cell_start[sn + 1] != cell_start[sn]) {
-                    mvin += clsc[sn * kCls + 1 + rev[d * 6 + q]];
-                }
+                if (sn >= 0) mvin += clsc[(size_t)sn * kCls + 1 + ((rv >> (3 * q)) & 7u)];
             }
             stay[j] = st;
             bth[j] = bt;
@@ -494,62 +521,83 @@ k_cell_scan(const StepConst P, RunState *__restrict__ rs,
     ScanVal inc = loc;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        ScanVal y = sv_shfl_up(inc, o);
+        const ScanVal y = sv_shfl_up(inc, o);
         if (lane >= o) inc = sv_add(inc, y);
     }
     if (lane == 31) s_warp[warp] = inc;
     __syncthreads();
     if (warp == 0) {
-        ScanVal wv = (lane < kScanThreads / 32) ? s_warp[lane] : ScanVal{0u, 0u, 0u};
+        const ScanVal wv = (lane < kScanThreads / 32) ? s_warp[lane] : ScanVal{0u, 0u, 0u};
         ScanVal wi = wv;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            ScanVal y = sv_shfl_up(wi, o);
+            const ScanVal y = sv_shfl_up(wi, o);
             if (lane >= o) wi = sv_add(wi, y);
         }
         if (lane < kScanThreads / 32) s_warp[lane] = ScanVal{wi.n - wv.n, wi.b - wv.b, wi.ne - wv.ne};
-        // lane 7 holds the tile total
         const ScanVal total = {__shfl_sync(FULL_MASK, wi.n, kScanThreads / 32 - 1),
                                __shfl_sync(FULL_MASK, wi.b, kScanThreads / 32 - 1),
                                __shfl_sync(FULL_MASK, wi.ne, kScanThreads / 32 - 1)};
-        if (lane == 0) {
-            ScanVal excl = {0u, 0u, 0u};
-            if (tile == 0) {
+        ScanVal excl = {0u, 0u, 0u};
+        if (tile == 0) {
+            if (lane == 0) {
                 tile_incl[tile] = make_uint4(total.n, total.b, total.ne, 0u);
                 __threadfence();
                 atomicExch(&tile_flag[tile], (epoch << 2) | 2u);
-            } else {
+            }
+        } else {
+            if (lane == 0) {
                 tile_agg[tile] = make_uint4(total.n, total.b, total.ne, 0u);
                 __threadfence();
                 atomicExch(&tile_flag[tile], (epoch << 2) | 1u);
-                int t = (int)tile - 1;
-                uint32_t spins = 0;
-                while (t >= 0) {
-                    const uint32_t f = atomicAdd(&tile_flag[t], 0u);
-                    if ((f >> 2) != epoch || (f & 3u) == 0u) {
-                        if (++spins > kSpinLimit) {
-                            set_error(rs, kErrTimeout, tile);
-                            break;
-                        }
-                        continue;
-                    }
+            }
+            // warp-wide look-back over windows of 32 predecessors
+            int wbase = (int)tile - 1;
+            uint32_t spins = 0;
+            while (true) {
+                const int tt = wbase - lane;
+                uint32_t f = (epoch << 2) | 2u;   // before tile 0: an inclusive prefix of zero
+                if (tt >= 0) f = atomicAdd(&tile_flag[tt], 0u);
+                const bool ready = (tt < 0) || (((f >> 2) == epoch) && ((f & 3u) != 0u));
+                if (__all_sync(FULL_MASK, ready)) {
                     __threadfence();
-                    const uint4 v = ((f & 3u) == 2u) ? __ldcg(&tile_incl[t]) : __ldcg(&tile_agg[t]);
-                    excl.n += v.x; excl.b += v.y; excl.ne += v.z;
-                    if ((f & 3u) == 2u) break;
-                    t--;
+                    const bool incl = (tt < 0) || ((f & 3u) == 2u);
+                    ScanVal v = {0u, 0u, 0u};
+                    if (tt >= 0) {
+                        const uint4 q = incl ? __ldcg(&tile_incl[tt]) : __ldcg(&tile_agg[tt]);
+                        v = ScanVal{q.x, q.y, q.z};
+                    }
+                    const uint32_t im = __ballot_sync(FULL_MASK, incl);
+                    // lanes up to the first inclusive one (nearest predecessor) contribute
+                    const int stop = im ? (__ffs(im) - 1) : 31;
+                    if (lane > stop) v = ScanVal{0u, 0u, 0u};
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) v = sv_add(v, sv_shfl_down(v, o));
+                    excl = sv_add(excl, ScanVal{__shfl_sync(FULL_MASK, v.n, 0), __shfl_sync(FULL_MASK, v.b, 0),
+                                                __shfl_sync(FULL_MASK, v.ne, 0)});
+                    if (im) break;
+                    wbase -= 32;
+                } else if (++spins > kSpinLimit) {
+                    if (lane == 0) set_error(rs, kErrTimeout, tile);
+                    break;
                 }
+            }
+            if (lane == 0) {
                 tile_incl[tile] = make_uint4(excl.n + total.n, excl.b + total.b, excl.ne + total.ne, 0u);
                 __threadfence();
                 atomicExch(&tile_flag[tile], (epoch << 2) | 2u);
             }
+        }
+        if (lane == 0) {
             s_prefix = excl;
             if (tile == ntiles - 1) {
                 const uint32_t tn = excl.n + total.n;
+                const uint32_t tne = excl.ne + total.ne;
                 rs->new_n_agents = tn;
-                rs->new_n_nonempty = excl.ne + total.ne;
+                rs->new_n_nonempty = tne;
                 rs->births = excl.b + total.b;
-                new_start[C] = tn;
+                new_ne_start[tne] = tn;
+                if (tn <= P.capacity) new_tile_first[(tn + kTileAgents - 1) / kTileAgents] = tne;
                 if (tn > P.capacity) set_error(rs, kErrCapacity, tn);
             }
         }
@@ -557,30 +605,40 @@ k_cell_scan(const StepConst P, RunState *__restrict__ rs,
     __syncthreads();
     ScanVal pre = sv_add(s_prefix, s_warp[warp]);
     {
-        ScanVal y = sv_shfl_up(inc, 1);
+        const ScanVal y = sv_shfl_up(inc, 1);
         if (lane >= 1) pre = sv_add(pre, y);
     }
 #pragma unroll
     for (int j = 0; j < kScanItems; j++) {
         const int d = base + j;
         if (d < C) {
-            new_start[d] = pre.n;
             sbase[d] = pre.n;
             bidbase[d] = pre.b;
             uint32_t run = pre.n + stay[j];
             const int nn = nnbr[d];
+            const uint32_t rv = rev[d];
             for (int q = 0; q < nn; q++) {
                 const int sn = nbr[d * 6 + q];
-                if (sn >= 0 && cell_start[sn + 1] != cell_start[sn]) {
-                    const int k = rev[d * 6 + q];
-                    const uint32_t m = clsc[sn * kCls + 1 + k];
-                    if (m) obase[sn * 6 + k] = run;
+                if (sn >= 0) {
+                    const uint32_t k = (rv >> (3 * q)) & 7u;
+                    const uint32_t m = clsc[(size_t)sn * kCls + 1 + k];
+                    if (m) obase[(size_t)sn * 6 + k] = run;
                     run += m;
                 }
             }
             bbase[d] = run;
             if (nnew[j] > 0u) {
                 new_nonempty[pre.ne] = (uint32_t)d;
+                new_ne_start[pre.ne] = pre.n;
+                // tiles begin at the first cell starting at or after t * kTileAgents
+                // (rows past the capacity are never written: the step fails with kErrCapacity)
+                const uint32_t e = min(pre.n + nnew[j], P.capacity);
+                if (pre.n % (uint32_t)kTileAgents == 0u && pre.n <= P.capacity) {
+                    new_tile_first[pre.n / kTileAgents] = pre.ne;
+                }
+                for (uint32_t t = pre.n / kTileAgents + 1u; t * (uint32_t)kTileAgents <= e; t++) {
+                    new_tile_first[t] = pre.ne + 1u;
+                }
                 if (nnew[j] > (uint32_t)kMaxCell) set_error(rs, kErrCellTooLarge, (uint32_t)d);
             }
             pre.n += nnew[j];
@@ -591,57 +649,99 @@ k_cell_scan(const StepConst P, RunState *__restrict__ rs,
 }
 
 // ----------------------------------------------------------------- scatter
-__global__ void __launch_bounds__(kWarpsPerCta * 32)
+struct ScatterSmem {
+    uint8_t code[kTileMax];
+    uint16_t rank[kTileMax];       // stable rank among the cell's agents of the same class
+    uint16_t cell[kTileMax];
+    uint32_t cstart[kTileCells + 1];
+    uint32_t sb[kTileCells];
+    uint32_t bb[kTileCells];
+    uint32_t bid[kTileCells];
+    uint32_t ob[kTileCells][6];
+    uint32_t t, r0, r1;
+};
+
+__global__ void __launch_bounds__(kTileThreads)
 k_scatter(const StepConst P, RunState *__restrict__ rs,
-          const uint32_t *__restrict__ cell_start, const uint32_t *__restrict__ nonempty,
+          const uint32_t *__restrict__ nonempty, const uint32_t *__restrict__ ne_start,
+          const uint32_t *__restrict__ tile_first,
           const int64_t *__restrict__ id, const float *__restrict__ birth,
           const float *__restrict__ age, const float *__restrict__ lastb,
           const uint8_t *__restrict__ outc, const int32_t *__restrict__ father,
           const uint16_t *__restrict__ brank, const uint8_t *__restrict__ nnbr,
           const uint32_t *__restrict__ sbase, const uint32_t *__restrict__ bbase,
           const uint32_t *__restrict__ bidbase, const uint32_t *__restrict__ obase,
+          uint32_t *__restrict__ clsc,
           int64_t *__restrict__ id2, float *__restrict__ birth2, float *__restrict__ age2,
           float *__restrict__ lastb2, uint8_t *__restrict__ meta2,
           int64_t *__restrict__ blog, uint64_t blog_cap) {
-    if (rs->error != 0u) return;   // state stays as before the step
-    const int warp = threadIdx.x >> 5;
-    const int lane = threadIdx.x & 31;
-    const uint32_t lt = lanemask_lt();
+    __shared__ ScatterSmem S;
+    if (rs->error != 0u) return;   // the state stays as before the step
+    const int tid = threadIdx.x;
     const int32_t step = rs->step;
     const float fT = (float)step;
     const int64_t next_id = rs->next_id;
     const uint64_t blog_base = rs->birth_log_n;
-    const uint32_t n_ne = rs->n_nonempty;
-    const uint32_t n_old = rs->n_agents;
+    const uint32_t N = rs->n_agents;
     const uint32_t cap = P.capacity;
-    for (uint32_t w = blockIdx.x * kWarpsPerCta + warp; w < n_ne; w += gridDim.x * kWarpsPerCta) {
-        const int c = (int)nonempty[w];
-        const uint32_t s = cell_start[c];
-        const int n = (int)(cell_start[c + 1] - s);
-        const uint32_t sb = sbase[c];
-        const uint32_t bb = bbase[c];
-        const uint32_t bid = bidbase[c];
-        const int nn = nnbr[c];
-        const uint32_t obv = (lane < nn) ? obase[c * 6 + lane] : 0u;
-        uint32_t run[kCls - 1];
-#pragma unroll
-        for (int k = 0; k < kCls - 1; k++) run[k] = 0;
-        for (int b = 0; b < n; b += 32) {
-            const int i = b + lane;
-            const bool in = i < n;
-            const uint32_t row = s + (uint32_t)i;
-            const uint8_t code = in ? outc[row] : (uint8_t)0;
-            const int cls = code & 7;
-            uint32_t r = 0;
-#pragma unroll
-            for (int k = 1; k < kCls; k++) {
-                const uint32_t mk = __ballot_sync(FULL_MASK, in && cls == k);
-                if (cls == k) r = run[k - 1] + __popc(mk & lt);
-                run[k - 1] += __popc(mk);
+    const uint32_t ntiles = (N + kTileAgents - 1) / kTileAgents;
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) {
+            const uint32_t t = atomicAdd(&rs->scatter_tiles, 1u);
+            S.t = t;
+            if (t < ntiles) {
+                S.r0 = tile_first[t];
+                S.r1 = tile_first[t + 1];
             }
-            const uint32_t mb = __shfl_sync(FULL_MASK, obv, (cls >= 2) ? (cls - 2) : 0);
-            if (in && cls != 0) {
-                const uint32_t dst = (cls == 1) ? (sb + r) : (mb + r);
+        }
+        __syncthreads();
+        if (S.t >= ntiles) break;
+        const uint32_t r0 = S.r0;
+        const int nc = (int)(S.r1 - r0);
+        if (nc == 0) continue;
+        const uint32_t a0 = ne_start[r0];
+        const int na = (int)(ne_start[r0 + nc] - a0);
+        if (na > kTileMax || nc > kTileCells) continue;   // reported by k_actions
+        for (int lc = tid; lc < nc; lc += kTileThreads) {
+            const uint32_t c = nonempty[r0 + lc];
+            S.cstart[lc] = ne_start[r0 + lc] - a0;
+            if (lc == nc - 1) S.cstart[nc] = ne_start[r0 + lc + 1] - a0;
+            S.sb[lc] = sbase[c];
+            S.bb[lc] = bbase[c];
+            S.bid[lc] = bidbase[c];
+            const int nn = nnbr[c];
+            for (int k = 0; k < nn; k++) S.ob[lc][k] = obase[(size_t)c * 6 + k];
+            // the class counts are consumed: clear them for the next step
+            uint4 *z = reinterpret_cast<uint4 *>(clsc + (size_t)c * kCls);
+            z[0] = make_uint4(0u, 0u, 0u, 0u);
+            z[1] = make_uint4(0u, 0u, 0u, 0u);
+        }
+        for (int i = tid; i < na; i += kTileThreads) S.code[i] = outc[a0 + i];
+        __syncthreads();
+        // stable ranks per (cell, class): one thread walks each cell; classes
+        // 1..4 and 5..7 counted in 16-bit fields of two words
+        for (int lc = tid; lc < nc; lc += kTileThreads) {
+            uint64_t lo = 0ull, hi = 0ull;
+            const int ce = (int)S.cstart[lc + 1];
+            for (int i = (int)S.cstart[lc]; i < ce; i++) {
+                S.cell[i] = (uint16_t)lc;
+                const int k = S.code[i] & 7;
+                if (k) {
+                    const int sh = 16 * ((k - 1) & 3);
+                    if (k <= 4) { S.rank[i] = (uint16_t)(lo >> sh); lo += 1ull << sh; }
+                    else { S.rank[i] = (uint16_t)(hi >> sh); hi += 1ull << sh; }
+                }
+            }
+        }
+        __syncthreads();
+        for (int i = tid; i < na; i += kTileThreads) {
+            const uint8_t code = S.code[i];
+            const int k = code & 7;
+            const uint32_t row = a0 + (uint32_t)i;
+            const int lc = S.cell[i];
+            if (k) {
+                const uint32_t dst = ((k == 1) ? S.sb[lc] : S.ob[lc][k - 2]) + S.rank[i];
                 if (dst >= cap) {   // inconsistent bases: record, never write out of range
                     set_error(rs, kErrInternal, 3u);
                 } else {
@@ -654,26 +754,27 @@ k_scatter(const StepConst P, RunState *__restrict__ rs,
                                            ((code & kOutFertile) ? kMetaFertile : 0));
                 }
             }
-            if (in && (code & kOutBirth)) {
+            if (code & kOutBirth) {
                 // SPopulation::createAgentAtIndex (core/SPopulation.cpp:880-900):
                 // gender = (uchar)(2 * wrandd()), females start FERTILE
                 const uint32_t rk = brank[row];
-                const uint32_t dst = bb + rk;
+                const uint32_t dst = S.bb[lc] + rk;
                 const int32_t fr = father[row];
-                const bool ok = dst < cap && fr >= 0 && (uint32_t)fr < n_old;
-                if (!ok) set_error(rs, kErrInternal, 4u);
-                const int64_t mid = id[row];
-                const uint32_t u = draw_block(P.seed, (uint32_t)step, mid, kStreamBirth).v[0];
-                const uint8_t g = (uint8_t)(u >> 31);
-                const int64_t baby = next_id + (int64_t)(bid + rk);
-                if (ok) {
+                const bool ok = dst < cap && fr >= 0 && (uint32_t)fr < N;
+                if (!ok) {
+                    set_error(rs, kErrInternal, 4u);
+                } else {
+                    const int64_t mid = id[row];
+                    const uint32_t u = draw_block(P.seed, (uint32_t)step, mid, kStreamBirth).v[0];
+                    const uint8_t g = (uint8_t)(u >> 31);
+                    const int64_t baby = next_id + (int64_t)(S.bid[lc] + rk);
                     id2[dst] = baby;
                     birth2[dst] = fT;
                     lastb2[dst] = 0.0f;
                     age2[dst] = 0.0f;
                     meta2[dst] = (uint8_t)(g ? kMetaGender : kMetaFertile);
                     if (P.log_births) {
-                        const uint64_t li = blog_base + (uint64_t)(bid + rk);
+                        const uint64_t li = blog_base + (uint64_t)(S.bid[lc] + rk);
                         if (li < blog_cap) {
                             blog[li * 3 + 0] = baby;
                             blog[li * 3 + 1] = mid;
@@ -686,7 +787,7 @@ k_scatter(const StepConst P, RunState *__restrict__ rs,
     }
     // the last CTA to finish commits the step
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
         __threadfence();
         const uint32_t done = atomicAdd(&rs->scatter_ctas_done, 1u);
         if (done == gridDim.x - 1) {
@@ -701,8 +802,9 @@ k_scatter(const StepConst P, RunState *__restrict__ rs,
             rs->n_nonempty = rs->new_n_nonempty;
             rs->next_id += (int64_t)rs->births;
             rs->birth_log_n += rs->births;
+            rs->action_tiles = 0u;
+            rs->scatter_tiles = 0u;
             rs->step = (int32_t)(st + 1u);
-            rs->scatter_ctas_done = 0u;
             __threadfence();
         }
     }
@@ -710,42 +812,43 @@ k_scatter(const StepConst P, RunState *__restrict__ rs,
 
 }  // namespace qhg
 
+static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B, int grid,
+                           cudaStream_t stream, cudaEvent_t *ev) {
+    using namespace qhg;
+    const int ntiles = (P->num_cells + kScanTile - 1) / kScanTile;
+    if (ev) cudaEventRecord(ev[0], stream);
+    k_actions<<<grid, kTileThreads, 0, stream>>>(
+        *P, rs, B->nonempty, B->ne_start, B->tile_first, B->id, B->birth, B->age, B->lastb, B->meta,
+        B->nbr, B->nnbr, B->K, B->wthr, B->wflag, B->outc, B->father, B->brank, B->clsc);
+    if (ev) cudaEventRecord(ev[1], stream);
+    k_cell_scan<<<ntiles, kScanThreads, 0, stream>>>(
+        *P, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->sbase, B->bbase, B->bidbase, B->obase,
+        B->nonempty2, B->ne_start2, B->tile_first2, B->tile_flag, B->tile_agg, B->tile_incl);
+    if (ev) cudaEventRecord(ev[2], stream);
+    k_scatter<<<grid, kTileThreads, 0, stream>>>(
+        *P, rs, B->nonempty, B->ne_start, B->tile_first, B->id, B->birth, B->age, B->lastb, B->outc, B->father,
+        B->brank, B->nnbr, B->sbase, B->bbase, B->bidbase, B->obase, B->clsc, B->id2, B->birth2,
+        B->age2, B->lastb2, B->meta2, B->blog, B->blog_cap);
+    if (ev) cudaEventRecord(ev[3], stream);
+}
+
 extern "C" int qhg_launch_step(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
                                int cell_grid, cudaStream_t stream) {
-    using namespace qhg;
-    const int C = P->num_cells;
-    const int ntiles = (C + kScanTile - 1) / kScanTile;
-    k_actions<<<cell_grid, kWarpsPerCta * 32, 0, stream>>>(
-        *P, rs, B->cell_start, B->nonempty, B->id, B->birth, B->age, B->lastb, B->meta,
-        B->nbr, B->nnbr, B->K, B->wthr, B->wflag, B->outc, B->father, B->brank, B->clsc);
-    k_cell_scan<<<ntiles, kScanThreads, 0, stream>>>(
-        *P, rs, B->cell_start, B->nbr, B->nnbr, B->rev, B->clsc, B->cell_start2, B->sbase, B->bbase,
-        B->bidbase, B->obase, B->nonempty2, B->tile_flag, B->tile_agg, B->tile_incl);
-    k_scatter<<<cell_grid, kWarpsPerCta * 32, 0, stream>>>(
-        *P, rs, B->cell_start, B->nonempty, B->id, B->birth, B->age, B->lastb, B->outc, B->father,
-        B->brank, B->nnbr, B->sbase, B->bbase, B->bidbase, B->obase, B->id2, B->birth2, B->age2,
-        B->lastb2, B->meta2, B->blog, B->blog_cap);
+    launch_kernels(P, rs, B, cell_grid, stream, nullptr);
     return (int)cudaGetLastError();
 }
 
 extern "C" int qhg_launch_step_timed(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
                                      int cell_grid, cudaStream_t stream, cudaEvent_t *ev) {
-    using namespace qhg;
-    const int C = P->num_cells;
-    const int ntiles = (C + kScanTile - 1) / kScanTile;
-    cudaEventRecord(ev[0], stream);
-    k_actions<<<cell_grid, kWarpsPerCta * 32, 0, stream>>>(
-        *P, rs, B->cell_start, B->nonempty, B->id, B->birth, B->age, B->lastb, B->meta,
-        B->nbr, B->nnbr, B->K, B->wthr, B->wflag, B->outc, B->father, B->brank, B->clsc);
-    cudaEventRecord(ev[1], stream);
-    k_cell_scan<<<ntiles, kScanThreads, 0, stream>>>(
-        *P, rs, B->cell_start, B->nbr, B->nnbr, B->rev, B->clsc, B->cell_start2, B->sbase, B->bbase,
-        B->bidbase, B->obase, B->nonempty2, B->tile_flag, B->tile_agg, B->tile_incl);
-    cudaEventRecord(ev[2], stream);
-    k_scatter<<<cell_grid, kWarpsPerCta * 32, 0, stream>>>(
-        *P, rs, B->cell_start, B->nonempty, B->id, B->birth, B->age, B->lastb, B->outc, B->father,
-        B->brank, B->nnbr, B->sbase, B->bbase, B->bidbase, B->obase, B->id2, B->birth2, B->age2,
-        B->lastb2, B->meta2, B->blog, B->blog_cap);
-    cudaEventRecord(ev[3], stream);
+    launch_kernels(P, rs, B, cell_grid, stream, ev);
     return (int)cudaGetLastError();
+}
+
+// CTAs of the tile kernels that fit on one SM at once (the smaller of the two)
+extern "C" int qhg_tile_ctas_per_sm(void) {
+    int a = 0, b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, qhg::k_actions, qhg::kTileThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, qhg::k_scatter, qhg::kTileThreads, 0);
+    const int m = a < b ? a : b;
+    return m > 0 ? m : 1;
 }

@@ -19,7 +19,6 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libqhg_gpu.so")
 
 QHG_FLAG_LOG_BIRTHS = 1
-QHG_FLAG_KERNEL_TIMING = 2
 
 ERRORS = {
     -1: "QHG_ERR_ARG", -2: "QHG_ERR_CUDA", -3: "QHG_ERR_NOMEM", -4: "QHG_ERR_STATE",
@@ -31,7 +30,8 @@ EXPORTS = [
     "qhg_gpu_last_error", "qhg_gpu_version", "qhg_gpu_create", "qhg_gpu_upload_grid",
     "qhg_gpu_upload_agents", "qhg_gpu_step", "qhg_gpu_sync", "qhg_gpu_num_agents",
     "qhg_gpu_current_step", "qhg_gpu_download", "qhg_gpu_counts", "qhg_gpu_stats",
-    "qhg_gpu_birth_log", "qhg_gpu_stream", "qhg_gpu_destroy", "qhg_gpu_kernel_times",
+    "qhg_gpu_birth_log", "qhg_gpu_stream", "qhg_gpu_destroy", "qhg_gpu_step_profiled",
+    "qhg_gpu_step_timed",
 ]
 
 
@@ -96,7 +96,8 @@ def load_library(path: str = LIB_PATH):
         "qhg_gpu_birth_log": (I, [P, P, P, P, ct.c_int64, P]),
         "qhg_gpu_stream": (I, [P, P]),
         "qhg_gpu_destroy": (I, [P]),
-        "qhg_gpu_kernel_times": (I, [P, P]),
+        "qhg_gpu_step_profiled": (I, [P, ct.c_int32, P]),
+        "qhg_gpu_step_timed": (I, [P, ct.c_int32, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -140,9 +141,9 @@ class GpuRun:
     """One simulation held by libqhg_gpu.so on a CUDA device."""
 
     def __init__(self, grid: Grid, actions: Sequence[Action], seed: int, genetics: Genetics = Genetics(),
-                 log_births: bool = False, capacity: int = 0, timing: bool = False, device: int = 0):
+                 log_births: bool = False, capacity: int = 0, device: int = 0):
         lib = load_library()
-        flags = (QHG_FLAG_LOG_BIRTHS if log_births else 0) | (QHG_FLAG_KERNEL_TIMING if timing else 0)
+        flags = QHG_FLAG_LOG_BIRTHS if log_births else 0
         self._desc = make_desc(actions, seed, genetics, capacity, flags, device)
         h = ct.c_void_p()
         _check(lib.qhg_gpu_create(ct.byref(self._desc), ct.byref(h)))
@@ -219,10 +220,23 @@ class GpuRun:
         o = np.argsort(b, kind="stable")
         return np.stack([b[o], m[o], f[o]], axis=1)
 
-    def kernel_times(self) -> np.ndarray:
-        t = np.zeros(4, dtype=np.float32)
-        _check(_lib.qhg_gpu_kernel_times(self.h, _p(t)))
-        return t
+    def step_profiled(self, n: int) -> np.ndarray:
+        """Runs n steps with per-kernel CUDA events; returns ms[n, 4]
+        (actions, cell scan, scatter, genomes)."""
+        t = np.zeros((max(1, n), 4), dtype=np.float32)
+        _check(_lib.qhg_gpu_step_profiled(self.h, int(n), _p(t)))
+        return t[:n]
+
+    def step_timed(self, n: int) -> float:
+        """Runs n steps between CUDA events on the run's stream; returns ms."""
+        ms = ct.c_float()
+        _check(_lib.qhg_gpu_step_timed(self.h, int(n), ct.byref(ms)))
+        return float(ms.value)
+
+    def stream_handle(self) -> int:
+        s = ct.c_void_p()
+        _check(_lib.qhg_gpu_stream(self.h, ct.byref(s)))
+        return int(s.value or 0)
 
     def close(self) -> None:
         if getattr(self, "h", None):
