@@ -50,6 +50,8 @@ struct qhg_run {
     uint8_t *d_nnbr = nullptr;
     uint32_t *d_rev = nullptr;
     double *d_K = nullptr;
+    ulonglong2 *d_vthr = nullptr;   // per-cell Verhulst thresholds of the coming step
+    std::vector<double> h_K;
     uint64_t *d_wthr = nullptr;
     uint8_t *d_wflag = nullptr;
     std::vector<int32_t> h_nbr;
@@ -110,6 +112,29 @@ static uint64_t host_prob_threshold(double x) {
     double y = x * 4294967296.0;
     if (y >= 4294967296.0) return 4294967296ull;
     return (uint64_t)std::ceil(y);
+}
+
+// the thresholds the device computes in verhulst_thresholds(), for the first
+// step after an upload (same expressions, same rounding)
+static ulonglong2 host_verhulst_thresholds(const StepConst &P, double Kcell, uint32_t n) {
+    const ActionConst &A = P.act[P.verhulst_act[0]];
+    double B, D;
+    const double K = (A.type == kVerhulst) ? A.K : Kcell;
+    if (A.type == kVerhulstVarK && K <= 0.0) {
+        B = 0.0;
+        D = 1.0;
+    } else {
+        const double r = (double)n / K;
+        B = A.b0 + A.th_b0 * r;
+        D = A.d0 + A.th_d0 * r;
+    }
+    uint64_t x = 0;
+    if (B > 0.0) x = host_prob_threshold(B) | (1ull << 62);
+    else if (B < 0.0) x = host_prob_threshold(-B) | (2ull << 62);
+    ulonglong2 v;
+    v.x = x;
+    v.y = host_prob_threshold(D);
+    return v;
 }
 
 // largest float f with (double)f <= x
@@ -283,10 +308,11 @@ extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_
             }
         }
     }
-    cudaFree(r->d_nbr); cudaFree(r->d_nnbr); cudaFree(r->d_rev); cudaFree(r->d_K);
+    cudaFree(r->d_nbr); cudaFree(r->d_nnbr); cudaFree(r->d_rev); cudaFree(r->d_K); cudaFree(r->d_vthr);
     cudaFree(r->d_wthr); cudaFree(r->d_wflag);
     cudaFree(r->d_clsc); cudaFree(r->d_sbase); cudaFree(r->d_bbase); cudaFree(r->d_bidb);
     cudaFree(r->d_obase); cudaFree(r->d_tflag); cudaFree(r->d_tagg); cudaFree(r->d_tincl);
+    r->d_vthr = nullptr;
     r->grid_ok = false;
     r->agents_ok = false;
     drop_graphs(r);
@@ -295,6 +321,7 @@ extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_
     CUDA_TRY(cudaMalloc(&r->d_nnbr, (size_t)C));
     CUDA_TRY(cudaMalloc(&r->d_rev, (size_t)C * sizeof(uint32_t)));
     CUDA_TRY(cudaMalloc(&r->d_K, (size_t)C * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&r->d_vthr, (size_t)C * sizeof(ulonglong2)));
     CUDA_TRY(cudaMalloc(&r->d_wthr, (size_t)C * 6 * sizeof(uint64_t)));
     CUDA_TRY(cudaMalloc(&r->d_wflag, (size_t)C));
     CUDA_TRY(cudaMalloc(&r->d_clsc, (size_t)C * kCls * sizeof(uint32_t)));
@@ -315,6 +342,7 @@ extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_
     CUDA_TRY(cudaMemsetAsync(r->d_tflag, 0, (size_t)ntiles * sizeof(uint32_t), r->stream));
     CUDA_TRY(cudaStreamSynchronize(r->stream));
     r->h_nbr.assign(nbr6, nbr6 + (size_t)C * 6);
+    r->h_K.assign(K, K + C);
     r->C = C;
     r->P.num_cells = C;
     r->grid_ok = true;
@@ -438,6 +466,12 @@ extern "C" int qhg_gpu_upload_agents(qhg_run *r, const qhg_agents_soa *a, int64_
     }
     CUDA_TRY(cudaMemcpyAsync(r->d_nes[0], nes.data(), nes.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, r->stream));
     CUDA_TRY(cudaMemcpyAsync(r->d_tf[0], tf.data(), tf.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, r->stream));
+    std::vector<ulonglong2> vthr;
+    if (r->P.n_verhulst > 0) {
+        vthr.resize(C);
+        for (int c = 0; c < C; c++) vthr[c] = host_verhulst_thresholds(r->P, r->h_K[c], cnt[(size_t)c + 1] - cnt[c]);
+        CUDA_TRY(cudaMemcpyAsync(r->d_vthr, vthr.data(), (size_t)C * sizeof(ulonglong2), cudaMemcpyHostToDevice, r->stream));
+    }
     CUDA_TRY(cudaMemsetAsync(r->d_clsc, 0, (size_t)C * kCls * sizeof(uint32_t), r->stream));
     memset(r->h_rs, 0, sizeof(RunState));
     r->h_rs->step = first_step;
@@ -463,7 +497,7 @@ static StepBuffers make_buffers(qhg_run *r, int cur) {
     B.nonempty2 = r->d_ne[nx]; B.ne_start2 = r->d_nes[nx]; B.tile_first2 = r->d_tf[nx];
     B.id2 = r->d_id[nx]; B.birth2 = r->d_birth[nx]; B.age2 = r->d_age[nx]; B.lastb2 = r->d_lastb[nx];
     B.meta2 = r->d_meta[nx];
-    B.nbr = r->d_nbr; B.nnbr = r->d_nnbr; B.rev = r->d_rev; B.K = r->d_K; B.wthr = r->d_wthr;
+    B.nbr = r->d_nbr; B.nnbr = r->d_nnbr; B.rev = r->d_rev; B.K = r->d_K; B.vthr = r->d_vthr; B.wthr = r->d_wthr;
     B.wflag = r->d_wflag;
     B.outc = r->d_outc; B.father = r->d_father; B.brank = r->d_brank; B.clsc = r->d_clsc;
     B.sbase = r->d_sbase; B.bbase = r->d_bbase; B.bidbase = r->d_bidb; B.obase = r->d_obase;
@@ -695,7 +729,7 @@ extern "C" int qhg_gpu_destroy(qhg_run *r) {
     if (r->stream) cudaStreamSynchronize(r->stream);
     drop_graphs(r);
     free_agents(r);
-    cudaFree(r->d_nbr); cudaFree(r->d_nnbr); cudaFree(r->d_rev); cudaFree(r->d_K);
+    cudaFree(r->d_nbr); cudaFree(r->d_nnbr); cudaFree(r->d_rev); cudaFree(r->d_K); cudaFree(r->d_vthr);
     cudaFree(r->d_wthr); cudaFree(r->d_wflag);
     cudaFree(r->d_clsc); cudaFree(r->d_sbase); cudaFree(r->d_bbase); cudaFree(r->d_bidb);
     cudaFree(r->d_obase); cudaFree(r->d_tflag); cudaFree(r->d_tagg); cudaFree(r->d_tincl);

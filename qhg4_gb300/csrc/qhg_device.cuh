@@ -114,6 +114,8 @@ struct StepBuffers {
     // rev packs, 3 bits per neighbour slot q, the slot of this cell in the
     // neighbour's own list
     const int32_t *nbr; const uint8_t *nnbr; const uint32_t *rev; const double *K;
+    // Verhulst thresholds of each cell for the coming step (written by the scan)
+    ulonglong2 *vthr;
     const uint64_t *wthr; const uint8_t *wflag;
     uint8_t *outc; int32_t *father; uint16_t *brank; uint32_t *clsc;
     uint32_t *sbase; uint32_t *bbase; uint32_t *bidbase; uint32_t *obase;

@@ -74,10 +74,47 @@ __device__ __forceinline__ uint64_t prob_threshold(double x) {
     return (uint64_t)ceil(y);
 }
 
-// per-cell class counts: slot 0 stay, 1..6 movers to neighbour slot 0..5, 7 births;
-// two 16-bit counters per shared word
-__device__ __forceinline__ void count_slot(uint32_t *cls, int slot) {
-    atomicAdd(&cls[slot >> 1], 1u << (16 * (slot & 1)));
+// LinearBirth / LinearDeath ::initialize for one cell holding n agents
+// (actions/LinearBirth.cpp:90-112, actions/LinearDeath.cpp:92-122), as
+// integer thresholds: x = birth (kind 1) or birth-rate death (kind 2)
+// threshold with the kind in bits 62-63, y = death threshold
+__device__ __forceinline__ ulonglong2 verhulst_thresholds(const StepConst &P, double Kcell, uint32_t n) {
+    const ActionConst &A = P.act[P.verhulst_act[0]];
+    double B, D;
+    const double K = (A.type == kVerhulst) ? A.K : Kcell;
+    if (A.type == kVerhulstVarK && K <= 0.0) {
+        B = 0.0;
+        D = 1.0;
+    } else {
+        const double r = __ddiv_rn((double)n, K);
+        B = __dadd_rn(A.b0, __dmul_rn(A.th_b0, r));
+        D = __dadd_rn(A.d0, __dmul_rn(A.th_d0, r));
+    }
+    uint64_t x = 0;
+    if (B > 0.0) x = prob_threshold(B) | (1ull << 62);
+    else if (B < 0.0) x = prob_threshold(-B) | (2ull << 62);
+    return make_ulonglong2(x, prob_threshold(D));
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Warp-aggregated shared-memory counter: lanes with the same key add `unit`
+// each to *addr with one atomic per key; every lane gets the old value plus
+// unit times its rank within the key.  All 32 lanes must call it (lanes with
+// valid == false pass along and get 0).
+__device__ __forceinline__ uint32_t warp_agg_add(bool valid, uint32_t key, uint32_t *addr, uint32_t unit) {
+    const uint32_t k = valid ? key : 0xffffffffu;
+    const uint32_t peers = __match_any_sync(FULL_MASK, k);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (valid && lane == leader) base = atomicAdd(addr, (uint32_t)__popc(peers) * unit);
+    base = __shfl_sync(FULL_MASK, base, leader);
+    return valid ? base + (uint32_t)__popc(peers & lanemask_lt()) * unit : 0u;
 }
 
 __device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t *red) {
@@ -98,6 +135,7 @@ __device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t *red) {
 struct ActionsSmem {
     int64_t id[kTileMax];
     uint8_t meta[kTileMax];
+    uint8_t head[kTileMax];        // first row of a cell
     uint8_t bfl[kTileMax];         // gives birth this step
     uint16_t cell[kTileMax];       // local cell index of each row
     int16_t mate[kTileMax];        // mate's row within the tile, -1 none
@@ -116,7 +154,7 @@ struct ActionsSmem {
     uint32_t t, r0, r1;
 };
 
-__global__ void __launch_bounds__(kTileThreads)
+__global__ void __launch_bounds__(kTileThreads, 4)
 k_actions(const StepConst P, RunState *__restrict__ rs,
           const uint32_t *__restrict__ nonempty, const uint32_t *__restrict__ ne_start,
           const uint32_t *__restrict__ tile_first,
@@ -124,7 +162,7 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
           const float *__restrict__ age, const float *__restrict__ lastb,
           const uint8_t *__restrict__ meta,
           const int32_t *__restrict__ nbr, const uint8_t *__restrict__ nnbr,
-          const double *__restrict__ Kc, const uint64_t *__restrict__ wthr,
+          const ulonglong2 *__restrict__ vthr, const uint64_t *__restrict__ wthr,
           const uint8_t *__restrict__ wflag,
           uint8_t *__restrict__ outc, int32_t *__restrict__ father, uint16_t *__restrict__ brank,
           uint32_t *__restrict__ clsc) {
@@ -137,20 +175,23 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
     const uint32_t ntiles = (N + kTileAgents - 1) / kTileAgents;
     uint32_t cnt_births = 0, cnt_deaths = 0, cnt_moves = 0;
 
-    for (;;) {
-        __syncthreads();
-        if (tid == 0) {
-            const uint32_t t = atomicAdd(&rs->action_tiles, 1u);
-            S.t = t;
-            if (t < ntiles) {
-                S.r0 = tile_first[t];
-                S.r1 = tile_first[t + 1];
-            }
+    // tiles are dealt out statically; the next tile's bounds and the current
+    // tile's agent fields are loaded early so that their latency overlaps the
+    // cell set-up and the pairing phases
+    constexpr int RA = kTileMax / kTileThreads;
+    uint32_t nr0 = 0, nr1 = 0;
+    if (blockIdx.x < ntiles) {
+        nr0 = tile_first[blockIdx.x];
+        nr1 = tile_first[blockIdx.x + 1];
+    }
+    for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const uint32_t r0 = nr0;
+        const int nc = (int)(nr1 - r0);
+        const uint32_t tn = t + gridDim.x;
+        if (tn < ntiles) {
+            nr0 = tile_first[tn];
+            nr1 = tile_first[tn + 1];
         }
-        __syncthreads();
-        if (S.t >= ntiles) break;
-        const uint32_t r0 = S.r0;
-        const int nc = (int)(S.r1 - r0);
         if (nc == 0) continue;
         const uint32_t a0 = ne_start[r0];
         const int na = (int)(ne_start[r0 + nc] - a0);
@@ -158,6 +199,21 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
             if (tid == 0) set_error(rs, kErrCellTooLarge, r0);
             continue;
         }
+        int64_t pid[RA];
+        uint8_t pm[RA];
+        float pb[RA], pa[RA], pl[RA];
+#pragma unroll
+        for (int j = 0; j < RA; j++) {
+            const int i = tid + j * kTileThreads;
+            if (i < na) {
+                pid[j] = id[a0 + i];
+                pm[j] = meta[a0 + i];
+                pb[j] = birth[a0 + i];
+                pa[j] = P.reads_age ? age[a0 + i] : 0.0f;
+                pl[j] = lastb[a0 + i];
+            }
+        }
+        __syncthreads();   // the previous tile is done with the shared arrays
         // ---- cells: ids, rows, Verhulst thresholds (LinearBirth / LinearDeath
         // ::initialize, actions/LinearBirth.cpp:90-112, actions/LinearDeath.cpp:92-122)
         for (int lc = tid; lc < nc; lc += kTileThreads) {
@@ -171,36 +227,53 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
             S.nm[lc] = 0u;
             S.cls[lc][0] = S.cls[lc][1] = S.cls[lc][2] = S.cls[lc][3] = 0u;
             if (P.n_verhulst > 0) {
-                const ActionConst &A = P.act[P.verhulst_act[0]];
-                double B, D;
-                const double K = (A.type == kVerhulst) ? A.K : Kc[c];
-                if (A.type == kVerhulstVarK && K <= 0.0) {
-                    B = 0.0;
-                    D = 1.0;
-                } else {
-                    const double r = __ddiv_rn((double)(ce - cs), K);
-                    B = __dadd_rn(A.b0, __dmul_rn(A.th_b0, r));
-                    D = __dadd_rn(A.d0, __dmul_rn(A.th_d0, r));
-                }
-                uint8_t kind = 0;
-                uint64_t tb = 0;
-                if (B > 0.0) { kind = 1; tb = prob_threshold(B); }
-                else if (B < 0.0) { kind = 2; tb = prob_threshold(-B); }
-                S.tk[lc] = kind;
-                S.tb[lc] = tb;
-                S.td[lc] = prob_threshold(D);
+                // computed by the previous step's cell scan for this step's counts
+                const ulonglong2 v = vthr[c];
+                S.tk[lc] = (uint8_t)(v.x >> 62);
+                S.tb[lc] = v.x & ((1ull << 62) - 1ull);
+                S.td[lc] = v.y;
             }
         }
-        for (int i = tid; i < na; i += kTileThreads) {
-            S.meta[i] = meta[a0 + i];
-            S.id[i] = id[a0 + i];
-            S.mate[i] = -1;
-            S.bfl[i] = 0;
+#pragma unroll
+        for (int j = 0; j < RA; j++) {
+            const int i = tid + j * kTileThreads;
+            if (i < na) {
+                S.meta[i] = pm[j];
+                S.id[i] = pid[j];
+                S.mate[i] = -1;
+                S.bfl[i] = 0;
+                S.head[i] = 0;
+            }
         }
         __syncthreads();
-        for (int lc = tid; lc < nc; lc += kTileThreads) {
-            const int ce = (int)S.cstart[lc + 1];
-            for (int i = (int)S.cstart[lc]; i < ce; i++) S.cell[i] = (uint16_t)lc;
+        for (int lc = tid; lc < nc; lc += kTileThreads) S.head[S.cstart[lc]] = 1;
+        __syncthreads();
+        // local cell of each row: count of cell heads up to the row (block scan
+        // over contiguous rows per thread)
+        {
+            const int i0 = tid * RA;
+            uint32_t h[RA];
+            uint32_t tot = 0;
+#pragma unroll
+            for (int j = 0; j < RA; j++) {
+                tot += (i0 + j < na) ? S.head[i0 + j] : 0u;
+                h[j] = tot;
+            }
+            const int lane = tid & 31, warp = tid >> 5;
+            uint32_t inc = tot;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(FULL_MASK, inc, o);
+                if (lane >= o) inc += y;
+            }
+            if (lane == 31) S.red[warp] = inc;
+            __syncthreads();
+            uint32_t base = inc - tot;
+            for (int w = 0; w < warp; w++) base += S.red[w];
+#pragma unroll
+            for (int j = 0; j < RA; j++) {
+                if (i0 + j < na) S.cell[i0 + j] = (uint16_t)(base + h[j] - 1u);
+            }
         }
         __syncthreads();
         // ---- RandomPair::findMates (actions/RandomPair.cpp:146-270), members in
@@ -208,17 +281,19 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
         if (P.has_pair) {
             // unsorted FERTILE lists: females from the cell's first row up, males
             // from its last row down
-            for (int i = tid; i < na; i += kTileThreads) {
-                const uint8_t m = S.meta[i];
-                if (m & kMetaFertile) {
-                    const int lc = S.cell[i];
-                    if (m & kMetaGender) {
-                        const uint32_t q = atomicAdd(&S.nm[lc], 1u);
-                        S.pick[S.cstart[lc + 1] - 1u - q] = (uint16_t)i;
-                    } else {
-                        const uint32_t q = atomicAdd(&S.nf[lc], 1u);
-                        S.pick[S.cstart[lc] + q] = (uint16_t)i;
-                    }
+#pragma unroll
+            for (int j = 0; j < RA; j++) {
+                const int i = tid + j * kTileThreads;
+                if (__all_sync(FULL_MASK, i >= na)) break;
+                const uint8_t m = (i < na) ? S.meta[i] : (uint8_t)0;
+                const bool fert = (m & kMetaFertile) != 0;
+                const bool male = (m & kMetaGender) != 0;
+                const int lc = fert ? S.cell[i] : 0;
+                uint32_t *ctr = male ? &S.nm[lc] : &S.nf[lc];
+                const uint32_t q = warp_agg_add(fert, ((uint32_t)lc << 1) | (male ? 1u : 0u), ctr, 1u);
+                if (fert) {
+                    if (male) S.pick[S.cstart[lc + 1] - 1u - q] = (uint16_t)i;
+                    else S.pick[S.cstart[lc] + q] = (uint16_t)i;
                 }
             }
             __syncthreads();
@@ -296,21 +371,27 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
             __syncthreads();
         }
         // ---- every action on every agent (SPopulation::doActions)
-        for (int i = tid; i < na; i += kTileThreads) {
+#pragma unroll
+        for (int j = 0; j < RA; j++) {
+            const int i = tid + j * kTileThreads;
+            if (__all_sync(FULL_MASK, i >= na)) break;
+            const bool in_tile = i < na;
+            int cls = 0, lc = 0;
+            bool bflag = false;
+            if (in_tile) {
             const uint32_t row = a0 + (uint32_t)i;
-            const int lc = S.cell[i];
+            lc = S.cell[i];
             const int c = S.cid[lc];
-            const uint8_t m8 = S.meta[i];
-            const float fb = birth[row];
-            float fa = P.reads_age ? age[row] : 0.0f;
-            const float fl = lastb[row];
+            const uint8_t m8 = pm[j];
+            const float fb = pb[j];
+            float fa = pa[j];
+            const float fl = pl[j];
             const bool female = !(m8 & kMetaGender);
             bool fert = (m8 & kMetaFertile) != 0;
             bool alive = true;
-            bool bflag = false;
             int dir = 0;
             AgentDraws dr;
-            dr.init(P.seed, (uint32_t)step, S.id[i]);
+            dr.init(P.seed, (uint32_t)step, pid[j]);
             for (int a = 0; a < P.n_act && alive; a++) {
                 const ActionConst &A = P.act[a];
                 switch (A.type) {
@@ -388,16 +469,21 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
                     break;
                 }
             }
-            const int cls = alive ? (1 + dir) : 0;
+            cls = alive ? (1 + dir) : 0;
             outc[row] = (uint8_t)(cls | (bflag ? kOutBirth : 0) | (fert ? kOutFertile : 0) |
                                   ((m8 & kMetaGender) ? kOutGender : 0));
-            if (cls) count_slot(S.cls[lc], cls - 1);
             if (bflag) {
                 father[row] = (int32_t)(a0 + (uint32_t)S.mate[i]);
                 S.bfl[i] = 1;
-                count_slot(S.cls[lc], 7);
                 cnt_births++;
             }
+            }
+            // per-cell class counts (slot 0 stay, 1..6 movers, 7 births), two
+            // 16-bit counters per shared word, one atomic per (cell, slot) and warp
+            const int slot = (cls > 0) ? cls - 1 : 0;
+            warp_agg_add(in_tile && cls > 0, ((uint32_t)lc << 3) | (uint32_t)slot, &S.cls[lc][slot >> 1],
+                         1u << (16 * (slot & 1)));
+            warp_agg_add(in_tile && bflag, ((uint32_t)lc << 3) | 7u, &S.cls[lc][3], 1u << 16);
         }
         __syncthreads();
         // ---- per cell: mothers' birth ranks by ID (births are numbered in
@@ -465,6 +551,7 @@ __global__ void __launch_bounds__(kScanThreads)
 k_cell_scan(const StepConst P, RunState *__restrict__ rs,
             const int32_t *__restrict__ nbr, const uint8_t *__restrict__ nnbr,
             const uint32_t *__restrict__ rev, const uint32_t *__restrict__ clsc,
+            const double *__restrict__ Kc, ulonglong2 *__restrict__ vthr,
             uint32_t *__restrict__ sbase, uint32_t *__restrict__ bbase,
             uint32_t *__restrict__ bidbase, uint32_t *__restrict__ obase,
             uint32_t *__restrict__ new_nonempty, uint32_t *__restrict__ new_ne_start,
@@ -630,6 +717,7 @@ k_cell_scan(const StepConst P, RunState *__restrict__ rs,
             if (nnew[j] > 0u) {
                 new_nonempty[pre.ne] = (uint32_t)d;
                 new_ne_start[pre.ne] = pre.n;
+                if (P.n_verhulst > 0) vthr[d] = verhulst_thresholds(P, Kc[d], nnew[j]);
                 // tiles begin at the first cell starting at or after t * kTileAgents
                 // (rows past the capacity are never written: the step fails with kErrCapacity)
                 const uint32_t e = min(pre.n + nnew[j], P.capacity);
@@ -651,6 +739,7 @@ k_cell_scan(const StepConst P, RunState *__restrict__ rs,
 // ----------------------------------------------------------------- scatter
 struct ScatterSmem {
     uint8_t code[kTileMax];
+    uint8_t head[kTileMax];        // first row of a cell
     uint16_t rank[kTileMax];       // stable rank among the cell's agents of the same class
     uint16_t cell[kTileMax];
     uint32_t cstart[kTileCells + 1];
@@ -658,6 +747,10 @@ struct ScatterSmem {
     uint32_t bb[kTileCells];
     uint32_t bid[kTileCells];
     uint32_t ob[kTileCells][6];
+    uint64_t clo[kTileCells];      // scan value at each cell's first row
+    uint64_t chi[kTileCells];
+    uint64_t wlo[kTileThreads / 32];
+    uint64_t whi[kTileThreads / 32];
     uint32_t t, r0, r1;
 };
 
@@ -685,27 +778,50 @@ k_scatter(const StepConst P, RunState *__restrict__ rs,
     const uint32_t N = rs->n_agents;
     const uint32_t cap = P.capacity;
     const uint32_t ntiles = (N + kTileAgents - 1) / kTileAgents;
-    for (;;) {
-        __syncthreads();
-        if (tid == 0) {
-            const uint32_t t = atomicAdd(&rs->scatter_tiles, 1u);
-            S.t = t;
-            if (t < ntiles) {
-                S.r0 = tile_first[t];
-                S.r1 = tile_first[t + 1];
-            }
+    constexpr int RA = kTileMax / kTileThreads;
+    uint32_t nr0 = 0, nr1 = 0;
+    if (blockIdx.x < ntiles) {
+        nr0 = tile_first[blockIdx.x];
+        nr1 = tile_first[blockIdx.x + 1];
+    }
+    for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const uint32_t r0 = nr0;
+        const int nc = (int)(nr1 - r0);
+        const uint32_t tn = t + gridDim.x;
+        if (tn < ntiles) {
+            nr0 = tile_first[tn];
+            nr1 = tile_first[tn + 1];
         }
-        __syncthreads();
-        if (S.t >= ntiles) break;
-        const uint32_t r0 = S.r0;
-        const int nc = (int)(S.r1 - r0);
         if (nc == 0) continue;
         const uint32_t a0 = ne_start[r0];
         const int na = (int)(ne_start[r0 + nc] - a0);
         if (na > kTileMax || nc > kTileCells) continue;   // reported by k_actions
+        uint8_t pc[RA];
+        int64_t pid[RA];
+        float pb[RA], pa[RA], pl[RA];
+#pragma unroll
+        for (int j = 0; j < RA; j++) {
+            const int i = tid + j * kTileThreads;
+            pc[j] = 0;
+            if (i < na) {
+                pc[j] = outc[a0 + i];
+                pid[j] = id[a0 + i];
+                pb[j] = birth[a0 + i];
+                pa[j] = P.age_from_birth ? 0.0f : age[a0 + i];
+                pl[j] = lastb[a0 + i];
+            }
+        }
+        __syncthreads();   // the previous tile is done with the shared arrays
+#pragma unroll
+        for (int j = 0; j < RA; j++) {
+            const int i = tid + j * kTileThreads;
+            if (i < na) S.head[i] = 0;
+        }
+        __syncthreads();
         for (int lc = tid; lc < nc; lc += kTileThreads) {
             const uint32_t c = nonempty[r0 + lc];
             S.cstart[lc] = ne_start[r0 + lc] - a0;
+            S.head[ne_start[r0 + lc] - a0] = 1;
             if (lc == nc - 1) S.cstart[nc] = ne_start[r0 + lc + 1] - a0;
             S.sb[lc] = sbase[c];
             S.bb[lc] = bbase[c];
@@ -717,26 +833,77 @@ k_scatter(const StepConst P, RunState *__restrict__ rs,
             z[0] = make_uint4(0u, 0u, 0u, 0u);
             z[1] = make_uint4(0u, 0u, 0u, 0u);
         }
-        for (int i = tid; i < na; i += kTileThreads) S.code[i] = outc[a0 + i];
+#pragma unroll
+        for (int j = 0; j < RA; j++) {
+            const int i = tid + j * kTileThreads;
+            if (i < na) S.code[i] = pc[j];
+        }
         __syncthreads();
-        // stable ranks per (cell, class): one thread walks each cell; classes
-        // 1..4 and 5..7 counted in 16-bit fields of two words
-        for (int lc = tid; lc < nc; lc += kTileThreads) {
-            uint64_t lo = 0ull, hi = 0ull;
-            const int ce = (int)S.cstart[lc + 1];
-            for (int i = (int)S.cstart[lc]; i < ce; i++) {
-                S.cell[i] = (uint16_t)lc;
-                const int k = S.code[i] & 7;
+        // stable ranks per (cell, class): a block-wide exclusive scan of one-hot
+        // class counters (classes 1..4 and 5..7 in 16-bit fields of two words)
+        // over the tile's rows, minus the value at the first row of the cell
+        {
+            constexpr int R = kTileMax / kTileThreads;
+            const int i0 = tid * R;
+            uint64_t lo[R], hi[R];
+            uint64_t tlo = 0ull, thi = 0ull;
+#pragma unroll
+            for (int j = 0; j < R; j++) {
+                const int i = i0 + j;
+                // field 3 of the high word counts cell heads (first rows)
+                if (i < na && S.head[i]) thi += 1ull << 48;
+                lo[j] = tlo;
+                hi[j] = thi;
+                const int k = (i < na) ? (S.code[i] & 7) : 0;
                 if (k) {
-                    const int sh = 16 * ((k - 1) & 3);
-                    if (k <= 4) { S.rank[i] = (uint16_t)(lo >> sh); lo += 1ull << sh; }
-                    else { S.rank[i] = (uint16_t)(hi >> sh); hi += 1ull << sh; }
+                    const uint64_t one = 1ull << (16 * ((k - 1) & 3));
+                    if (k <= 4) tlo += one; else thi += one;
+                }
+            }
+            const int lane = tid & 31, warp = tid >> 5;
+            uint64_t ilo = tlo, ihi = thi;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint64_t ylo = __shfl_up_sync(FULL_MASK, ilo, o);
+                const uint64_t yhi = __shfl_up_sync(FULL_MASK, ihi, o);
+                if (lane >= o) { ilo += ylo; ihi += yhi; }
+            }
+            if (lane == 31) { S.wlo[warp] = ilo; S.whi[warp] = ihi; }
+            __syncthreads();
+            uint64_t blo = ilo - tlo, bhi = ihi - thi;
+            for (int w = 0; w < warp; w++) { blo += S.wlo[w]; bhi += S.whi[w]; }
+#pragma unroll
+            for (int j = 0; j < R; j++) {
+                const int i = i0 + j;
+                if (i < na) {
+                    lo[j] += blo;
+                    hi[j] += bhi;
+                    const int lc = (int)(hi[j] >> 48) - 1;   // heads up to and including row i
+                    S.cell[i] = (uint16_t)lc;
+                    if (S.head[i]) { S.clo[lc] = lo[j]; S.chi[lc] = hi[j] & ((1ull << 48) - 1ull); }
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < R; j++) {
+                const int i = i0 + j;
+                if (i < na) {
+                    const int k = S.code[i] & 7;
+                    if (k) {
+                        const int lc = S.cell[i];
+                        const int sh = 16 * ((k - 1) & 3);
+                        const uint64_t v = (k <= 4) ? (lo[j] - S.clo[lc]) : ((hi[j] & ((1ull << 48) - 1ull)) - S.chi[lc]);
+                        S.rank[i] = (uint16_t)(v >> sh);
+                    }
                 }
             }
         }
         __syncthreads();
-        for (int i = tid; i < na; i += kTileThreads) {
-            const uint8_t code = S.code[i];
+#pragma unroll
+        for (int j = 0; j < RA; j++) {
+            const int i = tid + j * kTileThreads;
+            if (i >= na) break;
+            const uint8_t code = pc[j];
             const int k = code & 7;
             const uint32_t row = a0 + (uint32_t)i;
             const int lc = S.cell[i];
@@ -745,11 +912,11 @@ k_scatter(const StepConst P, RunState *__restrict__ rs,
                 if (dst >= cap) {   // inconsistent bases: record, never write out of range
                     set_error(rs, kErrInternal, 3u);
                 } else {
-                    const float fb = birth[row];
-                    id2[dst] = id[row];
+                    const float fb = pb[j];
+                    id2[dst] = pid[j];
                     birth2[dst] = fb;
-                    lastb2[dst] = lastb[row];
-                    age2[dst] = P.age_from_birth ? __fsub_rn(fT, fb) : age[row];
+                    lastb2[dst] = pl[j];
+                    age2[dst] = P.age_from_birth ? __fsub_rn(fT, fb) : pa[j];
                     meta2[dst] = (uint8_t)(((code & kOutGender) ? kMetaGender : 0) |
                                            ((code & kOutFertile) ? kMetaFertile : 0));
                 }
@@ -764,7 +931,7 @@ k_scatter(const StepConst P, RunState *__restrict__ rs,
                 if (!ok) {
                     set_error(rs, kErrInternal, 4u);
                 } else {
-                    const int64_t mid = id[row];
+                    const int64_t mid = pid[j];
                     const uint32_t u = draw_block(P.seed, (uint32_t)step, mid, kStreamBirth).v[0];
                     const uint8_t g = (uint8_t)(u >> 31);
                     const int64_t baby = next_id + (int64_t)(S.bid[lc] + rk);
@@ -819,10 +986,10 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
     if (ev) cudaEventRecord(ev[0], stream);
     k_actions<<<grid, kTileThreads, 0, stream>>>(
         *P, rs, B->nonempty, B->ne_start, B->tile_first, B->id, B->birth, B->age, B->lastb, B->meta,
-        B->nbr, B->nnbr, B->K, B->wthr, B->wflag, B->outc, B->father, B->brank, B->clsc);
+        B->nbr, B->nnbr, B->vthr, B->wthr, B->wflag, B->outc, B->father, B->brank, B->clsc);
     if (ev) cudaEventRecord(ev[1], stream);
     k_cell_scan<<<ntiles, kScanThreads, 0, stream>>>(
-        *P, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->sbase, B->bbase, B->bidbase, B->obase,
+        *P, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr, B->sbase, B->bbase, B->bidbase, B->obase,
         B->nonempty2, B->ne_start2, B->tile_first2, B->tile_flag, B->tile_agg, B->tile_incl);
     if (ev) cudaEventRecord(ev[2], stream);
     k_scatter<<<grid, kTileThreads, 0, stream>>>(
