@@ -19,6 +19,7 @@
 extern "C" int qhg_launch_step(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
                                int cell_grid, cudaStream_t stream);
 extern "C" int qhg_tile_ctas_per_sm(void);
+extern "C" int qhg_match_program(const int32_t *types, int n);
 extern "C" int qhg_launch_step_timed(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
                                      int cell_grid, cudaStream_t stream, cudaEvent_t *ev);
 
@@ -214,6 +215,8 @@ extern "C" int qhg_gpu_create(const qhg_run_desc *desc, qhg_run **out) {
         case kRandomMove:
         case kWeightedMove:
             A.pthr = host_prob_threshold(p[0]);
+            P.has_move = 1;
+            if (A.type == kWeightedMove) P.has_wmove = 1;
             w += 2;
             break;
         default:
@@ -225,6 +228,7 @@ extern "C" int qhg_gpu_create(const qhg_run_desc *desc, qhg_run **out) {
         delete r;
         return fail(QHG_ERR_ARG, "too many draws per agent");
     }
+    P.program = qhg_match_program(desc->action_type, desc->n_actions);
     cudaError_t e = cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&r->d_rs, sizeof(RunState));
     if (e == cudaSuccess) e = cudaMallocHost(&r->h_rs, sizeof(RunState));

@@ -77,6 +77,9 @@ struct StepConst {
     int32_t reads_age;       // some action reads the stored age before GetOld/OldAgeDeath sets it
     int32_t n_verhulst;
     int32_t verhulst_act[kMaxVerhulst];
+    int32_t program;         // specialised action program (0: interpreted)
+    int32_t has_move;        // RandomMove or WeightedMove present
+    int32_t has_wmove;       // WeightedMove present
     ActionConst act[kMaxActions];
 };
 

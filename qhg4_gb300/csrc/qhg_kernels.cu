@@ -132,6 +132,23 @@ __device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t *red) {
 }
 
 // ------------------------------------------------------------------ actions
+// Action programs compiled into specialised k_actions kernels.  Program 0
+// interprets the run's action list at run time; programs 1-3 are the orders
+// of the benchmark populations (ascending priority): 1 Fertility,
+// RandomPair, Verhulst, RandomMove, GetOld; 2 Fertility, RandomPair,
+// VerhulstVarK, WeightedMove, GetOld, OldAgeDeath; 3 as 1 with VerhulstVarK.
+__host__ __device__ constexpr int prog_len(int p) {
+    return p == 1 ? 5 : (p == 2 ? 6 : (p == 3 ? 5 : 0));
+}
+__host__ __device__ constexpr int prog_act(int p, int a) {
+    return p == 1 ? (a == 0 ? kFertility : a == 1 ? kRandomPair : a == 2 ? kVerhulst : a == 3 ? kRandomMove : kGetOld)
+         : p == 2 ? (a == 0 ? kFertility : a == 1 ? kRandomPair : a == 2 ? kVerhulstVarK : a == 3 ? kWeightedMove
+                     : a == 4 ? kGetOld : kOldAgeDeath)
+         : p == 3 ? (a == 0 ? kFertility : a == 1 ? kRandomPair : a == 2 ? kVerhulstVarK : a == 3 ? kRandomMove : kGetOld)
+         : -1;
+}
+constexpr int kNumPrograms = 4;
+
 struct ActionsSmem {
     int64_t id[kTileMax];
     uint8_t meta[kTileMax];
@@ -154,6 +171,7 @@ struct ActionsSmem {
     uint32_t t, r0, r1;
 };
 
+template <int PROG>
 __global__ void __launch_bounds__(kTileThreads, 4)
 k_actions(const StepConst P, RunState *__restrict__ rs,
           const uint32_t *__restrict__ nonempty, const uint32_t *__restrict__ ne_start,
@@ -226,6 +244,9 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
             S.nf[lc] = 0u;
             S.nm[lc] = 0u;
             S.cls[lc][0] = S.cls[lc][1] = S.cls[lc][2] = S.cls[lc][3] = 0u;
+            // neighbour and weight rows of the cell, read by the move actions
+            if (P.has_move) asm volatile("prefetch.global.L1 [%0];" ::"l"(nbr + (size_t)c * 6));
+            if (P.has_wmove) asm volatile("prefetch.global.L1 [%0];" ::"l"(wthr + (size_t)c * 6));
             if (P.n_verhulst > 0) {
                 // computed by the previous step's cell scan for this step's counts
                 const ulonglong2 v = vthr[c];
@@ -392,9 +413,12 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
             int dir = 0;
             AgentDraws dr;
             dr.init(P.seed, (uint32_t)step, pid[j]);
-            for (int a = 0; a < P.n_act && alive; a++) {
+            constexpr int NA = PROG ? prog_len(PROG) : kMaxActions;
+#pragma unroll (PROG ? NA : 1)
+            for (int a = 0; a < NA; a++) {
+                if ((PROG == 0 && a >= P.n_act) || !alive) break;
                 const ActionConst &A = P.act[a];
-                switch (A.type) {
+                switch (PROG ? prog_act(PROG, a) : A.type) {
                 case kGetOld:
                     fa = __fsub_rn(fT, fb);
                     break;
@@ -826,8 +850,10 @@ k_scatter(const StepConst P, RunState *__restrict__ rs,
             S.sb[lc] = sbase[c];
             S.bb[lc] = bbase[c];
             S.bid[lc] = bidbase[c];
-            const int nn = nnbr[c];
-            for (int k = 0; k < nn; k++) S.ob[lc][k] = obase[(size_t)c * 6 + k];
+            // all six slots (unused ones hold stale values that no agent reads),
+            // so that the loads do not wait for the neighbour count
+#pragma unroll
+            for (int k = 0; k < 6; k++) S.ob[lc][k] = obase[(size_t)c * 6 + k];
             // the class counts are consumed: clear them for the next step
             uint4 *z = reinterpret_cast<uint4 *>(clsc + (size_t)c * kCls);
             z[0] = make_uint4(0u, 0u, 0u, 0u);
@@ -984,9 +1010,17 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
     using namespace qhg;
     const int ntiles = (P->num_cells + kScanTile - 1) / kScanTile;
     if (ev) cudaEventRecord(ev[0], stream);
-    k_actions<<<grid, kTileThreads, 0, stream>>>(
-        *P, rs, B->nonempty, B->ne_start, B->tile_first, B->id, B->birth, B->age, B->lastb, B->meta,
-        B->nbr, B->nnbr, B->vthr, B->wthr, B->wflag, B->outc, B->father, B->brank, B->clsc);
+#define QHG_LAUNCH_ACTIONS(PR)                                                                       \
+    k_actions<PR><<<grid, kTileThreads, 0, stream>>>(                                                 \
+        *P, rs, B->nonempty, B->ne_start, B->tile_first, B->id, B->birth, B->age, B->lastb, B->meta,  \
+        B->nbr, B->nnbr, B->vthr, B->wthr, B->wflag, B->outc, B->father, B->brank, B->clsc)
+    switch (P->program) {
+    case 1: QHG_LAUNCH_ACTIONS(1); break;
+    case 2: QHG_LAUNCH_ACTIONS(2); break;
+    case 3: QHG_LAUNCH_ACTIONS(3); break;
+    default: QHG_LAUNCH_ACTIONS(0); break;
+    }
+#undef QHG_LAUNCH_ACTIONS
     if (ev) cudaEventRecord(ev[1], stream);
     k_cell_scan<<<ntiles, kScanThreads, 0, stream>>>(
         *P, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr, B->sbase, B->bbase, B->bidbase, B->obase,
@@ -1014,8 +1048,19 @@ extern "C" int qhg_launch_step_timed(const qhg::StepConst *P, qhg::RunState *rs,
 // CTAs of the tile kernels that fit on one SM at once (the smaller of the two)
 extern "C" int qhg_tile_ctas_per_sm(void) {
     int a = 0, b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, qhg::k_actions, qhg::kTileThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, qhg::k_actions<0>, qhg::kTileThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, qhg::k_scatter, qhg::kTileThreads, 0);
     const int m = a < b ? a : b;
     return m > 0 ? m : 1;
+}
+
+// the specialised action program matching a run's action list, 0 if none
+extern "C" int qhg_match_program(const int32_t *types, int n) {
+    for (int p = 1; p < qhg::kNumPrograms; p++) {
+        if (qhg::prog_len(p) != n) continue;
+        bool ok = true;
+        for (int a = 0; a < n && ok; a++) ok = (qhg::prog_act(p, a) == types[a]);
+        if (ok) return p;
+    }
+    return 0;
 }

@@ -124,12 +124,16 @@ def config1_actions(b0=0.2, d0=0.05, theta=0.01, K=30.0, move_p=0.1,
     ]
 
 
-def config2_actions(b0=0.2, d0=0.05, theta=0.01, move_p=0.2, max_age=64.0,
+def config2_actions(b0=0.5, d0=0.02, theta=0.01, move_p=0.2, max_age=64.0,
                     uncertainty=5.0 / 64.0, fert_min=15.0, fert_max=45.0,
                     interbirth=2.0) -> List[Action]:
     """Single large run: GetOld, Fertility, RandomPair, VerhulstVarK (per-cell
     K), OldAgeDeath (onset uniform in [60,70): max age 64, uncertainty 5/64)
-    and WeightedMove."""
+    and WeightedMove.  The run's Verhulst rates are not fixed by its
+    description; b0=0.5, d0=0.02, theta=0.01 keep a 20M population placed in
+    proportion to K near its equilibrium (the plain method's b0=0.2, d0=0.05
+    let it decay to a quarter within ~100 steps, because only paired fertile
+    females give birth)."""
     return [
         Action(ACT_FERTILITY, 2, (fert_min, fert_max, interbirth)),
         Action(ACT_RANDOMPAIR, 3),

@@ -60,3 +60,25 @@ def test_config2_small(gpu_lib):
     grid, agents, acts = case_config2()
     o, g, st = run_both(grid, agents, acts, 40, 5)
     assert_same(o, g, st, 40)
+
+
+def test_interpreted_program_order(gpu_lib):
+    """An action order that matches no specialised kernel program runs the
+    run-time interpreter; GetOld first, OldAgeDeath before Verhulst and both
+    move actions."""
+    grid, agents, _ = case_config2(n=12, N=20000, seed=11)
+    acts = [Action(ACT_GETOLD, 1), Action(ACT_FERTILITY, 2, (15.0, 45.0, 2.0)), Action(ACT_RANDOMPAIR, 3),
+            Action(ACT_OLDAGEDEATH, 4, (64.0, 5.0 / 64.0)), Action(ACT_VERHULSTVARK, 6, (0.25, 0.04, 0.01)),
+            Action(ACT_RANDOMMOVE, 7, (0.05,)), Action(ACT_WEIGHTEDMOVE, 8, (0.15,))]
+    o, g, st = run_both(grid, agents, acts, 30, 123)
+    assert_same(o, g, st, 30)
+
+
+def test_no_pairing_no_moves(gpu_lib):
+    """Without RandomPair no female has a mate: no births; no move actions."""
+    grid, agents, _ = case_config1(n=6, N=8000, seed=2)
+    acts = [Action(ACT_FERTILITY, 2, (15.0, 45.0, 2.0)), Action(ACT_VERHULST, 6, (0.2, 0.05, 0.01, 30.0)),
+            Action(ACT_GETOLD, 8)]
+    o, g, st = run_both(grid, agents, acts, 15, 5)
+    assert_same(o, g, st, 15)
+    assert st[:, 1].sum() == 0
