@@ -162,6 +162,32 @@ int qhg_gpu_step_profiled(qhg_run *run, int32_t nsteps, float *kernel_ms);
  * the run's stream, waits, and returns the device time in *elapsed_ms */
 int qhg_gpu_step_timed(qhg_run *run, int32_t nsteps, float *elapsed_ms);
 
+/*
+ * Per-cell census of a caller-owned agent table, for callers that cannot
+ * allocate device memory (a host runtime with its own fixed device pool, a
+ * real-time loop that must not hit cudaMalloc/cudaFree, a device whose heap
+ * is exhausted).  This entry point has no counterpart in the reference.
+ *
+ * d_agent_cell: device array of n_agents cell indices (any order);
+ * d_counts (num_cells) receives the live agents per cell and d_first_row
+ * (num_cells + 1) the exclusive prefix of the counts, i.e. the first row of
+ * each cell in a table sorted by cell, with the agent count last.  Runs on
+ * `stream` (a cudaStream_t, NULL for the default stream) and waits for it.
+ *
+ * It allocates nothing: its scratch (the look-back status words) is a
+ * file-scope __device__ array sized for QHG_CENSUS_MAX_CELLS cells, held by
+ * every GPU that loads the library until the process exits.  Larger grids
+ * are rejected with QHG_ERR_ARG.  The first call on a device looks up the
+ * array's device address with that device current, so make it before any
+ * stream capture.  All calls on a device share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller.
+ */
+#define QHG_CENSUS_MAX_CELLS  4194304
+int qhg_gpu_cell_census_noalloc(const int32_t *d_agent_cell, int64_t n_agents, int32_t num_cells,
+                                uint32_t *d_counts, uint32_t *d_first_row, void *stream);
+/* the last error of qhg_gpu_cell_census_noalloc on the calling thread */
+const char *qhg_gpu_census_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libqhg_gpu.so")
-SOURCES = ["qhg_kernels.cu", "qhg_api.cu"]
+SOURCES = ["qhg_kernels.cu", "qhg_api.cu", "qhg_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
          "-I" + os.path.join(HERE, "..", "include")]

@@ -31,7 +31,7 @@ EXPORTS = [
     "qhg_gpu_upload_agents", "qhg_gpu_step", "qhg_gpu_sync", "qhg_gpu_num_agents",
     "qhg_gpu_current_step", "qhg_gpu_download", "qhg_gpu_counts", "qhg_gpu_stats",
     "qhg_gpu_birth_log", "qhg_gpu_stream", "qhg_gpu_destroy", "qhg_gpu_step_profiled",
-    "qhg_gpu_step_timed",
+    "qhg_gpu_step_timed", "qhg_gpu_cell_census_noalloc", "qhg_gpu_census_last_error",
 ]
 
 
@@ -98,6 +98,8 @@ def load_library(path: str = LIB_PATH):
         "qhg_gpu_destroy": (I, [P]),
         "qhg_gpu_step_profiled": (I, [P, ct.c_int32, P]),
         "qhg_gpu_step_timed": (I, [P, ct.c_int32, P]),
+        "qhg_gpu_cell_census_noalloc": (I, [P, ct.c_int64, ct.c_int32, P, P, P]),
+        "qhg_gpu_census_last_error": (ct.c_char_p, []),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
