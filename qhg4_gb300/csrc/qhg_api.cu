@@ -20,6 +20,8 @@ extern "C" int qhg_launch_step(const qhg::StepConst *P, qhg::RunState *rs, const
                                int cell_grid, cudaStream_t stream);
 extern "C" int qhg_tile_ctas_per_sm(void);
 extern "C" int qhg_match_program(const int32_t *types, int n);
+extern "C" int qhg_launch_gather_genomes(const int32_t *gslot, const uint64_t *genome, uint32_t n, int words,
+                                         uint32_t slots, uint64_t *out, cudaStream_t stream);
 extern "C" int qhg_launch_step_timed(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
                                      int cell_grid, cudaStream_t stream, cudaEvent_t *ev);
 
@@ -75,6 +77,13 @@ struct qhg_run {
     uint4 *d_tagg = nullptr, *d_tincl = nullptr;
     int64_t *d_blog = nullptr;
     uint64_t blog_cap = 0;
+    // genetics: genome slab indexed by slot, each agent's slot (ping-pong with
+    // the table), the free slots (ping-pong) and one record per birth
+    uint32_t gcap = 0;
+    int32_t *d_gslot[2] = {nullptr, nullptr};
+    uint32_t *d_free[2] = {nullptr, nullptr};
+    uint64_t *d_genome = nullptr;
+    uint32_t *d_brec = nullptr;
     RunState *d_rs = nullptr;
     RunState *h_rs = nullptr;   // pinned
     // step state
@@ -83,7 +92,7 @@ struct qhg_run {
     bool grid_ok = false, agents_ok = false;
     int cell_grid = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     std::vector<int64_t> stage;  // host staging for uploads
 };
 
@@ -97,6 +106,13 @@ static void free_agents(qhg_run *r) {
     }
     cudaFree(r->d_outc); cudaFree(r->d_father); cudaFree(r->d_brank); cudaFree(r->d_blog);
     r->d_outc = nullptr; r->d_father = nullptr; r->d_brank = nullptr; r->d_blog = nullptr;
+    for (int p = 0; p < 2; p++) {
+        cudaFree(r->d_gslot[p]); cudaFree(r->d_free[p]);
+        r->d_gslot[p] = nullptr; r->d_free[p] = nullptr;
+    }
+    cudaFree(r->d_genome); cudaFree(r->d_brec);
+    r->d_genome = nullptr; r->d_brec = nullptr;
+    r->gcap = 0;
     r->cap = 0;
 }
 
@@ -145,6 +161,89 @@ static float float_floor_of(double x) {
     return f;
 }
 
+// Numerical Recipes' log-gamma, continued fraction and regularised incomplete
+// beta function I_x(a, b) (Press et al., Numerical Recipes in C, 2nd ed.,
+// 6.1 and 6.4), the functions the reference's utils/bino_tools.cpp uses.
+static double nr_lngamma(double xx) {
+    static const double c[6] = {76.18009172947146, -86.50532032941677, 24.01409824083091,
+                                -1.231739572450155, 0.1208650973866179e-2, -0.5395239384953e-5};
+    double y = xx + 1;
+    double t = xx + 5.5;
+    t -= (xx + 0.5) * std::log(t);
+    double ser = 1.000000000190015;
+    for (int j = 0; j < 6; j++) {
+        ser += c[j] / y;
+        y++;
+    }
+    return -t + std::log(2.5066282746310005 * ser / xx);
+}
+
+static double nr_beta_cf(double a, double b, double x) {
+    const double tiny = (double)1.0e-30f;
+    const double qab = a + b, qap = a + 1.0, qam = a - 1.0;
+    double c = 1.0;
+    double d = 1.0 - qab * x / qap;
+    if (std::fabs(d) < tiny) d = tiny;
+    d = 1.0 / d;
+    double h = d;
+    int m = 1;
+    for (; m <= 100; m++) {
+        const int m2 = 2 * m;
+        double aa = m * (b - m) * x / ((qam + m2) * (a + m2));
+        d = 1.0 + aa * d;
+        if (std::fabs(d) < tiny) d = tiny;
+        c = 1.0 + aa / c;
+        if (std::fabs(c) < tiny) c = tiny;
+        d = 1.0 / d;
+        h *= d * c;
+        aa = -(a + m) * (qab + m) * x / ((a + m2) * (qap + m2));
+        d = 1.0 + aa * d;
+        if (std::fabs(d) < tiny) d = tiny;
+        c = 1.0 + aa / c;
+        if (std::fabs(c) < tiny) c = tiny;
+        d = 1.0 / d;
+        const double del = d * c;
+        h *= del;
+        if (std::fabs(del - 1.0) < 3.0e-7) break;
+    }
+    return m > 100 ? -1.0 : h;
+}
+
+static double nr_beta_inc(double a, double b, double x) {
+    if (x < 0.0 || x > 1.0) return -1.0;
+    double bt = 0.0;
+    if (x != 0.0 && x != 1.0) {
+        bt = std::exp(nr_lngamma(a + b) - nr_lngamma(a) - nr_lngamma(b) + a * std::log(x) + b * std::log(1.0 - x));
+    }
+    if (x < (a + 1.0) / (a + b + 2.0)) return bt * nr_beta_cf(a, b, x) / a;
+    return 1.0 - bt * nr_beta_cf(b, a, 1.0 - x) / b;
+}
+
+// BinomialDist::buildTable (utils/BinomialDist.cpp:61-89): entry k-1 is
+// P(X < k) = 1 - I_p(k, n-k+1) for X ~ Binomial(n, p), k = 1, 2, ... until the
+// tail I_p drops to eps (the entry of that k included)
+static std::vector<double> binomial_table(double p, int n, double eps) {
+    std::vector<double> v;
+    int k = 1;
+    double tail = nr_beta_inc(k, n - k + 1, p);
+    while (tail > eps && k < n && v.size() <= (size_t)kMaxBinomial) {
+        v.push_back(tail);
+        k++;
+        tail = nr_beta_inc(k, n - k + 1, p);
+    }
+    v.push_back(tail);
+    for (double &x : v) x = 1 - x;
+    return v;
+}
+
+// BinomialDist::getN compares wrandd() = u / 2^32 > L; u / 2^32 > L <=> u > floor(L * 2^32)
+static int64_t bino_threshold(double L) {
+    const double y = std::floor(L * 4294967296.0);
+    if (y >= 4294967296.0) return 4294967296ll;
+    if (y < -1.0) return -1ll;
+    return (int64_t)y;
+}
+
 extern "C" const char *qhg_gpu_last_error(void) { return g_last_error.c_str(); }
 
 extern "C" const char *qhg_gpu_version(void) { return "qhg_gpu 0.1 (sm_103a)"; }
@@ -153,7 +252,14 @@ extern "C" int qhg_gpu_create(const qhg_run_desc *desc, qhg_run **out) {
     if (desc == nullptr || out == nullptr) return fail(QHG_ERR_ARG, "null argument");
     if (desc->n_actions < 0 || desc->n_actions > QHG_MAX_ACTIONS) return fail(QHG_ERR_ARG, "bad n_actions");
     if (desc->genome_size < 0) return fail(QHG_ERR_ARG, "bad genome_size");
-    if (desc->genome_size > 0) return fail(QHG_ERR_ARG, "genetics is not supported by this build");
+    if (desc->genome_size > kMaxGenomeBlocks * 64) return fail(QHG_ERR_ARG, "genome_size above 4096 loci");
+    if (desc->genome_size > 0 && desc->num_crossover != QHG_CROSSOVER_POISSON1 &&
+        (desc->num_crossover < 0 || desc->num_crossover > kMaxFixedCrossover)) {
+        return fail(QHG_ERR_ARG, "num_crossover must be QHG_CROSSOVER_POISSON1 or in 0..30");
+    }
+    if (desc->genome_size > 0 && !(desc->mutation_rate >= 0.0 && desc->mutation_rate < 1.0)) {
+        return fail(QHG_ERR_ARG, "mutation_rate must be in [0, 1)");
+    }
     int ndev = 0;
     CUDA_TRY(cudaGetDeviceCount(&ndev));
     if (desc->device < 0 || desc->device >= ndev) return fail(QHG_ERR_ARG, "bad device ordinal");
@@ -227,6 +333,21 @@ extern "C" int qhg_gpu_create(const qhg_run_desc *desc, qhg_run **out) {
     if (w > 4 * 64) {
         delete r;
         return fail(QHG_ERR_ARG, "too many draws per agent");
+    }
+    if (desc->genome_size > 0) {
+        P.genome_size = desc->genome_size;
+        P.genome_words = 2 * ((desc->genome_size + 63) / 64);
+        P.num_crossover = desc->num_crossover;
+        P.has_mutation = desc->mutation_rate > 0.0 ? 1 : 0;
+        if (P.has_mutation) {
+            std::vector<double> tab = binomial_table(desc->mutation_rate, 2 * desc->genome_size, 1e-6);
+            if ((int)tab.size() > kMaxBinomial) {
+                delete r;
+                return fail(QHG_ERR_ARG, "mutation rate too high: more than 64 mutation counts in the table");
+            }
+            P.n_binomial = (int32_t)tab.size();
+            for (size_t i = 0; i < tab.size(); i++) P.bino[i] = bino_threshold(tab[i]);
+        }
     }
     P.program = qhg_match_program(desc->action_type, desc->n_actions);
     cudaError_t e = cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking);
@@ -375,6 +496,19 @@ static int alloc_agents(qhg_run *r, uint32_t cap) {
     } else {
         r->blog_cap = 0;
     }
+    if (r->P.genome_words > 0) {
+        // slots in use during a step: the live agents plus the step's births
+        // (at most one per live female), so 2 * capacity never runs out
+        const uint64_t g = std::min<uint64_t>((uint64_t)cap * 2, 0x7fffffffull);
+        for (int p = 0; p < 2; p++) {
+            CUDA_TRY(cudaMalloc(&r->d_gslot[p], (size_t)cap * sizeof(int32_t)));
+            CUDA_TRY(cudaMalloc(&r->d_free[p], (size_t)g * sizeof(uint32_t)));
+        }
+        CUDA_TRY(cudaMalloc(&r->d_genome, (size_t)g * r->P.genome_words * sizeof(uint64_t)));
+        CUDA_TRY(cudaMalloc(&r->d_brec, (size_t)cap * 5 * sizeof(uint32_t)));
+        r->gcap = (uint32_t)g;
+        r->P.genome_capacity = (uint32_t)g;
+    }
     r->cap = cap;
     r->P.capacity = cap;
     return QHG_OK;
@@ -387,6 +521,7 @@ extern "C" int qhg_gpu_upload_agents(qhg_run *r, const qhg_agents_soa *a, int64_
                   a->last_birth == nullptr || a->gender == nullptr || a->state == nullptr)) {
         return fail(QHG_ERR_ARG, "null agent column");
     }
+    if (n > 0 && r->P.genome_words > 0 && a->genome == nullptr) return fail(QHG_ERR_ARG, "null genome column");
     if (first_step < 0) return fail(QHG_ERR_ARG, "negative first step");
     CUDA_TRY(cudaSetDevice(r->desc.device));
     const int C = r->C;
@@ -470,6 +605,20 @@ extern "C" int qhg_gpu_upload_agents(qhg_run *r, const qhg_agents_soa *a, int64_
     }
     CUDA_TRY(cudaMemcpyAsync(r->d_nes[0], nes.data(), nes.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, r->stream));
     CUDA_TRY(cudaMemcpyAsync(r->d_tf[0], tf.data(), tf.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, r->stream));
+    std::vector<uint64_t> h_gen;
+    std::vector<int32_t> h_gslot;
+    if (r->P.genome_words > 0 && live > 0) {
+        // row k of the sorted table owns genome slot k
+        const size_t gw = (size_t)r->P.genome_words;
+        h_gen.resize((size_t)live * gw);
+        h_gslot.resize((size_t)live);
+        for (int64_t k = 0; k < live; k++) {
+            memcpy(&h_gen[(size_t)k * gw], a->genome + (size_t)order[(size_t)k] * gw, gw * sizeof(uint64_t));
+            h_gslot[(size_t)k] = (int32_t)k;
+        }
+        CUDA_TRY(cudaMemcpyAsync(r->d_genome, h_gen.data(), h_gen.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, r->stream));
+        CUDA_TRY(cudaMemcpyAsync(r->d_gslot[0], h_gslot.data(), live * sizeof(int32_t), cudaMemcpyHostToDevice, r->stream));
+    }
     std::vector<ulonglong2> vthr;
     if (r->P.n_verhulst > 0) {
         vthr.resize(C);
@@ -482,6 +631,7 @@ extern "C" int qhg_gpu_upload_agents(qhg_run *r, const qhg_agents_soa *a, int64_
     r->h_rs->n_agents = (uint32_t)live;
     r->h_rs->next_id = maxid + 1;
     r->h_rs->n_nonempty = (uint32_t)ne.size();
+    r->h_rs->hwm = (uint32_t)live;
     CUDA_TRY(cudaMemcpyAsync(r->d_rs, r->h_rs, sizeof(RunState), cudaMemcpyHostToDevice, r->stream));
     const int ntiles = (C + kScanTile - 1) / kScanTile;
     CUDA_TRY(cudaMemsetAsync(r->d_tflag, 0, (size_t)ntiles * sizeof(uint32_t), r->stream));
@@ -507,6 +657,9 @@ static StepBuffers make_buffers(qhg_run *r, int cur) {
     B.sbase = r->d_sbase; B.bbase = r->d_bbase; B.bidbase = r->d_bidb; B.obase = r->d_obase;
     B.tile_flag = r->d_tflag; B.tile_agg = r->d_tagg; B.tile_incl = r->d_tincl;
     B.blog = r->d_blog; B.blog_cap = r->blog_cap;
+    B.gslot = r->d_gslot[cur]; B.gslot2 = r->d_gslot[nx];
+    B.freelist = r->d_free[cur]; B.freelist2 = r->d_free[nx];
+    B.genome = r->d_genome; B.brec = r->d_brec;
     return B;
 }
 
@@ -546,7 +699,7 @@ extern "C" int qhg_gpu_step_timed(qhg_run *r, int32_t nsteps, float *elapsed_ms)
     if (r == nullptr || elapsed_ms == nullptr) return fail(QHG_ERR_ARG, "null argument");
     CUDA_TRY(cudaSetDevice(r->desc.device));
     if (r->ev[0] == nullptr) {
-        for (int i = 0; i < 4; i++) CUDA_TRY(cudaEventCreate(&r->ev[i]));
+        for (int i = 0; i < 5; i++) CUDA_TRY(cudaEventCreate(&r->ev[i]));
     }
     CUDA_TRY(cudaEventRecord(r->ev[0], r->stream));
     int rc = qhg_gpu_step(r, nsteps);
@@ -562,19 +715,19 @@ extern "C" int qhg_gpu_step_profiled(qhg_run *r, int32_t nsteps, float *kernel_m
     if (!r->grid_ok || !r->agents_ok) return fail(QHG_ERR_STATE, "upload grid and agents first");
     CUDA_TRY(cudaSetDevice(r->desc.device));
     if (r->ev[0] == nullptr) {
-        for (int i = 0; i < 4; i++) CUDA_TRY(cudaEventCreate(&r->ev[i]));
+        for (int i = 0; i < 5; i++) CUDA_TRY(cudaEventCreate(&r->ev[i]));
     }
     for (int32_t s = 0; s < nsteps; s++) {
         StepBuffers B = make_buffers(r, r->cur);
         int le = qhg_launch_step_timed(&r->P, r->d_rs, &B, r->cell_grid, r->stream, r->ev);
         if (le != 0) return fail(QHG_ERR_CUDA, std::string("launch: ") + cudaGetErrorString((cudaError_t)le));
-        CUDA_TRY(cudaEventSynchronize(r->ev[3]));
-        for (int k = 0; k < 3; k++) {
+        const bool gen = r->P.genome_words > 0;
+        CUDA_TRY(cudaEventSynchronize(r->ev[gen ? 4 : 3]));
+        for (int k = 0; k < 4; k++) {
             float ms = 0.0f;
-            CUDA_TRY(cudaEventElapsedTime(&ms, r->ev[k], r->ev[k + 1]));
+            if (k < 3 || gen) CUDA_TRY(cudaEventElapsedTime(&ms, r->ev[k], r->ev[k + 1]));
             kernel_ms[s * 4 + k] = ms;
         }
-        kernel_ms[s * 4 + 3] = 0.0f;
         r->cur ^= 1;
     }
     return QHG_OK;
@@ -594,6 +747,7 @@ static int pull_state(qhg_run *r) {
         r->h_rs->scatter_ctas_done = 0u;
         r->h_rs->action_tiles = 0u;
         r->h_rs->scatter_tiles = 0u;
+        r->h_rs->dead_count = 0u;
         // the failed step's partial statistics would be counted again on retry
         unsigned long long *st = r->h_rs->stats[(uint32_t)r->h_rs->step % kStatsRing];
         st[0] = st[1] = st[2] = st[3] = 0ull;
@@ -671,6 +825,17 @@ extern "C" int qhg_gpu_download(qhg_run *r, qhg_agents_soa *o, int64_t cap, int6
         o->gender[i] = meta[(size_t)i] & kMetaGender;
         o->state[i] = (meta[(size_t)i] & kMetaFertile) ? QHG_LS_FERTILE : QHG_LS_ALIVE;
     }
+    if (r->P.genome_words > 0 && o->genome != nullptr && N > 0) {
+        const size_t gw = (size_t)r->P.genome_words;
+        uint64_t *tmp = nullptr;
+        CUDA_TRY(cudaMalloc(&tmp, (size_t)N * gw * sizeof(uint64_t)));
+        int le = qhg_launch_gather_genomes(r->d_gslot[cur], r->d_genome, (uint32_t)N, r->P.genome_words,
+                                           r->gcap, tmp, r->stream);
+        cudaError_t e = le == 0 ? cudaStreamSynchronize(r->stream) : (cudaError_t)le;
+        if (e == cudaSuccess) e = cudaMemcpy(o->genome, tmp, (size_t)N * gw * sizeof(uint64_t), cudaMemcpyDeviceToHost);
+        cudaFree(tmp);
+        if (e != cudaSuccess) return fail(QHG_ERR_CUDA, std::string("genome gather: ") + cudaGetErrorString(e));
+    }
     return QHG_OK;
 }
 
@@ -739,7 +904,7 @@ extern "C" int qhg_gpu_destroy(qhg_run *r) {
     cudaFree(r->d_obase); cudaFree(r->d_tflag); cudaFree(r->d_tagg); cudaFree(r->d_tincl);
     cudaFree(r->d_rs);
     cudaFreeHost(r->h_rs);
-    for (int i = 0; i < 4; i++) {
+    for (int i = 0; i < 5; i++) {
         if (r->ev[i]) cudaEventDestroy(r->ev[i]);
     }
     if (r->stream) cudaStreamDestroy(r->stream);

@@ -29,6 +29,14 @@ constexpr uint32_t kStreamActions = 0u;
 constexpr uint32_t kStreamPair = 64u;
 constexpr uint32_t kStreamBirth = 128u;
 
+// genetics: at most 64 blocks of 64 loci per strand, Poisson(1) counts capped
+// at 16, and at most 128 draws of the birth stream per newborn
+constexpr int kMaxGenomeBlocks = 64;
+constexpr int kMaxBinomial = 64;
+constexpr int kBirthDraws = 128;
+constexpr int kMaxFixedCrossover = 30;   // 3 + 2*30 + 1 + 64 draws fit kBirthDraws
+constexpr int kCrossoverPoisson1 = -100;
+
 // agent meta byte: bit 0 gender, bit 1 fertile (life state 5, else 1)
 constexpr uint8_t kMetaGender = 1u;
 constexpr uint8_t kMetaFertile = 2u;
@@ -73,6 +81,15 @@ struct StepConst {
     int32_t num_cells;
     int32_t log_births;
     int32_t genome_words;    // 2 * blocks, 0 without genetics
+    int32_t genome_size;     // loci per strand
+    int32_t num_crossover;   // > 0 fixed count, 0 none, kCrossoverPoisson1
+    int32_t has_mutation;    // mutation rate > 0
+    int32_t n_binomial;      // entries of the mutation-count table
+    uint32_t genome_capacity;  // genome slots
+    // BinomialDist::getN as integer thresholds: the count is the first i
+    // with u <= bino[i] (u the 32-bit draw), n_binomial if none; bino[i] =
+    // floor(L_i * 2^32) of the table entry L_i, so u / 2^32 > L_i <=> u > bino[i]
+    int64_t bino[kMaxBinomial];
     uint32_t capacity;
     int32_t reads_age;       // some action reads the stored age before GetOld/OldAgeDeath sets it
     int32_t n_verhulst;
@@ -100,6 +117,13 @@ struct RunState {
     uint32_t new_n_nonempty;
     uint32_t births;
     uint64_t birth_log_n;
+    // genome slots: the free list of the current step (slots of agents that
+    // died in the previous step, plus unused ones carried over) and the
+    // high-water mark of never used slots
+    uint32_t nfree;
+    uint32_t hwm;
+    uint32_t dead_count;     // deaths of this step pushed to the next free list
+    int32_t genome_step;     // step whose newborns k_genomes builds
     // statistics ring: [step % kStatsRing][live, births, deaths, moves]
     unsigned long long stats[kStatsRing][4];
 };
@@ -124,6 +148,14 @@ struct StepBuffers {
     uint32_t *sbase; uint32_t *bbase; uint32_t *bidbase; uint32_t *obase;
     uint32_t *tile_flag; uint4 *tile_agg; uint4 *tile_incl;
     int64_t *blog; uint64_t blog_cap;
+    // genetics: genome slot per agent (current, next), the genome slab
+    // (genome_capacity x genome_words), free lists (current, next), and one
+    // record per newborn by global birth rank: {mother slot, father slot,
+    // baby slot, mother ID low, mother ID high}
+    const int32_t *gslot; int32_t *gslot2;
+    uint64_t *genome;
+    const uint32_t *freelist; uint32_t *freelist2;
+    uint32_t *brec;
 };
 
 // ------------------------------------------------------------- Philox

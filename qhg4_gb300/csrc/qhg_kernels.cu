@@ -24,6 +24,7 @@
 //
 // The reference runs these as SPopulation::initializeStep / doActions /
 // finalizeStep (core/SPopulation.cpp:394-577, 596-724, 1058-1092, 509-536).
+#include <algorithm>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -791,7 +792,10 @@ k_scatter(const StepConst P, RunState *__restrict__ rs,
           uint32_t *__restrict__ clsc,
           int64_t *__restrict__ id2, float *__restrict__ birth2, float *__restrict__ age2,
           float *__restrict__ lastb2, uint8_t *__restrict__ meta2,
-          int64_t *__restrict__ blog, uint64_t blog_cap) {
+          int64_t *__restrict__ blog, uint64_t blog_cap,
+          const int32_t *__restrict__ gslot, int32_t *__restrict__ gslot2,
+          const uint32_t *__restrict__ freelist, uint32_t *__restrict__ freelist2,
+          uint32_t *__restrict__ brec) {
     __shared__ ScatterSmem S;
     if (rs->error != 0u) return;   // the state stays as before the step
     const int tid = threadIdx.x;
@@ -803,6 +807,20 @@ k_scatter(const StepConst P, RunState *__restrict__ rs,
     const uint32_t cap = P.capacity;
     const uint32_t ntiles = (N + kTileAgents - 1) / kTileAgents;
     constexpr int RA = kTileMax / kTileThreads;
+    // genome slots (SPopulation::recycleDeadSpaceNew, core/SPopulation.cpp:596-724):
+    // newborns take the slots freed by the previous step's deaths, in birth
+    // order, then never used slots; this step's deaths free theirs for the
+    // next step, so a newborn never overwrites a parent of the same step
+    const bool genetics = P.genome_words > 0;
+    const uint32_t births = rs->births;
+    const uint32_t nfree = rs->nfree;
+    const uint32_t hwm = rs->hwm;
+    const uint32_t carry = nfree > births ? nfree - births : 0u;
+    if (genetics) {
+        for (uint32_t q = blockIdx.x * blockDim.x + tid; q < carry; q += gridDim.x * blockDim.x) {
+            freelist2[q] = freelist[births + q];
+        }
+    }
     uint32_t nr0 = 0, nr1 = 0;
     if (blockIdx.x < ntiles) {
         nr0 = tile_first[blockIdx.x];
@@ -823,11 +841,14 @@ k_scatter(const StepConst P, RunState *__restrict__ rs,
         uint8_t pc[RA];
         int64_t pid[RA];
         float pb[RA], pa[RA], pl[RA];
+        int32_t pg[RA];
 #pragma unroll
         for (int j = 0; j < RA; j++) {
             const int i = tid + j * kTileThreads;
             pc[j] = 0;
+            pg[j] = 0;
             if (i < na) {
+                if (genetics) pg[j] = gslot[a0 + i];
                 pc[j] = outc[a0 + i];
                 pid[j] = id[a0 + i];
                 pb[j] = birth[a0 + i];
@@ -928,9 +949,19 @@ k_scatter(const StepConst P, RunState *__restrict__ rs,
 #pragma unroll
         for (int j = 0; j < RA; j++) {
             const int i = tid + j * kTileThreads;
-            if (i >= na) break;
+            if (__all_sync(FULL_MASK, i >= na)) break;
+            const bool in_tile = i < na;
             const uint8_t code = pc[j];
             const int k = code & 7;
+            if (genetics) {
+                // the genome slot of an agent dying this step goes to the next free list
+                const uint32_t q = warp_agg_add(in_tile && k == 0, 0u, &rs->dead_count, 1u);
+                if (in_tile && k == 0) {
+                    if (carry + q < P.genome_capacity) freelist2[carry + q] = (uint32_t)pg[j];
+                    else set_error(rs, kErrInternal, 5u);
+                }
+            }
+            if (!in_tile) continue;
             const uint32_t row = a0 + (uint32_t)i;
             const int lc = S.cell[i];
             if (k) {
@@ -945,6 +976,7 @@ k_scatter(const StepConst P, RunState *__restrict__ rs,
                     age2[dst] = P.age_from_birth ? __fsub_rn(fT, fb) : pa[j];
                     meta2[dst] = (uint8_t)(((code & kOutGender) ? kMetaGender : 0) |
                                            ((code & kOutFertile) ? kMetaFertile : 0));
+                    if (genetics) gslot2[dst] = pg[j];
                 }
             }
             if (code & kOutBirth) {
@@ -966,6 +998,21 @@ k_scatter(const StepConst P, RunState *__restrict__ rs,
                     lastb2[dst] = 0.0f;
                     age2[dst] = 0.0f;
                     meta2[dst] = (uint8_t)(g ? kMetaGender : kMetaFertile);
+                    if (genetics) {
+                        const uint32_t gr = S.bid[lc] + rk;   // birth rank of the step
+                        const uint32_t bs = gr < nfree ? freelist[gr] : hwm + (gr - nfree);
+                        if (bs >= P.genome_capacity) {
+                            set_error(rs, kErrCapacity, bs);
+                        } else {
+                            gslot2[dst] = (int32_t)bs;
+                            uint32_t *br = brec + (size_t)gr * 5;
+                            br[0] = (uint32_t)pg[j];
+                            br[1] = (uint32_t)gslot[fr];
+                            br[2] = bs;
+                            br[3] = (uint32_t)(uint64_t)mid;
+                            br[4] = (uint32_t)((uint64_t)mid >> 32);
+                        }
+                    }
                     if (P.log_births) {
                         const uint64_t li = blog_base + (uint64_t)(S.bid[lc] + rk);
                         if (li < blog_cap) {
@@ -986,7 +1033,10 @@ k_scatter(const StepConst P, RunState *__restrict__ rs,
         if (done == gridDim.x - 1) {
             __threadfence();
             rs->scatter_ctas_done = 0u;
-            if (atomicAdd(&rs->error, 0u) != 0u) return;   // a CTA failed: keep the old table
+            if (atomicAdd(&rs->error, 0u) != 0u) {   // a CTA failed: keep the old table
+                rs->dead_count = 0u;
+                return;
+            }
             const uint32_t st = (uint32_t)rs->step;
             rs->stats[st % kStatsRing][0] = rs->new_n_agents;
             unsigned long long *nx = rs->stats[(st + 1u) % kStatsRing];
@@ -997,13 +1047,175 @@ k_scatter(const StepConst P, RunState *__restrict__ rs,
             rs->birth_log_n += rs->births;
             rs->action_tiles = 0u;
             rs->scatter_tiles = 0u;
+            if (P.genome_words > 0) {
+                const uint32_t b = rs->births, nf = rs->nfree;
+                rs->hwm += (b > nf) ? b - nf : 0u;
+                rs->nfree = (nf > b ? nf - b : 0u) + rs->dead_count;
+                rs->dead_count = 0u;
+                rs->genome_step = (int32_t)st;
+            }
             rs->step = (int32_t)(st + 1u);
             __threadfence();
         }
     }
 }
 
+// ----------------------------------------------------------------- genomes
+// Poisson(1) inverse-CDF thresholds floor(P(K <= k) * 2^32), k = 0..15, exact
+__constant__ uint32_t kPoisson1Cdf32[16] = {
+    1580030168u, 3160060337u, 3950075421u, 4213413783u, 4279248373u,
+    4292415291u, 4294609777u, 4294923276u, 4294962463u, 4294966817u,
+    4294967252u, 4294967292u, 4294967295u, 4294967295u, 4294967295u,
+    4294967295u};
+
+__device__ __forceinline__ int poisson1(uint32_t u) {
+    int k = 0;
+    while (k < 16 && u >= kPoisson1Cdf32[k]) k++;
+    return k;
+}
+
+// BitGeneUtils::makeMultiMask (genes/BitGeneUtils.cpp:90-109), including its
+// behaviour for breaks that are not in ascending order
+__device__ uint64_t multi_mask(const uint32_t *br, int nb) {
+    uint32_t k = 1u - (uint32_t)(nb % 2);
+    uint64_t out = 0;
+    int i = nb - 1;
+    for (uint32_t j = 0; j < 64; j++) {
+        if ((i >= 0) && (j == 64u - br[i])) {
+            i--;
+            k = 1u - k;
+        }
+        out = (out << 1) + k;
+    }
+    return out;
+}
+
+// draw k of the newborn's birth stream, lane L holding block L
+__device__ __forceinline__ uint32_t birth_draw(const Draw4 &d, int k) {
+    const int src = k >> 2;
+    const uint32_t w0 = __shfl_sync(FULL_MASK, d.v[0], src);
+    const uint32_t w1 = __shfl_sync(FULL_MASK, d.v[1], src);
+    const uint32_t w2 = __shfl_sync(FULL_MASK, d.v[2], src);
+    const uint32_t w3 = __shfl_sync(FULL_MASK, d.v[3], src);
+    const int q = k & 3;
+    return q == 0 ? w0 : (q == 1 ? w1 : (q == 2 ? w2 : w3));
+}
+
+// one strand word of a crossed parent genome (BitGeneUtils::crossOver,
+// genes/BitGeneUtils.cpp:116-188): strand `sel` of the parent genome after
+// nbk breaks drawn from draws kb.. of the stream, at block b
+__device__ __forceinline__ uint64_t crossed_word(const Draw4 &d, int kb, int nbk, uint32_t nbits, int b,
+                                                 const uint64_t *g, int nblk, int sel) {
+    // every lane walks all breaks (the shuffles need the whole warp) and keeps
+    // those in its own block, in draw order
+    uint32_t br[32];
+    int before = 0, nb = 0;
+    for (int t = 0; t < nbk; t++) {
+        const uint32_t pos = (uint32_t)(((uint64_t)nbits * (uint64_t)birth_draw(d, kb + t)) >> 32);
+        const int blk = (int)(pos >> 6);
+        before += (blk < b) ? 1 : 0;
+        if (blk == b && nb < 32) br[nb++] = pos & 63u;
+    }
+    const uint64_t m = nb > 0 ? multi_mask(br, nb) : ~0ull;
+    const int cur = (before & 1) ^ sel;
+    const uint64_t A = g[cur * nblk + b];
+    const uint64_t B = g[(1 - cur) * nblk + b];
+    return (m & A) | (~m & B);
+}
+
+// Genetics::makeOffspring (actions/Genetics.cpp:285-337), one warp per
+// newborn.  Birth stream of the mother: draw 0 gender (k_scatter), 1 and 2
+// the strands taken from mother and father, then (Poisson mode) the two
+// crossover counts, the mother's and the father's breakpoints, the mutation
+// count and the mutation positions.
+__global__ void __launch_bounds__(256)
+k_genomes(const StepConst P, RunState *__restrict__ rs, uint64_t *__restrict__ genome,
+          const uint32_t *__restrict__ brec) {
+    if (rs->error != 0u) return;
+    const uint32_t nbirths = rs->births;
+    const uint32_t step = (uint32_t)rs->genome_step;
+    const int lane = threadIdx.x & 31;
+    const int gw = P.genome_words;
+    const int nblk = gw >> 1;
+    const uint32_t nbits = (uint32_t)nblk * 64u;
+    for (uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < nbirths;
+         g += (gridDim.x * blockDim.x) >> 5) {
+        const uint32_t ms = __ldg(&brec[(size_t)g * 5 + 0]);
+        const uint32_t fs = __ldg(&brec[(size_t)g * 5 + 1]);
+        const uint32_t bs = __ldg(&brec[(size_t)g * 5 + 2]);
+        const uint64_t mid = (uint64_t)__ldg(&brec[(size_t)g * 5 + 3]) |
+                             ((uint64_t)__ldg(&brec[(size_t)g * 5 + 4]) << 32);
+        const Draw4 d = draw_block(P.seed, step, (int64_t)mid, kStreamBirth + (uint32_t)lane);
+        const int i1 = (int)(birth_draw(d, 1) >> 31);
+        const int i2 = (int)(birth_draw(d, 2) >> 31);
+        int k = 3, nM = 0, nF = 0;
+        if (P.num_crossover == kCrossoverPoisson1) {
+            nM = poisson1(birth_draw(d, 3));
+            nF = poisson1(birth_draw(d, 4));
+            k = 5;
+        } else if (P.num_crossover > 0) {
+            nM = nF = P.num_crossover;
+        }
+        const int kMom = k, kDad = k + nM;
+        k += nM + nF;
+        int nmut = 0;
+        if (P.has_mutation) {
+            const uint32_t u = birth_draw(d, k);
+            while (nmut < P.n_binomial && (int64_t)u > P.bino[nmut]) nmut++;
+            k++;
+        }
+        if (k + nmut > kBirthDraws) {
+            if (lane == 0) set_error(rs, kErrInternal, 6u);
+            continue;
+        }
+        const uint64_t *gm = genome + (size_t)ms * gw;
+        const uint64_t *gf = genome + (size_t)fs * gw;
+        uint64_t *gb = genome + (size_t)bs * gw;
+        for (int b0 = 0; b0 < nblk; b0 += 32) {
+            const int b = b0 + lane;
+            const int bb = b < nblk ? b : 0;
+            uint64_t w0 = crossed_word(d, kMom, nM, nbits, bb, gm, nblk, i1);
+            uint64_t w1 = crossed_word(d, kDad, nF, nbits, bb, gf, nblk, i2);
+            // BitGeneUtils::mutateNucs (genes/BitGeneUtils.cpp:57-75): flips at
+            // wrandi(0, 2 * genome size) over both strands of the newborn
+            for (int t = 0; t < nmut; t++) {
+                const uint32_t pos = (uint32_t)(((uint64_t)(2u * (uint32_t)P.genome_size) *
+                                                 (uint64_t)birth_draw(d, k + t)) >> 32);
+                const int w = (int)(pos >> 6);
+                const uint64_t bit = 1ull << (pos & 63u);
+                if (w == b) w0 ^= bit;
+                if (w == nblk + b) w1 ^= bit;
+            }
+            if (b < nblk) {
+                gb[b] = w0;
+                gb[nblk + b] = w1;
+            }
+        }
+    }
+}
+
+// genomes of the table's rows in row order (download)
+__global__ void k_gather_genomes(const int32_t *__restrict__ gslot, const uint64_t *__restrict__ genome,
+                                 uint32_t n, int words, uint32_t slots, uint64_t *__restrict__ out) {
+    const uint64_t total = (uint64_t)n * (uint64_t)words;
+    for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+         q += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t row = (uint32_t)(q / (uint64_t)words);
+        const int w = (int)(q % (uint64_t)words);
+        const int32_t sl = gslot[row];
+        out[q] = (sl >= 0 && (uint32_t)sl < slots) ? genome[(size_t)sl * words + w] : 0ull;
+    }
+}
+
 }  // namespace qhg
+
+extern "C" int qhg_launch_gather_genomes(const int32_t *gslot, const uint64_t *genome, uint32_t n, int words,
+                                         uint32_t slots, uint64_t *out, cudaStream_t stream) {
+    const uint64_t total = (uint64_t)n * (uint64_t)words;
+    const uint64_t blocks = std::min<uint64_t>((total + 255) / 256, 65535);
+    if (blocks > 0) qhg::k_gather_genomes<<<(unsigned)blocks, 256, 0, stream>>>(gslot, genome, n, words, slots, out);
+    return (int)cudaGetLastError();
+}
 
 static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B, int grid,
                            cudaStream_t stream, cudaEvent_t *ev) {
@@ -1029,8 +1241,13 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
     k_scatter<<<grid, kTileThreads, 0, stream>>>(
         *P, rs, B->nonempty, B->ne_start, B->tile_first, B->id, B->birth, B->age, B->lastb, B->outc, B->father,
         B->brank, B->nnbr, B->sbase, B->bbase, B->bidbase, B->obase, B->clsc, B->id2, B->birth2,
-        B->age2, B->lastb2, B->meta2, B->blog, B->blog_cap);
+        B->age2, B->lastb2, B->meta2, B->blog, B->blog_cap, B->gslot, B->gslot2, B->freelist,
+        B->freelist2, B->brec);
     if (ev) cudaEventRecord(ev[3], stream);
+    if (P->genome_words > 0) {
+        k_genomes<<<grid, 256, 0, stream>>>(*P, rs, B->genome, B->brec);
+        if (ev) cudaEventRecord(ev[4], stream);
+    }
 }
 
 extern "C" int qhg_launch_step(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,

@@ -11,7 +11,8 @@ import pytest
 from oracle import port
 from qhg4_gb300.gpu import GpuRun
 from qhg4_gb300.spec import (ACT_FERTILITY, ACT_GETOLD, ACT_OLDAGEDEATH, ACT_RANDOMMOVE, ACT_RANDOMPAIR,
-                             ACT_VERHULST, ACT_VERHULSTVARK, ACT_WEIGHTEDMOVE, Action)
+                             ACT_VERHULST, ACT_VERHULSTVARK, ACT_WEIGHTEDMOVE, CROSSOVER_POISSON1, Action,
+                             Genetics, config3_actions)
 from qhg4_gb300.workload import make_agents, terrain_grid, uniform_grid
 
 from helpers import case_config1, case_config2, table_diff
@@ -19,10 +20,10 @@ from helpers import case_config1, case_config2, table_diff
 pytestmark = pytest.mark.gpu
 
 
-def run_both(grid, agents, actions, steps, seed, chunks=(None,)):
-    o = port.OracleRun(grid, actions, seed)
+def run_both(grid, agents, actions, steps, seed, chunks=(None,), genetics=Genetics()):
+    o = port.OracleRun(grid, actions, seed, genetics)
     o.load(agents)
-    g = GpuRun(grid, actions, seed, log_births=True)
+    g = GpuRun(grid, actions, seed, genetics, log_births=True)
     g.load(agents)
     done = 0
     ost = []
@@ -82,3 +83,17 @@ def test_no_pairing_no_moves(gpu_lib):
     o, g, st = run_both(grid, agents, acts, 15, 5)
     assert_same(o, g, st, 15)
     assert st[:, 1].sum() == 0
+
+
+@pytest.mark.parametrize("genetics", [Genetics(4096, CROSSOVER_POISSON1, 1e-4), Genetics(1000, 3, 1e-3),
+                                      Genetics(100, 0, 0.0), Genetics(64, 1, 0.0)],
+                         ids=["poisson_4096", "fixed3_1000", "nocross_100", "fixed1_64"])
+def test_genetics(gpu_lib, genetics):
+    """Genetics::makeOffspring: crossover (Poisson(1) or fixed counts, none),
+    mutation counts from the binomial table, genomes whose size is not a
+    multiple of 64 loci; genome slots of the dead reused by later births."""
+    grid = uniform_grid(5, 40.0)
+    agents = make_agents(grid, 3000, seed=31, age_max=50.0, genome_blocks=genetics.num_blocks)
+    o, g, st = run_both(grid, agents, config3_actions(), 20, 77, chunks=(3, 17), genetics=genetics)
+    assert_same(o, g, st, 20)
+    assert st[:, 1].sum() > 0 and st[:, 2].sum() > 0
