@@ -17,13 +17,13 @@
 #include "../../include/qhg_gpu.h"
 
 extern "C" int qhg_launch_step(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
-                               int cell_grid, cudaStream_t stream);
-extern "C" int qhg_tile_ctas_per_sm(void);
+                               const qhg::LaunchShape *L, cudaStream_t stream);
+extern "C" void qhg_tile_ctas_per_sm(int *actions, int *scatter);
 extern "C" int qhg_match_program(const int32_t *types, int n);
 extern "C" int qhg_launch_gather_genomes(const int32_t *gslot, const uint64_t *genome, uint32_t n, int words,
                                          uint32_t slots, uint64_t *out, cudaStream_t stream);
 extern "C" int qhg_launch_step_timed(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
-                                     int cell_grid, cudaStream_t stream, cudaEvent_t *ev);
+                                     const qhg::LaunchShape *L, cudaStream_t stream, cudaEvent_t *ev);
 
 using namespace qhg;
 
@@ -90,7 +90,7 @@ struct qhg_run {
     int cur = 0;                 // table holding the current step
     int32_t upload_step = 0;
     bool grid_ok = false, agents_ok = false;
-    int cell_grid = 0;
+    LaunchShape shape = {1, 1};
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     std::vector<int64_t> stage;  // host staging for uploads
@@ -362,8 +362,11 @@ extern "C" int qhg_gpu_create(const qhg_run_desc *desc, qhg_run **out) {
     memset(r->h_rs, 0, sizeof(RunState));
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, desc->device);
-    // persistent grid of the tile kernels: as many CTAs as fit at once
-    r->cell_grid = std::max(1, nsm) * std::max(1, qhg_tile_ctas_per_sm());
+    // persistent grids of the tile kernels: as many CTAs as fit at once
+    int ca = 1, cs = 1;
+    qhg_tile_ctas_per_sm(&ca, &cs);
+    r->shape.actions_grid = std::max(1, nsm) * ca;
+    r->shape.scatter_grid = std::max(1, nsm) * cs;
     *out = r;
     return QHG_OK;
 }
@@ -667,7 +670,7 @@ static int build_graph(qhg_run *r, int cur) {
     StepBuffers B = make_buffers(r, cur);
     cudaGraph_t g = nullptr;
     CUDA_TRY(cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal));
-    int le = qhg_launch_step(&r->P, r->d_rs, &B, r->cell_grid, r->stream);
+    int le = qhg_launch_step(&r->P, r->d_rs, &B, &r->shape, r->stream);
     cudaError_t ee = cudaStreamEndCapture(r->stream, &g);
     if (le != 0 || ee != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
@@ -719,7 +722,7 @@ extern "C" int qhg_gpu_step_profiled(qhg_run *r, int32_t nsteps, float *kernel_m
     }
     for (int32_t s = 0; s < nsteps; s++) {
         StepBuffers B = make_buffers(r, r->cur);
-        int le = qhg_launch_step_timed(&r->P, r->d_rs, &B, r->cell_grid, r->stream, r->ev);
+        int le = qhg_launch_step_timed(&r->P, r->d_rs, &B, &r->shape, r->stream, r->ev);
         if (le != 0) return fail(QHG_ERR_CUDA, std::string("launch: ") + cudaGetErrorString((cudaError_t)le));
         const bool gen = r->P.genome_words > 0;
         CUDA_TRY(cudaEventSynchronize(r->ev[gen ? 4 : 3]));

@@ -158,6 +158,13 @@ struct StepBuffers {
     uint32_t *brec;
 };
 
+// grid sizes of the persistent tile kernels (CTAs); results do not depend
+// on them (tiles are dealt out statically, draws are keyed by agent ID)
+struct LaunchShape {
+    int actions_grid;
+    int scatter_grid;
+};
+
 // ------------------------------------------------------------- Philox
 struct Draw4 { uint32_t v[4]; };
 

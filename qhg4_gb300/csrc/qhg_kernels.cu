@@ -151,7 +151,7 @@ __host__ __device__ constexpr int prog_act(int p, int a) {
 constexpr int kNumPrograms = 4;
 
 struct ActionsSmem {
-    int64_t id[kTileMax];
+    int64_t fid[kTileMax];         // IDs of the unsorted FERTILE lists (same positions as pick)
     uint8_t meta[kTileMax];
     uint8_t head[kTileMax];        // first row of a cell
     uint8_t bfl[kTileMax];         // gives birth this step
@@ -160,6 +160,9 @@ struct ActionsSmem {
     uint16_t frank[kTileMax];      // rank of a FERTILE agent among its cell's FERTILE agents of its sex (by ID)
     uint16_t list[kTileMax];       // at each cell's rows: FERTILE females by ID, then FERTILE males by ID
     uint16_t pick[kTileMax];       // at each cell's rows: unsorted FERTILE lists, later the pick values
+    uint16_t pkrow[kTileMax];      // rows of the tile's pairing members that draw (dense)
+    uint16_t oadq[kTileMax];       // rows whose OldAgeDeath needs its draw (dense)
+    uint8_t oc[kTileMax];          // outcome byte before the deferred OldAgeDeath draws
     uint32_t cstart[kTileCells + 1];  // first row of each cell, relative to the tile
     int32_t cid[kTileCells];
     uint32_t nf[kTileCells];
@@ -169,8 +172,13 @@ struct ActionsSmem {
     uint8_t tk[kTileCells];
     uint32_t cls[kTileCells][4];
     uint32_t red[kTileThreads / 32];
-    uint32_t t, r0, r1;
+    uint32_t npick, noad;
 };
+
+// OldAgeDeath is the last action of program 2: its draw (needed only by
+// agents whose age lies inside the death window) is made in a dense pass
+// after the other actions, so that warps do not run Philox for a few lanes
+__host__ __device__ constexpr bool prog_defers_oad(int p) { return p == 2; }
 
 template <int PROG>
 __global__ void __launch_bounds__(kTileThreads, 4)
@@ -261,7 +269,6 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
             const int i = tid + j * kTileThreads;
             if (i < na) {
                 S.meta[i] = pm[j];
-                S.id[i] = pid[j];
                 S.mate[i] = -1;
                 S.bfl[i] = 0;
                 S.head[i] = 0;
@@ -269,6 +276,7 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
         }
         __syncthreads();
         for (int lc = tid; lc < nc; lc += kTileThreads) S.head[S.cstart[lc]] = 1;
+        if (tid == 0) { S.npick = 0u; S.noad = 0u; }
         __syncthreads();
         // local cell of each row: count of cell heads up to the row (block scan
         // over contiguous rows per thread)
@@ -302,107 +310,111 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
         // ID order, each pick drawn from the pairing stream of the picking member
         if (P.has_pair) {
             // unsorted FERTILE lists: females from the cell's first row up, males
-            // from its last row down
+            // from its last row down (with their IDs beside them)
 #pragma unroll
             for (int j = 0; j < RA; j++) {
                 const int i = tid + j * kTileThreads;
                 if (__all_sync(FULL_MASK, i >= na)) break;
-                const uint8_t m = (i < na) ? S.meta[i] : (uint8_t)0;
+                const uint8_t m = (i < na) ? pm[j] : (uint8_t)0;
                 const bool fert = (m & kMetaFertile) != 0;
                 const bool male = (m & kMetaGender) != 0;
                 const int lc = fert ? S.cell[i] : 0;
                 uint32_t *ctr = male ? &S.nm[lc] : &S.nf[lc];
                 const uint32_t q = warp_agg_add(fert, ((uint32_t)lc << 1) | (male ? 1u : 0u), ctr, 1u);
                 if (fert) {
-                    if (male) S.pick[S.cstart[lc + 1] - 1u - q] = (uint16_t)i;
-                    else S.pick[S.cstart[lc] + q] = (uint16_t)i;
+                    const uint32_t pos = male ? (S.cstart[lc + 1] - 1u - q) : (S.cstart[lc] + q);
+                    S.pick[pos] = (uint16_t)i;
+                    S.fid[pos] = pid[j];
                 }
             }
             __syncthreads();
             // rank by ID within the own sex's list (IDs are unique)
-            for (int i = tid; i < na; i += kTileThreads) {
-                const uint8_t m = S.meta[i];
-                if (m & kMetaFertile) {
+#pragma unroll
+            for (int j = 0; j < RA; j++) {
+                const int i = tid + j * kTileThreads;
+                if (i < na && (pm[j] & kMetaFertile)) {
                     const int lc = S.cell[i];
-                    const int64_t x = S.id[i];
-                    int r = 0;
-                    if (m & kMetaGender) {
-                        const int e = (int)S.cstart[lc + 1];
-                        const int b = e - (int)S.nm[lc];
-                        for (int q = b; q < e; q++) r += (S.id[S.pick[q]] < x) ? 1 : 0;
+                    const int64_t x = pid[j];
+                    int b, e;
+                    if (pm[j] & kMetaGender) {
+                        e = (int)S.cstart[lc + 1];
+                        b = e - (int)S.nm[lc];
                     } else {
-                        const int b = (int)S.cstart[lc];
-                        const int e = b + (int)S.nf[lc];
-                        for (int q = b; q < e; q++) r += (S.id[S.pick[q]] < x) ? 1 : 0;
+                        b = (int)S.cstart[lc];
+                        e = b + (int)S.nf[lc];
                     }
+                    int r = 0;
+                    for (int q = b; q < e; q++) r += (S.fid[q] < x) ? 1 : 0;
                     S.frank[i] = (uint16_t)r;
                 }
             }
             __syncthreads();
-            for (int i = tid; i < na; i += kTileThreads) {
-                const uint8_t m = S.meta[i];
-                if (m & kMetaFertile) {
+#pragma unroll
+            for (int j = 0; j < RA; j++) {
+                const int i = tid + j * kTileThreads;
+                if (i < na && (pm[j] & kMetaFertile)) {
                     const int lc = S.cell[i];
-                    const uint32_t off = (m & kMetaGender) ? S.nf[lc] : 0u;
+                    const uint32_t off = (pm[j] & kMetaGender) ? S.nf[lc] : 0u;
                     S.list[S.cstart[lc] + off + S.frank[i]] = (uint16_t)i;
+                }
+            }
+            __syncthreads();
+            // the members of the smaller side pick, in ID order; gather them densely
+            for (int lc = tid; lc < nc; lc += kTileThreads) {
+                const uint32_t nF = S.nf[lc], nM = S.nm[lc];
+                if (nF > 0u && nM > 0u) {
+                    const bool femSmall = nF <= nM;
+                    const uint32_t m = femSmall ? nF : nM;
+                    const uint32_t at = atomicAdd(&S.npick, m);
+                    const uint32_t from = S.cstart[lc] + (femSmall ? 0u : nF);
+                    for (uint32_t q = 0; q < m; q++) S.pkrow[at + q] = S.list[from + q];
                 }
             }
             __syncthreads();
             // pick j takes the pick[j]-th still unpaired member of the larger
             // side, pick[j] = (int)wrandr(0, nL - j)
-            for (int i = tid; i < na; i += kTileThreads) {
-                const uint8_t m = S.meta[i];
-                if (m & kMetaFertile) {
-                    const int lc = S.cell[i];
-                    const uint32_t nF = S.nf[lc], nM = S.nm[lc];
-                    const bool femSmall = nF <= nM;
-                    if (nF > 0u && nM > 0u && (((m & kMetaGender) == 0) == femSmall)) {
-                        const uint32_t j = S.frank[i];
-                        const uint32_t nL = femSmall ? nM : nF;
-                        const uint32_t u = draw_block(P.seed, (uint32_t)step, S.id[i], kStreamPair).v[0];
-                        S.pick[S.cstart[lc] + j] = (uint16_t)(((uint64_t)(nL - j) * (uint64_t)u) >> 32);
-                    }
-                }
+            const uint32_t npk = S.npick;
+            for (uint32_t q = tid; q < npk; q += kTileThreads) {
+                const int i = S.pkrow[q];
+                const int lc = S.cell[i];
+                const uint32_t nF = S.nf[lc], nM = S.nm[lc];
+                const uint32_t nL = (nF <= nM) ? nM : nF;
+                const uint32_t j = S.frank[i];
+                const uint32_t u = draw_block(P.seed, (uint32_t)step, id[a0 + i], kStreamPair).v[0];
+                S.pick[S.cstart[lc] + j] = (uint16_t)(((uint64_t)(nL - j) * (uint64_t)u) >> 32);
             }
             __syncthreads();
             // the member taken by pick j, decoded on its own: start from pick[j]
             // and for i = j-1 down to 0 step over the member pick i took when it
             // lies at or below
-            for (int i = tid; i < na; i += kTileThreads) {
-                const uint8_t m = S.meta[i];
-                if (m & kMetaFertile) {
-                    const int lc = S.cell[i];
-                    const uint32_t nF = S.nf[lc], nM = S.nm[lc];
-                    const bool femSmall = nF <= nM;
-                    if (nF > 0u && nM > 0u && (((m & kMetaGender) == 0) == femSmall)) {
-                        const int cs = (int)S.cstart[lc];
-                        const int j = S.frank[i];
-                        uint32_t p = S.pick[cs + j];
-                        for (int q = j - 1; q >= 0; q--) p += (p >= S.pick[cs + q]) ? 1u : 0u;
-                        const uint32_t nL = femSmall ? nM : nF;
-                        if (p >= nL) {   // cannot happen: every pick finds a free member
-                            set_error(rs, kErrInternal, 1u);
-                        } else {
-                            const int partner = S.list[cs + (femSmall ? (int)nF : 0) + (int)p];
-                            S.mate[i] = (int16_t)partner;
-                            S.mate[partner] = (int16_t)i;
-                        }
-                    }
+            for (uint32_t q = tid; q < npk; q += kTileThreads) {
+                const int i = S.pkrow[q];
+                const int lc = S.cell[i];
+                const uint32_t nF = S.nf[lc], nM = S.nm[lc];
+                const bool femSmall = nF <= nM;
+                const int cs = (int)S.cstart[lc];
+                const int j = S.frank[i];
+                uint32_t p = S.pick[cs + j];
+                for (int k = j - 1; k >= 0; k--) p += (p >= S.pick[cs + k]) ? 1u : 0u;
+                const uint32_t nL = femSmall ? nM : nF;
+                if (p >= nL) {   // cannot happen: every pick finds a free member
+                    set_error(rs, kErrInternal, 1u);
+                } else {
+                    const int partner = S.list[cs + (femSmall ? (int)nF : 0) + (int)p];
+                    S.mate[i] = (int16_t)partner;
+                    S.mate[partner] = (int16_t)i;
                 }
             }
             __syncthreads();
         }
         // ---- every action on every agent (SPopulation::doActions)
+        constexpr bool kDeferOad = prog_defers_oad(PROG);
 #pragma unroll
         for (int j = 0; j < RA; j++) {
             const int i = tid + j * kTileThreads;
-            if (__all_sync(FULL_MASK, i >= na)) break;
-            const bool in_tile = i < na;
-            int cls = 0, lc = 0;
-            bool bflag = false;
-            if (in_tile) {
+            if (i >= na) break;
             const uint32_t row = a0 + (uint32_t)i;
-            lc = S.cell[i];
+            const int lc = S.cell[i];
             const int c = S.cid[lc];
             const uint8_t m8 = pm[j];
             const float fb = pb[j];
@@ -411,6 +423,7 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
             const bool female = !(m8 & kMetaGender);
             bool fert = (m8 & kMetaFertile) != 0;
             bool alive = true;
+            bool bflag = false;
             int dir = 0;
             AgentDraws dr;
             dr.init(P.seed, (uint32_t)step, pid[j]);
@@ -446,11 +459,13 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
                 }
                 case kOldAgeDeath: {
                     fa = __fsub_rn(fT, fb);
-                    bool die;
+                    bool die = false;
                     if (fa <= A.age_lo) {
                         die = false;
                     } else if (fa > A.age_hi) {
                         die = true;
+                    } else if (kDeferOad) {
+                        S.oadq[atomicAdd(&S.noad, 1u)] = (uint16_t)i;
                     } else {
                         const uint32_t u = dr.get(A.window);
                         const double t = __dmul_rn(__dmul_rn(A.oad_w, (double)u), 2.3283064365386962890625e-10);
@@ -481,7 +496,7 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
                             d = (int)(((uint64_t)(nn + 1) * (uint64_t)u2) >> 32);
                         } else {
                             d = 0;
-                            for (int j = 0; j < nn; j++) d += (wthr[c * 6 + j] <= (uint64_t)u2) ? 1 : 0;
+                            for (int q = 0; q < nn; q++) d += (wthr[c * 6 + q] <= (uint64_t)u2) ? 1 : 0;
                         }
                         if (d > 0) {
                             const int to = nbr[c * 6 + d - 1];
@@ -494,17 +509,49 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
                     break;
                 }
             }
-            cls = alive ? (1 + dir) : 0;
-            outc[row] = (uint8_t)(cls | (bflag ? kOutBirth : 0) | (fert ? kOutFertile : 0) |
-                                  ((m8 & kMetaGender) ? kOutGender : 0));
+            const int cls = alive ? (1 + dir) : 0;
+            S.oc[i] = (uint8_t)(cls | (bflag ? kOutBirth : 0) | (fert ? kOutFertile : 0) |
+                                ((m8 & kMetaGender) ? kOutGender : 0));
+            S.bfl[i] = bflag ? 1 : 0;
             if (bflag) {
                 father[row] = (int32_t)(a0 + (uint32_t)S.mate[i]);
-                S.bfl[i] = 1;
                 cnt_births++;
             }
+        }
+        if (kDeferOad) {
+            // OldAgeDeath::execute (actions/OldAgeDeath.cpp:57-60) for the agents
+            // inside the death window: age > M + wrandr(1 - U*M, 1 + U*M)
+            __syncthreads();
+            const uint32_t nq = S.noad;
+            constexpr int kOad = prog_len(PROG) - 1;
+            const ActionConst &A = P.act[kOad];
+            for (uint32_t q = tid; q < nq; q += kTileThreads) {
+                const int i = S.oadq[q];
+                const float fa = __fsub_rn(fT, birth[a0 + i]);
+                const uint32_t w = A.window;
+                const uint32_t u = pick4(draw_block(P.seed, (uint32_t)step, id[a0 + i], kStreamActions + (w >> 2)), w & 3u);
+                const double t = __dmul_rn(__dmul_rn(A.oad_w, (double)u), 2.3283064365386962890625e-10);
+                const double thr = __dadd_rn(A.oad_M, __dadd_rn(A.oad_a, t));
+                if ((double)fa > thr) {
+                    S.oc[i] = (uint8_t)(S.oc[i] & ~7u);
+                    cnt_deaths++;
+                }
             }
-            // per-cell class counts (slot 0 stay, 1..6 movers, 7 births), two
-            // 16-bit counters per shared word, one atomic per (cell, slot) and warp
+        }
+        __syncthreads();
+        // outcome bytes and per-cell class counts (slot 0 stay, 1..6 movers,
+        // 7 births), two 16-bit counters per shared word, one atomic per
+        // (cell, slot) and warp
+#pragma unroll
+        for (int j = 0; j < RA; j++) {
+            const int i = tid + j * kTileThreads;
+            if (__all_sync(FULL_MASK, i >= na)) break;
+            const bool in_tile = i < na;
+            const uint8_t oc = in_tile ? S.oc[i] : (uint8_t)0;
+            const int cls = oc & 7;
+            const bool bflag = (oc & kOutBirth) != 0;
+            const int lc = in_tile ? S.cell[i] : 0;
+            if (in_tile) outc[a0 + (uint32_t)i] = oc;
             const int slot = (cls > 0) ? cls - 1 : 0;
             warp_agg_add(in_tile && cls > 0, ((uint32_t)lc << 3) | (uint32_t)slot, &S.cls[lc][slot >> 1],
                          1u << (16 * (slot & 1)));
@@ -776,10 +823,11 @@ struct ScatterSmem {
     uint64_t chi[kTileCells];
     uint64_t wlo[kTileThreads / 32];
     uint64_t whi[kTileThreads / 32];
-    uint32_t t, r0, r1;
+    uint16_t brow[kTileMax];       // rows of the tile's mothers (dense)
+    uint32_t nb;
 };
 
-__global__ void __launch_bounds__(kTileThreads)
+__global__ void __launch_bounds__(kTileThreads, 4)
 k_scatter(const StepConst P, RunState *__restrict__ rs,
           const uint32_t *__restrict__ nonempty, const uint32_t *__restrict__ ne_start,
           const uint32_t *__restrict__ tile_first,
@@ -857,6 +905,7 @@ k_scatter(const StepConst P, RunState *__restrict__ rs,
             }
         }
         __syncthreads();   // the previous tile is done with the shared arrays
+        if (tid == 0) S.nb = 0u;
 #pragma unroll
         for (int j = 0; j < RA; j++) {
             const int i = tid + j * kTileThreads;
@@ -962,7 +1011,6 @@ k_scatter(const StepConst P, RunState *__restrict__ rs,
                 }
             }
             if (!in_tile) continue;
-            const uint32_t row = a0 + (uint32_t)i;
             const int lc = S.cell[i];
             if (k) {
                 const uint32_t dst = ((k == 1) ? S.sb[lc] : S.ob[lc][k - 2]) + S.rank[i];
@@ -979,48 +1027,55 @@ k_scatter(const StepConst P, RunState *__restrict__ rs,
                     if (genetics) gslot2[dst] = pg[j];
                 }
             }
-            if (code & kOutBirth) {
-                // SPopulation::createAgentAtIndex (core/SPopulation.cpp:880-900):
-                // gender = (uchar)(2 * wrandd()), females start FERTILE
-                const uint32_t rk = brank[row];
-                const uint32_t dst = S.bb[lc] + rk;
-                const int32_t fr = father[row];
-                const bool ok = dst < cap && fr >= 0 && (uint32_t)fr < N;
-                if (!ok) {
-                    set_error(rs, kErrInternal, 4u);
+            if (code & kOutBirth) S.brow[atomicAdd(&S.nb, 1u)] = (uint16_t)i;
+        }
+        __syncthreads();
+        // newborns, one thread per mother (SPopulation::createAgentAtIndex,
+        // core/SPopulation.cpp:880-900): gender = (uchar)(2 * wrandd()) from the
+        // mother's birth stream, females start FERTILE
+        const uint32_t nbt = S.nb;
+        for (uint32_t q = tid; q < nbt; q += kTileThreads) {
+            const int i = S.brow[q];
+            const uint32_t row = a0 + (uint32_t)i;
+            const int lc = S.cell[i];
+            const uint32_t rk = brank[row];
+            const uint32_t dst = S.bb[lc] + rk;
+            const int32_t fr = father[row];
+            const bool ok = dst < cap && fr >= 0 && (uint32_t)fr < N;
+            if (!ok) {
+                set_error(rs, kErrInternal, 4u);
+                continue;
+            }
+            const int64_t mid = id[row];
+            const uint32_t u = draw_block(P.seed, (uint32_t)step, mid, kStreamBirth).v[0];
+            const uint8_t g = (uint8_t)(u >> 31);
+            const int64_t baby = next_id + (int64_t)(S.bid[lc] + rk);
+            id2[dst] = baby;
+            birth2[dst] = fT;
+            lastb2[dst] = 0.0f;
+            age2[dst] = 0.0f;
+            meta2[dst] = (uint8_t)(g ? kMetaGender : kMetaFertile);
+            if (genetics) {
+                const uint32_t gr = S.bid[lc] + rk;   // birth rank of the step
+                const uint32_t bs = gr < nfree ? freelist[gr] : hwm + (gr - nfree);
+                if (bs >= P.genome_capacity) {
+                    set_error(rs, kErrCapacity, bs);
                 } else {
-                    const int64_t mid = pid[j];
-                    const uint32_t u = draw_block(P.seed, (uint32_t)step, mid, kStreamBirth).v[0];
-                    const uint8_t g = (uint8_t)(u >> 31);
-                    const int64_t baby = next_id + (int64_t)(S.bid[lc] + rk);
-                    id2[dst] = baby;
-                    birth2[dst] = fT;
-                    lastb2[dst] = 0.0f;
-                    age2[dst] = 0.0f;
-                    meta2[dst] = (uint8_t)(g ? kMetaGender : kMetaFertile);
-                    if (genetics) {
-                        const uint32_t gr = S.bid[lc] + rk;   // birth rank of the step
-                        const uint32_t bs = gr < nfree ? freelist[gr] : hwm + (gr - nfree);
-                        if (bs >= P.genome_capacity) {
-                            set_error(rs, kErrCapacity, bs);
-                        } else {
-                            gslot2[dst] = (int32_t)bs;
-                            uint32_t *br = brec + (size_t)gr * 5;
-                            br[0] = (uint32_t)pg[j];
-                            br[1] = (uint32_t)gslot[fr];
-                            br[2] = bs;
-                            br[3] = (uint32_t)(uint64_t)mid;
-                            br[4] = (uint32_t)((uint64_t)mid >> 32);
-                        }
-                    }
-                    if (P.log_births) {
-                        const uint64_t li = blog_base + (uint64_t)(S.bid[lc] + rk);
-                        if (li < blog_cap) {
-                            blog[li * 3 + 0] = baby;
-                            blog[li * 3 + 1] = mid;
-                            blog[li * 3 + 2] = id[fr];
-                        }
-                    }
+                    gslot2[dst] = (int32_t)bs;
+                    uint32_t *br = brec + (size_t)gr * 5;
+                    br[0] = (uint32_t)gslot[row];
+                    br[1] = (uint32_t)gslot[fr];
+                    br[2] = bs;
+                    br[3] = (uint32_t)(uint64_t)mid;
+                    br[4] = (uint32_t)((uint64_t)mid >> 32);
+                }
+            }
+            if (P.log_births) {
+                const uint64_t li = blog_base + (uint64_t)(S.bid[lc] + rk);
+                if (li < blog_cap) {
+                    blog[li * 3 + 0] = baby;
+                    blog[li * 3 + 1] = mid;
+                    blog[li * 3 + 2] = id[fr];
                 }
             }
         }
@@ -1217,13 +1272,13 @@ extern "C" int qhg_launch_gather_genomes(const int32_t *gslot, const uint64_t *g
     return (int)cudaGetLastError();
 }
 
-static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B, int grid,
-                           cudaStream_t stream, cudaEvent_t *ev) {
+static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
+                           const qhg::LaunchShape &L, cudaStream_t stream, cudaEvent_t *ev) {
     using namespace qhg;
     const int ntiles = (P->num_cells + kScanTile - 1) / kScanTile;
     if (ev) cudaEventRecord(ev[0], stream);
 #define QHG_LAUNCH_ACTIONS(PR)                                                                       \
-    k_actions<PR><<<grid, kTileThreads, 0, stream>>>(                                                 \
+    k_actions<PR><<<L.actions_grid, kTileThreads, 0, stream>>>(                                                 \
         *P, rs, B->nonempty, B->ne_start, B->tile_first, B->id, B->birth, B->age, B->lastb, B->meta,  \
         B->nbr, B->nnbr, B->vthr, B->wthr, B->wflag, B->outc, B->father, B->brank, B->clsc)
     switch (P->program) {
@@ -1238,37 +1293,37 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
         *P, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr, B->sbase, B->bbase, B->bidbase, B->obase,
         B->nonempty2, B->ne_start2, B->tile_first2, B->tile_flag, B->tile_agg, B->tile_incl);
     if (ev) cudaEventRecord(ev[2], stream);
-    k_scatter<<<grid, kTileThreads, 0, stream>>>(
+    k_scatter<<<L.scatter_grid, kTileThreads, 0, stream>>>(
         *P, rs, B->nonempty, B->ne_start, B->tile_first, B->id, B->birth, B->age, B->lastb, B->outc, B->father,
         B->brank, B->nnbr, B->sbase, B->bbase, B->bidbase, B->obase, B->clsc, B->id2, B->birth2,
         B->age2, B->lastb2, B->meta2, B->blog, B->blog_cap, B->gslot, B->gslot2, B->freelist,
         B->freelist2, B->brec);
     if (ev) cudaEventRecord(ev[3], stream);
     if (P->genome_words > 0) {
-        k_genomes<<<grid, 256, 0, stream>>>(*P, rs, B->genome, B->brec);
+        k_genomes<<<L.scatter_grid, 256, 0, stream>>>(*P, rs, B->genome, B->brec);
         if (ev) cudaEventRecord(ev[4], stream);
     }
 }
 
 extern "C" int qhg_launch_step(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
-                               int cell_grid, cudaStream_t stream) {
-    launch_kernels(P, rs, B, cell_grid, stream, nullptr);
+                               const qhg::LaunchShape *L, cudaStream_t stream) {
+    launch_kernels(P, rs, B, *L, stream, nullptr);
     return (int)cudaGetLastError();
 }
 
 extern "C" int qhg_launch_step_timed(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
-                                     int cell_grid, cudaStream_t stream, cudaEvent_t *ev) {
-    launch_kernels(P, rs, B, cell_grid, stream, ev);
+                                     const qhg::LaunchShape *L, cudaStream_t stream, cudaEvent_t *ev) {
+    launch_kernels(P, rs, B, *L, stream, ev);
     return (int)cudaGetLastError();
 }
 
-// CTAs of the tile kernels that fit on one SM at once (the smaller of the two)
-extern "C" int qhg_tile_ctas_per_sm(void) {
+// CTAs of each tile kernel that fit on one SM at once
+extern "C" void qhg_tile_ctas_per_sm(int *actions, int *scatter) {
     int a = 0, b = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, qhg::k_actions<0>, qhg::kTileThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, qhg::k_scatter, qhg::kTileThreads, 0);
-    const int m = a < b ? a : b;
-    return m > 0 ? m : 1;
+    *actions = a > 0 ? a : 1;
+    *scatter = b > 0 ? b : 1;
 }
 
 // the specialised action program matching a run's action list, 0 if none
