@@ -162,6 +162,69 @@ int qhg_gpu_step_profiled(qhg_run *run, int32_t nsteps, float *kernel_ms);
  * the run's stream, waits, and returns the device time in *elapsed_ms */
 int qhg_gpu_step_timed(qhg_run *run, int32_t nsteps, float *elapsed_ms);
 
+/* ------------------------------------------------------------------------
+ * Batches: many independent runs of one action list in one device table,
+ * stepped together (one launch of each step kernel over all runs, captured
+ * as a CUDA graph).  Runs differ in seed, grid, population and action
+ * parameters; every run's results are the same as those of the run alone
+ * through qhg_gpu_* with the same inputs.  Runs can join (qhg_batch_add_run)
+ * and leave (qhg_batch_remove_run) between steps: this is what served
+ * execution builds on.  The reference has no batched form: a QHG4 process
+ * runs one simulation; these calls replace running qhg_gpu_* (or the
+ * reference) once per simulation.
+ * ------------------------------------------------------------------------ */
+typedef struct qhg_batch qhg_batch;
+
+typedef struct {
+    int32_t  n_actions;                         /* action types in execution order (as qhg_run_desc) */
+    int32_t  action_type[QHG_MAX_ACTIONS];
+    int64_t  agent_capacity;                    /* rows of the shared agent table */
+    int64_t  cell_capacity;                     /* cells of all runs in the batch at once */
+    int64_t  stage_capacity;                    /* agents admitted between two steps */
+    int32_t  max_runs;                          /* runs in the batch at once */
+    int32_t  device;
+} qhg_batch_desc;
+
+typedef struct {
+    uint64_t seed;
+    double   action_param[QHG_MAX_ACTIONS][4];  /* this run's parameters (slots as qhg_run_desc) */
+} qhg_batch_run_desc;
+
+typedef struct {
+    int32_t active;       /* 0 once removed */
+    int32_t cell0;        /* first cell of the run in the batch's cell space */
+    int32_t num_cells;
+    int32_t steps_done;   /* steps the run has executed */
+} qhg_batch_run_status;
+
+const char *qhg_batch_last_error(void);
+int qhg_batch_create(const qhg_batch_desc *desc, qhg_batch **out);
+/* admits a run (grid as qhg_gpu_upload_grid, agents as qhg_gpu_upload_agents
+ * with first step 0); its agents enter at the next qhg_batch_step, after
+ * which it has done 0 steps.  *run receives its index. */
+int qhg_batch_add_run(qhg_batch *batch, const qhg_batch_run_desc *run_desc, const int32_t *nbr6,
+                      const uint8_t *nnbr, const double *K, int32_t num_cells, const qhg_agents_soa *agents,
+                      int64_t n, int32_t *run);
+/* the run's agents leave at the next step; read its results before */
+int qhg_batch_remove_run(qhg_batch *batch, int32_t run);
+int qhg_batch_step(qhg_batch *batch, int32_t nsteps);
+int qhg_batch_step_timed(qhg_batch *batch, int32_t nsteps, float *elapsed_ms);
+int qhg_batch_sync(qhg_batch *batch);
+int qhg_batch_num_agents(qhg_batch *batch, int64_t *n);
+int qhg_batch_run_info(qhg_batch *batch, int32_t run, qhg_batch_run_status *info);
+/* statistics of the run's last nsteps steps (nsteps <= 64) */
+int qhg_batch_stats(qhg_batch *batch, int32_t run, int32_t nsteps, qhg_step_stats *out);
+/* the run's agents ordered by cell, cells relative to the run's grid */
+int qhg_batch_download(qhg_batch *batch, int32_t run, qhg_agents_soa *out, int64_t cap, int64_t *n);
+int qhg_batch_counts(qhg_batch *batch, int32_t run, uint32_t *cell_counts);
+/* launch shape of the persistent kernels (CTAs per SM); results do not
+ * depend on it */
+int qhg_batch_set_shape(qhg_batch *batch, int32_t actions_ctas_per_sm, int32_t scatter_ctas_per_sm);
+int qhg_batch_get_shape(qhg_batch *batch, int32_t *actions_ctas_per_sm, int32_t *scatter_ctas_per_sm,
+                        int32_t *max_actions, int32_t *max_scatter);
+int qhg_batch_stream(qhg_batch *batch, void **stream);
+int qhg_batch_destroy(qhg_batch *batch);
+
 /*
  * Per-cell census of a caller-owned agent table, for callers that cannot
  * allocate device memory (a host runtime with its own fixed device pool, a

@@ -14,16 +14,18 @@
 #include <cuda_runtime.h>
 
 #include "qhg_device.cuh"
+#include "qhg_host.h"
 #include "../../include/qhg_gpu.h"
 
 extern "C" int qhg_launch_step(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
-                               const qhg::LaunchShape *L, cudaStream_t stream);
+                               const qhg::BatchBuffers *BB, const qhg::LaunchShape *L, cudaStream_t stream);
 extern "C" void qhg_tile_ctas_per_sm(int *actions, int *scatter);
 extern "C" int qhg_match_program(const int32_t *types, int n);
 extern "C" int qhg_launch_gather_genomes(const int32_t *gslot, const uint64_t *genome, uint32_t n, int words,
                                          uint32_t slots, uint64_t *out, cudaStream_t stream);
 extern "C" int qhg_launch_step_timed(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
-                                     const qhg::LaunchShape *L, cudaStream_t stream, cudaEvent_t *ev);
+                                     const qhg::BatchBuffers *BB, const qhg::LaunchShape *L, cudaStream_t stream,
+                                     cudaEvent_t *ev);
 
 using namespace qhg;
 
@@ -244,6 +246,139 @@ static int64_t bino_threshold(double L) {
     return (int64_t)y;
 }
 
+// Per-action constants and the step flags of an action list given in
+// execution order; draw windows are handed out in that order.
+int qhg_host_actions(StepConst &P, int n, const int32_t *types, const double (*params)[4], std::string &err) {
+    uint32_t w = 0;
+    for (int a = 0; a < n; a++) {
+        ActionConst &A = P.act[a];
+        const double *p = params[a];
+        A.type = types[a];
+        A.window = w;
+        switch (A.type) {
+        case kGetOld:
+            P.age_from_birth = 1;
+            break;
+        case kFertility:
+            A.f0 = (float)p[0]; A.f1 = (float)p[1]; A.f2 = (float)p[2];
+            if (!P.age_from_birth) P.reads_age = 1;   // reads the age before any GetOld sets it
+            break;
+        case kRandomPair:
+            P.has_pair = 1;
+            break;
+        case kVerhulst:
+        case kVerhulstVarK:
+            if (P.n_verhulst >= kMaxVerhulst) {
+                err = "more than one Verhulst action";
+                return -1;
+            }
+            A.vslot = P.n_verhulst;
+            P.verhulst_act[P.n_verhulst++] = a;
+            A.b0 = p[0]; A.d0 = p[1]; A.th = p[2];
+            A.th_b0 = p[2] - p[0];
+            A.th_d0 = p[2] - p[1];
+            A.K = p[3];
+            w += 2;
+            break;
+        case kOldAgeDeath: {
+            // OldAgeDeath::execute (actions/OldAgeDeath.cpp:57-60):
+            // age > M + wrandr(1 - U*M, 1 + U*M)
+            const double M = p[0], U = p[1];
+            const double lo = 1 - U * M;
+            const double hi = 1 + U * M;
+            const double wd = hi - lo;
+            A.oad_M = M; A.oad_a = lo; A.oad_w = wd;
+            const double g0 = M + (lo + (wd * 0.0) / 4294967296.0);
+            const double g1 = M + (lo + (wd * 4294967295.0) / 4294967296.0);
+            A.age_lo = float_floor_of(g0);
+            A.age_hi = float_floor_of(g1);
+            P.age_from_birth = 1;
+            w += 1;
+            break;
+        }
+        case kRandomMove:
+        case kWeightedMove:
+            A.pthr = host_prob_threshold(p[0]);
+            P.has_move = 1;
+            if (A.type == kWeightedMove) P.has_wmove = 1;
+            w += 2;
+            break;
+        default:
+            err = "unknown action type";
+            return -1;
+        }
+    }
+    if (w > 4 * 64) {
+        err = "too many draws per agent";
+        return -1;
+    }
+    return 0;
+}
+
+// Grid tables of one run: rev packs, 3 bits per neighbour slot q, the slot
+// of the cell in the neighbour's own list; wthr holds the WeightedMove
+// thresholds (SingleEvaluator's cumulated weights, actions/SingleEvaluator.cpp:174-241,
+// as integers: dR2 = wrandd()*W[n] < W[j]  <=>  u < T_j) and wflag marks cells
+// whose weights are all equal.
+int qhg_host_grid_tables(int C, const int32_t *nbr6, const uint8_t *nnbr, const double *K, bool wm,
+                         std::vector<uint32_t> &rev, std::vector<uint64_t> &wthr, std::vector<uint8_t> &wflag,
+                         std::string &err) {
+    rev.assign((size_t)C, 0u);
+    for (int c = 0; c < C; c++) {
+        if (nnbr[c] > 6) { err = "more than 6 neighbours"; return -1; }
+        for (int j = 0; j < 6; j++) {
+            const int d = nbr6[(size_t)c * 6 + j];
+            if (d >= C || d < -1) { err = "neighbour index out of range"; return -1; }
+            if (j >= nnbr[c] || d < 0) continue;
+            int k = -1;
+            for (int q = 0; q < nnbr[d]; q++) {
+                if (nbr6[(size_t)d * 6 + q] == c) { k = q; break; }
+            }
+            if (k < 0) { err = "neighbour table is not symmetric"; return -1; }
+            rev[(size_t)c] |= (uint32_t)k << (3 * j);
+        }
+    }
+    wthr.assign((size_t)C * 6, 0);
+    wflag.assign((size_t)C, 0);
+    if (!wm) return 0;
+    std::vector<double> W((size_t)C * 7);
+    for (int c = 0; c < C; c++) {
+        const double dV = K[c];
+        W[(size_t)c * 7] = (dV > 0) ? dV : 0;
+    }
+    for (int c = 0; c < C; c++) {
+        double dW = W[(size_t)c * 7];
+        for (int i = 0; i < 6; i++) {
+            double dCW = 0;
+            const int ni = nbr6[(size_t)c * 6 + i];
+            if (ni >= 0) dCW = W[(size_t)ni * 7];
+            dCW = (dCW > 0) ? dCW : 0;
+            dW = dW + dCW;
+            W[(size_t)c * 7 + i + 1] = dW;
+        }
+    }
+    for (int c = 0; c < C; c++) {
+        const int nn = nnbr[c];
+        const double *Wc = &W[(size_t)c * 7];
+        const double Wn = Wc[nn];
+        if (Wc[0] == Wn) {
+            wflag[c] = 1;
+            continue;
+        }
+        auto f = [&](uint64_t u) { return ((1.0 * (double)u) / 4294967296.0) * Wn; };
+        for (int j = 0; j < nn; j++) {
+            const double x = Wc[j];
+            // smallest u in [0, 2^32] with f(u) >= x  (f(2^32) counts as +inf)
+            double g = std::floor(x / Wn * 4294967296.0);
+            uint64_t u = (g <= 0) ? 0ull : (g >= 4294967296.0 ? 4294967296ull : (uint64_t)g);
+            while (u > 0 && f(u - 1) >= x) u--;
+            while (u < 4294967296ull && f(u) < x) u++;
+            wthr[(size_t)c * 6 + j] = u;
+        }
+    }
+    return 0;
+}
+
 extern "C" const char *qhg_gpu_last_error(void) { return g_last_error.c_str(); }
 
 extern "C" const char *qhg_gpu_version(void) { return "qhg_gpu 0.1 (sm_103a)"; }
@@ -271,68 +406,12 @@ extern "C" int qhg_gpu_create(const qhg_run_desc *desc, qhg_run **out) {
     P.seed = desc->seed;
     P.n_act = desc->n_actions;
     P.log_births = (desc->flags & QHG_FLAG_LOG_BIRTHS) ? 1 : 0;
-    uint32_t w = 0;
-    for (int a = 0; a < desc->n_actions; a++) {
-        ActionConst &A = P.act[a];
-        const double *p = desc->action_param[a];
-        A.type = desc->action_type[a];
-        A.window = w;
-        switch (A.type) {
-        case kGetOld:
-            P.age_from_birth = 1;
-            break;
-        case kFertility:
-            A.f0 = (float)p[0]; A.f1 = (float)p[1]; A.f2 = (float)p[2];
-            if (!P.age_from_birth) P.reads_age = 1;   // reads the age before any GetOld sets it
-            break;
-        case kRandomPair:
-            P.has_pair = 1;
-            break;
-        case kVerhulst:
-        case kVerhulstVarK:
-            if (P.n_verhulst >= kMaxVerhulst) {
-                delete r;
-                return fail(QHG_ERR_ARG, "more than 2 Verhulst actions");
-            }
-            A.vslot = P.n_verhulst;
-            P.verhulst_act[P.n_verhulst++] = a;
-            A.b0 = p[0]; A.d0 = p[1]; A.th = p[2];
-            A.th_b0 = p[2] - p[0];
-            A.th_d0 = p[2] - p[1];
-            A.K = p[3];
-            w += 2;
-            break;
-        case kOldAgeDeath: {
-            // OldAgeDeath::execute (actions/OldAgeDeath.cpp:57-60):
-            // age > M + wrandr(1 - U*M, 1 + U*M)
-            const double M = p[0], U = p[1];
-            const double a = 1 - U * M;
-            const double b = 1 + U * M;
-            const double wd = b - a;
-            A.oad_M = M; A.oad_a = a; A.oad_w = wd;
-            const double g0 = M + (a + (wd * 0.0) / 4294967296.0);
-            const double g1 = M + (a + (wd * 4294967295.0) / 4294967296.0);
-            A.age_lo = float_floor_of(g0);
-            A.age_hi = float_floor_of(g1);
-            P.age_from_birth = 1;
-            w += 1;
-            break;
-        }
-        case kRandomMove:
-        case kWeightedMove:
-            A.pthr = host_prob_threshold(p[0]);
-            P.has_move = 1;
-            if (A.type == kWeightedMove) P.has_wmove = 1;
-            w += 2;
-            break;
-        default:
+    {
+        std::string err;
+        if (qhg_host_actions(P, desc->n_actions, desc->action_type, desc->action_param, err) != 0) {
             delete r;
-            return fail(QHG_ERR_ARG, "unknown action type");
+            return fail(QHG_ERR_ARG, err);
         }
-    }
-    if (w > 4 * 64) {
-        delete r;
-        return fail(QHG_ERR_ARG, "too many draws per agent");
     }
     if (desc->genome_size > 0) {
         P.genome_size = desc->genome_size;
@@ -378,62 +457,13 @@ extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_
     }
     CUDA_TRY(cudaSetDevice(r->desc.device));
     const int C = num_cells;
-    std::vector<uint32_t> rev((size_t)C, 0u);
-    for (int c = 0; c < C; c++) {
-        if (nnbr[c] > 6) return fail(QHG_ERR_ARG, "more than 6 neighbours");
-        for (int j = 0; j < 6; j++) {
-            const int d = nbr6[(size_t)c * 6 + j];
-            if (d >= C || d < -1) return fail(QHG_ERR_ARG, "neighbour index out of range");
-            if (j >= nnbr[c] || d < 0) continue;
-            int k = -1;
-            for (int q = 0; q < nnbr[d]; q++) {
-                if (nbr6[(size_t)d * 6 + q] == c) { k = q; break; }
-            }
-            if (k < 0) return fail(QHG_ERR_ARG, "neighbour table is not symmetric");
-            rev[(size_t)c] |= (uint32_t)k << (3 * j);
-        }
-    }
-    // WeightedMove: cumulated weights (SingleEvaluator, actions/SingleEvaluator.cpp:174-241)
-    // turned into integer thresholds: dR2 = wrandd()*W[n] < W[j]  <=>  u < T_j
-    std::vector<uint64_t> wthr((size_t)C * 6, 0);
-    std::vector<uint8_t> wflag(C, 0);
-    bool has_wm = false;
-    for (int a = 0; a < r->P.n_act; a++) has_wm |= (r->P.act[a].type == kWeightedMove);
-    if (has_wm) {
-        std::vector<double> W((size_t)C * 7);
-        for (int c = 0; c < C; c++) {
-            const double dV = K[c];
-            W[(size_t)c * 7] = (dV > 0) ? dV : 0;
-        }
-        for (int c = 0; c < C; c++) {
-            double dW = W[(size_t)c * 7];
-            for (int i = 0; i < 6; i++) {
-                double dCW = 0;
-                const int ni = nbr6[(size_t)c * 6 + i];
-                if (ni >= 0) dCW = W[(size_t)ni * 7];
-                dCW = (dCW > 0) ? dCW : 0;
-                dW = dW + dCW;
-                W[(size_t)c * 7 + i + 1] = dW;
-            }
-        }
-        for (int c = 0; c < C; c++) {
-            const int nn = nnbr[c];
-            const double *Wc = &W[(size_t)c * 7];
-            const double Wn = Wc[nn];
-            if (Wc[0] == Wn) {
-                wflag[c] = 1;
-                continue;
-            }
-            auto f = [&](uint64_t u) { return ((1.0 * (double)u) / 4294967296.0) * Wn; };
-            for (int j = 0; j < nn; j++) {
-                const double x = Wc[j];
-                // smallest u in [0, 2^32] with f(u) >= x  (f(2^32) counts as +inf)
-                double g = std::floor(x / Wn * 4294967296.0);
-                uint64_t u = (g <= 0) ? 0ull : (g >= 4294967296.0 ? 4294967296ull : (uint64_t)g);
-                while (u > 0 && f(u - 1) >= x) u--;
-                while (u < 4294967296ull && f(u) < x) u++;
-                wthr[(size_t)c * 6 + j] = u;
-            }
+    std::vector<uint32_t> rev;
+    std::vector<uint64_t> wthr;
+    std::vector<uint8_t> wflag;
+    {
+        std::string err;
+        if (qhg_host_grid_tables(C, nbr6, nnbr, K, r->P.has_wmove != 0, rev, wthr, wflag, err) != 0) {
+            return fail(QHG_ERR_ARG, err);
         }
     }
     cudaFree(r->d_nbr); cudaFree(r->d_nnbr); cudaFree(r->d_rev); cudaFree(r->d_K); cudaFree(r->d_vthr);
@@ -670,7 +700,7 @@ static int build_graph(qhg_run *r, int cur) {
     StepBuffers B = make_buffers(r, cur);
     cudaGraph_t g = nullptr;
     CUDA_TRY(cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal));
-    int le = qhg_launch_step(&r->P, r->d_rs, &B, &r->shape, r->stream);
+    int le = qhg_launch_step(&r->P, r->d_rs, &B, nullptr, &r->shape, r->stream);
     cudaError_t ee = cudaStreamEndCapture(r->stream, &g);
     if (le != 0 || ee != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
@@ -722,7 +752,7 @@ extern "C" int qhg_gpu_step_profiled(qhg_run *r, int32_t nsteps, float *kernel_m
     }
     for (int32_t s = 0; s < nsteps; s++) {
         StepBuffers B = make_buffers(r, r->cur);
-        int le = qhg_launch_step_timed(&r->P, r->d_rs, &B, &r->shape, r->stream, r->ev);
+        int le = qhg_launch_step_timed(&r->P, r->d_rs, &B, nullptr, &r->shape, r->stream, r->ev);
         if (le != 0) return fail(QHG_ERR_CUDA, std::string("launch: ") + cudaGetErrorString((cudaError_t)le));
         const bool gen = r->P.genome_words > 0;
         CUDA_TRY(cudaEventSynchronize(r->ev[gen ? 4 : 3]));

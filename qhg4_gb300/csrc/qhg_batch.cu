@@ -1,0 +1,736 @@
+// Host side of the batch API declared in include/qhg_gpu.h (qhg_batch_*).
+//
+// A batch keeps many independent runs of one action list in one device
+// table: every run owns a contiguous range of cells (its own grid, neighbour
+// indices offset into the range) and therefore a contiguous range of rows of
+// the cell-sorted agent table.  One step of the batch is one launch of each
+// step kernel over all runs (k_actions, k_cell_scan, k_scatter in their batch
+// form, plus k_inject), captured as a CUDA graph per table parity.  Per-run
+// values -- seed, step offset, action parameters -- come from a run table in
+// device memory; results of a run are the same as those of the run alone.
+//
+// Admission places a run's grid into a free cell range and stages its agents;
+// the next step's cell scan counts them and k_inject writes them after the
+// newborns of their cells, so the run's step 0 is the batch step after that.
+// Removal clears the run's active flag: its agents leave at the next step and
+// its cell range is free after it.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "qhg_device.cuh"
+#include "qhg_host.h"
+#include "../../include/qhg_gpu.h"
+
+using namespace qhg;
+
+namespace {
+
+thread_local std::string g_batch_error;
+
+int bfail(int code, const std::string &msg) {
+    g_batch_error = msg;
+    return code;
+}
+
+#define BCUDA(expr)                                                                      \
+    do {                                                                                 \
+        cudaError_t e_ = (expr);                                                         \
+        if (e_ != cudaSuccess) {                                                         \
+            return bfail(e_ == cudaErrorMemoryAllocation ? QHG_ERR_NOMEM : QHG_ERR_CUDA, \
+                         std::string(#expr) + ": " + cudaGetErrorString(e_));            \
+        }                                                                                \
+    } while (0)
+
+struct RunSlot {
+    bool used = false;      // holds a run (active or leaving)
+    bool active = false;
+    uint32_t cell0 = 0, cell1 = 0;
+    int32_t step0 = 0;      // batch step of the run's step 0
+    int32_t left_at = -1;   // batch step at which its agents leave (-1: still in)
+};
+
+}  // namespace
+
+struct qhg_batch {
+    qhg_batch_desc desc;
+    cudaStream_t stream = nullptr;
+    StepConst P;
+    LaunchShape shape = {1, 1};
+    int nsm = 1, max_ctas_actions = 1, max_ctas_scatter = 1;
+    uint32_t cell_cap = 0, agent_cap = 0, stage_cap = 0;
+    int max_runs = 0;
+    uint32_t cell_hwm = 0;   // cells scanned per step (end of the highest range in use)
+    // grid of all runs
+    int32_t *d_nbr = nullptr;
+    uint8_t *d_nnbr = nullptr;
+    uint32_t *d_rev = nullptr;
+    double *d_K = nullptr;
+    ulonglong2 *d_vthr = nullptr;
+    uint64_t *d_wthr = nullptr;
+    uint8_t *d_wflag = nullptr;
+    uint32_t *d_crun = nullptr;
+    // tables (ping-pong)
+    int64_t *d_id[2] = {nullptr, nullptr};
+    float *d_birth[2] = {nullptr, nullptr};
+    float *d_age[2] = {nullptr, nullptr};
+    float *d_lastb[2] = {nullptr, nullptr};
+    uint8_t *d_meta[2] = {nullptr, nullptr};
+    uint32_t *d_ne[2] = {nullptr, nullptr};
+    uint32_t *d_nes[2] = {nullptr, nullptr};
+    uint32_t *d_tf[2] = {nullptr, nullptr};
+    // scratch of a step
+    uint8_t *d_outc = nullptr;
+    int32_t *d_father = nullptr;
+    uint16_t *d_brank = nullptr;
+    uint32_t *d_clsc = nullptr, *d_sbase = nullptr, *d_bbase = nullptr, *d_bidb = nullptr, *d_obase = nullptr;
+    uint32_t *d_tflag = nullptr;
+    uint4 *d_tagg = nullptr, *d_tincl = nullptr;
+    // runs
+    BatchRun *d_runs = nullptr;
+    int64_t *d_rnext = nullptr;
+    uint32_t *d_rstat = nullptr;
+    // admission
+    uint32_t *d_inj = nullptr, *d_istart = nullptr, *d_ibase = nullptr, *d_injdone = nullptr;
+    int64_t *d_sid = nullptr;
+    float *d_sbirth = nullptr, *d_sage = nullptr, *d_slastb = nullptr;
+    uint8_t *d_smeta = nullptr;
+    uint32_t *d_scell = nullptr;
+    uint32_t staged = 0;            // rows staged for the next step
+    // download scratch
+    uint32_t *d_rowcell = nullptr;
+    RunState *d_rs = nullptr;
+    RunState *h_rs = nullptr;
+    std::vector<RunSlot> slots;
+    std::vector<BatchRun> h_runs;
+    int32_t gstep = 0;              // batch steps launched
+    int cur = 0;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+};
+
+namespace {
+
+void drop_graphs(qhg_batch *b) {
+    for (int p = 0; p < 2; p++) {
+        if (b->graph[p]) cudaGraphExecDestroy(b->graph[p]);
+        b->graph[p] = nullptr;
+    }
+}
+
+StepBuffers make_buffers(qhg_batch *b, int cur) {
+    const int nx = cur ^ 1;
+    StepBuffers B;
+    memset(&B, 0, sizeof(B));
+    B.nonempty = b->d_ne[cur]; B.ne_start = b->d_nes[cur]; B.tile_first = b->d_tf[cur];
+    B.id = b->d_id[cur]; B.birth = b->d_birth[cur]; B.age = b->d_age[cur]; B.lastb = b->d_lastb[cur];
+    B.meta = b->d_meta[cur];
+    B.nonempty2 = b->d_ne[nx]; B.ne_start2 = b->d_nes[nx]; B.tile_first2 = b->d_tf[nx];
+    B.id2 = b->d_id[nx]; B.birth2 = b->d_birth[nx]; B.age2 = b->d_age[nx]; B.lastb2 = b->d_lastb[nx];
+    B.meta2 = b->d_meta[nx];
+    B.nbr = b->d_nbr; B.nnbr = b->d_nnbr; B.rev = b->d_rev; B.K = b->d_K; B.vthr = b->d_vthr;
+    B.wthr = b->d_wthr; B.wflag = b->d_wflag;
+    B.outc = b->d_outc; B.father = b->d_father; B.brank = b->d_brank; B.clsc = b->d_clsc;
+    B.sbase = b->d_sbase; B.bbase = b->d_bbase; B.bidbase = b->d_bidb; B.obase = b->d_obase;
+    B.tile_flag = b->d_tflag; B.tile_agg = b->d_tagg; B.tile_incl = b->d_tincl;
+    return B;
+}
+
+BatchBuffers make_batch_buffers(qhg_batch *b) {
+    BatchBuffers BB;
+    BB.crun = b->d_crun;
+    BB.runs = b->d_runs;
+    BB.rnext = b->d_rnext;
+    BB.rstat = b->d_rstat;
+    BB.nruns = b->max_runs;
+    BB.inj = b->d_inj;
+    BB.istart = b->d_istart;
+    BB.ibase = b->d_ibase;
+    BB.sid = b->d_sid; BB.sbirth = b->d_sbirth; BB.sage = b->d_sage; BB.slastb = b->d_slastb;
+    BB.smeta = b->d_smeta; BB.scell = b->d_scell;
+    BB.inj_ctas_done = b->d_injdone;
+    return BB;
+}
+
+// step constants with the cells in use
+void refresh_cells(qhg_batch *b) {
+    uint32_t hwm = 0;
+    for (const RunSlot &s : b->slots) {
+        if (s.used) hwm = std::max(hwm, s.cell1);
+    }
+    hwm = std::max<uint32_t>(hwm, 1u);
+    if (hwm != b->cell_hwm) {
+        b->cell_hwm = hwm;
+        b->P.num_cells = (int32_t)hwm;
+        drop_graphs(b);
+    }
+}
+
+int build_graph(qhg_batch *b, int cur) {
+    StepBuffers B = make_buffers(b, cur);
+    BatchBuffers BB = make_batch_buffers(b);
+    cudaGraph_t g = nullptr;
+    BCUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    int le = qhg_launch_step(&b->P, b->d_rs, &B, &BB, &b->shape, b->stream);
+    cudaError_t ee = cudaStreamEndCapture(b->stream, &g);
+    if (le != 0 || ee != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return bfail(QHG_ERR_CUDA, std::string("graph capture failed: ") +
+                                       cudaGetErrorString(le != 0 ? (cudaError_t)le : ee));
+    }
+    cudaError_t ie = cudaGraphInstantiate(&b->graph[cur], g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) return bfail(QHG_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+    return QHG_OK;
+}
+
+// reads the run state; a device-side error keeps the last committed step
+int pull_state(qhg_batch *b) {
+    BCUDA(cudaMemcpyAsync(b->h_rs, b->d_rs, sizeof(RunState), cudaMemcpyDeviceToHost, b->stream));
+    BCUDA(cudaStreamSynchronize(b->stream));
+    if (b->h_rs->error != 0u) {
+        const uint32_t code = b->h_rs->error, info = b->h_rs->error_info;
+        // a failed step is not retried: the batch stops at its last committed step
+        char buf[160];
+        snprintf(buf, sizeof(buf), "device error %u/%u in batch step %d; the batch must be rebuilt", code, info,
+                 b->h_rs->step);
+        return bfail(code == kErrCellTooLarge ? QHG_ERR_CELL_TOO_LARGE
+                     : code == kErrCapacity   ? QHG_ERR_CAPACITY
+                     : code == kErrTimeout    ? QHG_ERR_TIMEOUT
+                                              : QHG_ERR_DEVICE,
+                     buf);
+    }
+    return QHG_OK;
+}
+
+int check_slot(qhg_batch *b, int32_t run) {
+    if (run < 0 || run >= b->max_runs || !b->slots[(size_t)run].used) return bfail(QHG_ERR_ARG, "no such run");
+    return QHG_OK;
+}
+
+}  // namespace
+
+extern "C" const char *qhg_batch_last_error(void) { return g_batch_error.c_str(); }
+
+extern "C" int qhg_batch_create(const qhg_batch_desc *desc, qhg_batch **out) {
+    if (desc == nullptr || out == nullptr) return bfail(QHG_ERR_ARG, "null argument");
+    if (desc->n_actions < 0 || desc->n_actions > QHG_MAX_ACTIONS) return bfail(QHG_ERR_ARG, "bad n_actions");
+    if (desc->max_runs <= 0 || desc->cell_capacity <= 0 || desc->agent_capacity <= 0 || desc->stage_capacity <= 0) {
+        return bfail(QHG_ERR_ARG, "capacities must be positive");
+    }
+    if (desc->agent_capacity > 0x7fffffffLL || desc->cell_capacity > 0x7fffffffLL ||
+        desc->stage_capacity > 0x7fffffffLL) {
+        return bfail(QHG_ERR_ARG, "capacities above 2^31-1");
+    }
+    int ndev = 0;
+    BCUDA(cudaGetDeviceCount(&ndev));
+    if (desc->device < 0 || desc->device >= ndev) return bfail(QHG_ERR_ARG, "bad device ordinal");
+    BCUDA(cudaSetDevice(desc->device));
+    qhg_batch *b = new qhg_batch();
+    b->desc = *desc;
+    StepConst &P = b->P;
+    memset(&P, 0, sizeof(P));
+    // the action list (types and draw windows) is the batch's; parameters are per run
+    double zero[QHG_MAX_ACTIONS][4];
+    memset(zero, 0, sizeof(zero));
+    std::string err;
+    if (qhg_host_actions(P, desc->n_actions, desc->action_type, zero, err) != 0) {
+        delete b;
+        return bfail(QHG_ERR_ARG, err);
+    }
+    P.n_act = desc->n_actions;
+    P.program = qhg_match_program(desc->action_type, desc->n_actions) == 1 ? 1 : 0;
+    b->cell_cap = (uint32_t)desc->cell_capacity;
+    b->agent_cap = (uint32_t)desc->agent_capacity;
+    b->stage_cap = (uint32_t)desc->stage_capacity;
+    b->max_runs = desc->max_runs;
+    P.capacity = b->agent_cap;
+    b->slots.assign((size_t)b->max_runs, RunSlot());
+    b->h_runs.assign((size_t)b->max_runs, BatchRun());
+    memset(b->h_runs.data(), 0, b->h_runs.size() * sizeof(BatchRun));
+    const size_t C = b->cell_cap, N = b->agent_cap, S = b->stage_cap, R = (size_t)b->max_runs;
+    const size_t nscan = (C + kScanTile - 1) / kScanTile;
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    auto A = [&](void **p, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+    };
+    A((void **)&b->d_nbr, C * 6 * sizeof(int32_t));
+    A((void **)&b->d_nnbr, C);
+    A((void **)&b->d_rev, C * sizeof(uint32_t));
+    A((void **)&b->d_K, C * sizeof(double));
+    A((void **)&b->d_vthr, C * sizeof(ulonglong2));
+    A((void **)&b->d_wthr, C * 6 * sizeof(uint64_t));
+    A((void **)&b->d_wflag, C);
+    A((void **)&b->d_crun, C * sizeof(uint32_t));
+    for (int p = 0; p < 2; p++) {
+        A((void **)&b->d_id[p], N * sizeof(int64_t));
+        A((void **)&b->d_birth[p], N * sizeof(float));
+        A((void **)&b->d_age[p], N * sizeof(float));
+        A((void **)&b->d_lastb[p], N * sizeof(float));
+        A((void **)&b->d_meta[p], N);
+        A((void **)&b->d_ne[p], C * sizeof(uint32_t));
+        A((void **)&b->d_nes[p], (C + 1) * sizeof(uint32_t));
+        A((void **)&b->d_tf[p], (N / kTileAgents + 2) * sizeof(uint32_t));
+    }
+    A((void **)&b->d_outc, N);
+    A((void **)&b->d_father, N * sizeof(int32_t));
+    A((void **)&b->d_brank, N * sizeof(uint16_t));
+    A((void **)&b->d_clsc, C * kCls * sizeof(uint32_t));
+    A((void **)&b->d_sbase, C * sizeof(uint32_t));
+    A((void **)&b->d_bbase, C * sizeof(uint32_t));
+    A((void **)&b->d_bidb, C * sizeof(uint32_t));
+    A((void **)&b->d_obase, C * 6 * sizeof(uint32_t));
+    A((void **)&b->d_tflag, nscan * sizeof(uint32_t));
+    A((void **)&b->d_tagg, nscan * sizeof(uint4));
+    A((void **)&b->d_tincl, nscan * sizeof(uint4));
+    A((void **)&b->d_runs, R * sizeof(BatchRun));
+    A((void **)&b->d_rnext, R * sizeof(int64_t));
+    A((void **)&b->d_rstat, R * kBatchRing * 4 * sizeof(uint32_t));
+    A((void **)&b->d_inj, C * sizeof(uint32_t));
+    A((void **)&b->d_istart, C * sizeof(uint32_t));
+    A((void **)&b->d_ibase, C * sizeof(uint32_t));
+    A((void **)&b->d_injdone, sizeof(uint32_t));
+    A((void **)&b->d_sid, S * sizeof(int64_t));
+    A((void **)&b->d_sbirth, S * sizeof(float));
+    A((void **)&b->d_sage, S * sizeof(float));
+    A((void **)&b->d_slastb, S * sizeof(float));
+    A((void **)&b->d_smeta, S);
+    A((void **)&b->d_scell, S * sizeof(uint32_t));
+    A((void **)&b->d_rs, sizeof(RunState));
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&b->h_rs, sizeof(RunState));
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_clsc, 0, C * kCls * sizeof(uint32_t), b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_crun, 0xff, C * sizeof(uint32_t), b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_inj, 0, C * sizeof(uint32_t), b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_nnbr, 0, C, b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_tflag, 0, nscan * sizeof(uint32_t), b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_injdone, 0, sizeof(uint32_t), b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_rstat, 0, R * kBatchRing * 4 * sizeof(uint32_t), b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_runs, 0, R * sizeof(BatchRun), b->stream);
+    if (e == cudaSuccess) {
+        // an empty table: no agents, no non-empty cells
+        memset(b->h_rs, 0, sizeof(RunState));
+        e = cudaMemcpyAsync(b->d_rs, b->h_rs, sizeof(RunState), cudaMemcpyHostToDevice, b->stream);
+    }
+    const uint32_t zero2[2] = {0u, 0u};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_nes[0], zero2, sizeof(uint32_t), cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b->d_tf[0], zero2, 2 * sizeof(uint32_t), cudaMemcpyHostToDevice, b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) {
+        const std::string msg = std::string("batch create: ") + cudaGetErrorString(e);
+        qhg_batch_destroy(b);
+        return bfail(e == cudaErrorMemoryAllocation ? QHG_ERR_NOMEM : QHG_ERR_CUDA, msg);
+    }
+    cudaDeviceGetAttribute(&b->nsm, cudaDevAttrMultiProcessorCount, desc->device);
+    b->nsm = std::max(1, b->nsm);
+    qhg_tile_ctas_per_sm(&b->max_ctas_actions, &b->max_ctas_scatter);
+    b->shape.actions_grid = b->nsm * b->max_ctas_actions;
+    b->shape.scatter_grid = b->nsm * b->max_ctas_scatter;
+    refresh_cells(b);
+    *out = b;
+    return QHG_OK;
+}
+
+extern "C" int qhg_batch_add_run(qhg_batch *b, const qhg_batch_run_desc *rd, const int32_t *nbr6,
+                                 const uint8_t *nnbr, const double *K, int32_t num_cells,
+                                 const qhg_agents_soa *a, int64_t n, int32_t *run_out) {
+    if (b == nullptr || rd == nullptr || nbr6 == nullptr || nnbr == nullptr || K == nullptr || num_cells <= 0 ||
+        run_out == nullptr || n < 0 || (n > 0 && a == nullptr)) {
+        return bfail(QHG_ERR_ARG, "bad run arguments");
+    }
+    if (n > 0 && (a->id == nullptr || a->cell == nullptr || a->birth == nullptr || a->age == nullptr ||
+                  a->last_birth == nullptr || a->gender == nullptr || a->state == nullptr)) {
+        return bfail(QHG_ERR_ARG, "null agent column");
+    }
+    BCUDA(cudaSetDevice(b->desc.device));
+    // a free run slot; slots of runs that left are reusable once their leaving step has been launched
+    int r = -1;
+    for (int q = 0; q < b->max_runs; q++) {
+        if (!b->slots[(size_t)q].used) { r = q; break; }
+    }
+    if (r < 0) return bfail(QHG_ERR_CAPACITY, "no free run slot");
+    // first free cell range that fits
+    const uint32_t C = (uint32_t)num_cells;
+    std::vector<std::pair<uint32_t, uint32_t>> used;
+    for (const RunSlot &s : b->slots) {
+        if (s.used) used.push_back({s.cell0, s.cell1});
+    }
+    std::sort(used.begin(), used.end());
+    uint32_t at = 0;
+    bool found = false;
+    for (const auto &u : used) {
+        if (u.first >= at && u.first - at >= C) { found = true; break; }
+        at = std::max(at, u.second);
+    }
+    if (!found && (uint64_t)at + C <= b->cell_cap) found = true;
+    if (!found) return bfail(QHG_ERR_CAPACITY, "no free cell range of that size");
+    const uint32_t c0 = at;
+    // grid tables of the run, neighbours offset into its range
+    std::vector<uint32_t> rev;
+    std::vector<uint64_t> wthr;
+    std::vector<uint8_t> wflag;
+    std::string err;
+    if (qhg_host_grid_tables(num_cells, nbr6, nnbr, K, b->P.has_wmove != 0, rev, wthr, wflag, err) != 0) {
+        return bfail(QHG_ERR_ARG, err);
+    }
+    std::vector<int32_t> gnbr((size_t)C * 6);
+    for (size_t q = 0; q < gnbr.size(); q++) gnbr[q] = nbr6[q] >= 0 ? nbr6[q] + (int32_t)c0 : -1;
+    // agents: live rows grouped by cell (input order kept within a cell)
+    std::vector<uint32_t> cnt((size_t)C + 1, 0);
+    int64_t live = 0, maxid = -1;
+    for (int64_t i = 0; i < n; i++) {
+        if (a->state[i] == 0) continue;
+        const int32_t c = a->cell[i];
+        if (c < 0 || c >= num_cells) return bfail(QHG_ERR_ARG, "agent cell out of range");
+        cnt[(size_t)c + 1]++;
+        live++;
+        maxid = std::max<int64_t>(maxid, a->id[i]);
+    }
+    for (uint32_t c = 0; c < C; c++) {
+        if (cnt[(size_t)c + 1] > (uint32_t)kMaxCell) {
+            return bfail(QHG_ERR_CELL_TOO_LARGE, "a cell holds more than QHG_MAX_CELL_AGENTS agents");
+        }
+        cnt[(size_t)c + 1] += cnt[c];
+    }
+    if ((uint64_t)b->staged + (uint64_t)live > b->stage_cap) {
+        return bfail(QHG_ERR_CAPACITY, "staging area full: step the batch before admitting more agents");
+    }
+    const uint32_t s0 = b->staged;
+    std::vector<int64_t> sid((size_t)live);
+    std::vector<float> sb((size_t)live), sa((size_t)live), sl((size_t)live);
+    std::vector<uint8_t> sm((size_t)live);
+    std::vector<uint32_t> sc((size_t)live), inj(C, 0u), ist(C, 0u);
+    {
+        std::vector<uint32_t> pos(cnt.begin(), cnt.end() - 1);
+        for (int64_t i = 0; i < n; i++) {
+            if (a->state[i] == 0) continue;
+            const uint32_t k = pos[(size_t)a->cell[i]]++;
+            sid[k] = a->id[i];
+            sb[k] = a->birth[i];
+            sa[k] = a->age[i];
+            sl[k] = a->last_birth[i];
+            sm[k] = (uint8_t)((a->gender[i] & 1u) | (a->state[i] == QHG_LS_FERTILE ? kMetaFertile : 0));
+            sc[k] = c0 + (uint32_t)a->cell[i];
+        }
+        for (uint32_t c = 0; c < C; c++) {
+            inj[c] = cnt[(size_t)c + 1] - cnt[c];
+            ist[c] = s0 + cnt[c];
+        }
+    }
+    // the run's constants: its parameters for the batch's action types
+    BatchRun R;
+    memset(&R, 0, sizeof(R));
+    {
+        StepConst tmp;
+        memset(&tmp, 0, sizeof(tmp));
+        if (qhg_host_actions(tmp, b->P.n_act, b->desc.action_type, rd->action_param, err) != 0) {
+            return bfail(QHG_ERR_ARG, err);
+        }
+        for (int q = 0; q < b->P.n_act; q++) R.act[q] = tmp.act[q];
+    }
+    R.seed = rd->seed;
+    R.step0 = b->gstep + 1;
+    R.active = 1u;
+    R.cell0 = c0;
+    R.cell1 = c0 + C;
+    const int64_t nid = maxid + 1;
+    cudaStream_t st = b->stream;
+    BCUDA(cudaMemcpyAsync(b->d_nbr + (size_t)c0 * 6, gnbr.data(), gnbr.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    BCUDA(cudaMemcpyAsync(b->d_nnbr + c0, nnbr, C, cudaMemcpyHostToDevice, st));
+    BCUDA(cudaMemcpyAsync(b->d_rev + c0, rev.data(), C * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    BCUDA(cudaMemcpyAsync(b->d_K + c0, K, C * sizeof(double), cudaMemcpyHostToDevice, st));
+    BCUDA(cudaMemcpyAsync(b->d_wthr + (size_t)c0 * 6, wthr.data(), wthr.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
+    BCUDA(cudaMemcpyAsync(b->d_wflag + c0, wflag.data(), C, cudaMemcpyHostToDevice, st));
+    std::vector<uint32_t> crun(C, (uint32_t)r);
+    BCUDA(cudaMemcpyAsync(b->d_crun + c0, crun.data(), C * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    BCUDA(cudaMemsetAsync(b->d_clsc + (size_t)c0 * kCls, 0, (size_t)C * kCls * sizeof(uint32_t), st));
+    BCUDA(cudaMemcpyAsync(b->d_inj + c0, inj.data(), C * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    BCUDA(cudaMemcpyAsync(b->d_istart + c0, ist.data(), C * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    if (live > 0) {
+        BCUDA(cudaMemcpyAsync(b->d_sid + s0, sid.data(), live * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+        BCUDA(cudaMemcpyAsync(b->d_sbirth + s0, sb.data(), live * sizeof(float), cudaMemcpyHostToDevice, st));
+        BCUDA(cudaMemcpyAsync(b->d_sage + s0, sa.data(), live * sizeof(float), cudaMemcpyHostToDevice, st));
+        BCUDA(cudaMemcpyAsync(b->d_slastb + s0, sl.data(), live * sizeof(float), cudaMemcpyHostToDevice, st));
+        BCUDA(cudaMemcpyAsync(b->d_smeta + s0, sm.data(), live, cudaMemcpyHostToDevice, st));
+        BCUDA(cudaMemcpyAsync(b->d_scell + s0, sc.data(), live * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    }
+    BCUDA(cudaMemcpyAsync(b->d_runs + r, &R, sizeof(BatchRun), cudaMemcpyHostToDevice, st));
+    BCUDA(cudaMemcpyAsync(b->d_rnext + r, &nid, sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    BCUDA(cudaMemsetAsync(b->d_rstat + (size_t)r * kBatchRing * 4, 0, kBatchRing * 4 * sizeof(uint32_t), st));
+    // the host buffers above are freed on return: wait for the copies
+    BCUDA(cudaStreamSynchronize(st));
+    b->staged = s0 + (uint32_t)live;
+    RunSlot &s = b->slots[(size_t)r];
+    s.used = true;
+    s.active = true;
+    s.cell0 = c0;
+    s.cell1 = c0 + C;
+    s.step0 = R.step0;
+    s.left_at = -1;
+    b->h_runs[(size_t)r] = R;
+    refresh_cells(b);
+    *run_out = r;
+    return QHG_OK;
+}
+
+extern "C" int qhg_batch_remove_run(qhg_batch *b, int32_t run) {
+    if (b == nullptr) return bfail(QHG_ERR_ARG, "null batch");
+    int rc = check_slot(b, run);
+    if (rc != QHG_OK) return rc;
+    RunSlot &s = b->slots[(size_t)run];
+    if (!s.active) return bfail(QHG_ERR_STATE, "run already removed");
+    BCUDA(cudaSetDevice(b->desc.device));
+    const uint32_t zero = 0u;
+    BCUDA(cudaMemcpyAsync(reinterpret_cast<char *>(b->d_runs + run) + offsetof(BatchRun, active), &zero,
+                          sizeof(uint32_t), cudaMemcpyHostToDevice, b->stream));
+    BCUDA(cudaStreamSynchronize(b->stream));
+    s.active = false;
+    s.left_at = b->gstep;   // its agents are dropped by the next step
+    b->h_runs[(size_t)run].active = 0u;
+    return QHG_OK;
+}
+
+// after the leaving step of a run has been launched, its cells belong to no
+// run; stream order puts these writes after that step
+static int retire_runs(qhg_batch *b) {
+    bool changed = false;
+    for (size_t q = 0; q < b->slots.size(); q++) {
+        RunSlot &s = b->slots[q];
+        if (s.used && !s.active && s.left_at >= 0 && b->gstep > s.left_at) {
+            BCUDA(cudaMemsetAsync(b->d_crun + s.cell0, 0xff, (size_t)(s.cell1 - s.cell0) * sizeof(uint32_t), b->stream));
+            BCUDA(cudaMemsetAsync(b->d_nnbr + s.cell0, 0, (size_t)(s.cell1 - s.cell0), b->stream));
+            s.used = false;
+            changed = true;
+        }
+    }
+    if (changed) refresh_cells(b);
+    return QHG_OK;
+}
+
+extern "C" int qhg_batch_step(qhg_batch *b, int32_t nsteps) {
+    if (b == nullptr || nsteps < 0) return bfail(QHG_ERR_ARG, "bad step arguments");
+    BCUDA(cudaSetDevice(b->desc.device));
+    for (int32_t k = 0; k < nsteps; k++) {
+        if (b->staged > 0) {
+            const uint32_t n = b->staged;
+            BCUDA(cudaMemcpyAsync(reinterpret_cast<char *>(b->d_rs) + offsetof(RunState, n_staged), &n,
+                                  sizeof(uint32_t), cudaMemcpyHostToDevice, b->stream));
+            // the copy reads `n` from this stack frame: wait for it
+            BCUDA(cudaStreamSynchronize(b->stream));
+        }
+        if (b->graph[b->cur] == nullptr) {
+            int rc = build_graph(b, b->cur);
+            if (rc != QHG_OK) return rc;
+        }
+        BCUDA(cudaGraphLaunch(b->graph[b->cur], b->stream));
+        b->cur ^= 1;
+        b->gstep++;
+        b->staged = 0;
+        int rc = retire_runs(b);
+        if (rc != QHG_OK) return rc;
+    }
+    return QHG_OK;
+}
+
+extern "C" int qhg_batch_step_timed(qhg_batch *b, int32_t nsteps, float *elapsed_ms) {
+    if (b == nullptr || elapsed_ms == nullptr) return bfail(QHG_ERR_ARG, "null argument");
+    BCUDA(cudaSetDevice(b->desc.device));
+    if (b->ev[0] == nullptr) {
+        for (int i = 0; i < 5; i++) BCUDA(cudaEventCreate(&b->ev[i]));
+    }
+    BCUDA(cudaEventRecord(b->ev[0], b->stream));
+    int rc = qhg_batch_step(b, nsteps);
+    if (rc != QHG_OK) return rc;
+    BCUDA(cudaEventRecord(b->ev[1], b->stream));
+    BCUDA(cudaEventSynchronize(b->ev[1]));
+    BCUDA(cudaEventElapsedTime(elapsed_ms, b->ev[0], b->ev[1]));
+    return pull_state(b);
+}
+
+extern "C" int qhg_batch_sync(qhg_batch *b) {
+    if (b == nullptr) return bfail(QHG_ERR_ARG, "null batch");
+    BCUDA(cudaSetDevice(b->desc.device));
+    return pull_state(b);
+}
+
+extern "C" int qhg_batch_set_shape(qhg_batch *b, int32_t actions_ctas_per_sm, int32_t scatter_ctas_per_sm) {
+    if (b == nullptr) return bfail(QHG_ERR_ARG, "null batch");
+    if (actions_ctas_per_sm < 1 || actions_ctas_per_sm > b->max_ctas_actions || scatter_ctas_per_sm < 1 ||
+        scatter_ctas_per_sm > b->max_ctas_scatter) {
+        return bfail(QHG_ERR_ARG, "CTAs per SM outside what fits");
+    }
+    b->shape.actions_grid = b->nsm * actions_ctas_per_sm;
+    b->shape.scatter_grid = b->nsm * scatter_ctas_per_sm;
+    drop_graphs(b);
+    return QHG_OK;
+}
+
+extern "C" int qhg_batch_get_shape(qhg_batch *b, int32_t *actions_ctas_per_sm, int32_t *scatter_ctas_per_sm,
+                                   int32_t *max_actions, int32_t *max_scatter) {
+    if (b == nullptr) return bfail(QHG_ERR_ARG, "null batch");
+    if (actions_ctas_per_sm) *actions_ctas_per_sm = b->shape.actions_grid / b->nsm;
+    if (scatter_ctas_per_sm) *scatter_ctas_per_sm = b->shape.scatter_grid / b->nsm;
+    if (max_actions) *max_actions = b->max_ctas_actions;
+    if (max_scatter) *max_scatter = b->max_ctas_scatter;
+    return QHG_OK;
+}
+
+extern "C" int qhg_batch_run_info(qhg_batch *b, int32_t run, qhg_batch_run_status *info) {
+    if (b == nullptr || info == nullptr) return bfail(QHG_ERR_ARG, "null argument");
+    int rc = check_slot(b, run);
+    if (rc != QHG_OK) return rc;
+    const RunSlot &s = b->slots[(size_t)run];
+    info->active = s.active ? 1 : 0;
+    info->cell0 = (int32_t)s.cell0;
+    info->num_cells = (int32_t)(s.cell1 - s.cell0);
+    const int32_t end = s.active ? b->gstep : std::min(b->gstep, s.left_at);
+    info->steps_done = std::max(0, end - s.step0);
+    return QHG_OK;
+}
+
+extern "C" int qhg_batch_num_agents(qhg_batch *b, int64_t *n) {
+    if (b == nullptr || n == nullptr) return bfail(QHG_ERR_ARG, "null argument");
+    int rc = qhg_batch_sync(b);
+    if (rc != QHG_OK) return rc;
+    *n = b->h_rs->n_agents;
+    return QHG_OK;
+}
+
+extern "C" int qhg_batch_stats(qhg_batch *b, int32_t run, int32_t nsteps, qhg_step_stats *out) {
+    if (b == nullptr || out == nullptr || nsteps < 0 || nsteps > kBatchRing) {
+        return bfail(QHG_ERR_ARG, "bad stats arguments (at most 64 steps)");
+    }
+    int rc = check_slot(b, run);
+    if (rc != QHG_OK) return rc;
+    rc = qhg_batch_sync(b);
+    if (rc != QHG_OK) return rc;
+    const RunSlot &s = b->slots[(size_t)run];
+    const int32_t end = s.active ? b->gstep : std::min(b->gstep, s.left_at);
+    if (end - s.step0 < nsteps) return bfail(QHG_ERR_ARG, "the run has not done that many steps");
+    std::vector<uint32_t> ring((size_t)kBatchRing * 4);
+    BCUDA(cudaMemcpy(ring.data(), b->d_rstat + (size_t)run * kBatchRing * 4, ring.size() * sizeof(uint32_t),
+                     cudaMemcpyDeviceToHost));
+    for (int32_t k = 0; k < nsteps; k++) {
+        const uint32_t g = (uint32_t)(end - nsteps + k);
+        const uint32_t *v = &ring[(size_t)(g % kBatchRing) * 4];
+        out[k].live = v[0]; out[k].births = v[1]; out[k].deaths = v[2]; out[k].moves = v[3];
+    }
+    return QHG_OK;
+}
+
+// rows of a run in the current table: its first row, agents, cell of each row
+static int run_rows(qhg_batch *b, int32_t run, uint32_t *row0, uint32_t *count) {
+    const RunSlot &s = b->slots[(size_t)run];
+    if (!s.active || b->gstep <= s.step0 - 1) return bfail(QHG_ERR_STATE, "the run's agents are not in the table");
+    // the last step's scan left each cell's first row in sbase and the run's
+    // live count in its statistics slot
+    uint32_t r0 = 0, v[4] = {0, 0, 0, 0};
+    BCUDA(cudaMemcpy(&r0, b->d_sbase + s.cell0, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    const uint32_t g = (uint32_t)(b->gstep - 1);
+    BCUDA(cudaMemcpy(v, b->d_rstat + ((size_t)run * kBatchRing + g % kBatchRing) * 4, sizeof(v),
+                     cudaMemcpyDeviceToHost));
+    *row0 = r0;
+    *count = v[0];
+    return QHG_OK;
+}
+
+extern "C" int qhg_launch_run_cells(const uint32_t *nonempty, const uint32_t *ne_start, uint32_t n_nonempty,
+                                    uint32_t cell0, uint32_t cell1, uint32_t row0, uint32_t nrows,
+                                    uint32_t *row_cell, uint32_t *counts, cudaStream_t stream);
+
+extern "C" int qhg_batch_download(qhg_batch *b, int32_t run, qhg_agents_soa *o, int64_t cap, int64_t *n) {
+    if (b == nullptr || o == nullptr || n == nullptr) return bfail(QHG_ERR_ARG, "null argument");
+    int rc = check_slot(b, run);
+    if (rc != QHG_OK) return rc;
+    rc = qhg_batch_sync(b);
+    if (rc != QHG_OK) return rc;
+    uint32_t row0 = 0, cnt = 0;
+    rc = run_rows(b, run, &row0, &cnt);
+    if (rc != QHG_OK) return rc;
+    *n = cnt;
+    if (cap < (int64_t)cnt) return bfail(QHG_ERR_ARG, "output arrays too small");
+    if (cnt == 0) return QHG_OK;
+    const RunSlot &s = b->slots[(size_t)run];
+    const int cur = b->cur;
+    uint32_t *d_cell = nullptr;
+    BCUDA(cudaMalloc(&d_cell, (size_t)cnt * sizeof(uint32_t)));
+    int le = qhg_launch_run_cells(b->d_ne[cur], b->d_nes[cur], b->h_rs->n_nonempty, s.cell0, s.cell1, row0, cnt,
+                                  d_cell, nullptr, b->stream);
+    cudaError_t e = le == 0 ? cudaStreamSynchronize(b->stream) : (cudaError_t)le;
+    std::vector<uint32_t> cells(cnt);
+    std::vector<uint8_t> meta(cnt);
+    if (e == cudaSuccess) e = cudaMemcpy(cells.data(), d_cell, cnt * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    cudaFree(d_cell);
+    if (e == cudaSuccess) e = cudaMemcpy(o->id, b->d_id[cur] + row0, cnt * sizeof(int64_t), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(o->birth, b->d_birth[cur] + row0, cnt * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(o->age, b->d_age[cur] + row0, cnt * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(o->last_birth, b->d_lastb[cur] + row0, cnt * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(meta.data(), b->d_meta[cur] + row0, cnt, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return bfail(QHG_ERR_CUDA, std::string("batch download: ") + cudaGetErrorString(e));
+    for (uint32_t i = 0; i < cnt; i++) {
+        o->cell[i] = (int32_t)(cells[i] - s.cell0);
+        o->gender[i] = meta[i] & kMetaGender;
+        o->state[i] = (meta[i] & kMetaFertile) ? QHG_LS_FERTILE : QHG_LS_ALIVE;
+    }
+    return QHG_OK;
+}
+
+extern "C" int qhg_batch_counts(qhg_batch *b, int32_t run, uint32_t *counts) {
+    if (b == nullptr || counts == nullptr) return bfail(QHG_ERR_ARG, "null argument");
+    int rc = check_slot(b, run);
+    if (rc != QHG_OK) return rc;
+    rc = qhg_batch_sync(b);
+    if (rc != QHG_OK) return rc;
+    uint32_t row0 = 0, cnt = 0;
+    rc = run_rows(b, run, &row0, &cnt);
+    if (rc != QHG_OK) return rc;
+    const RunSlot &s = b->slots[(size_t)run];
+    const uint32_t C = s.cell1 - s.cell0;
+    uint32_t *d_cnt = nullptr;
+    BCUDA(cudaMalloc(&d_cnt, (size_t)C * sizeof(uint32_t)));
+    cudaError_t e = cudaMemsetAsync(d_cnt, 0, (size_t)C * sizeof(uint32_t), b->stream);
+    if (e == cudaSuccess) {
+        int le = qhg_launch_run_cells(b->d_ne[b->cur], b->d_nes[b->cur], b->h_rs->n_nonempty, s.cell0, s.cell1, row0,
+                                      cnt, nullptr, d_cnt, b->stream);
+        e = le == 0 ? cudaStreamSynchronize(b->stream) : (cudaError_t)le;
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(counts, d_cnt, (size_t)C * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    cudaFree(d_cnt);
+    if (e != cudaSuccess) return bfail(QHG_ERR_CUDA, std::string("batch counts: ") + cudaGetErrorString(e));
+    return QHG_OK;
+}
+
+extern "C" int qhg_batch_stream(qhg_batch *b, void **stream) {
+    if (b == nullptr || stream == nullptr) return bfail(QHG_ERR_ARG, "null argument");
+    *stream = (void *)b->stream;
+    return QHG_OK;
+}
+
+extern "C" int qhg_batch_destroy(qhg_batch *b) {
+    if (b == nullptr) return QHG_OK;
+    cudaSetDevice(b->desc.device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    drop_graphs(b);
+    void *ptrs[] = {b->d_nbr, b->d_nnbr, b->d_rev, b->d_K, b->d_vthr, b->d_wthr, b->d_wflag, b->d_crun,
+                    b->d_outc, b->d_father, b->d_brank, b->d_clsc, b->d_sbase, b->d_bbase, b->d_bidb,
+                    b->d_obase, b->d_tflag, b->d_tagg, b->d_tincl, b->d_runs, b->d_rnext, b->d_rstat,
+                    b->d_inj, b->d_istart, b->d_ibase, b->d_injdone, b->d_sid, b->d_sbirth, b->d_sage,
+                    b->d_slastb, b->d_smeta, b->d_scell, b->d_rowcell, b->d_rs};
+    for (void *p : ptrs) cudaFree(p);
+    for (int p = 0; p < 2; p++) {
+        cudaFree(b->d_id[p]); cudaFree(b->d_birth[p]); cudaFree(b->d_age[p]); cudaFree(b->d_lastb[p]);
+        cudaFree(b->d_meta[p]); cudaFree(b->d_ne[p]); cudaFree(b->d_nes[p]); cudaFree(b->d_tf[p]);
+    }
+    if (b->h_rs) cudaFreeHost(b->h_rs);
+    for (int i = 0; i < 5; i++) {
+        if (b->ev[i]) cudaEventDestroy(b->ev[i]);
+    }
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return QHG_OK;
+}

@@ -22,6 +22,8 @@ constexpr int kScanThreads = 256;
 constexpr int kScanItems = 2;            // cells per thread in the cell scan
 constexpr int kScanTile = kScanThreads * kScanItems;
 constexpr int kStatsRing = 1024;
+constexpr int kBatchRing = 64;           // per-run statistics ring of a batch (steps)
+constexpr uint32_t kNoRun = 0xffffffffu; // run index of a batch cell that belongs to no run
 constexpr uint32_t kSpinLimit = 1u << 24;  // bounded waits in the look-back
 
 // random stream bases (Philox counter word 0), see oracle/philox4x32.h
@@ -46,6 +48,8 @@ constexpr uint8_t kMetaFertile = 2u;
 constexpr uint8_t kOutBirth = 8u;
 constexpr uint8_t kOutFertile = 16u;
 constexpr uint8_t kOutGender = 32u;
+constexpr uint8_t kOutMoved = 64u;    // registered a move (statistics only)
+constexpr uint8_t kOutDropped = 128u; // left with its run (batches): not a death
 
 // per-cell class counts: [0] stay, [1..6] movers per neighbour slot, [7] births
 constexpr int kCls = 8;
@@ -124,6 +128,7 @@ struct RunState {
     uint32_t hwm;
     uint32_t dead_count;     // deaths of this step pushed to the next free list
     int32_t genome_step;     // step whose newborns k_genomes builds
+    uint32_t n_staged;       // batches: agents waiting to be placed by k_inject
     // statistics ring: [step % kStatsRing][live, births, deaths, moves]
     unsigned long long stats[kStatsRing][4];
 };
@@ -156,6 +161,36 @@ struct StepBuffers {
     uint64_t *genome;
     const uint32_t *freelist; uint32_t *freelist2;
     uint32_t *brec;
+};
+
+// One run of a batch: its seed, the batch step at which its step 0 runs,
+// its cell range and its action parameters (the batch's action types and
+// draw windows, the run's own values).  Runs with active == 0 leave the
+// batch at the next step.
+struct BatchRun {
+    uint64_t seed;
+    int32_t step0;
+    uint32_t active;
+    uint32_t cell0, cell1;
+    ActionConst act[kMaxActions];
+};
+
+// device pointers of a batch step (in addition to StepBuffers)
+struct BatchBuffers {
+    const uint32_t *crun;       // run of each cell (kNoRun: free)
+    const BatchRun *runs;
+    int64_t *rnext;             // next agent ID of each run
+    // per run and ring slot (batch step % kBatchRing): live, births, deaths, moves
+    uint32_t *rstat;
+    int32_t nruns;              // run slots in use (upper bound of run indices)
+    // admission: staged agents sorted by cell, their count per cell and the
+    // first staged row of each cell; placed by k_inject after the scatter
+    uint32_t *inj;
+    const uint32_t *istart;
+    uint32_t *ibase;
+    const int64_t *sid; const float *sbirth; const float *sage; const float *slastb;
+    const uint8_t *smeta; const uint32_t *scell;
+    uint32_t *inj_ctas_done;
 };
 
 // grid sizes of the persistent tile kernels (CTAs); results do not depend

@@ -1,0 +1,24 @@
+// Host-side helpers shared by the single-run API (qhg_api.cu) and the batch
+// API (qhg_batch.cu): action constants, grid tables, launches.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "qhg_device.cuh"
+
+int qhg_host_actions(qhg::StepConst &P, int n, const int32_t *types, const double (*params)[4], std::string &err);
+int qhg_host_grid_tables(int C, const int32_t *nbr6, const uint8_t *nnbr, const double *K, bool wm,
+                         std::vector<uint32_t> &rev, std::vector<uint64_t> &wthr, std::vector<uint8_t> &wflag,
+                         std::string &err);
+
+extern "C" int qhg_launch_step(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
+                               const qhg::BatchBuffers *BB, const qhg::LaunchShape *L, cudaStream_t stream);
+extern "C" int qhg_launch_step_timed(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
+                                     const qhg::BatchBuffers *BB, const qhg::LaunchShape *L, cudaStream_t stream,
+                                     cudaEvent_t *ev);
+extern "C" void qhg_tile_ctas_per_sm(int *actions, int *scatter);
+extern "C" int qhg_match_program(const int32_t *types, int n);

@@ -25,6 +25,7 @@
 // The reference runs these as SPopulation::initializeStep / doActions /
 // finalizeStep (core/SPopulation.cpp:394-577, 596-724, 1058-1092, 509-536).
 #include <algorithm>
+#include <cstring>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -79,8 +80,7 @@ __device__ __forceinline__ uint64_t prob_threshold(double x) {
 // (actions/LinearBirth.cpp:90-112, actions/LinearDeath.cpp:92-122), as
 // integer thresholds: x = birth (kind 1) or birth-rate death (kind 2)
 // threshold with the kind in bits 62-63, y = death threshold
-__device__ __forceinline__ ulonglong2 verhulst_thresholds(const StepConst &P, double Kcell, uint32_t n) {
-    const ActionConst &A = P.act[P.verhulst_act[0]];
+__device__ __forceinline__ ulonglong2 verhulst_thresholds(const ActionConst &A, double Kcell, uint32_t n) {
     double B, D;
     const double K = (A.type == kVerhulst) ? A.K : Kcell;
     if (A.type == kVerhulstVarK && K <= 0.0) {
@@ -160,11 +160,12 @@ struct ActionsSmem {
     uint16_t frank[kTileMax];      // rank of a FERTILE agent among its cell's FERTILE agents of its sex (by ID)
     uint16_t list[kTileMax];       // at each cell's rows: FERTILE females by ID, then FERTILE males by ID
     uint16_t pick[kTileMax];       // at each cell's rows: unsorted FERTILE lists, later the pick values
-    uint16_t pkrow[kTileMax];      // rows of the tile's pairing members that draw (dense)
+    alignas(4) uint16_t pkrow[kTileMax];  // rows of the tile's pairing members that draw (dense)
     uint16_t oadq[kTileMax];       // rows whose OldAgeDeath needs its draw (dense)
     uint8_t oc[kTileMax];          // outcome byte before the deferred OldAgeDeath draws
     uint32_t cstart[kTileCells + 1];  // first row of each cell, relative to the tile
     int32_t cid[kTileCells];
+    uint32_t crun[kTileCells];     // batches: run of each cell
     uint32_t nf[kTileCells];
     uint32_t nm[kTileCells];
     uint64_t tb[kTileCells];       // Verhulst: birth threshold (kind 1) or birth-rate death threshold (kind 2)
@@ -180,9 +181,9 @@ struct ActionsSmem {
 // after the other actions, so that warps do not run Philox for a few lanes
 __host__ __device__ constexpr bool prog_defers_oad(int p) { return p == 2; }
 
-template <int PROG>
+template <int PROG, bool BATCH>
 __global__ void __launch_bounds__(kTileThreads, 4)
-k_actions(const StepConst P, RunState *__restrict__ rs,
+k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
           const uint32_t *__restrict__ nonempty, const uint32_t *__restrict__ ne_start,
           const uint32_t *__restrict__ tile_first,
           const int64_t *__restrict__ id, const float *__restrict__ birth,
@@ -250,6 +251,7 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
             S.cid[lc] = c;
             S.cstart[lc] = cs;
             if (lc == nc - 1) S.cstart[nc] = ce;
+            if (BATCH) S.crun[lc] = BB.crun[c];
             S.nf[lc] = 0u;
             S.nm[lc] = 0u;
             S.cls[lc][0] = S.cls[lc][1] = S.cls[lc][2] = S.cls[lc][3] = 0u;
@@ -306,6 +308,14 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
             }
         }
         __syncthreads();
+        if (BATCH) {
+            // agents of a run that leaves the batch take no part in pairing
+#pragma unroll
+            for (int j = 0; j < RA; j++) {
+                const int i = tid + j * kTileThreads;
+                if (i < na && !BB.runs[S.crun[S.cell[i]]].active) pm[j] &= (uint8_t)~kMetaFertile;
+            }
+        }
         // ---- RandomPair::findMates (actions/RandomPair.cpp:146-270), members in
         // ID order, each pick drawn from the pairing stream of the picking member
         if (P.has_pair) {
@@ -380,7 +390,14 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
                 const uint32_t nF = S.nf[lc], nM = S.nm[lc];
                 const uint32_t nL = (nF <= nM) ? nM : nF;
                 const uint32_t j = S.frank[i];
-                const uint32_t u = draw_block(P.seed, (uint32_t)step, id[a0 + i], kStreamPair).v[0];
+                uint64_t sd = P.seed;
+                int32_t st = step;
+                if (BATCH) {
+                    const BatchRun &R = BB.runs[S.crun[lc]];
+                    sd = R.seed;
+                    st = step - R.step0;
+                }
+                const uint32_t u = draw_block(sd, (uint32_t)st, id[a0 + i], kStreamPair).v[0];
                 S.pick[S.cstart[lc] + j] = (uint16_t)(((uint64_t)(nL - j) * (uint64_t)u) >> 32);
             }
             __syncthreads();
@@ -409,6 +426,10 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
         }
         // ---- every action on every agent (SPopulation::doActions)
         constexpr bool kDeferOad = prog_defers_oad(PROG);
+        uint32_t *const dm = reinterpret_cast<uint32_t *>(S.pkrow);   // batches: deaths | moves << 16 per cell
+        if (BATCH) {
+            for (int lc = tid; lc < nc; lc += kTileThreads) dm[lc] = 0u;
+        }
 #pragma unroll
         for (int j = 0; j < RA; j++) {
             const int i = tid + j * kTileThreads;
@@ -417,6 +438,15 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
             const int lc = S.cell[i];
             const int c = S.cid[lc];
             const uint8_t m8 = pm[j];
+            const BatchRun *R = BATCH ? BB.runs + S.crun[lc] : nullptr;
+            if (BATCH && !R->active) {   // the run leaves the batch: drop its agents
+                S.oc[i] = kOutDropped;
+                S.bfl[i] = 0;
+                continue;
+            }
+            const uint64_t seed = BATCH ? R->seed : P.seed;
+            const int32_t stepR = BATCH ? step - R->step0 : step;
+            const float fTR = BATCH ? (float)stepR : fT;
             const float fb = pb[j];
             float fa = pa[j];
             const float fl = pl[j];
@@ -426,18 +456,18 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
             bool bflag = false;
             int dir = 0;
             AgentDraws dr;
-            dr.init(P.seed, (uint32_t)step, pid[j]);
+            dr.init(seed, (uint32_t)stepR, pid[j]);
             constexpr int NA = PROG ? prog_len(PROG) : kMaxActions;
 #pragma unroll (PROG ? NA : 1)
             for (int a = 0; a < NA; a++) {
                 if ((PROG == 0 && a >= P.n_act) || !alive) break;
-                const ActionConst &A = P.act[a];
+                const ActionConst &A = BATCH ? R->act[a] : P.act[a];
                 switch (PROG ? prog_act(PROG, a) : A.type) {
                 case kGetOld:
-                    fa = __fsub_rn(fT, fb);
+                    fa = __fsub_rn(fTR, fb);
                     break;
                 case kFertility:
-                    if (female) fert = (fa > A.f0) && (fa < A.f1) && (__fsub_rn(fT, fl) > A.f2);
+                    if (female) fert = (fa > A.f0) && (fa < A.f1) && (__fsub_rn(fTR, fl) > A.f2);
                     else fert = fa > A.f0;
                     break;
                 case kVerhulst:
@@ -458,7 +488,7 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
                     break;
                 }
                 case kOldAgeDeath: {
-                    fa = __fsub_rn(fT, fb);
+                    fa = __fsub_rn(fTR, fb);
                     bool die = false;
                     if (fa <= A.age_lo) {
                         die = false;
@@ -511,7 +541,7 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
             }
             const int cls = alive ? (1 + dir) : 0;
             S.oc[i] = (uint8_t)(cls | (bflag ? kOutBirth : 0) | (fert ? kOutFertile : 0) |
-                                ((m8 & kMetaGender) ? kOutGender : 0));
+                                ((m8 & kMetaGender) ? kOutGender : 0) | (dir > 0 ? kOutMoved : 0));
             S.bfl[i] = bflag ? 1 : 0;
             if (bflag) {
                 father[row] = (int32_t)(a0 + (uint32_t)S.mate[i]);
@@ -524,12 +554,15 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
             __syncthreads();
             const uint32_t nq = S.noad;
             constexpr int kOad = prog_len(PROG) - 1;
-            const ActionConst &A = P.act[kOad];
             for (uint32_t q = tid; q < nq; q += kTileThreads) {
                 const int i = S.oadq[q];
-                const float fa = __fsub_rn(fT, birth[a0 + i]);
+                const BatchRun *R = BATCH ? BB.runs + S.crun[S.cell[i]] : nullptr;
+                const ActionConst &A = BATCH ? R->act[kOad] : P.act[kOad];
+                const int32_t stepR = BATCH ? step - R->step0 : step;
+                const float fa = __fsub_rn((float)stepR, birth[a0 + i]);
                 const uint32_t w = A.window;
-                const uint32_t u = pick4(draw_block(P.seed, (uint32_t)step, id[a0 + i], kStreamActions + (w >> 2)), w & 3u);
+                const uint32_t u = pick4(draw_block(BATCH ? R->seed : P.seed, (uint32_t)stepR, id[a0 + i],
+                                                    kStreamActions + (w >> 2)), w & 3u);
                 const double t = __dmul_rn(__dmul_rn(A.oad_w, (double)u), 2.3283064365386962890625e-10);
                 const double thr = __dadd_rn(A.oad_M, __dadd_rn(A.oad_a, t));
                 if ((double)fa > thr) {
@@ -556,6 +589,10 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
             warp_agg_add(in_tile && cls > 0, ((uint32_t)lc << 3) | (uint32_t)slot, &S.cls[lc][slot >> 1],
                          1u << (16 * (slot & 1)));
             warp_agg_add(in_tile && bflag, ((uint32_t)lc << 3) | 7u, &S.cls[lc][3], 1u << 16);
+            if (BATCH) {
+                warp_agg_add(in_tile && cls == 0 && !(oc & kOutDropped), (uint32_t)lc, &dm[lc], 1u);
+                warp_agg_add(in_tile && (oc & kOutMoved), (uint32_t)lc, &dm[lc], 1u << 16);
+            }
         }
         __syncthreads();
         // ---- per cell: mothers' birth ranks by ID (births are numbered in
@@ -573,11 +610,14 @@ k_actions(const StepConst P, RunState *__restrict__ rs,
             const uint32_t c = (uint32_t)S.cid[lc];
             uint4 *dst = reinterpret_cast<uint4 *>(clsc + (size_t)c * kCls);
             const uint32_t w0 = S.cls[lc][0], w1 = S.cls[lc][1], w2 = S.cls[lc][2], w3 = S.cls[lc][3];
+            // slot 7: births, in batches also deaths << 10 and registered moves << 20
+            const uint32_t b7 = BATCH ? ((w3 >> 16) | ((dm[lc] & 0xffffu) << 10) | ((dm[lc] >> 16) << 20)) : (w3 >> 16);
             dst[0] = make_uint4(w0 & 0xffffu, w0 >> 16, w1 & 0xffffu, w1 >> 16);
-            dst[1] = make_uint4(w2 & 0xffffu, w2 >> 16, w3 & 0xffffu, w3 >> 16);
+            dst[1] = make_uint4(w2 & 0xffffu, w2 >> 16, w3 & 0xffffu, b7);
         }
     }
-    // statistics of the step
+    // statistics of the step (batches: per run, by the cell scan)
+    if (BATCH) return;
     const uint32_t tb_ = block_sum(cnt_births, S.red);
     const uint32_t td_ = block_sum(cnt_deaths, S.red);
     const uint32_t tm_ = block_sum(cnt_moves, S.red);
@@ -619,8 +659,34 @@ __device__ __forceinline__ ScanVal sv_shfl_down(ScanVal v, int o) {
 // Look-back status words: (epoch << 2) | 1 aggregate ready, | 2 inclusive
 // prefix ready.  The epoch is the step number, so words of earlier steps read
 // as not ready; the host clears them whenever the step counter is reset.
+// Per-run sums of a batch step over the cells a warp holds: one atomic per
+// run and value; lanes with r == kNoRun add nothing.
+__device__ __forceinline__ void batch_run_stats(uint32_t *rstat, uint32_t slot, uint32_t r, uint32_t n,
+                                                uint32_t b, uint32_t d, uint32_t m) {
+    const int lane = threadIdx.x & 31;
+    uint32_t todo = __ballot_sync(FULL_MASK, r != kNoRun);
+    while (todo) {
+        const int leader = __ffs(todo) - 1;
+        const uint32_t rr = __shfl_sync(FULL_MASK, r, leader);
+        const bool mine = (r == rr);
+        const uint32_t sn = __reduce_add_sync(FULL_MASK, mine ? n : 0u);
+        const uint32_t sb = __reduce_add_sync(FULL_MASK, mine ? b : 0u);
+        const uint32_t sd = __reduce_add_sync(FULL_MASK, mine ? d : 0u);
+        const uint32_t sm = __reduce_add_sync(FULL_MASK, mine ? m : 0u);
+        if (lane == leader) {
+            uint32_t *q = rstat + ((size_t)rr * kBatchRing + slot) * 4;
+            if (sn) atomicAdd(q + 0, sn);
+            if (sb) atomicAdd(q + 1, sb);
+            if (sd) atomicAdd(q + 2, sd);
+            if (sm) atomicAdd(q + 3, sm);
+        }
+        todo &= ~__ballot_sync(FULL_MASK, mine);
+    }
+}
+
+template <bool BATCH>
 __global__ void __launch_bounds__(kScanThreads)
-k_cell_scan(const StepConst P, RunState *__restrict__ rs,
+k_cell_scan(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             const int32_t *__restrict__ nbr, const uint8_t *__restrict__ nnbr,
             const uint32_t *__restrict__ rev, const uint32_t *__restrict__ clsc,
             const double *__restrict__ Kc, ulonglong2 *__restrict__ vthr,
@@ -652,15 +718,19 @@ k_cell_scan(const StepConst P, RunState *__restrict__ rs,
     const int base = (int)tile * kScanTile + threadIdx.x * kScanItems;
 
     uint32_t nnew[kScanItems], stay[kScanItems], bth[kScanItems];
+    uint32_t crn[kScanItems];
+    uint32_t rsum_n = 0u, rsum_b = 0u, rsum_d = 0u, rsum_m = 0u, rcur = kNoRun;
     ScanVal loc = {0u, 0u, 0u};
 #pragma unroll
     for (int j = 0; j < kScanItems; j++) {
         const int d = base + j;
         nnew[j] = stay[j] = bth[j] = 0u;
+        crn[j] = kNoRun;
         if (d < C) {
             // class counts of empty cells are zero (cleared by the scatter)
             const uint32_t st = clsc[(size_t)d * kCls + 0];
-            const uint32_t bt = clsc[(size_t)d * kCls + 7];
+            const uint32_t c7 = clsc[(size_t)d * kCls + 7];
+            const uint32_t bt = c7 & 0x3ffu;
             const int nn = nnbr[d];
             const uint32_t rv = rev[d];
             uint32_t mvin = 0;
@@ -671,11 +741,35 @@ k_cell_scan(const StepConst P, RunState *__restrict__ rs,
             stay[j] = st;
             bth[j] = bt;
             nnew[j] = st + mvin + bt;
+            if (BATCH) {
+                const uint32_t r = BB.crun[d];
+                crn[j] = r;
+                nnew[j] += BB.inj[d];
+                if (r != kNoRun) {
+                    // cells of a thread are consecutive: one run or two
+                    if (r != rcur) {
+                        if (rcur != kNoRun) {
+                            uint32_t *q = BB.rstat + ((size_t)rcur * kBatchRing + (uint32_t)rs->step % kBatchRing) * 4;
+                            if (rsum_n) atomicAdd(q + 0, rsum_n);
+                            if (rsum_b) atomicAdd(q + 1, rsum_b);
+                            if (rsum_d) atomicAdd(q + 2, rsum_d);
+                            if (rsum_m) atomicAdd(q + 3, rsum_m);
+                        }
+                        rcur = r;
+                        rsum_n = rsum_b = rsum_d = rsum_m = 0u;
+                    }
+                    rsum_n += nnew[j];
+                    rsum_b += bt;
+                    rsum_d += (c7 >> 10) & 0x3ffu;
+                    rsum_m += c7 >> 20;
+                }
+            }
             loc.n += nnew[j];
             loc.b += bt;
             loc.ne += (nnew[j] > 0u) ? 1u : 0u;
         }
     }
+    if (BATCH) batch_run_stats(BB.rstat, (uint32_t)rs->step % kBatchRing, rcur, rsum_n, rsum_b, rsum_d, rsum_m);
     // block scan of the per-thread totals
     ScanVal inc = loc;
 #pragma unroll
@@ -786,10 +880,17 @@ k_cell_scan(const StepConst P, RunState *__restrict__ rs,
                 }
             }
             bbase[d] = run;
+            if (BATCH && BB.inj[d] > 0u) BB.ibase[d] = run + bth[j];   // admitted agents follow the newborns
             if (nnew[j] > 0u) {
                 new_nonempty[pre.ne] = (uint32_t)d;
                 new_ne_start[pre.ne] = pre.n;
-                if (P.n_verhulst > 0) vthr[d] = verhulst_thresholds(P, Kc[d], nnew[j]);
+                if (P.n_verhulst > 0) {
+                    if (!BATCH) {
+                        vthr[d] = verhulst_thresholds(P.act[P.verhulst_act[0]], Kc[d], nnew[j]);
+                    } else if (crn[j] != kNoRun) {
+                        vthr[d] = verhulst_thresholds(BB.runs[crn[j]].act[P.verhulst_act[0]], Kc[d], nnew[j]);
+                    }
+                }
                 // tiles begin at the first cell starting at or after t * kTileAgents
                 // (rows past the capacity are never written: the step fails with kErrCapacity)
                 const uint32_t e = min(pre.n + nnew[j], P.capacity);
@@ -824,11 +925,15 @@ struct ScatterSmem {
     uint64_t wlo[kTileThreads / 32];
     uint64_t whi[kTileThreads / 32];
     uint16_t brow[kTileMax];       // rows of the tile's mothers (dense)
+    uint32_t crn[kTileCells];      // batches: run of each cell
+    float cft[kTileCells];         // batches: time of the cell's run
     uint32_t nb;
+    uint32_t last;
 };
 
+template <bool BATCH>
 __global__ void __launch_bounds__(kTileThreads, 4)
-k_scatter(const StepConst P, RunState *__restrict__ rs,
+k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
           const uint32_t *__restrict__ nonempty, const uint32_t *__restrict__ ne_start,
           const uint32_t *__restrict__ tile_first,
           const int64_t *__restrict__ id, const float *__restrict__ birth,
@@ -920,6 +1025,14 @@ k_scatter(const StepConst P, RunState *__restrict__ rs,
             S.sb[lc] = sbase[c];
             S.bb[lc] = bbase[c];
             S.bid[lc] = bidbase[c];
+            if (BATCH) {
+                // birth ranks and IDs count within the run
+                const uint32_t r = BB.crun[c];
+                const BatchRun &R = BB.runs[r];
+                S.crn[lc] = r;
+                S.bid[lc] = bidbase[c] - bidbase[R.cell0];
+                S.cft[lc] = (float)(step - R.step0);
+            }
             // all six slots (unused ones hold stale values that no agent reads),
             // so that the loads do not wait for the neighbour count
 #pragma unroll
@@ -1021,7 +1134,7 @@ k_scatter(const StepConst P, RunState *__restrict__ rs,
                     id2[dst] = pid[j];
                     birth2[dst] = fb;
                     lastb2[dst] = pl[j];
-                    age2[dst] = P.age_from_birth ? __fsub_rn(fT, fb) : pa[j];
+                    age2[dst] = P.age_from_birth ? __fsub_rn(BATCH ? S.cft[lc] : fT, fb) : pa[j];
                     meta2[dst] = (uint8_t)(((code & kOutGender) ? kMetaGender : 0) |
                                            ((code & kOutFertile) ? kMetaFertile : 0));
                     if (genetics) gslot2[dst] = pg[j];
@@ -1047,11 +1160,22 @@ k_scatter(const StepConst P, RunState *__restrict__ rs,
                 continue;
             }
             const int64_t mid = id[row];
-            const uint32_t u = draw_block(P.seed, (uint32_t)step, mid, kStreamBirth).v[0];
+            uint64_t sd = P.seed;
+            int32_t st = step;
+            float ft = fT;
+            int64_t nid = next_id;
+            if (BATCH) {
+                const BatchRun &R = BB.runs[S.crn[lc]];
+                sd = R.seed;
+                st = step - R.step0;
+                ft = S.cft[lc];
+                nid = BB.rnext[S.crn[lc]];
+            }
+            const uint32_t u = draw_block(sd, (uint32_t)st, mid, kStreamBirth).v[0];
             const uint8_t g = (uint8_t)(u >> 31);
-            const int64_t baby = next_id + (int64_t)(S.bid[lc] + rk);
+            const int64_t baby = nid + (int64_t)(S.bid[lc] + rk);
             id2[dst] = baby;
-            birth2[dst] = fT;
+            birth2[dst] = ft;
             lastb2[dst] = 0.0f;
             age2[dst] = 0.0f;
             meta2[dst] = (uint8_t)(g ? kMetaGender : kMetaFertile);
@@ -1085,13 +1209,31 @@ k_scatter(const StepConst P, RunState *__restrict__ rs,
     if (tid == 0) {
         __threadfence();
         const uint32_t done = atomicAdd(&rs->scatter_ctas_done, 1u);
+        S.last = 0u;
         if (done == gridDim.x - 1) {
             __threadfence();
             rs->scatter_ctas_done = 0u;
             if (atomicAdd(&rs->error, 0u) != 0u) {   // a CTA failed: keep the old table
                 rs->dead_count = 0u;
-                return;
+            } else {
+                S.last = 1u;
             }
+        }
+    }
+    __syncthreads();
+    if (BATCH && S.last) {
+        // per run: next ID after this step's births; the next ring slot starts at zero
+        const uint32_t sl = (uint32_t)step % kBatchRing, sn = ((uint32_t)step + 1u) % kBatchRing;
+        for (int r = tid; r < BB.nruns; r += kTileThreads) {
+            BB.rnext[r] += (int64_t)BB.rstat[((size_t)r * kBatchRing + sl) * 4 + 1];
+            uint4 *z = reinterpret_cast<uint4 *>(BB.rstat + ((size_t)r * kBatchRing + sn) * 4);
+            *z = make_uint4(0u, 0u, 0u, 0u);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    if (tid == 0) {
+        if (S.last) {
             const uint32_t st = (uint32_t)rs->step;
             rs->stats[st % kStatsRing][0] = rs->new_n_agents;
             unsigned long long *nx = rs->stats[(st + 1u) % kStatsRing];
@@ -1249,6 +1391,44 @@ k_genomes(const StepConst P, RunState *__restrict__ rs, uint64_t *__restrict__ g
     }
 }
 
+// Batches: agents of runs admitted at this step, staged sorted by cell,
+// written after the cell's newborns (the cell scan counted them and left
+// their first row in ibase).  The last CTA clears the staging count.
+__global__ void __launch_bounds__(256)
+k_inject(RunState *__restrict__ rs, const BatchBuffers BB, int64_t *__restrict__ id2,
+         float *__restrict__ birth2, float *__restrict__ age2, float *__restrict__ lastb2,
+         uint8_t *__restrict__ meta2, uint32_t cap) {
+    __shared__ uint32_t s_last;
+    if (rs->error != 0u) return;
+    const uint32_t n = rs->n_staged;
+    if (n == 0u) return;
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const uint32_t d = BB.scell[q];
+        const uint32_t first = BB.istart[d];
+        const uint32_t dst = BB.ibase[d] + (q - first);
+        if (dst >= cap) {
+            set_error(rs, kErrCapacity, dst);
+            continue;
+        }
+        id2[dst] = BB.sid[q];
+        birth2[dst] = BB.sbirth[q];
+        age2[dst] = BB.sage[q];
+        lastb2[dst] = BB.slastb[q];
+        meta2[dst] = BB.smeta[q];
+        if (q == first) BB.inj[d] = 0u;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        s_last = (atomicAdd(BB.inj_ctas_done, 1u) == gridDim.x - 1) ? 1u : 0u;
+        if (s_last) {
+            *BB.inj_ctas_done = 0u;
+            rs->n_staged = 0u;
+            __threadfence();
+        }
+    }
+}
+
 // genomes of the table's rows in row order (download)
 __global__ void k_gather_genomes(const int32_t *__restrict__ gslot, const uint64_t *__restrict__ genome,
                                  uint32_t n, int words, uint32_t slots, uint64_t *__restrict__ out) {
@@ -1262,7 +1442,36 @@ __global__ void k_gather_genomes(const int32_t *__restrict__ gslot, const uint64
     }
 }
 
+// rows of one batch run in the current table: the cell of each row and the
+// agents per cell (either output may be null)
+__global__ void k_run_cells(const uint32_t *__restrict__ nonempty, const uint32_t *__restrict__ ne_start,
+                            uint32_t nne, uint32_t cell0, uint32_t cell1, uint32_t row0, uint32_t nrows,
+                            uint32_t *__restrict__ row_cell, uint32_t *__restrict__ counts) {
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nne; k += gridDim.x * blockDim.x) {
+        const uint32_t c = nonempty[k];
+        if (c < cell0 || c >= cell1) continue;
+        const uint32_t r0 = ne_start[k], r1 = ne_start[k + 1];
+        if (counts) counts[c - cell0] = r1 - r0;
+        if (row_cell) {
+            for (uint32_t r = r0; r < r1; r++) {
+                if (r >= row0 && r - row0 < nrows) row_cell[r - row0] = c;
+            }
+        }
+    }
+}
+
 }  // namespace qhg
+
+extern "C" int qhg_launch_run_cells(const uint32_t *nonempty, const uint32_t *ne_start, uint32_t n_nonempty,
+                                    uint32_t cell0, uint32_t cell1, uint32_t row0, uint32_t nrows,
+                                    uint32_t *row_cell, uint32_t *counts, cudaStream_t stream) {
+    const uint32_t blocks = std::min<uint32_t>((n_nonempty + 255) / 256, 4096u);
+    if (blocks > 0) {
+        qhg::k_run_cells<<<blocks, 256, 0, stream>>>(nonempty, ne_start, n_nonempty, cell0, cell1, row0, nrows,
+                                                     row_cell, counts);
+    }
+    return (int)cudaGetLastError();
+}
 
 extern "C" int qhg_launch_gather_genomes(const int32_t *gslot, const uint64_t *genome, uint32_t n, int words,
                                          uint32_t slots, uint64_t *out, cudaStream_t stream) {
@@ -1273,55 +1482,80 @@ extern "C" int qhg_launch_gather_genomes(const int32_t *gslot, const uint64_t *g
 }
 
 static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
-                           const qhg::LaunchShape &L, cudaStream_t stream, cudaEvent_t *ev) {
+                           const qhg::BatchBuffers *BBp, const qhg::LaunchShape &L, cudaStream_t stream,
+                           cudaEvent_t *ev) {
     using namespace qhg;
     const int ntiles = (P->num_cells + kScanTile - 1) / kScanTile;
+    const bool batch = BBp != nullptr;
+    BatchBuffers BB;
+    if (batch) BB = *BBp;
+    else memset(&BB, 0, sizeof(BB));
     if (ev) cudaEventRecord(ev[0], stream);
-#define QHG_LAUNCH_ACTIONS(PR)                                                                       \
-    k_actions<PR><<<L.actions_grid, kTileThreads, 0, stream>>>(                                                 \
-        *P, rs, B->nonempty, B->ne_start, B->tile_first, B->id, B->birth, B->age, B->lastb, B->meta,  \
+#define QHG_LAUNCH_ACTIONS(PR, BT)                                                                        \
+    k_actions<PR, BT><<<L.actions_grid, kTileThreads, 0, stream>>>(                                      \
+        *P, BB, rs, B->nonempty, B->ne_start, B->tile_first, B->id, B->birth, B->age, B->lastb, B->meta, \
         B->nbr, B->nnbr, B->vthr, B->wthr, B->wflag, B->outc, B->father, B->brank, B->clsc)
-    switch (P->program) {
-    case 1: QHG_LAUNCH_ACTIONS(1); break;
-    case 2: QHG_LAUNCH_ACTIONS(2); break;
-    case 3: QHG_LAUNCH_ACTIONS(3); break;
-    default: QHG_LAUNCH_ACTIONS(0); break;
+    if (batch) {
+        switch (P->program) {
+        case 1: QHG_LAUNCH_ACTIONS(1, true); break;
+        default: QHG_LAUNCH_ACTIONS(0, true); break;
+        }
+    } else {
+        switch (P->program) {
+        case 1: QHG_LAUNCH_ACTIONS(1, false); break;
+        case 2: QHG_LAUNCH_ACTIONS(2, false); break;
+        case 3: QHG_LAUNCH_ACTIONS(3, false); break;
+        default: QHG_LAUNCH_ACTIONS(0, false); break;
+        }
     }
 #undef QHG_LAUNCH_ACTIONS
     if (ev) cudaEventRecord(ev[1], stream);
-    k_cell_scan<<<ntiles, kScanThreads, 0, stream>>>(
-        *P, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr, B->sbase, B->bbase, B->bidbase, B->obase,
-        B->nonempty2, B->ne_start2, B->tile_first2, B->tile_flag, B->tile_agg, B->tile_incl);
+#define QHG_LAUNCH_SCAN(BT)                                                                                 \
+    k_cell_scan<BT><<<ntiles, kScanThreads, 0, stream>>>(                                                   \
+        *P, BB, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr, B->sbase, B->bbase, B->bidbase,       \
+        B->obase, B->nonempty2, B->ne_start2, B->tile_first2, B->tile_flag, B->tile_agg, B->tile_incl)
+    if (batch) QHG_LAUNCH_SCAN(true);
+    else QHG_LAUNCH_SCAN(false);
+#undef QHG_LAUNCH_SCAN
     if (ev) cudaEventRecord(ev[2], stream);
-    k_scatter<<<L.scatter_grid, kTileThreads, 0, stream>>>(
-        *P, rs, B->nonempty, B->ne_start, B->tile_first, B->id, B->birth, B->age, B->lastb, B->outc, B->father,
-        B->brank, B->nnbr, B->sbase, B->bbase, B->bidbase, B->obase, B->clsc, B->id2, B->birth2,
-        B->age2, B->lastb2, B->meta2, B->blog, B->blog_cap, B->gslot, B->gslot2, B->freelist,
-        B->freelist2, B->brec);
+#define QHG_LAUNCH_SCATTER(BT)                                                                              \
+    k_scatter<BT><<<L.scatter_grid, kTileThreads, 0, stream>>>(                                             \
+        *P, BB, rs, B->nonempty, B->ne_start, B->tile_first, B->id, B->birth, B->age, B->lastb, B->outc,   \
+        B->father, B->brank, B->nnbr, B->sbase, B->bbase, B->bidbase, B->obase, B->clsc, B->id2, B->birth2, \
+        B->age2, B->lastb2, B->meta2, B->blog, B->blog_cap, B->gslot, B->gslot2, B->freelist,              \
+        B->freelist2, B->brec)
+    if (batch) QHG_LAUNCH_SCATTER(true);
+    else QHG_LAUNCH_SCATTER(false);
+#undef QHG_LAUNCH_SCATTER
     if (ev) cudaEventRecord(ev[3], stream);
-    if (P->genome_words > 0) {
+    if (batch) {
+        k_inject<<<L.scatter_grid, 256, 0, stream>>>(rs, BB, B->id2, B->birth2, B->age2, B->lastb2, B->meta2,
+                                                     P->capacity);
+        if (ev) cudaEventRecord(ev[4], stream);
+    } else if (P->genome_words > 0) {
         k_genomes<<<L.scatter_grid, 256, 0, stream>>>(*P, rs, B->genome, B->brec);
         if (ev) cudaEventRecord(ev[4], stream);
     }
 }
 
 extern "C" int qhg_launch_step(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
-                               const qhg::LaunchShape *L, cudaStream_t stream) {
-    launch_kernels(P, rs, B, *L, stream, nullptr);
+                               const qhg::BatchBuffers *BB, const qhg::LaunchShape *L, cudaStream_t stream) {
+    launch_kernels(P, rs, B, BB, *L, stream, nullptr);
     return (int)cudaGetLastError();
 }
 
 extern "C" int qhg_launch_step_timed(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
-                                     const qhg::LaunchShape *L, cudaStream_t stream, cudaEvent_t *ev) {
-    launch_kernels(P, rs, B, *L, stream, ev);
+                                     const qhg::BatchBuffers *BB, const qhg::LaunchShape *L, cudaStream_t stream,
+                                     cudaEvent_t *ev) {
+    launch_kernels(P, rs, B, BB, *L, stream, ev);
     return (int)cudaGetLastError();
 }
 
 // CTAs of each tile kernel that fit on one SM at once
 extern "C" void qhg_tile_ctas_per_sm(int *actions, int *scatter) {
     int a = 0, b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, qhg::k_actions<0>, qhg::kTileThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, qhg::k_scatter, qhg::kTileThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, qhg::k_actions<0, false>, qhg::kTileThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, qhg::k_scatter<false>, qhg::kTileThreads, 0);
     *actions = a > 0 ? a : 1;
     *scatter = b > 0 ? b : 1;
 }

@@ -32,6 +32,10 @@ EXPORTS = [
     "qhg_gpu_current_step", "qhg_gpu_download", "qhg_gpu_counts", "qhg_gpu_stats",
     "qhg_gpu_birth_log", "qhg_gpu_stream", "qhg_gpu_destroy", "qhg_gpu_step_profiled",
     "qhg_gpu_step_timed", "qhg_gpu_cell_census_noalloc", "qhg_gpu_census_last_error",
+    "qhg_batch_last_error", "qhg_batch_create", "qhg_batch_add_run", "qhg_batch_remove_run",
+    "qhg_batch_step", "qhg_batch_step_timed", "qhg_batch_sync", "qhg_batch_num_agents",
+    "qhg_batch_run_info", "qhg_batch_stats", "qhg_batch_download", "qhg_batch_counts",
+    "qhg_batch_set_shape", "qhg_batch_get_shape", "qhg_batch_stream", "qhg_batch_destroy",
 ]
 
 
@@ -100,6 +104,22 @@ def load_library(path: str = LIB_PATH):
         "qhg_gpu_step_timed": (I, [P, ct.c_int32, P]),
         "qhg_gpu_cell_census_noalloc": (I, [P, ct.c_int64, ct.c_int32, P, P, P]),
         "qhg_gpu_census_last_error": (ct.c_char_p, []),
+        "qhg_batch_last_error": (ct.c_char_p, []),
+        "qhg_batch_create": (I, [P, P]),
+        "qhg_batch_add_run": (I, [P, P, P, P, P, ct.c_int32, P, ct.c_int64, P]),
+        "qhg_batch_remove_run": (I, [P, ct.c_int32]),
+        "qhg_batch_step": (I, [P, ct.c_int32]),
+        "qhg_batch_step_timed": (I, [P, ct.c_int32, P]),
+        "qhg_batch_sync": (I, [P]),
+        "qhg_batch_num_agents": (I, [P, P]),
+        "qhg_batch_run_info": (I, [P, ct.c_int32, P]),
+        "qhg_batch_stats": (I, [P, ct.c_int32, ct.c_int32, P]),
+        "qhg_batch_download": (I, [P, ct.c_int32, P, ct.c_int64, P]),
+        "qhg_batch_counts": (I, [P, ct.c_int32, P]),
+        "qhg_batch_set_shape": (I, [P, ct.c_int32, ct.c_int32]),
+        "qhg_batch_get_shape": (I, [P, P, P, P, P]),
+        "qhg_batch_stream": (I, [P, P]),
+        "qhg_batch_destroy": (I, [P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -1,0 +1,102 @@
+"""Batches (qhg_batch_*): every run of a batch must give, bit for bit, what
+the same run gives alone through the single-run path -- agent tables sorted
+by ID, per-cell counts and per-step statistics -- however the runs join and
+leave and whatever launch shape the batch uses.
+
+A run admitted between two batch steps enters the table during the next
+batch step and does its step 0 in the one after: after k batch steps it has
+done k - 1 steps."""
+import numpy as np
+import pytest
+
+from qhg4_gb300.batch import Autotuner, GpuBatch
+from qhg4_gb300.gpu import GpuRun
+from qhg4_gb300.spec import config1_actions, config2_actions
+from qhg4_gb300.workload import make_agents, terrain_grid, uniform_grid
+
+from helpers import table_diff
+
+pytestmark = pytest.mark.gpu
+
+
+def plain_case(k):
+    rng = np.random.default_rng(100 + k)
+    g = uniform_grid(int(rng.choice([6, 8, 10, 12])), 30.0)
+    n = int(rng.integers(2000, 12000))
+    acts = config1_actions(b0=float(rng.uniform(0.1, 0.6)), d0=float(rng.uniform(0.02, 0.08)),
+                           move_p=float(rng.uniform(0.05, 0.3)))
+    return g, make_agents(g, n, seed=200 + k, age_max=50.0), acts, 1000 + k
+
+
+def alone(grid, agents, acts, seed, steps):
+    r = GpuRun(grid, acts, seed)
+    r.load(agents)
+    r.step(steps)
+    return r
+
+
+def same_as_alone(batch, run, case, steps):
+    grid, agents, acts, seed = case
+    assert batch.steps_done(run) == steps
+    r = alone(grid, agents, acts, seed, steps)
+    d = table_diff(batch.agents(run), r.agents())
+    assert d is None, f"run {run}: {d}"
+    assert np.array_equal(batch.counts(run), r.counts())
+    k = min(steps, 64)
+    if k > 0:
+        assert np.array_equal(batch.stats(run, k), r.stats(k))
+    r.close()
+
+
+def test_batch_runs_equal_alone_with_joins_and_leaves(gpu_lib):
+    cases = [plain_case(k) for k in range(6)]
+    b = GpuBatch(config1_actions(), agent_capacity=400_000, cell_capacity=8_000, max_runs=4)
+    ids = {}
+    for k in range(3):
+        g, a, acts, seed = cases[k]
+        ids[k] = b.add_run(g, acts, seed, a)
+    b.step(7)
+    for k in (3,):
+        g, a, acts, seed = cases[k]
+        ids[k] = b.add_run(g, acts, seed, a)
+    b.step(5)
+    same_as_alone(b, ids[1], cases[1], 11)
+    b.remove_run(ids[1])
+    b.step(3)
+    # the freed slot and cells go to a new run
+    g, a, acts, seed = cases[4]
+    ids[4] = b.add_run(g, acts, seed, a)
+    b.step(20)
+    for k, steps in ((0, 34), (2, 34), (3, 27), (4, 19)):
+        same_as_alone(b, ids[k], cases[k], steps)
+
+
+def test_batch_shape_does_not_change_results(gpu_lib):
+    cases = [plain_case(k) for k in range(3)]
+    b = GpuBatch(config1_actions(), agent_capacity=200_000, cell_capacity=5_000, max_runs=3)
+    ids = [b.add_run(g, acts, seed, a) for g, a, acts, seed in cases]
+    b.step(2)
+    _, _, ma, ms = b.shape()
+    for k, (sa, ss) in enumerate(((1, 1), (ma, 1), (1, ms), (ma, ms))):
+        b.set_shape(sa, ss)
+        b.step(3)
+    tuner = Autotuner(trial_steps=1)
+    tuner.tune(b)
+    b.step(2)
+    for k, r in enumerate(ids):
+        same_as_alone(b, r, cases[k], b.steps_done(r))
+
+
+def test_batch_large_run_actions(gpu_lib):
+    """VerhulstVarK, OldAgeDeath and WeightedMove through the batch's
+    interpreted action program."""
+    cases = []
+    for k in range(3):
+        g = terrain_grid(8 + 2 * k, seed=30 + k)
+        a = make_agents(g, 15_000 + 5_000 * k, seed=300 + k, age_max=60.0, proportional_to_K=True)
+        cases.append((g, a, config2_actions(b0=0.4 + 0.05 * k, move_p=0.1 + 0.05 * k), 50 + k))
+    b = GpuBatch(config2_actions(), agent_capacity=400_000, cell_capacity=6_000, max_runs=3)
+    ids = [b.add_run(g, acts, seed, a) for g, a, acts, seed in cases]
+    b.step(25)
+    for k, r in enumerate(ids):
+        same_as_alone(b, r, cases[k], 24)
