@@ -303,6 +303,14 @@ def run_ours(args, world, rank, local, dist):
                "steps": job_steps, "detail": "qhg_gpu_upload_agents from host arrays + per-step "
                "qhg_gpu_step(1) and qhg_gpu_stats(1) + final qhg_gpu_download, wall clock"}
 
+    # the batched ensemble beside the single large run (256 runs, 500 steps each)
+    batched = None
+    if not args.skip_batched:
+        run.close()
+        batched = measure_ensemble(args.ensemble_runs, args.ensemble_steps, device, args.plain_runs,
+                                   seed=2024 + rank)
+        batched["workload"] = ("batched ensemble: runs with grid n in {32,64,128}, agents log-uniform "
+                               "[1e4,2e6], per-run b0, d0, p and seed (= run index); plain method's actions")
     cpu = None
     if rank == 0 and not args.skip_cpu:
         cs = max(1, args.cpu_steps)
@@ -320,9 +328,103 @@ def run_ours(args, world, rank, local, dist):
             "config": {"workload": args.workload, "detail": wl["desc"], "agents": N0, "cells": C,
                        "agents_at_timed_start": n_start, "parallelism": f"replicas x{world}",
                        "l2": "inputs larger than L2 (hot table ~21 B x agents > 129 MB)"},
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "batched": batched,
             "gpu_launches": 3 * args.steps * world,
         }
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def measure_ensemble(n_runs: int, steps: int, device: int, plain_runs: int, seed: int = 2024):
+    """Batched ensemble (many independent runs in one batch) against the
+    plain path running the same runs one at a time.  Both time only the
+    stepping on the device (CUDA events); admission/upload and graph
+    building are outside, the e2e figures include them."""
+    from qhg4_gb300.batch import Autotuner, GpuBatch
+    from qhg4_gb300.ensemble import ensemble_specs
+    from qhg4_gb300.gpu import GpuRun
+    t_gen = time.perf_counter()
+    specs = ensemble_specs(n_runs=n_runs, steps=steps, seed=seed)
+    t_gen = time.perf_counter() - t_gen
+    n0 = sum(len(s.agents) for s in specs)
+    cells = sum(s.grid.num_cells for s in specs)
+    # ---- batched
+    t_job = time.perf_counter()
+    # room for every run at twice its start or at 40 agents per cell (K = 30), whichever is larger
+    cap = sum(max(2 * len(s.agents), 40 * s.grid.num_cells) for s in specs) + 65536
+    b = GpuBatch(config1_actions(), agent_capacity=cap, cell_capacity=cells, max_runs=n_runs,
+                 stage_capacity=n0, device=device)
+    ids = [b.add_run(s.grid, s.actions, s.seed, s.agents) for s in specs]
+    b.step(1)   # the runs' agents enter the table
+    tuner = Autotuner(trial_steps=2, span=2)
+    shape = tuner.tune(b)
+    done = b.steps_done(ids[0])
+    left = steps - done
+    b.step(1)   # graph of the other table parity
+    left -= 1
+    ms_b, as_b = 0.0, 0
+    n_start = b.num_agents()
+    while left > 0:
+        k = min(left, 200)
+        ms_b += b.step_timed(k)
+        live = b.live_history(k)
+        as_b += n_start + int(live[:-1].sum())
+        n_start = int(live[-1])
+        left -= k
+    finals = [len(b.agents(r, sort_by_id=False)) for r in ids]
+    hist = b.live_history(steps + 1)
+    b.close()
+    t_job = time.perf_counter() - t_job
+    as_job = int(hist[:-1].sum())   # agents at the start of every step of every run
+    # ---- plain, one run at a time (the first plain_runs runs)
+    ms_p, as_p, wall_p, as_p_all = 0.0, 0, 0.0, 0
+    np_runs = min(plain_runs, n_runs)
+    for s in specs[:np_runs]:
+        t0 = time.perf_counter()
+        r = GpuRun(s.grid, s.actions, s.seed, capacity=max(2 * len(s.agents), 40 * s.grid.num_cells) + 65536,
+                   device=device)
+        r.load(s.agents)
+        r.step(2)   # both graphs built outside the timed steps
+        st0 = r.stats(2)
+        k = s.steps - 2
+        ms_p += r.step_timed(k)
+        st = r.stats(k)
+        as_p += int(st0[-1, 0]) + int(st[:-1, 0].sum())
+        as_p_all += len(s.agents) + int(st0[0, 0]) + int(st0[-1, 0]) + int(st[:-1, 0].sum())
+        r.agents(sort_by_id=False)
+        r.close()
+        wall_p += time.perf_counter() - t0
+    bat = as_b / (ms_b / 1000.0) if ms_b > 0 else 0.0
+    pla = as_p / (ms_p / 1000.0) if ms_p > 0 else 0.0
+    return {
+        "value": bat, "unit": "agent-steps/s", "plain_value": pla,
+        "speedup_vs_plain": bat / pla if pla > 0 else None,
+        "runs": n_runs, "steps_per_run": steps, "initial_agents": n0, "cells": cells,
+        "timed_steps": steps - done - 1, "batched_ms": ms_b, "plain_runs": np_runs, "plain_ms": ms_p,
+        "shape": {"actions_ctas_per_sm": shape[0], "scatter_ctas_per_sm": shape[1],
+                  "trials": [[list(c), t] for c, t in tuner.trials.get(Autotuner.bucket(n0), [])]},
+        "final_agents": int(sum(finals)),
+        "e2e": {"value": as_job / t_job, "unit": "agent-steps/s", "job_s": t_job,
+                "plain_value": as_p_all / wall_p if wall_p > 0 else None, "plain_job_s": wall_p,
+                "detail": "admission of every run from host arrays, all steps, download of every run's "
+                          "final table; plain: create, upload, all steps, download, one run after another"},
+        "generation_s": t_gen,
+    }
+
+
+def run_ensemble(args, world, rank, local, dist):
+    device = local if world > 1 else args.device
+    res = measure_ensemble(args.ensemble_runs, args.ensemble_steps, device, args.plain_runs, seed=args.seed + rank)
+    if rank == 0:
+        line = {"metric": METRIC, "value": res["value"], "unit": "agent-steps/s", "n_gpus": world,
+                "steps": res["timed_steps"], "warmup": res["steps_per_run"] - res["timed_steps"],
+                "ms_per_step": res["batched_ms"] / max(1, res["timed_steps"]), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "int32/f32/f64",
+                "data": "synthetic (seeded; shapes and distributions of the configuration)",
+                "config": {"workload": "ensemble", "detail": "batched ensemble: runs with grid n in {32,64,128}, "
+                           "agents log-uniform [1e4,2e6], per-run b0, d0, p and seed; plain method's actions",
+                           "parallelism": f"replicas x{world}"},
+                "batched": res}
         print(json.dumps(line), flush=True)
     return 0
 
@@ -333,7 +435,10 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="large")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["ensemble"], default="large")
+    ap.add_argument("--ensemble-runs", type=int, default=256)
+    ap.add_argument("--ensemble-steps", type=int, default=500)
+    ap.add_argument("--plain-runs", type=int, default=256)
     ap.add_argument("--seed", type=int, default=42)
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--profile-steps", type=int, default=3)
@@ -341,6 +446,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=0)
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-batched", action="store_true")
     args = ap.parse_args()
     if args.warmup < 0 or args.steps < 0:
         ap.error("steps and warmup must be >= 0")
@@ -348,6 +454,8 @@ def main():
     try:
         if args.impl == "reference":
             return run_reference(args, world, rank, dist)
+        if args.workload == "ensemble":
+            return run_ensemble(args, world, rank, local, dist)
         return run_ours(args, world, rank, local, dist)
     finally:
         if dist is not None:

@@ -214,6 +214,8 @@ int qhg_batch_num_agents(qhg_batch *batch, int64_t *n);
 int qhg_batch_run_info(qhg_batch *batch, int32_t run, qhg_batch_run_status *info);
 /* statistics of the run's last nsteps steps (nsteps <= 64) */
 int qhg_batch_stats(qhg_batch *batch, int32_t run, int32_t nsteps, qhg_step_stats *out);
+/* agents of all runs after each of the batch's last nsteps steps (<= 1024) */
+int qhg_batch_live_history(qhg_batch *batch, int32_t nsteps, uint64_t *live);
 /* the run's agents ordered by cell, cells relative to the run's grid */
 int qhg_batch_download(qhg_batch *batch, int32_t run, qhg_agents_soa *out, int64_t cap, int64_t *n);
 int qhg_batch_counts(qhg_batch *batch, int32_t run, uint32_t *cell_counts);

@@ -123,6 +123,12 @@ class GpuBatch:
         _bcheck(load_library().qhg_batch_num_agents(self.h, ct.byref(n)))
         return int(n.value)
 
+    def live_history(self, nsteps: int) -> np.ndarray:
+        """Agents of all runs after each of the batch's last nsteps (<= 1024) steps."""
+        out = np.zeros(max(1, nsteps), dtype=np.uint64)
+        _bcheck(load_library().qhg_batch_live_history(self.h, int(nsteps), _p(out)))
+        return out[:nsteps]
+
     def run_info(self, run: int) -> BatchRunStatus:
         st = BatchRunStatus()
         _bcheck(load_library().qhg_batch_run_info(self.h, int(run), ct.byref(st)))
@@ -188,6 +194,7 @@ class Autotuner:
     timing ``trial_steps`` real steps of the batch with every candidate."""
 
     trial_steps: int = 2
+    span: int = 3          # candidates: the top `span` CTAs-per-SM values of each kernel
     table: Dict[int, Tuple[int, int]] = field(default_factory=dict)
     trials: Dict[int, List[Tuple[Tuple[int, int], float]]] = field(default_factory=dict)
 
@@ -197,7 +204,8 @@ class Autotuner:
 
     def candidates(self, batch: GpuBatch) -> List[Tuple[int, int]]:
         _, _, ma, ms = batch.shape()
-        return [(a, s) for a in range(max(1, ma - 2), ma + 1) for s in range(max(1, ms - 2), ms + 1)]
+        return [(a, s) for a in range(max(1, ma - self.span + 1), ma + 1)
+                for s in range(max(1, ms - self.span + 1), ms + 1)]
 
     def tune(self, batch: GpuBatch) -> Tuple[int, int]:
         """Sets the batch's shape for its current size, measuring once per

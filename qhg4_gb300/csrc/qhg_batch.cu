@@ -623,6 +623,19 @@ extern "C" int qhg_batch_stats(qhg_batch *b, int32_t run, int32_t nsteps, qhg_st
     return QHG_OK;
 }
 
+extern "C" int qhg_batch_live_history(qhg_batch *b, int32_t nsteps, uint64_t *live) {
+    if (b == nullptr || live == nullptr || nsteps < 0 || nsteps > kStatsRing || nsteps > b->gstep) {
+        return bfail(QHG_ERR_ARG, "bad history arguments (at most 1024 steps, at most the steps done)");
+    }
+    int rc = qhg_batch_sync(b);
+    if (rc != QHG_OK) return rc;
+    for (int32_t k = 0; k < nsteps; k++) {
+        const uint32_t g = (uint32_t)(b->gstep - nsteps + k);
+        live[k] = b->h_rs->stats[g % kStatsRing][0];
+    }
+    return QHG_OK;
+}
+
 // rows of a run in the current table: its first row, agents, cell of each row
 static int run_rows(qhg_batch *b, int32_t run, uint32_t *row0, uint32_t *count) {
     const RunSlot &s = b->slots[(size_t)run];

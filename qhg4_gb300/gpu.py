@@ -36,6 +36,7 @@ EXPORTS = [
     "qhg_batch_step", "qhg_batch_step_timed", "qhg_batch_sync", "qhg_batch_num_agents",
     "qhg_batch_run_info", "qhg_batch_stats", "qhg_batch_download", "qhg_batch_counts",
     "qhg_batch_set_shape", "qhg_batch_get_shape", "qhg_batch_stream", "qhg_batch_destroy",
+    "qhg_batch_live_history",
 ]
 
 
@@ -120,6 +121,7 @@ def load_library(path: str = LIB_PATH):
         "qhg_batch_get_shape": (I, [P, P, P, P, P]),
         "qhg_batch_stream": (I, [P, P]),
         "qhg_batch_destroy": (I, [P]),
+        "qhg_batch_live_history": (I, [P, ct.c_int32, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
