@@ -311,6 +311,11 @@ def run_ours(args, world, rank, local, dist):
                                    seed=2024 + rank)
         batched["workload"] = ("batched ensemble: runs with grid n in {32,64,128}, agents log-uniform "
                                "[1e4,2e6], per-run b0, d0, p and seed (= run index); plain method's actions")
+    served = None
+    if not args.skip_served:
+        served = measure_served(args.served_jobs, args.served_rate, device, args.hbm_budget_gb * 1e9, seed=7 + rank)
+        served["workload"] = ("served stream: Poisson arrivals; grid n in {32,64,128,256}, agents log-uniform "
+                              "[1e4,1e7], steps U[50,1000]; HBM-footprint admission; snapshots every 100 steps")
     cpu = None
     if rank == 0 and not args.skip_cpu:
         cs = max(1, args.cpu_steps)
@@ -329,6 +334,7 @@ def run_ours(args, world, rank, local, dist):
                        "agents_at_timed_start": n_start, "parallelism": f"replicas x{world}",
                        "l2": "inputs larger than L2 (hot table ~21 B x agents > 129 MB)"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "batched": batched,
+            "served": served,
             "gpu_launches": 3 * args.steps * world,
         }
         print(json.dumps(line), flush=True)
@@ -412,6 +418,56 @@ def measure_ensemble(n_runs: int, steps: int, device: int, plain_runs: int, seed
     }
 
 
+def measure_served(n_jobs: int, rate: float, device: int, budget: float, seed: int = 7):
+    """Served stream: Poisson arrivals, admission under the HBM budget,
+    continuous batching, snapshots every 100 steps written by a thread.
+    Latency = completion - arrival (wall clock); value = agent-steps of all
+    jobs / wall time from the first arrival to the last completion."""
+    import tempfile
+    from qhg4_gb300.serve import Server, job_stream, summarize
+    t_gen = time.perf_counter()
+    jobs = job_stream(n_jobs, rate=rate, seed=seed)
+    t_gen = time.perf_counter() - t_gen
+    need_rows = sum(j.rows for j in jobs)
+    need_cells = sum(j.grid.num_cells for j in jobs)
+    with tempfile.TemporaryDirectory() as snapdir:
+        # the batch is sized for the budget, or for the whole stream when that is smaller
+        from qhg4_gb300.serve import BYTES_PER_AGENT, BYTES_PER_CELL
+        rows = min(need_rows, int(budget * 0.9 / BYTES_PER_AGENT), 2**31 - 1)
+        cells = min(need_cells, int(budget * 0.1 / BYTES_PER_CELL))
+        srv = Server(hbm_budget=budget, agent_capacity=rows, cell_capacity=cells, max_runs=256,
+                     snapshot_every=100, snapshot_dir=snapdir, chunk=16, device=device)
+        t0 = time.perf_counter()
+        done = srv.serve(jobs)
+        wall = time.perf_counter() - t0
+        n_snap = sum(len(j.snapshots) for j in done)
+        busy = srv.busy_s
+        srv.close()
+    first = min(j.arrival for j in jobs)
+    res = summarize(done, wall - first)
+    res.update({"rate_jobs_per_s": rate, "hbm_budget_gb": budget / 1e9, "batch_rows": rows, "batch_cells": cells,
+                "snapshots": n_snap, "gpu_loop_s": busy, "generation_s": t_gen,
+                "initial_agents": int(sum(len(j.agents) for j in jobs)),
+                "max_wait_s": float(max(j.admitted - j.arrival for j in done))})
+    return res
+
+
+def run_served(args, world, rank, local, dist):
+    device = local if world > 1 else args.device
+    res = measure_served(args.served_jobs, args.served_rate, device, args.hbm_budget_gb * 1e9, seed=7 + rank)
+    if rank == 0:
+        line = {"metric": METRIC, "value": res["value"], "unit": "agent-steps/s", "n_gpus": world,
+                "steps": None, "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "int32/f32/f64",
+                "data": "synthetic (seeded; shapes and distributions of the configuration)",
+                "config": {"workload": "served", "detail": "Poisson arrivals; grid n in {32,64,128,256}, agents "
+                           "log-uniform [1e4,1e7], steps U[50,1000]; plain method's actions with per-job "
+                           "b0, d0, p", "parallelism": f"replicas x{world}"},
+                "served": res}
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_ensemble(args, world, rank, local, dist):
     device = local if world > 1 else args.device
     res = measure_ensemble(args.ensemble_runs, args.ensemble_steps, device, args.plain_runs, seed=args.seed + rank)
@@ -435,7 +491,10 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["ensemble"], default="large")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["ensemble", "served"], default="large")
+    ap.add_argument("--served-jobs", type=int, default=100)
+    ap.add_argument("--served-rate", type=float, default=20.0)
+    ap.add_argument("--hbm-budget-gb", type=float, default=150.0)
     ap.add_argument("--ensemble-runs", type=int, default=256)
     ap.add_argument("--ensemble-steps", type=int, default=500)
     ap.add_argument("--plain-runs", type=int, default=256)
@@ -447,6 +506,7 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-batched", action="store_true")
+    ap.add_argument("--skip-served", action="store_true")
     args = ap.parse_args()
     if args.warmup < 0 or args.steps < 0:
         ap.error("steps and warmup must be >= 0")
@@ -456,6 +516,8 @@ def main():
             return run_reference(args, world, rank, dist)
         if args.workload == "ensemble":
             return run_ensemble(args, world, rank, local, dist)
+        if args.workload == "served":
+            return run_served(args, world, rank, local, dist)
         return run_ours(args, world, rank, local, dist)
     finally:
         if dist is not None:

@@ -66,7 +66,7 @@ extern "C" {
 #define QHG_ACT_WEIGHTEDMOVE  7  /* WeightedMove  actions/WeightedMove.cpp:45-106 */
 
 #define QHG_MAX_ACTIONS       16
-#define QHG_MAX_CELL_AGENTS   512    /* agents one cell may hold */
+#define QHG_MAX_CELL_AGENTS   4608   /* agents one cell may hold */
 #define QHG_CROSSOVER_POISSON1 (-100) /* Poisson(1) breakpoints per parent */
 
 /* life states stored in the agent table (core/SPopulation.h:69-73) */
@@ -219,6 +219,21 @@ int qhg_batch_live_history(qhg_batch *batch, int32_t nsteps, uint64_t *live);
 /* the run's agents ordered by cell, cells relative to the run's grid */
 int qhg_batch_download(qhg_batch *batch, int32_t run, qhg_agents_soa *out, int64_t cap, int64_t *n);
 int qhg_batch_counts(qhg_batch *batch, int32_t run, uint32_t *cell_counts);
+/* Starts copying the run's current table into the caller's buffers on a
+ * copy stream and returns without waiting for the copy (the buffers should
+ * be page-locked for that); *n receives the rows, *run_step the run's steps
+ * done.  The next batch step overlaps the copy; the one after waits for it.
+ * Unlike qhg_batch_download, `cell` receives cells of the batch's cell space
+ * (uint32, subtract the run's cell0) and `state` the raw meta byte (bit 0
+ * gender, bit 1 FERTILE); `gender` is not written.  Call
+ * qhg_batch_snapshot_wait before reading the buffers. */
+int qhg_batch_snapshot_async(qhg_batch *batch, int32_t run, qhg_agents_soa *out, int64_t cap, int64_t *n,
+                             int32_t *run_step);
+int qhg_batch_snapshot_wait(qhg_batch *batch);
+/* page-locked host memory for qhg_batch_snapshot_async (errors through
+ * qhg_batch_last_error) */
+int qhg_host_buffer_alloc(int64_t bytes, void **out);
+int qhg_host_buffer_free(void *p);
 /* launch shape of the persistent kernels (CTAs per SM); results do not
  * depend on it */
 int qhg_batch_set_shape(qhg_batch *batch, int32_t actions_ctas_per_sm, int32_t scatter_ctas_per_sm);

@@ -92,7 +92,7 @@ struct qhg_run {
     int cur = 0;                 // table holding the current step
     int32_t upload_step = 0;
     bool grid_ok = false, agents_ok = false;
-    LaunchShape shape = {1, 1};
+    LaunchShape shape = {1, 1, 1};
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     std::vector<int64_t> stage;  // host staging for uploads
@@ -446,6 +446,7 @@ extern "C" int qhg_gpu_create(const qhg_run_desc *desc, qhg_run **out) {
     qhg_tile_ctas_per_sm(&ca, &cs);
     r->shape.actions_grid = std::max(1, nsm) * ca;
     r->shape.scatter_grid = std::max(1, nsm) * cs;
+    r->shape.big_grid = std::max(1, nsm);
     *out = r;
     return QHG_OK;
 }
@@ -562,6 +563,7 @@ extern "C" int qhg_gpu_upload_agents(qhg_run *r, const qhg_agents_soa *a, int64_
     std::vector<uint32_t> cnt((size_t)C + 1, 0);
     int64_t live = 0;
     int64_t maxid = -1;
+    uint32_t max_cell = 0;
     for (int64_t i = 0; i < n; i++) {
         if (a->state[i] == 0) continue;
         const int32_t c = a->cell[i];
@@ -571,9 +573,10 @@ extern "C" int qhg_gpu_upload_agents(qhg_run *r, const qhg_agents_soa *a, int64_
         maxid = std::max<int64_t>(maxid, a->id[i]);
     }
     for (int c = 0; c < C; c++) {
-        if (cnt[(size_t)c + 1] > (uint32_t)kMaxCell) {
+        if (cnt[(size_t)c + 1] > (uint32_t)kMaxCellBig) {
             return fail(QHG_ERR_CELL_TOO_LARGE, "a cell holds more than QHG_MAX_CELL_AGENTS agents");
         }
+        max_cell = std::max(max_cell, cnt[(size_t)c + 1]);
         cnt[(size_t)c + 1] += cnt[(size_t)c];
     }
     uint64_t want = r->desc.agent_capacity > 0 ? (uint64_t)r->desc.agent_capacity : (uint64_t)live * 4 + 65536;
@@ -665,6 +668,8 @@ extern "C" int qhg_gpu_upload_agents(qhg_run *r, const qhg_agents_soa *a, int64_
     r->h_rs->next_id = maxid + 1;
     r->h_rs->n_nonempty = (uint32_t)ne.size();
     r->h_rs->hwm = (uint32_t)live;
+    r->h_rs->big = max_cell > (uint32_t)kMaxCell ? 1u : 0u;
+    r->h_rs->big_next = r->h_rs->big;
     CUDA_TRY(cudaMemcpyAsync(r->d_rs, r->h_rs, sizeof(RunState), cudaMemcpyHostToDevice, r->stream));
     const int ntiles = (C + kScanTile - 1) / kScanTile;
     CUDA_TRY(cudaMemsetAsync(r->d_tflag, 0, (size_t)ntiles * sizeof(uint32_t), r->stream));
@@ -781,6 +786,7 @@ static int pull_state(qhg_run *r) {
         r->h_rs->action_tiles = 0u;
         r->h_rs->scatter_tiles = 0u;
         r->h_rs->dead_count = 0u;
+        r->h_rs->max_cell = 0u;
         // the failed step's partial statistics would be counted again on retry
         unsigned long long *st = r->h_rs->stats[(uint32_t)r->h_rs->step % kStatsRing];
         st[0] = st[1] = st[2] = st[3] = 0ull;
@@ -792,7 +798,7 @@ static int pull_state(qhg_run *r) {
         char buf[160];
         switch (code) {
         case kErrCellTooLarge:
-            snprintf(buf, sizeof(buf), "cell %u would hold more than %d agents (step %d kept)", info, kMaxCell, r->h_rs->step);
+            snprintf(buf, sizeof(buf), "cell %u would hold more than %d agents (step %d kept)", info, kMaxCellBig, r->h_rs->step);
             return fail(QHG_ERR_CELL_TOO_LARGE, buf);
         case kErrCapacity:
             snprintf(buf, sizeof(buf), "%u agents exceed the capacity %u (step %d kept)", info, r->cap, r->h_rs->step);

@@ -62,7 +62,7 @@ struct qhg_batch {
     qhg_batch_desc desc;
     cudaStream_t stream = nullptr;
     StepConst P;
-    LaunchShape shape = {1, 1};
+    LaunchShape shape = {1, 1, 1};
     int nsm = 1, max_ctas_actions = 1, max_ctas_scatter = 1;
     uint32_t cell_cap = 0, agent_cap = 0, stage_cap = 0;
     int max_runs = 0;
@@ -98,13 +98,19 @@ struct qhg_batch {
     uint32_t *d_rstat = nullptr;
     // admission
     uint32_t *d_inj = nullptr, *d_istart = nullptr, *d_ibase = nullptr, *d_injdone = nullptr;
+    uint32_t *d_cstat = nullptr;
     int64_t *d_sid = nullptr;
     float *d_sbirth = nullptr, *d_sage = nullptr, *d_slastb = nullptr;
     uint8_t *d_smeta = nullptr;
     uint32_t *d_scell = nullptr;
     uint32_t staged = 0;            // rows staged for the next step
-    // download scratch
+    // snapshots: cells of the copied rows, a copy stream, and the event that the
+    // step after next (which overwrites the copied table) waits for
     uint32_t *d_rowcell = nullptr;
+    uint32_t rowcell_cap = 0;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t copy_done = nullptr;
+    int32_t copy_table_step = -1;   // batch step after which the copied table is overwritten
     RunState *d_rs = nullptr;
     RunState *h_rs = nullptr;
     std::vector<RunSlot> slots;
@@ -155,6 +161,7 @@ BatchBuffers make_batch_buffers(qhg_batch *b) {
     BB.sid = b->d_sid; BB.sbirth = b->d_sbirth; BB.sage = b->d_sage; BB.slastb = b->d_slastb;
     BB.smeta = b->d_smeta; BB.scell = b->d_scell;
     BB.inj_ctas_done = b->d_injdone;
+    BB.cstat = b->d_cstat;
     return BB;
 }
 
@@ -296,6 +303,7 @@ extern "C" int qhg_batch_create(const qhg_batch_desc *desc, qhg_batch **out) {
     A((void **)&b->d_istart, C * sizeof(uint32_t));
     A((void **)&b->d_ibase, C * sizeof(uint32_t));
     A((void **)&b->d_injdone, sizeof(uint32_t));
+    A((void **)&b->d_cstat, C * sizeof(uint32_t));
     A((void **)&b->d_sid, S * sizeof(int64_t));
     A((void **)&b->d_sbirth, S * sizeof(float));
     A((void **)&b->d_sage, S * sizeof(float));
@@ -307,6 +315,7 @@ extern "C" int qhg_batch_create(const qhg_batch_desc *desc, qhg_batch **out) {
     if (e == cudaSuccess) e = cudaMemsetAsync(b->d_clsc, 0, C * kCls * sizeof(uint32_t), b->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->d_crun, 0xff, C * sizeof(uint32_t), b->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->d_inj, 0, C * sizeof(uint32_t), b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_cstat, 0, C * sizeof(uint32_t), b->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->d_nnbr, 0, C, b->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->d_tflag, 0, nscan * sizeof(uint32_t), b->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->d_injdone, 0, sizeof(uint32_t), b->stream);
@@ -331,6 +340,7 @@ extern "C" int qhg_batch_create(const qhg_batch_desc *desc, qhg_batch **out) {
     qhg_tile_ctas_per_sm(&b->max_ctas_actions, &b->max_ctas_scatter);
     b->shape.actions_grid = b->nsm * b->max_ctas_actions;
     b->shape.scatter_grid = b->nsm * b->max_ctas_scatter;
+    b->shape.big_grid = b->nsm;
     refresh_cells(b);
     *out = b;
     return QHG_OK;
@@ -392,7 +402,7 @@ extern "C" int qhg_batch_add_run(qhg_batch *b, const qhg_batch_run_desc *rd, con
         maxid = std::max<int64_t>(maxid, a->id[i]);
     }
     for (uint32_t c = 0; c < C; c++) {
-        if (cnt[(size_t)c + 1] > (uint32_t)kMaxCell) {
+        if (cnt[(size_t)c + 1] > (uint32_t)kMaxCellBig) {
             return bfail(QHG_ERR_CELL_TOO_LARGE, "a cell holds more than QHG_MAX_CELL_AGENTS agents");
         }
         cnt[(size_t)c + 1] += cnt[c];
@@ -526,6 +536,11 @@ extern "C" int qhg_batch_step(qhg_batch *b, int32_t nsteps) {
         if (b->graph[b->cur] == nullptr) {
             int rc = build_graph(b, b->cur);
             if (rc != QHG_OK) return rc;
+        }
+        if (b->copy_table_step >= 0 && b->gstep >= b->copy_table_step) {
+            // this step writes the table a snapshot is still copying from
+            BCUDA(cudaStreamWaitEvent(b->stream, b->copy_done, 0));
+            b->copy_table_step = -1;
         }
         BCUDA(cudaGraphLaunch(b->graph[b->cur], b->stream));
         b->cur ^= 1;
@@ -693,6 +708,73 @@ extern "C" int qhg_batch_download(qhg_batch *b, int32_t run, qhg_agents_soa *o, 
     return QHG_OK;
 }
 
+extern "C" int qhg_batch_snapshot_async(qhg_batch *b, int32_t run, qhg_agents_soa *o, int64_t cap, int64_t *n,
+                                        int32_t *run_step) {
+    if (b == nullptr || o == nullptr || n == nullptr) return bfail(QHG_ERR_ARG, "null argument");
+    int rc = check_slot(b, run);
+    if (rc != QHG_OK) return rc;
+    // the table of the last launched step is complete once the stream is idle
+    rc = qhg_batch_sync(b);
+    if (rc != QHG_OK) return rc;
+    uint32_t row0 = 0, cnt = 0;
+    rc = run_rows(b, run, &row0, &cnt);
+    if (rc != QHG_OK) return rc;
+    *n = cnt;
+    const RunSlot &s = b->slots[(size_t)run];
+    if (run_step) *run_step = b->gstep - s.step0;
+    if (cap < (int64_t)cnt) return bfail(QHG_ERR_ARG, "output arrays too small");
+    if (b->copy_stream == nullptr) {
+        BCUDA(cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking));
+        BCUDA(cudaEventCreateWithFlags(&b->copy_done, cudaEventDisableTiming));
+    }
+    // earlier snapshot copies still use the cell buffer
+    BCUDA(cudaStreamSynchronize(b->copy_stream));
+    if (cnt > b->rowcell_cap) {
+        cudaFree(b->d_rowcell);
+        b->d_rowcell = nullptr;
+        b->rowcell_cap = 0;
+        BCUDA(cudaMalloc(&b->d_rowcell, (size_t)cnt * sizeof(uint32_t)));
+        b->rowcell_cap = cnt;
+    }
+    if (cnt == 0) return QHG_OK;
+    const int cur = b->cur;
+    cudaStream_t cs = b->copy_stream;
+    int le = qhg_launch_run_cells(b->d_ne[cur], b->d_nes[cur], b->h_rs->n_nonempty, s.cell0, s.cell1, row0, cnt,
+                                  b->d_rowcell, nullptr, cs);
+    if (le != 0) return bfail(QHG_ERR_CUDA, std::string("snapshot cells: ") + cudaGetErrorString((cudaError_t)le));
+    // cells as uint32 in the batch's cell space and the meta byte; the caller
+    // converts them (cell - cell0, gender = meta & 1, state from meta & 2)
+    BCUDA(cudaMemcpyAsync(o->cell, b->d_rowcell, cnt * sizeof(uint32_t), cudaMemcpyDeviceToHost, cs));
+    BCUDA(cudaMemcpyAsync(o->id, b->d_id[cur] + row0, cnt * sizeof(int64_t), cudaMemcpyDeviceToHost, cs));
+    BCUDA(cudaMemcpyAsync(o->birth, b->d_birth[cur] + row0, cnt * sizeof(float), cudaMemcpyDeviceToHost, cs));
+    BCUDA(cudaMemcpyAsync(o->age, b->d_age[cur] + row0, cnt * sizeof(float), cudaMemcpyDeviceToHost, cs));
+    BCUDA(cudaMemcpyAsync(o->last_birth, b->d_lastb[cur] + row0, cnt * sizeof(float), cudaMemcpyDeviceToHost, cs));
+    BCUDA(cudaMemcpyAsync(o->state, b->d_meta[cur] + row0, cnt, cudaMemcpyDeviceToHost, cs));
+    BCUDA(cudaEventRecord(b->copy_done, cs));
+    // the next step reads this table, the one after it rewrites it
+    b->copy_table_step = b->gstep + 1;
+    return QHG_OK;
+}
+
+extern "C" int qhg_host_buffer_alloc(int64_t bytes, void **out) {
+    if (out == nullptr || bytes < 0) return bfail(QHG_ERR_ARG, "bad buffer arguments");
+    *out = nullptr;
+    if (bytes == 0) return QHG_OK;
+    BCUDA(cudaHostAlloc(out, (size_t)bytes, cudaHostAllocPortable));
+    return QHG_OK;
+}
+
+extern "C" int qhg_host_buffer_free(void *p) {
+    if (p) BCUDA(cudaFreeHost(p));
+    return QHG_OK;
+}
+
+extern "C" int qhg_batch_snapshot_wait(qhg_batch *b) {
+    if (b == nullptr) return bfail(QHG_ERR_ARG, "null batch");
+    if (b->copy_stream) BCUDA(cudaStreamSynchronize(b->copy_stream));
+    return QHG_OK;
+}
+
 extern "C" int qhg_batch_counts(qhg_batch *b, int32_t run, uint32_t *counts) {
     if (b == nullptr || counts == nullptr) return bfail(QHG_ERR_ARG, "null argument");
     int rc = check_slot(b, run);
@@ -728,11 +810,12 @@ extern "C" int qhg_batch_destroy(qhg_batch *b) {
     if (b == nullptr) return QHG_OK;
     cudaSetDevice(b->desc.device);
     if (b->stream) cudaStreamSynchronize(b->stream);
+    if (b->copy_stream) cudaStreamSynchronize(b->copy_stream);
     drop_graphs(b);
     void *ptrs[] = {b->d_nbr, b->d_nnbr, b->d_rev, b->d_K, b->d_vthr, b->d_wthr, b->d_wflag, b->d_crun,
                     b->d_outc, b->d_father, b->d_brank, b->d_clsc, b->d_sbase, b->d_bbase, b->d_bidb,
                     b->d_obase, b->d_tflag, b->d_tagg, b->d_tincl, b->d_runs, b->d_rnext, b->d_rstat,
-                    b->d_inj, b->d_istart, b->d_ibase, b->d_injdone, b->d_sid, b->d_sbirth, b->d_sage,
+                    b->d_inj, b->d_istart, b->d_ibase, b->d_injdone, b->d_cstat, b->d_sid, b->d_sbirth, b->d_sage,
                     b->d_slastb, b->d_smeta, b->d_scell, b->d_rowcell, b->d_rs};
     for (void *p : ptrs) cudaFree(p);
     for (int p = 0; p < 2; p++) {
@@ -743,6 +826,8 @@ extern "C" int qhg_batch_destroy(qhg_batch *b) {
     for (int i = 0; i < 5; i++) {
         if (b->ev[i]) cudaEventDestroy(b->ev[i]);
     }
+    if (b->copy_done) cudaEventDestroy(b->copy_done);
+    if (b->copy_stream) cudaStreamDestroy(b->copy_stream);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
     return QHG_OK;

@@ -11,13 +11,22 @@ namespace qhg {
 // ---------------------------------------------------------------- layout
 constexpr int kMaxActions = 16;
 constexpr int kMaxVerhulst = 1;          // Verhulst / VerhulstVarK actions per population
-constexpr int kMaxCell = 512;            // agents one cell may hold
+constexpr int kMaxCell = 512;            // agents per cell of the normal tile kernels
+constexpr int kMaxCellBig = 4608;        // agents one cell may hold (big-cell tile kernels)
 // agent kernels work on cell-aligned tiles: tile t holds the non-empty cells
 // whose first row lies in [t*kTileAgents, (t+1)*kTileAgents)
 constexpr int kTileAgents = 512;
 constexpr int kTileMax = kTileAgents + kMaxCell;  // rows a tile can hold
 constexpr int kTileCells = kTileAgents;           // cells a tile can hold
 constexpr int kTileThreads = 256;
+// geometry of the tile kernels: the normal form (256 threads, cells of up to
+// kMaxCell agents) and the big-cell form used for steps in which some cell
+// holds more (1024 threads, one CTA per SM)
+template <bool BIG>
+struct Tile {
+    static constexpr int kThreads = BIG ? 1024 : kTileThreads;
+    static constexpr int kMax = BIG ? kTileAgents + kMaxCellBig : kTileMax;
+};
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 2;            // cells per thread in the cell scan
 constexpr int kScanTile = kScanThreads * kScanItems;
@@ -129,6 +138,9 @@ struct RunState {
     uint32_t dead_count;     // deaths of this step pushed to the next free list
     int32_t genome_step;     // step whose newborns k_genomes builds
     uint32_t n_staged;       // batches: agents waiting to be placed by k_inject
+    uint32_t big;            // 1: some cell holds more than kMaxCell agents (big-cell kernels run)
+    uint32_t big_next;       // the same for the table the step writes (set by its commit)
+    uint32_t max_cell;       // largest cell of the next table (cell scan)
     // statistics ring: [step % kStatsRing][live, births, deaths, moves]
     unsigned long long stats[kStatsRing][4];
 };
@@ -191,6 +203,7 @@ struct BatchBuffers {
     const int64_t *sid; const float *sbirth; const float *sage; const float *slastb;
     const uint8_t *smeta; const uint32_t *scell;
     uint32_t *inj_ctas_done;
+    uint32_t *cstat;            // per cell: deaths | registered moves << 16 of the step
 };
 
 // grid sizes of the persistent tile kernels (CTAs); results do not depend
@@ -198,6 +211,7 @@ struct BatchBuffers {
 struct LaunchShape {
     int actions_grid;
     int scatter_grid;
+    int big_grid;      // CTAs of the big-cell forms (one per SM)
 };
 
 // ------------------------------------------------------------- Philox

@@ -150,19 +150,20 @@ __host__ __device__ constexpr int prog_act(int p, int a) {
 }
 constexpr int kNumPrograms = 4;
 
-struct ActionsSmem {
-    int64_t fid[kTileMax];         // IDs of the unsorted FERTILE lists (same positions as pick)
-    uint8_t meta[kTileMax];
-    uint8_t head[kTileMax];        // first row of a cell
-    uint8_t bfl[kTileMax];         // gives birth this step
-    uint16_t cell[kTileMax];       // local cell index of each row
-    int16_t mate[kTileMax];        // mate's row within the tile, -1 none
-    uint16_t frank[kTileMax];      // rank of a FERTILE agent among its cell's FERTILE agents of its sex (by ID)
-    uint16_t list[kTileMax];       // at each cell's rows: FERTILE females by ID, then FERTILE males by ID
-    uint16_t pick[kTileMax];       // at each cell's rows: unsorted FERTILE lists, later the pick values
-    alignas(4) uint16_t pkrow[kTileMax];  // rows of the tile's pairing members that draw (dense)
-    uint16_t oadq[kTileMax];       // rows whose OldAgeDeath needs its draw (dense)
-    uint8_t oc[kTileMax];          // outcome byte before the deferred OldAgeDeath draws
+template <int TM, int TT>
+struct ActionsSmemT {
+    int64_t fid[TM];         // IDs of the unsorted FERTILE lists (same positions as pick)
+    uint8_t meta[TM];
+    uint8_t head[TM];        // first row of a cell
+    uint8_t bfl[TM];         // gives birth this step
+    uint16_t cell[TM];       // local cell index of each row
+    int16_t mate[TM];        // mate's row within the tile, -1 none
+    uint16_t frank[TM];      // rank of a FERTILE agent among its cell's FERTILE agents of its sex (by ID)
+    uint16_t list[TM];       // at each cell's rows: FERTILE females by ID, then FERTILE males by ID
+    uint16_t pick[TM];       // at each cell's rows: unsorted FERTILE lists, later the pick values
+    alignas(4) uint16_t pkrow[TM];  // rows of the tile's pairing members that draw (dense)
+    uint16_t oadq[TM];       // rows whose OldAgeDeath needs its draw (dense)
+    uint8_t oc[TM];          // outcome byte before the deferred OldAgeDeath draws
     uint32_t cstart[kTileCells + 1];  // first row of each cell, relative to the tile
     int32_t cid[kTileCells];
     uint32_t crun[kTileCells];     // batches: run of each cell
@@ -172,7 +173,7 @@ struct ActionsSmem {
     uint64_t td[kTileCells];       // LinearDeath threshold
     uint8_t tk[kTileCells];
     uint32_t cls[kTileCells][4];
-    uint32_t red[kTileThreads / 32];
+    uint32_t red[TT / 32];
     uint32_t npick, noad;
 };
 
@@ -181,8 +182,8 @@ struct ActionsSmem {
 // after the other actions, so that warps do not run Philox for a few lanes
 __host__ __device__ constexpr bool prog_defers_oad(int p) { return p == 2; }
 
-template <int PROG, bool BATCH>
-__global__ void __launch_bounds__(kTileThreads, 4)
+template <int PROG, bool BATCH, bool BIG>
+__global__ void __launch_bounds__(Tile<BIG>::kThreads, BIG ? 1 : 4)
 k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
           const uint32_t *__restrict__ nonempty, const uint32_t *__restrict__ ne_start,
           const uint32_t *__restrict__ tile_first,
@@ -194,8 +195,12 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
           const uint8_t *__restrict__ wflag,
           uint8_t *__restrict__ outc, int32_t *__restrict__ father, uint16_t *__restrict__ brank,
           uint32_t *__restrict__ clsc) {
-    __shared__ ActionsSmem S;
+    constexpr int TT = Tile<BIG>::kThreads;
+    constexpr int TM = Tile<BIG>::kMax;
+    extern __shared__ __align__(16) unsigned char qhg_smem[];
+    ActionsSmemT<TM, TT> &S = *reinterpret_cast<ActionsSmemT<TM, TT> *>(qhg_smem);
     if (rs->error != 0u) return;   // an earlier kernel failed: keep the state
+    if (rs->big != (BIG ? 1u : 0u)) return;   // the other form runs this step
     const int tid = threadIdx.x;
     const int32_t step = rs->step;
     const float fT = (float)step;
@@ -206,7 +211,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
     // tiles are dealt out statically; the next tile's bounds and the current
     // tile's agent fields are loaded early so that their latency overlaps the
     // cell set-up and the pairing phases
-    constexpr int RA = kTileMax / kTileThreads;
+    constexpr int RA = TM / TT;
     uint32_t nr0 = 0, nr1 = 0;
     if (blockIdx.x < ntiles) {
         nr0 = tile_first[blockIdx.x];
@@ -223,7 +228,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
         if (nc == 0) continue;
         const uint32_t a0 = ne_start[r0];
         const int na = (int)(ne_start[r0 + nc] - a0);
-        if (na > kTileMax || nc > kTileCells) {
+        if (na > TM || nc > kTileCells) {
             if (tid == 0) set_error(rs, kErrCellTooLarge, r0);
             continue;
         }
@@ -232,7 +237,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
         float pb[RA], pa[RA], pl[RA];
 #pragma unroll
         for (int j = 0; j < RA; j++) {
-            const int i = tid + j * kTileThreads;
+            const int i = tid + j * TT;
             if (i < na) {
                 pid[j] = id[a0 + i];
                 pm[j] = meta[a0 + i];
@@ -244,7 +249,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
         __syncthreads();   // the previous tile is done with the shared arrays
         // ---- cells: ids, rows, Verhulst thresholds (LinearBirth / LinearDeath
         // ::initialize, actions/LinearBirth.cpp:90-112, actions/LinearDeath.cpp:92-122)
-        for (int lc = tid; lc < nc; lc += kTileThreads) {
+        for (int lc = tid; lc < nc; lc += TT) {
             const int c = (int)nonempty[r0 + lc];
             const uint32_t cs = ne_start[r0 + lc] - a0;
             const uint32_t ce = ne_start[r0 + lc + 1] - a0;
@@ -268,7 +273,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
         }
 #pragma unroll
         for (int j = 0; j < RA; j++) {
-            const int i = tid + j * kTileThreads;
+            const int i = tid + j * TT;
             if (i < na) {
                 S.meta[i] = pm[j];
                 S.mate[i] = -1;
@@ -277,7 +282,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             }
         }
         __syncthreads();
-        for (int lc = tid; lc < nc; lc += kTileThreads) S.head[S.cstart[lc]] = 1;
+        for (int lc = tid; lc < nc; lc += TT) S.head[S.cstart[lc]] = 1;
         if (tid == 0) { S.npick = 0u; S.noad = 0u; }
         __syncthreads();
         // local cell of each row: count of cell heads up to the row (block scan
@@ -312,7 +317,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             // agents of a run that leaves the batch take no part in pairing
 #pragma unroll
             for (int j = 0; j < RA; j++) {
-                const int i = tid + j * kTileThreads;
+                const int i = tid + j * TT;
                 if (i < na && !BB.runs[S.crun[S.cell[i]]].active) pm[j] &= (uint8_t)~kMetaFertile;
             }
         }
@@ -323,7 +328,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             // from its last row down (with their IDs beside them)
 #pragma unroll
             for (int j = 0; j < RA; j++) {
-                const int i = tid + j * kTileThreads;
+                const int i = tid + j * TT;
                 if (__all_sync(FULL_MASK, i >= na)) break;
                 const uint8_t m = (i < na) ? pm[j] : (uint8_t)0;
                 const bool fert = (m & kMetaFertile) != 0;
@@ -341,7 +346,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             // rank by ID within the own sex's list (IDs are unique)
 #pragma unroll
             for (int j = 0; j < RA; j++) {
-                const int i = tid + j * kTileThreads;
+                const int i = tid + j * TT;
                 if (i < na && (pm[j] & kMetaFertile)) {
                     const int lc = S.cell[i];
                     const int64_t x = pid[j];
@@ -361,7 +366,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             __syncthreads();
 #pragma unroll
             for (int j = 0; j < RA; j++) {
-                const int i = tid + j * kTileThreads;
+                const int i = tid + j * TT;
                 if (i < na && (pm[j] & kMetaFertile)) {
                     const int lc = S.cell[i];
                     const uint32_t off = (pm[j] & kMetaGender) ? S.nf[lc] : 0u;
@@ -370,7 +375,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             }
             __syncthreads();
             // the members of the smaller side pick, in ID order; gather them densely
-            for (int lc = tid; lc < nc; lc += kTileThreads) {
+            for (int lc = tid; lc < nc; lc += TT) {
                 const uint32_t nF = S.nf[lc], nM = S.nm[lc];
                 if (nF > 0u && nM > 0u) {
                     const bool femSmall = nF <= nM;
@@ -384,7 +389,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             // pick j takes the pick[j]-th still unpaired member of the larger
             // side, pick[j] = (int)wrandr(0, nL - j)
             const uint32_t npk = S.npick;
-            for (uint32_t q = tid; q < npk; q += kTileThreads) {
+            for (uint32_t q = tid; q < npk; q += TT) {
                 const int i = S.pkrow[q];
                 const int lc = S.cell[i];
                 const uint32_t nF = S.nf[lc], nM = S.nm[lc];
@@ -404,7 +409,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             // the member taken by pick j, decoded on its own: start from pick[j]
             // and for i = j-1 down to 0 step over the member pick i took when it
             // lies at or below
-            for (uint32_t q = tid; q < npk; q += kTileThreads) {
+            for (uint32_t q = tid; q < npk; q += TT) {
                 const int i = S.pkrow[q];
                 const int lc = S.cell[i];
                 const uint32_t nF = S.nf[lc], nM = S.nm[lc];
@@ -428,11 +433,11 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
         constexpr bool kDeferOad = prog_defers_oad(PROG);
         uint32_t *const dm = reinterpret_cast<uint32_t *>(S.pkrow);   // batches: deaths | moves << 16 per cell
         if (BATCH) {
-            for (int lc = tid; lc < nc; lc += kTileThreads) dm[lc] = 0u;
+            for (int lc = tid; lc < nc; lc += TT) dm[lc] = 0u;
         }
 #pragma unroll
         for (int j = 0; j < RA; j++) {
-            const int i = tid + j * kTileThreads;
+            const int i = tid + j * TT;
             if (i >= na) break;
             const uint32_t row = a0 + (uint32_t)i;
             const int lc = S.cell[i];
@@ -554,7 +559,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             __syncthreads();
             const uint32_t nq = S.noad;
             constexpr int kOad = prog_len(PROG) - 1;
-            for (uint32_t q = tid; q < nq; q += kTileThreads) {
+            for (uint32_t q = tid; q < nq; q += TT) {
                 const int i = S.oadq[q];
                 const BatchRun *R = BATCH ? BB.runs + S.crun[S.cell[i]] : nullptr;
                 const ActionConst &A = BATCH ? R->act[kOad] : P.act[kOad];
@@ -577,7 +582,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
         // (cell, slot) and warp
 #pragma unroll
         for (int j = 0; j < RA; j++) {
-            const int i = tid + j * kTileThreads;
+            const int i = tid + j * TT;
             if (__all_sync(FULL_MASK, i >= na)) break;
             const bool in_tile = i < na;
             const uint8_t oc = in_tile ? S.oc[i] : (uint8_t)0;
@@ -597,7 +602,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
         __syncthreads();
         // ---- per cell: mothers' birth ranks by ID (births are numbered in
         // (cell, mother ID) order) and the class counts
-        for (int lc = tid; lc < nc; lc += kTileThreads) {
+        for (int lc = tid; lc < nc; lc += TT) {
             const int cs = (int)S.cstart[lc];
             const int nF = (int)S.nf[lc];
             uint32_t r = 0;
@@ -610,10 +615,9 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             const uint32_t c = (uint32_t)S.cid[lc];
             uint4 *dst = reinterpret_cast<uint4 *>(clsc + (size_t)c * kCls);
             const uint32_t w0 = S.cls[lc][0], w1 = S.cls[lc][1], w2 = S.cls[lc][2], w3 = S.cls[lc][3];
-            // slot 7: births, in batches also deaths << 10 and registered moves << 20
-            const uint32_t b7 = BATCH ? ((w3 >> 16) | ((dm[lc] & 0xffffu) << 10) | ((dm[lc] >> 16) << 20)) : (w3 >> 16);
             dst[0] = make_uint4(w0 & 0xffffu, w0 >> 16, w1 & 0xffffu, w1 >> 16);
-            dst[1] = make_uint4(w2 & 0xffffu, w2 >> 16, w3 & 0xffffu, b7);
+            dst[1] = make_uint4(w2 & 0xffffu, w2 >> 16, w3 & 0xffffu, w3 >> 16);
+            if (BATCH) BB.cstat[c] = dm[lc];   // deaths | registered moves << 16
         }
     }
     // statistics of the step (batches: per run, by the cell scan)
@@ -729,8 +733,7 @@ k_cell_scan(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
         if (d < C) {
             // class counts of empty cells are zero (cleared by the scatter)
             const uint32_t st = clsc[(size_t)d * kCls + 0];
-            const uint32_t c7 = clsc[(size_t)d * kCls + 7];
-            const uint32_t bt = c7 & 0x3ffu;
+            const uint32_t bt = clsc[(size_t)d * kCls + 7];
             const int nn = nnbr[d];
             const uint32_t rv = rev[d];
             uint32_t mvin = 0;
@@ -758,10 +761,12 @@ k_cell_scan(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                         rcur = r;
                         rsum_n = rsum_b = rsum_d = rsum_m = 0u;
                     }
+                    const uint32_t cs = BB.cstat[d];
+                    if (cs) BB.cstat[d] = 0u;   // consumed
                     rsum_n += nnew[j];
                     rsum_b += bt;
-                    rsum_d += (c7 >> 10) & 0x3ffu;
-                    rsum_m += c7 >> 20;
+                    rsum_d += cs & 0xffffu;
+                    rsum_m += cs >> 16;
                 }
             }
             loc.n += nnew[j];
@@ -856,6 +861,7 @@ k_cell_scan(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
         }
     }
     __syncthreads();
+    uint32_t cmax = 0u;   // largest cell of this thread in the next table
     ScanVal pre = sv_add(s_prefix, s_warp[warp]);
     {
         const ScanVal y = sv_shfl_up(inc, 1);
@@ -900,21 +906,26 @@ k_cell_scan(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                 for (uint32_t t = pre.n / kTileAgents + 1u; t * (uint32_t)kTileAgents <= e; t++) {
                     new_tile_first[t] = pre.ne + 1u;
                 }
-                if (nnew[j] > (uint32_t)kMaxCell) set_error(rs, kErrCellTooLarge, (uint32_t)d);
+                if (nnew[j] > (uint32_t)kMaxCellBig) set_error(rs, kErrCellTooLarge, (uint32_t)d);
+                cmax = max(cmax, nnew[j]);
             }
             pre.n += nnew[j];
             pre.b += bth[j];
             pre.ne += (nnew[j] > 0u) ? 1u : 0u;
         }
     }
+    // the next step runs the big-cell kernels when a cell exceeds kMaxCell
+    cmax = __reduce_max_sync(FULL_MASK, cmax);
+    if (lane == 0 && cmax > (uint32_t)kMaxCell) atomicMax(&rs->max_cell, cmax);
 }
 
 // ----------------------------------------------------------------- scatter
-struct ScatterSmem {
-    uint8_t code[kTileMax];
-    uint8_t head[kTileMax];        // first row of a cell
-    uint16_t rank[kTileMax];       // stable rank among the cell's agents of the same class
-    uint16_t cell[kTileMax];
+template <int TM, int TT>
+struct ScatterSmemT {
+    uint8_t code[TM];
+    uint8_t head[TM];        // first row of a cell
+    uint16_t rank[TM];       // stable rank among the cell's agents of the same class
+    uint16_t cell[TM];
     uint32_t cstart[kTileCells + 1];
     uint32_t sb[kTileCells];
     uint32_t bb[kTileCells];
@@ -922,17 +933,17 @@ struct ScatterSmem {
     uint32_t ob[kTileCells][6];
     uint64_t clo[kTileCells];      // scan value at each cell's first row
     uint64_t chi[kTileCells];
-    uint64_t wlo[kTileThreads / 32];
-    uint64_t whi[kTileThreads / 32];
-    uint16_t brow[kTileMax];       // rows of the tile's mothers (dense)
+    uint64_t wlo[TT / 32];
+    uint64_t whi[TT / 32];
+    uint16_t brow[TM];       // rows of the tile's mothers (dense)
     uint32_t crn[kTileCells];      // batches: run of each cell
     float cft[kTileCells];         // batches: time of the cell's run
     uint32_t nb;
     uint32_t last;
 };
 
-template <bool BATCH>
-__global__ void __launch_bounds__(kTileThreads, 4)
+template <bool BATCH, bool BIG>
+__global__ void __launch_bounds__(Tile<BIG>::kThreads, BIG ? 1 : 4)
 k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
           const uint32_t *__restrict__ nonempty, const uint32_t *__restrict__ ne_start,
           const uint32_t *__restrict__ tile_first,
@@ -949,8 +960,29 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
           const int32_t *__restrict__ gslot, int32_t *__restrict__ gslot2,
           const uint32_t *__restrict__ freelist, uint32_t *__restrict__ freelist2,
           uint32_t *__restrict__ brec) {
-    __shared__ ScatterSmem S;
+    constexpr int TT = Tile<BIG>::kThreads;
+    constexpr int TM = Tile<BIG>::kMax;
+    extern __shared__ __align__(16) unsigned char qhg_smem[];
+    ScatterSmemT<TM, TT> &S = *reinterpret_cast<ScatterSmemT<TM, TT> *>(qhg_smem);
     if (rs->error != 0u) return;   // the state stays as before the step
+    // The form of this step is read once per CTA.  The normal form is
+    // launched first; its commit only records the next step's form, and the
+    // big form -- launched second -- applies it, from its last CTA, whether it
+    // ran the step or not, so that no CTA of either form sees the flag change.
+    if (threadIdx.x == 0) S.last = rs->big;
+    __syncthreads();
+    if (S.last != (BIG ? 1u : 0u)) {
+        if (BIG && threadIdx.x == 0) {
+            __threadfence();
+            if (atomicAdd(&rs->scatter_ctas_done, 1u) == gridDim.x - 1) {
+                rs->scatter_ctas_done = 0u;
+                rs->big = rs->big_next;
+                __threadfence();
+            }
+        }
+        return;
+    }
+    __syncthreads();
     const int tid = threadIdx.x;
     const int32_t step = rs->step;
     const float fT = (float)step;
@@ -959,7 +991,7 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
     const uint32_t N = rs->n_agents;
     const uint32_t cap = P.capacity;
     const uint32_t ntiles = (N + kTileAgents - 1) / kTileAgents;
-    constexpr int RA = kTileMax / kTileThreads;
+    constexpr int RA = TM / TT;
     // genome slots (SPopulation::recycleDeadSpaceNew, core/SPopulation.cpp:596-724):
     // newborns take the slots freed by the previous step's deaths, in birth
     // order, then never used slots; this step's deaths free theirs for the
@@ -990,14 +1022,14 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
         if (nc == 0) continue;
         const uint32_t a0 = ne_start[r0];
         const int na = (int)(ne_start[r0 + nc] - a0);
-        if (na > kTileMax || nc > kTileCells) continue;   // reported by k_actions
+        if (na > TM || nc > kTileCells) continue;   // reported by k_actions
         uint8_t pc[RA];
         int64_t pid[RA];
         float pb[RA], pa[RA], pl[RA];
         int32_t pg[RA];
 #pragma unroll
         for (int j = 0; j < RA; j++) {
-            const int i = tid + j * kTileThreads;
+            const int i = tid + j * TT;
             pc[j] = 0;
             pg[j] = 0;
             if (i < na) {
@@ -1013,11 +1045,11 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
         if (tid == 0) S.nb = 0u;
 #pragma unroll
         for (int j = 0; j < RA; j++) {
-            const int i = tid + j * kTileThreads;
+            const int i = tid + j * TT;
             if (i < na) S.head[i] = 0;
         }
         __syncthreads();
-        for (int lc = tid; lc < nc; lc += kTileThreads) {
+        for (int lc = tid; lc < nc; lc += TT) {
             const uint32_t c = nonempty[r0 + lc];
             S.cstart[lc] = ne_start[r0 + lc] - a0;
             S.head[ne_start[r0 + lc] - a0] = 1;
@@ -1044,7 +1076,7 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
         }
 #pragma unroll
         for (int j = 0; j < RA; j++) {
-            const int i = tid + j * kTileThreads;
+            const int i = tid + j * TT;
             if (i < na) S.code[i] = pc[j];
         }
         __syncthreads();
@@ -1052,7 +1084,7 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
         // class counters (classes 1..4 and 5..7 in 16-bit fields of two words)
         // over the tile's rows, minus the value at the first row of the cell
         {
-            constexpr int R = kTileMax / kTileThreads;
+            constexpr int R = TM / TT;
             const int i0 = tid * R;
             uint64_t lo[R], hi[R];
             uint64_t tlo = 0ull, thi = 0ull;
@@ -1110,7 +1142,7 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
         __syncthreads();
 #pragma unroll
         for (int j = 0; j < RA; j++) {
-            const int i = tid + j * kTileThreads;
+            const int i = tid + j * TT;
             if (__all_sync(FULL_MASK, i >= na)) break;
             const bool in_tile = i < na;
             const uint8_t code = pc[j];
@@ -1147,7 +1179,7 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
         // core/SPopulation.cpp:880-900): gender = (uchar)(2 * wrandd()) from the
         // mother's birth stream, females start FERTILE
         const uint32_t nbt = S.nb;
-        for (uint32_t q = tid; q < nbt; q += kTileThreads) {
+        for (uint32_t q = tid; q < nbt; q += TT) {
             const int i = S.brow[q];
             const uint32_t row = a0 + (uint32_t)i;
             const int lc = S.cell[i];
@@ -1224,7 +1256,7 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
     if (BATCH && S.last) {
         // per run: next ID after this step's births; the next ring slot starts at zero
         const uint32_t sl = (uint32_t)step % kBatchRing, sn = ((uint32_t)step + 1u) % kBatchRing;
-        for (int r = tid; r < BB.nruns; r += kTileThreads) {
+        for (int r = tid; r < BB.nruns; r += TT) {
             BB.rnext[r] += (int64_t)BB.rstat[((size_t)r * kBatchRing + sl) * 4 + 1];
             uint4 *z = reinterpret_cast<uint4 *>(BB.rstat + ((size_t)r * kBatchRing + sn) * 4);
             *z = make_uint4(0u, 0u, 0u, 0u);
@@ -1240,6 +1272,9 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             nx[0] = 0ull; nx[1] = 0ull; nx[2] = 0ull; nx[3] = 0ull;
             rs->n_agents = rs->new_n_agents;
             rs->n_nonempty = rs->new_n_nonempty;
+            rs->big_next = (rs->max_cell > (uint32_t)kMaxCell) ? 1u : 0u;
+            if (BIG) rs->big = rs->big_next;
+            rs->max_cell = 0u;
             rs->next_id += (int64_t)rs->births;
             rs->birth_log_n += rs->births;
             rs->action_tiles = 0u;
@@ -1481,32 +1516,68 @@ extern "C" int qhg_launch_gather_genomes(const int32_t *gslot, const uint64_t *g
     return (int)cudaGetLastError();
 }
 
+// dynamic shared memory of the tile kernels (above the 48 KB default: the
+// attribute is set once per device before the first launch)
+template <int PROG, bool BATCH, bool BIG>
+static void set_actions_attr() {
+    cudaFuncSetAttribute(qhg::k_actions<PROG, BATCH, BIG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(qhg::ActionsSmemT<qhg::Tile<BIG>::kMax, qhg::Tile<BIG>::kThreads>));
+}
+template <bool BATCH, bool BIG>
+static void set_scatter_attr() {
+    cudaFuncSetAttribute(qhg::k_scatter<BATCH, BIG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(qhg::ScatterSmemT<qhg::Tile<BIG>::kMax, qhg::Tile<BIG>::kThreads>));
+}
+
+static void set_tile_attributes() {
+    static bool done[64] = {false};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64 || done[dev]) return;
+    set_actions_attr<0, false, false>(); set_actions_attr<1, false, false>();
+    set_actions_attr<2, false, false>(); set_actions_attr<3, false, false>();
+    set_actions_attr<0, true, false>(); set_actions_attr<1, true, false>();
+    set_actions_attr<0, false, true>(); set_actions_attr<0, true, true>();
+    set_scatter_attr<false, false>(); set_scatter_attr<true, false>();
+    set_scatter_attr<false, true>(); set_scatter_attr<true, true>();
+    done[dev] = true;
+}
+
 static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
                            const qhg::BatchBuffers *BBp, const qhg::LaunchShape &L, cudaStream_t stream,
                            cudaEvent_t *ev) {
     using namespace qhg;
+    set_tile_attributes();
     const int ntiles = (P->num_cells + kScanTile - 1) / kScanTile;
     const bool batch = BBp != nullptr;
     BatchBuffers BB;
     if (batch) BB = *BBp;
     else memset(&BB, 0, sizeof(BB));
+    constexpr size_t kSmA = sizeof(ActionsSmemT<Tile<false>::kMax, Tile<false>::kThreads>);
+    constexpr size_t kSmAB = sizeof(ActionsSmemT<Tile<true>::kMax, Tile<true>::kThreads>);
+    constexpr size_t kSmS = sizeof(ScatterSmemT<Tile<false>::kMax, Tile<false>::kThreads>);
+    constexpr size_t kSmSB = sizeof(ScatterSmemT<Tile<true>::kMax, Tile<true>::kThreads>);
     if (ev) cudaEventRecord(ev[0], stream);
-#define QHG_LAUNCH_ACTIONS(PR, BT)                                                                        \
-    k_actions<PR, BT><<<L.actions_grid, kTileThreads, 0, stream>>>(                                      \
+    // both forms are launched; the one that does not match the step's cell
+    // sizes (RunState::big, set by the previous step) returns at once
+#define QHG_LAUNCH_ACTIONS(PR, BT, BG, GRID, SM)                                                          \
+    k_actions<PR, BT, BG><<<GRID, Tile<BG>::kThreads, SM, stream>>>(                                      \
         *P, BB, rs, B->nonempty, B->ne_start, B->tile_first, B->id, B->birth, B->age, B->lastb, B->meta, \
         B->nbr, B->nnbr, B->vthr, B->wthr, B->wflag, B->outc, B->father, B->brank, B->clsc)
     if (batch) {
         switch (P->program) {
-        case 1: QHG_LAUNCH_ACTIONS(1, true); break;
-        default: QHG_LAUNCH_ACTIONS(0, true); break;
+        case 1: QHG_LAUNCH_ACTIONS(1, true, false, L.actions_grid, kSmA); break;
+        default: QHG_LAUNCH_ACTIONS(0, true, false, L.actions_grid, kSmA); break;
         }
+        QHG_LAUNCH_ACTIONS(0, true, true, L.big_grid, kSmAB);
     } else {
         switch (P->program) {
-        case 1: QHG_LAUNCH_ACTIONS(1, false); break;
-        case 2: QHG_LAUNCH_ACTIONS(2, false); break;
-        case 3: QHG_LAUNCH_ACTIONS(3, false); break;
-        default: QHG_LAUNCH_ACTIONS(0, false); break;
+        case 1: QHG_LAUNCH_ACTIONS(1, false, false, L.actions_grid, kSmA); break;
+        case 2: QHG_LAUNCH_ACTIONS(2, false, false, L.actions_grid, kSmA); break;
+        case 3: QHG_LAUNCH_ACTIONS(3, false, false, L.actions_grid, kSmA); break;
+        default: QHG_LAUNCH_ACTIONS(0, false, false, L.actions_grid, kSmA); break;
         }
+        QHG_LAUNCH_ACTIONS(0, false, true, L.big_grid, kSmAB);
     }
 #undef QHG_LAUNCH_ACTIONS
     if (ev) cudaEventRecord(ev[1], stream);
@@ -1518,14 +1589,19 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
     else QHG_LAUNCH_SCAN(false);
 #undef QHG_LAUNCH_SCAN
     if (ev) cudaEventRecord(ev[2], stream);
-#define QHG_LAUNCH_SCATTER(BT)                                                                              \
-    k_scatter<BT><<<L.scatter_grid, kTileThreads, 0, stream>>>(                                             \
+#define QHG_LAUNCH_SCATTER(BT, BG, GRID, SM)                                                                \
+    k_scatter<BT, BG><<<GRID, Tile<BG>::kThreads, SM, stream>>>(                                            \
         *P, BB, rs, B->nonempty, B->ne_start, B->tile_first, B->id, B->birth, B->age, B->lastb, B->outc,   \
         B->father, B->brank, B->nnbr, B->sbase, B->bbase, B->bidbase, B->obase, B->clsc, B->id2, B->birth2, \
         B->age2, B->lastb2, B->meta2, B->blog, B->blog_cap, B->gslot, B->gslot2, B->freelist,              \
         B->freelist2, B->brec)
-    if (batch) QHG_LAUNCH_SCATTER(true);
-    else QHG_LAUNCH_SCATTER(false);
+    if (batch) {
+        QHG_LAUNCH_SCATTER(true, false, L.scatter_grid, kSmS);
+        QHG_LAUNCH_SCATTER(true, true, L.big_grid, kSmSB);
+    } else {
+        QHG_LAUNCH_SCATTER(false, false, L.scatter_grid, kSmS);
+        QHG_LAUNCH_SCATTER(false, true, L.big_grid, kSmSB);
+    }
 #undef QHG_LAUNCH_SCATTER
     if (ev) cudaEventRecord(ev[3], stream);
     if (batch) {
@@ -1551,11 +1627,16 @@ extern "C" int qhg_launch_step_timed(const qhg::StepConst *P, qhg::RunState *rs,
     return (int)cudaGetLastError();
 }
 
-// CTAs of each tile kernel that fit on one SM at once
+// CTAs of each tile kernel (normal form) that fit on one SM at once
 extern "C" void qhg_tile_ctas_per_sm(int *actions, int *scatter) {
     int a = 0, b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, qhg::k_actions<0, false>, qhg::kTileThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, qhg::k_scatter<false>, qhg::kTileThreads, 0);
+    set_tile_attributes();
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &a, qhg::k_actions<0, false, false>, qhg::kTileThreads,
+        sizeof(qhg::ActionsSmemT<qhg::Tile<false>::kMax, qhg::Tile<false>::kThreads>));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &b, qhg::k_scatter<false, false>, qhg::kTileThreads,
+        sizeof(qhg::ScatterSmemT<qhg::Tile<false>::kMax, qhg::Tile<false>::kThreads>));
     *actions = a > 0 ? a : 1;
     *scatter = b > 0 ? b : 1;
 }

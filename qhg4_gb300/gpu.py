@@ -36,7 +36,8 @@ EXPORTS = [
     "qhg_batch_step", "qhg_batch_step_timed", "qhg_batch_sync", "qhg_batch_num_agents",
     "qhg_batch_run_info", "qhg_batch_stats", "qhg_batch_download", "qhg_batch_counts",
     "qhg_batch_set_shape", "qhg_batch_get_shape", "qhg_batch_stream", "qhg_batch_destroy",
-    "qhg_batch_live_history",
+    "qhg_batch_live_history", "qhg_batch_snapshot_async", "qhg_batch_snapshot_wait",
+    "qhg_host_buffer_alloc", "qhg_host_buffer_free",
 ]
 
 
@@ -122,6 +123,10 @@ def load_library(path: str = LIB_PATH):
         "qhg_batch_stream": (I, [P, P]),
         "qhg_batch_destroy": (I, [P]),
         "qhg_batch_live_history": (I, [P, ct.c_int32, P]),
+        "qhg_batch_snapshot_async": (I, [P, ct.c_int32, P, ct.c_int64, P, P]),
+        "qhg_batch_snapshot_wait": (I, [P]),
+        "qhg_host_buffer_alloc": (I, [ct.c_int64, P]),
+        "qhg_host_buffer_free": (I, [P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -13,7 +13,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def declared_functions():
     src = open(os.path.join(ROOT, "include", "qhg_gpu.h")).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b(qhg_(?:gpu|batch)_\w+)\s*\(", src)))
+    return sorted(set(re.findall(r"\b(qhg_(?:gpu|batch|host)_\w+)\s*\(", src)))
 
 
 def test_library_exports_header():

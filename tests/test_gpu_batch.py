@@ -100,3 +100,16 @@ def test_batch_large_run_actions(gpu_lib):
     b.step(25)
     for k, r in enumerate(ids):
         same_as_alone(b, r, cases[k], 24)
+
+
+def test_batch_with_a_dense_run(gpu_lib):
+    """One run with cells of more than 512 agents puts the batch's steps into
+    the big-cell kernels; the other runs are unaffected."""
+    cases = [plain_case(k) for k in range(2)]
+    g = uniform_grid(4, 1000.0)
+    cases.append((g, make_agents(g, 100_000, seed=77, age_max=50.0), config1_actions(K=1000.0), 5))
+    b = GpuBatch(config1_actions(), agent_capacity=600_000, cell_capacity=4_000, max_runs=3)
+    ids = [b.add_run(gg, acts, seed, a) for gg, a, acts, seed in cases]
+    b.step(12)
+    for k, r in enumerate(ids):
+        same_as_alone(b, r, cases[k], 11)

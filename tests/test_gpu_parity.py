@@ -12,7 +12,7 @@ from oracle import port
 from qhg4_gb300.gpu import GpuRun
 from qhg4_gb300.spec import (ACT_FERTILITY, ACT_GETOLD, ACT_OLDAGEDEATH, ACT_RANDOMMOVE, ACT_RANDOMPAIR,
                              ACT_VERHULST, ACT_VERHULSTVARK, ACT_WEIGHTEDMOVE, CROSSOVER_POISSON1, Action,
-                             Genetics, config3_actions)
+                             Genetics, config1_actions, config3_actions)
 from qhg4_gb300.workload import make_agents, terrain_grid, uniform_grid
 
 from helpers import case_config1, case_config2, table_diff
@@ -97,3 +97,16 @@ def test_genetics(gpu_lib, genetics):
     o, g, st = run_both(grid, agents, config3_actions(), 20, 77, chunks=(3, 17), genetics=genetics)
     assert_same(o, g, st, 20)
     assert st[:, 1].sum() > 0 and st[:, 2].sum() > 0
+
+
+@pytest.mark.parametrize("K,N", [(1000.0, 120_000), (300.0, 90_000)], ids=["dense", "dense_to_sparse"])
+def test_big_cells(gpu_lib, K, N):
+    """Cells of more than 512 agents run the big-cell kernels (1024 threads
+    per tile); the step after the largest cell drops to 512 or fewer, the
+    normal ones again."""
+    grid = uniform_grid(4, K)
+    agents = make_agents(grid, N, seed=41, age_max=50.0)
+    acts = config1_actions(K=K)
+    o, g, st = run_both(grid, agents, acts, 30, 9, chunks=(1, 29))
+    assert_same(o, g, st, 30)
+    assert o.counts().max() > 0
