@@ -54,11 +54,18 @@ def cases():
              Action(ACT_RANDOMMOVE, 7, (0.05,)), Action(ACT_WEIGHTEDMOVE, 8, (0.15,))]
     yield ("mixed_order", g5, make_agents(g5, 8000, seed=15, age_max=70.0, proportional_to_K=True), acts5,
            Genetics(), 25, 123)
+    # cells of more than 512 agents (the big-cell kernels), thinning out below it
+    g6 = uniform_grid(3, 400.0)
+    yield ("dense_cells", g6, make_agents(g6, 60000, seed=16, age_max=50.0), config1_actions(K=400.0),
+           Genetics(), 12, 31)
 
 
 def main():
+    only = set(sys.argv[1:])
     with tempfile.TemporaryDirectory() as work:
         for name, grid, agents, acts, gen, steps, seed in cases():
+            if only and name not in only:
+                continue
             out = run_reference("philox", work, grid, agents, acts, steps, seed, gen, threads=4)
             if out.draw_errors != 0:
                 raise RuntimeError(f"{name}: {out.draw_errors} draws outside a keyed stream")
