@@ -83,7 +83,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.QUERY,
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
@@ -93,9 +93,20 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
 
-    def stop(self):
+    def wait_first(self, timeout: float = 5.0) -> None:
+        """Waits until nvidia-smi has delivered a sample (it starts slowly)."""
+        t0 = time.perf_counter()
+        while self.proc is not None and not self.lines and time.perf_counter() - t0 < timeout:
+            time.sleep(0.02)
+
+    def mark(self) -> float:
+        return time.perf_counter()
+
+    def stop(self, t_from: float = None, t_to: float = None):
+        """Clocks of the samples taken between t_from and t_to (all samples
+        if that window holds none)."""
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -107,7 +118,11 @@ class ClockSampler:
             self.thread.join(timeout=2)
         sm, smax, reasons, busy = [], [], set(), []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        lines = [ln for t, ln in self.lines if t_from is not None and t_from <= t <= t_to]
+        window = bool(lines)
+        if not lines:
+            lines = [ln for _, ln in self.lines]
+        for ln in lines:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 10:
                 continue
@@ -126,7 +141,8 @@ class ClockSampler:
         load = busy if busy else sm
         return {"sm_mhz": float(np.median(load)) if load else None,
                 "sm_max_mhz": float(max(smax)) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm), "samples_busy": len(busy)}
+                "reasons": sorted(reasons), "samples": len(sm), "samples_busy": len(busy),
+                "window": "timed region" if window else "whole measurement (no sample inside the timed region)"}
 
 
 def read_peaks():
@@ -237,10 +253,12 @@ def run_ours(args, world, rank, local, dist):
     n_start = run.num_agents()
     sampler = ClockSampler(device)
     sampler.start()
-    time.sleep(0.3)
+    sampler.wait_first()
     if dist is not None:
         dist.barrier()
+    t_on = sampler.mark()
     ms = run.step_timed(args.steps)
+    t_off = sampler.mark()
     if dist is not None:
         dist.barrier()
     st = run.stats(args.steps) if args.steps > 0 else np.zeros((0, 4), np.uint64)
@@ -253,7 +271,7 @@ def run_ours(args, world, rank, local, dist):
     prof_agents = (n_prof_start + int(pst[:-1, 0].sum())) / prof_steps
     if os.environ.get("QHG_BENCH_DEBUG"):
         sys.stderr.write(f"timed stats tail {st[-3:].tolist()} profiled stats {pst.tolist()} kms {kms.tolist()}\n")
-    clocks = sampler.stop()
+    clocks = sampler.stop(t_on, t_off)
     t_max = gather_max(dist, ms / 1000.0)
     total = gather_sum(dist, float(agent_steps))
     value = total / t_max if t_max > 0 else 0.0
@@ -488,7 +506,7 @@ def run_ensemble(args, world, rank, local, dist):
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=195)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["ensemble", "served"], default="large")

@@ -58,7 +58,7 @@ struct qhg_run {
     ulonglong2 *d_vthr = nullptr;   // per-cell Verhulst thresholds of the coming step
     std::vector<double> h_K;
     uint64_t *d_wthr = nullptr;
-    uint8_t *d_wflag = nullptr;
+    uint32_t *d_cmove = nullptr;
     std::vector<int32_t> h_nbr;
     // agents (ping-pong)
     uint32_t cap = 0;
@@ -318,10 +318,11 @@ int qhg_host_actions(StepConst &P, int n, const int32_t *types, const double (*p
 // Grid tables of one run: rev packs, 3 bits per neighbour slot q, the slot
 // of the cell in the neighbour's own list; wthr holds the WeightedMove
 // thresholds (SingleEvaluator's cumulated weights, actions/SingleEvaluator.cpp:174-241,
-// as integers: dR2 = wrandd()*W[n] < W[j]  <=>  u < T_j) and wflag marks cells
-// whose weights are all equal.
+// as integers: dR2 = wrandd()*W[n] < W[j]  <=>  u < T_j); cmove packs per cell
+// the neighbour count (bits 0-2), the slots that hold a neighbour (bits 8-13)
+// and whether all weights are equal (bit 16).
 int qhg_host_grid_tables(int C, const int32_t *nbr6, const uint8_t *nnbr, const double *K, bool wm,
-                         std::vector<uint32_t> &rev, std::vector<uint64_t> &wthr, std::vector<uint8_t> &wflag,
+                         std::vector<uint32_t> &rev, std::vector<uint64_t> &wthr, std::vector<uint32_t> &cmove,
                          std::string &err) {
     rev.assign((size_t)C, 0u);
     for (int c = 0; c < C; c++) {
@@ -339,7 +340,12 @@ int qhg_host_grid_tables(int C, const int32_t *nbr6, const uint8_t *nnbr, const 
         }
     }
     wthr.assign((size_t)C * 6, 0);
-    wflag.assign((size_t)C, 0);
+    cmove.assign((size_t)C, 0u);
+    for (int c = 0; c < C; c++) {
+        uint32_t vm = 0;
+        for (int j = 0; j < 6; j++) vm |= (nbr6[(size_t)c * 6 + j] >= 0 ? 1u : 0u) << j;
+        cmove[c] = (uint32_t)nnbr[c] | (vm << 8);
+    }
     if (!wm) return 0;
     std::vector<double> W((size_t)C * 7);
     for (int c = 0; c < C; c++) {
@@ -362,7 +368,7 @@ int qhg_host_grid_tables(int C, const int32_t *nbr6, const uint8_t *nnbr, const 
         const double *Wc = &W[(size_t)c * 7];
         const double Wn = Wc[nn];
         if (Wc[0] == Wn) {
-            wflag[c] = 1;
+            cmove[c] |= 1u << 16;
             continue;
         }
         auto f = [&](uint64_t u) { return ((1.0 * (double)u) / 4294967296.0) * Wn; };
@@ -460,15 +466,15 @@ extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_
     const int C = num_cells;
     std::vector<uint32_t> rev;
     std::vector<uint64_t> wthr;
-    std::vector<uint8_t> wflag;
+    std::vector<uint32_t> cmove;
     {
         std::string err;
-        if (qhg_host_grid_tables(C, nbr6, nnbr, K, r->P.has_wmove != 0, rev, wthr, wflag, err) != 0) {
+        if (qhg_host_grid_tables(C, nbr6, nnbr, K, r->P.has_wmove != 0, rev, wthr, cmove, err) != 0) {
             return fail(QHG_ERR_ARG, err);
         }
     }
     cudaFree(r->d_nbr); cudaFree(r->d_nnbr); cudaFree(r->d_rev); cudaFree(r->d_K); cudaFree(r->d_vthr);
-    cudaFree(r->d_wthr); cudaFree(r->d_wflag);
+    cudaFree(r->d_wthr); cudaFree(r->d_cmove);
     cudaFree(r->d_clsc); cudaFree(r->d_sbase); cudaFree(r->d_bbase); cudaFree(r->d_bidb);
     cudaFree(r->d_obase); cudaFree(r->d_tflag); cudaFree(r->d_tagg); cudaFree(r->d_tincl);
     r->d_vthr = nullptr;
@@ -482,7 +488,7 @@ extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_
     CUDA_TRY(cudaMalloc(&r->d_K, (size_t)C * sizeof(double)));
     CUDA_TRY(cudaMalloc(&r->d_vthr, (size_t)C * sizeof(ulonglong2)));
     CUDA_TRY(cudaMalloc(&r->d_wthr, (size_t)C * 6 * sizeof(uint64_t)));
-    CUDA_TRY(cudaMalloc(&r->d_wflag, (size_t)C));
+    CUDA_TRY(cudaMalloc(&r->d_cmove, (size_t)C * sizeof(uint32_t)));
     CUDA_TRY(cudaMalloc(&r->d_clsc, (size_t)C * kCls * sizeof(uint32_t)));
     CUDA_TRY(cudaMalloc(&r->d_sbase, (size_t)C * sizeof(uint32_t)));
     CUDA_TRY(cudaMalloc(&r->d_bbase, (size_t)C * sizeof(uint32_t)));
@@ -497,7 +503,7 @@ extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_
     CUDA_TRY(cudaMemsetAsync(r->d_clsc, 0, (size_t)C * kCls * sizeof(uint32_t), r->stream));
     CUDA_TRY(cudaMemcpyAsync(r->d_K, K, (size_t)C * sizeof(double), cudaMemcpyHostToDevice, r->stream));
     CUDA_TRY(cudaMemcpyAsync(r->d_wthr, wthr.data(), (size_t)C * 6 * sizeof(uint64_t), cudaMemcpyHostToDevice, r->stream));
-    CUDA_TRY(cudaMemcpyAsync(r->d_wflag, wflag.data(), (size_t)C, cudaMemcpyHostToDevice, r->stream));
+    CUDA_TRY(cudaMemcpyAsync(r->d_cmove, cmove.data(), (size_t)C * sizeof(uint32_t), cudaMemcpyHostToDevice, r->stream));
     CUDA_TRY(cudaMemsetAsync(r->d_tflag, 0, (size_t)ntiles * sizeof(uint32_t), r->stream));
     CUDA_TRY(cudaStreamSynchronize(r->stream));
     r->h_nbr.assign(nbr6, nbr6 + (size_t)C * 6);
@@ -690,7 +696,7 @@ static StepBuffers make_buffers(qhg_run *r, int cur) {
     B.id2 = r->d_id[nx]; B.birth2 = r->d_birth[nx]; B.age2 = r->d_age[nx]; B.lastb2 = r->d_lastb[nx];
     B.meta2 = r->d_meta[nx];
     B.nbr = r->d_nbr; B.nnbr = r->d_nnbr; B.rev = r->d_rev; B.K = r->d_K; B.vthr = r->d_vthr; B.wthr = r->d_wthr;
-    B.wflag = r->d_wflag;
+    B.cmove = r->d_cmove;
     B.outc = r->d_outc; B.father = r->d_father; B.brank = r->d_brank; B.clsc = r->d_clsc;
     B.sbase = r->d_sbase; B.bbase = r->d_bbase; B.bidbase = r->d_bidb; B.obase = r->d_obase;
     B.tile_flag = r->d_tflag; B.tile_agg = r->d_tagg; B.tile_incl = r->d_tincl;
@@ -938,7 +944,7 @@ extern "C" int qhg_gpu_destroy(qhg_run *r) {
     drop_graphs(r);
     free_agents(r);
     cudaFree(r->d_nbr); cudaFree(r->d_nnbr); cudaFree(r->d_rev); cudaFree(r->d_K); cudaFree(r->d_vthr);
-    cudaFree(r->d_wthr); cudaFree(r->d_wflag);
+    cudaFree(r->d_wthr); cudaFree(r->d_cmove);
     cudaFree(r->d_clsc); cudaFree(r->d_sbase); cudaFree(r->d_bbase); cudaFree(r->d_bidb);
     cudaFree(r->d_obase); cudaFree(r->d_tflag); cudaFree(r->d_tagg); cudaFree(r->d_tincl);
     cudaFree(r->d_rs);

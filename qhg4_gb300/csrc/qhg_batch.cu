@@ -74,7 +74,7 @@ struct qhg_batch {
     double *d_K = nullptr;
     ulonglong2 *d_vthr = nullptr;
     uint64_t *d_wthr = nullptr;
-    uint8_t *d_wflag = nullptr;
+    uint32_t *d_cmove = nullptr;
     uint32_t *d_crun = nullptr;
     // tables (ping-pong)
     int64_t *d_id[2] = {nullptr, nullptr};
@@ -141,7 +141,7 @@ StepBuffers make_buffers(qhg_batch *b, int cur) {
     B.id2 = b->d_id[nx]; B.birth2 = b->d_birth[nx]; B.age2 = b->d_age[nx]; B.lastb2 = b->d_lastb[nx];
     B.meta2 = b->d_meta[nx];
     B.nbr = b->d_nbr; B.nnbr = b->d_nnbr; B.rev = b->d_rev; B.K = b->d_K; B.vthr = b->d_vthr;
-    B.wthr = b->d_wthr; B.wflag = b->d_wflag;
+    B.wthr = b->d_wthr; B.cmove = b->d_cmove;
     B.outc = b->d_outc; B.father = b->d_father; B.brank = b->d_brank; B.clsc = b->d_clsc;
     B.sbase = b->d_sbase; B.bbase = b->d_bbase; B.bidbase = b->d_bidb; B.obase = b->d_obase;
     B.tile_flag = b->d_tflag; B.tile_agg = b->d_tagg; B.tile_incl = b->d_tincl;
@@ -273,7 +273,7 @@ extern "C" int qhg_batch_create(const qhg_batch_desc *desc, qhg_batch **out) {
     A((void **)&b->d_K, C * sizeof(double));
     A((void **)&b->d_vthr, C * sizeof(ulonglong2));
     A((void **)&b->d_wthr, C * 6 * sizeof(uint64_t));
-    A((void **)&b->d_wflag, C);
+    A((void **)&b->d_cmove, C * sizeof(uint32_t));
     A((void **)&b->d_crun, C * sizeof(uint32_t));
     for (int p = 0; p < 2; p++) {
         A((void **)&b->d_id[p], N * sizeof(int64_t));
@@ -383,9 +383,9 @@ extern "C" int qhg_batch_add_run(qhg_batch *b, const qhg_batch_run_desc *rd, con
     // grid tables of the run, neighbours offset into its range
     std::vector<uint32_t> rev;
     std::vector<uint64_t> wthr;
-    std::vector<uint8_t> wflag;
+    std::vector<uint32_t> cmove;
     std::string err;
-    if (qhg_host_grid_tables(num_cells, nbr6, nnbr, K, b->P.has_wmove != 0, rev, wthr, wflag, err) != 0) {
+    if (qhg_host_grid_tables(num_cells, nbr6, nnbr, K, b->P.has_wmove != 0, rev, wthr, cmove, err) != 0) {
         return bfail(QHG_ERR_ARG, err);
     }
     std::vector<int32_t> gnbr((size_t)C * 6);
@@ -455,7 +455,7 @@ extern "C" int qhg_batch_add_run(qhg_batch *b, const qhg_batch_run_desc *rd, con
     BCUDA(cudaMemcpyAsync(b->d_rev + c0, rev.data(), C * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
     BCUDA(cudaMemcpyAsync(b->d_K + c0, K, C * sizeof(double), cudaMemcpyHostToDevice, st));
     BCUDA(cudaMemcpyAsync(b->d_wthr + (size_t)c0 * 6, wthr.data(), wthr.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, st));
-    BCUDA(cudaMemcpyAsync(b->d_wflag + c0, wflag.data(), C, cudaMemcpyHostToDevice, st));
+    BCUDA(cudaMemcpyAsync(b->d_cmove + c0, cmove.data(), C * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
     std::vector<uint32_t> crun(C, (uint32_t)r);
     BCUDA(cudaMemcpyAsync(b->d_crun + c0, crun.data(), C * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
     BCUDA(cudaMemsetAsync(b->d_clsc + (size_t)c0 * kCls, 0, (size_t)C * kCls * sizeof(uint32_t), st));
@@ -812,7 +812,7 @@ extern "C" int qhg_batch_destroy(qhg_batch *b) {
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->copy_stream) cudaStreamSynchronize(b->copy_stream);
     drop_graphs(b);
-    void *ptrs[] = {b->d_nbr, b->d_nnbr, b->d_rev, b->d_K, b->d_vthr, b->d_wthr, b->d_wflag, b->d_crun,
+    void *ptrs[] = {b->d_nbr, b->d_nnbr, b->d_rev, b->d_K, b->d_vthr, b->d_wthr, b->d_cmove, b->d_crun,
                     b->d_outc, b->d_father, b->d_brank, b->d_clsc, b->d_sbase, b->d_bbase, b->d_bidb,
                     b->d_obase, b->d_tflag, b->d_tagg, b->d_tincl, b->d_runs, b->d_rnext, b->d_rstat,
                     b->d_inj, b->d_istart, b->d_ibase, b->d_injdone, b->d_cstat, b->d_sid, b->d_sbirth, b->d_sage,

@@ -160,7 +160,10 @@ struct StepBuffers {
     const int32_t *nbr; const uint8_t *nnbr; const uint32_t *rev; const double *K;
     // Verhulst thresholds of each cell for the coming step (written by the scan)
     ulonglong2 *vthr;
-    const uint64_t *wthr; const uint8_t *wflag;
+    // moves: WeightedMove thresholds (6 per cell) and one word per cell:
+    // bits 0-2 neighbour count, bits 8-13 valid neighbour slots, bit 16 all
+    // weights equal
+    const uint64_t *wthr; const uint32_t *cmove;
     uint8_t *outc; int32_t *father; uint16_t *brank; uint32_t *clsc;
     uint32_t *sbase; uint32_t *bbase; uint32_t *bidbase; uint32_t *obase;
     uint32_t *tile_flag; uint4 *tile_agg; uint4 *tile_incl;

@@ -12,7 +12,7 @@
 
 int qhg_host_actions(qhg::StepConst &P, int n, const int32_t *types, const double (*params)[4], std::string &err);
 int qhg_host_grid_tables(int C, const int32_t *nbr6, const uint8_t *nnbr, const double *K, bool wm,
-                         std::vector<uint32_t> &rev, std::vector<uint64_t> &wthr, std::vector<uint8_t> &wflag,
+                         std::vector<uint32_t> &rev, std::vector<uint64_t> &wthr, std::vector<uint32_t> &cmove,
                          std::string &err);
 
 extern "C" int qhg_launch_step(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,

@@ -172,6 +172,9 @@ struct ActionsSmemT {
     uint64_t tb[kTileCells];       // Verhulst: birth threshold (kind 1) or birth-rate death threshold (kind 2)
     uint64_t td[kTileCells];       // LinearDeath threshold
     uint8_t tk[kTileCells];
+    uint8_t nn[kTileCells];        // moves: neighbours of each cell
+    uint8_t vm[kTileCells];        // moves: bit q set when neighbour slot q holds a cell
+    uint8_t wf[kTileCells];        // WeightedMove: all weights of the cell equal
     uint32_t cls[kTileCells][4];
     uint32_t red[TT / 32];
     uint32_t npick, noad;
@@ -192,7 +195,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
           const uint8_t *__restrict__ meta,
           const int32_t *__restrict__ nbr, const uint8_t *__restrict__ nnbr,
           const ulonglong2 *__restrict__ vthr, const uint64_t *__restrict__ wthr,
-          const uint8_t *__restrict__ wflag,
+          const uint32_t *__restrict__ cmove,
           uint8_t *__restrict__ outc, int32_t *__restrict__ father, uint16_t *__restrict__ brank,
           uint32_t *__restrict__ clsc) {
     constexpr int TT = Tile<BIG>::kThreads;
@@ -260,9 +263,15 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             S.nf[lc] = 0u;
             S.nm[lc] = 0u;
             S.cls[lc][0] = S.cls[lc][1] = S.cls[lc][2] = S.cls[lc][3] = 0u;
-            // neighbour and weight rows of the cell, read by the move actions
-            if (P.has_move) asm volatile("prefetch.global.L1 [%0];" ::"l"(nbr + (size_t)c * 6));
-            if (P.has_wmove) asm volatile("prefetch.global.L1 [%0];" ::"l"(wthr + (size_t)c * 6));
+            // the neighbour row of the cell as a count and a mask of valid slots,
+            // so that moving agents read no neighbour data from memory
+            if (P.has_move) {
+                const uint32_t cm = cmove[c];
+                S.nn[lc] = (uint8_t)(cm & 7u);
+                S.vm[lc] = (uint8_t)((cm >> 8) & 63u);
+                S.wf[lc] = (uint8_t)((cm >> 16) & 1u);
+                if (P.has_wmove) asm volatile("prefetch.global.L1 [%0];" ::"l"(wthr + (size_t)c * 6));
+            }
             if (P.n_verhulst > 0) {
                 // computed by the previous step's cell scan for this step's counts
                 const ulonglong2 v = vthr[c];
@@ -431,6 +440,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
         }
         // ---- every action on every agent (SPopulation::doActions)
         constexpr bool kDeferOad = prog_defers_oad(PROG);
+        static_assert(sizeof(uint16_t) * TM >= sizeof(uint32_t) * kTileCells, "per-cell counters alias pkrow");
         uint32_t *const dm = reinterpret_cast<uint32_t *>(S.pkrow);   // batches: deaths | moves << 16 per cell
         if (BATCH) {
             for (int lc = tid; lc < nc; lc += TT) dm[lc] = 0u;
@@ -512,31 +522,25 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                 }
                 case kRandomMove: {
                     if ((uint64_t)dr.get(A.window) < A.pthr) {
-                        const int nn = nnbr[c];
+                        const int nn = S.nn[lc];
                         const uint32_t u2 = dr.get(A.window + 1);
                         const int d = (int)(((uint64_t)(nn + 1) * (uint64_t)u2) >> 32);
-                        if (d > 0) {
-                            const int to = nbr[c * 6 + d - 1];
-                            if (to >= 0) { dir = d; cnt_moves++; }
-                        }
+                        if (d > 0 && ((S.vm[lc] >> (d - 1)) & 1u)) { dir = d; cnt_moves++; }
                     }
                     break;
                 }
                 case kWeightedMove: {
                     if ((uint64_t)dr.get(A.window) < A.pthr) {
-                        const int nn = nnbr[c];
+                        const int nn = S.nn[lc];
                         const uint32_t u2 = dr.get(A.window + 1);
                         int d;
-                        if (wflag[c] & 1u) {
+                        if (S.wf[lc] & 1u) {
                             d = (int)(((uint64_t)(nn + 1) * (uint64_t)u2) >> 32);
                         } else {
                             d = 0;
                             for (int q = 0; q < nn; q++) d += (wthr[c * 6 + q] <= (uint64_t)u2) ? 1 : 0;
                         }
-                        if (d > 0) {
-                            const int to = nbr[c * 6 + d - 1];
-                            if (to >= 0) { dir = d; cnt_moves++; }
-                        }
+                        if (d > 0 && ((S.vm[lc] >> (d - 1)) & 1u)) { dir = d; cnt_moves++; }
                     }
                     break;
                 }
@@ -1563,7 +1567,7 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
 #define QHG_LAUNCH_ACTIONS(PR, BT, BG, GRID, SM)                                                          \
     k_actions<PR, BT, BG><<<GRID, Tile<BG>::kThreads, SM, stream>>>(                                      \
         *P, BB, rs, B->nonempty, B->ne_start, B->tile_first, B->id, B->birth, B->age, B->lastb, B->meta, \
-        B->nbr, B->nnbr, B->vthr, B->wthr, B->wflag, B->outc, B->father, B->brank, B->clsc)
+        B->nbr, B->nnbr, B->vthr, B->wthr, B->cmove, B->outc, B->father, B->brank, B->clsc)
     if (batch) {
         switch (P->program) {
         case 1: QHG_LAUNCH_ACTIONS(1, true, false, L.actions_grid, kSmA); break;
