@@ -145,6 +145,15 @@ int qhg_gpu_stats(qhg_run *run, int32_t nsteps, qhg_step_stats *out);
 /* birth log (QHG_FLAG_LOG_BIRTHS): rows (baby, mother, father) */
 int qhg_gpu_birth_log(qhg_run *run, int64_t *baby, int64_t *mother, int64_t *father, int64_t cap,
                       int64_t *n);
+/* The next agent ID the run gives out (IDGen::getID, core/IDGen.h:28).
+ * Checkpoint/resume (the reference's dumpSpeciesDataQDF and --resume,
+ * core/SPopulation.cpp:2138, app/SimParams.cpp:357): the state of a run is
+ * its agent table, its step and this counter; qhg_gpu_upload_agents with
+ * first_step = the saved step followed by qhg_gpu_set_next_id restores it,
+ * and the resumed run continues exactly as the uninterrupted one.  The ID
+ * must exceed every live agent's ID; set it after the upload, before a step. */
+int qhg_gpu_next_id(qhg_run *run, int64_t *next_id);
+int qhg_gpu_set_next_id(qhg_run *run, int64_t next_id);
 /* the run's CUDA stream (cudaStream_t) */
 int qhg_gpu_stream(qhg_run *run, void **stream);
 int qhg_gpu_destroy(qhg_run *run);

@@ -91,6 +91,7 @@ struct qhg_run {
     // step state
     int cur = 0;                 // table holding the current step
     int32_t upload_step = 0;
+    int64_t upload_max_id = -1;
     bool grid_ok = false, agents_ok = false;
     LaunchShape shape = {1, 1, 1};
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -672,6 +673,7 @@ extern "C" int qhg_gpu_upload_agents(qhg_run *r, const qhg_agents_soa *a, int64_
     r->h_rs->step = first_step;
     r->h_rs->n_agents = (uint32_t)live;
     r->h_rs->next_id = maxid + 1;
+    r->upload_max_id = maxid;
     r->h_rs->n_nonempty = (uint32_t)ne.size();
     r->h_rs->hwm = (uint32_t)live;
     r->h_rs->big = max_cell > (uint32_t)kMaxCell ? 1u : 0u;
@@ -928,6 +930,27 @@ extern "C" int qhg_gpu_birth_log(qhg_run *r, int64_t *baby, int64_t *mother, int
     for (uint64_t i = 0; i < total; i++) {
         baby[i] = tmp[i * 3]; mother[i] = tmp[i * 3 + 1]; father[i] = tmp[i * 3 + 2];
     }
+    return QHG_OK;
+}
+
+extern "C" int qhg_gpu_next_id(qhg_run *r, int64_t *next_id) {
+    if (r == nullptr || next_id == nullptr) return fail(QHG_ERR_ARG, "null argument");
+    int rc = qhg_gpu_sync(r);
+    if (rc != QHG_OK) return rc;
+    *next_id = r->h_rs->next_id;
+    return QHG_OK;
+}
+
+extern "C" int qhg_gpu_set_next_id(qhg_run *r, int64_t next_id) {
+    if (r == nullptr) return fail(QHG_ERR_ARG, "null run");
+    if (!r->agents_ok) return fail(QHG_ERR_STATE, "upload the agents first");
+    int rc = qhg_gpu_sync(r);
+    if (rc != QHG_OK) return rc;
+    if (next_id < r->upload_max_id + 1) return fail(QHG_ERR_ARG, "next ID not above every live agent's ID");
+    CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char *>(r->d_rs) + offsetof(RunState, next_id), &next_id,
+                             sizeof(int64_t), cudaMemcpyHostToDevice, r->stream));
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    r->h_rs->next_id = next_id;
     return QHG_OK;
 }
 

@@ -37,7 +37,7 @@ EXPORTS = [
     "qhg_batch_run_info", "qhg_batch_stats", "qhg_batch_download", "qhg_batch_counts",
     "qhg_batch_set_shape", "qhg_batch_get_shape", "qhg_batch_stream", "qhg_batch_destroy",
     "qhg_batch_live_history", "qhg_batch_snapshot_async", "qhg_batch_snapshot_wait",
-    "qhg_host_buffer_alloc", "qhg_host_buffer_free",
+    "qhg_host_buffer_alloc", "qhg_host_buffer_free", "qhg_gpu_next_id", "qhg_gpu_set_next_id",
 ]
 
 
@@ -127,6 +127,8 @@ def load_library(path: str = LIB_PATH):
         "qhg_batch_snapshot_wait": (I, [P]),
         "qhg_host_buffer_alloc": (I, [ct.c_int64, P]),
         "qhg_host_buffer_free": (I, [P]),
+        "qhg_gpu_next_id": (I, [P, P]),
+        "qhg_gpu_set_next_id": (I, [P, ct.c_int64]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -261,6 +263,14 @@ class GpuRun:
         ms = ct.c_float()
         _check(_lib.qhg_gpu_step_timed(self.h, int(n), ct.byref(ms)))
         return float(ms.value)
+
+    def next_id(self) -> int:
+        v = ct.c_int64()
+        _check(_lib.qhg_gpu_next_id(self.h, ct.byref(v)))
+        return int(v.value)
+
+    def set_next_id(self, next_id: int) -> None:
+        _check(_lib.qhg_gpu_set_next_id(self.h, int(next_id)))
 
     def stream_handle(self) -> int:
         s = ct.c_void_p()

@@ -1,0 +1,243 @@
+/*
+ * GpuPop<T>: a QHG4 population whose per-step update runs on the GPU
+ * through libqhg_gpu.so (include/qhg_gpu.h), as a drop-in for the CPU
+ * SPopulation<T> (core/SPopulation.h:86-107) under QHG4's PopLooper
+ * (core/PopLooper.cpp:166-200), loaded like every population through the
+ * dynpops createPop/getInfo ABI (dynpops/WrapperTemplate.cpp.tmp:14-30).
+ *
+ * Compiled against the QHG4 source tree (its core/, actions/, utils/ and io/
+ * headers); see Makefile in this directory.
+ *
+ * What changes against SPopulation<T>:
+ *   preLoop        after SPopulation's preLoop: creates the GPU run from the
+ *                  action list given by addGpuAction (types and parameters in
+ *                  QHG_ACT_* slots), uploads the cell grid (SCellGrid
+ *                  neighbours), the capacity array and the live agents of the
+ *                  LayerBuf
+ *   initializeStep, doActions
+ *                  nothing: the GPU step does pairing, rates, every action's
+ *                  execute, births, deaths, moves and counts
+ *   finalizeStep   one qhg_gpu_step; counts are read back when asked for
+ *   updateNumAgentsPerCell, updateTotal
+ *                  per-cell counts and total from the GPU
+ *   preWrite, postLoop
+ *                  copy the GPU table back into the LayerBuf first, so that
+ *                  the reference's writers see the current agents
+ *
+ * Draws come from the keyed Philox stream of the GPU library (seed, step,
+ * agent ID, action): a GPU population reproduces the reference's Philox
+ * test build bit for bit and the stock WELL512 populations in distribution.
+ * T must be the reference's Agent with m_fAge and m_fLastBirth.
+ */
+#ifndef QHG_GPUPOP_H
+#define QHG_GPUPOP_H
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "Action.h"
+#include "SPopulation.h"
+#include "LBController.h"
+#include "SCellGrid.h"
+#include "qhg_gpu.h"
+
+template<typename T>
+class GpuPop : public SPopulation<T> {
+public:
+    GpuPop(SCellGrid *pCG, PopFinder *pPopFinder, int iLayerSize, IDGen **apIDG, uint32_t *aulState,
+           uint *aiSeeds)
+        : SPopulation<T>(pCG, pPopFinder, iLayerSize, apIDG, aulState, aiSeeds),
+          m_pRun(NULL), m_bStale(false), m_iDevice(0) {
+        // the GPU run's seed from the population's generator state
+        m_ulSeed = (aulState != NULL) ? ((uint64_t)aulState[0] | ((uint64_t)aulState[1] << 32)) : 0;
+    }
+
+    virtual ~GpuPop() {
+        if (m_pRun != NULL) qhg_gpu_destroy(m_pRun);
+    }
+
+    // one action: its QHG_ACT_* type, its priority and class name (the
+    // execution order is SPopulation::setPrioList's: priority, then name)
+    // and its parameter slots
+    void addGpuAction(int32_t iType, uint iPrio, const std::string &sName, const double adP[4]) {
+        GpuAction a;
+        a.iType = iType;
+        a.iPrio = iPrio;
+        a.sName = sName;
+        for (int k = 0; k < 4; k++) a.adP[k] = adP[k];
+        m_vActions.push_back(a);
+    }
+    // capacity per cell (VerhulstVarK's K, WeightedMove's weights)
+    void setGpuCapacity(const double *adK, int iNumCells) { m_vK.assign(adK, adK + iNumCells); }
+    void setGpuDevice(int iDevice) { m_iDevice = iDevice; }
+
+    virtual int preLoop() {
+        int iResult = SPopulation<T>::preLoop();
+        if (iResult == 0) iResult = startGpu();
+        return iResult;
+    }
+
+    virtual int initializeStep(float fTime) { return (m_pRun != NULL) ? 0 : -1; }
+    virtual int doActions(uint iPrio, float fTime) { return 0; }
+
+    virtual int finalizeStep() {
+        if ((m_pRun == NULL) || (qhg_gpu_step(m_pRun, 1) != QHG_OK)) return -1;
+        m_bStale = true;
+        return 0;
+    }
+
+    virtual void updateNumAgentsPerCell() {
+        if (m_pRun == NULL) {
+            SPopulation<T>::updateNumAgentsPerCell();
+            return;
+        }
+        pullCounts();
+    }
+
+    virtual void updateTotal() {
+        if (m_pRun == NULL) {
+            SPopulation<T>::updateTotal();
+            return;
+        }
+        pullCounts();
+    }
+
+    virtual int preWrite(float fTime) {
+        int iResult = copyBack();
+        if (iResult == 0) iResult = SPopulation<T>::preWrite(fTime);
+        return iResult;
+    }
+
+    virtual int postLoop() {
+        int iResult = copyBack();
+        if (m_pRun != NULL) {
+            qhg_gpu_destroy(m_pRun);
+            m_pRun = NULL;
+        }
+        if (iResult == 0) iResult = SPopulation<T>::postLoop();
+        return iResult;
+    }
+
+    // the last error of the GPU library
+    const char *gpuError() const { return qhg_gpu_last_error(); }
+
+protected:
+    struct GpuAction {
+        int32_t iType;
+        uint iPrio;
+        std::string sName;
+        double adP[4];
+    };
+
+    int startGpu() {
+        std::vector<GpuAction> v(m_vActions);
+        std::stable_sort(v.begin(), v.end(), [](const GpuAction &a, const GpuAction &b) {
+            return (a.iPrio != b.iPrio) ? (a.iPrio < b.iPrio) : (a.sName < b.sName);
+        });
+        if (v.size() > QHG_MAX_ACTIONS) return -1;
+        qhg_run_desc d;
+        memset(&d, 0, sizeof(d));
+        d.seed = m_ulSeed;
+        d.n_actions = (int32_t)v.size();
+        for (size_t i = 0; i < v.size(); i++) {
+            d.action_type[i] = v[i].iType;
+            for (int k = 0; k < 4; k++) d.action_param[i][k] = v[i].adP[k];
+        }
+        d.device = m_iDevice;
+        if (qhg_gpu_create(&d, &m_pRun) != QHG_OK) return -1;
+        // grid: neighbours of each cell, -1 padded to 6
+        const int C = (int)this->m_pCG->m_iNumCells;
+        std::vector<int32_t> vNbr((size_t)C * 6, -1);
+        std::vector<uint8_t> vN((size_t)C, 0);
+        for (int c = 0; c < C; c++) {
+            const SCell &cell = this->m_pCG->m_aCells[c];
+            const int n = std::min<int>(cell.m_iNumNeighbors, 6);
+            vN[c] = (uint8_t)n;
+            for (int j = 0; j < n; j++) vNbr[(size_t)c * 6 + j] = (int32_t)cell.m_aNeighbors[j];
+        }
+        if (m_vK.size() != (size_t)C) m_vK.assign((size_t)C, 0.0);
+        if (qhg_gpu_upload_grid(m_pRun, vNbr.data(), vN.data(), m_vK.data(), C) != QHG_OK) return -1;
+        // live agents of the LayerBuf
+        std::vector<int64_t> vID;
+        std::vector<int32_t> vCell;
+        std::vector<float> vBirth, vAge, vLast;
+        std::vector<uint8_t> vGender, vState;
+        const int iFirst = this->getFirstAgentIndex();
+        if (iFirst != LBController::NIL) {
+            const int iLast = this->getLastAgentIndex();
+            for (int iA = iFirst; iA <= iLast; iA++) {
+                const T &a = this->m_aAgents[iA];
+                if (a.m_iLifeState <= 0) continue;
+                vID.push_back((int64_t)a.m_ulID);
+                vCell.push_back((int32_t)a.m_iCellIndex);
+                vBirth.push_back(a.m_fBirthTime);
+                vAge.push_back(a.m_fAge);
+                vLast.push_back(a.m_fLastBirth);
+                vGender.push_back((uint8_t)a.m_iGender);
+                vState.push_back((uint8_t)a.m_iLifeState);
+            }
+        }
+        qhg_agents_soa s = {vID.data(), vCell.data(), vBirth.data(), vAge.data(), vLast.data(),
+                            vGender.data(), vState.data(), NULL};
+        if (qhg_gpu_upload_agents(m_pRun, &s, (int64_t)vID.size(), 0) != QHG_OK) return -1;
+        m_bStale = false;
+        return 0;
+    }
+
+    void pullCounts() {
+        const int C = (int)this->m_pCG->m_iNumCells;
+        std::vector<uint32_t> v((size_t)C);
+        if (qhg_gpu_counts(m_pRun, v.data()) != QHG_OK) return;
+        ulong iTotal = 0;
+        for (int c = 0; c < C; c++) {
+            this->m_aiNumAgentsPerCell[c] = v[c];
+            iTotal += v[c];
+        }
+        this->m_iTotal = iTotal;
+    }
+
+    // the GPU table into the LayerBuf (all slots rewritten)
+    int copyBack() {
+        if ((m_pRun == NULL) || !m_bStale) return 0;
+        int64_t n = 0;
+        if (qhg_gpu_num_agents(m_pRun, &n) != QHG_OK) return -1;
+        std::vector<int64_t> vID((size_t)n);
+        std::vector<int32_t> vCell((size_t)n);
+        std::vector<float> vBirth((size_t)n), vAge((size_t)n), vLast((size_t)n);
+        std::vector<uint8_t> vGender((size_t)n), vState((size_t)n);
+        qhg_agents_soa s = {vID.data(), vCell.data(), vBirth.data(), vAge.data(), vLast.data(),
+                            vGender.data(), vState.data(), NULL};
+        int64_t got = 0;
+        if (qhg_gpu_download(m_pRun, &s, n, &got) != QHG_OK) return -1;
+        this->m_pAgentController->clear();
+        if (got > 0) {
+            const int iStart = (int)this->m_pAgentController->reserveSpace2((uint)got);
+            for (int64_t i = 0; i < got; i++) {
+                T &a = this->m_aAgents[iStart + (int)i];
+                a.m_iLifeState = vState[(size_t)i];
+                a.m_iCellIndex = vCell[(size_t)i];
+                a.m_ulID = (idtype)vID[(size_t)i];
+                a.m_ulCellID = this->m_pCG->m_aCells[vCell[(size_t)i]].m_iGlobalID;
+                a.m_fBirthTime = vBirth[(size_t)i];
+                a.m_iGender = vGender[(size_t)i];
+                a.m_fAge = vAge[(size_t)i];
+                a.m_fLastBirth = vLast[(size_t)i];
+            }
+        }
+        pullCounts();
+        m_bStale = false;
+        return 0;
+    }
+
+    qhg_run *m_pRun;
+    bool m_bStale;
+    int m_iDevice;
+    uint64_t m_ulSeed;
+    std::vector<GpuAction> m_vActions;
+    std::vector<double> m_vK;
+};
+
+#endif
