@@ -71,7 +71,7 @@ struct qhg_run {
     uint32_t *d_nes[2] = {nullptr, nullptr};   // their first rows (+ agent count)
     uint32_t *d_tf[2] = {nullptr, nullptr};    // first non-empty cell of each tile
     // scratch
-    uint8_t *d_outc = nullptr;
+    uint32_t *d_outc = nullptr;
     int32_t *d_father = nullptr;
     uint16_t *d_brank = nullptr;
     uint32_t *d_clsc = nullptr, *d_sbase = nullptr, *d_bbase = nullptr, *d_bidb = nullptr, *d_obase = nullptr;
@@ -528,7 +528,7 @@ static int alloc_agents(qhg_run *r, uint32_t cap) {
         CUDA_TRY(cudaMalloc(&r->d_nes[p], (size_t)(C + 1) * sizeof(uint32_t)));
         CUDA_TRY(cudaMalloc(&r->d_tf[p], ((size_t)cap / kTileAgents + 2) * sizeof(uint32_t)));
     }
-    CUDA_TRY(cudaMalloc(&r->d_outc, (size_t)cap));
+    CUDA_TRY(cudaMalloc(&r->d_outc, (size_t)cap * sizeof(uint32_t)));
     CUDA_TRY(cudaMalloc(&r->d_father, (size_t)cap * sizeof(int32_t)));
     CUDA_TRY(cudaMalloc(&r->d_brank, (size_t)cap * sizeof(uint16_t)));
     if (r->P.log_births) {

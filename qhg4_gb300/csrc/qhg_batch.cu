@@ -86,7 +86,7 @@ struct qhg_batch {
     uint32_t *d_nes[2] = {nullptr, nullptr};
     uint32_t *d_tf[2] = {nullptr, nullptr};
     // scratch of a step
-    uint8_t *d_outc = nullptr;
+    uint32_t *d_outc = nullptr;
     int32_t *d_father = nullptr;
     uint16_t *d_brank = nullptr;
     uint32_t *d_clsc = nullptr, *d_sbase = nullptr, *d_bbase = nullptr, *d_bidb = nullptr, *d_obase = nullptr;
@@ -285,7 +285,7 @@ extern "C" int qhg_batch_create(const qhg_batch_desc *desc, qhg_batch **out) {
         A((void **)&b->d_nes[p], (C + 1) * sizeof(uint32_t));
         A((void **)&b->d_tf[p], (N / kTileAgents + 2) * sizeof(uint32_t));
     }
-    A((void **)&b->d_outc, N);
+    A((void **)&b->d_outc, N * sizeof(uint32_t));
     A((void **)&b->d_father, N * sizeof(int32_t));
     A((void **)&b->d_brank, N * sizeof(uint16_t));
     A((void **)&b->d_clsc, C * kCls * sizeof(uint32_t));

@@ -164,7 +164,9 @@ struct StepBuffers {
     // bits 0-2 neighbour count, bits 8-13 valid neighbour slots, bit 16 all
     // weights equal
     const uint64_t *wthr; const uint32_t *cmove;
-    uint8_t *outc; int32_t *father; uint16_t *brank; uint32_t *clsc;
+    // outcome word per agent: outcome byte | local cell << 8 | rank in its
+    // cell's class << 17
+    uint32_t *outc; int32_t *father; uint16_t *brank; uint32_t *clsc;
     uint32_t *sbase; uint32_t *bbase; uint32_t *bidbase; uint32_t *obase;
     uint32_t *tile_flag; uint4 *tile_agg; uint4 *tile_incl;
     int64_t *blog; uint64_t blog_cap;

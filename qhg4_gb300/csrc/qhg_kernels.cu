@@ -196,7 +196,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
           const int32_t *__restrict__ nbr, const uint8_t *__restrict__ nnbr,
           const ulonglong2 *__restrict__ vthr, const uint64_t *__restrict__ wthr,
           const uint32_t *__restrict__ cmove,
-          uint8_t *__restrict__ outc, int32_t *__restrict__ father, uint16_t *__restrict__ brank,
+          uint32_t *__restrict__ outc, int32_t *__restrict__ father, uint16_t *__restrict__ brank,
           uint32_t *__restrict__ clsc) {
     constexpr int TT = Tile<BIG>::kThreads;
     constexpr int TM = Tile<BIG>::kMax;
@@ -581,9 +581,11 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             }
         }
         __syncthreads();
-        // outcome bytes and per-cell class counts (slot 0 stay, 1..6 movers,
+        // outcome words and per-cell class counts (slot 0 stay, 1..6 movers,
         // 7 births), two 16-bit counters per shared word, one atomic per
-        // (cell, slot) and warp
+        // (cell, slot) and warp.  The count an agent finds is its rank in its
+        // cell's class, which the scatter uses as its offset: rows of a cell
+        // are not in ID order, nothing depends on their order.
 #pragma unroll
         for (int j = 0; j < RA; j++) {
             const int i = tid + j * TT;
@@ -593,10 +595,12 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             const int cls = oc & 7;
             const bool bflag = (oc & kOutBirth) != 0;
             const int lc = in_tile ? S.cell[i] : 0;
-            if (in_tile) outc[a0 + (uint32_t)i] = oc;
             const int slot = (cls > 0) ? cls - 1 : 0;
-            warp_agg_add(in_tile && cls > 0, ((uint32_t)lc << 3) | (uint32_t)slot, &S.cls[lc][slot >> 1],
-                         1u << (16 * (slot & 1)));
+            const uint32_t q = warp_agg_add(in_tile && cls > 0, ((uint32_t)lc << 3) | (uint32_t)slot,
+                                            &S.cls[lc][slot >> 1], 1u << (16 * (slot & 1)));
+            const uint32_t rank = (q >> (16 * (slot & 1))) & 0xffffu;
+            // outcome byte | local cell << 8 | rank in the cell's class << 17
+            if (in_tile) outc[a0 + (uint32_t)i] = (uint32_t)oc | ((uint32_t)lc << 8) | (rank << 17);
             warp_agg_add(in_tile && bflag, ((uint32_t)lc << 3) | 7u, &S.cls[lc][3], 1u << 16);
             if (BATCH) {
                 warp_agg_add(in_tile && cls == 0 && !(oc & kOutDropped), (uint32_t)lc, &dm[lc], 1u);
@@ -926,20 +930,11 @@ k_cell_scan(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
 // ----------------------------------------------------------------- scatter
 template <int TM, int TT>
 struct ScatterSmemT {
-    uint8_t code[TM];
-    uint8_t head[TM];        // first row of a cell
-    uint16_t rank[TM];       // stable rank among the cell's agents of the same class
-    uint16_t cell[TM];
-    uint32_t cstart[kTileCells + 1];
-    uint32_t sb[kTileCells];
-    uint32_t bb[kTileCells];
-    uint32_t bid[kTileCells];
-    uint32_t ob[kTileCells][6];
-    uint64_t clo[kTileCells];      // scan value at each cell's first row
-    uint64_t chi[kTileCells];
-    uint64_t wlo[TT / 32];
-    uint64_t whi[TT / 32];
-    uint16_t brow[TM];       // rows of the tile's mothers (dense)
+    uint32_t sb[kTileCells];       // first row of the cell's stayers in the next table
+    uint32_t bb[kTileCells];       // first row of its newborns
+    uint32_t bid[kTileCells];      // birth number of its first newborn
+    uint32_t ob[kTileCells][6];    // first row of its movers, per neighbour slot
+    uint32_t brow[TM];             // the tile's mothers: row | local cell << 16 (dense)
     uint32_t crn[kTileCells];      // batches: run of each cell
     float cft[kTileCells];         // batches: time of the cell's run
     uint32_t nb;
@@ -953,7 +948,7 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
           const uint32_t *__restrict__ tile_first,
           const int64_t *__restrict__ id, const float *__restrict__ birth,
           const float *__restrict__ age, const float *__restrict__ lastb,
-          const uint8_t *__restrict__ outc, const int32_t *__restrict__ father,
+          const uint32_t *__restrict__ outc, const int32_t *__restrict__ father,
           const uint16_t *__restrict__ brank, const uint8_t *__restrict__ nnbr,
           const uint32_t *__restrict__ sbase, const uint32_t *__restrict__ bbase,
           const uint32_t *__restrict__ bidbase, const uint32_t *__restrict__ obase,
@@ -1027,7 +1022,7 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
         const uint32_t a0 = ne_start[r0];
         const int na = (int)(ne_start[r0 + nc] - a0);
         if (na > TM || nc > kTileCells) continue;   // reported by k_actions
-        uint8_t pc[RA];
+        uint32_t pc[RA];
         int64_t pid[RA];
         float pb[RA], pa[RA], pl[RA];
         int32_t pg[RA];
@@ -1047,17 +1042,8 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
         }
         __syncthreads();   // the previous tile is done with the shared arrays
         if (tid == 0) S.nb = 0u;
-#pragma unroll
-        for (int j = 0; j < RA; j++) {
-            const int i = tid + j * TT;
-            if (i < na) S.head[i] = 0;
-        }
-        __syncthreads();
         for (int lc = tid; lc < nc; lc += TT) {
             const uint32_t c = nonempty[r0 + lc];
-            S.cstart[lc] = ne_start[r0 + lc] - a0;
-            S.head[ne_start[r0 + lc] - a0] = 1;
-            if (lc == nc - 1) S.cstart[nc] = ne_start[r0 + lc + 1] - a0;
             S.sb[lc] = sbase[c];
             S.bb[lc] = bbase[c];
             S.bid[lc] = bidbase[c];
@@ -1078,78 +1064,15 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             z[0] = make_uint4(0u, 0u, 0u, 0u);
             z[1] = make_uint4(0u, 0u, 0u, 0u);
         }
-#pragma unroll
-        for (int j = 0; j < RA; j++) {
-            const int i = tid + j * TT;
-            if (i < na) S.code[i] = pc[j];
-        }
         __syncthreads();
-        // stable ranks per (cell, class): a block-wide exclusive scan of one-hot
-        // class counters (classes 1..4 and 5..7 in 16-bit fields of two words)
-        // over the tile's rows, minus the value at the first row of the cell
-        {
-            constexpr int R = TM / TT;
-            const int i0 = tid * R;
-            uint64_t lo[R], hi[R];
-            uint64_t tlo = 0ull, thi = 0ull;
-#pragma unroll
-            for (int j = 0; j < R; j++) {
-                const int i = i0 + j;
-                // field 3 of the high word counts cell heads (first rows)
-                if (i < na && S.head[i]) thi += 1ull << 48;
-                lo[j] = tlo;
-                hi[j] = thi;
-                const int k = (i < na) ? (S.code[i] & 7) : 0;
-                if (k) {
-                    const uint64_t one = 1ull << (16 * ((k - 1) & 3));
-                    if (k <= 4) tlo += one; else thi += one;
-                }
-            }
-            const int lane = tid & 31, warp = tid >> 5;
-            uint64_t ilo = tlo, ihi = thi;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint64_t ylo = __shfl_up_sync(FULL_MASK, ilo, o);
-                const uint64_t yhi = __shfl_up_sync(FULL_MASK, ihi, o);
-                if (lane >= o) { ilo += ylo; ihi += yhi; }
-            }
-            if (lane == 31) { S.wlo[warp] = ilo; S.whi[warp] = ihi; }
-            __syncthreads();
-            uint64_t blo = ilo - tlo, bhi = ihi - thi;
-            for (int w = 0; w < warp; w++) { blo += S.wlo[w]; bhi += S.whi[w]; }
-#pragma unroll
-            for (int j = 0; j < R; j++) {
-                const int i = i0 + j;
-                if (i < na) {
-                    lo[j] += blo;
-                    hi[j] += bhi;
-                    const int lc = (int)(hi[j] >> 48) - 1;   // heads up to and including row i
-                    S.cell[i] = (uint16_t)lc;
-                    if (S.head[i]) { S.clo[lc] = lo[j]; S.chi[lc] = hi[j] & ((1ull << 48) - 1ull); }
-                }
-            }
-            __syncthreads();
-#pragma unroll
-            for (int j = 0; j < R; j++) {
-                const int i = i0 + j;
-                if (i < na) {
-                    const int k = S.code[i] & 7;
-                    if (k) {
-                        const int lc = S.cell[i];
-                        const int sh = 16 * ((k - 1) & 3);
-                        const uint64_t v = (k <= 4) ? (lo[j] - S.clo[lc]) : ((hi[j] & ((1ull << 48) - 1ull)) - S.chi[lc]);
-                        S.rank[i] = (uint16_t)(v >> sh);
-                    }
-                }
-            }
-        }
-        __syncthreads();
+        // every agent to its cell's class base + its rank in the class (from
+        // k_actions): survivors and movers into the next table
 #pragma unroll
         for (int j = 0; j < RA; j++) {
             const int i = tid + j * TT;
             if (__all_sync(FULL_MASK, i >= na)) break;
             const bool in_tile = i < na;
-            const uint8_t code = pc[j];
+            const uint32_t code = pc[j];
             const int k = code & 7;
             if (genetics) {
                 // the genome slot of an agent dying this step goes to the next free list
@@ -1160,9 +1083,13 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                 }
             }
             if (!in_tile) continue;
-            const int lc = S.cell[i];
+            const int lc = (int)((code >> 8) & 511u);
+            if (lc >= nc) {   // inconsistent outcome word: record, never index past the tile
+                set_error(rs, kErrInternal, 7u);
+                continue;
+            }
             if (k) {
-                const uint32_t dst = ((k == 1) ? S.sb[lc] : S.ob[lc][k - 2]) + S.rank[i];
+                const uint32_t dst = ((k == 1) ? S.sb[lc] : S.ob[lc][k - 2]) + (code >> 17);
                 if (dst >= cap) {   // inconsistent bases: record, never write out of range
                     set_error(rs, kErrInternal, 3u);
                 } else {
@@ -1176,7 +1103,7 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                     if (genetics) gslot2[dst] = pg[j];
                 }
             }
-            if (code & kOutBirth) S.brow[atomicAdd(&S.nb, 1u)] = (uint16_t)i;
+            if (code & kOutBirth) S.brow[atomicAdd(&S.nb, 1u)] = (uint32_t)i | ((uint32_t)lc << 16);
         }
         __syncthreads();
         // newborns, one thread per mother (SPopulation::createAgentAtIndex,
@@ -1184,9 +1111,9 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
         // mother's birth stream, females start FERTILE
         const uint32_t nbt = S.nb;
         for (uint32_t q = tid; q < nbt; q += TT) {
-            const int i = S.brow[q];
+            const int i = (int)(S.brow[q] & 0xffffu);
             const uint32_t row = a0 + (uint32_t)i;
-            const int lc = S.cell[i];
+            const int lc = (int)(S.brow[q] >> 16);
             const uint32_t rk = brank[row];
             const uint32_t dst = S.bb[lc] + rk;
             const int32_t fr = father[row];
