@@ -23,6 +23,10 @@ extern "C" void qhg_tile_ctas_per_sm(int *actions, int *scatter);
 extern "C" int qhg_match_program(const int32_t *types, int n);
 extern "C" int qhg_launch_gather_genomes(const int32_t *gslot, const uint64_t *genome, uint32_t n, int words,
                                          uint32_t slots, uint64_t *out, cudaStream_t stream);
+extern "C" int qhg_launch_upload(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
+                                 const int32_t *cell, const uint8_t *gender, const uint8_t *state, const int64_t *sid,
+                                 const float *sbirth, const float *sage, const float *slastb, int64_t n,
+                                 int32_t *gslot_out, cudaStream_t stream);
 extern "C" int qhg_launch_step_timed(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
                                      const qhg::BatchBuffers *BB, const qhg::LaunchShape *L, cudaStream_t stream,
                                      cudaEvent_t *ev);
@@ -132,29 +136,6 @@ static uint64_t host_prob_threshold(double x) {
     double y = x * 4294967296.0;
     if (y >= 4294967296.0) return 4294967296ull;
     return (uint64_t)std::ceil(y);
-}
-
-// the thresholds the device computes in verhulst_thresholds(), for the first
-// step after an upload (same expressions, same rounding)
-static ulonglong2 host_verhulst_thresholds(const StepConst &P, double Kcell, uint32_t n) {
-    const ActionConst &A = P.act[P.verhulst_act[0]];
-    double B, D;
-    const double K = (A.type == kVerhulst) ? A.K : Kcell;
-    if (A.type == kVerhulstVarK && K <= 0.0) {
-        B = 0.0;
-        D = 1.0;
-    } else {
-        const double r = (double)n / K;
-        B = A.b0 + A.th_b0 * r;
-        D = A.d0 + A.th_d0 * r;
-    }
-    uint64_t x = 0;
-    if (B > 0.0) x = host_prob_threshold(B) | (1ull << 62);
-    else if (B < 0.0) x = host_prob_threshold(-B) | (2ull << 62);
-    ulonglong2 v;
-    v.x = x;
-    v.y = host_prob_threshold(D);
-    return v;
 }
 
 // largest float f with (double)f <= x
@@ -555,6 +536,11 @@ static int alloc_agents(qhg_run *r, uint32_t cap) {
     return QHG_OK;
 }
 
+static StepBuffers make_buffers(qhg_run *r, int cur);
+
+// Uploads are sorted by cell on the device (k_upload_count, k_cell_scan,
+// k_upload_place): the caller's columns are copied as they are, with the
+// next table's buffers as staging.
 extern "C" int qhg_gpu_upload_agents(qhg_run *r, const qhg_agents_soa *a, int64_t n, int32_t first_step) {
     if (r == nullptr || a == nullptr || n < 0) return fail(QHG_ERR_ARG, "bad agent arguments");
     if (!r->grid_ok) return fail(QHG_ERR_STATE, "upload the grid before the agents");
@@ -566,122 +552,81 @@ extern "C" int qhg_gpu_upload_agents(qhg_run *r, const qhg_agents_soa *a, int64_
     if (first_step < 0) return fail(QHG_ERR_ARG, "negative first step");
     CUDA_TRY(cudaSetDevice(r->desc.device));
     const int C = r->C;
-    // live rows, ordered by (cell, id)
-    std::vector<uint32_t> cnt((size_t)C + 1, 0);
-    int64_t live = 0;
-    int64_t maxid = -1;
-    uint32_t max_cell = 0;
-    for (int64_t i = 0; i < n; i++) {
-        if (a->state[i] == 0) continue;
-        const int32_t c = a->cell[i];
-        if (c < 0 || c >= C) return fail(QHG_ERR_ARG, "agent cell out of range");
-        cnt[(size_t)c + 1]++;
-        live++;
-        maxid = std::max<int64_t>(maxid, a->id[i]);
-    }
-    for (int c = 0; c < C; c++) {
-        if (cnt[(size_t)c + 1] > (uint32_t)kMaxCellBig) {
-            return fail(QHG_ERR_CELL_TOO_LARGE, "a cell holds more than QHG_MAX_CELL_AGENTS agents");
-        }
-        max_cell = std::max(max_cell, cnt[(size_t)c + 1]);
-        cnt[(size_t)c + 1] += cnt[(size_t)c];
-    }
-    uint64_t want = r->desc.agent_capacity > 0 ? (uint64_t)r->desc.agent_capacity : (uint64_t)live * 4 + 65536;
-    if (want < (uint64_t)live) want = (uint64_t)live;
+    // the capacity also holds the staged input rows (dead ones included)
+    uint64_t want = r->desc.agent_capacity > 0 ? (uint64_t)r->desc.agent_capacity : (uint64_t)n * 4 + 65536;
+    if (want < (uint64_t)n) want = (uint64_t)n;
     if (want > 0x7fffffffull) return fail(QHG_ERR_CAPACITY, "agent capacity above 2^31-1");
-    // rows grouped by cell, input order kept within a cell (counting sort)
-    std::vector<int64_t> order((size_t)live);
-    {
-        std::vector<uint32_t> pos(cnt.begin(), cnt.end() - 1);
-        for (int64_t i = 0; i < n; i++) {
-            if (a->state[i] == 0) continue;
-            order[pos[a->cell[i]]++] = i;
-        }
-    }
-    std::vector<int64_t> h_id((size_t)live);
-    std::vector<float> h_birth((size_t)live), h_age((size_t)live), h_lastb((size_t)live);
-    std::vector<uint8_t> h_meta((size_t)live);
-    for (int64_t k = 0; k < live; k++) {
-        const int64_t i = order[(size_t)k];
-        h_id[(size_t)k] = a->id[i];
-        h_birth[(size_t)k] = a->birth[i];
-        h_age[(size_t)k] = a->age[i];
-        h_lastb[(size_t)k] = a->last_birth[i];
-        h_meta[(size_t)k] = (uint8_t)((a->gender[i] & 1u) | (a->state[i] == QHG_LS_FERTILE ? kMetaFertile : 0));
-    }
-    std::vector<uint32_t> ne, nes;
-    for (int c = 0; c < C; c++) {
-        if (cnt[(size_t)c + 1] != cnt[(size_t)c]) {
-            ne.push_back((uint32_t)c);
-            nes.push_back(cnt[(size_t)c]);
-        }
-    }
-    nes.push_back((uint32_t)live);
-    // first non-empty cell of each tile (tile t starts at row t * kTileAgents)
-    const uint32_t ntl = (uint32_t)((live + kTileAgents - 1) / kTileAgents);
-    std::vector<uint32_t> tf((size_t)ntl + 1);
-    {
-        uint32_t r = 0;
-        for (uint32_t t = 0; t <= ntl; t++) {
-            const uint64_t row = (uint64_t)t * kTileAgents;
-            while (r < ne.size() && nes[r] < row) r++;
-            tf[t] = r;
-        }
-    }
     drop_graphs(r);
     r->agents_ok = false;
     if (r->cap != (uint32_t)want || r->d_id[0] == nullptr) {
         int rc = alloc_agents(r, (uint32_t)want);
         if (rc != QHG_OK) return rc;
     }
-    r->cur = 0;
-    r->upload_step = first_step;
-    if (live > 0) {
-        CUDA_TRY(cudaMemcpyAsync(r->d_id[0], h_id.data(), live * sizeof(int64_t), cudaMemcpyHostToDevice, r->stream));
-        CUDA_TRY(cudaMemcpyAsync(r->d_birth[0], h_birth.data(), live * sizeof(float), cudaMemcpyHostToDevice, r->stream));
-        CUDA_TRY(cudaMemcpyAsync(r->d_age[0], h_age.data(), live * sizeof(float), cudaMemcpyHostToDevice, r->stream));
-        CUDA_TRY(cudaMemcpyAsync(r->d_lastb[0], h_lastb.data(), live * sizeof(float), cudaMemcpyHostToDevice, r->stream));
-        CUDA_TRY(cudaMemcpyAsync(r->d_meta[0], h_meta.data(), live, cudaMemcpyHostToDevice, r->stream));
-    }
-    if (!ne.empty()) {
-        CUDA_TRY(cudaMemcpyAsync(r->d_ne[0], ne.data(), ne.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, r->stream));
-    }
-    CUDA_TRY(cudaMemcpyAsync(r->d_nes[0], nes.data(), nes.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, r->stream));
-    CUDA_TRY(cudaMemcpyAsync(r->d_tf[0], tf.data(), tf.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, r->stream));
-    std::vector<uint64_t> h_gen;
-    std::vector<int32_t> h_gslot;
-    if (r->P.genome_words > 0 && live > 0) {
-        // row k of the sorted table owns genome slot k
-        const size_t gw = (size_t)r->P.genome_words;
-        h_gen.resize((size_t)live * gw);
-        h_gslot.resize((size_t)live);
-        for (int64_t k = 0; k < live; k++) {
-            memcpy(&h_gen[(size_t)k * gw], a->genome + (size_t)order[(size_t)k] * gw, gw * sizeof(uint64_t));
-            h_gslot[(size_t)k] = (int32_t)k;
+    cudaStream_t st = r->stream;
+    // staging: table 1's columns, the father column for cells, the birth-rank
+    // column for gender and state
+    int32_t *s_cell = r->d_father;
+    uint8_t *s_gender = reinterpret_cast<uint8_t *>(r->d_brank);
+    uint8_t *s_state = s_gender + r->cap;
+    if (n > 0) {
+        CUDA_TRY(cudaMemcpyAsync(r->d_id[1], a->id, n * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(r->d_birth[1], a->birth, n * sizeof(float), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(r->d_age[1], a->age, n * sizeof(float), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(r->d_lastb[1], a->last_birth, n * sizeof(float), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(s_cell, a->cell, n * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(s_gender, a->gender, n, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(s_state, a->state, n, cudaMemcpyHostToDevice, st));
+        if (r->P.genome_words > 0) {
+            // genome slot = input row
+            CUDA_TRY(cudaMemcpyAsync(r->d_genome, a->genome, (size_t)n * r->P.genome_words * sizeof(uint64_t),
+                                     cudaMemcpyHostToDevice, st));
         }
-        CUDA_TRY(cudaMemcpyAsync(r->d_genome, h_gen.data(), h_gen.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, r->stream));
-        CUDA_TRY(cudaMemcpyAsync(r->d_gslot[0], h_gslot.data(), live * sizeof(int32_t), cudaMemcpyHostToDevice, r->stream));
     }
-    std::vector<ulonglong2> vthr;
-    if (r->P.n_verhulst > 0) {
-        vthr.resize(C);
-        for (int c = 0; c < C; c++) vthr[c] = host_verhulst_thresholds(r->P, r->h_K[c], cnt[(size_t)c + 1] - cnt[c]);
-        CUDA_TRY(cudaMemcpyAsync(r->d_vthr, vthr.data(), (size_t)C * sizeof(ulonglong2), cudaMemcpyHostToDevice, r->stream));
-    }
-    CUDA_TRY(cudaMemsetAsync(r->d_clsc, 0, (size_t)C * kCls * sizeof(uint32_t), r->stream));
     memset(r->h_rs, 0, sizeof(RunState));
     r->h_rs->step = first_step;
-    r->h_rs->n_agents = (uint32_t)live;
-    r->h_rs->next_id = maxid + 1;
-    r->upload_max_id = maxid;
-    r->h_rs->n_nonempty = (uint32_t)ne.size();
-    r->h_rs->hwm = (uint32_t)live;
-    r->h_rs->big = max_cell > (uint32_t)kMaxCell ? 1u : 0u;
-    r->h_rs->big_next = r->h_rs->big;
-    CUDA_TRY(cudaMemcpyAsync(r->d_rs, r->h_rs, sizeof(RunState), cudaMemcpyHostToDevice, r->stream));
+    r->h_rs->next_id = -1;   // the largest ID, by the count kernel
+    CUDA_TRY(cudaMemcpyAsync(r->d_rs, r->h_rs, sizeof(RunState), cudaMemcpyHostToDevice, st));
     const int ntiles = (C + kScanTile - 1) / kScanTile;
-    CUDA_TRY(cudaMemsetAsync(r->d_tflag, 0, (size_t)ntiles * sizeof(uint32_t), r->stream));
-    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    CUDA_TRY(cudaMemsetAsync(r->d_tflag, 0, (size_t)ntiles * sizeof(uint32_t), st));
+    CUDA_TRY(cudaMemsetAsync(r->d_clsc, 0, (size_t)C * kCls * sizeof(uint32_t), st));
+    // the scan writes the lists of the table in buffer 0 ("next" of buffer 1)
+    StepBuffers B = make_buffers(r, 1);
+    int le = qhg_launch_upload(&r->P, r->d_rs, &B, s_cell, s_gender, s_state, r->d_id[1], r->d_birth[1],
+                               r->d_age[1], r->d_lastb[1], n, r->P.genome_words > 0 ? r->d_gslot[0] : nullptr, st);
+    if (le != 0) return fail(QHG_ERR_CUDA, std::string("upload: ") + cudaGetErrorString((cudaError_t)le));
+    CUDA_TRY(cudaMemcpyAsync(r->h_rs, r->d_rs, sizeof(RunState), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    RunState *h = r->h_rs;
+    if (h->error != 0u) {
+        const uint32_t code = h->error;
+        memset(h, 0, sizeof(RunState));
+        CUDA_TRY(cudaMemcpyAsync(r->d_rs, h, sizeof(RunState), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemsetAsync(r->d_clsc, 0, (size_t)C * kCls * sizeof(uint32_t), st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        if (code == kErrBadCell) return fail(QHG_ERR_ARG, "agent cell out of range");
+        if (code == kErrCellTooLarge) return fail(QHG_ERR_CELL_TOO_LARGE, "a cell holds more than QHG_MAX_CELL_AGENTS agents");
+        if (code == kErrCapacity) return fail(QHG_ERR_CAPACITY, "agents exceed the capacity");
+        return fail(QHG_ERR_DEVICE, "upload failed on the device");
+    }
+    // commit the uploaded table as the current one
+    const int64_t maxid = h->next_id;
+    const uint32_t live = h->new_n_agents;
+    const uint32_t nne = h->new_n_nonempty;
+    const uint32_t big = h->max_cell > (uint32_t)kMaxCell ? 1u : 0u;
+    memset(h, 0, sizeof(RunState));
+    h->step = first_step;
+    h->n_agents = live;
+    h->n_nonempty = nne;
+    h->next_id = maxid + 1;
+    h->hwm = (uint32_t)n;
+    h->big = big;
+    h->big_next = big;
+    CUDA_TRY(cudaMemcpyAsync(r->d_rs, h, sizeof(RunState), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemsetAsync(r->d_tflag, 0, (size_t)ntiles * sizeof(uint32_t), st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    r->cur = 0;
+    r->upload_step = first_step;
+    r->upload_max_id = maxid;
     r->agents_ok = true;
     return QHG_OK;
 }

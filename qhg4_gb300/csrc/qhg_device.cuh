@@ -69,7 +69,7 @@ enum ActionType : int32_t {
 };
 
 enum ErrorCode : uint32_t {
-    kErrNone = 0, kErrCellTooLarge = 1, kErrTimeout = 2, kErrCapacity = 3, kErrInternal = 4
+    kErrNone = 0, kErrCellTooLarge = 1, kErrTimeout = 2, kErrCapacity = 3, kErrInternal = 4, kErrBadCell = 5
 };
 
 // constants of one action, prepared on the host

@@ -1395,6 +1395,61 @@ k_inject(RunState *__restrict__ rs, const BatchBuffers BB, int64_t *__restrict__
     }
 }
 
+// ------------------------------------------------------------------ upload
+// An upload on the device: the caller's columns are copied as they are into
+// staging buffers; k_upload_count counts the live agents of each cell (into
+// the class-count slot 0 of the cell, as if they all stayed), k_cell_scan
+// lays out the table from those counts exactly as after a step (first rows,
+// non-empty cells, tiles, Verhulst thresholds), and k_upload_place puts each
+// agent at its cell's first row + a countdown of the cell's count (which
+// leaves the counts at zero, as a step's scatter does).  The order of the
+// agents within a cell is arbitrary: nothing depends on it.
+__global__ void k_upload_count(RunState *__restrict__ rs, const int32_t *__restrict__ cell,
+                               const uint8_t *__restrict__ state, const int64_t *__restrict__ id, int64_t n,
+                               int C, uint32_t *__restrict__ clsc) {
+    long long mx = -1;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t q = base + threadIdx.x;
+        bool live = false;
+        int32_t c = 0;
+        if (q < n && state[q] != 0) {
+            c = cell[q];
+            if (c < 0 || c >= C) set_error(rs, kErrBadCell, (uint32_t)q);
+            else live = true;
+            mx = max(mx, (long long)id[q]);
+        }
+        warp_agg_add(live, live ? (uint32_t)c : 0u, &clsc[(size_t)(live ? c : 0) * kCls], 1u);
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, (long long)__shfl_down_sync(FULL_MASK, mx, o));
+    if ((threadIdx.x & 31) == 0 && mx >= 0) atomicMax(reinterpret_cast<long long *>(&rs->next_id), mx);
+}
+
+__global__ void k_upload_place(RunState *__restrict__ rs, const int32_t *__restrict__ cell,
+                               const uint8_t *__restrict__ gender, const uint8_t *__restrict__ state,
+                               const int64_t *__restrict__ sid, const float *__restrict__ sbirth,
+                               const float *__restrict__ sage, const float *__restrict__ slastb, int64_t n,
+                               uint32_t cap, const uint32_t *__restrict__ sbase, uint32_t *__restrict__ clsc,
+                               int64_t *__restrict__ id, float *__restrict__ birth, float *__restrict__ age,
+                               float *__restrict__ lastb, uint8_t *__restrict__ meta, int32_t *__restrict__ gslot) {
+    if (rs->error != 0u) return;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const uint8_t st = state[q];
+        if (st == 0) continue;
+        const int32_t c = cell[q];
+        const uint32_t pos = sbase[c] + atomicSub(&clsc[(size_t)c * kCls], 1u) - 1u;
+        if (pos >= cap) {
+            set_error(rs, kErrCapacity, pos);
+            continue;
+        }
+        id[pos] = sid[q];
+        birth[pos] = sbirth[q];
+        age[pos] = sage[q];
+        lastb[pos] = slastb[q];
+        meta[pos] = (uint8_t)((gender[q] & 1u) | (st == 5 ? kMetaFertile : 0));
+        if (gslot) gslot[pos] = (int32_t)q;   // genome slot = input row
+    }
+}
+
 // genomes of the table's rows in row order (download)
 __global__ void k_gather_genomes(const int32_t *__restrict__ gslot, const uint64_t *__restrict__ genome,
                                  uint32_t n, int words, uint32_t slots, uint64_t *__restrict__ out) {
@@ -1435,6 +1490,29 @@ extern "C" int qhg_launch_run_cells(const uint32_t *nonempty, const uint32_t *ne
     if (blocks > 0) {
         qhg::k_run_cells<<<blocks, 256, 0, stream>>>(nonempty, ne_start, n_nonempty, cell0, cell1, row0, nrows,
                                                      row_cell, counts);
+    }
+    return (int)cudaGetLastError();
+}
+
+extern "C" int qhg_launch_upload(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
+                                 const int32_t *cell, const uint8_t *gender, const uint8_t *state, const int64_t *sid,
+                                 const float *sbirth, const float *sage, const float *slastb, int64_t n,
+                                 int32_t *gslot_out, cudaStream_t stream) {
+    using namespace qhg;
+    const int ntiles = (P->num_cells + kScanTile - 1) / kScanTile;
+    const int64_t blk = std::min<int64_t>((n + 255) / 256, 65535);
+    if (n > 0) {
+        k_upload_count<<<(unsigned)blk, 256, 0, stream>>>(rs, cell, state, sid, n, P->num_cells, B->clsc);
+    }
+    BatchBuffers BB;
+    memset(&BB, 0, sizeof(BB));
+    k_cell_scan<false><<<ntiles, kScanThreads, 0, stream>>>(
+        *P, BB, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr, B->sbase, B->bbase, B->bidbase,
+        B->obase, B->nonempty2, B->ne_start2, B->tile_first2, B->tile_flag, B->tile_agg, B->tile_incl);
+    if (n > 0) {
+        k_upload_place<<<(unsigned)blk, 256, 0, stream>>>(rs, cell, gender, state, sid, sbirth, sage, slastb, n,
+                                                        P->capacity, B->sbase, B->clsc, B->id2, B->birth2,
+                                                        B->age2, B->lastb2, B->meta2, gslot_out);
     }
     return (int)cudaGetLastError();
 }
