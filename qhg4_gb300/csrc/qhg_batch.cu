@@ -97,7 +97,9 @@ struct qhg_batch {
     int64_t *d_rnext = nullptr;
     uint32_t *d_rstat = nullptr;
     // admission
-    uint32_t *d_inj = nullptr, *d_istart = nullptr, *d_ibase = nullptr, *d_injdone = nullptr;
+    uint32_t *d_inj = nullptr, *d_ibase = nullptr, *d_injdone = nullptr;
+    uint8_t *d_sgender = nullptr;
+    unsigned long long *d_stage_err = nullptr;
     uint32_t *d_cstat = nullptr;
     int64_t *d_sid = nullptr;
     float *d_sbirth = nullptr, *d_sage = nullptr, *d_slastb = nullptr;
@@ -156,7 +158,6 @@ BatchBuffers make_batch_buffers(qhg_batch *b) {
     BB.rstat = b->d_rstat;
     BB.nruns = b->max_runs;
     BB.inj = b->d_inj;
-    BB.istart = b->d_istart;
     BB.ibase = b->d_ibase;
     BB.sid = b->d_sid; BB.sbirth = b->d_sbirth; BB.sage = b->d_sage; BB.slastb = b->d_slastb;
     BB.smeta = b->d_smeta; BB.scell = b->d_scell;
@@ -300,7 +301,8 @@ extern "C" int qhg_batch_create(const qhg_batch_desc *desc, qhg_batch **out) {
     A((void **)&b->d_rnext, R * sizeof(int64_t));
     A((void **)&b->d_rstat, R * kBatchRing * 4 * sizeof(uint32_t));
     A((void **)&b->d_inj, C * sizeof(uint32_t));
-    A((void **)&b->d_istart, C * sizeof(uint32_t));
+    A((void **)&b->d_sgender, S);
+    A((void **)&b->d_stage_err, 4 * sizeof(unsigned long long));
     A((void **)&b->d_ibase, C * sizeof(uint32_t));
     A((void **)&b->d_injdone, sizeof(uint32_t));
     A((void **)&b->d_cstat, C * sizeof(uint32_t));
@@ -390,48 +392,11 @@ extern "C" int qhg_batch_add_run(qhg_batch *b, const qhg_batch_run_desc *rd, con
     }
     std::vector<int32_t> gnbr((size_t)C * 6);
     for (size_t q = 0; q < gnbr.size(); q++) gnbr[q] = nbr6[q] >= 0 ? nbr6[q] + (int32_t)c0 : -1;
-    // agents: live rows grouped by cell (input order kept within a cell)
-    std::vector<uint32_t> cnt((size_t)C + 1, 0);
-    int64_t live = 0, maxid = -1;
-    for (int64_t i = 0; i < n; i++) {
-        if (a->state[i] == 0) continue;
-        const int32_t c = a->cell[i];
-        if (c < 0 || c >= num_cells) return bfail(QHG_ERR_ARG, "agent cell out of range");
-        cnt[(size_t)c + 1]++;
-        live++;
-        maxid = std::max<int64_t>(maxid, a->id[i]);
-    }
-    for (uint32_t c = 0; c < C; c++) {
-        if (cnt[(size_t)c + 1] > (uint32_t)kMaxCellBig) {
-            return bfail(QHG_ERR_CELL_TOO_LARGE, "a cell holds more than QHG_MAX_CELL_AGENTS agents");
-        }
-        cnt[(size_t)c + 1] += cnt[c];
-    }
-    if ((uint64_t)b->staged + (uint64_t)live > b->stage_cap) {
+    // agents: staged as given; k_batch_stage counts them per cell on the device
+    if ((uint64_t)b->staged + (uint64_t)n > b->stage_cap) {
         return bfail(QHG_ERR_CAPACITY, "staging area full: step the batch before admitting more agents");
     }
     const uint32_t s0 = b->staged;
-    std::vector<int64_t> sid((size_t)live);
-    std::vector<float> sb((size_t)live), sa((size_t)live), sl((size_t)live);
-    std::vector<uint8_t> sm((size_t)live);
-    std::vector<uint32_t> sc((size_t)live), inj(C, 0u), ist(C, 0u);
-    {
-        std::vector<uint32_t> pos(cnt.begin(), cnt.end() - 1);
-        for (int64_t i = 0; i < n; i++) {
-            if (a->state[i] == 0) continue;
-            const uint32_t k = pos[(size_t)a->cell[i]]++;
-            sid[k] = a->id[i];
-            sb[k] = a->birth[i];
-            sa[k] = a->age[i];
-            sl[k] = a->last_birth[i];
-            sm[k] = (uint8_t)((a->gender[i] & 1u) | (a->state[i] == QHG_LS_FERTILE ? kMetaFertile : 0));
-            sc[k] = c0 + (uint32_t)a->cell[i];
-        }
-        for (uint32_t c = 0; c < C; c++) {
-            inj[c] = cnt[(size_t)c + 1] - cnt[c];
-            ist[c] = s0 + cnt[c];
-        }
-    }
     // the run's constants: its parameters for the batch's action types
     BatchRun R;
     memset(&R, 0, sizeof(R));
@@ -448,7 +413,6 @@ extern "C" int qhg_batch_add_run(qhg_batch *b, const qhg_batch_run_desc *rd, con
     R.active = 1u;
     R.cell0 = c0;
     R.cell1 = c0 + C;
-    const int64_t nid = maxid + 1;
     cudaStream_t st = b->stream;
     BCUDA(cudaMemcpyAsync(b->d_nbr + (size_t)c0 * 6, gnbr.data(), gnbr.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
     BCUDA(cudaMemcpyAsync(b->d_nnbr + c0, nnbr, C, cudaMemcpyHostToDevice, st));
@@ -459,22 +423,41 @@ extern "C" int qhg_batch_add_run(qhg_batch *b, const qhg_batch_run_desc *rd, con
     std::vector<uint32_t> crun(C, (uint32_t)r);
     BCUDA(cudaMemcpyAsync(b->d_crun + c0, crun.data(), C * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
     BCUDA(cudaMemsetAsync(b->d_clsc + (size_t)c0 * kCls, 0, (size_t)C * kCls * sizeof(uint32_t), st));
-    BCUDA(cudaMemcpyAsync(b->d_inj + c0, inj.data(), C * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-    BCUDA(cudaMemcpyAsync(b->d_istart + c0, ist.data(), C * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-    if (live > 0) {
-        BCUDA(cudaMemcpyAsync(b->d_sid + s0, sid.data(), live * sizeof(int64_t), cudaMemcpyHostToDevice, st));
-        BCUDA(cudaMemcpyAsync(b->d_sbirth + s0, sb.data(), live * sizeof(float), cudaMemcpyHostToDevice, st));
-        BCUDA(cudaMemcpyAsync(b->d_sage + s0, sa.data(), live * sizeof(float), cudaMemcpyHostToDevice, st));
-        BCUDA(cudaMemcpyAsync(b->d_slastb + s0, sl.data(), live * sizeof(float), cudaMemcpyHostToDevice, st));
-        BCUDA(cudaMemcpyAsync(b->d_smeta + s0, sm.data(), live, cudaMemcpyHostToDevice, st));
-        BCUDA(cudaMemcpyAsync(b->d_scell + s0, sc.data(), live * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    BCUDA(cudaMemsetAsync(b->d_inj + c0, 0, C * sizeof(uint32_t), st));
+    unsigned long long herr[3] = {0ull, 0ull, ~0ull};   // code, info, largest ID (-1)
+    BCUDA(cudaMemcpyAsync(b->d_stage_err, herr, sizeof(herr), cudaMemcpyHostToDevice, st));
+    if (n > 0) {
+        // the run's rows as given: state in the meta column, gender beside it,
+        // cells in the cell column (turned into the batch's cells in place)
+        BCUDA(cudaMemcpyAsync(b->d_sid + s0, a->id, n * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+        BCUDA(cudaMemcpyAsync(b->d_sbirth + s0, a->birth, n * sizeof(float), cudaMemcpyHostToDevice, st));
+        BCUDA(cudaMemcpyAsync(b->d_sage + s0, a->age, n * sizeof(float), cudaMemcpyHostToDevice, st));
+        BCUDA(cudaMemcpyAsync(b->d_slastb + s0, a->last_birth, n * sizeof(float), cudaMemcpyHostToDevice, st));
+        BCUDA(cudaMemcpyAsync(b->d_smeta + s0, a->state, n, cudaMemcpyHostToDevice, st));
+        BCUDA(cudaMemcpyAsync(b->d_sgender + s0, a->gender, n, cudaMemcpyHostToDevice, st));
+        BCUDA(cudaMemcpyAsync(b->d_scell + s0, a->cell, n * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+        int le = qhg_launch_batch_stage(s0, (uint32_t)n, c0, C, reinterpret_cast<const int32_t *>(b->d_scell + s0),
+                                        b->d_smeta, b->d_sgender, b->d_sid, b->d_scell, b->d_inj, b->d_stage_err,
+                                        st);
+        if (le != 0) return bfail(QHG_ERR_CUDA, std::string("staging: ") + cudaGetErrorString((cudaError_t)le));
     }
+    BCUDA(cudaMemcpyAsync(herr, b->d_stage_err, sizeof(herr), cudaMemcpyDeviceToHost, st));
+    BCUDA(cudaStreamSynchronize(st));
+    if (herr[0] != 0ull) {
+        // nothing of the run stays: its cells' counts back to zero
+        BCUDA(cudaMemsetAsync(b->d_inj + c0, 0, C * sizeof(uint32_t), st));
+        BCUDA(cudaMemsetAsync(b->d_crun + c0, 0xff, C * sizeof(uint32_t), st));
+        BCUDA(cudaStreamSynchronize(st));
+        if (herr[0] == kErrBadCell) return bfail(QHG_ERR_ARG, "agent cell out of range");
+        return bfail(QHG_ERR_CELL_TOO_LARGE, "a cell holds more than QHG_MAX_CELL_AGENTS agents");
+    }
+    const int64_t nid = (int64_t)herr[2] + 1;
     BCUDA(cudaMemcpyAsync(b->d_runs + r, &R, sizeof(BatchRun), cudaMemcpyHostToDevice, st));
     BCUDA(cudaMemcpyAsync(b->d_rnext + r, &nid, sizeof(int64_t), cudaMemcpyHostToDevice, st));
     BCUDA(cudaMemsetAsync(b->d_rstat + (size_t)r * kBatchRing * 4, 0, kBatchRing * 4 * sizeof(uint32_t), st));
     // the host buffers above are freed on return: wait for the copies
     BCUDA(cudaStreamSynchronize(st));
-    b->staged = s0 + (uint32_t)live;
+    b->staged = s0 + (uint32_t)n;
     RunSlot &s = b->slots[(size_t)r];
     s.used = true;
     s.active = true;
@@ -667,10 +650,6 @@ static int run_rows(qhg_batch *b, int32_t run, uint32_t *row0, uint32_t *count) 
     return QHG_OK;
 }
 
-extern "C" int qhg_launch_run_cells(const uint32_t *nonempty, const uint32_t *ne_start, uint32_t n_nonempty,
-                                    uint32_t cell0, uint32_t cell1, uint32_t row0, uint32_t nrows,
-                                    uint32_t *row_cell, uint32_t *counts, cudaStream_t stream);
-
 extern "C" int qhg_batch_download(qhg_batch *b, int32_t run, qhg_agents_soa *o, int64_t cap, int64_t *n) {
     if (b == nullptr || o == nullptr || n == nullptr) return bfail(QHG_ERR_ARG, "null argument");
     int rc = check_slot(b, run);
@@ -815,7 +794,7 @@ extern "C" int qhg_batch_destroy(qhg_batch *b) {
     void *ptrs[] = {b->d_nbr, b->d_nnbr, b->d_rev, b->d_K, b->d_vthr, b->d_wthr, b->d_cmove, b->d_crun,
                     b->d_outc, b->d_father, b->d_brank, b->d_clsc, b->d_sbase, b->d_bbase, b->d_bidb,
                     b->d_obase, b->d_tflag, b->d_tagg, b->d_tincl, b->d_runs, b->d_rnext, b->d_rstat,
-                    b->d_inj, b->d_istart, b->d_ibase, b->d_injdone, b->d_cstat, b->d_sid, b->d_sbirth, b->d_sage,
+                    b->d_inj, b->d_sgender, b->d_stage_err, b->d_ibase, b->d_injdone, b->d_cstat, b->d_sid, b->d_sbirth, b->d_sage,
                     b->d_slastb, b->d_smeta, b->d_scell, b->d_rowcell, b->d_rs};
     for (void *p : ptrs) cudaFree(p);
     for (int p = 0; p < 2; p++) {

@@ -33,6 +33,7 @@ constexpr int kScanTile = kScanThreads * kScanItems;
 constexpr int kStatsRing = 1024;
 constexpr int kBatchRing = 64;           // per-run statistics ring of a batch (steps)
 constexpr uint32_t kNoRun = 0xffffffffu; // run index of a batch cell that belongs to no run
+constexpr uint8_t kStagedDead = 0xffu;   // meta byte of a staged row that is not admitted
 constexpr uint32_t kSpinLimit = 1u << 24;  // bounded waits in the look-back
 
 // random stream bases (Philox counter word 0), see oracle/philox4x32.h
@@ -200,10 +201,9 @@ struct BatchBuffers {
     // per run and ring slot (batch step % kBatchRing): live, births, deaths, moves
     uint32_t *rstat;
     int32_t nruns;              // run slots in use (upper bound of run indices)
-    // admission: staged agents sorted by cell, their count per cell and the
-    // first staged row of each cell; placed by k_inject after the scatter
+    // admission: staged agents (any order), their count per cell; placed by
+    // k_inject after the scatter
     uint32_t *inj;
-    const uint32_t *istart;
     uint32_t *ibase;
     const int64_t *sid; const float *sbirth; const float *sage; const float *slastb;
     const uint8_t *smeta; const uint32_t *scell;

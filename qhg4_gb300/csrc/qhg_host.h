@@ -22,3 +22,10 @@ extern "C" int qhg_launch_step_timed(const qhg::StepConst *P, qhg::RunState *rs,
                                      cudaEvent_t *ev);
 extern "C" void qhg_tile_ctas_per_sm(int *actions, int *scatter);
 extern "C" int qhg_match_program(const int32_t *types, int n);
+
+extern "C" int qhg_launch_batch_stage(uint32_t s0, uint32_t n, uint32_t cell0, uint32_t ncells, const int32_t *cell,
+                                      uint8_t *smeta, const uint8_t *sgender, const int64_t *sid, uint32_t *scell,
+                                      uint32_t *inj, unsigned long long *err, cudaStream_t stream);
+extern "C" int qhg_launch_run_cells(const uint32_t *nonempty, const uint32_t *ne_start, uint32_t n_nonempty,
+                                    uint32_t cell0, uint32_t cell1, uint32_t row0, uint32_t nrows,
+                                    uint32_t *row_cell, uint32_t *counts, cudaStream_t stream);

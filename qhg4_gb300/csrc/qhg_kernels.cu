@@ -601,10 +601,15 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             const uint32_t rank = (q >> (16 * (slot & 1))) & 0xffffu;
             // outcome byte | local cell << 8 | rank in the cell's class << 17
             if (in_tile) outc[a0 + (uint32_t)i] = (uint32_t)oc | ((uint32_t)lc << 8) | (rank << 17);
-            warp_agg_add(in_tile && bflag, ((uint32_t)lc << 3) | 7u, &S.cls[lc][3], 1u << 16);
+            // births are rare: most warps have none and skip the aggregation
+            if (__any_sync(FULL_MASK, in_tile && bflag)) {
+                warp_agg_add(in_tile && bflag, ((uint32_t)lc << 3) | 7u, &S.cls[lc][3], 1u << 16);
+            }
             if (BATCH) {
-                warp_agg_add(in_tile && cls == 0 && !(oc & kOutDropped), (uint32_t)lc, &dm[lc], 1u);
-                warp_agg_add(in_tile && (oc & kOutMoved), (uint32_t)lc, &dm[lc], 1u << 16);
+                const bool died = in_tile && cls == 0 && !(oc & kOutDropped);
+                const bool moved = in_tile && (oc & kOutMoved);
+                if (__any_sync(FULL_MASK, died)) warp_agg_add(died, (uint32_t)lc, &dm[lc], 1u);
+                if (__any_sync(FULL_MASK, moved)) warp_agg_add(moved, (uint32_t)lc, &dm[lc], 1u << 16);
             }
         }
         __syncthreads();
@@ -1074,7 +1079,7 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             const bool in_tile = i < na;
             const uint32_t code = pc[j];
             const int k = code & 7;
-            if (genetics) {
+            if (genetics && __any_sync(FULL_MASK, in_tile && k == 0)) {
                 // the genome slot of an agent dying this step goes to the next free list
                 const uint32_t q = warp_agg_add(in_tile && k == 0, 0u, &rs->dead_count, 1u);
                 if (in_tile && k == 0) {
@@ -1369,9 +1374,11 @@ k_inject(RunState *__restrict__ rs, const BatchBuffers BB, int64_t *__restrict__
     const uint32_t n = rs->n_staged;
     if (n == 0u) return;
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const uint8_t m = BB.smeta[q];
+        if (m == kStagedDead) continue;
         const uint32_t d = BB.scell[q];
-        const uint32_t first = BB.istart[d];
-        const uint32_t dst = BB.ibase[d] + (q - first);
+        // a countdown of the cell's admitted agents (which leaves it at zero)
+        const uint32_t dst = BB.ibase[d] + atomicSub(&BB.inj[d], 1u) - 1u;
         if (dst >= cap) {
             set_error(rs, kErrCapacity, dst);
             continue;
@@ -1380,8 +1387,7 @@ k_inject(RunState *__restrict__ rs, const BatchBuffers BB, int64_t *__restrict__
         birth2[dst] = BB.sbirth[q];
         age2[dst] = BB.sage[q];
         lastb2[dst] = BB.slastb[q];
-        meta2[dst] = BB.smeta[q];
-        if (q == first) BB.inj[d] = 0u;
+        meta2[dst] = m;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -1393,6 +1399,46 @@ k_inject(RunState *__restrict__ rs, const BatchBuffers BB, int64_t *__restrict__
             __threadfence();
         }
     }
+}
+
+// Batches: prepares agents staged as the caller gave them (rows s0..s0+n of
+// the staging area, with the state in smeta and the gender in sgender):
+// meta byte, cell in the batch's cell space, per-cell counts of the
+// admitted agents (inj), the largest ID.  err = {code, info, max ID}.
+__global__ void k_batch_stage(uint32_t s0, uint32_t n, uint32_t cell0, uint32_t ncells,
+                              const int32_t *__restrict__ cell, uint8_t *__restrict__ smeta,
+                              const uint8_t *__restrict__ sgender, const int64_t *__restrict__ sid,
+                              uint32_t *__restrict__ scell, uint32_t *__restrict__ inj,
+                              unsigned long long *__restrict__ err) {
+    long long mx = -1;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t k = base + threadIdx.x;
+        bool live = false;
+        uint32_t d = 0;
+        if (k < n) {
+            const uint32_t q = s0 + k;
+            const uint8_t st = smeta[q];
+            if (st == 0) {
+                smeta[q] = kStagedDead;
+            } else {
+                const int32_t c = cell[k];
+                if (c < 0 || (uint32_t)c >= ncells) {
+                    atomicCAS(&err[0], 0ull, (unsigned long long)kErrBadCell);
+                    smeta[q] = kStagedDead;
+                } else {
+                    live = true;
+                    d = cell0 + (uint32_t)c;
+                    scell[q] = d;
+                    smeta[q] = (uint8_t)((sgender[q] & 1u) | (st == 5 ? kMetaFertile : 0));
+                    mx = max(mx, (long long)sid[q]);
+                }
+            }
+        }
+        const uint32_t pos = warp_agg_add(live, d, &inj[live ? d : 0], 1u);
+        if (live && pos >= (uint32_t)kMaxCellBig) atomicCAS(&err[0], 0ull, (unsigned long long)kErrCellTooLarge);
+    }
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, (long long)__shfl_down_sync(FULL_MASK, mx, o));
+    if ((threadIdx.x & 31) == 0 && mx >= 0) atomicMax(reinterpret_cast<long long *>(&err[2]), mx);
 }
 
 // ------------------------------------------------------------------ upload
@@ -1490,6 +1536,16 @@ extern "C" int qhg_launch_run_cells(const uint32_t *nonempty, const uint32_t *ne
     if (blocks > 0) {
         qhg::k_run_cells<<<blocks, 256, 0, stream>>>(nonempty, ne_start, n_nonempty, cell0, cell1, row0, nrows,
                                                      row_cell, counts);
+    }
+    return (int)cudaGetLastError();
+}
+
+extern "C" int qhg_launch_batch_stage(uint32_t s0, uint32_t n, uint32_t cell0, uint32_t ncells, const int32_t *cell,
+                                      uint8_t *smeta, const uint8_t *sgender, const int64_t *sid, uint32_t *scell,
+                                      uint32_t *inj, unsigned long long *err, cudaStream_t stream) {
+    const uint32_t blk = std::min<uint32_t>((n + 255) / 256, 65535u);
+    if (blk > 0) {
+        qhg::k_batch_stage<<<blk, 256, 0, stream>>>(s0, n, cell0, ncells, cell, smeta, sgender, sid, scell, inj, err);
     }
     return (int)cudaGetLastError();
 }
