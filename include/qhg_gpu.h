@@ -154,6 +154,14 @@ int qhg_gpu_birth_log(qhg_run *run, int64_t *baby, int64_t *mother, int64_t *fat
  * must exceed every live agent's ID; set it after the upload, before a step. */
 int qhg_gpu_next_id(qhg_run *run, int64_t *next_id);
 int qhg_gpu_set_next_id(qhg_run *run, int64_t next_id);
+/* For tests of failure detection: the next step's cell scan withholds the
+ * status of scan tile `tile` (cells tile*512 ..), so that the look-back of
+ * the tile after it waits until its limit (about one second), gives up and
+ * the step fails with QHG_ERR_TIMEOUT -- reported by the next qhg_gpu_sync;
+ * the run keeps its last step and can be stepped again.  Nothing faults or
+ * hangs: every device-side wait of the library is bounded this way.  The
+ * grid must have more than 512 cells; tile < (cells + 511) / 512 - 1. */
+int qhg_gpu_test_stall_scan(qhg_run *run, int32_t tile);
 /* the run's CUDA stream (cudaStream_t) */
 int qhg_gpu_stream(qhg_run *run, void **stream);
 int qhg_gpu_destroy(qhg_run *run);

@@ -59,7 +59,7 @@ struct qhg_run {
     uint8_t *d_nnbr = nullptr;
     uint32_t *d_rev = nullptr;
     double *d_K = nullptr;
-    ulonglong2 *d_vthr = nullptr;   // per-cell Verhulst thresholds of the coming step
+    ulonglong2 *d_vthr[2] = {nullptr, nullptr};   // per-cell Verhulst thresholds, per table
     std::vector<double> h_K;
     uint64_t *d_wthr = nullptr;
     uint32_t *d_cmove = nullptr;
@@ -455,11 +455,11 @@ extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_
             return fail(QHG_ERR_ARG, err);
         }
     }
-    cudaFree(r->d_nbr); cudaFree(r->d_nnbr); cudaFree(r->d_rev); cudaFree(r->d_K); cudaFree(r->d_vthr);
+    cudaFree(r->d_nbr); cudaFree(r->d_nnbr); cudaFree(r->d_rev); cudaFree(r->d_K); cudaFree(r->d_vthr[0]); cudaFree(r->d_vthr[1]);
     cudaFree(r->d_wthr); cudaFree(r->d_cmove);
     cudaFree(r->d_clsc); cudaFree(r->d_sbase); cudaFree(r->d_bbase); cudaFree(r->d_bidb);
     cudaFree(r->d_obase); cudaFree(r->d_tflag); cudaFree(r->d_tagg); cudaFree(r->d_tincl);
-    r->d_vthr = nullptr;
+    r->d_vthr[0] = r->d_vthr[1] = nullptr;
     r->grid_ok = false;
     r->agents_ok = false;
     drop_graphs(r);
@@ -468,7 +468,8 @@ extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_
     CUDA_TRY(cudaMalloc(&r->d_nnbr, (size_t)C));
     CUDA_TRY(cudaMalloc(&r->d_rev, (size_t)C * sizeof(uint32_t)));
     CUDA_TRY(cudaMalloc(&r->d_K, (size_t)C * sizeof(double)));
-    CUDA_TRY(cudaMalloc(&r->d_vthr, (size_t)C * sizeof(ulonglong2)));
+    CUDA_TRY(cudaMalloc(&r->d_vthr[0], (size_t)C * sizeof(ulonglong2)));
+    CUDA_TRY(cudaMalloc(&r->d_vthr[1], (size_t)C * sizeof(ulonglong2)));
     CUDA_TRY(cudaMalloc(&r->d_wthr, (size_t)C * 6 * sizeof(uint64_t)));
     CUDA_TRY(cudaMalloc(&r->d_cmove, (size_t)C * sizeof(uint32_t)));
     CUDA_TRY(cudaMalloc(&r->d_clsc, (size_t)C * kCls * sizeof(uint32_t)));
@@ -642,7 +643,7 @@ static StepBuffers make_buffers(qhg_run *r, int cur) {
     B.nonempty2 = r->d_ne[nx]; B.ne_start2 = r->d_nes[nx]; B.tile_first2 = r->d_tf[nx];
     B.id2 = r->d_id[nx]; B.birth2 = r->d_birth[nx]; B.age2 = r->d_age[nx]; B.lastb2 = r->d_lastb[nx];
     B.meta2 = r->d_meta[nx];
-    B.nbr = r->d_nbr; B.nnbr = r->d_nnbr; B.rev = r->d_rev; B.K = r->d_K; B.vthr = r->d_vthr; B.wthr = r->d_wthr;
+    B.nbr = r->d_nbr; B.nnbr = r->d_nnbr; B.rev = r->d_rev; B.K = r->d_K; B.vthr = r->d_vthr[cur]; B.vthr2 = r->d_vthr[nx]; B.wthr = r->d_wthr;
     B.cmove = r->d_cmove;
     B.outc = r->d_outc; B.father = r->d_father; B.brank = r->d_brank; B.clsc = r->d_clsc;
     B.sbase = r->d_sbase; B.bbase = r->d_bbase; B.bidbase = r->d_bidb; B.obase = r->d_obase;
@@ -740,6 +741,7 @@ static int pull_state(qhg_run *r) {
         r->h_rs->scatter_tiles = 0u;
         r->h_rs->dead_count = 0u;
         r->h_rs->max_cell = 0u;
+        r->h_rs->stall_tile = 0u;
         // the failed step's partial statistics would be counted again on retry
         unsigned long long *st = r->h_rs->stats[(uint32_t)r->h_rs->step % kStatsRing];
         st[0] = st[1] = st[2] = st[3] = 0ull;
@@ -899,6 +901,18 @@ extern "C" int qhg_gpu_set_next_id(qhg_run *r, int64_t next_id) {
     return QHG_OK;
 }
 
+extern "C" int qhg_gpu_test_stall_scan(qhg_run *r, int32_t tile) {
+    if (r == nullptr) return fail(QHG_ERR_ARG, "null run");
+    const int ntiles = (r->C + kScanTile - 1) / kScanTile;
+    if (tile < 0 || tile >= ntiles - 1) return fail(QHG_ERR_ARG, "the tile must have a successor");
+    CUDA_TRY(cudaSetDevice(r->desc.device));
+    const uint32_t v = (uint32_t)tile + 1u;
+    CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char *>(r->d_rs) + offsetof(RunState, stall_tile), &v,
+                             sizeof(uint32_t), cudaMemcpyHostToDevice, r->stream));
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    return QHG_OK;
+}
+
 extern "C" int qhg_gpu_stream(qhg_run *r, void **stream) {
     if (r == nullptr || stream == nullptr) return fail(QHG_ERR_ARG, "null argument");
     *stream = (void *)r->stream;
@@ -911,7 +925,7 @@ extern "C" int qhg_gpu_destroy(qhg_run *r) {
     if (r->stream) cudaStreamSynchronize(r->stream);
     drop_graphs(r);
     free_agents(r);
-    cudaFree(r->d_nbr); cudaFree(r->d_nnbr); cudaFree(r->d_rev); cudaFree(r->d_K); cudaFree(r->d_vthr);
+    cudaFree(r->d_nbr); cudaFree(r->d_nnbr); cudaFree(r->d_rev); cudaFree(r->d_K); cudaFree(r->d_vthr[0]); cudaFree(r->d_vthr[1]);
     cudaFree(r->d_wthr); cudaFree(r->d_cmove);
     cudaFree(r->d_clsc); cudaFree(r->d_sbase); cudaFree(r->d_bbase); cudaFree(r->d_bidb);
     cudaFree(r->d_obase); cudaFree(r->d_tflag); cudaFree(r->d_tagg); cudaFree(r->d_tincl);

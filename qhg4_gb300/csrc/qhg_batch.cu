@@ -72,7 +72,7 @@ struct qhg_batch {
     uint8_t *d_nnbr = nullptr;
     uint32_t *d_rev = nullptr;
     double *d_K = nullptr;
-    ulonglong2 *d_vthr = nullptr;
+    ulonglong2 *d_vthr[2] = {nullptr, nullptr};
     uint64_t *d_wthr = nullptr;
     uint32_t *d_cmove = nullptr;
     uint32_t *d_crun = nullptr;
@@ -142,7 +142,7 @@ StepBuffers make_buffers(qhg_batch *b, int cur) {
     B.nonempty2 = b->d_ne[nx]; B.ne_start2 = b->d_nes[nx]; B.tile_first2 = b->d_tf[nx];
     B.id2 = b->d_id[nx]; B.birth2 = b->d_birth[nx]; B.age2 = b->d_age[nx]; B.lastb2 = b->d_lastb[nx];
     B.meta2 = b->d_meta[nx];
-    B.nbr = b->d_nbr; B.nnbr = b->d_nnbr; B.rev = b->d_rev; B.K = b->d_K; B.vthr = b->d_vthr;
+    B.nbr = b->d_nbr; B.nnbr = b->d_nnbr; B.rev = b->d_rev; B.K = b->d_K; B.vthr = b->d_vthr[cur]; B.vthr2 = b->d_vthr[nx];
     B.wthr = b->d_wthr; B.cmove = b->d_cmove;
     B.outc = b->d_outc; B.father = b->d_father; B.brank = b->d_brank; B.clsc = b->d_clsc;
     B.sbase = b->d_sbase; B.bbase = b->d_bbase; B.bidbase = b->d_bidb; B.obase = b->d_obase;
@@ -272,7 +272,8 @@ extern "C" int qhg_batch_create(const qhg_batch_desc *desc, qhg_batch **out) {
     A((void **)&b->d_nnbr, C);
     A((void **)&b->d_rev, C * sizeof(uint32_t));
     A((void **)&b->d_K, C * sizeof(double));
-    A((void **)&b->d_vthr, C * sizeof(ulonglong2));
+    A((void **)&b->d_vthr[0], C * sizeof(ulonglong2));
+    A((void **)&b->d_vthr[1], C * sizeof(ulonglong2));
     A((void **)&b->d_wthr, C * 6 * sizeof(uint64_t));
     A((void **)&b->d_cmove, C * sizeof(uint32_t));
     A((void **)&b->d_crun, C * sizeof(uint32_t));
@@ -791,7 +792,7 @@ extern "C" int qhg_batch_destroy(qhg_batch *b) {
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->copy_stream) cudaStreamSynchronize(b->copy_stream);
     drop_graphs(b);
-    void *ptrs[] = {b->d_nbr, b->d_nnbr, b->d_rev, b->d_K, b->d_vthr, b->d_wthr, b->d_cmove, b->d_crun,
+    void *ptrs[] = {b->d_nbr, b->d_nnbr, b->d_rev, b->d_K, b->d_vthr[0], b->d_vthr[1], b->d_wthr, b->d_cmove, b->d_crun,
                     b->d_outc, b->d_father, b->d_brank, b->d_clsc, b->d_sbase, b->d_bbase, b->d_bidb,
                     b->d_obase, b->d_tflag, b->d_tagg, b->d_tincl, b->d_runs, b->d_rnext, b->d_rstat,
                     b->d_inj, b->d_sgender, b->d_stage_err, b->d_ibase, b->d_injdone, b->d_cstat, b->d_sid, b->d_sbirth, b->d_sage,

@@ -34,7 +34,8 @@ constexpr int kStatsRing = 1024;
 constexpr int kBatchRing = 64;           // per-run statistics ring of a batch (steps)
 constexpr uint32_t kNoRun = 0xffffffffu; // run index of a batch cell that belongs to no run
 constexpr uint8_t kStagedDead = 0xffu;   // meta byte of a staged row that is not admitted
-constexpr uint32_t kSpinLimit = 1u << 24;  // bounded waits in the look-back
+constexpr uint32_t kSpinLimit = 1u << 26;  // bounded waits in the look-back (polls)
+constexpr uint64_t kWaitLimitNs = 1000000000ull;  // ... and their time limit (1 s)
 
 // random stream bases (Philox counter word 0), see oracle/philox4x32.h
 constexpr uint32_t kStreamActions = 0u;
@@ -142,6 +143,7 @@ struct RunState {
     uint32_t big;            // 1: some cell holds more than kMaxCell agents (big-cell kernels run)
     uint32_t big_next;       // the same for the table the step writes (set by its commit)
     uint32_t max_cell;       // largest cell of the next table (cell scan)
+    uint32_t stall_tile;     // tests of the bounded waits: tile + 1 whose scan status is withheld once
     // statistics ring: [step % kStatsRing][live, births, deaths, moves]
     unsigned long long stats[kStatsRing][4];
 };
@@ -159,8 +161,10 @@ struct StepBuffers {
     // rev packs, 3 bits per neighbour slot q, the slot of this cell in the
     // neighbour's own list
     const int32_t *nbr; const uint8_t *nnbr; const uint32_t *rev; const double *K;
-    // Verhulst thresholds of each cell for the coming step (written by the scan)
-    ulonglong2 *vthr;
+    // Verhulst thresholds of each cell: for this step's table (read by
+    // k_actions) and for the next table (written by the scan); kept per table
+    // so that a failed step leaves the current ones intact for its retry
+    const ulonglong2 *vthr; ulonglong2 *vthr2;
     // moves: WeightedMove thresholds (6 per cell) and one word per cell:
     // bits 0-2 neighbour count, bits 8-13 valid neighbour slots, bit 16 all
     // weights equal

@@ -62,6 +62,12 @@ struct AgentDraws {
     }
 };
 
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 __device__ __forceinline__ void set_error(RunState *rs, uint32_t code, uint32_t info) {
     if (atomicCAS(&rs->error, 0u, code) == 0u) {
         rs->error_info = info;
@@ -726,13 +732,17 @@ k_cell_scan(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
     }
     __syncthreads();
     const uint32_t tile = s_tile;
-    if (tile >= ntiles) {   // stale tile counter: refuse rather than index past the status arrays
-        if (threadIdx.x == 0) set_error(rs, kErrInternal, 2u);
-        return;
-    }
+    // a tile counter that did not start at zero hands out numbers past the
+    // last tile: never index past the status arrays (the tile left out makes
+    // its successor's bounded wait fail and report the step)
+    if (tile >= ntiles) return;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int base = (int)tile * kScanTile + threadIdx.x * kScanItems;
+    // a test of the bounded waits withholds this tile's status once: its
+    // successor's look-back runs out, the step fails with kErrTimeout
+    const bool withhold = (rs->stall_tile == tile + 1u);
+    if (withhold && threadIdx.x == 0) rs->stall_tile = 0u;
 
     uint32_t nnew[kScanItems], stay[kScanItems], bth[kScanItems];
     uint32_t crn[kScanItems];
@@ -814,17 +824,18 @@ k_cell_scan(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             if (lane == 0) {
                 tile_incl[tile] = make_uint4(total.n, total.b, total.ne, 0u);
                 __threadfence();
-                atomicExch(&tile_flag[tile], (epoch << 2) | 2u);
+                if (!withhold) atomicExch(&tile_flag[tile], (epoch << 2) | 2u);
             }
         } else {
             if (lane == 0) {
                 tile_agg[tile] = make_uint4(total.n, total.b, total.ne, 0u);
                 __threadfence();
-                atomicExch(&tile_flag[tile], (epoch << 2) | 1u);
+                if (!withhold) atomicExch(&tile_flag[tile], (epoch << 2) | 1u);
             }
             // warp-wide look-back over windows of 32 predecessors
             int wbase = (int)tile - 1;
             uint32_t spins = 0;
+            const uint64_t t_start = globaltimer_ns();
             while (true) {
                 const int tt = wbase - lane;
                 uint32_t f = (epoch << 2) | 2u;   // before tile 0: an inclusive prefix of zero
@@ -848,7 +859,8 @@ k_cell_scan(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                                                 __shfl_sync(FULL_MASK, v.ne, 0)});
                     if (im) break;
                     wbase -= 32;
-                } else if (++spins > kSpinLimit) {
+                } else if (++spins > kSpinLimit || globaltimer_ns() - t_start > kWaitLimitNs) {
+                    // a predecessor never published: give up, report, return
                     if (lane == 0) set_error(rs, kErrTimeout, tile);
                     break;
                 }
@@ -856,7 +868,7 @@ k_cell_scan(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             if (lane == 0) {
                 tile_incl[tile] = make_uint4(excl.n + total.n, excl.b + total.b, excl.ne + total.ne, 0u);
                 __threadfence();
-                atomicExch(&tile_flag[tile], (epoch << 2) | 2u);
+                if (!withhold) atomicExch(&tile_flag[tile], (epoch << 2) | 2u);
             }
         }
         if (lane == 0) {
@@ -1563,7 +1575,7 @@ extern "C" int qhg_launch_upload(const qhg::StepConst *P, qhg::RunState *rs, con
     BatchBuffers BB;
     memset(&BB, 0, sizeof(BB));
     k_cell_scan<false><<<ntiles, kScanThreads, 0, stream>>>(
-        *P, BB, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr, B->sbase, B->bbase, B->bidbase,
+        *P, BB, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr2, B->sbase, B->bbase, B->bidbase,
         B->obase, B->nonempty2, B->ne_start2, B->tile_first2, B->tile_flag, B->tile_agg, B->tile_incl);
     if (n > 0) {
         k_upload_place<<<(unsigned)blk, 256, 0, stream>>>(rs, cell, gender, state, sid, sbirth, sage, slastb, n,
@@ -1648,7 +1660,7 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
     if (ev) cudaEventRecord(ev[1], stream);
 #define QHG_LAUNCH_SCAN(BT)                                                                                 \
     k_cell_scan<BT><<<ntiles, kScanThreads, 0, stream>>>(                                                   \
-        *P, BB, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr, B->sbase, B->bbase, B->bidbase,       \
+        *P, BB, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr2, B->sbase, B->bbase, B->bidbase,       \
         B->obase, B->nonempty2, B->ne_start2, B->tile_first2, B->tile_flag, B->tile_agg, B->tile_incl)
     if (batch) QHG_LAUNCH_SCAN(true);
     else QHG_LAUNCH_SCAN(false);

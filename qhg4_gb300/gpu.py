@@ -38,6 +38,7 @@ EXPORTS = [
     "qhg_batch_set_shape", "qhg_batch_get_shape", "qhg_batch_stream", "qhg_batch_destroy",
     "qhg_batch_live_history", "qhg_batch_snapshot_async", "qhg_batch_snapshot_wait",
     "qhg_host_buffer_alloc", "qhg_host_buffer_free", "qhg_gpu_next_id", "qhg_gpu_set_next_id",
+    "qhg_gpu_test_stall_scan",
 ]
 
 
@@ -129,6 +130,7 @@ def load_library(path: str = LIB_PATH):
         "qhg_host_buffer_free": (I, [P]),
         "qhg_gpu_next_id": (I, [P, P]),
         "qhg_gpu_set_next_id": (I, [P, ct.c_int64]),
+        "qhg_gpu_test_stall_scan": (I, [P, ct.c_int32]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -271,6 +273,10 @@ class GpuRun:
 
     def set_next_id(self, next_id: int) -> None:
         _check(_lib.qhg_gpu_set_next_id(self.h, int(next_id)))
+
+    def test_stall_scan(self, tile: int = 0) -> None:
+        """Makes the next step fail through a bounded wait (tests of failure detection)."""
+        _check(_lib.qhg_gpu_test_stall_scan(self.h, int(tile)))
 
     def stream_handle(self) -> int:
         s = ct.c_void_p()
