@@ -183,7 +183,7 @@ struct ActionsSmemT {
     uint8_t wf[kTileCells];        // WeightedMove: all weights of the cell equal
     uint32_t cls[kTileCells][4];
     uint32_t red[TT / 32];
-    uint32_t npick, noad;
+    uint32_t npick, noad, nfert;
 };
 
 // OldAgeDeath is the last action of program 2: its draw (needed only by
@@ -298,7 +298,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
         }
         __syncthreads();
         for (int lc = tid; lc < nc; lc += TT) S.head[S.cstart[lc]] = 1;
-        if (tid == 0) { S.npick = 0u; S.noad = 0u; }
+        if (tid == 0) { S.npick = 0u; S.noad = 0u; S.nfert = 0u; }
         __syncthreads();
         // local cell of each row: count of cell heads up to the row (block scan
         // over contiguous rows per thread)
@@ -351,42 +351,42 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                 const int lc = fert ? S.cell[i] : 0;
                 uint32_t *ctr = male ? &S.nm[lc] : &S.nf[lc];
                 const uint32_t q = warp_agg_add(fert, ((uint32_t)lc << 1) | (male ? 1u : 0u), ctr, 1u);
+                // the tile's FERTILE agents also go to a dense list (their list
+                // positions), so that the rank loop below runs on full warps
+                const uint32_t fb = __ballot_sync(FULL_MASK, fert);
+                uint32_t fbase = 0;
+                if ((tid & 31) == 0 && fb) fbase = atomicAdd(&S.nfert, (uint32_t)__popc(fb));
+                fbase = __shfl_sync(FULL_MASK, fbase, 0);
                 if (fert) {
                     const uint32_t pos = male ? (S.cstart[lc + 1] - 1u - q) : (S.cstart[lc] + q);
                     S.pick[pos] = (uint16_t)i;
                     S.fid[pos] = pid[j];
+                    S.oadq[fbase + __popc(fb & lanemask_lt())] = (uint16_t)pos;
                 }
             }
             __syncthreads();
-            // rank by ID within the own sex's list (IDs are unique)
-#pragma unroll
-            for (int j = 0; j < RA; j++) {
-                const int i = tid + j * TT;
-                if (i < na && (pm[j] & kMetaFertile)) {
-                    const int lc = S.cell[i];
-                    const int64_t x = pid[j];
-                    int b, e;
-                    if (pm[j] & kMetaGender) {
-                        e = (int)S.cstart[lc + 1];
-                        b = e - (int)S.nm[lc];
-                    } else {
-                        b = (int)S.cstart[lc];
-                        e = b + (int)S.nf[lc];
-                    }
-                    int r = 0;
-                    for (int q = b; q < e; q++) r += (S.fid[q] < x) ? 1 : 0;
-                    S.frank[i] = (uint16_t)r;
+            // rank by ID within the own sex's list (IDs are unique), over the
+            // dense list of FERTILE agents; each agent goes to its place in
+            // its cell's ID-ordered lists (females, then males)
+            const uint32_t nfe = S.nfert;
+            for (uint32_t q = tid; q < nfe; q += TT) {
+                const int pos = S.oadq[q];
+                const int i = S.pick[pos];
+                const int lc = S.cell[i];
+                const int64_t x = S.fid[pos];
+                const bool male = (S.meta[i] & kMetaGender) != 0;
+                int b, e;
+                if (male) {
+                    e = (int)S.cstart[lc + 1];
+                    b = e - (int)S.nm[lc];
+                } else {
+                    b = (int)S.cstart[lc];
+                    e = b + (int)S.nf[lc];
                 }
-            }
-            __syncthreads();
-#pragma unroll
-            for (int j = 0; j < RA; j++) {
-                const int i = tid + j * TT;
-                if (i < na && (pm[j] & kMetaFertile)) {
-                    const int lc = S.cell[i];
-                    const uint32_t off = (pm[j] & kMetaGender) ? S.nf[lc] : 0u;
-                    S.list[S.cstart[lc] + off + S.frank[i]] = (uint16_t)i;
-                }
+                int r = 0;
+                for (int k = b; k < e; k++) r += (S.fid[k] < x) ? 1 : 0;
+                S.frank[i] = (uint16_t)r;
+                S.list[S.cstart[lc] + (male ? S.nf[lc] : 0u) + (uint32_t)r] = (uint16_t)i;
             }
             __syncthreads();
             // the members of the smaller side pick, in ID order; gather them densely
