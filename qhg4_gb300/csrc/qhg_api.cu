@@ -72,6 +72,7 @@ struct qhg_run {
     float *d_lastb[2] = {nullptr, nullptr};
     uint8_t *d_meta[2] = {nullptr, nullptr};
     uint32_t *d_ne[2] = {nullptr, nullptr};    // non-empty cells in index order
+    uint32_t *d_necm[2] = {nullptr, nullptr};  // their move words, by position in that list
     uint32_t *d_nes[2] = {nullptr, nullptr};   // their first rows (+ agent count)
     uint32_t *d_tf[2] = {nullptr, nullptr};    // first non-empty cell of each tile
     // scratch
@@ -107,7 +108,8 @@ static void free_agents(qhg_run *r) {
     for (int p = 0; p < 2; p++) {
         cudaFree(r->d_id[p]); cudaFree(r->d_birth[p]); cudaFree(r->d_age[p]); cudaFree(r->d_lastb[p]);
         cudaFree(r->d_meta[p]); cudaFree(r->d_ne[p]); cudaFree(r->d_nes[p]); cudaFree(r->d_tf[p]);
-        r->d_tf[p] = nullptr;
+        cudaFree(r->d_necm[p]);
+        r->d_tf[p] = nullptr; r->d_necm[p] = nullptr;
         r->d_id[p] = nullptr; r->d_birth[p] = r->d_age[p] = r->d_lastb[p] = nullptr;
         r->d_meta[p] = nullptr; r->d_ne[p] = r->d_nes[p] = nullptr;
     }
@@ -507,6 +509,7 @@ static int alloc_agents(qhg_run *r, uint32_t cap) {
         CUDA_TRY(cudaMalloc(&r->d_lastb[p], (size_t)cap * sizeof(float)));
         CUDA_TRY(cudaMalloc(&r->d_meta[p], (size_t)cap));
         CUDA_TRY(cudaMalloc(&r->d_ne[p], (size_t)C * sizeof(uint32_t)));
+        CUDA_TRY(cudaMalloc(&r->d_necm[p], (size_t)C * sizeof(uint32_t)));
         CUDA_TRY(cudaMalloc(&r->d_nes[p], (size_t)(C + 1) * sizeof(uint32_t)));
         CUDA_TRY(cudaMalloc(&r->d_tf[p], ((size_t)cap / kTileAgents + 2) * sizeof(uint32_t)));
     }
@@ -644,7 +647,7 @@ static StepBuffers make_buffers(qhg_run *r, int cur) {
     B.id2 = r->d_id[nx]; B.birth2 = r->d_birth[nx]; B.age2 = r->d_age[nx]; B.lastb2 = r->d_lastb[nx];
     B.meta2 = r->d_meta[nx];
     B.nbr = r->d_nbr; B.nnbr = r->d_nnbr; B.rev = r->d_rev; B.K = r->d_K; B.vthr = r->d_vthr[cur]; B.vthr2 = r->d_vthr[nx]; B.wthr = r->d_wthr;
-    B.cmove = r->d_cmove;
+    B.cmove = r->d_cmove; B.necm = r->d_necm[cur]; B.necm2 = r->d_necm[nx];
     B.outc = r->d_outc; B.father = r->d_father; B.brank = r->d_brank; B.clsc = r->d_clsc;
     B.sbase = r->d_sbase; B.bbase = r->d_bbase; B.bidbase = r->d_bidb; B.obase = r->d_obase;
     B.tile_flag = r->d_tflag; B.tile_agg = r->d_tagg; B.tile_incl = r->d_tincl;

@@ -83,6 +83,7 @@ struct qhg_batch {
     float *d_lastb[2] = {nullptr, nullptr};
     uint8_t *d_meta[2] = {nullptr, nullptr};
     uint32_t *d_ne[2] = {nullptr, nullptr};
+    uint32_t *d_necm[2] = {nullptr, nullptr};
     uint32_t *d_nes[2] = {nullptr, nullptr};
     uint32_t *d_tf[2] = {nullptr, nullptr};
     // scratch of a step
@@ -143,7 +144,7 @@ StepBuffers make_buffers(qhg_batch *b, int cur) {
     B.id2 = b->d_id[nx]; B.birth2 = b->d_birth[nx]; B.age2 = b->d_age[nx]; B.lastb2 = b->d_lastb[nx];
     B.meta2 = b->d_meta[nx];
     B.nbr = b->d_nbr; B.nnbr = b->d_nnbr; B.rev = b->d_rev; B.K = b->d_K; B.vthr = b->d_vthr[cur]; B.vthr2 = b->d_vthr[nx];
-    B.wthr = b->d_wthr; B.cmove = b->d_cmove;
+    B.wthr = b->d_wthr; B.cmove = b->d_cmove; B.necm = b->d_necm[cur]; B.necm2 = b->d_necm[nx];
     B.outc = b->d_outc; B.father = b->d_father; B.brank = b->d_brank; B.clsc = b->d_clsc;
     B.sbase = b->d_sbase; B.bbase = b->d_bbase; B.bidbase = b->d_bidb; B.obase = b->d_obase;
     B.tile_flag = b->d_tflag; B.tile_agg = b->d_tagg; B.tile_incl = b->d_tincl;
@@ -284,6 +285,7 @@ extern "C" int qhg_batch_create(const qhg_batch_desc *desc, qhg_batch **out) {
         A((void **)&b->d_lastb[p], N * sizeof(float));
         A((void **)&b->d_meta[p], N);
         A((void **)&b->d_ne[p], C * sizeof(uint32_t));
+        A((void **)&b->d_necm[p], C * sizeof(uint32_t));
         A((void **)&b->d_nes[p], (C + 1) * sizeof(uint32_t));
         A((void **)&b->d_tf[p], (N / kTileAgents + 2) * sizeof(uint32_t));
     }
@@ -801,6 +803,7 @@ extern "C" int qhg_batch_destroy(qhg_batch *b) {
     for (int p = 0; p < 2; p++) {
         cudaFree(b->d_id[p]); cudaFree(b->d_birth[p]); cudaFree(b->d_age[p]); cudaFree(b->d_lastb[p]);
         cudaFree(b->d_meta[p]); cudaFree(b->d_ne[p]); cudaFree(b->d_nes[p]); cudaFree(b->d_tf[p]);
+        cudaFree(b->d_necm[p]);
     }
     if (b->h_rs) cudaFreeHost(b->h_rs);
     for (int i = 0; i < 5; i++) {

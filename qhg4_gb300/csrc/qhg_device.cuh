@@ -161,14 +161,19 @@ struct StepBuffers {
     // rev packs, 3 bits per neighbour slot q, the slot of this cell in the
     // neighbour's own list
     const int32_t *nbr; const uint8_t *nnbr; const uint32_t *rev; const double *K;
-    // Verhulst thresholds of each cell: for this step's table (read by
-    // k_actions) and for the next table (written by the scan); kept per table
-    // so that a failed step leaves the current ones intact for its retry
+    // Verhulst thresholds of each non-empty cell, by its position in the
+    // non-empty list: for this step's table (read by k_actions) and for the
+    // next table (written by the scan); kept per table so that a failed step
+    // leaves the current ones intact for its retry
     const ulonglong2 *vthr; ulonglong2 *vthr2;
     // moves: WeightedMove thresholds (6 per cell) and one word per cell:
     // bits 0-2 neighbour count, bits 8-13 valid neighbour slots, bit 16 all
     // weights equal
     const uint64_t *wthr; const uint32_t *cmove;
+    // the move word of each non-empty cell by its position in the non-empty
+    // list (current table, next table), copied from cmove by the cell scan;
+    // the Verhulst thresholds above are stored by the same positions
+    const uint32_t *necm; uint32_t *necm2;
     // outcome word per agent: outcome byte | local cell << 8 | rank in its
     // cell's class << 17
     uint32_t *outc; int32_t *father; uint16_t *brank; uint32_t *clsc;

@@ -156,40 +156,162 @@ __host__ __device__ constexpr int prog_act(int p, int a) {
 }
 constexpr int kNumPrograms = 4;
 
-template <int TM, int TT>
+template <int TM, int TT, bool BATCH>
 struct ActionsSmemT {
-    int64_t fid[TM];         // IDs of the unsorted FERTILE lists (same positions as pick)
-    uint8_t meta[TM];
-    uint8_t head[TM];        // first row of a cell
-    uint8_t bfl[TM];         // gives birth this step
+    int64_t fid[TM];         // IDs of the unsorted FERTILE lists (same positions as pick), then of the OldAgeDeath queue
+    float ofa[TM];           // ages of the OldAgeDeath queue
     uint16_t cell[TM];       // local cell index of each row
     int16_t mate[TM];        // mate's row within the tile, -1 none
     uint16_t frank[TM];      // rank of a FERTILE agent among its cell's FERTILE agents of its sex (by ID)
     uint16_t list[TM];       // at each cell's rows: FERTILE females by ID, then FERTILE males by ID
-    uint16_t pick[TM];       // at each cell's rows: unsorted FERTILE lists, later the pick values
-    alignas(4) uint16_t pkrow[TM];  // rows of the tile's pairing members that draw (dense)
-    uint16_t oadq[TM];       // rows whose OldAgeDeath needs its draw (dense)
-    uint8_t oc[TM];          // outcome byte before the deferred OldAgeDeath draws
+    uint16_t pick[TM];       // at each cell's rows: unsorted FERTILE lists (rows), then the mothers' ID ranks
+    uint16_t pkpos[TM];      // list positions of the tile's picking members (dense)
+    uint16_t oadq[TM];       // list positions of the tile's FERTILE agents (dense), then at each
+                             // cell's rows the pick values, then the OldAgeDeath queue (rows)
+    uint8_t oc[TM];          // outcome byte
     uint32_t cstart[kTileCells + 1];  // first row of each cell, relative to the tile
     int32_t cid[kTileCells];
-    uint32_t crun[kTileCells];     // batches: run of each cell
-    uint32_t nf[kTileCells];
-    uint32_t nm[kTileCells];
+    uint32_t crun[BATCH ? kTileCells : 1];   // batches: run of each cell
+    uint32_t dm[BATCH ? kTileCells : 1];     // batches: deaths | moves << 16 per cell
+    uint32_t nfm[kTileCells];      // FERTILE females | FERTILE males << 16
     uint64_t tb[kTileCells];       // Verhulst: birth threshold (kind 1) or birth-rate death threshold (kind 2)
     uint64_t td[kTileCells];       // LinearDeath threshold
     uint8_t tk[kTileCells];
     uint8_t nn[kTileCells];        // moves: neighbours of each cell
     uint8_t vm[kTileCells];        // moves: bit q set when neighbour slot q holds a cell
     uint8_t wf[kTileCells];        // WeightedMove: all weights of the cell equal
-    uint32_t cls[kTileCells][4];
+    uint32_t cls[kTileCells][4];   // class counts, two 16-bit counters per word
     uint32_t red[TT / 32];
-    uint32_t npick, noad, nfert;
+    uint32_t npick, noad, nfert, idhi;
 };
 
 // OldAgeDeath is the last action of program 2: its draw (needed only by
 // agents whose age lies inside the death window) is made in a dense pass
 // after the other actions, so that warps do not run Philox for a few lanes
 __host__ __device__ constexpr bool prog_defers_oad(int p) { return p == 2; }
+
+// Rank of an agent's outcome in its cell's class (slot 0 stay, 1..6 movers
+// per neighbour slot) from a warp-aggregated shared counter; every lane of
+// the warp calls it.  The rank is the agent's offset in the class: rows of a
+// cell are not kept in ID order, and nothing depends on their order.
+__device__ __forceinline__ uint32_t class_rank(bool counted, int lc, int cls, uint32_t (*cnt)[4]) {
+    const int slot = (cls > 0) ? cls - 1 : 0;
+    const uint32_t q = warp_agg_add(counted, ((uint32_t)lc << 3) | (uint32_t)slot, &cnt[lc][slot >> 1],
+                                    1u << (16 * (slot & 1)));
+    return (q >> (16 * (slot & 1))) & 0xffffu;
+}
+
+// cell constants one agent's actions read
+struct CellView {
+    uint64_t tb, td;      // Verhulst: birth (kind 1) or birth-rate death (kind 2) threshold, death threshold
+    uint32_t tk;          // Verhulst kind (0 none)
+    uint32_t nn, vm, wf;  // moves: neighbour count, valid neighbour slots, all weights equal
+    uint32_t c;           // cell index (WeightedMove thresholds)
+};
+
+// Every action of one agent in execution order (SPopulation::doActions,
+// core/SPopulation.cpp:554-577; GetOld actions/GetOld.cpp:37-48, Fertility
+// actions/Fertility.cpp:49-73, LinearBirth/LinearDeath actions/LinearBirth.cpp:122-166,
+// actions/LinearDeath.cpp:131-150, OldAgeDeath actions/OldAgeDeath.cpp:48-67,
+// RandomMove actions/RandomMove.cpp:65-100, WeightedMove actions/WeightedMove.cpp:45-106).
+// Returns the outcome byte.  With DEFER_OAD an agent inside the OldAgeDeath
+// window is left alive with `queued` set: its draw is made by the caller.
+// `fa` is the agent's age after the actions (the input age on entry).
+template <int PROG, bool BATCH, bool DEFER_OAD>
+__device__ __forceinline__ uint8_t agent_outcome(const StepConst &P, const BatchRun *R, int32_t step, float fT,
+                                                 int64_t id, uint8_t m8, float fb, float fa_in, float fl,
+                                                 bool mated, const CellView &cv, const uint64_t *__restrict__ wthr,
+                                                 float &fa, bool &queued, uint32_t &cnt_deaths,
+                                                 uint32_t &cnt_moves) {
+    const uint64_t seed = BATCH ? R->seed : P.seed;
+    const int32_t stepR = BATCH ? step - R->step0 : step;
+    const float fTR = BATCH ? (float)stepR : fT;
+    fa = fa_in;
+    const bool female = !(m8 & kMetaGender);
+    bool fert = (m8 & kMetaFertile) != 0;
+    bool alive = true;
+    bool bflag = false;
+    int dir = 0;
+    AgentDraws dr;
+    dr.init(seed, (uint32_t)stepR, id);
+    constexpr int NA = PROG ? prog_len(PROG) : kMaxActions;
+#pragma unroll (PROG ? NA : 1)
+    for (int a = 0; a < NA; a++) {
+        if ((PROG == 0 && a >= P.n_act) || !alive) break;
+        const ActionConst &A = BATCH ? R->act[a] : P.act[a];
+        switch (PROG ? prog_act(PROG, a) : A.type) {
+        case kGetOld:
+            fa = __fsub_rn(fTR, fb);
+            break;
+        case kFertility:
+            if (female) fert = (fa > A.f0) && (fa < A.f1) && (__fsub_rn(fTR, fl) > A.f2);
+            else fert = fa > A.f0;
+            break;
+        case kVerhulst:
+        case kVerhulstVarK: {
+            uint32_t k = A.window;
+            if (cv.tk == 1u) {
+                if (female && mated) {
+                    if ((uint64_t)dr.get(k++) < cv.tb) bflag = true;
+                }
+            } else if (cv.tk == 2u) {
+                if ((uint64_t)dr.get(k++) < cv.tb) alive = false;
+            }
+            if (alive) {
+                if ((uint64_t)dr.get(k) < cv.td) alive = false;
+            }
+            if (!alive) cnt_deaths++;
+            break;
+        }
+        case kOldAgeDeath: {
+            fa = __fsub_rn(fTR, fb);
+            bool die = false;
+            if (fa <= A.age_lo) {
+                die = false;
+            } else if (fa > A.age_hi) {
+                die = true;
+            } else if (DEFER_OAD) {
+                queued = true;
+            } else {
+                const uint32_t u = dr.get(A.window);
+                const double t = __dmul_rn(__dmul_rn(A.oad_w, (double)u), 2.3283064365386962890625e-10);
+                const double thr = __dadd_rn(A.oad_M, __dadd_rn(A.oad_a, t));
+                die = (double)fa > thr;
+            }
+            if (die) { alive = false; cnt_deaths++; }
+            break;
+        }
+        case kRandomMove: {
+            if ((uint64_t)dr.get(A.window) < A.pthr) {
+                const uint32_t u2 = dr.get(A.window + 1);
+                const int d = (int)(((uint64_t)(cv.nn + 1u) * (uint64_t)u2) >> 32);
+                if (d > 0 && ((cv.vm >> (d - 1)) & 1u)) { dir = d; cnt_moves++; }
+            }
+            break;
+        }
+        case kWeightedMove: {
+            if ((uint64_t)dr.get(A.window) < A.pthr) {
+                const uint32_t u2 = dr.get(A.window + 1);
+                int d;
+                if (cv.wf & 1u) {
+                    d = (int)(((uint64_t)(cv.nn + 1u) * (uint64_t)u2) >> 32);
+                } else {
+                    d = 0;
+                    const uint64_t *w = wthr + (size_t)cv.c * 6;
+                    for (int q = 0; q < (int)cv.nn; q++) d += (w[q] <= (uint64_t)u2) ? 1 : 0;
+                }
+                if (d > 0 && ((cv.vm >> (d - 1)) & 1u)) { dir = d; cnt_moves++; }
+            }
+            break;
+        }
+        default:
+            break;
+        }
+    }
+    const int cls = alive ? (1 + dir) : 0;
+    return (uint8_t)(cls | (bflag ? kOutBirth : 0) | (fert ? kOutFertile : 0) |
+                     ((m8 & kMetaGender) ? kOutGender : 0) | (dir > 0 ? kOutMoved : 0));
+}
 
 template <int PROG, bool BATCH, bool BIG>
 __global__ void __launch_bounds__(Tile<BIG>::kThreads, BIG ? 1 : 4)
@@ -199,46 +321,52 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
           const int64_t *__restrict__ id, const float *__restrict__ birth,
           const float *__restrict__ age, const float *__restrict__ lastb,
           const uint8_t *__restrict__ meta,
-          const int32_t *__restrict__ nbr, const uint8_t *__restrict__ nnbr,
           const ulonglong2 *__restrict__ vthr, const uint64_t *__restrict__ wthr,
-          const uint32_t *__restrict__ cmove,
+          const uint32_t *__restrict__ necm,
           uint32_t *__restrict__ outc, int32_t *__restrict__ father, uint16_t *__restrict__ brank,
           uint32_t *__restrict__ clsc) {
     constexpr int TT = Tile<BIG>::kThreads;
     constexpr int TM = Tile<BIG>::kMax;
     extern __shared__ __align__(16) unsigned char qhg_smem[];
-    ActionsSmemT<TM, TT> &S = *reinterpret_cast<ActionsSmemT<TM, TT> *>(qhg_smem);
+    ActionsSmemT<TM, TT, BATCH> &S = *reinterpret_cast<ActionsSmemT<TM, TT, BATCH> *>(qhg_smem);
     if (rs->error != 0u) return;   // an earlier kernel failed: keep the state
     if (rs->big != (BIG ? 1u : 0u)) return;   // the other form runs this step
     const int tid = threadIdx.x;
+    const int lane = tid & 31;
     const int32_t step = rs->step;
     const float fT = (float)step;
     const uint32_t N = rs->n_agents;
     const uint32_t ntiles = (N + kTileAgents - 1) / kTileAgents;
     uint32_t cnt_births = 0, cnt_deaths = 0, cnt_moves = 0;
-
-    // tiles are dealt out statically; the next tile's bounds and the current
-    // tile's agent fields are loaded early so that their latency overlaps the
-    // cell set-up and the pairing phases
     constexpr int RA = TM / TT;
-    uint32_t nr0 = 0, nr1 = 0;
+    constexpr bool kDeferOad = prog_defers_oad(PROG);
+
+    // tiles are dealt out statically.  The bounds of the CTA's next tile
+    // (first non-empty cell, first row) are loaded one tile ahead, so that a
+    // tile's agent fields and cell data are requested together at its start
+    uint32_t nr0 = 0, nr1 = 0, na0 = 0, na1 = 0;
     if (blockIdx.x < ntiles) {
         nr0 = tile_first[blockIdx.x];
         nr1 = tile_first[blockIdx.x + 1];
+        na0 = ne_start[nr0];
+        na1 = ne_start[nr1];
     }
     for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const uint32_t r0 = nr0;
         const int nc = (int)(nr1 - r0);
+        const uint32_t a0 = na0;
+        const int na = (int)(na1 - na0);
         const uint32_t tn = t + gridDim.x;
         if (tn < ntiles) {
             nr0 = tile_first[tn];
             nr1 = tile_first[tn + 1];
         }
-        if (nc == 0) continue;
-        const uint32_t a0 = ne_start[r0];
-        const int na = (int)(ne_start[r0 + nc] - a0);
-        if (na > TM || nc > kTileCells) {
-            if (tid == 0) set_error(rs, kErrCellTooLarge, r0);
+        if (nc == 0 || na > TM || nc > kTileCells) {
+            if (nc != 0 && tid == 0) set_error(rs, kErrCellTooLarge, r0);
+            if (tn < ntiles) {
+                na0 = ne_start[nr0];
+                na1 = ne_start[nr1];
+            }
             continue;
         }
         int64_t pid[RA];
@@ -258,76 +386,60 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
         __syncthreads();   // the previous tile is done with the shared arrays
         // ---- cells: ids, rows, Verhulst thresholds (LinearBirth / LinearDeath
         // ::initialize, actions/LinearBirth.cpp:90-112, actions/LinearDeath.cpp:92-122)
+        // and move words, both stored by position in the non-empty list
         for (int lc = tid; lc < nc; lc += TT) {
-            const int c = (int)nonempty[r0 + lc];
-            const uint32_t cs = ne_start[r0 + lc] - a0;
-            const uint32_t ce = ne_start[r0 + lc + 1] - a0;
-            S.cid[lc] = c;
+            const uint32_t r = r0 + (uint32_t)lc;
+            const uint32_t c = nonempty[r];
+            const uint32_t cs = ne_start[r] - a0;
+            uint32_t cm = 0u;
+            ulonglong2 v = make_ulonglong2(0ull, 0ull);
+            if (P.has_move) cm = necm[r];
+            if (P.n_verhulst > 0) v = vthr[r];   // computed by the previous step's cell scan
+            S.cid[lc] = (int32_t)c;
             S.cstart[lc] = cs;
-            if (lc == nc - 1) S.cstart[nc] = ce;
-            if (BATCH) S.crun[lc] = BB.crun[c];
-            S.nf[lc] = 0u;
-            S.nm[lc] = 0u;
+            if (lc == nc - 1) S.cstart[nc] = (uint32_t)na;
+            if (BATCH) {
+                S.crun[lc] = BB.crun[c];
+                S.dm[lc] = 0u;
+            }
+            S.nfm[lc] = 0u;
             S.cls[lc][0] = S.cls[lc][1] = S.cls[lc][2] = S.cls[lc][3] = 0u;
             // the neighbour row of the cell as a count and a mask of valid slots,
             // so that moving agents read no neighbour data from memory
-            if (P.has_move) {
-                const uint32_t cm = cmove[c];
-                S.nn[lc] = (uint8_t)(cm & 7u);
-                S.vm[lc] = (uint8_t)((cm >> 8) & 63u);
-                S.wf[lc] = (uint8_t)((cm >> 16) & 1u);
-                if (P.has_wmove) asm volatile("prefetch.global.L1 [%0];" ::"l"(wthr + (size_t)c * 6));
-            }
-            if (P.n_verhulst > 0) {
-                // computed by the previous step's cell scan for this step's counts
-                const ulonglong2 v = vthr[c];
-                S.tk[lc] = (uint8_t)(v.x >> 62);
-                S.tb[lc] = v.x & ((1ull << 62) - 1ull);
-                S.td[lc] = v.y;
-            }
+            S.nn[lc] = (uint8_t)(cm & 7u);
+            S.vm[lc] = (uint8_t)((cm >> 8) & 63u);
+            S.wf[lc] = (uint8_t)((cm >> 16) & 1u);
+            S.tk[lc] = (uint8_t)(v.x >> 62);
+            S.tb[lc] = v.x & ((1ull << 62) - 1ull);
+            S.td[lc] = v.y;
+            if (P.has_wmove) asm volatile("prefetch.global.L1 [%0];" ::"l"(wthr + (size_t)c * 6));
         }
 #pragma unroll
         for (int j = 0; j < RA; j++) {
             const int i = tid + j * TT;
-            if (i < na) {
-                S.meta[i] = pm[j];
-                S.mate[i] = -1;
-                S.bfl[i] = 0;
-                S.head[i] = 0;
-            }
+            if (i < na) S.mate[i] = -1;
         }
+        if (tid == 0) { S.npick = 0u; S.noad = 0u; S.nfert = 0u; S.idhi = 0u; }
         __syncthreads();
-        for (int lc = tid; lc < nc; lc += TT) S.head[S.cstart[lc]] = 1;
-        if (tid == 0) { S.npick = 0u; S.noad = 0u; S.nfert = 0u; }
-        __syncthreads();
-        // local cell of each row: count of cell heads up to the row (block scan
-        // over contiguous rows per thread)
+        // local cell of each row: binary search of the cells' first rows (the
+        // searches of a thread's rows run side by side)
         {
-            const int i0 = tid * RA;
-            uint32_t h[RA];
-            uint32_t tot = 0;
+            int lo[RA];
+#pragma unroll
+            for (int j = 0; j < RA; j++) lo[j] = 0;
+            for (int s = 1 << (31 - __clz(nc)); s > 0; s >>= 1) {
+#pragma unroll
+                for (int j = 0; j < RA; j++) {
+                    const int m = lo[j] + s;
+                    if (m < nc && (int)S.cstart[m] <= tid + j * TT) lo[j] = m;
+                }
+            }
 #pragma unroll
             for (int j = 0; j < RA; j++) {
-                tot += (i0 + j < na) ? S.head[i0 + j] : 0u;
-                h[j] = tot;
-            }
-            const int lane = tid & 31, warp = tid >> 5;
-            uint32_t inc = tot;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(FULL_MASK, inc, o);
-                if (lane >= o) inc += y;
-            }
-            if (lane == 31) S.red[warp] = inc;
-            __syncthreads();
-            uint32_t base = inc - tot;
-            for (int w = 0; w < warp; w++) base += S.red[w];
-#pragma unroll
-            for (int j = 0; j < RA; j++) {
-                if (i0 + j < na) S.cell[i0 + j] = (uint16_t)(base + h[j] - 1u);
+                const int i = tid + j * TT;
+                if (i < na) S.cell[i] = (uint16_t)lo[j];
             }
         }
-        __syncthreads();
         if (BATCH) {
             // agents of a run that leaves the batch take no part in pairing
 #pragma unroll
@@ -349,13 +461,14 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                 const bool fert = (m & kMetaFertile) != 0;
                 const bool male = (m & kMetaGender) != 0;
                 const int lc = fert ? S.cell[i] : 0;
-                uint32_t *ctr = male ? &S.nm[lc] : &S.nf[lc];
-                const uint32_t q = warp_agg_add(fert, ((uint32_t)lc << 1) | (male ? 1u : 0u), ctr, 1u);
+                const uint32_t q0 = warp_agg_add(fert, ((uint32_t)lc << 1) | (male ? 1u : 0u), &S.nfm[lc],
+                                                 male ? 0x10000u : 1u);
+                const uint32_t q = male ? (q0 >> 16) : (q0 & 0xffffu);
                 // the tile's FERTILE agents also go to a dense list (their list
                 // positions), so that the rank loop below runs on full warps
                 const uint32_t fb = __ballot_sync(FULL_MASK, fert);
                 uint32_t fbase = 0;
-                if ((tid & 31) == 0 && fb) fbase = atomicAdd(&S.nfert, (uint32_t)__popc(fb));
+                if (lane == 0 && fb) fbase = atomicAdd(&S.nfert, (uint32_t)__popc(fb));
                 fbase = __shfl_sync(FULL_MASK, fbase, 0);
                 if (fert) {
                     const uint32_t pos = male ? (S.cstart[lc + 1] - 1u - q) : (S.cstart[lc] + q);
@@ -363,51 +476,65 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                     S.fid[pos] = pid[j];
                     S.oadq[fbase + __popc(fb & lanemask_lt())] = (uint16_t)pos;
                 }
+                // high words of the IDs: the ranks compare 32-bit keys while all are zero
+                const uint32_t hi = __reduce_or_sync(FULL_MASK, fert ? (uint32_t)((uint64_t)pid[j] >> 32) : 0u);
+                if (lane == 0 && hi) atomicOr(&S.idhi, hi);
             }
             __syncthreads();
             // rank by ID within the own sex's list (IDs are unique), over the
-            // dense list of FERTILE agents; each agent goes to its place in
-            // its cell's ID-ordered lists (females, then males)
+            // dense list of FERTILE agents; each agent goes to its place in its
+            // cell's ID-ordered lists (females, then males), and the members of
+            // the smaller side (the picking side) to the dense list of pickers
             const uint32_t nfe = S.nfert;
-            for (uint32_t q = tid; q < nfe; q += TT) {
-                const int pos = S.oadq[q];
-                const int i = S.pick[pos];
-                const int lc = S.cell[i];
-                const int64_t x = S.fid[pos];
-                const bool male = (S.meta[i] & kMetaGender) != 0;
-                int b, e;
-                if (male) {
-                    e = (int)S.cstart[lc + 1];
-                    b = e - (int)S.nm[lc];
-                } else {
-                    b = (int)S.cstart[lc];
-                    e = b + (int)S.nf[lc];
+            const bool k32 = S.idhi == 0u;
+            const uint32_t *f32 = reinterpret_cast<const uint32_t *>(S.fid);
+            for (uint32_t qb = 0; qb < nfe; qb += TT) {
+                const uint32_t q = qb + (uint32_t)tid;
+                bool picker = false;
+                int pos = 0;
+                if (q < nfe) {
+                    pos = S.oadq[q];
+                    const int i = S.pick[pos];
+                    const int lc = S.cell[i];
+                    const int cs = (int)S.cstart[lc], ce = (int)S.cstart[lc + 1];
+                    const uint32_t w = S.nfm[lc];
+                    const int nF = (int)(w & 0xffffu), nM = (int)(w >> 16);
+                    const bool male = pos >= cs + nF;
+                    const int b = male ? ce - nM : cs;
+                    const int e = male ? ce : cs + nF;
+                    int r = 0;
+                    if (k32) {
+                        const uint32_t x = f32[2 * pos];
+                        int k = b;
+                        for (; k + 4 <= e; k += 4) {
+                            r += (f32[2 * k] < x ? 1 : 0) + (f32[2 * k + 2] < x ? 1 : 0) +
+                                 (f32[2 * k + 4] < x ? 1 : 0) + (f32[2 * k + 6] < x ? 1 : 0);
+                        }
+                        for (; k < e; k++) r += (f32[2 * k] < x) ? 1 : 0;
+                    } else {
+                        const int64_t x = S.fid[pos];
+                        for (int k = b; k < e; k++) r += (S.fid[k] < x) ? 1 : 0;
+                    }
+                    S.frank[i] = (uint16_t)r;
+                    S.list[cs + (male ? nF : 0) + r] = (uint16_t)i;
+                    picker = nF > 0 && nM > 0 && (male == (nM < nF));
                 }
-                int r = 0;
-                for (int k = b; k < e; k++) r += (S.fid[k] < x) ? 1 : 0;
-                S.frank[i] = (uint16_t)r;
-                S.list[S.cstart[lc] + (male ? S.nf[lc] : 0u) + (uint32_t)r] = (uint16_t)i;
-            }
-            __syncthreads();
-            // the members of the smaller side pick, in ID order; gather them densely
-            for (int lc = tid; lc < nc; lc += TT) {
-                const uint32_t nF = S.nf[lc], nM = S.nm[lc];
-                if (nF > 0u && nM > 0u) {
-                    const bool femSmall = nF <= nM;
-                    const uint32_t m = femSmall ? nF : nM;
-                    const uint32_t at = atomicAdd(&S.npick, m);
-                    const uint32_t from = S.cstart[lc] + (femSmall ? 0u : nF);
-                    for (uint32_t q = 0; q < m; q++) S.pkrow[at + q] = S.list[from + q];
-                }
+                const uint32_t pk = __ballot_sync(FULL_MASK, picker);
+                uint32_t pbase = 0;
+                if (lane == 0 && pk) pbase = atomicAdd(&S.npick, (uint32_t)__popc(pk));
+                pbase = __shfl_sync(FULL_MASK, pbase, 0);
+                if (picker) S.pkpos[pbase + __popc(pk & lanemask_lt())] = (uint16_t)pos;
             }
             __syncthreads();
             // pick j takes the pick[j]-th still unpaired member of the larger
             // side, pick[j] = (int)wrandr(0, nL - j)
             const uint32_t npk = S.npick;
             for (uint32_t q = tid; q < npk; q += TT) {
-                const int i = S.pkrow[q];
+                const int pos = S.pkpos[q];
+                const int i = S.pick[pos];
                 const int lc = S.cell[i];
-                const uint32_t nF = S.nf[lc], nM = S.nm[lc];
+                const uint32_t w = S.nfm[lc];
+                const uint32_t nF = w & 0xffffu, nM = w >> 16;
                 const uint32_t nL = (nF <= nM) ? nM : nF;
                 const uint32_t j = S.frank[i];
                 uint64_t sd = P.seed;
@@ -417,22 +544,23 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                     sd = R.seed;
                     st = step - R.step0;
                 }
-                const uint32_t u = draw_block(sd, (uint32_t)st, id[a0 + i], kStreamPair).v[0];
-                S.pick[S.cstart[lc] + j] = (uint16_t)(((uint64_t)(nL - j) * (uint64_t)u) >> 32);
+                const uint32_t u = draw_block(sd, (uint32_t)st, S.fid[pos], kStreamPair).v[0];
+                S.oadq[S.cstart[lc] + j] = (uint16_t)(((uint64_t)(nL - j) * (uint64_t)u) >> 32);
             }
             __syncthreads();
             // the member taken by pick j, decoded on its own: start from pick[j]
             // and for i = j-1 down to 0 step over the member pick i took when it
             // lies at or below
             for (uint32_t q = tid; q < npk; q += TT) {
-                const int i = S.pkrow[q];
+                const int i = S.pick[S.pkpos[q]];
                 const int lc = S.cell[i];
-                const uint32_t nF = S.nf[lc], nM = S.nm[lc];
+                const uint32_t w = S.nfm[lc];
+                const uint32_t nF = w & 0xffffu, nM = w >> 16;
                 const bool femSmall = nF <= nM;
                 const int cs = (int)S.cstart[lc];
                 const int j = S.frank[i];
-                uint32_t p = S.pick[cs + j];
-                for (int k = j - 1; k >= 0; k--) p += (p >= S.pick[cs + k]) ? 1u : 0u;
+                uint32_t p = S.oadq[cs + j];
+                for (int k = j - 1; k >= 0; k--) p += (p >= S.oadq[cs + k]) ? 1u : 0u;
                 const uint32_t nL = femSmall ? nM : nF;
                 if (p >= nL) {   // cannot happen: every pick finds a free member
                     set_error(rs, kErrInternal, 1u);
@@ -444,123 +572,82 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             }
             __syncthreads();
         }
-        // ---- every action on every agent (SPopulation::doActions)
-        constexpr bool kDeferOad = prog_defers_oad(PROG);
-        static_assert(sizeof(uint16_t) * TM >= sizeof(uint32_t) * kTileCells, "per-cell counters alias pkrow");
-        uint32_t *const dm = reinterpret_cast<uint32_t *>(S.pkrow);   // batches: deaths | moves << 16 per cell
-        if (BATCH) {
-            for (int lc = tid; lc < nc; lc += TT) dm[lc] = 0u;
+        // the next tile's first row and end, requested while this tile works
+        if (tn < ntiles) {
+            na0 = ne_start[nr0];
+            na1 = ne_start[nr1];
         }
+        // ---- every action on every agent (SPopulation::doActions), then the
+        // outcome word with the agent's rank in its cell's class; agents
+        // inside the OldAgeDeath window wait for the dense pass below
+        uint32_t mothers = 0u;   // bit j: row tid + j*TT gives birth
 #pragma unroll
         for (int j = 0; j < RA; j++) {
             const int i = tid + j * TT;
-            if (i >= na) break;
-            const uint32_t row = a0 + (uint32_t)i;
-            const int lc = S.cell[i];
-            const int c = S.cid[lc];
-            const uint8_t m8 = pm[j];
-            const BatchRun *R = BATCH ? BB.runs + S.crun[lc] : nullptr;
-            if (BATCH && !R->active) {   // the run leaves the batch: drop its agents
-                S.oc[i] = kOutDropped;
-                S.bfl[i] = 0;
-                continue;
+            if (__all_sync(FULL_MASK, i >= na)) break;
+            const bool in_tile = i < na;
+            uint8_t oc = 0;
+            bool queued = false;
+            float fa = 0.0f;
+            int lc = 0;
+            if (in_tile) {
+                const uint32_t row = a0 + (uint32_t)i;
+                lc = S.cell[i];
+                const int c = S.cid[lc];
+                const uint8_t m8 = pm[j];
+                const BatchRun *R = BATCH ? BB.runs + S.crun[lc] : nullptr;
+                if (BATCH && !R->active) {   // the run leaves the batch: drop its agents
+                    oc = kOutDropped;
+                } else {
+                    CellView cv;
+                    cv.tk = S.tk[lc];
+                    cv.tb = S.tb[lc];
+                    cv.td = S.td[lc];
+                    cv.nn = S.nn[lc];
+                    cv.vm = S.vm[lc];
+                    cv.wf = S.wf[lc];
+                    cv.c = (uint32_t)c;
+                    const int mate = S.mate[i];
+                    oc = agent_outcome<PROG, BATCH, kDeferOad>(P, R, step, fT, pid[j], m8, pb[j], pa[j], pl[j],
+                                                               mate >= 0, cv, wthr, fa, queued, cnt_deaths, cnt_moves);
+                    if (oc & kOutBirth) {
+                        father[row] = (int32_t)(a0 + (uint32_t)mate);
+                        cnt_births++;
+                        mothers |= 1u << j;
+                    }
+                }
+                S.oc[i] = oc;
             }
-            const uint64_t seed = BATCH ? R->seed : P.seed;
-            const int32_t stepR = BATCH ? step - R->step0 : step;
-            const float fTR = BATCH ? (float)stepR : fT;
-            const float fb = pb[j];
-            float fa = pa[j];
-            const float fl = pl[j];
-            const bool female = !(m8 & kMetaGender);
-            bool fert = (m8 & kMetaFertile) != 0;
-            bool alive = true;
-            bool bflag = false;
-            int dir = 0;
-            AgentDraws dr;
-            dr.init(seed, (uint32_t)stepR, pid[j]);
-            constexpr int NA = PROG ? prog_len(PROG) : kMaxActions;
-#pragma unroll (PROG ? NA : 1)
-            for (int a = 0; a < NA; a++) {
-                if ((PROG == 0 && a >= P.n_act) || !alive) break;
-                const ActionConst &A = BATCH ? R->act[a] : P.act[a];
-                switch (PROG ? prog_act(PROG, a) : A.type) {
-                case kGetOld:
-                    fa = __fsub_rn(fTR, fb);
-                    break;
-                case kFertility:
-                    if (female) fert = (fa > A.f0) && (fa < A.f1) && (__fsub_rn(fTR, fl) > A.f2);
-                    else fert = fa > A.f0;
-                    break;
-                case kVerhulst:
-                case kVerhulstVarK: {
-                    uint32_t k = A.window;
-                    const int kind = S.tk[lc];
-                    if (kind == 1) {
-                        if (female && S.mate[i] >= 0) {
-                            if ((uint64_t)dr.get(k++) < S.tb[lc]) bflag = true;
-                        }
-                    } else if (kind == 2) {
-                        if ((uint64_t)dr.get(k++) < S.tb[lc]) alive = false;
+            if (kDeferOad) {
+                const uint32_t qm = __ballot_sync(FULL_MASK, queued);
+                if (qm) {
+                    uint32_t qbase = 0;
+                    if (lane == 0) qbase = atomicAdd(&S.noad, (uint32_t)__popc(qm));
+                    qbase = __shfl_sync(FULL_MASK, qbase, 0);
+                    if (queued) {
+                        const uint32_t q = qbase + __popc(qm & lanemask_lt());
+                        S.oadq[q] = (uint16_t)i;
+                        S.fid[q] = pid[j];
+                        S.ofa[q] = fa;
                     }
-                    if (alive) {
-                        if ((uint64_t)dr.get(k) < S.td[lc]) alive = false;
-                    }
-                    if (!alive) cnt_deaths++;
-                    break;
-                }
-                case kOldAgeDeath: {
-                    fa = __fsub_rn(fTR, fb);
-                    bool die = false;
-                    if (fa <= A.age_lo) {
-                        die = false;
-                    } else if (fa > A.age_hi) {
-                        die = true;
-                    } else if (kDeferOad) {
-                        S.oadq[atomicAdd(&S.noad, 1u)] = (uint16_t)i;
-                    } else {
-                        const uint32_t u = dr.get(A.window);
-                        const double t = __dmul_rn(__dmul_rn(A.oad_w, (double)u), 2.3283064365386962890625e-10);
-                        const double thr = __dadd_rn(A.oad_M, __dadd_rn(A.oad_a, t));
-                        die = (double)fa > thr;
-                    }
-                    if (die) { alive = false; cnt_deaths++; }
-                    break;
-                }
-                case kRandomMove: {
-                    if ((uint64_t)dr.get(A.window) < A.pthr) {
-                        const int nn = S.nn[lc];
-                        const uint32_t u2 = dr.get(A.window + 1);
-                        const int d = (int)(((uint64_t)(nn + 1) * (uint64_t)u2) >> 32);
-                        if (d > 0 && ((S.vm[lc] >> (d - 1)) & 1u)) { dir = d; cnt_moves++; }
-                    }
-                    break;
-                }
-                case kWeightedMove: {
-                    if ((uint64_t)dr.get(A.window) < A.pthr) {
-                        const int nn = S.nn[lc];
-                        const uint32_t u2 = dr.get(A.window + 1);
-                        int d;
-                        if (S.wf[lc] & 1u) {
-                            d = (int)(((uint64_t)(nn + 1) * (uint64_t)u2) >> 32);
-                        } else {
-                            d = 0;
-                            for (int q = 0; q < nn; q++) d += (wthr[c * 6 + q] <= (uint64_t)u2) ? 1 : 0;
-                        }
-                        if (d > 0 && ((S.vm[lc] >> (d - 1)) & 1u)) { dir = d; cnt_moves++; }
-                    }
-                    break;
-                }
-                default:
-                    break;
                 }
             }
-            const int cls = alive ? (1 + dir) : 0;
-            S.oc[i] = (uint8_t)(cls | (bflag ? kOutBirth : 0) | (fert ? kOutFertile : 0) |
-                                ((m8 & kMetaGender) ? kOutGender : 0) | (dir > 0 ? kOutMoved : 0));
-            S.bfl[i] = bflag ? 1 : 0;
-            if (bflag) {
-                father[row] = (int32_t)(a0 + (uint32_t)S.mate[i]);
-                cnt_births++;
+            // outcome word: outcome byte | local cell << 8 | rank in the cell's class << 17
+            const int cls = oc & 7;
+            const uint32_t rank = class_rank(in_tile && !queued && cls > 0, lc, cls, S.cls);
+            if (in_tile && !queued) outc[a0 + (uint32_t)i] = (uint32_t)oc | ((uint32_t)lc << 8) | (rank << 17);
+            // mothers: a list per cell of their ID ranks (births are rare: most
+            // warps have none and skip the aggregation)
+            const bool mother = (mothers >> j) & 1u;
+            if (__any_sync(FULL_MASK, mother)) {
+                const uint32_t mq = warp_agg_add(mother, ((uint32_t)lc << 3) | 7u, &S.cls[lc][3], 1u << 16) >> 16;
+                if (mother) S.pick[S.cstart[lc] + mq] = S.frank[i];
+            }
+            if (BATCH) {
+                const bool died = in_tile && !queued && cls == 0 && !(oc & kOutDropped);
+                const bool moved = in_tile && !queued && (oc & kOutMoved);
+                if (__any_sync(FULL_MASK, died)) warp_agg_add(died, (uint32_t)lc, &S.dm[lc], 1u);
+                if (__any_sync(FULL_MASK, moved)) warp_agg_add(moved, (uint32_t)lc, &S.dm[lc], 1u << 16);
             }
         }
         if (kDeferOad) {
@@ -569,74 +656,62 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             __syncthreads();
             const uint32_t nq = S.noad;
             constexpr int kOad = prog_len(PROG) - 1;
-            for (uint32_t q = tid; q < nq; q += TT) {
-                const int i = S.oadq[q];
-                const BatchRun *R = BATCH ? BB.runs + S.crun[S.cell[i]] : nullptr;
-                const ActionConst &A = BATCH ? R->act[kOad] : P.act[kOad];
-                const int32_t stepR = BATCH ? step - R->step0 : step;
-                const float fa = __fsub_rn((float)stepR, birth[a0 + i]);
-                const uint32_t w = A.window;
-                const uint32_t u = pick4(draw_block(BATCH ? R->seed : P.seed, (uint32_t)stepR, id[a0 + i],
-                                                    kStreamActions + (w >> 2)), w & 3u);
-                const double t = __dmul_rn(__dmul_rn(A.oad_w, (double)u), 2.3283064365386962890625e-10);
-                const double thr = __dadd_rn(A.oad_M, __dadd_rn(A.oad_a, t));
-                if ((double)fa > thr) {
-                    S.oc[i] = (uint8_t)(S.oc[i] & ~7u);
-                    cnt_deaths++;
+            for (uint32_t qb = 0; qb < nq; qb += TT) {
+                const uint32_t q = qb + (uint32_t)tid;
+                const bool valid = q < nq;
+                int i = 0, lc = 0;
+                uint8_t oc = 0;
+                if (valid) {
+                    i = S.oadq[q];
+                    lc = S.cell[i];
+                    oc = S.oc[i];
+                    const BatchRun *R = BATCH ? BB.runs + S.crun[lc] : nullptr;
+                    const ActionConst &A = BATCH ? R->act[kOad] : P.act[kOad];
+                    const int32_t stepR = BATCH ? step - R->step0 : step;
+                    const uint32_t w = A.window;
+                    const uint32_t u = pick4(draw_block(BATCH ? R->seed : P.seed, (uint32_t)stepR, S.fid[q],
+                                                        kStreamActions + (w >> 2)), w & 3u);
+                    const double th = __dmul_rn(__dmul_rn(A.oad_w, (double)u), 2.3283064365386962890625e-10);
+                    const double thr = __dadd_rn(A.oad_M, __dadd_rn(A.oad_a, th));
+                    if ((double)S.ofa[q] > thr) {
+                        oc = (uint8_t)(oc & ~7u);
+                        cnt_deaths++;
+                    }
+                }
+                const int cls = oc & 7;
+                const uint32_t rank = class_rank(valid && cls > 0, lc, cls, S.cls);
+                if (valid) outc[a0 + (uint32_t)i] = (uint32_t)oc | ((uint32_t)lc << 8) | (rank << 17);
+                if (BATCH) {
+                    const bool died = valid && cls == 0;
+                    const bool moved = valid && (oc & kOutMoved);
+                    if (__any_sync(FULL_MASK, died)) warp_agg_add(died, (uint32_t)lc, &S.dm[lc], 1u);
+                    if (__any_sync(FULL_MASK, moved)) warp_agg_add(moved, (uint32_t)lc, &S.dm[lc], 1u << 16);
                 }
             }
         }
         __syncthreads();
-        // outcome words and per-cell class counts (slot 0 stay, 1..6 movers,
-        // 7 births), two 16-bit counters per shared word, one atomic per
-        // (cell, slot) and warp.  The count an agent finds is its rank in its
-        // cell's class, which the scatter uses as its offset: rows of a cell
-        // are not in ID order, nothing depends on their order.
-#pragma unroll
-        for (int j = 0; j < RA; j++) {
-            const int i = tid + j * TT;
-            if (__all_sync(FULL_MASK, i >= na)) break;
-            const bool in_tile = i < na;
-            const uint8_t oc = in_tile ? S.oc[i] : (uint8_t)0;
-            const int cls = oc & 7;
-            const bool bflag = (oc & kOutBirth) != 0;
-            const int lc = in_tile ? S.cell[i] : 0;
-            const int slot = (cls > 0) ? cls - 1 : 0;
-            const uint32_t q = warp_agg_add(in_tile && cls > 0, ((uint32_t)lc << 3) | (uint32_t)slot,
-                                            &S.cls[lc][slot >> 1], 1u << (16 * (slot & 1)));
-            const uint32_t rank = (q >> (16 * (slot & 1))) & 0xffffu;
-            // outcome byte | local cell << 8 | rank in the cell's class << 17
-            if (in_tile) outc[a0 + (uint32_t)i] = (uint32_t)oc | ((uint32_t)lc << 8) | (rank << 17);
-            // births are rare: most warps have none and skip the aggregation
-            if (__any_sync(FULL_MASK, in_tile && bflag)) {
-                warp_agg_add(in_tile && bflag, ((uint32_t)lc << 3) | 7u, &S.cls[lc][3], 1u << 16);
-            }
-            if (BATCH) {
-                const bool died = in_tile && cls == 0 && !(oc & kOutDropped);
-                const bool moved = in_tile && (oc & kOutMoved);
-                if (__any_sync(FULL_MASK, died)) warp_agg_add(died, (uint32_t)lc, &dm[lc], 1u);
-                if (__any_sync(FULL_MASK, moved)) warp_agg_add(moved, (uint32_t)lc, &dm[lc], 1u << 16);
-            }
-        }
-        __syncthreads();
-        // ---- per cell: mothers' birth ranks by ID (births are numbered in
-        // (cell, mother ID) order) and the class counts
+        // ---- per cell: the class counts; per mother: her birth rank, the
+        // number of her cell's mothers with a smaller ID (births are numbered
+        // in (cell, mother ID) order)
         for (int lc = tid; lc < nc; lc += TT) {
-            const int cs = (int)S.cstart[lc];
-            const int nF = (int)S.nf[lc];
-            uint32_t r = 0;
-            if (S.cls[lc][3] >> 16) {
-                for (int q = 0; q < nF; q++) {
-                    const int ai = S.list[cs + q];
-                    if (S.bfl[ai]) brank[a0 + ai] = (uint16_t)(r++);
-                }
-            }
             const uint32_t c = (uint32_t)S.cid[lc];
             uint4 *dst = reinterpret_cast<uint4 *>(clsc + (size_t)c * kCls);
             const uint32_t w0 = S.cls[lc][0], w1 = S.cls[lc][1], w2 = S.cls[lc][2], w3 = S.cls[lc][3];
             dst[0] = make_uint4(w0 & 0xffffu, w0 >> 16, w1 & 0xffffu, w1 >> 16);
             dst[1] = make_uint4(w2 & 0xffffu, w2 >> 16, w3 & 0xffffu, w3 >> 16);
-            if (BATCH) BB.cstat[c] = dm[lc];   // deaths | registered moves << 16
+            if (BATCH) BB.cstat[c] = S.dm[lc];   // deaths | registered moves << 16
+        }
+#pragma unroll
+        for (int j = 0; j < RA; j++) {
+            if (!((mothers >> j) & 1u)) continue;
+            const int i = tid + j * TT;
+            const int lc = S.cell[i];
+            const int cs = (int)S.cstart[lc];
+            const int nmo = (int)(S.cls[lc][3] >> 16);
+            const uint32_t fr = S.frank[i];
+            uint32_t r = 0;
+            for (int k = 0; k < nmo; k++) r += (S.pick[cs + k] < fr) ? 1u : 0u;
+            brank[a0 + (uint32_t)i] = (uint16_t)r;
         }
     }
     // statistics of the step (batches: per run, by the cell scan)
@@ -713,6 +788,7 @@ k_cell_scan(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             const int32_t *__restrict__ nbr, const uint8_t *__restrict__ nnbr,
             const uint32_t *__restrict__ rev, const uint32_t *__restrict__ clsc,
             const double *__restrict__ Kc, ulonglong2 *__restrict__ vthr,
+            const uint32_t *__restrict__ cmove, uint32_t *__restrict__ necm,
             uint32_t *__restrict__ sbase, uint32_t *__restrict__ bbase,
             uint32_t *__restrict__ bidbase, uint32_t *__restrict__ obase,
             uint32_t *__restrict__ new_nonempty, uint32_t *__restrict__ new_ne_start,
@@ -915,13 +991,16 @@ k_cell_scan(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             if (nnew[j] > 0u) {
                 new_nonempty[pre.ne] = (uint32_t)d;
                 new_ne_start[pre.ne] = pre.n;
+                // the next step's Verhulst thresholds and move word of the cell, by
+                // its position in the next table's non-empty list
                 if (P.n_verhulst > 0) {
                     if (!BATCH) {
-                        vthr[d] = verhulst_thresholds(P.act[P.verhulst_act[0]], Kc[d], nnew[j]);
+                        vthr[pre.ne] = verhulst_thresholds(P.act[P.verhulst_act[0]], Kc[d], nnew[j]);
                     } else if (crn[j] != kNoRun) {
-                        vthr[d] = verhulst_thresholds(BB.runs[crn[j]].act[P.verhulst_act[0]], Kc[d], nnew[j]);
+                        vthr[pre.ne] = verhulst_thresholds(BB.runs[crn[j]].act[P.verhulst_act[0]], Kc[d], nnew[j]);
                     }
                 }
+                if (P.has_move) necm[pre.ne] = cmove[d];
                 // tiles begin at the first cell starting at or after t * kTileAgents
                 // (rows past the capacity are never written: the step fails with kErrCapacity)
                 const uint32_t e = min(pre.n + nnew[j], P.capacity);
@@ -945,16 +1024,79 @@ k_cell_scan(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
 }
 
 // ----------------------------------------------------------------- scatter
+// The last CTA of a step's scatter commits the step: agent and cell counts,
+// next ID, statistics, genome free list, the form of the next step (the big
+// form applies it).  Every thread of the CTA calls it; `flag` is a shared word.
+template <bool BATCH, bool BIG>
+__device__ __forceinline__ void commit_step(const StepConst &P, const BatchBuffers &BB, RunState *__restrict__ rs,
+                                            uint32_t *flag) {
+    const int tid = threadIdx.x;
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        const uint32_t done = atomicAdd(&rs->scatter_ctas_done, 1u);
+        *flag = 0u;
+        if (done == gridDim.x - 1) {
+            __threadfence();
+            rs->scatter_ctas_done = 0u;
+            if (atomicAdd(&rs->error, 0u) != 0u) {   // a CTA failed: keep the old table
+                rs->dead_count = 0u;
+            } else {
+                *flag = 1u;
+            }
+        }
+    }
+    __syncthreads();
+    const uint32_t step = (uint32_t)rs->step;
+    if (BATCH && *flag) {
+        // per run: next ID after this step's births; the next ring slot starts at zero
+        const uint32_t sl = step % kBatchRing, sn = (step + 1u) % kBatchRing;
+        for (int r = tid; r < BB.nruns; r += blockDim.x) {
+            BB.rnext[r] += (int64_t)BB.rstat[((size_t)r * kBatchRing + sl) * 4 + 1];
+            uint4 *z = reinterpret_cast<uint4 *>(BB.rstat + ((size_t)r * kBatchRing + sn) * 4);
+            *z = make_uint4(0u, 0u, 0u, 0u);
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    if (tid == 0 && *flag) {
+        rs->stats[step % kStatsRing][0] = rs->new_n_agents;
+        unsigned long long *nx = rs->stats[(step + 1u) % kStatsRing];
+        nx[0] = 0ull; nx[1] = 0ull; nx[2] = 0ull; nx[3] = 0ull;
+        rs->n_agents = rs->new_n_agents;
+        rs->n_nonempty = rs->new_n_nonempty;
+        rs->big_next = (rs->max_cell > (uint32_t)kMaxCell) ? 1u : 0u;
+        if (BIG) rs->big = rs->big_next;
+        rs->max_cell = 0u;
+        rs->next_id += (int64_t)rs->births;
+        rs->birth_log_n += rs->births;
+        rs->action_tiles = 0u;
+        rs->scatter_tiles = 0u;
+        if (P.genome_words > 0) {
+            const uint32_t b = rs->births, nf = rs->nfree;
+            rs->hwm += (b > nf) ? b - nf : 0u;
+            rs->nfree = (nf > b ? nf - b : 0u) + rs->dead_count;
+            rs->dead_count = 0u;
+            rs->genome_step = (int32_t)step;
+        }
+        rs->step = (int32_t)(step + 1u);
+        __threadfence();
+    }
+}
+
 template <int TM, int TT>
 struct ScatterSmemT {
     uint32_t sb[kTileCells];       // first row of the cell's stayers in the next table
     uint32_t bb[kTileCells];       // first row of its newborns
     uint32_t bid[kTileCells];      // birth number of its first newborn
     uint32_t ob[kTileCells][6];    // first row of its movers, per neighbour slot
-    uint32_t brow[TM];             // the tile's mothers: row | local cell << 16 (dense)
+    int64_t bmid[TM];              // the tile's mothers (dense): IDs,
+    uint32_t brow[TM];             // ... row | local cell << 16,
+    int32_t bfr[TM];               // ... their mates' rows,
+    uint16_t brk[TM];              // ... their birth ranks in the cell
     uint32_t crn[kTileCells];      // batches: run of each cell
     float cft[kTileCells];         // batches: time of the cell's run
-    uint32_t nb;
+    uint32_t nb[2];                // mothers of the tile, by parity of the CTA's tile count
     uint32_t last;
 };
 
@@ -1000,6 +1142,7 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
     }
     __syncthreads();
     const int tid = threadIdx.x;
+    const int lane = tid & 31;
     const int32_t step = rs->step;
     const float fT = (float)step;
     const int64_t next_id = rs->next_id;
@@ -1022,23 +1165,33 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             freelist2[q] = freelist[births + q];
         }
     }
-    uint32_t nr0 = 0, nr1 = 0;
+    if (tid == 0) { S.nb[0] = 0u; S.nb[1] = 0u; }
+    // the bounds of the CTA's next tile are loaded one tile ahead
+    uint32_t nr0 = 0, nr1 = 0, na0 = 0, na1 = 0;
     if (blockIdx.x < ntiles) {
         nr0 = tile_first[blockIdx.x];
         nr1 = tile_first[blockIdx.x + 1];
+        na0 = ne_start[nr0];
+        na1 = ne_start[nr1];
     }
+    uint32_t par = 0u;   // parity of the tiles this CTA has worked on
     for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const uint32_t r0 = nr0;
         const int nc = (int)(nr1 - r0);
+        const uint32_t a0 = na0;
+        const int na = (int)(na1 - na0);
         const uint32_t tn = t + gridDim.x;
         if (tn < ntiles) {
             nr0 = tile_first[tn];
             nr1 = tile_first[tn + 1];
         }
-        if (nc == 0) continue;
-        const uint32_t a0 = ne_start[r0];
-        const int na = (int)(ne_start[r0 + nc] - a0);
-        if (na > TM || nc > kTileCells) continue;   // reported by k_actions
+        if (nc == 0 || na > TM || nc > kTileCells) {   // reported by k_actions
+            if (tn < ntiles) {
+                na0 = ne_start[nr0];
+                na1 = ne_start[nr1];
+            }
+            continue;
+        }
         uint32_t pc[RA];
         int64_t pid[RA];
         float pb[RA], pa[RA], pl[RA];
@@ -1058,7 +1211,6 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             }
         }
         __syncthreads();   // the previous tile is done with the shared arrays
-        if (tid == 0) S.nb = 0u;
         for (int lc = tid; lc < nc; lc += TT) {
             const uint32_t c = nonempty[r0 + lc];
             S.sb[lc] = sbase[c];
@@ -1081,6 +1233,34 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             z[0] = make_uint4(0u, 0u, 0u, 0u);
             z[1] = make_uint4(0u, 0u, 0u, 0u);
         }
+        // the tile's mothers to a dense list, with their mates and birth ranks
+        // (written by k_actions), read while the cell bases are on their way
+        if (tid == 0) S.nb[par ^ 1u] = 0u;   // the counter of the next tile
+#pragma unroll
+        for (int j = 0; j < RA; j++) {
+            const int i = tid + j * TT;
+            if (__all_sync(FULL_MASK, i >= na)) break;
+            const bool mo = i < na && (pc[j] & kOutBirth);
+            const uint32_t mm = __ballot_sync(FULL_MASK, mo);
+            if (mm) {
+                uint32_t base = 0;
+                if (lane == 0) base = atomicAdd(&S.nb[par], (uint32_t)__popc(mm));
+                base = __shfl_sync(FULL_MASK, base, 0);
+                if (mo) {
+                    const uint32_t q = base + __popc(mm & lanemask_lt());
+                    const uint32_t row = a0 + (uint32_t)i;
+                    S.brow[q] = (uint32_t)i | (((pc[j] >> 8) & 511u) << 16);
+                    S.bfr[q] = father[row];
+                    S.brk[q] = brank[row];
+                    S.bmid[q] = pid[j];
+                }
+            }
+        }
+        // the next tile's first row and end, requested while this tile works
+        if (tn < ntiles) {
+            na0 = ne_start[nr0];
+            na1 = ne_start[nr1];
+        }
         __syncthreads();
         // every agent to its cell's class base + its rank in the class (from
         // k_actions): survivors and movers into the next table
@@ -1099,47 +1279,44 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                     else set_error(rs, kErrInternal, 5u);
                 }
             }
-            if (!in_tile) continue;
+            if (!in_tile || k == 0) continue;
             const int lc = (int)((code >> 8) & 511u);
             if (lc >= nc) {   // inconsistent outcome word: record, never index past the tile
                 set_error(rs, kErrInternal, 7u);
                 continue;
             }
-            if (k) {
-                const uint32_t dst = ((k == 1) ? S.sb[lc] : S.ob[lc][k - 2]) + (code >> 17);
-                if (dst >= cap) {   // inconsistent bases: record, never write out of range
-                    set_error(rs, kErrInternal, 3u);
-                } else {
-                    const float fb = pb[j];
-                    id2[dst] = pid[j];
-                    birth2[dst] = fb;
-                    lastb2[dst] = pl[j];
-                    age2[dst] = P.age_from_birth ? __fsub_rn(BATCH ? S.cft[lc] : fT, fb) : pa[j];
-                    meta2[dst] = (uint8_t)(((code & kOutGender) ? kMetaGender : 0) |
-                                           ((code & kOutFertile) ? kMetaFertile : 0));
-                    if (genetics) gslot2[dst] = pg[j];
-                }
+            const uint32_t dst = ((k == 1) ? S.sb[lc] : S.ob[lc][k - 2]) + (code >> 17);
+            if (dst >= cap) {   // inconsistent bases: record, never write out of range
+                set_error(rs, kErrInternal, 3u);
+            } else {
+                const float fb = pb[j];
+                id2[dst] = pid[j];
+                birth2[dst] = fb;
+                lastb2[dst] = pl[j];
+                age2[dst] = P.age_from_birth ? __fsub_rn(BATCH ? S.cft[lc] : fT, fb) : pa[j];
+                meta2[dst] = (uint8_t)(((code & kOutGender) ? kMetaGender : 0) |
+                                       ((code & kOutFertile) ? kMetaFertile : 0));
+                if (genetics) gslot2[dst] = pg[j];
             }
-            if (code & kOutBirth) S.brow[atomicAdd(&S.nb, 1u)] = (uint32_t)i | ((uint32_t)lc << 16);
         }
         __syncthreads();
         // newborns, one thread per mother (SPopulation::createAgentAtIndex,
         // core/SPopulation.cpp:880-900): gender = (uchar)(2 * wrandd()) from the
         // mother's birth stream, females start FERTILE
-        const uint32_t nbt = S.nb;
+        const uint32_t nbt = S.nb[par];
         for (uint32_t q = tid; q < nbt; q += TT) {
             const int i = (int)(S.brow[q] & 0xffffu);
             const uint32_t row = a0 + (uint32_t)i;
             const int lc = (int)(S.brow[q] >> 16);
-            const uint32_t rk = brank[row];
-            const uint32_t dst = S.bb[lc] + rk;
-            const int32_t fr = father[row];
+            const uint32_t rk = S.brk[q];
+            const int32_t fr = S.bfr[q];
+            const uint32_t dst = (lc < nc ? S.bb[lc] : cap) + rk;
             const bool ok = dst < cap && fr >= 0 && (uint32_t)fr < N;
             if (!ok) {
                 set_error(rs, kErrInternal, 4u);
                 continue;
             }
-            const int64_t mid = id[row];
+            const int64_t mid = S.bmid[q];
             uint64_t sd = P.seed;
             int32_t st = step;
             float ft = fT;
@@ -1183,61 +1360,444 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                 }
             }
         }
+        par ^= 1u;
     }
-    // the last CTA to finish commits the step
-    __syncthreads();
-    if (tid == 0) {
-        __threadfence();
-        const uint32_t done = atomicAdd(&rs->scatter_ctas_done, 1u);
-        S.last = 0u;
-        if (done == gridDim.x - 1) {
-            __threadfence();
-            rs->scatter_ctas_done = 0u;
-            if (atomicAdd(&rs->error, 0u) != 0u) {   // a CTA failed: keep the old table
-                rs->dead_count = 0u;
+    commit_step<BATCH, BIG>(P, BB, rs, &S.last);
+}
+
+// ------------------------------------------------------ warp-per-cell kernels
+// The normal form of a step (no cell above kMaxCell agents): one warp works
+// on one non-empty cell at a time, with warp-level synchronisation only.
+// The warps of the grid take the cells of the non-empty list in turn
+// (warp g: cells g, g + G, g + 2G, ...; G the warps of the grid).
+constexpr int kCellThreads = 256;
+constexpr int kCellWarps = kCellThreads / 32;
+
+// per-warp shared memory of k_actions_cell (a cell of up to kMaxCell agents)
+struct CellWarpSmem {
+    uint32_t fk[kMaxCell];       // FERTILE members: low words of their IDs (list order)
+    uint16_t frow[kMaxCell];     // ... their rows in the cell; females from 0 up, males from n-1 down
+    uint16_t sidx[kMaxCell];     // list positions in ID order: females [0, nF), males [n - nM, n)
+    int16_t mate[kMaxCell];      // mate's row of each row, -1 none
+    uint16_t pick[kMaxCell / 2]; // pick value of each member of the smaller side (ID order)
+    uint8_t oc[kMaxCell];        // outcome byte of each row
+    uint32_t cnt[8];             // class counts: [0] stay, [1..6] movers per neighbour slot
+};
+
+// ID ranks of the FERTILE list entries [b, b + m) among themselves: entry k
+// goes to sidx[b + rank].  IDs are compared by their low words while all
+// high words are zero (wide == false), else in full (read from the table).
+__device__ __forceinline__ void rank_list(CellWarpSmem &W, int b, int m, bool wide, const int64_t *__restrict__ id,
+                                          uint32_t s) {
+    const int lane = threadIdx.x & 31;
+    for (int k0 = 0; k0 < m; k0 += 32) {
+        const int k = k0 + lane;
+        if (k < m) {
+            int r = 0;
+            if (!wide) {
+                const uint32_t x = W.fk[b + k];
+                int j = 0;
+                for (; j + 4 <= m; j += 4) {
+                    r += (W.fk[b + j] < x ? 1 : 0) + (W.fk[b + j + 1] < x ? 1 : 0) +
+                         (W.fk[b + j + 2] < x ? 1 : 0) + (W.fk[b + j + 3] < x ? 1 : 0);
+                }
+                for (; j < m; j++) r += (W.fk[b + j] < x) ? 1 : 0;
             } else {
-                S.last = 1u;
+                const int64_t x = id[s + W.frow[b + k]];
+                for (int j = 0; j < m; j++) r += (id[s + W.frow[b + j]] < x) ? 1 : 0;
+            }
+            W.sidx[b + r] = (uint16_t)(b + k);
+        }
+    }
+}
+
+template <int PROG, bool BATCH>
+__global__ void __launch_bounds__(kCellThreads, 4)
+k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
+               const uint32_t *__restrict__ nonempty, const uint32_t *__restrict__ ne_start,
+               const int64_t *__restrict__ id, const float *__restrict__ birth,
+               const float *__restrict__ age, const float *__restrict__ lastb,
+               const uint8_t *__restrict__ meta,
+               const ulonglong2 *__restrict__ vthr, const uint64_t *__restrict__ wthr,
+               const uint32_t *__restrict__ necm,
+               uint32_t *__restrict__ outc, int32_t *__restrict__ father, uint16_t *__restrict__ brank,
+               uint32_t *__restrict__ clsc) {
+    extern __shared__ __align__(16) unsigned char qhg_smem[];
+    __shared__ uint32_t red[kCellWarps];
+    CellWarpSmem &W = reinterpret_cast<CellWarpSmem *>(qhg_smem)[threadIdx.x >> 5];
+    if (rs->error != 0u) return;   // an earlier kernel failed: keep the state
+    if (rs->big != 0u) return;     // the big-cell form runs this step
+    const int lane = threadIdx.x & 31;
+    const uint32_t lt = lanemask_lt();
+    const int32_t step = rs->step;
+    const float fT = (float)step;
+    const uint32_t nne = rs->n_nonempty;
+    const uint32_t G = gridDim.x * kCellWarps;
+    uint32_t cnt_births = 0, cnt_deaths = 0, cnt_moves = 0;
+    // the bounds of the warp's next cell are loaded one cell ahead
+    uint32_t r = blockIdx.x * kCellWarps + (threadIdx.x >> 5);
+    uint32_t nb0 = 0, nb1 = 0;
+    if (r < nne) {
+        nb0 = ne_start[r];
+        nb1 = ne_start[r + 1];
+    }
+    for (; r < nne; r += G) {
+        const uint32_t s = nb0;
+        const int n = (int)(nb1 - nb0);
+        const uint32_t rn = r + G;
+        if (rn < nne) {
+            nb0 = ne_start[rn];
+            nb1 = ne_start[rn + 1];
+        }
+        // the cell: index, Verhulst thresholds (LinearBirth / LinearDeath
+        // ::initialize, actions/LinearBirth.cpp:90-112, actions/LinearDeath.cpp:92-122,
+        // computed by the previous step's cell scan) and move word
+        const uint32_t c = nonempty[r];
+        ulonglong2 v = make_ulonglong2(0ull, 0ull);
+        uint32_t cm = 0u;
+        if (P.n_verhulst > 0) v = vthr[r];
+        if (P.has_move) cm = necm[r];
+        if (n > kMaxCell) {   // cannot happen: such steps run the big-cell form
+            if (lane == 0) set_error(rs, kErrCellTooLarge, c);
+            continue;
+        }
+        const BatchRun *R = BATCH ? BB.runs + BB.crun[c] : nullptr;
+        const bool keep = !BATCH || R->active;   // a run that leaves the batch drops its agents
+        // ---- RandomPair::findMates (actions/RandomPair.cpp:146-270): FERTILE
+        // lists, ranked by ID; the members of the smaller side pick, in ID
+        // order, each pick drawn from the pairing stream of the picking member
+        int nF = 0, nM = 0;
+        bool wide = false;
+        if (P.has_pair && keep) {
+            for (int b = 0; b < n; b += 32) {
+                const int row = b + lane;
+                const bool valid = row < n;
+                const uint8_t m8 = valid ? meta[s + row] : (uint8_t)0;
+                const bool fert = (m8 & kMetaFertile) != 0;
+                const bool male = (m8 & kMetaGender) != 0;
+                int64_t x = 0;
+                if (fert) x = id[s + row];
+                const uint32_t fm = __ballot_sync(FULL_MASK, fert && !male);
+                const uint32_t mm = __ballot_sync(FULL_MASK, fert && male);
+                if (fert) {
+                    const int pos = male ? n - 1 - (nM + __popc(mm & lt)) : nF + __popc(fm & lt);
+                    W.fk[pos] = (uint32_t)(uint64_t)x;
+                    W.frow[pos] = (uint16_t)row;
+                }
+                if (valid) W.mate[row] = -1;
+                wide |= __any_sync(FULL_MASK, ((uint64_t)x >> 32) != 0ull);
+                nF += __popc(fm);
+                nM += __popc(mm);
+            }
+        }
+        const bool pairs = nF > 0 && nM > 0;
+        if (pairs) {
+            __syncwarp();
+            rank_list(W, 0, nF, wide, id, s);
+            rank_list(W, n - nM, nM, wide, id, s);
+            __syncwarp();
+            const bool femSmall = nF <= nM;
+            const int m = femSmall ? nF : nM;
+            const uint32_t nL = (uint32_t)(femSmall ? nM : nF);
+            const int sb = femSmall ? 0 : n - nM;   // smaller side in sidx
+            const int lb = femSmall ? n - nM : 0;   // larger side
+            uint64_t sd = P.seed;
+            int32_t st = step;
+            if (BATCH) {
+                sd = R->seed;
+                st = step - R->step0;
+            }
+            // pick j takes the pick[j]-th still unpaired member of the larger
+            // side, pick[j] = (int)wrandr(0, nL - j)
+            for (int j = lane; j < m; j += 32) {
+                const int pos = W.sidx[sb + j];
+                const int64_t x = wide ? id[s + W.frow[pos]] : (int64_t)W.fk[pos];
+                const uint32_t u = draw_block(sd, (uint32_t)st, x, kStreamPair).v[0];
+                W.pick[j] = (uint16_t)(((uint64_t)(nL - (uint32_t)j) * (uint64_t)u) >> 32);
+            }
+            __syncwarp();
+            // the member taken by pick j, decoded on its own: start from pick[j]
+            // and for i = j-1 down to 0 step over the member pick i took when it
+            // lies at or below (the lanes walk i down together)
+            for (int j0 = 0; j0 < m; j0 += 32) {
+                const int j = j0 + lane;
+                uint32_t p = (j < m) ? W.pick[j] : 0u;
+                const int top = min(m, j0 + 32) - 1;
+                for (int k = top - 1; k >= 0; k--) {
+                    const uint32_t pk = W.pick[k];
+                    if (k < j) p += (p >= pk) ? 1u : 0u;
+                }
+                if (j < m) {
+                    if (p >= nL) {   // cannot happen: every pick finds a free member
+                        set_error(rs, kErrInternal, 1u);
+                    } else {
+                        const int a = W.frow[W.sidx[sb + j]];
+                        const int b = W.frow[W.sidx[lb + (int)p]];
+                        W.mate[a] = (int16_t)b;
+                        W.mate[b] = (int16_t)a;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+        // ---- every action on every agent of the cell, then the outcome word
+        // with the agent's rank in its cell's class
+        CellView cv;
+        cv.tk = (uint32_t)(v.x >> 62);
+        cv.tb = v.x & ((1ull << 62) - 1ull);
+        cv.td = v.y;
+        cv.nn = cm & 7u;
+        cv.vm = (cm >> 8) & 63u;
+        cv.wf = (cm >> 16) & 1u;
+        cv.c = c;
+        if (lane < 8) W.cnt[lane] = 0u;
+        uint32_t births = 0, dead = 0, moved = 0;
+        __syncwarp();
+        for (int b = 0; b < n; b += 32) {
+            const int row = b + lane;
+            const bool valid = row < n;
+            uint8_t oc = 0;
+            if (valid) {
+                const uint32_t g = s + (uint32_t)row;
+                const uint8_t m8 = meta[g];
+                if (!keep) {
+                    oc = kOutDropped;
+                } else {
+                    const int mate = pairs ? W.mate[row] : -1;
+                    float fa;
+                    bool queued = false;
+                    oc = agent_outcome<PROG, BATCH, false>(P, R, step, fT, id[g], m8, birth[g],
+                                                           P.reads_age ? age[g] : 0.0f, lastb[g], mate >= 0, cv,
+                                                           wthr, fa, queued, cnt_deaths, cnt_moves);
+                    if (oc & kOutBirth) {
+                        father[g] = (int32_t)(s + (uint32_t)mate);
+                        cnt_births++;
+                    }
+                }
+                W.oc[row] = oc;
+            }
+            const int cls = oc & 7;
+            const bool counted = valid && cls > 0;
+            const uint32_t slot = counted ? (uint32_t)(cls - 1) : 0u;
+            const uint32_t peers = __match_any_sync(FULL_MASK, counted ? slot : 0xffu);
+            const uint32_t base = counted ? W.cnt[slot] : 0u;
+            __syncwarp();
+            if (counted && (peers & lt) == 0u) W.cnt[slot] = base + (uint32_t)__popc(peers);
+            // outcome byte | rank in the cell's class << 17
+            if (valid) outc[s + (uint32_t)row] = (uint32_t)oc | ((base + (uint32_t)__popc(peers & lt)) << 17);
+            births += __popc(__ballot_sync(FULL_MASK, valid && (oc & kOutBirth)));
+            if (BATCH) {
+                dead += __popc(__ballot_sync(FULL_MASK, valid && cls == 0 && !(oc & kOutDropped)));
+                moved += __popc(__ballot_sync(FULL_MASK, valid && (oc & kOutMoved)));
+            }
+            __syncwarp();
+        }
+        // ---- mothers' birth ranks: births are numbered in (cell, mother ID)
+        // order; mothers are FERTILE females, walked in ID order
+        if (births > 0u) {
+            uint32_t run = 0;
+            for (int q0 = 0; q0 < nF; q0 += 32) {
+                const int q = q0 + lane;
+                bool mo = false;
+                int row = 0;
+                if (q < nF) {
+                    row = W.frow[W.sidx[q]];
+                    mo = (W.oc[row] & kOutBirth) != 0;
+                }
+                const uint32_t mb = __ballot_sync(FULL_MASK, mo);
+                if (mo) brank[s + (uint32_t)row] = (uint16_t)(run + (uint32_t)__popc(mb & lt));
+                run += (uint32_t)__popc(mb);
+            }
+        }
+        // class counts of the cell: stay, movers per neighbour slot, births
+        if (lane < 8) clsc[(size_t)c * kCls + lane] = (lane < 7) ? W.cnt[lane] : births;
+        if (BATCH && lane == 0) BB.cstat[c] = dead | (moved << 16);   // deaths | registered moves << 16
+        __syncwarp();
+    }
+    // statistics of the step (batches: per run, by the cell scan)
+    if (BATCH) return;
+    const uint32_t tb_ = block_sum(cnt_births, red);
+    const uint32_t td_ = block_sum(cnt_deaths, red);
+    const uint32_t tm_ = block_sum(cnt_moves, red);
+    if (threadIdx.x == 0 && (tb_ | td_ | tm_)) {
+        unsigned long long *st = rs->stats[(uint32_t)step % kStatsRing];
+        atomicAdd(&st[1], (unsigned long long)tb_);
+        atomicAdd(&st[2], (unsigned long long)td_);
+        atomicAdd(&st[3], (unsigned long long)tm_);
+    }
+}
+
+template <bool BATCH>
+__global__ void __launch_bounds__(kCellThreads, 4)
+k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
+               const uint32_t *__restrict__ nonempty, const uint32_t *__restrict__ ne_start,
+               const int64_t *__restrict__ id, const float *__restrict__ birth,
+               const float *__restrict__ age, const float *__restrict__ lastb,
+               const uint32_t *__restrict__ outc, const int32_t *__restrict__ father,
+               const uint16_t *__restrict__ brank,
+               const uint32_t *__restrict__ sbase, const uint32_t *__restrict__ bbase,
+               const uint32_t *__restrict__ bidbase, const uint32_t *__restrict__ obase,
+               uint32_t *__restrict__ clsc,
+               int64_t *__restrict__ id2, float *__restrict__ birth2, float *__restrict__ age2,
+               float *__restrict__ lastb2, uint8_t *__restrict__ meta2,
+               int64_t *__restrict__ blog, uint64_t blog_cap,
+               const int32_t *__restrict__ gslot, int32_t *__restrict__ gslot2,
+               const uint32_t *__restrict__ freelist, uint32_t *__restrict__ freelist2,
+               uint32_t *__restrict__ brec) {
+    __shared__ uint32_t s_flag;
+    if (rs->error != 0u) return;   // the state stays as before the step
+    // the form of the step is read once per CTA (the big form, launched
+    // after this one, applies the next step's form)
+    if (threadIdx.x == 0) s_flag = rs->big;
+    __syncthreads();
+    if (s_flag != 0u) return;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int32_t step = rs->step;
+    const float fT = (float)step;
+    const int64_t next_id = rs->next_id;
+    const uint64_t blog_base = rs->birth_log_n;
+    const uint32_t N = rs->n_agents;
+    const uint32_t nne = rs->n_nonempty;
+    const uint32_t cap = P.capacity;
+    const uint32_t G = gridDim.x * kCellWarps;
+    // genome slots (SPopulation::recycleDeadSpaceNew, core/SPopulation.cpp:596-724):
+    // newborns take the slots freed by the previous step's deaths, in birth
+    // order, then never used slots; this step's deaths free theirs for the
+    // next step, so a newborn never overwrites a parent of the same step
+    const bool genetics = P.genome_words > 0;
+    const uint32_t births = rs->births;
+    const uint32_t nfree = rs->nfree;
+    const uint32_t hwm = rs->hwm;
+    const uint32_t carry = nfree > births ? nfree - births : 0u;
+    if (genetics) {
+        for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < carry; q += gridDim.x * blockDim.x) {
+            freelist2[q] = freelist[births + q];
+        }
+    }
+    uint32_t r = blockIdx.x * kCellWarps + (threadIdx.x >> 5);
+    uint32_t nb0 = 0, nb1 = 0;
+    if (r < nne) {
+        nb0 = ne_start[r];
+        nb1 = ne_start[r + 1];
+    }
+    for (; r < nne; r += G) {
+        const uint32_t s = nb0;
+        const int n = (int)(nb1 - nb0);
+        const uint32_t rn = r + G;
+        if (rn < nne) {
+            nb0 = ne_start[rn];
+            nb1 = ne_start[rn + 1];
+        }
+        // the cell's bases in the next table: stayers, newborns (and their
+        // birth numbers), movers per neighbour slot (lane k holds slot k)
+        const uint32_t c = nonempty[r];
+        const uint32_t sb = sbase[c];
+        const uint32_t bb = bbase[c];
+        uint32_t bid = bidbase[c];
+        const uint32_t ob = (lane < 6) ? obase[(size_t)c * 6 + lane] : 0u;
+        float ft = fT;
+        uint64_t sd = P.seed;
+        int32_t st = step;
+        int64_t nid = next_id;
+        if (BATCH) {
+            // birth ranks and IDs count within the run
+            const uint32_t rr = BB.crun[c];
+            const BatchRun &R = BB.runs[rr];
+            bid -= bidbase[R.cell0];
+            ft = (float)(step - R.step0);
+            sd = R.seed;
+            st = step - R.step0;
+            nid = BB.rnext[rr];
+        }
+        // the class counts are consumed: clear them for the next step
+        if (lane < 2) reinterpret_cast<uint4 *>(clsc + (size_t)c * kCls)[lane] = make_uint4(0u, 0u, 0u, 0u);
+        for (int b = 0; b < n; b += 32) {
+            const int row = b + lane;
+            const bool valid = row < n;
+            const uint32_t g = s + (uint32_t)row;
+            uint32_t code = 0u;
+            int64_t x = 0;
+            float fb = 0.0f, fa = 0.0f, fl = 0.0f;
+            int32_t gs = 0;
+            if (valid) {
+                code = outc[g];
+                x = id[g];
+                fb = birth[g];
+                fa = P.age_from_birth ? 0.0f : age[g];
+                fl = lastb[g];
+                if (genetics) gs = gslot[g];
+            }
+            const int k = code & 7;
+            const uint32_t obk = __shfl_sync(FULL_MASK, ob, k >= 2 ? k - 2 : 0);
+            if (genetics && __any_sync(FULL_MASK, valid && k == 0)) {
+                // the genome slot of an agent dying this step goes to the next free list
+                const uint32_t q = warp_agg_add(valid && k == 0, 0u, &rs->dead_count, 1u);
+                if (valid && k == 0) {
+                    if (carry + q < P.genome_capacity) freelist2[carry + q] = (uint32_t)gs;
+                    else set_error(rs, kErrInternal, 5u);
+                }
+            }
+            // every survivor to its cell's class base + its rank in the class
+            if (valid && k > 0) {
+                const uint32_t dst = ((k == 1) ? sb : obk) + (code >> 17);
+                if (dst >= cap) {   // inconsistent bases: record, never write out of range
+                    set_error(rs, kErrInternal, 3u);
+                } else {
+                    id2[dst] = x;
+                    birth2[dst] = fb;
+                    lastb2[dst] = fl;
+                    age2[dst] = P.age_from_birth ? __fsub_rn(ft, fb) : fa;
+                    meta2[dst] = (uint8_t)(((code & kOutGender) ? kMetaGender : 0) |
+                                           ((code & kOutFertile) ? kMetaFertile : 0));
+                    if (genetics) gslot2[dst] = gs;
+                }
+            }
+            // newborns (SPopulation::createAgentAtIndex, core/SPopulation.cpp:880-900):
+            // gender = (uchar)(2 * wrandd()) from the mother's birth stream,
+            // females start FERTILE
+            if (valid && (code & kOutBirth)) {
+                const uint32_t rk = brank[g];
+                const int32_t fr = father[g];
+                const uint32_t dst = bb + rk;
+                if (dst >= cap || fr < 0 || (uint32_t)fr >= N) {
+                    set_error(rs, kErrInternal, 4u);
+                } else {
+                    const uint32_t u = draw_block(sd, (uint32_t)st, x, kStreamBirth).v[0];
+                    const int64_t baby = nid + (int64_t)(bid + rk);
+                    id2[dst] = baby;
+                    birth2[dst] = ft;
+                    lastb2[dst] = 0.0f;
+                    age2[dst] = 0.0f;
+                    meta2[dst] = (uint8_t)((u >> 31) ? kMetaGender : kMetaFertile);
+                    if (genetics) {
+                        const uint32_t gr = bid + rk;   // birth rank of the step
+                        const uint32_t bs = gr < nfree ? freelist[gr] : hwm + (gr - nfree);
+                        if (bs >= P.genome_capacity) {
+                            set_error(rs, kErrCapacity, bs);
+                        } else {
+                            gslot2[dst] = (int32_t)bs;
+                            uint32_t *br = brec + (size_t)gr * 5;
+                            br[0] = (uint32_t)gs;
+                            br[1] = (uint32_t)gslot[fr];
+                            br[2] = bs;
+                            br[3] = (uint32_t)(uint64_t)x;
+                            br[4] = (uint32_t)((uint64_t)x >> 32);
+                        }
+                    }
+                    if (P.log_births) {
+                        const uint64_t li = blog_base + (uint64_t)(bid + rk);
+                        if (li < blog_cap) {
+                            blog[li * 3 + 0] = baby;
+                            blog[li * 3 + 1] = x;
+                            blog[li * 3 + 2] = id[fr];
+                        }
+                    }
+                }
             }
         }
     }
-    __syncthreads();
-    if (BATCH && S.last) {
-        // per run: next ID after this step's births; the next ring slot starts at zero
-        const uint32_t sl = (uint32_t)step % kBatchRing, sn = ((uint32_t)step + 1u) % kBatchRing;
-        for (int r = tid; r < BB.nruns; r += TT) {
-            BB.rnext[r] += (int64_t)BB.rstat[((size_t)r * kBatchRing + sl) * 4 + 1];
-            uint4 *z = reinterpret_cast<uint4 *>(BB.rstat + ((size_t)r * kBatchRing + sn) * 4);
-            *z = make_uint4(0u, 0u, 0u, 0u);
-        }
-        __threadfence();
-    }
-    __syncthreads();
-    if (tid == 0) {
-        if (S.last) {
-            const uint32_t st = (uint32_t)rs->step;
-            rs->stats[st % kStatsRing][0] = rs->new_n_agents;
-            unsigned long long *nx = rs->stats[(st + 1u) % kStatsRing];
-            nx[0] = 0ull; nx[1] = 0ull; nx[2] = 0ull; nx[3] = 0ull;
-            rs->n_agents = rs->new_n_agents;
-            rs->n_nonempty = rs->new_n_nonempty;
-            rs->big_next = (rs->max_cell > (uint32_t)kMaxCell) ? 1u : 0u;
-            if (BIG) rs->big = rs->big_next;
-            rs->max_cell = 0u;
-            rs->next_id += (int64_t)rs->births;
-            rs->birth_log_n += rs->births;
-            rs->action_tiles = 0u;
-            rs->scatter_tiles = 0u;
-            if (P.genome_words > 0) {
-                const uint32_t b = rs->births, nf = rs->nfree;
-                rs->hwm += (b > nf) ? b - nf : 0u;
-                rs->nfree = (nf > b ? nf - b : 0u) + rs->dead_count;
-                rs->dead_count = 0u;
-                rs->genome_step = (int32_t)st;
-            }
-            rs->step = (int32_t)(st + 1u);
-            __threadfence();
-        }
-    }
+    commit_step<BATCH, false>(P, BB, rs, &s_flag);
 }
 
 // ----------------------------------------------------------------- genomes
@@ -1575,7 +2135,7 @@ extern "C" int qhg_launch_upload(const qhg::StepConst *P, qhg::RunState *rs, con
     BatchBuffers BB;
     memset(&BB, 0, sizeof(BB));
     k_cell_scan<false><<<ntiles, kScanThreads, 0, stream>>>(
-        *P, BB, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr2, B->sbase, B->bbase, B->bidbase,
+        *P, BB, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr2, B->cmove, B->necm2, B->sbase, B->bbase, B->bidbase,
         B->obase, B->nonempty2, B->ne_start2, B->tile_first2, B->tile_flag, B->tile_agg, B->tile_incl);
     if (n > 0) {
         k_upload_place<<<(unsigned)blk, 256, 0, stream>>>(rs, cell, gender, state, sid, sbirth, sage, slastb, n,
@@ -1598,7 +2158,7 @@ extern "C" int qhg_launch_gather_genomes(const int32_t *gslot, const uint64_t *g
 template <int PROG, bool BATCH, bool BIG>
 static void set_actions_attr() {
     cudaFuncSetAttribute(qhg::k_actions<PROG, BATCH, BIG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sizeof(qhg::ActionsSmemT<qhg::Tile<BIG>::kMax, qhg::Tile<BIG>::kThreads>));
+                         (int)sizeof(qhg::ActionsSmemT<qhg::Tile<BIG>::kMax, qhg::Tile<BIG>::kThreads, BATCH>));
 }
 template <bool BATCH, bool BIG>
 static void set_scatter_attr() {
@@ -1606,16 +2166,20 @@ static void set_scatter_attr() {
                          (int)sizeof(qhg::ScatterSmemT<qhg::Tile<BIG>::kMax, qhg::Tile<BIG>::kThreads>));
 }
 
+template <int PROG, bool BATCH>
+static void set_cell_attr() {
+    cudaFuncSetAttribute(qhg::k_actions_cell<PROG, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(sizeof(qhg::CellWarpSmem) * qhg::kCellWarps));
+}
+
 static void set_tile_attributes() {
     static bool done[64] = {false};
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64 || done[dev]) return;
-    set_actions_attr<0, false, false>(); set_actions_attr<1, false, false>();
-    set_actions_attr<2, false, false>(); set_actions_attr<3, false, false>();
-    set_actions_attr<0, true, false>(); set_actions_attr<1, true, false>();
+    set_cell_attr<0, false>(); set_cell_attr<1, false>(); set_cell_attr<2, false>(); set_cell_attr<3, false>();
+    set_cell_attr<0, true>(); set_cell_attr<1, true>();
     set_actions_attr<0, false, true>(); set_actions_attr<0, true, true>();
-    set_scatter_attr<false, false>(); set_scatter_attr<true, false>();
     set_scatter_attr<false, true>(); set_scatter_attr<true, true>();
     done[dev] = true;
 }
@@ -1630,9 +2194,9 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
     BatchBuffers BB;
     if (batch) BB = *BBp;
     else memset(&BB, 0, sizeof(BB));
-    constexpr size_t kSmA = sizeof(ActionsSmemT<Tile<false>::kMax, Tile<false>::kThreads>);
-    constexpr size_t kSmAB = sizeof(ActionsSmemT<Tile<true>::kMax, Tile<true>::kThreads>);
-    constexpr size_t kSmS = sizeof(ScatterSmemT<Tile<false>::kMax, Tile<false>::kThreads>);
+    constexpr size_t kSmC = sizeof(CellWarpSmem) * kCellWarps;
+    const size_t kSmAB = batch ? sizeof(ActionsSmemT<Tile<true>::kMax, Tile<true>::kThreads, true>)
+                               : sizeof(ActionsSmemT<Tile<true>::kMax, Tile<true>::kThreads, false>);
     constexpr size_t kSmSB = sizeof(ScatterSmemT<Tile<true>::kMax, Tile<true>::kThreads>);
     if (ev) cudaEventRecord(ev[0], stream);
     // both forms are launched; the one that does not match the step's cell
@@ -1640,27 +2204,32 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
 #define QHG_LAUNCH_ACTIONS(PR, BT, BG, GRID, SM)                                                          \
     k_actions<PR, BT, BG><<<GRID, Tile<BG>::kThreads, SM, stream>>>(                                      \
         *P, BB, rs, B->nonempty, B->ne_start, B->tile_first, B->id, B->birth, B->age, B->lastb, B->meta, \
-        B->nbr, B->nnbr, B->vthr, B->wthr, B->cmove, B->outc, B->father, B->brank, B->clsc)
+        B->vthr, B->wthr, B->necm, B->outc, B->father, B->brank, B->clsc)
+#define QHG_LAUNCH_CELL(PR, BT)                                                                            \
+    k_actions_cell<PR, BT><<<L.actions_grid, kCellThreads, kSmC, stream>>>(                                \
+        *P, BB, rs, B->nonempty, B->ne_start, B->id, B->birth, B->age, B->lastb, B->meta, B->vthr, B->wthr, \
+        B->necm, B->outc, B->father, B->brank, B->clsc)
     if (batch) {
         switch (P->program) {
-        case 1: QHG_LAUNCH_ACTIONS(1, true, false, L.actions_grid, kSmA); break;
-        default: QHG_LAUNCH_ACTIONS(0, true, false, L.actions_grid, kSmA); break;
+        case 1: QHG_LAUNCH_CELL(1, true); break;
+        default: QHG_LAUNCH_CELL(0, true); break;
         }
         QHG_LAUNCH_ACTIONS(0, true, true, L.big_grid, kSmAB);
     } else {
         switch (P->program) {
-        case 1: QHG_LAUNCH_ACTIONS(1, false, false, L.actions_grid, kSmA); break;
-        case 2: QHG_LAUNCH_ACTIONS(2, false, false, L.actions_grid, kSmA); break;
-        case 3: QHG_LAUNCH_ACTIONS(3, false, false, L.actions_grid, kSmA); break;
-        default: QHG_LAUNCH_ACTIONS(0, false, false, L.actions_grid, kSmA); break;
+        case 1: QHG_LAUNCH_CELL(1, false); break;
+        case 2: QHG_LAUNCH_CELL(2, false); break;
+        case 3: QHG_LAUNCH_CELL(3, false); break;
+        default: QHG_LAUNCH_CELL(0, false); break;
         }
         QHG_LAUNCH_ACTIONS(0, false, true, L.big_grid, kSmAB);
     }
+#undef QHG_LAUNCH_CELL
 #undef QHG_LAUNCH_ACTIONS
     if (ev) cudaEventRecord(ev[1], stream);
 #define QHG_LAUNCH_SCAN(BT)                                                                                 \
     k_cell_scan<BT><<<ntiles, kScanThreads, 0, stream>>>(                                                   \
-        *P, BB, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr2, B->sbase, B->bbase, B->bidbase,       \
+        *P, BB, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr2, B->cmove, B->necm2, B->sbase, B->bbase, B->bidbase,       \
         B->obase, B->nonempty2, B->ne_start2, B->tile_first2, B->tile_flag, B->tile_agg, B->tile_incl)
     if (batch) QHG_LAUNCH_SCAN(true);
     else QHG_LAUNCH_SCAN(false);
@@ -1672,13 +2241,19 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
         B->father, B->brank, B->nnbr, B->sbase, B->bbase, B->bidbase, B->obase, B->clsc, B->id2, B->birth2, \
         B->age2, B->lastb2, B->meta2, B->blog, B->blog_cap, B->gslot, B->gslot2, B->freelist,              \
         B->freelist2, B->brec)
+#define QHG_LAUNCH_SCATTER_CELL(BT)                                                                        \
+    k_scatter_cell<BT><<<L.scatter_grid, kCellThreads, 0, stream>>>(                                       \
+        *P, BB, rs, B->nonempty, B->ne_start, B->id, B->birth, B->age, B->lastb, B->outc, B->father,       \
+        B->brank, B->sbase, B->bbase, B->bidbase, B->obase, B->clsc, B->id2, B->birth2, B->age2, B->lastb2, \
+        B->meta2, B->blog, B->blog_cap, B->gslot, B->gslot2, B->freelist, B->freelist2, B->brec)
     if (batch) {
-        QHG_LAUNCH_SCATTER(true, false, L.scatter_grid, kSmS);
+        QHG_LAUNCH_SCATTER_CELL(true);
         QHG_LAUNCH_SCATTER(true, true, L.big_grid, kSmSB);
     } else {
-        QHG_LAUNCH_SCATTER(false, false, L.scatter_grid, kSmS);
+        QHG_LAUNCH_SCATTER_CELL(false);
         QHG_LAUNCH_SCATTER(false, true, L.big_grid, kSmSB);
     }
+#undef QHG_LAUNCH_SCATTER_CELL
 #undef QHG_LAUNCH_SCATTER
     if (ev) cudaEventRecord(ev[3], stream);
     if (batch) {
@@ -1708,12 +2283,9 @@ extern "C" int qhg_launch_step_timed(const qhg::StepConst *P, qhg::RunState *rs,
 extern "C" void qhg_tile_ctas_per_sm(int *actions, int *scatter) {
     int a = 0, b = 0;
     set_tile_attributes();
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &a, qhg::k_actions<0, false, false>, qhg::kTileThreads,
-        sizeof(qhg::ActionsSmemT<qhg::Tile<false>::kMax, qhg::Tile<false>::kThreads>));
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &b, qhg::k_scatter<false, false>, qhg::kTileThreads,
-        sizeof(qhg::ScatterSmemT<qhg::Tile<false>::kMax, qhg::Tile<false>::kThreads>));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, qhg::k_actions_cell<0, false>, qhg::kCellThreads,
+                                                  sizeof(qhg::CellWarpSmem) * qhg::kCellWarps);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, qhg::k_scatter_cell<false>, qhg::kCellThreads, 0);
     *actions = a > 0 ? a : 1;
     *scatter = b > 0 ? b : 1;
 }

@@ -110,3 +110,23 @@ def test_big_cells(gpu_lib, K, N):
     o, g, st = run_both(grid, agents, acts, 30, 9, chunks=(1, 29))
     assert_same(o, g, st, 30)
     assert o.counts().max() > 0
+
+
+def test_ids_past_32_bits(gpu_lib):
+    """Agent IDs around 2^32 (and newborn IDs above it): pairing ranks IDs by
+    their full 64 bits, and draws are keyed by the full ID."""
+    grid, agents, acts = case_config2(n=12, N=30000, seed=17)
+    agents.id = agents.id + np.int64(2**32 - 15000)
+    o, g, st = run_both(grid, agents, acts, 12, 3)
+    assert_same(o, g, st, 12)
+    assert st[:, 1].sum() > 0
+
+
+def test_dense_cells_multi_warp_lists(gpu_lib):
+    """Cells of a few hundred agents: FERTILE lists longer than a warp, more
+    than 32 picks per cell."""
+    grid = uniform_grid(3, 400.0)
+    agents = make_agents(grid, 25000, seed=8, age_max=50.0)
+    o, g, st = run_both(grid, agents, config1_actions(K=400.0), 20, 21)
+    assert_same(o, g, st, 20)
+    assert 64 < o.counts().max() <= 512
