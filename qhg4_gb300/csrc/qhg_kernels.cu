@@ -42,7 +42,9 @@ __device__ __forceinline__ uint32_t pick4(const Draw4 &d, uint32_t k) {
 }
 
 // draws of one agent in one step: the per-agent action stream, caching the
-// last Philox block
+// last Philox block.  The first block is drawn at once, where the warp is
+// converged (the actions' draws are taken under divergent conditions, and
+// most of them fall in that block).
 struct AgentDraws {
     uint64_t seed;
     int64_t id;
@@ -50,7 +52,8 @@ struct AgentDraws {
     uint32_t blk;
     Draw4 d;
     __device__ __forceinline__ void init(uint64_t s, uint32_t st, int64_t i) {
-        seed = s; step = st; id = i; blk = 0xffffffffu;
+        seed = s; step = st; id = i; blk = kStreamActions;
+        d = draw_block(s, st, i, kStreamActions);
     }
     __device__ __forceinline__ uint32_t get(uint32_t k) {
         const uint32_t b = kStreamActions + (k >> 2);
@@ -189,6 +192,15 @@ struct ActionsSmemT {
 // agents whose age lies inside the death window) is made in a dense pass
 // after the other actions, so that warps do not run Philox for a few lanes
 __host__ __device__ constexpr bool prog_defers_oad(int p) { return p == 2; }
+// position of OldAgeDeath in a specialised program, -1 if it has none
+__host__ __device__ constexpr int prog_oad_index(int p) {
+    return p == 0 ? -1 : (prog_act(p, 0) == kOldAgeDeath ? 0 : prog_act(p, 1) == kOldAgeDeath ? 1
+                          : prog_act(p, 2) == kOldAgeDeath ? 2 : prog_act(p, 3) == kOldAgeDeath ? 3
+                          : prog_act(p, 4) == kOldAgeDeath ? 4 : prog_act(p, 5) == kOldAgeDeath ? 5 : -1);
+}
+// how agent_outcome treats an agent inside the OldAgeDeath window: draw and
+// decide, leave it to the caller (queued), or apply a decision made before
+constexpr int kOadDraw = 0, kOadQueue = 1, kOadGiven = 2;
 
 // Rank of an agent's outcome in its cell's class (slot 0 stay, 1..6 movers
 // per neighbour slot) from a warp-aggregated shared counter; every lane of
@@ -214,14 +226,15 @@ struct CellView {
 // actions/Fertility.cpp:49-73, LinearBirth/LinearDeath actions/LinearBirth.cpp:122-166,
 // actions/LinearDeath.cpp:131-150, OldAgeDeath actions/OldAgeDeath.cpp:48-67,
 // RandomMove actions/RandomMove.cpp:65-100, WeightedMove actions/WeightedMove.cpp:45-106).
-// Returns the outcome byte.  With DEFER_OAD an agent inside the OldAgeDeath
-// window is left alive with `queued` set: its draw is made by the caller.
+// Returns the outcome byte.  An agent inside the OldAgeDeath window draws
+// (OAD == kOadDraw), is left alive with `queued` set for the caller to draw
+// (kOadQueue), or dies as `oad_die` says (kOadGiven).
 // `fa` is the agent's age after the actions (the input age on entry).
-template <int PROG, bool BATCH, bool DEFER_OAD>
+template <int PROG, bool BATCH, int OAD>
 __device__ __forceinline__ uint8_t agent_outcome(const StepConst &P, const BatchRun *R, int32_t step, float fT,
                                                  int64_t id, uint8_t m8, float fb, float fa_in, float fl,
                                                  bool mated, const CellView &cv, const uint64_t *__restrict__ wthr,
-                                                 float &fa, bool &queued, uint32_t &cnt_deaths,
+                                                 bool oad_die, float &fa, bool &queued, uint32_t &cnt_deaths,
                                                  uint32_t &cnt_moves) {
     const uint64_t seed = BATCH ? R->seed : P.seed;
     const int32_t stepR = BATCH ? step - R->step0 : step;
@@ -270,8 +283,10 @@ __device__ __forceinline__ uint8_t agent_outcome(const StepConst &P, const Batch
                 die = false;
             } else if (fa > A.age_hi) {
                 die = true;
-            } else if (DEFER_OAD) {
+            } else if (OAD == kOadQueue) {
                 queued = true;
+            } else if (OAD == kOadGiven) {
+                die = oad_die;
             } else {
                 const uint32_t u = dr.get(A.window);
                 const double t = __dmul_rn(__dmul_rn(A.oad_w, (double)u), 2.3283064365386962890625e-10);
@@ -608,8 +623,9 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                     cv.wf = S.wf[lc];
                     cv.c = (uint32_t)c;
                     const int mate = S.mate[i];
-                    oc = agent_outcome<PROG, BATCH, kDeferOad>(P, R, step, fT, pid[j], m8, pb[j], pa[j], pl[j],
-                                                               mate >= 0, cv, wthr, fa, queued, cnt_deaths, cnt_moves);
+                    oc = agent_outcome<PROG, BATCH, kDeferOad ? kOadQueue : kOadDraw>(
+                        P, R, step, fT, pid[j], m8, pb[j], pa[j], pl[j], mate >= 0, cv, wthr, false, fa, queued,
+                        cnt_deaths, cnt_moves);
                     if (oc & kOutBirth) {
                         father[row] = (int32_t)(a0 + (uint32_t)mate);
                         cnt_births++;
@@ -1381,21 +1397,29 @@ struct CellWarpSmem {
     int16_t mate[kMaxCell];      // mate's row of each row, -1 none
     uint16_t pick[kMaxCell / 2]; // pick value of each member of the smaller side (ID order)
     uint8_t oc[kMaxCell];        // outcome byte of each row
+    uint32_t odie[kMaxCell / 32];  // OldAgeDeath decided in advance: bit per row, set = dies
+    uint32_t oinw[kMaxCell / 32];  // rows inside the OldAgeDeath age window, bit per row
     uint32_t cnt[8];             // class counts: [0] stay, [1..6] movers per neighbour slot
+    uint64_t wt[6];              // WeightedMove thresholds of the cell
 };
 
-// ID ranks of the FERTILE list entries [b, b + m) among themselves: entry k
-// goes to sidx[b + rank].  IDs are compared by their low words while all
+// ID ranks of the FERTILE list entries among their own sex: females are the
+// entries [0, nF), males [n - nM, n); entry k goes to sidx[region + rank].
+// One pass over both lists.  IDs are compared by their low words while all
 // high words are zero (wide == false), else in full (read from the table).
-__device__ __forceinline__ void rank_list(CellWarpSmem &W, int b, int m, bool wide, const int64_t *__restrict__ id,
-                                          uint32_t s) {
+__device__ __forceinline__ void rank_lists(CellWarpSmem &W, int n, int nF, int nM, bool wide,
+                                           const int64_t *__restrict__ id, uint32_t s) {
     const int lane = threadIdx.x & 31;
-    for (int k0 = 0; k0 < m; k0 += 32) {
-        const int k = k0 + lane;
-        if (k < m) {
+    for (int t0 = 0; t0 < nF + nM; t0 += 32) {
+        const int t = t0 + lane;
+        if (t < nF + nM) {
+            const bool male = t >= nF;
+            const int b = male ? n - nM : 0;
+            const int m = male ? nM : nF;
+            const int k = b + (male ? t - nF : t);
             int r = 0;
             if (!wide) {
-                const uint32_t x = W.fk[b + k];
+                const uint32_t x = W.fk[k];
                 int j = 0;
                 for (; j + 4 <= m; j += 4) {
                     r += (W.fk[b + j] < x ? 1 : 0) + (W.fk[b + j + 1] < x ? 1 : 0) +
@@ -1403,10 +1427,10 @@ __device__ __forceinline__ void rank_list(CellWarpSmem &W, int b, int m, bool wi
                 }
                 for (; j < m; j++) r += (W.fk[b + j] < x) ? 1 : 0;
             } else {
-                const int64_t x = id[s + W.frow[b + k]];
+                const int64_t x = id[s + W.frow[k]];
                 for (int j = 0; j < m; j++) r += (id[s + W.frow[b + j]] < x) ? 1 : 0;
             }
-            W.sidx[b + r] = (uint16_t)(b + k);
+            W.sidx[b + r] = (uint16_t)k;
         }
     }
 }
@@ -1427,6 +1451,10 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
     CellWarpSmem &W = reinterpret_cast<CellWarpSmem *>(qhg_smem)[threadIdx.x >> 5];
     if (rs->error != 0u) return;   // an earlier kernel failed: keep the state
     if (rs->big != 0u) return;     // the big-cell form runs this step
+    // OldAgeDeath of a specialised program is decided before the other
+    // actions, in the same dense draw pass as the pairing picks
+    constexpr int kOad = prog_oad_index(PROG);
+    constexpr bool kEarlyOad = kOad >= 0;
     const int lane = threadIdx.x & 31;
     const uint32_t lt = lanemask_lt();
     const int32_t step = rs->step;
@@ -1457,26 +1485,36 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
         uint32_t cm = 0u;
         if (P.n_verhulst > 0) v = vthr[r];
         if (P.has_move) cm = necm[r];
+        const uint64_t wl = (P.has_wmove && lane < 6) ? wthr[(size_t)c * 6 + lane] : 0ull;
         if (n > kMaxCell) {   // cannot happen: such steps run the big-cell form
             if (lane == 0) set_error(rs, kErrCellTooLarge, c);
             continue;
         }
         const BatchRun *R = BATCH ? BB.runs + BB.crun[c] : nullptr;
         const bool keep = !BATCH || R->active;   // a run that leaves the batch drops its agents
+        const uint64_t sd = BATCH ? R->seed : P.seed;
+        const int32_t stR = BATCH ? step - R->step0 : step;
+        const float fTR = BATCH ? (float)stR : fT;
         // ---- RandomPair::findMates (actions/RandomPair.cpp:146-270): FERTILE
         // lists, ranked by ID; the members of the smaller side pick, in ID
-        // order, each pick drawn from the pairing stream of the picking member
-        int nF = 0, nM = 0;
+        // order, each pick drawn from the pairing stream of the picking member.
+        // With an early OldAgeDeath, the agents inside its age window are
+        // marked.
+        int nF = 0, nM = 0, nq = 0;
         bool wide = false;
-        if (P.has_pair && keep) {
+        if (keep && (P.has_pair || kEarlyOad)) {
             for (int b = 0; b < n; b += 32) {
                 const int row = b + lane;
                 const bool valid = row < n;
-                const uint8_t m8 = valid ? meta[s + row] : (uint8_t)0;
-                const bool fert = (m8 & kMetaFertile) != 0;
-                const bool male = (m8 & kMetaGender) != 0;
+                bool fert = false, male = false;
                 int64_t x = 0;
-                if (fert) x = id[s + row];
+                if (P.has_pair) {
+                    const uint8_t m8 = valid ? meta[s + row] : (uint8_t)0;
+                    fert = (m8 & kMetaFertile) != 0;
+                    male = (m8 & kMetaGender) != 0;
+                    if (fert) x = id[s + row];
+                    if (valid) W.mate[row] = -1;
+                }
                 const uint32_t fm = __ballot_sync(FULL_MASK, fert && !male);
                 const uint32_t mm = __ballot_sync(FULL_MASK, fert && male);
                 if (fert) {
@@ -1484,38 +1522,82 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                     W.fk[pos] = (uint32_t)(uint64_t)x;
                     W.frow[pos] = (uint16_t)row;
                 }
-                if (valid) W.mate[row] = -1;
                 wide |= __any_sync(FULL_MASK, ((uint64_t)x >> 32) != 0ull);
                 nF += __popc(fm);
                 nM += __popc(mm);
+                if (kEarlyOad) {
+                    const ActionConst &A = BATCH ? R->act[kOad] : P.act[kOad];
+                    bool inw = false;
+                    if (valid) {
+                        const float fa = __fsub_rn(fTR, birth[s + row]);
+                        inw = !(fa <= A.age_lo) && !(fa > A.age_hi);
+                    }
+                    const uint32_t qm = __ballot_sync(FULL_MASK, inw);
+                    nq += __popc(qm);
+                    if (lane == 0) {
+                        W.oinw[b >> 5] = qm;
+                        W.odie[b >> 5] = 0u;
+                    }
+                }
             }
+            __syncwarp();
         }
+        if (lane < 6) W.wt[lane] = wl;   // read in the action pass below, after warp syncs
         const bool pairs = nF > 0 && nM > 0;
         if (pairs) {
+            rank_lists(W, n, nF, nM, wide, id, s);
             __syncwarp();
-            rank_list(W, 0, nF, wide, id, s);
-            rank_list(W, n - nM, nM, wide, id, s);
-            __syncwarp();
-            const bool femSmall = nF <= nM;
-            const int m = femSmall ? nF : nM;
-            const uint32_t nL = (uint32_t)(femSmall ? nM : nF);
-            const int sb = femSmall ? 0 : n - nM;   // smaller side in sidx
-            const int lb = femSmall ? n - nM : 0;   // larger side
-            uint64_t sd = P.seed;
-            int32_t st = step;
-            if (BATCH) {
-                sd = R->seed;
-                st = step - R->step0;
+        }
+        const bool femSmall = nF <= nM;
+        const int m = pairs ? (femSmall ? nF : nM) : 0;
+        const uint32_t nL = (uint32_t)(femSmall ? nM : nF);
+        const int sb = femSmall ? 0 : n - nM;   // smaller side in sidx
+        const int lb = femSmall ? n - nM : 0;   // larger side
+        // ---- one dense pass of draws: pick j (j < m) takes the pick[j]-th
+        // still unpaired member of the larger side, pick[j] = (int)wrandr(0,
+        // nL - j); then the OldAgeDeath draws of the agents in its window:
+        // age > M + wrandr(1 - U*M, 1 + U*M) (actions/OldAgeDeath.cpp:57-60)
+        for (int t0 = 0; t0 < m + nq; t0 += 32) {
+            const int t = t0 + lane;
+            if (t < m + nq) {
+                // one Philox block per lane, from the picking member's pairing
+                // stream or the old agent's action stream
+                int64_t x;
+                uint32_t blk, wd = 0u;
+                int row = 0;
+                if (t < m) {
+                    const int pos = W.sidx[sb + t];
+                    x = wide ? id[s + W.frow[pos]] : (int64_t)W.fk[pos];
+                    blk = kStreamPair;
+                } else {
+                    // the (t - m)-th marked row: find its chunk, then its bit
+                    int k = t - m, ch = 0;
+                    uint32_t cmsk = W.oinw[0];
+                    while (k >= __popc(cmsk)) {
+                        k -= __popc(cmsk);
+                        cmsk = W.oinw[++ch];
+                    }
+                    row = (ch << 5) + (int)__fns(cmsk, 0, k + 1);
+                    x = id[s + row];
+                    const uint32_t w = (BATCH ? R->act[kOad > 0 ? kOad : 0] : P.act[kOad > 0 ? kOad : 0]).window;
+                    blk = kStreamActions + (w >> 2);
+                    wd = w & 3u;
+                }
+                const Draw4 d4 = draw_block(sd, (uint32_t)stR, x, blk);
+                if (t < m) {
+                    W.pick[t] = (uint16_t)(((uint64_t)(nL - (uint32_t)t) * (uint64_t)d4.v[0]) >> 32);
+                } else if (kEarlyOad) {
+                    const ActionConst &A = BATCH ? R->act[kOad > 0 ? kOad : 0] : P.act[kOad > 0 ? kOad : 0];
+                    const float fa = __fsub_rn(fTR, birth[s + row]);
+                    const uint32_t u = pick4(d4, wd);
+                    const double th = __dmul_rn(__dmul_rn(A.oad_w, (double)u), 2.3283064365386962890625e-10);
+                    const double thr = __dadd_rn(A.oad_M, __dadd_rn(A.oad_a, th));
+                    if ((double)fa > thr) atomicOr(&W.odie[row >> 5], 1u << (row & 31));
+                }
             }
-            // pick j takes the pick[j]-th still unpaired member of the larger
-            // side, pick[j] = (int)wrandr(0, nL - j)
-            for (int j = lane; j < m; j += 32) {
-                const int pos = W.sidx[sb + j];
-                const int64_t x = wide ? id[s + W.frow[pos]] : (int64_t)W.fk[pos];
-                const uint32_t u = draw_block(sd, (uint32_t)st, x, kStreamPair).v[0];
-                W.pick[j] = (uint16_t)(((uint64_t)(nL - (uint32_t)j) * (uint64_t)u) >> 32);
-            }
-            __syncwarp();
+        }
+        __syncwarp();
+        if (pairs) {
             // the member taken by pick j, decoded on its own: start from pick[j]
             // and for i = j-1 down to 0 step over the member pick i took when it
             // lies at or below (the lanes walk i down together)
@@ -1549,7 +1631,7 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
         cv.nn = cm & 7u;
         cv.vm = (cm >> 8) & 63u;
         cv.wf = (cm >> 16) & 1u;
-        cv.c = c;
+        cv.c = 0u;   // the thresholds of this cell are W.wt
         if (lane < 8) W.cnt[lane] = 0u;
         uint32_t births = 0, dead = 0, moved = 0;
         __syncwarp();
@@ -1564,11 +1646,12 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                     oc = kOutDropped;
                 } else {
                     const int mate = pairs ? W.mate[row] : -1;
+                    const bool odie = kEarlyOad && ((W.odie[b >> 5] >> lane) & 1u);
                     float fa;
                     bool queued = false;
-                    oc = agent_outcome<PROG, BATCH, false>(P, R, step, fT, id[g], m8, birth[g],
-                                                           P.reads_age ? age[g] : 0.0f, lastb[g], mate >= 0, cv,
-                                                           wthr, fa, queued, cnt_deaths, cnt_moves);
+                    oc = agent_outcome<PROG, BATCH, kEarlyOad ? kOadGiven : kOadDraw>(
+                        P, R, step, fT, id[g], m8, birth[g], P.reads_age ? age[g] : 0.0f, lastb[g], mate >= 0, cv,
+                        W.wt, odie, fa, queued, cnt_deaths, cnt_moves);
                     if (oc & kOutBirth) {
                         father[g] = (int32_t)(s + (uint32_t)mate);
                         cnt_births++;
@@ -1675,23 +1758,26 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
             freelist2[q] = freelist[births + q];
         }
     }
+    // the bounds and index of the warp's next cell are loaded one cell ahead
     uint32_t r = blockIdx.x * kCellWarps + (threadIdx.x >> 5);
-    uint32_t nb0 = 0, nb1 = 0;
+    uint32_t nb0 = 0, nb1 = 0, nc0 = 0;
     if (r < nne) {
         nb0 = ne_start[r];
         nb1 = ne_start[r + 1];
+        nc0 = nonempty[r];
     }
     for (; r < nne; r += G) {
         const uint32_t s = nb0;
         const int n = (int)(nb1 - nb0);
+        const uint32_t c = nc0;
         const uint32_t rn = r + G;
         if (rn < nne) {
             nb0 = ne_start[rn];
             nb1 = ne_start[rn + 1];
+            nc0 = nonempty[rn];
         }
         // the cell's bases in the next table: stayers, newborns (and their
         // birth numbers), movers per neighbour slot (lane k holds slot k)
-        const uint32_t c = nonempty[r];
         const uint32_t sb = sbase[c];
         const uint32_t bb = bbase[c];
         uint32_t bid = bidbase[c];
