@@ -1503,40 +1503,61 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
         int nF = 0, nM = 0, nq = 0;
         bool wide = false;
         if (keep && (P.has_pair || kEarlyOad)) {
-            for (int b = 0; b < n; b += 32) {
-                const int row = b + lane;
-                const bool valid = row < n;
-                bool fert = false, male = false;
-                int64_t x = 0;
-                if (P.has_pair) {
-                    const uint8_t m8 = valid ? meta[s + row] : (uint8_t)0;
-                    fert = (m8 & kMetaFertile) != 0;
-                    male = (m8 & kMetaGender) != 0;
-                    if (fert) x = id[s + row];
-                    if (valid) W.mate[row] = -1;
-                }
-                const uint32_t fm = __ballot_sync(FULL_MASK, fert && !male);
-                const uint32_t mm = __ballot_sync(FULL_MASK, fert && male);
-                if (fert) {
-                    const int pos = male ? n - 1 - (nM + __popc(mm & lt)) : nF + __popc(fm & lt);
-                    W.fk[pos] = (uint32_t)(uint64_t)x;
-                    W.frow[pos] = (uint16_t)row;
-                }
-                wide |= __any_sync(FULL_MASK, ((uint64_t)x >> 32) != 0ull);
-                nF += __popc(fm);
-                nM += __popc(mm);
-                if (kEarlyOad) {
-                    const ActionConst &A = BATCH ? R->act[kOad] : P.act[kOad];
-                    bool inw = false;
-                    if (valid) {
-                        const float fa = __fsub_rn(fTR, birth[s + row]);
-                        inw = !(fa <= A.age_lo) && !(fa > A.age_hi);
+            // groups of kGroupA chunks of 32 rows: a group's loads are issued
+            // together (one chunk: larger groups cost registers that the later
+            // passes need)
+            constexpr int kGroupA = 1;
+            for (int b0 = 0; b0 < n; b0 += 32 * kGroupA) {
+                uint8_t m8s[kGroupA];
+                int64_t xs[kGroupA];
+                float fbs[kGroupA];
+#pragma unroll
+                for (int q = 0; q < kGroupA; q++) {
+                    const int row = b0 + q * 32 + lane;
+                    m8s[q] = 0;
+                    xs[q] = 0;
+                    fbs[q] = 0.0f;
+                    if (row < n) {
+                        if (P.has_pair) {
+                            m8s[q] = meta[s + row];
+                            xs[q] = id[s + row];
+                        }
+                        if (kEarlyOad) fbs[q] = birth[s + row];
                     }
-                    const uint32_t qm = __ballot_sync(FULL_MASK, inw);
-                    nq += __popc(qm);
-                    if (lane == 0) {
-                        W.oinw[b >> 5] = qm;
-                        W.odie[b >> 5] = 0u;
+                }
+#pragma unroll
+                for (int q = 0; q < kGroupA; q++) {
+                    const int b = b0 + q * 32;
+                    if (b >= n) break;   // the same for the whole warp
+                    const int row = b + lane;
+                    const bool valid = row < n;
+                    const bool fert = (m8s[q] & kMetaFertile) != 0;
+                    const bool male = (m8s[q] & kMetaGender) != 0;
+                    const int64_t x = fert ? xs[q] : 0;
+                    if (P.has_pair && valid) W.mate[row] = -1;
+                    const uint32_t fm = __ballot_sync(FULL_MASK, fert && !male);
+                    const uint32_t mm = __ballot_sync(FULL_MASK, fert && male);
+                    if (fert) {
+                        const int pos = male ? n - 1 - (nM + __popc(mm & lt)) : nF + __popc(fm & lt);
+                        W.fk[pos] = (uint32_t)(uint64_t)x;
+                        W.frow[pos] = (uint16_t)row;
+                    }
+                    wide |= __any_sync(FULL_MASK, ((uint64_t)x >> 32) != 0ull);
+                    nF += __popc(fm);
+                    nM += __popc(mm);
+                    if (kEarlyOad) {
+                        const ActionConst &A = BATCH ? R->act[kOad] : P.act[kOad];
+                        bool inw = false;
+                        if (valid) {
+                            const float fa = __fsub_rn(fTR, fbs[q]);
+                            inw = !(fa <= A.age_lo) && !(fa > A.age_hi);
+                        }
+                        const uint32_t qm = __ballot_sync(FULL_MASK, inw);
+                        nq += __popc(qm);
+                        if (lane == 0) {
+                            W.oinw[b >> 5] = qm;
+                            W.odie[b >> 5] = 0u;
+                        }
                     }
                 }
             }
@@ -1635,45 +1656,69 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
         if (lane < 8) W.cnt[lane] = 0u;
         uint32_t births = 0, dead = 0, moved = 0;
         __syncwarp();
-        for (int b = 0; b < n; b += 32) {
-            const int row = b + lane;
-            const bool valid = row < n;
-            uint8_t oc = 0;
-            if (valid) {
-                const uint32_t g = s + (uint32_t)row;
-                const uint8_t m8 = meta[g];
-                if (!keep) {
-                    oc = kOutDropped;
-                } else {
-                    const int mate = pairs ? W.mate[row] : -1;
-                    const bool odie = kEarlyOad && ((W.odie[b >> 5] >> lane) & 1u);
-                    float fa;
-                    bool queued = false;
-                    oc = agent_outcome<PROG, BATCH, kEarlyOad ? kOadGiven : kOadDraw>(
-                        P, R, step, fT, id[g], m8, birth[g], P.reads_age ? age[g] : 0.0f, lastb[g], mate >= 0, cv,
-                        W.wt, odie, fa, queued, cnt_deaths, cnt_moves);
-                    if (oc & kOutBirth) {
-                        father[g] = (int32_t)(s + (uint32_t)mate);
-                        cnt_births++;
-                    }
+        // groups of kGroupD chunks of 32 rows (one chunk: see kGroupA)
+        constexpr int kGroupD = 1;
+        for (int b0 = 0; b0 < n; b0 += 32 * kGroupD) {
+            uint8_t m8s[kGroupD];
+            int64_t xs[kGroupD];
+            float fbs[kGroupD], fas[kGroupD], fls[kGroupD];
+#pragma unroll
+            for (int q = 0; q < kGroupD; q++) {
+                const int row = b0 + q * 32 + lane;
+                m8s[q] = 0;
+                xs[q] = 0;
+                fbs[q] = fas[q] = fls[q] = 0.0f;
+                if (row < n) {
+                    const uint32_t g = s + (uint32_t)row;
+                    m8s[q] = meta[g];
+                    xs[q] = id[g];
+                    fbs[q] = birth[g];
+                    if (P.reads_age) fas[q] = age[g];
+                    fls[q] = lastb[g];
                 }
-                W.oc[row] = oc;
             }
-            const int cls = oc & 7;
-            const bool counted = valid && cls > 0;
-            const uint32_t slot = counted ? (uint32_t)(cls - 1) : 0u;
-            const uint32_t peers = __match_any_sync(FULL_MASK, counted ? slot : 0xffu);
-            const uint32_t base = counted ? W.cnt[slot] : 0u;
-            __syncwarp();
-            if (counted && (peers & lt) == 0u) W.cnt[slot] = base + (uint32_t)__popc(peers);
-            // outcome byte | rank in the cell's class << 17
-            if (valid) outc[s + (uint32_t)row] = (uint32_t)oc | ((base + (uint32_t)__popc(peers & lt)) << 17);
-            births += __popc(__ballot_sync(FULL_MASK, valid && (oc & kOutBirth)));
-            if (BATCH) {
-                dead += __popc(__ballot_sync(FULL_MASK, valid && cls == 0 && !(oc & kOutDropped)));
-                moved += __popc(__ballot_sync(FULL_MASK, valid && (oc & kOutMoved)));
+#pragma unroll
+            for (int q = 0; q < kGroupD; q++) {
+                const int b = b0 + q * 32;
+                if (b >= n) break;   // the same for the whole warp
+                const int row = b + lane;
+                const bool valid = row < n;
+                uint8_t oc = 0;
+                if (valid) {
+                    const uint32_t g = s + (uint32_t)row;
+                    if (!keep) {
+                        oc = kOutDropped;
+                    } else {
+                        const int mate = pairs ? W.mate[row] : -1;
+                        const bool odie = kEarlyOad && ((W.odie[b >> 5] >> lane) & 1u);
+                        float fa;
+                        bool queued = false;
+                        oc = agent_outcome<PROG, BATCH, kEarlyOad ? kOadGiven : kOadDraw>(
+                            P, R, step, fT, xs[q], m8s[q], fbs[q], fas[q], fls[q], mate >= 0, cv, W.wt, odie, fa,
+                            queued, cnt_deaths, cnt_moves);
+                        if (oc & kOutBirth) {
+                            father[g] = (int32_t)(s + (uint32_t)mate);
+                            cnt_births++;
+                        }
+                    }
+                    W.oc[row] = oc;
+                }
+                const int cls = oc & 7;
+                const bool counted = valid && cls > 0;
+                const uint32_t slot = counted ? (uint32_t)(cls - 1) : 0u;
+                const uint32_t peers = __match_any_sync(FULL_MASK, counted ? slot : 0xffu);
+                const uint32_t base = counted ? W.cnt[slot] : 0u;
+                __syncwarp();
+                if (counted && (peers & lt) == 0u) W.cnt[slot] = base + (uint32_t)__popc(peers);
+                // outcome byte | rank in the cell's class << 17
+                if (valid) outc[s + (uint32_t)row] = (uint32_t)oc | ((base + (uint32_t)__popc(peers & lt)) << 17);
+                births += __popc(__ballot_sync(FULL_MASK, valid && (oc & kOutBirth)));
+                if (BATCH) {
+                    dead += __popc(__ballot_sync(FULL_MASK, valid && cls == 0 && !(oc & kOutDropped)));
+                    moved += __popc(__ballot_sync(FULL_MASK, valid && (oc & kOutMoved)));
+                }
+                __syncwarp();
             }
-            __syncwarp();
         }
         // ---- mothers' birth ranks: births are numbered in (cell, mother ID)
         // order; mothers are FERTILE females, walked in ID order
@@ -1798,85 +1843,105 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
         }
         // the class counts are consumed: clear them for the next step
         if (lane < 2) reinterpret_cast<uint4 *>(clsc + (size_t)c * kCls)[lane] = make_uint4(0u, 0u, 0u, 0u);
-        for (int b = 0; b < n; b += 32) {
-            const int row = b + lane;
-            const bool valid = row < n;
-            const uint32_t g = s + (uint32_t)row;
-            uint32_t code = 0u;
-            int64_t x = 0;
-            float fb = 0.0f, fa = 0.0f, fl = 0.0f;
-            int32_t gs = 0;
-            if (valid) {
-                code = outc[g];
-                x = id[g];
-                fb = birth[g];
-                fa = P.age_from_birth ? 0.0f : age[g];
-                fl = lastb[g];
-                if (genetics) gs = gslot[g];
-            }
-            const int k = code & 7;
-            const uint32_t obk = __shfl_sync(FULL_MASK, ob, k >= 2 ? k - 2 : 0);
-            if (genetics && __any_sync(FULL_MASK, valid && k == 0)) {
-                // the genome slot of an agent dying this step goes to the next free list
-                const uint32_t q = warp_agg_add(valid && k == 0, 0u, &rs->dead_count, 1u);
-                if (valid && k == 0) {
-                    if (carry + q < P.genome_capacity) freelist2[carry + q] = (uint32_t)gs;
-                    else set_error(rs, kErrInternal, 5u);
+        // the rows of the cell in groups of kGroup chunks of 32: the loads of a
+        // group are issued together, then its chunks are written out
+        constexpr int kGroup = 4;
+        for (int b0 = 0; b0 < n; b0 += 32 * kGroup) {
+            uint32_t codes[kGroup];
+            int64_t xs[kGroup];
+            float fbs[kGroup], fas[kGroup], fls[kGroup];
+            int32_t gss[kGroup];
+#pragma unroll
+            for (int q = 0; q < kGroup; q++) {
+                const int row = b0 + q * 32 + lane;
+                codes[q] = 0u;
+                xs[q] = 0;
+                fbs[q] = fas[q] = fls[q] = 0.0f;
+                gss[q] = 0;
+                if (row < n) {
+                    const uint32_t g = s + (uint32_t)row;
+                    codes[q] = outc[g];
+                    xs[q] = id[g];
+                    fbs[q] = birth[g];
+                    if (!P.age_from_birth) fas[q] = age[g];
+                    fls[q] = lastb[g];
+                    if (genetics) gss[q] = gslot[g];
                 }
             }
-            // every survivor to its cell's class base + its rank in the class
-            if (valid && k > 0) {
-                const uint32_t dst = ((k == 1) ? sb : obk) + (code >> 17);
-                if (dst >= cap) {   // inconsistent bases: record, never write out of range
-                    set_error(rs, kErrInternal, 3u);
-                } else {
-                    id2[dst] = x;
-                    birth2[dst] = fb;
-                    lastb2[dst] = fl;
-                    age2[dst] = P.age_from_birth ? __fsub_rn(ft, fb) : fa;
-                    meta2[dst] = (uint8_t)(((code & kOutGender) ? kMetaGender : 0) |
-                                           ((code & kOutFertile) ? kMetaFertile : 0));
-                    if (genetics) gslot2[dst] = gs;
-                }
-            }
-            // newborns (SPopulation::createAgentAtIndex, core/SPopulation.cpp:880-900):
-            // gender = (uchar)(2 * wrandd()) from the mother's birth stream,
-            // females start FERTILE
-            if (valid && (code & kOutBirth)) {
-                const uint32_t rk = brank[g];
-                const int32_t fr = father[g];
-                const uint32_t dst = bb + rk;
-                if (dst >= cap || fr < 0 || (uint32_t)fr >= N) {
-                    set_error(rs, kErrInternal, 4u);
-                } else {
-                    const uint32_t u = draw_block(sd, (uint32_t)st, x, kStreamBirth).v[0];
-                    const int64_t baby = nid + (int64_t)(bid + rk);
-                    id2[dst] = baby;
-                    birth2[dst] = ft;
-                    lastb2[dst] = 0.0f;
-                    age2[dst] = 0.0f;
-                    meta2[dst] = (uint8_t)((u >> 31) ? kMetaGender : kMetaFertile);
-                    if (genetics) {
-                        const uint32_t gr = bid + rk;   // birth rank of the step
-                        const uint32_t bs = gr < nfree ? freelist[gr] : hwm + (gr - nfree);
-                        if (bs >= P.genome_capacity) {
-                            set_error(rs, kErrCapacity, bs);
-                        } else {
-                            gslot2[dst] = (int32_t)bs;
-                            uint32_t *br = brec + (size_t)gr * 5;
-                            br[0] = (uint32_t)gs;
-                            br[1] = (uint32_t)gslot[fr];
-                            br[2] = bs;
-                            br[3] = (uint32_t)(uint64_t)x;
-                            br[4] = (uint32_t)((uint64_t)x >> 32);
-                        }
+#pragma unroll
+            for (int q = 0; q < kGroup; q++) {
+                if (b0 + q * 32 >= n) break;   // the same for the whole warp
+                const int row = b0 + q * 32 + lane;
+                const bool valid = row < n;
+                const uint32_t g = s + (uint32_t)row;
+                const uint32_t code = codes[q];
+                const int64_t x = xs[q];
+                const float fb = fbs[q], fa = fas[q], fl = fls[q];
+                const int32_t gs = gss[q];
+                const int k = code & 7;
+                const uint32_t obk = __shfl_sync(FULL_MASK, ob, k >= 2 ? k - 2 : 0);
+                if (genetics && __any_sync(FULL_MASK, valid && k == 0)) {
+                    // the genome slot of an agent dying this step goes to the next free list
+                    const uint32_t q = warp_agg_add(valid && k == 0, 0u, &rs->dead_count, 1u);
+                    if (valid && k == 0) {
+                        if (carry + q < P.genome_capacity) freelist2[carry + q] = (uint32_t)gs;
+                        else set_error(rs, kErrInternal, 5u);
                     }
-                    if (P.log_births) {
-                        const uint64_t li = blog_base + (uint64_t)(bid + rk);
-                        if (li < blog_cap) {
-                            blog[li * 3 + 0] = baby;
-                            blog[li * 3 + 1] = x;
-                            blog[li * 3 + 2] = id[fr];
+                }
+                // every survivor to its cell's class base + its rank in the class
+                if (valid && k > 0) {
+                    const uint32_t dst = ((k == 1) ? sb : obk) + (code >> 17);
+                    if (dst >= cap) {   // inconsistent bases: record, never write out of range
+                        set_error(rs, kErrInternal, 3u);
+                    } else {
+                        id2[dst] = x;
+                        birth2[dst] = fb;
+                        lastb2[dst] = fl;
+                        age2[dst] = P.age_from_birth ? __fsub_rn(ft, fb) : fa;
+                        meta2[dst] = (uint8_t)(((code & kOutGender) ? kMetaGender : 0) |
+                                               ((code & kOutFertile) ? kMetaFertile : 0));
+                        if (genetics) gslot2[dst] = gs;
+                    }
+                }
+                // newborns (SPopulation::createAgentAtIndex, core/SPopulation.cpp:880-900):
+                // gender = (uchar)(2 * wrandd()) from the mother's birth stream,
+                // females start FERTILE
+                if (valid && (code & kOutBirth)) {
+                    const uint32_t rk = brank[g];
+                    const int32_t fr = father[g];
+                    const uint32_t dst = bb + rk;
+                    if (dst >= cap || fr < 0 || (uint32_t)fr >= N) {
+                        set_error(rs, kErrInternal, 4u);
+                    } else {
+                        const uint32_t u = draw_block(sd, (uint32_t)st, x, kStreamBirth).v[0];
+                        const int64_t baby = nid + (int64_t)(bid + rk);
+                        id2[dst] = baby;
+                        birth2[dst] = ft;
+                        lastb2[dst] = 0.0f;
+                        age2[dst] = 0.0f;
+                        meta2[dst] = (uint8_t)((u >> 31) ? kMetaGender : kMetaFertile);
+                        if (genetics) {
+                            const uint32_t gr = bid + rk;   // birth rank of the step
+                            const uint32_t bs = gr < nfree ? freelist[gr] : hwm + (gr - nfree);
+                            if (bs >= P.genome_capacity) {
+                                set_error(rs, kErrCapacity, bs);
+                            } else {
+                                gslot2[dst] = (int32_t)bs;
+                                uint32_t *br = brec + (size_t)gr * 5;
+                                br[0] = (uint32_t)gs;
+                                br[1] = (uint32_t)gslot[fr];
+                                br[2] = bs;
+                                br[3] = (uint32_t)(uint64_t)x;
+                                br[4] = (uint32_t)((uint64_t)x >> 32);
+                            }
+                        }
+                        if (P.log_births) {
+                            const uint64_t li = blog_base + (uint64_t)(bid + rk);
+                            if (li < blog_cap) {
+                                blog[li * 3 + 0] = baby;
+                                blog[li * 3 + 1] = x;
+                                blog[li * 3 + 2] = id[fr];
+                            }
                         }
                     }
                 }
