@@ -616,15 +616,15 @@ extern "C" int qhg_gpu_upload_agents(qhg_run *r, const qhg_agents_soa *a, int64_
     const int64_t maxid = h->next_id;
     const uint32_t live = h->new_n_agents;
     const uint32_t nne = h->new_n_nonempty;
-    const uint32_t big = h->max_cell > (uint32_t)kMaxCell ? 1u : 0u;
+    const uint32_t form = step_form(h->max_cell, live, nne);
     memset(h, 0, sizeof(RunState));
     h->step = first_step;
     h->n_agents = live;
     h->n_nonempty = nne;
     h->next_id = maxid + 1;
     h->hwm = (uint32_t)n;
-    h->big = big;
-    h->big_next = big;
+    h->form = form;
+    h->form_next = form;
     CUDA_TRY(cudaMemcpyAsync(r->d_rs, h, sizeof(RunState), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemsetAsync(r->d_tflag, 0, (size_t)ntiles * sizeof(uint32_t), st));
     CUDA_TRY(cudaStreamSynchronize(st));

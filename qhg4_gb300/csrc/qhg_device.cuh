@@ -27,6 +27,17 @@ struct Tile {
     static constexpr int kThreads = BIG ? 1024 : kTileThreads;
     static constexpr int kMax = BIG ? kTileAgents + kMaxCellBig : kTileMax;
 };
+// The kernels of a step, chosen from the table the step reads: cell-aligned
+// tiles of kTileAgents agents for tables of small cells, one warp per cell
+// for tables whose non-empty cells hold kDenseCell agents or more on
+// average, the big-cell tiles when some cell holds more than kMaxCell.
+// Results do not depend on the form.
+constexpr uint32_t kFormTile = 0u, kFormBig = 1u, kFormCell = 2u;
+constexpr uint32_t kDenseCell = 24u;
+__host__ __device__ inline uint32_t step_form(uint32_t max_cell, uint32_t n_agents, uint32_t n_nonempty) {
+    if (max_cell > (uint32_t)kMaxCell) return kFormBig;
+    return ((uint64_t)n_agents >= (uint64_t)kDenseCell * n_nonempty) ? kFormCell : kFormTile;
+}
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 2;            // cells per thread in the cell scan
 constexpr int kScanTile = kScanThreads * kScanItems;
@@ -140,8 +151,8 @@ struct RunState {
     uint32_t dead_count;     // deaths of this step pushed to the next free list
     int32_t genome_step;     // step whose newborns k_genomes builds
     uint32_t n_staged;       // batches: agents waiting to be placed by k_inject
-    uint32_t big;            // 1: some cell holds more than kMaxCell agents (big-cell kernels run)
-    uint32_t big_next;       // the same for the table the step writes (set by its commit)
+    uint32_t form;           // kernels of the step (kFormTile, kFormBig, kFormCell)
+    uint32_t form_next;      // the same for the table the step writes (set by its commit)
     uint32_t max_cell;       // largest cell of the next table (cell scan)
     uint32_t stall_tile;     // tests of the bounded waits: tile + 1 whose scan status is withheld once
     // statistics ring: [step % kStatsRing][live, births, deaths, moves]

@@ -345,7 +345,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
     extern __shared__ __align__(16) unsigned char qhg_smem[];
     ActionsSmemT<TM, TT, BATCH> &S = *reinterpret_cast<ActionsSmemT<TM, TT, BATCH> *>(qhg_smem);
     if (rs->error != 0u) return;   // an earlier kernel failed: keep the state
-    if (rs->big != (BIG ? 1u : 0u)) return;   // the other form runs this step
+    if (rs->form != (BIG ? kFormBig : kFormTile)) return;   // another form runs this step
     const int tid = threadIdx.x;
     const int lane = tid & 31;
     const int32_t step = rs->step;
@@ -1081,8 +1081,8 @@ __device__ __forceinline__ void commit_step(const StepConst &P, const BatchBuffe
         nx[0] = 0ull; nx[1] = 0ull; nx[2] = 0ull; nx[3] = 0ull;
         rs->n_agents = rs->new_n_agents;
         rs->n_nonempty = rs->new_n_nonempty;
-        rs->big_next = (rs->max_cell > (uint32_t)kMaxCell) ? 1u : 0u;
-        if (BIG) rs->big = rs->big_next;
+        rs->form_next = step_form(rs->max_cell, rs->new_n_agents, rs->new_n_nonempty);
+        if (BIG) rs->form = rs->form_next;
         rs->max_cell = 0u;
         rs->next_id += (int64_t)rs->births;
         rs->birth_log_n += rs->births;
@@ -1139,18 +1139,18 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
     extern __shared__ __align__(16) unsigned char qhg_smem[];
     ScatterSmemT<TM, TT> &S = *reinterpret_cast<ScatterSmemT<TM, TT> *>(qhg_smem);
     if (rs->error != 0u) return;   // the state stays as before the step
-    // The form of this step is read once per CTA.  The normal form is
-    // launched first; its commit only records the next step's form, and the
-    // big form -- launched second -- applies it, from its last CTA, whether it
-    // ran the step or not, so that no CTA of either form sees the flag change.
-    if (threadIdx.x == 0) S.last = rs->big;
+    // The form of this step is read once per CTA.  The tile and cell forms
+    // are launched first; their commit only records the next step's form, and
+    // the big form -- launched last -- applies it, from its last CTA, whether
+    // it ran the step or not, so that no CTA of any form sees the flag change.
+    if (threadIdx.x == 0) S.last = rs->form;
     __syncthreads();
-    if (S.last != (BIG ? 1u : 0u)) {
+    if (S.last != (BIG ? kFormBig : kFormTile)) {
         if (BIG && threadIdx.x == 0) {
             __threadfence();
             if (atomicAdd(&rs->scatter_ctas_done, 1u) == gridDim.x - 1) {
                 rs->scatter_ctas_done = 0u;
-                rs->big = rs->big_next;
+                rs->form = rs->form_next;
                 __threadfence();
             }
         }
@@ -1450,7 +1450,7 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
     __shared__ uint32_t red[kCellWarps];
     CellWarpSmem &W = reinterpret_cast<CellWarpSmem *>(qhg_smem)[threadIdx.x >> 5];
     if (rs->error != 0u) return;   // an earlier kernel failed: keep the state
-    if (rs->big != 0u) return;     // the big-cell form runs this step
+    if (rs->form != kFormCell) return;   // another form runs this step
     // OldAgeDeath of a specialised program is decided before the other
     // actions, in the same dense draw pass as the pairing picks
     constexpr int kOad = prog_oad_index(PROG);
@@ -1775,10 +1775,10 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
     __shared__ uint32_t s_flag;
     if (rs->error != 0u) return;   // the state stays as before the step
     // the form of the step is read once per CTA (the big form, launched
-    // after this one, applies the next step's form)
-    if (threadIdx.x == 0) s_flag = rs->big;
+    // last, applies the next step's form)
+    if (threadIdx.x == 0) s_flag = rs->form;
     __syncthreads();
-    if (s_flag != 0u) return;
+    if (s_flag != kFormCell) return;
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const int32_t step = rs->step;
@@ -2330,7 +2330,11 @@ static void set_tile_attributes() {
     if (dev < 0 || dev >= 64 || done[dev]) return;
     set_cell_attr<0, false>(); set_cell_attr<1, false>(); set_cell_attr<2, false>(); set_cell_attr<3, false>();
     set_cell_attr<0, true>(); set_cell_attr<1, true>();
+    set_actions_attr<0, false, false>(); set_actions_attr<1, false, false>();
+    set_actions_attr<2, false, false>(); set_actions_attr<3, false, false>();
+    set_actions_attr<0, true, false>(); set_actions_attr<1, true, false>();
     set_actions_attr<0, false, true>(); set_actions_attr<0, true, true>();
+    set_scatter_attr<false, false>(); set_scatter_attr<true, false>();
     set_scatter_attr<false, true>(); set_scatter_attr<true, true>();
     done[dev] = true;
 }
@@ -2346,12 +2350,15 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
     if (batch) BB = *BBp;
     else memset(&BB, 0, sizeof(BB));
     constexpr size_t kSmC = sizeof(CellWarpSmem) * kCellWarps;
+    const size_t kSmA = batch ? sizeof(ActionsSmemT<Tile<false>::kMax, Tile<false>::kThreads, true>)
+                              : sizeof(ActionsSmemT<Tile<false>::kMax, Tile<false>::kThreads, false>);
+    constexpr size_t kSmS = sizeof(ScatterSmemT<Tile<false>::kMax, Tile<false>::kThreads>);
     const size_t kSmAB = batch ? sizeof(ActionsSmemT<Tile<true>::kMax, Tile<true>::kThreads, true>)
                                : sizeof(ActionsSmemT<Tile<true>::kMax, Tile<true>::kThreads, false>);
     constexpr size_t kSmSB = sizeof(ScatterSmemT<Tile<true>::kMax, Tile<true>::kThreads>);
     if (ev) cudaEventRecord(ev[0], stream);
-    // both forms are launched; the one that does not match the step's cell
-    // sizes (RunState::big, set by the previous step) returns at once
+    // every form is launched; those that do not match the step's table
+    // (RunState::form, set by the previous step) return at once
 #define QHG_LAUNCH_ACTIONS(PR, BT, BG, GRID, SM)                                                          \
     k_actions<PR, BT, BG><<<GRID, Tile<BG>::kThreads, SM, stream>>>(                                      \
         *P, BB, rs, B->nonempty, B->ne_start, B->tile_first, B->id, B->birth, B->age, B->lastb, B->meta, \
@@ -2362,16 +2369,16 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
         B->necm, B->outc, B->father, B->brank, B->clsc)
     if (batch) {
         switch (P->program) {
-        case 1: QHG_LAUNCH_CELL(1, true); break;
-        default: QHG_LAUNCH_CELL(0, true); break;
+        case 1: QHG_LAUNCH_ACTIONS(1, true, false, L.actions_grid, kSmA); QHG_LAUNCH_CELL(1, true); break;
+        default: QHG_LAUNCH_ACTIONS(0, true, false, L.actions_grid, kSmA); QHG_LAUNCH_CELL(0, true); break;
         }
         QHG_LAUNCH_ACTIONS(0, true, true, L.big_grid, kSmAB);
     } else {
         switch (P->program) {
-        case 1: QHG_LAUNCH_CELL(1, false); break;
-        case 2: QHG_LAUNCH_CELL(2, false); break;
-        case 3: QHG_LAUNCH_CELL(3, false); break;
-        default: QHG_LAUNCH_CELL(0, false); break;
+        case 1: QHG_LAUNCH_ACTIONS(1, false, false, L.actions_grid, kSmA); QHG_LAUNCH_CELL(1, false); break;
+        case 2: QHG_LAUNCH_ACTIONS(2, false, false, L.actions_grid, kSmA); QHG_LAUNCH_CELL(2, false); break;
+        case 3: QHG_LAUNCH_ACTIONS(3, false, false, L.actions_grid, kSmA); QHG_LAUNCH_CELL(3, false); break;
+        default: QHG_LAUNCH_ACTIONS(0, false, false, L.actions_grid, kSmA); QHG_LAUNCH_CELL(0, false); break;
         }
         QHG_LAUNCH_ACTIONS(0, false, true, L.big_grid, kSmAB);
     }
@@ -2398,9 +2405,11 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
         B->brank, B->sbase, B->bbase, B->bidbase, B->obase, B->clsc, B->id2, B->birth2, B->age2, B->lastb2, \
         B->meta2, B->blog, B->blog_cap, B->gslot, B->gslot2, B->freelist, B->freelist2, B->brec)
     if (batch) {
+        QHG_LAUNCH_SCATTER(true, false, L.scatter_grid, kSmS);
         QHG_LAUNCH_SCATTER_CELL(true);
         QHG_LAUNCH_SCATTER(true, true, L.big_grid, kSmSB);
     } else {
+        QHG_LAUNCH_SCATTER(false, false, L.scatter_grid, kSmS);
         QHG_LAUNCH_SCATTER_CELL(false);
         QHG_LAUNCH_SCATTER(false, true, L.big_grid, kSmSB);
     }
@@ -2431,12 +2440,21 @@ extern "C" int qhg_launch_step_timed(const qhg::StepConst *P, qhg::RunState *rs,
 }
 
 // CTAs of each tile kernel (normal form) that fit on one SM at once
+// (tile and cell forms share the launch shape: the smaller of the two)
 extern "C" void qhg_tile_ctas_per_sm(int *actions, int *scatter) {
-    int a = 0, b = 0;
+    int a = 0, b = 0, ac = 0, bc = 0;
     set_tile_attributes();
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, qhg::k_actions_cell<0, false>, qhg::kCellThreads,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &a, qhg::k_actions<0, false, false>, qhg::kTileThreads,
+        sizeof(qhg::ActionsSmemT<qhg::Tile<false>::kMax, qhg::Tile<false>::kThreads, false>));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &b, qhg::k_scatter<false, false>, qhg::kTileThreads,
+        sizeof(qhg::ScatterSmemT<qhg::Tile<false>::kMax, qhg::Tile<false>::kThreads>));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ac, qhg::k_actions_cell<0, false>, qhg::kCellThreads,
                                                   sizeof(qhg::CellWarpSmem) * qhg::kCellWarps);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, qhg::k_scatter_cell<false>, qhg::kCellThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bc, qhg::k_scatter_cell<false>, qhg::kCellThreads, 0);
+    a = std::min(a, ac);
+    b = std::min(b, bc);
     *actions = a > 0 ? a : 1;
     *scatter = b > 0 ? b : 1;
 }
