@@ -394,6 +394,7 @@ extern "C" int qhg_gpu_create(const qhg_run_desc *desc, qhg_run **out) {
     StepConst &P = r->P;
     memset(&P, 0, sizeof(P));
     P.seed = desc->seed;
+    philox_round_keys(P.seed, P.rkey);
     P.n_act = desc->n_actions;
     P.log_births = (desc->flags & QHG_FLAG_LOG_BIRTHS) ? 1 : 0;
     {

@@ -101,6 +101,7 @@ struct ActionConst {
 
 struct StepConst {
     uint64_t seed;
+    uint32_t rkey[20];       // Philox round keys of the seed (philox_round_keys)
     int32_t n_act;
     int32_t age_from_birth;  // GetOld or OldAgeDeath runs: a survivor's age is t - birth
     int32_t has_pair;
@@ -242,29 +243,69 @@ struct LaunchShape {
 // ------------------------------------------------------------- Philox
 struct Draw4 { uint32_t v[4]; };
 
+constexpr uint32_t kPhiloxM0 = 0xD2511F53u, kPhiloxM1 = 0xCD9E8D57u;
+constexpr uint32_t kPhiloxW0 = 0x9E3779B9u, kPhiloxW1 = 0xBB67AE85u;
+
+// Philox4x32-10 (Salmon et al., SC'11); each round's two 32x32-bit products
+// are taken as one 64-bit product each (high and low words)
 __device__ __forceinline__ Draw4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
                                                uint32_t k0, uint32_t k1) {
 #pragma unroll
     for (int r = 0; r < 10; r++) {
-        uint32_t lo0 = 0xD2511F53u * c0;
-        uint32_t hi0 = __umulhi(0xD2511F53u, c0);
-        uint32_t lo1 = 0xCD9E8D57u * c2;
-        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2);
-        uint32_t n0 = hi1 ^ c1 ^ k0;
-        uint32_t n2 = hi0 ^ c3 ^ k1;
-        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
-        k0 += 0x9E3779B9u;
-        k1 += 0xBB67AE85u;
+        const uint64_t p0 = (uint64_t)kPhiloxM0 * c0;
+        const uint64_t p1 = (uint64_t)kPhiloxM1 * c2;
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+        const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        c0 = n0; c1 = (uint32_t)p1; c2 = n2; c3 = (uint32_t)p0;
+        k0 += kPhiloxW0;
+        k1 += kPhiloxW1;
     }
     Draw4 d;
     d.v[0] = c0; d.v[1] = c1; d.v[2] = c2; d.v[3] = c3;
     return d;
 }
 
+// the same with the ten round keys given (rk[2r], rk[2r+1] for round r)
+__device__ __forceinline__ Draw4 philox4x32_10_rk(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                                  const uint32_t *rk) {
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+        const uint64_t p0 = (uint64_t)kPhiloxM0 * c0;
+        const uint64_t p1 = (uint64_t)kPhiloxM1 * c2;
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ rk[2 * r];
+        const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ rk[2 * r + 1];
+        c0 = n0; c1 = (uint32_t)p1; c2 = n2; c3 = (uint32_t)p0;
+    }
+    Draw4 d;
+    d.v[0] = c0; d.v[1] = c1; d.v[2] = c2; d.v[3] = c3;
+    return d;
+}
+
+// round keys of a seed (host and device)
+__host__ __device__ inline void philox_round_keys(uint64_t seed, uint32_t *rk) {
+    uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    for (int r = 0; r < 10; r++) {
+        rk[2 * r] = k0;
+        rk[2 * r + 1] = k1;
+        k0 += kPhiloxW0;
+        k1 += kPhiloxW1;
+    }
+}
+
 // the block `blk` of the stream (seed, step, id)
 __device__ __forceinline__ Draw4 draw_block(uint64_t seed, uint32_t step, int64_t id, uint32_t blk) {
     uint64_t u = (uint64_t)id;
     return philox4x32_10(blk, step, (uint32_t)u, (uint32_t)(u >> 32), (uint32_t)seed, (uint32_t)(seed >> 32));
+}
+
+// the block `blk` of an agent's stream: from the run's precomputed round keys
+// (a single run: kernel-parameter constants) or from the run's seed (batches)
+template <bool BATCH>
+__device__ __forceinline__ Draw4 run_block(const StepConst &P, uint64_t seed, uint32_t step, int64_t id,
+                                           uint32_t blk) {
+    if (BATCH) return draw_block(seed, step, id, blk);
+    const uint64_t u = (uint64_t)id;
+    return philox4x32_10_rk(blk, step, (uint32_t)u, (uint32_t)(u >> 32), P.rkey);
 }
 
 }  // namespace qhg

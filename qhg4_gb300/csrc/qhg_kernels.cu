@@ -45,20 +45,21 @@ __device__ __forceinline__ uint32_t pick4(const Draw4 &d, uint32_t k) {
 // last Philox block.  The first block is drawn at once, where the warp is
 // converged (the actions' draws are taken under divergent conditions, and
 // most of them fall in that block).
+template <bool BATCH>
 struct AgentDraws {
     uint64_t seed;
     int64_t id;
     uint32_t step;
     uint32_t blk;
     Draw4 d;
-    __device__ __forceinline__ void init(uint64_t s, uint32_t st, int64_t i) {
+    __device__ __forceinline__ void init(const StepConst &P, uint64_t s, uint32_t st, int64_t i) {
         seed = s; step = st; id = i; blk = kStreamActions;
-        d = draw_block(s, st, i, kStreamActions);
+        d = run_block<BATCH>(P, s, st, i, kStreamActions);
     }
-    __device__ __forceinline__ uint32_t get(uint32_t k) {
+    __device__ __forceinline__ uint32_t get(const StepConst &P, uint32_t k) {
         const uint32_t b = kStreamActions + (k >> 2);
         if (b != blk) {
-            d = draw_block(seed, step, id, b);
+            d = run_block<BATCH>(P, seed, step, id, b);
             blk = b;
         }
         return pick4(d, k & 3u);
@@ -198,6 +199,16 @@ __host__ __device__ constexpr int prog_oad_index(int p) {
                           : prog_act(p, 2) == kOldAgeDeath ? 2 : prog_act(p, 3) == kOldAgeDeath ? 3
                           : prog_act(p, 4) == kOldAgeDeath ? 4 : prog_act(p, 5) == kOldAgeDeath ? 5 : -1);
 }
+// position of an action type in a specialised program (-1 if absent); for
+// Verhulst either of its two forms, for moves either of the two move actions
+__host__ __device__ constexpr int prog_index(int p, int t0, int t1) {
+    return p == 0 ? -1 : (prog_act(p, 0) == t0 || prog_act(p, 0) == t1 ? 0
+                          : prog_act(p, 1) == t0 || prog_act(p, 1) == t1 ? 1
+                          : prog_act(p, 2) == t0 || prog_act(p, 2) == t1 ? 2
+                          : prog_act(p, 3) == t0 || prog_act(p, 3) == t1 ? 3
+                          : prog_act(p, 4) == t0 || prog_act(p, 4) == t1 ? 4
+                          : prog_act(p, 5) == t0 || prog_act(p, 5) == t1 ? 5 : -1);
+}
 // how agent_outcome treats an agent inside the OldAgeDeath window: draw and
 // decide, leave it to the caller (queued), or apply a decision made before
 constexpr int kOadDraw = 0, kOadQueue = 1, kOadGiven = 2;
@@ -245,8 +256,8 @@ __device__ __forceinline__ uint8_t agent_outcome(const StepConst &P, const Batch
     bool alive = true;
     bool bflag = false;
     int dir = 0;
-    AgentDraws dr;
-    dr.init(seed, (uint32_t)stepR, id);
+    AgentDraws<BATCH> dr;
+    dr.init(P, seed, (uint32_t)stepR, id);
     constexpr int NA = PROG ? prog_len(PROG) : kMaxActions;
 #pragma unroll (PROG ? NA : 1)
     for (int a = 0; a < NA; a++) {
@@ -265,13 +276,13 @@ __device__ __forceinline__ uint8_t agent_outcome(const StepConst &P, const Batch
             uint32_t k = A.window;
             if (cv.tk == 1u) {
                 if (female && mated) {
-                    if ((uint64_t)dr.get(k++) < cv.tb) bflag = true;
+                    if ((uint64_t)dr.get(P, k++) < cv.tb) bflag = true;
                 }
             } else if (cv.tk == 2u) {
-                if ((uint64_t)dr.get(k++) < cv.tb) alive = false;
+                if ((uint64_t)dr.get(P, k++) < cv.tb) alive = false;
             }
             if (alive) {
-                if ((uint64_t)dr.get(k) < cv.td) alive = false;
+                if ((uint64_t)dr.get(P, k) < cv.td) alive = false;
             }
             if (!alive) cnt_deaths++;
             break;
@@ -288,7 +299,7 @@ __device__ __forceinline__ uint8_t agent_outcome(const StepConst &P, const Batch
             } else if (OAD == kOadGiven) {
                 die = oad_die;
             } else {
-                const uint32_t u = dr.get(A.window);
+                const uint32_t u = dr.get(P, A.window);
                 const double t = __dmul_rn(__dmul_rn(A.oad_w, (double)u), 2.3283064365386962890625e-10);
                 const double thr = __dadd_rn(A.oad_M, __dadd_rn(A.oad_a, t));
                 die = (double)fa > thr;
@@ -297,16 +308,16 @@ __device__ __forceinline__ uint8_t agent_outcome(const StepConst &P, const Batch
             break;
         }
         case kRandomMove: {
-            if ((uint64_t)dr.get(A.window) < A.pthr) {
-                const uint32_t u2 = dr.get(A.window + 1);
+            if ((uint64_t)dr.get(P, A.window) < A.pthr) {
+                const uint32_t u2 = dr.get(P, A.window + 1);
                 const int d = (int)(((uint64_t)(cv.nn + 1u) * (uint64_t)u2) >> 32);
                 if (d > 0 && ((cv.vm >> (d - 1)) & 1u)) { dir = d; cnt_moves++; }
             }
             break;
         }
         case kWeightedMove: {
-            if ((uint64_t)dr.get(A.window) < A.pthr) {
-                const uint32_t u2 = dr.get(A.window + 1);
+            if ((uint64_t)dr.get(P, A.window) < A.pthr) {
+                const uint32_t u2 = dr.get(P, A.window + 1);
                 int d;
                 if (cv.wf & 1u) {
                     d = (int)(((uint64_t)(cv.nn + 1u) * (uint64_t)u2) >> 32);
@@ -326,6 +337,86 @@ __device__ __forceinline__ uint8_t agent_outcome(const StepConst &P, const Batch
     const int cls = alive ? (1 + dir) : 0;
     return (uint8_t)(cls | (bflag ? kOutBirth : 0) | (fert ? kOutFertile : 0) |
                      ((m8 & kMetaGender) ? kOutGender : 0) | (dir > 0 ? kOutMoved : 0));
+}
+
+// The actions of a specialised program (Fertility, RandomPair, Verhulst,
+// a move, GetOld[, OldAgeDeath]) for one agent, before its mate is known:
+// the outcome for both cases where it depends on a mate (a FERTILE female in
+// a cell whose Verhulst birth rate is positive: with a mate she draws for a
+// birth first and the death draw is the next one).  Bits of the state:
+constexpr uint32_t kStDir = 7u;        // move direction (neighbour slot + 1), 0 none
+constexpr uint32_t kStFert = 8u;       // FERTILE after Fertility
+constexpr uint32_t kStGender = 16u;
+constexpr uint32_t kStMateDep = 32u;   // the outcome depends on a mate
+constexpr uint32_t kStDeadU = 64u;     // Verhulst kills it (without a mate)
+constexpr uint32_t kStDeadM = 128u;    // Verhulst kills it (with a mate)
+constexpr uint32_t kStBirthM = 256u;   // gives birth (with a mate)
+constexpr int kStOad = 9;              // bits 9-10, OldAgeDeath: 0 survives, 1 dies, 2 inside the window
+
+template <int PROG, bool BATCH>
+__device__ __forceinline__ uint32_t agent_state(const StepConst &P, const BatchRun *R, int32_t step, float fT,
+                                                int64_t id, uint8_t m8, float fb, float fa, float fl,
+                                                const CellView &cv, const uint64_t *wt) {
+    constexpr int iF = prog_index(PROG, kFertility, kFertility);
+    constexpr int iV = prog_index(PROG, kVerhulst, kVerhulstVarK);
+    constexpr int iM = prog_index(PROG, kRandomMove, kWeightedMove);
+    constexpr int iO = prog_index(PROG, kOldAgeDeath, kOldAgeDeath);
+    static_assert(PROG == 0 || (iF >= 0 && iV > iF && iM > iV), "program order: Fertility, Verhulst, move");
+    if constexpr (PROG == 0) {
+        return 0u;
+    } else {
+    constexpr bool kWeighted = prog_act(PROG, iM) == kWeightedMove;
+    const int32_t stepR = BATCH ? step - R->step0 : step;
+    const float fTR = BATCH ? (float)stepR : fT;
+    AgentDraws<BATCH> dr;
+    dr.init(P, BATCH ? R->seed : P.seed, (uint32_t)stepR, id);
+    const bool female = !(m8 & kMetaGender);
+    uint32_t st = female ? 0u : kStGender;
+    {   // Fertility::execute (actions/Fertility.cpp:49-73)
+        const ActionConst &A = BATCH ? R->act[iF] : P.act[iF];
+        const bool fert = female ? (fa > A.f0) && (fa < A.f1) && (__fsub_rn(fTR, fl) > A.f2) : fa > A.f0;
+        if (fert) st |= kStFert;
+    }
+    {   // LinearBirth / LinearDeath ::execute (actions/LinearBirth.cpp:122-166,
+        // actions/LinearDeath.cpp:131-150)
+        const ActionConst &A = BATCH ? R->act[iV] : P.act[iV];
+        const uint32_t u0 = dr.get(P, A.window), u1 = dr.get(P, A.window + 1u);
+        if (cv.tk == 1u) {
+            if (female && (m8 & kMetaFertile)) {
+                st |= kStMateDep;
+                if ((uint64_t)u0 < cv.tb) st |= kStBirthM;
+                if ((uint64_t)u1 < cv.td) st |= kStDeadM;
+            }
+            if ((uint64_t)u0 < cv.td) st |= kStDeadU;
+        } else if (cv.tk == 2u) {
+            if ((uint64_t)u0 < cv.tb || (uint64_t)u1 < cv.td) st |= kStDeadU;
+        } else {
+            if ((uint64_t)u0 < cv.td) st |= kStDeadU;
+        }
+    }
+    {   // RandomMove / WeightedMove ::execute (actions/RandomMove.cpp:65-100,
+        // actions/WeightedMove.cpp:45-106), for an agent still alive
+        const ActionConst &A = BATCH ? R->act[iM] : P.act[iM];
+        if ((uint64_t)dr.get(P, A.window) < A.pthr) {
+            const uint32_t u2 = dr.get(P, A.window + 1u);
+            int d;
+            if (!kWeighted || (cv.wf & 1u)) {
+                d = (int)(((uint64_t)(cv.nn + 1u) * (uint64_t)u2) >> 32);
+            } else {
+                d = 0;
+                for (int q = 0; q < (int)cv.nn; q++) d += (wt[q] <= (uint64_t)u2) ? 1 : 0;
+            }
+            if (d > 0 && ((cv.vm >> (d - 1)) & 1u)) st |= (uint32_t)d;
+        }
+    }
+    if (iO >= 0) {   // OldAgeDeath::execute (actions/OldAgeDeath.cpp:48-67): the window test
+        const ActionConst &A = BATCH ? R->act[iO > 0 ? iO : 0] : P.act[iO > 0 ? iO : 0];
+        const float fa2 = __fsub_rn(fTR, fb);
+        const uint32_t o = (fa2 <= A.age_lo) ? 0u : ((fa2 > A.age_hi) ? 1u : 2u);
+        st |= o << kStOad;
+    }
+    return st;
+    }
 }
 
 template <int PROG, bool BATCH, bool BIG>
@@ -559,7 +650,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                     sd = R.seed;
                     st = step - R.step0;
                 }
-                const uint32_t u = draw_block(sd, (uint32_t)st, S.fid[pos], kStreamPair).v[0];
+                const uint32_t u = run_block<BATCH>(P, sd, (uint32_t)st, S.fid[pos], kStreamPair).v[0];
                 S.oadq[S.cstart[lc] + j] = (uint16_t)(((uint64_t)(nL - j) * (uint64_t)u) >> 32);
             }
             __syncthreads();
@@ -685,7 +776,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                     const ActionConst &A = BATCH ? R->act[kOad] : P.act[kOad];
                     const int32_t stepR = BATCH ? step - R->step0 : step;
                     const uint32_t w = A.window;
-                    const uint32_t u = pick4(draw_block(BATCH ? R->seed : P.seed, (uint32_t)stepR, S.fid[q],
+                    const uint32_t u = pick4(run_block<BATCH>(P, BATCH ? R->seed : P.seed, (uint32_t)stepR, S.fid[q],
                                                         kStreamActions + (w >> 2)), w & 3u);
                     const double th = __dmul_rn(__dmul_rn(A.oad_w, (double)u), 2.3283064365386962890625e-10);
                     const double thr = __dadd_rn(A.oad_M, __dadd_rn(A.oad_a, th));
@@ -1344,7 +1435,7 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                 ft = S.cft[lc];
                 nid = BB.rnext[S.crn[lc]];
             }
-            const uint32_t u = draw_block(sd, (uint32_t)st, mid, kStreamBirth).v[0];
+            const uint32_t u = run_block<BATCH>(P, sd, (uint32_t)st, mid, kStreamBirth).v[0];
             const uint8_t g = (uint8_t)(u >> 31);
             const int64_t baby = nid + (int64_t)(S.bid[lc] + rk);
             id2[dst] = baby;
@@ -1396,7 +1487,7 @@ struct CellWarpSmem {
     uint16_t sidx[kMaxCell];     // list positions in ID order: females [0, nF), males [n - nM, n)
     int16_t mate[kMaxCell];      // mate's row of each row, -1 none
     uint16_t pick[kMaxCell / 2]; // pick value of each member of the smaller side (ID order)
-    uint8_t oc[kMaxCell];        // outcome byte of each row
+    uint16_t st[kMaxCell];       // per row: state before the pairing (agent_state), then the outcome byte
     uint32_t odie[kMaxCell / 32];  // OldAgeDeath decided in advance: bit per row, set = dies
     uint32_t oinw[kMaxCell / 32];  // rows inside the OldAgeDeath age window, bit per row
     uint32_t cnt[8];             // class counts: [0] stay, [1..6] movers per neighbour slot
@@ -1455,6 +1546,10 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
     // actions, in the same dense draw pass as the pairing picks
     constexpr int kOad = prog_oad_index(PROG);
     constexpr bool kEarlyOad = kOad >= 0;
+    // a specialised program reads each agent once: its actions run with the
+    // FERTILE lists (keeping both outcomes where the outcome depends on a
+    // mate), the outcome is settled after the pairing
+    constexpr bool kOnePass = PROG > 0;
     const int lane = threadIdx.x & 31;
     const uint32_t lt = lanemask_lt();
     const int32_t step = rs->step;
@@ -1495,6 +1590,16 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
         const uint64_t sd = BATCH ? R->seed : P.seed;
         const int32_t stR = BATCH ? step - R->step0 : step;
         const float fTR = BATCH ? (float)stR : fT;
+        CellView cv;
+        cv.tk = (uint32_t)(v.x >> 62);
+        cv.tb = v.x & ((1ull << 62) - 1ull);
+        cv.td = v.y;
+        cv.nn = cm & 7u;
+        cv.vm = (cm >> 8) & 63u;
+        cv.wf = (cm >> 16) & 1u;
+        cv.c = 0u;   // the WeightedMove thresholds of this cell are W.wt
+        if (lane < 6) W.wt[lane] = wl;
+        __syncwarp();
         // ---- RandomPair::findMates (actions/RandomPair.cpp:146-270): FERTILE
         // lists, ranked by ID; the members of the smaller side pick, in ID
         // order, each pick drawn from the pairing stream of the picking member.
@@ -1502,7 +1607,7 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
         // marked.
         int nF = 0, nM = 0, nq = 0;
         bool wide = false;
-        if (keep && (P.has_pair || kEarlyOad)) {
+        if (keep && (kOnePass || P.has_pair || kEarlyOad)) {
             // groups of kGroupA chunks of 32 rows: a group's loads are issued
             // together (one chunk: larger groups cost registers that the later
             // passes need)
@@ -1510,19 +1615,24 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
             for (int b0 = 0; b0 < n; b0 += 32 * kGroupA) {
                 uint8_t m8s[kGroupA];
                 int64_t xs[kGroupA];
-                float fbs[kGroupA];
+                float fbs[kGroupA], fas[kGroupA], fls[kGroupA];
 #pragma unroll
                 for (int q = 0; q < kGroupA; q++) {
                     const int row = b0 + q * 32 + lane;
                     m8s[q] = 0;
                     xs[q] = 0;
-                    fbs[q] = 0.0f;
+                    fbs[q] = fas[q] = fls[q] = 0.0f;
                     if (row < n) {
-                        if (P.has_pair) {
-                            m8s[q] = meta[s + row];
-                            xs[q] = id[s + row];
+                        const uint32_t g = s + (uint32_t)row;
+                        if (kOnePass || P.has_pair) {
+                            m8s[q] = meta[g];
+                            xs[q] = id[g];
                         }
-                        if (kEarlyOad) fbs[q] = birth[s + row];
+                        if (kOnePass || kEarlyOad) fbs[q] = birth[g];
+                        if (kOnePass) {
+                            if (P.reads_age) fas[q] = age[g];
+                            fls[q] = lastb[g];
+                        }
                     }
                 }
 #pragma unroll
@@ -1531,9 +1641,14 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                     if (b >= n) break;   // the same for the whole warp
                     const int row = b + lane;
                     const bool valid = row < n;
-                    const bool fert = (m8s[q] & kMetaFertile) != 0;
+                    const bool fert = P.has_pair && (m8s[q] & kMetaFertile) != 0;
                     const bool male = (m8s[q] & kMetaGender) != 0;
                     const int64_t x = fert ? xs[q] : 0;
+                    uint32_t stt = 0u;
+                    if (kOnePass && valid) {
+                        stt = agent_state<PROG, BATCH>(P, R, step, fT, xs[q], m8s[q], fbs[q], fas[q], fls[q], cv, W.wt);
+                        W.st[row] = (uint16_t)stt;
+                    }
                     if (P.has_pair && valid) W.mate[row] = -1;
                     const uint32_t fm = __ballot_sync(FULL_MASK, fert && !male);
                     const uint32_t mm = __ballot_sync(FULL_MASK, fert && male);
@@ -1549,8 +1664,14 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                         const ActionConst &A = BATCH ? R->act[kOad] : P.act[kOad];
                         bool inw = false;
                         if (valid) {
-                            const float fa = __fsub_rn(fTR, fbs[q]);
-                            inw = !(fa <= A.age_lo) && !(fa > A.age_hi);
+                            if (kOnePass) {
+                                // inside the window and alive after Verhulst in some case
+                                const bool may_live = !(stt & kStDeadU) || ((stt & kStMateDep) && !(stt & kStDeadM));
+                                inw = ((stt >> kStOad) & 3u) == 2u && may_live;
+                            } else {
+                                const float fa = __fsub_rn(fTR, fbs[q]);
+                                inw = !(fa <= A.age_lo) && !(fa > A.age_hi);
+                            }
                         }
                         const uint32_t qm = __ballot_sync(FULL_MASK, inw);
                         nq += __popc(qm);
@@ -1563,7 +1684,6 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
             }
             __syncwarp();
         }
-        if (lane < 6) W.wt[lane] = wl;   // read in the action pass below, after warp syncs
         const bool pairs = nF > 0 && nM > 0;
         if (pairs) {
             rank_lists(W, n, nF, nM, wide, id, s);
@@ -1604,7 +1724,7 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                     blk = kStreamActions + (w >> 2);
                     wd = w & 3u;
                 }
-                const Draw4 d4 = draw_block(sd, (uint32_t)stR, x, blk);
+                const Draw4 d4 = run_block<BATCH>(P, sd, (uint32_t)stR, x, blk);
                 if (t < m) {
                     W.pick[t] = (uint16_t)(((uint64_t)(nL - (uint32_t)t) * (uint64_t)d4.v[0]) >> 32);
                 } else if (kEarlyOad) {
@@ -1643,16 +1763,9 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
             }
             __syncwarp();
         }
-        // ---- every action on every agent of the cell, then the outcome word
-        // with the agent's rank in its cell's class
-        CellView cv;
-        cv.tk = (uint32_t)(v.x >> 62);
-        cv.tb = v.x & ((1ull << 62) - 1ull);
-        cv.td = v.y;
-        cv.nn = cm & 7u;
-        cv.vm = (cm >> 8) & 63u;
-        cv.wf = (cm >> 16) & 1u;
-        cv.c = 0u;   // the thresholds of this cell are W.wt
+        // ---- every agent's outcome (a specialised program: settled from its
+        // state and its mate; otherwise every action in execution order), then
+        // the outcome word with the agent's rank in its cell's class
         if (lane < 8) W.cnt[lane] = 0u;
         uint32_t births = 0, dead = 0, moved = 0;
         __syncwarp();
@@ -1668,7 +1781,7 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                 m8s[q] = 0;
                 xs[q] = 0;
                 fbs[q] = fas[q] = fls[q] = 0.0f;
-                if (row < n) {
+                if (!kOnePass && row < n) {
                     const uint32_t g = s + (uint32_t)row;
                     m8s[q] = meta[g];
                     xs[q] = id[g];
@@ -1688,6 +1801,31 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                     const uint32_t g = s + (uint32_t)row;
                     if (!keep) {
                         oc = kOutDropped;
+                    } else if (kOnePass) {
+                        // LinearBirth / LinearDeath with or without a mate, the move
+                        // and OldAgeDeath of an agent still alive
+                        const uint32_t stt = W.st[row];
+                        const int mate = pairs ? W.mate[row] : -1;
+                        const bool mated = (stt & kStMateDep) && mate >= 0;
+                        const bool bflag = mated && (stt & kStBirthM);
+                        bool alive = !(stt & (mated ? kStDeadM : kStDeadU));
+                        if (!alive) cnt_deaths++;
+                        const uint32_t dir = alive ? (stt & kStDir) : 0u;
+                        if (dir) cnt_moves++;
+                        if (kEarlyOad && alive) {
+                            const uint32_t o = (stt >> kStOad) & 3u;
+                            if (o == 1u || (o == 2u && ((W.odie[b >> 5] >> lane) & 1u))) {
+                                alive = false;
+                                cnt_deaths++;
+                            }
+                        }
+                        oc = (uint8_t)((alive ? 1u + dir : 0u) | (bflag ? kOutBirth : 0) |
+                                       ((stt & kStFert) ? kOutFertile : 0) | ((stt & kStGender) ? kOutGender : 0) |
+                                       (dir ? kOutMoved : 0));
+                        if (bflag) {
+                            father[g] = (int32_t)(s + (uint32_t)mate);
+                            cnt_births++;
+                        }
                     } else {
                         const int mate = pairs ? W.mate[row] : -1;
                         const bool odie = kEarlyOad && ((W.odie[b >> 5] >> lane) & 1u);
@@ -1701,7 +1839,7 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                             cnt_births++;
                         }
                     }
-                    W.oc[row] = oc;
+                    W.st[row] = oc;
                 }
                 const int cls = oc & 7;
                 const bool counted = valid && cls > 0;
@@ -1730,7 +1868,7 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                 int row = 0;
                 if (q < nF) {
                     row = W.frow[W.sidx[q]];
-                    mo = (W.oc[row] & kOutBirth) != 0;
+                    mo = (W.st[row] & kOutBirth) != 0;
                 }
                 const uint32_t mb = __ballot_sync(FULL_MASK, mo);
                 if (mo) brank[s + (uint32_t)row] = (uint16_t)(run + (uint32_t)__popc(mb & lt));
@@ -1913,7 +2051,7 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                     if (dst >= cap || fr < 0 || (uint32_t)fr >= N) {
                         set_error(rs, kErrInternal, 4u);
                     } else {
-                        const uint32_t u = draw_block(sd, (uint32_t)st, x, kStreamBirth).v[0];
+                        const uint32_t u = run_block<BATCH>(P, sd, (uint32_t)st, x, kStreamBirth).v[0];
                         const int64_t baby = nid + (int64_t)(bid + rk);
                         id2[dst] = baby;
                         birth2[dst] = ft;
@@ -2036,7 +2174,7 @@ k_genomes(const StepConst P, RunState *__restrict__ rs, uint64_t *__restrict__ g
         const uint32_t bs = __ldg(&brec[(size_t)g * 5 + 2]);
         const uint64_t mid = (uint64_t)__ldg(&brec[(size_t)g * 5 + 3]) |
                              ((uint64_t)__ldg(&brec[(size_t)g * 5 + 4]) << 32);
-        const Draw4 d = draw_block(P.seed, step, (int64_t)mid, kStreamBirth + (uint32_t)lane);
+        const Draw4 d = run_block<false>(P, P.seed, step, (int64_t)mid, kStreamBirth + (uint32_t)lane);
         const int i1 = (int)(birth_draw(d, 1) >> 31);
         const int i2 = (int)(birth_draw(d, 2) >> 31);
         int k = 3, nM = 0, nF = 0;
