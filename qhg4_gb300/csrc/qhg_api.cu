@@ -21,6 +21,7 @@ extern "C" int qhg_launch_step(const qhg::StepConst *P, qhg::RunState *rs, const
                                const qhg::BatchBuffers *BB, const qhg::LaunchShape *L, cudaStream_t stream);
 extern "C" void qhg_tile_ctas_per_sm(int *actions, int *scatter);
 extern "C" int qhg_match_program(const int32_t *types, int n);
+extern "C" uint32_t qhg_program_window(int p, int a);
 extern "C" int qhg_launch_gather_genomes(const int32_t *gslot, const uint64_t *genome, uint32_t n, int words,
                                          uint32_t slots, uint64_t *out, cudaStream_t stream);
 extern "C" int qhg_launch_upload(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
@@ -420,6 +421,11 @@ extern "C" int qhg_gpu_create(const qhg_run_desc *desc, qhg_run **out) {
         }
     }
     P.program = qhg_match_program(desc->action_type, desc->n_actions);
+    // a specialised program takes its draws at fixed windows: keep it only if
+    // the windows handed out match them
+    for (int a = 0; P.program > 0 && a < desc->n_actions; a++) {
+        if (P.act[a].window != qhg_program_window(P.program, a)) P.program = 0;
+    }
     cudaError_t e = cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&r->d_rs, sizeof(RunState));
     if (e == cudaSuccess) e = cudaMallocHost(&r->h_rs, sizeof(RunState));

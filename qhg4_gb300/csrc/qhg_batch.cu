@@ -255,6 +255,11 @@ extern "C" int qhg_batch_create(const qhg_batch_desc *desc, qhg_batch **out) {
     }
     P.n_act = desc->n_actions;
     P.program = qhg_match_program(desc->action_type, desc->n_actions) == 1 ? 1 : 0;
+    // a specialised program takes its draws at fixed windows: keep it only if
+    // the windows handed out match them
+    for (int a = 0; P.program > 0 && a < desc->n_actions; a++) {
+        if (P.act[a].window != qhg_program_window(P.program, a)) P.program = 0;
+    }
     b->cell_cap = (uint32_t)desc->cell_capacity;
     b->agent_cap = (uint32_t)desc->agent_capacity;
     b->stage_cap = (uint32_t)desc->stage_capacity;

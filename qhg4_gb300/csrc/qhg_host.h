@@ -22,6 +22,7 @@ extern "C" int qhg_launch_step_timed(const qhg::StepConst *P, qhg::RunState *rs,
                                      cudaEvent_t *ev);
 extern "C" void qhg_tile_ctas_per_sm(int *actions, int *scatter);
 extern "C" int qhg_match_program(const int32_t *types, int n);
+extern "C" uint32_t qhg_program_window(int p, int a);
 
 extern "C" int qhg_launch_batch_stage(uint32_t s0, uint32_t n, uint32_t cell0, uint32_t ncells, const int32_t *cell,
                                       uint8_t *smeta, const uint8_t *sgender, const int64_t *sid, uint32_t *scell,

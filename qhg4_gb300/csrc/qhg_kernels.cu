@@ -209,6 +209,16 @@ __host__ __device__ constexpr int prog_index(int p, int t0, int t1) {
                           : prog_act(p, 4) == t0 || prog_act(p, 4) == t1 ? 4
                           : prog_act(p, 5) == t0 || prog_act(p, 5) == t1 ? 5 : -1);
 }
+// draws an action takes from the agent's action stream, and the first draw
+// (window) of action a of a specialised program: windows follow execution
+// order, as the host hands them out
+__host__ __device__ constexpr uint32_t action_draws(int t) {
+    return (t == kVerhulst || t == kVerhulstVarK || t == kRandomMove || t == kWeightedMove) ? 2u
+           : (t == kOldAgeDeath ? 1u : 0u);
+}
+__host__ __device__ constexpr uint32_t prog_window(int p, int a) {
+    return a <= 0 ? 0u : prog_window(p, a - 1) + action_draws(prog_act(p, a - 1));
+}
 // how agent_outcome treats an agent inside the OldAgeDeath window: draw and
 // decide, leave it to the caller (queued), or apply a decision made before
 constexpr int kOadDraw = 0, kOadQueue = 1, kOadGiven = 2;
@@ -368,8 +378,10 @@ __device__ __forceinline__ uint32_t agent_state(const StepConst &P, const BatchR
     constexpr bool kWeighted = prog_act(PROG, iM) == kWeightedMove;
     const int32_t stepR = BATCH ? step - R->step0 : step;
     const float fTR = BATCH ? (float)stepR : fT;
-    AgentDraws<BATCH> dr;
-    dr.init(P, BATCH ? R->seed : P.seed, (uint32_t)stepR, id);
+    // the Verhulst and move draws lie in the first block of the stream
+    constexpr uint32_t kWV = prog_window(PROG, iV), kWM = prog_window(PROG, iM);
+    static_assert(kWV + 1u < 4u && kWM + 1u < 4u, "draws outside the first block");
+    const Draw4 d = run_block<BATCH>(P, BATCH ? R->seed : P.seed, (uint32_t)stepR, id, kStreamActions);
     const bool female = !(m8 & kMetaGender);
     uint32_t st = female ? 0u : kStGender;
     {   // Fertility::execute (actions/Fertility.cpp:49-73)
@@ -379,8 +391,7 @@ __device__ __forceinline__ uint32_t agent_state(const StepConst &P, const BatchR
     }
     {   // LinearBirth / LinearDeath ::execute (actions/LinearBirth.cpp:122-166,
         // actions/LinearDeath.cpp:131-150)
-        const ActionConst &A = BATCH ? R->act[iV] : P.act[iV];
-        const uint32_t u0 = dr.get(P, A.window), u1 = dr.get(P, A.window + 1u);
+        const uint32_t u0 = d.v[kWV], u1 = d.v[kWV + 1u];
         if (cv.tk == 1u) {
             if (female && (m8 & kMetaFertile)) {
                 st |= kStMateDep;
@@ -397,8 +408,8 @@ __device__ __forceinline__ uint32_t agent_state(const StepConst &P, const BatchR
     {   // RandomMove / WeightedMove ::execute (actions/RandomMove.cpp:65-100,
         // actions/WeightedMove.cpp:45-106), for an agent still alive
         const ActionConst &A = BATCH ? R->act[iM] : P.act[iM];
-        if ((uint64_t)dr.get(P, A.window) < A.pthr) {
-            const uint32_t u2 = dr.get(P, A.window + 1u);
+        if ((uint64_t)d.v[kWM] < A.pthr) {
+            const uint32_t u2 = d.v[kWM + 1u];
             int d;
             if (!kWeighted || (cv.wf & 1u)) {
                 d = (int)(((uint64_t)(cv.nn + 1u) * (uint64_t)u2) >> 32);
@@ -1720,7 +1731,7 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                     }
                     row = (ch << 5) + (int)__fns(cmsk, 0, k + 1);
                     x = id[s + row];
-                    const uint32_t w = (BATCH ? R->act[kOad > 0 ? kOad : 0] : P.act[kOad > 0 ? kOad : 0]).window;
+                    constexpr uint32_t w = prog_window(PROG, kOad > 0 ? kOad : 0);
                     blk = kStreamActions + (w >> 2);
                     wd = w & 3u;
                 }
@@ -2596,6 +2607,9 @@ extern "C" void qhg_tile_ctas_per_sm(int *actions, int *scatter) {
     *actions = a > 0 ? a : 1;
     *scatter = b > 0 ? b : 1;
 }
+
+// first draw of action a of specialised program p (the host checks its windows against it)
+extern "C" uint32_t qhg_program_window(int p, int a) { return qhg::prog_window(p, a); }
 
 // the specialised action program matching a run's action list, 0 if none
 extern "C" int qhg_match_program(const int32_t *types, int n) {
