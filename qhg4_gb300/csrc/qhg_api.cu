@@ -510,17 +510,17 @@ static int alloc_agents(qhg_run *r, uint32_t cap) {
     free_agents(r);
     const int C = r->C;
     for (int p = 0; p < 2; p++) {
-        CUDA_TRY(cudaMalloc(&r->d_id[p], (size_t)cap * sizeof(int64_t)));
-        CUDA_TRY(cudaMalloc(&r->d_birth[p], (size_t)cap * sizeof(float)));
-        CUDA_TRY(cudaMalloc(&r->d_age[p], (size_t)cap * sizeof(float)));
-        CUDA_TRY(cudaMalloc(&r->d_lastb[p], (size_t)cap * sizeof(float)));
-        CUDA_TRY(cudaMalloc(&r->d_meta[p], (size_t)cap));
+        CUDA_TRY(cudaMalloc(&r->d_id[p], (size_t)cap * sizeof(int64_t) + kColumnPad));
+        CUDA_TRY(cudaMalloc(&r->d_birth[p], (size_t)cap * sizeof(float) + kColumnPad));
+        CUDA_TRY(cudaMalloc(&r->d_age[p], (size_t)cap * sizeof(float) + kColumnPad));
+        CUDA_TRY(cudaMalloc(&r->d_lastb[p], (size_t)cap * sizeof(float) + kColumnPad));
+        CUDA_TRY(cudaMalloc(&r->d_meta[p], (size_t)cap + kColumnPad));
         CUDA_TRY(cudaMalloc(&r->d_ne[p], (size_t)C * sizeof(uint32_t)));
         CUDA_TRY(cudaMalloc(&r->d_necm[p], (size_t)C * sizeof(uint32_t)));
         CUDA_TRY(cudaMalloc(&r->d_nes[p], (size_t)(C + 1) * sizeof(uint32_t)));
         CUDA_TRY(cudaMalloc(&r->d_tf[p], ((size_t)cap / kTileAgents + 2) * sizeof(uint32_t)));
     }
-    CUDA_TRY(cudaMalloc(&r->d_outc, (size_t)cap * sizeof(uint32_t)));
+    CUDA_TRY(cudaMalloc(&r->d_outc, (size_t)cap * sizeof(uint32_t) + kColumnPad));
     CUDA_TRY(cudaMalloc(&r->d_father, (size_t)cap * sizeof(int32_t)));
     CUDA_TRY(cudaMalloc(&r->d_brank, (size_t)cap * sizeof(uint16_t)));
     if (r->P.log_births) {
@@ -534,7 +534,7 @@ static int alloc_agents(qhg_run *r, uint32_t cap) {
         // (at most one per live female), so 2 * capacity never runs out
         const uint64_t g = std::min<uint64_t>((uint64_t)cap * 2, 0x7fffffffull);
         for (int p = 0; p < 2; p++) {
-            CUDA_TRY(cudaMalloc(&r->d_gslot[p], (size_t)cap * sizeof(int32_t)));
+            CUDA_TRY(cudaMalloc(&r->d_gslot[p], (size_t)cap * sizeof(int32_t) + kColumnPad));
             CUDA_TRY(cudaMalloc(&r->d_free[p], (size_t)g * sizeof(uint32_t)));
         }
         CUDA_TRY(cudaMalloc(&r->d_genome, (size_t)g * r->P.genome_words * sizeof(uint64_t)));

@@ -284,17 +284,17 @@ extern "C" int qhg_batch_create(const qhg_batch_desc *desc, qhg_batch **out) {
     A((void **)&b->d_cmove, C * sizeof(uint32_t));
     A((void **)&b->d_crun, C * sizeof(uint32_t));
     for (int p = 0; p < 2; p++) {
-        A((void **)&b->d_id[p], N * sizeof(int64_t));
-        A((void **)&b->d_birth[p], N * sizeof(float));
-        A((void **)&b->d_age[p], N * sizeof(float));
-        A((void **)&b->d_lastb[p], N * sizeof(float));
-        A((void **)&b->d_meta[p], N);
+        A((void **)&b->d_id[p], N * sizeof(int64_t) + kColumnPad);
+        A((void **)&b->d_birth[p], N * sizeof(float) + kColumnPad);
+        A((void **)&b->d_age[p], N * sizeof(float) + kColumnPad);
+        A((void **)&b->d_lastb[p], N * sizeof(float) + kColumnPad);
+        A((void **)&b->d_meta[p], N + kColumnPad);
         A((void **)&b->d_ne[p], C * sizeof(uint32_t));
         A((void **)&b->d_necm[p], C * sizeof(uint32_t));
         A((void **)&b->d_nes[p], (C + 1) * sizeof(uint32_t));
         A((void **)&b->d_tf[p], (N / kTileAgents + 2) * sizeof(uint32_t));
     }
-    A((void **)&b->d_outc, N * sizeof(uint32_t));
+    A((void **)&b->d_outc, N * sizeof(uint32_t) + kColumnPad);
     A((void **)&b->d_father, N * sizeof(int32_t));
     A((void **)&b->d_brank, N * sizeof(uint16_t));
     A((void **)&b->d_clsc, C * kCls * sizeof(uint32_t));

@@ -38,6 +38,9 @@ __host__ __device__ inline uint32_t step_form(uint32_t max_cell, uint32_t n_agen
     if (max_cell > (uint32_t)kMaxCell) return kFormBig;
     return ((uint64_t)n_agents >= (uint64_t)kDenseCell * n_nonempty) ? kFormCell : kFormTile;
 }
+// bytes every agent column is allocated beyond its rows: bulk copies read
+// whole 16-byte units around a row range
+constexpr size_t kColumnPad = 64;
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 2;            // cells per thread in the cell scan
 constexpr int kScanTile = kScanThreads * kScanItems;

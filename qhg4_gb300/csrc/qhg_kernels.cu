@@ -1904,6 +1904,75 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
     }
 }
 
+// ---- rows staged in shared memory by bulk copies (cp.async.bulk with
+// completion counted on an mbarrier): a warp copies the rows of its next
+// piece of work while it writes out the current one
+constexpr int kStageRows = 128;   // rows of one staged piece (a cell, or a part of a larger one)
+constexpr uint32_t kStageSpinLimit = 1u << 24;   // polls of a staging wait (with the time limit kWaitLimitNs)
+
+// bytes of one staged column of kStageRows rows of `elem` bytes: room for the
+// 16-byte units around an unaligned row range
+__host__ __device__ constexpr uint32_t stage_col_bytes(uint32_t elem) { return (uint32_t)kStageRows * elem + 32u; }
+// one staging buffer of the scatter: outcome words, IDs, birth times, last
+// births, ages (when the table's ages are not derived from birth times),
+// genome slots (genetics)
+__host__ __device__ inline uint32_t scatter_stage_bytes(bool age_col, bool gslot_col) {
+    return stage_col_bytes(4) + stage_col_bytes(8) + 2u * stage_col_bytes(4) + (age_col ? stage_col_bytes(4) : 0u) +
+           (gslot_col ? stage_col_bytes(4) : 0u);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0u;
+}
+
+// waits for the phase `parity` of an mbarrier to complete; false when the
+// wait ran out of polls or time
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+    uint32_t spins = 0;
+    const uint64_t t0 = globaltimer_ns();
+    while (!mbar_try_wait(bar, parity)) {
+        if (++spins > kStageSpinLimit || globaltimer_ns() - t0 > kWaitLimitNs) return false;
+    }
+    return true;
+}
+
+// bulk copy of `bytes` (a multiple of 16) from global to shared memory, both
+// 16-byte aligned, counted on `bar`
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// the 16-byte units holding rows [a, a + n) of a column of `elem`-byte
+// values: start offset (bytes) and size; the rows begin `head` bytes in
+__device__ __forceinline__ void stage_range(uint32_t a, uint32_t n, uint32_t elem, size_t &off, uint32_t &bytes,
+                                            uint32_t &head) {
+    const size_t lo = (size_t)a * elem, hi = (size_t)(a + n) * elem;
+    off = lo & ~(size_t)15;
+    bytes = (uint32_t)(((hi + 15) & ~(size_t)15) - off);
+    head = (uint32_t)(lo - off);
+}
+
 template <bool BATCH>
 __global__ void __launch_bounds__(kCellThreads, 4)
 k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
@@ -1921,7 +1990,9 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                const int32_t *__restrict__ gslot, int32_t *__restrict__ gslot2,
                const uint32_t *__restrict__ freelist, uint32_t *__restrict__ freelist2,
                uint32_t *__restrict__ brec) {
+    extern __shared__ __align__(16) unsigned char qhg_smem[];
     __shared__ uint32_t s_flag;
+    __shared__ __align__(8) uint64_t s_bar[kCellWarps][2];
     if (rs->error != 0u) return;   // the state stays as before the step
     // the form of the step is read once per CTA (the big form, launched
     // last, applies the next step's form)
@@ -1930,6 +2001,7 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
     if (s_flag != kFormCell) return;
     __syncthreads();
     const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
     const int32_t step = rs->step;
     const float fT = (float)step;
     const int64_t next_id = rs->next_id;
@@ -1943,6 +2015,7 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
     // order, then never used slots; this step's deaths free theirs for the
     // next step, so a newborn never overwrites a parent of the same step
     const bool genetics = P.genome_words > 0;
+    const bool age_col = !P.age_from_birth;
     const uint32_t births = rs->births;
     const uint32_t nfree = rs->nfree;
     const uint32_t hwm = rs->hwm;
@@ -1952,149 +2025,232 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
             freelist2[q] = freelist[births + q];
         }
     }
-    // the bounds and index of the warp's next cell are loaded one cell ahead
-    uint32_t r = blockIdx.x * kCellWarps + (threadIdx.x >> 5);
-    uint32_t nb0 = 0, nb1 = 0, nc0 = 0;
-    if (r < nne) {
-        nb0 = ne_start[r];
-        nb1 = ne_start[r + 1];
-        nc0 = nonempty[r];
+    // the warp's two staging buffers and their mbarriers
+    const uint32_t sbytes = scatter_stage_bytes(age_col, genetics);
+    unsigned char *stage0 = qhg_smem + (size_t)warp * 2u * sbytes;
+    uint64_t *bar = s_bar[warp];
+    if (lane == 0) {
+        mbar_init(&bar[0], 1u);
+        mbar_init(&bar[1], 1u);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    for (; r < nne; r += G) {
-        const uint32_t s = nb0;
-        const int n = (int)(nb1 - nb0);
-        const uint32_t c = nc0;
-        const uint32_t rn = r + G;
-        if (rn < nne) {
-            nb0 = ne_start[rn];
-            nb1 = ne_start[rn + 1];
-            nc0 = nonempty[rn];
+    __syncwarp();
+    uint32_t parity = 0u;     // bit b: phase parity of buffer b's next completion
+    uint32_t inflight = 0u;   // bit b: copies into buffer b not yet waited for (lane 0's view)
+
+    // copies rows [g, g + cnt) of the staged columns into buffer b (lane 0)
+    auto issue = [&](int b, uint32_t g, uint32_t cnt) {
+        if (lane != 0) return;
+        // earlier reads of the buffer by the warp are ordered before the copy
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        inflight |= 1u << b;
+        unsigned char *buf = stage0 + (size_t)b * sbytes;
+        size_t off[6];
+        uint32_t by[6], hd[6], total = 0u;
+        stage_range(g, cnt, 4, off[0], by[0], hd[0]);
+        stage_range(g, cnt, 8, off[1], by[1], hd[1]);
+        stage_range(g, cnt, 4, off[2], by[2], hd[2]);
+        stage_range(g, cnt, 4, off[3], by[3], hd[3]);
+        stage_range(g, cnt, 4, off[4], by[4], hd[4]);
+        stage_range(g, cnt, 4, off[5], by[5], hd[5]);
+        total = by[0] + by[1] + by[2] + by[3] + (age_col ? by[4] : 0u) + (genetics ? by[5] : 0u);
+        mbar_arrive_expect_tx(&bar[b], total);
+        unsigned char *d = buf;
+        bulk_g2s(d, reinterpret_cast<const unsigned char *>(outc) + off[0], by[0], &bar[b]);
+        d += stage_col_bytes(4);
+        bulk_g2s(d, reinterpret_cast<const unsigned char *>(id) + off[1], by[1], &bar[b]);
+        d += stage_col_bytes(8);
+        bulk_g2s(d, reinterpret_cast<const unsigned char *>(birth) + off[2], by[2], &bar[b]);
+        d += stage_col_bytes(4);
+        bulk_g2s(d, reinterpret_cast<const unsigned char *>(lastb) + off[3], by[3], &bar[b]);
+        d += stage_col_bytes(4);
+        if (age_col) {
+            bulk_g2s(d, reinterpret_cast<const unsigned char *>(age) + off[4], by[4], &bar[b]);
+            d += stage_col_bytes(4);
         }
-        // the cell's bases in the next table: stayers, newborns (and their
-        // birth numbers), movers per neighbour slot (lane k holds slot k)
-        const uint32_t sb = sbase[c];
-        const uint32_t bb = bbase[c];
-        uint32_t bid = bidbase[c];
-        const uint32_t ob = (lane < 6) ? obase[(size_t)c * 6 + lane] : 0u;
-        float ft = fT;
-        uint64_t sd = P.seed;
-        int32_t st = step;
-        int64_t nid = next_id;
-        if (BATCH) {
-            // birth ranks and IDs count within the run
-            const uint32_t rr = BB.crun[c];
-            const BatchRun &R = BB.runs[rr];
-            bid -= bidbase[R.cell0];
-            ft = (float)(step - R.step0);
-            sd = R.seed;
-            st = step - R.step0;
-            nid = BB.rnext[rr];
+        if (genetics) bulk_g2s(d, reinterpret_cast<const unsigned char *>(gslot) + off[5], by[5], &bar[b]);
+    };
+
+    // pieces of work: the warp's cells in turn (cells r, r + G, ...), each in
+    // parts of at most kStageRows rows.  The piece being written (cur) and the
+    // one being copied (nxt); the bounds of the cell after nxt's are loaded ahead.
+    uint32_t r = blockIdx.x * kCellWarps + (uint32_t)warp;
+    uint32_t cs = 0, cn = 0;           // cur: cell start row and rows
+    int coff = 0;                      // cur: first row of the piece within the cell
+    uint32_t ns_ = 0, nn_ = 0;         // bounds of the cell r + G
+    if (r < nne) {
+        cs = ne_start[r];
+        cn = ne_start[r + 1] - cs;
+        if (r + G < nne) {
+            ns_ = ne_start[r + G];
+            nn_ = ne_start[r + G + 1] - ns_;
         }
-        // the class counts are consumed: clear them for the next step
-        if (lane < 2) reinterpret_cast<uint4 *>(clsc + (size_t)c * kCls)[lane] = make_uint4(0u, 0u, 0u, 0u);
-        // the rows of the cell in groups of kGroup chunks of 32: the loads of a
-        // group are issued together, then its chunks are written out
-        constexpr int kGroup = 4;
-        for (int b0 = 0; b0 < n; b0 += 32 * kGroup) {
-            uint32_t codes[kGroup];
-            int64_t xs[kGroup];
-            float fbs[kGroup], fas[kGroup], fls[kGroup];
-            int32_t gss[kGroup];
-#pragma unroll
-            for (int q = 0; q < kGroup; q++) {
-                const int row = b0 + q * 32 + lane;
-                codes[q] = 0u;
-                xs[q] = 0;
-                fbs[q] = fas[q] = fls[q] = 0.0f;
-                gss[q] = 0;
-                if (row < n) {
-                    const uint32_t g = s + (uint32_t)row;
-                    codes[q] = outc[g];
-                    xs[q] = id[g];
-                    fbs[q] = birth[g];
-                    if (!P.age_from_birth) fas[q] = age[g];
-                    fls[q] = lastb[g];
-                    if (genetics) gss[q] = gslot[g];
+        issue(0, cs, min(cn, (uint32_t)kStageRows));
+    }
+    int buf = 0;
+    bool failed = false;
+    // cell data of cur's cell, loaded when its first piece starts
+    uint32_t c = 0, sb = 0, bb = 0, bid = 0, ob = 0;
+    float ft = fT;
+    uint64_t sd = P.seed;
+    int32_t st = step;
+    int64_t nid = next_id;
+    while (r < nne) {
+        // the next piece: the rest of this cell, or the next cell's first part
+        uint32_t xr = r;
+        int xoff = coff + kStageRows;
+        uint32_t xs = cs, xn = cn;
+        if ((uint32_t)xoff >= cn) {
+            xr = r + G;
+            xoff = 0;
+            xs = ns_;
+            xn = nn_;
+        }
+        if (xr < nne) issue(buf ^ 1, xs + (uint32_t)xoff, min(xn - (uint32_t)xoff, (uint32_t)kStageRows));
+        if (coff == 0) {
+            // the cell's bases in the next table: stayers, newborns (and their
+            // birth numbers), movers per neighbour slot (lane k holds slot k)
+            c = nonempty[r];
+            sb = sbase[c];
+            bb = bbase[c];
+            bid = bidbase[c];
+            ob = (lane < 6) ? obase[(size_t)c * 6 + lane] : 0u;
+            if (BATCH) {
+                // birth ranks and IDs count within the run
+                const uint32_t rr = BB.crun[c];
+                const BatchRun &R = BB.runs[rr];
+                bid -= bidbase[R.cell0];
+                ft = (float)(step - R.step0);
+                sd = R.seed;
+                st = step - R.step0;
+                nid = BB.rnext[rr];
+            }
+            // the class counts are consumed: clear them for the next step
+            if (lane < 2) reinterpret_cast<uint4 *>(clsc + (size_t)c * kCls)[lane] = make_uint4(0u, 0u, 0u, 0u);
+        }
+        // the rows of the piece, staged
+        if (!mbar_wait_bounded(&bar[buf], (parity >> buf) & 1u)) {
+            if (lane == 0) set_error(rs, kErrTimeout, 0x5ca7u);
+            failed = true;
+            break;
+        }
+        parity ^= 1u << buf;
+        inflight &= ~(1u << buf);
+        const unsigned char *sp = stage0 + (size_t)buf * sbytes;
+        const uint32_t g0 = cs + (uint32_t)coff;
+        const int pn = min((int)cn - coff, kStageRows);
+        const uint32_t h4 = (g0 & 3u) * 4u, h8 = (g0 & 1u) * 8u;   // heads of 4- and 8-byte columns
+        const uint32_t *s_outc = reinterpret_cast<const uint32_t *>(sp + h4);
+        const int64_t *s_id = reinterpret_cast<const int64_t *>(sp + stage_col_bytes(4) + h8);
+        const float *s_birth = reinterpret_cast<const float *>(sp + stage_col_bytes(4) + stage_col_bytes(8) + h4);
+        const float *s_lastb =
+            reinterpret_cast<const float *>(sp + 2u * stage_col_bytes(4) + stage_col_bytes(8) + h4);
+        const float *s_age = reinterpret_cast<const float *>(sp + 3u * stage_col_bytes(4) + stage_col_bytes(8) + h4);
+        const int32_t *s_gslot = reinterpret_cast<const int32_t *>(
+            sp + (3u + (age_col ? 1u : 0u)) * stage_col_bytes(4) + stage_col_bytes(8) + h4);
+        for (int b = 0; b < pn; b += 32) {
+            const int i = b + lane;
+            const bool valid = i < pn;
+            const uint32_t g = g0 + (uint32_t)i;
+            uint32_t code = 0u;
+            int64_t x = 0;
+            float fb = 0.0f, fa = 0.0f, fl = 0.0f;
+            int32_t gs = 0;
+            if (valid) {
+                code = s_outc[i];
+                x = s_id[i];
+                fb = s_birth[i];
+                if (age_col) fa = s_age[i];
+                fl = s_lastb[i];
+                if (genetics) gs = s_gslot[i];
+            }
+            const int k = code & 7;
+            const uint32_t obk = __shfl_sync(FULL_MASK, ob, k >= 2 ? k - 2 : 0);
+            if (genetics && __any_sync(FULL_MASK, valid && k == 0)) {
+                // the genome slot of an agent dying this step goes to the next free list
+                const uint32_t q = warp_agg_add(valid && k == 0, 0u, &rs->dead_count, 1u);
+                if (valid && k == 0) {
+                    if (carry + q < P.genome_capacity) freelist2[carry + q] = (uint32_t)gs;
+                    else set_error(rs, kErrInternal, 5u);
                 }
             }
-#pragma unroll
-            for (int q = 0; q < kGroup; q++) {
-                if (b0 + q * 32 >= n) break;   // the same for the whole warp
-                const int row = b0 + q * 32 + lane;
-                const bool valid = row < n;
-                const uint32_t g = s + (uint32_t)row;
-                const uint32_t code = codes[q];
-                const int64_t x = xs[q];
-                const float fb = fbs[q], fa = fas[q], fl = fls[q];
-                const int32_t gs = gss[q];
-                const int k = code & 7;
-                const uint32_t obk = __shfl_sync(FULL_MASK, ob, k >= 2 ? k - 2 : 0);
-                if (genetics && __any_sync(FULL_MASK, valid && k == 0)) {
-                    // the genome slot of an agent dying this step goes to the next free list
-                    const uint32_t q = warp_agg_add(valid && k == 0, 0u, &rs->dead_count, 1u);
-                    if (valid && k == 0) {
-                        if (carry + q < P.genome_capacity) freelist2[carry + q] = (uint32_t)gs;
-                        else set_error(rs, kErrInternal, 5u);
-                    }
+            // every survivor to its cell's class base + its rank in the class
+            if (valid && k > 0) {
+                const uint32_t dst = ((k == 1) ? sb : obk) + (code >> 17);
+                if (dst >= cap) {   // inconsistent bases: record, never write out of range
+                    set_error(rs, kErrInternal, 3u);
+                } else {
+                    id2[dst] = x;
+                    birth2[dst] = fb;
+                    lastb2[dst] = fl;
+                    age2[dst] = P.age_from_birth ? __fsub_rn(ft, fb) : fa;
+                    meta2[dst] = (uint8_t)(((code & kOutGender) ? kMetaGender : 0) |
+                                           ((code & kOutFertile) ? kMetaFertile : 0));
+                    if (genetics) gslot2[dst] = gs;
                 }
-                // every survivor to its cell's class base + its rank in the class
-                if (valid && k > 0) {
-                    const uint32_t dst = ((k == 1) ? sb : obk) + (code >> 17);
-                    if (dst >= cap) {   // inconsistent bases: record, never write out of range
-                        set_error(rs, kErrInternal, 3u);
-                    } else {
-                        id2[dst] = x;
-                        birth2[dst] = fb;
-                        lastb2[dst] = fl;
-                        age2[dst] = P.age_from_birth ? __fsub_rn(ft, fb) : fa;
-                        meta2[dst] = (uint8_t)(((code & kOutGender) ? kMetaGender : 0) |
-                                               ((code & kOutFertile) ? kMetaFertile : 0));
-                        if (genetics) gslot2[dst] = gs;
-                    }
-                }
-                // newborns (SPopulation::createAgentAtIndex, core/SPopulation.cpp:880-900):
-                // gender = (uchar)(2 * wrandd()) from the mother's birth stream,
-                // females start FERTILE
-                if (valid && (code & kOutBirth)) {
-                    const uint32_t rk = brank[g];
-                    const int32_t fr = father[g];
-                    const uint32_t dst = bb + rk;
-                    if (dst >= cap || fr < 0 || (uint32_t)fr >= N) {
-                        set_error(rs, kErrInternal, 4u);
-                    } else {
-                        const uint32_t u = run_block<BATCH>(P, sd, (uint32_t)st, x, kStreamBirth).v[0];
-                        const int64_t baby = nid + (int64_t)(bid + rk);
-                        id2[dst] = baby;
-                        birth2[dst] = ft;
-                        lastb2[dst] = 0.0f;
-                        age2[dst] = 0.0f;
-                        meta2[dst] = (uint8_t)((u >> 31) ? kMetaGender : kMetaFertile);
-                        if (genetics) {
-                            const uint32_t gr = bid + rk;   // birth rank of the step
-                            const uint32_t bs = gr < nfree ? freelist[gr] : hwm + (gr - nfree);
-                            if (bs >= P.genome_capacity) {
-                                set_error(rs, kErrCapacity, bs);
-                            } else {
-                                gslot2[dst] = (int32_t)bs;
-                                uint32_t *br = brec + (size_t)gr * 5;
-                                br[0] = (uint32_t)gs;
-                                br[1] = (uint32_t)gslot[fr];
-                                br[2] = bs;
-                                br[3] = (uint32_t)(uint64_t)x;
-                                br[4] = (uint32_t)((uint64_t)x >> 32);
-                            }
+            }
+            // newborns (SPopulation::createAgentAtIndex, core/SPopulation.cpp:880-900):
+            // gender = (uchar)(2 * wrandd()) from the mother's birth stream,
+            // females start FERTILE
+            if (valid && (code & kOutBirth)) {
+                const uint32_t rk = brank[g];
+                const int32_t fr = father[g];
+                const uint32_t dst = bb + rk;
+                if (dst >= cap || fr < 0 || (uint32_t)fr >= N) {
+                    set_error(rs, kErrInternal, 4u);
+                } else {
+                    const uint32_t u = run_block<BATCH>(P, sd, (uint32_t)st, x, kStreamBirth).v[0];
+                    const int64_t baby = nid + (int64_t)(bid + rk);
+                    id2[dst] = baby;
+                    birth2[dst] = ft;
+                    lastb2[dst] = 0.0f;
+                    age2[dst] = 0.0f;
+                    meta2[dst] = (uint8_t)((u >> 31) ? kMetaGender : kMetaFertile);
+                    if (genetics) {
+                        const uint32_t gr = bid + rk;   // birth rank of the step
+                        const uint32_t bs = gr < nfree ? freelist[gr] : hwm + (gr - nfree);
+                        if (bs >= P.genome_capacity) {
+                            set_error(rs, kErrCapacity, bs);
+                        } else {
+                            gslot2[dst] = (int32_t)bs;
+                            uint32_t *br = brec + (size_t)gr * 5;
+                            br[0] = (uint32_t)gs;
+                            br[1] = (uint32_t)gslot[fr];
+                            br[2] = bs;
+                            br[3] = (uint32_t)(uint64_t)x;
+                            br[4] = (uint32_t)((uint64_t)x >> 32);
                         }
-                        if (P.log_births) {
-                            const uint64_t li = blog_base + (uint64_t)(bid + rk);
-                            if (li < blog_cap) {
-                                blog[li * 3 + 0] = baby;
-                                blog[li * 3 + 1] = x;
-                                blog[li * 3 + 2] = id[fr];
-                            }
+                    }
+                    if (P.log_births) {
+                        const uint64_t li = blog_base + (uint64_t)(bid + rk);
+                        if (li < blog_cap) {
+                            blog[li * 3 + 0] = baby;
+                            blog[li * 3 + 1] = x;
+                            blog[li * 3 + 2] = id[fr];
                         }
                     }
                 }
             }
+        }
+        __syncwarp();   // the buffer is read out before it is copied into again
+        // advance: the next piece becomes the current one
+        if (xr != r) {
+            cs = ns_;
+            cn = nn_;
+            if (xr + G < nne) {
+                ns_ = ne_start[xr + G];
+                nn_ = ne_start[xr + G + 1] - ns_;
+            }
+        }
+        r = xr;
+        coff = xoff;
+        buf ^= 1;
+    }
+    if (failed) {
+        // copies still in flight land before the kernel ends (waits bounded again)
+        const uint32_t fl = __shfl_sync(FULL_MASK, inflight, 0);
+        for (int b = 0; b < 2; b++) {
+            if ((fl >> b) & 1u) mbar_wait_bounded(&bar[b], (parity >> b) & 1u);
         }
     }
     commit_step<BATCH, false>(P, BB, rs, &s_flag);
@@ -2466,6 +2622,12 @@ static void set_scatter_attr() {
                          (int)sizeof(qhg::ScatterSmemT<qhg::Tile<BIG>::kMax, qhg::Tile<BIG>::kThreads>));
 }
 
+template <bool BATCH>
+static void set_scatter_cell_attr() {
+    cudaFuncSetAttribute(qhg::k_scatter_cell<BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(2 * qhg::kCellWarps * qhg::scatter_stage_bytes(true, true)));
+}
+
 template <int PROG, bool BATCH>
 static void set_cell_attr() {
     cudaFuncSetAttribute(qhg::k_actions_cell<PROG, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -2479,6 +2641,7 @@ static void set_tile_attributes() {
     if (dev < 0 || dev >= 64 || done[dev]) return;
     set_cell_attr<0, false>(); set_cell_attr<1, false>(); set_cell_attr<2, false>(); set_cell_attr<3, false>();
     set_cell_attr<0, true>(); set_cell_attr<1, true>();
+    set_scatter_cell_attr<false>(); set_scatter_cell_attr<true>();
     set_actions_attr<0, false, false>(); set_actions_attr<1, false, false>();
     set_actions_attr<2, false, false>(); set_actions_attr<3, false, false>();
     set_actions_attr<0, true, false>(); set_actions_attr<1, true, false>();
@@ -2499,6 +2662,7 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
     if (batch) BB = *BBp;
     else memset(&BB, 0, sizeof(BB));
     constexpr size_t kSmC = sizeof(CellWarpSmem) * kCellWarps;
+    const size_t kSmSC = (size_t)2 * kCellWarps * scatter_stage_bytes(!P->age_from_birth, P->genome_words > 0);
     const size_t kSmA = batch ? sizeof(ActionsSmemT<Tile<false>::kMax, Tile<false>::kThreads, true>)
                               : sizeof(ActionsSmemT<Tile<false>::kMax, Tile<false>::kThreads, false>);
     constexpr size_t kSmS = sizeof(ScatterSmemT<Tile<false>::kMax, Tile<false>::kThreads>);
@@ -2549,7 +2713,7 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
         B->age2, B->lastb2, B->meta2, B->blog, B->blog_cap, B->gslot, B->gslot2, B->freelist,              \
         B->freelist2, B->brec)
 #define QHG_LAUNCH_SCATTER_CELL(BT)                                                                        \
-    k_scatter_cell<BT><<<L.scatter_grid, kCellThreads, 0, stream>>>(                                       \
+    k_scatter_cell<BT><<<L.scatter_grid, kCellThreads, kSmSC, stream>>>(                                   \
         *P, BB, rs, B->nonempty, B->ne_start, B->id, B->birth, B->age, B->lastb, B->outc, B->father,       \
         B->brank, B->sbase, B->bbase, B->bidbase, B->obase, B->clsc, B->id2, B->birth2, B->age2, B->lastb2, \
         B->meta2, B->blog, B->blog_cap, B->gslot, B->gslot2, B->freelist, B->freelist2, B->brec)
@@ -2601,7 +2765,8 @@ extern "C" void qhg_tile_ctas_per_sm(int *actions, int *scatter) {
         sizeof(qhg::ScatterSmemT<qhg::Tile<false>::kMax, qhg::Tile<false>::kThreads>));
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ac, qhg::k_actions_cell<0, false>, qhg::kCellThreads,
                                                   sizeof(qhg::CellWarpSmem) * qhg::kCellWarps);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bc, qhg::k_scatter_cell<false>, qhg::kCellThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bc, qhg::k_scatter_cell<false>, qhg::kCellThreads,
+                                                  2 * qhg::kCellWarps * qhg::scatter_stage_bytes(false, false));
     a = std::min(a, ac);
     b = std::min(b, bc);
     *actions = a > 0 ? a : 1;
