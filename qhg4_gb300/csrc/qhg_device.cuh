@@ -29,20 +29,22 @@ struct Tile {
 };
 // The kernels of a step, chosen from the table the step reads: cell-aligned
 // tiles of kTileAgents agents for tables of small cells, one warp per cell
-// for tables whose non-empty cells hold kDenseCell agents or more on
-// average, the big-cell tiles when some cell holds more than kMaxCell.
-// Results do not depend on the form.
+// for tables whose non-empty cells hold kDenseCell agents or more on average
+// and none more than kMaxCellWarp, the big-cell tiles when some cell holds
+// more than kMaxCell.  Results do not depend on the form.
 constexpr uint32_t kFormTile = 0u, kFormBig = 1u, kFormCell = 2u;
 constexpr uint32_t kDenseCell = 24u;
+constexpr int kMaxCellWarp = 256;        // agents per cell of the warp-per-cell kernels
 __host__ __device__ inline uint32_t step_form(uint32_t max_cell, uint32_t n_agents, uint32_t n_nonempty) {
     if (max_cell > (uint32_t)kMaxCell) return kFormBig;
+    if (max_cell > (uint32_t)kMaxCellWarp) return kFormTile;
     return ((uint64_t)n_agents >= (uint64_t)kDenseCell * n_nonempty) ? kFormCell : kFormTile;
 }
 // bytes every agent column is allocated beyond its rows: bulk copies read
 // whole 16-byte units around a row range
 constexpr size_t kColumnPad = 64;
 constexpr int kScanThreads = 256;
-constexpr int kScanItems = 2;            // cells per thread in the cell scan
+constexpr int kScanItems = 1;            // cells per thread in the cell scan
 constexpr int kScanTile = kScanThreads * kScanItems;
 constexpr int kStatsRing = 1024;
 constexpr int kBatchRing = 64;           // per-run statistics ring of a batch (steps)
@@ -157,7 +159,7 @@ struct RunState {
     uint32_t n_staged;       // batches: agents waiting to be placed by k_inject
     uint32_t form;           // kernels of the step (kFormTile, kFormBig, kFormCell)
     uint32_t form_next;      // the same for the table the step writes (set by its commit)
-    uint32_t max_cell;       // largest cell of the next table (cell scan)
+    uint32_t max_cell;       // largest cell of the next table when above kMaxCellWarp (cell scan)
     uint32_t stall_tile;     // tests of the bounded waits: tile + 1 whose scan status is withheld once
     // statistics ring: [step % kStatsRing][live, births, deaths, moves]
     unsigned long long stats[kStatsRing][4];

@@ -1136,9 +1136,9 @@ k_cell_scan(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             pre.ne += (nnew[j] > 0u) ? 1u : 0u;
         }
     }
-    // the next step runs the big-cell kernels when a cell exceeds kMaxCell
+    // the next step's form depends on cells above kMaxCellWarp (and kMaxCell)
     cmax = __reduce_max_sync(FULL_MASK, cmax);
-    if (lane == 0 && cmax > (uint32_t)kMaxCell) atomicMax(&rs->max_cell, cmax);
+    if (lane == 0 && cmax > (uint32_t)kMaxCellWarp) atomicMax(&rs->max_cell, cmax);
 }
 
 // ----------------------------------------------------------------- scatter
@@ -1491,16 +1491,16 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
 constexpr int kCellThreads = 256;
 constexpr int kCellWarps = kCellThreads / 32;
 
-// per-warp shared memory of k_actions_cell (a cell of up to kMaxCell agents)
+// per-warp shared memory of k_actions_cell (a cell of up to kMaxCellWarp agents)
 struct CellWarpSmem {
-    uint32_t fk[kMaxCell];       // FERTILE members: low words of their IDs (list order)
-    uint16_t frow[kMaxCell];     // ... their rows in the cell; females from 0 up, males from n-1 down
-    uint16_t sidx[kMaxCell];     // list positions in ID order: females [0, nF), males [n - nM, n)
-    int16_t mate[kMaxCell];      // mate's row of each row, -1 none
-    uint16_t pick[kMaxCell / 2]; // pick value of each member of the smaller side (ID order)
-    uint16_t st[kMaxCell];       // per row: state before the pairing (agent_state), then the outcome byte
-    uint32_t odie[kMaxCell / 32];  // OldAgeDeath decided in advance: bit per row, set = dies
-    uint32_t oinw[kMaxCell / 32];  // rows inside the OldAgeDeath age window, bit per row
+    uint32_t fk[kMaxCellWarp];       // FERTILE members: low words of their IDs (list order)
+    uint16_t frow[kMaxCellWarp];     // ... their rows in the cell; females from 0 up, males from n-1 down
+    uint16_t sidx[kMaxCellWarp];     // list positions in ID order: females [0, nF), males [n - nM, n)
+    int16_t mate[kMaxCellWarp];      // mate's row of each row, -1 none
+    uint16_t pick[kMaxCellWarp / 2]; // pick value of each member of the smaller side (ID order)
+    uint16_t st[kMaxCellWarp];       // per row: state before the pairing (agent_state), then the outcome byte
+    uint32_t odie[kMaxCellWarp / 32];  // OldAgeDeath decided in advance: bit per row, set = dies
+    uint32_t oinw[kMaxCellWarp / 32];  // rows inside the OldAgeDeath age window, bit per row
     uint32_t cnt[8];             // class counts: [0] stay, [1..6] movers per neighbour slot
     uint64_t wt[6];              // WeightedMove thresholds of the cell
 };
@@ -1592,7 +1592,7 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
         if (P.n_verhulst > 0) v = vthr[r];
         if (P.has_move) cm = necm[r];
         const uint64_t wl = (P.has_wmove && lane < 6) ? wthr[(size_t)c * 6 + lane] : 0ull;
-        if (n > kMaxCell) {   // cannot happen: such steps run the big-cell form
+        if (n > kMaxCellWarp) {   // cannot happen: such steps run a tile form
             if (lane == 0) set_error(rs, kErrCellTooLarge, c);
             continue;
         }
@@ -2651,6 +2651,29 @@ static void set_tile_attributes() {
     done[dev] = true;
 }
 
+// grids of the cell form: every SM filled with as many CTAs of each cell
+// kernel as fit (once per device)
+struct CellGrids {
+    int actions, scatter;
+};
+static CellGrids cell_grids() {
+    static CellGrids g[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) dev = 0;
+    if (g[dev].actions == 0) {
+        int nsm = 1, a = 0, b = 0;
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, qhg::k_actions_cell<2, false>, qhg::kCellThreads,
+                                                      sizeof(qhg::CellWarpSmem) * qhg::kCellWarps);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, qhg::k_scatter_cell<false>, qhg::kCellThreads,
+                                                      2 * qhg::kCellWarps * qhg::scatter_stage_bytes(true, true));
+        g[dev].actions = std::max(1, nsm) * std::max(1, a);
+        g[dev].scatter = std::max(1, nsm) * std::max(1, b);
+    }
+    return g[dev];
+}
+
 static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
                            const qhg::BatchBuffers *BBp, const qhg::LaunchShape &L, cudaStream_t stream,
                            cudaEvent_t *ev) {
@@ -2662,6 +2685,7 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
     if (batch) BB = *BBp;
     else memset(&BB, 0, sizeof(BB));
     constexpr size_t kSmC = sizeof(CellWarpSmem) * kCellWarps;
+    const CellGrids CG = cell_grids();
     const size_t kSmSC = (size_t)2 * kCellWarps * scatter_stage_bytes(!P->age_from_birth, P->genome_words > 0);
     const size_t kSmA = batch ? sizeof(ActionsSmemT<Tile<false>::kMax, Tile<false>::kThreads, true>)
                               : sizeof(ActionsSmemT<Tile<false>::kMax, Tile<false>::kThreads, false>);
@@ -2677,7 +2701,7 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
         *P, BB, rs, B->nonempty, B->ne_start, B->tile_first, B->id, B->birth, B->age, B->lastb, B->meta, \
         B->vthr, B->wthr, B->necm, B->outc, B->father, B->brank, B->clsc)
 #define QHG_LAUNCH_CELL(PR, BT)                                                                            \
-    k_actions_cell<PR, BT><<<L.actions_grid, kCellThreads, kSmC, stream>>>(                                \
+    k_actions_cell<PR, BT><<<CG.actions, kCellThreads, kSmC, stream>>>(                                    \
         *P, BB, rs, B->nonempty, B->ne_start, B->id, B->birth, B->age, B->lastb, B->meta, B->vthr, B->wthr, \
         B->necm, B->outc, B->father, B->brank, B->clsc)
     if (batch) {
@@ -2713,7 +2737,7 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
         B->age2, B->lastb2, B->meta2, B->blog, B->blog_cap, B->gslot, B->gslot2, B->freelist,              \
         B->freelist2, B->brec)
 #define QHG_LAUNCH_SCATTER_CELL(BT)                                                                        \
-    k_scatter_cell<BT><<<L.scatter_grid, kCellThreads, kSmSC, stream>>>(                                   \
+    k_scatter_cell<BT><<<CG.scatter, kCellThreads, kSmSC, stream>>>(                                       \
         *P, BB, rs, B->nonempty, B->ne_start, B->id, B->birth, B->age, B->lastb, B->outc, B->father,       \
         B->brank, B->sbase, B->bbase, B->bidbase, B->obase, B->clsc, B->id2, B->birth2, B->age2, B->lastb2, \
         B->meta2, B->blog, B->blog_cap, B->gslot, B->gslot2, B->freelist, B->freelist2, B->brec)
@@ -2753,9 +2777,9 @@ extern "C" int qhg_launch_step_timed(const qhg::StepConst *P, qhg::RunState *rs,
 }
 
 // CTAs of each tile kernel (normal form) that fit on one SM at once
-// (tile and cell forms share the launch shape: the smaller of the two)
+// (the launch shape of the tile form; the cell form sizes its grids itself)
 extern "C" void qhg_tile_ctas_per_sm(int *actions, int *scatter) {
-    int a = 0, b = 0, ac = 0, bc = 0;
+    int a = 0, b = 0;
     set_tile_attributes();
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         &a, qhg::k_actions<0, false, false>, qhg::kTileThreads,
@@ -2763,12 +2787,6 @@ extern "C" void qhg_tile_ctas_per_sm(int *actions, int *scatter) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         &b, qhg::k_scatter<false, false>, qhg::kTileThreads,
         sizeof(qhg::ScatterSmemT<qhg::Tile<false>::kMax, qhg::Tile<false>::kThreads>));
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ac, qhg::k_actions_cell<0, false>, qhg::kCellThreads,
-                                                  sizeof(qhg::CellWarpSmem) * qhg::kCellWarps);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bc, qhg::k_scatter_cell<false>, qhg::kCellThreads,
-                                                  2 * qhg::kCellWarps * qhg::scatter_stage_bytes(false, false));
-    a = std::min(a, ac);
-    b = std::min(b, bc);
     *actions = a > 0 ? a : 1;
     *scatter = b > 0 ? b : 1;
 }

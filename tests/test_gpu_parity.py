@@ -122,11 +122,13 @@ def test_ids_past_32_bits(gpu_lib):
     assert st[:, 1].sum() > 0
 
 
-def test_dense_cells_multi_warp_lists(gpu_lib):
+@pytest.mark.parametrize("K,N", [(200.0, 18000), (400.0, 25000)], ids=["cell_form", "tile_form"])
+def test_dense_cells_multi_warp_lists(gpu_lib, K, N):
     """Cells of a few hundred agents: FERTILE lists longer than a warp, more
-    than 32 picks per cell."""
-    grid = uniform_grid(3, 400.0)
-    agents = make_agents(grid, 25000, seed=8, age_max=50.0)
-    o, g, st = run_both(grid, agents, config1_actions(K=400.0), 20, 21)
+    than 32 picks per cell (warp-per-cell form up to 256 agents per cell,
+    tile form above)."""
+    grid = uniform_grid(3, K)
+    agents = make_agents(grid, N, seed=8, age_max=50.0)
+    o, g, st = run_both(grid, agents, config1_actions(K=K), 20, 21)
     assert_same(o, g, st, 20)
     assert 64 < o.counts().max() <= 512
