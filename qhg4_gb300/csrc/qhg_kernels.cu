@@ -1931,14 +1931,17 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t by
     asm volatile("mbarrier.arrive.expect_tx.shared.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
 
+// one test of the phase, the thread suspended in hardware for up to about
+// kStageSuspendNs while the phase is incomplete
+constexpr uint32_t kStageSuspendNs = 20000u;
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(kStageSuspendNs)
         : "memory");
     return ok != 0u;
 }
