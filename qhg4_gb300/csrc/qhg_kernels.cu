@@ -1491,51 +1491,25 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
 constexpr int kCellThreads = 256;
 constexpr int kCellWarps = kCellThreads / 32;
 
-// per-warp shared memory of k_actions_cell (a cell of up to kMaxCellWarp agents)
+// per-warp shared memory of k_actions_cell: a group of up to kGroupCells
+// adjacent non-empty cells holding up to kMaxCellWarp agents together, rows
+// numbered within the group
+constexpr int kGroupCells = 2;
 struct CellWarpSmem {
-    uint32_t fk[kMaxCellWarp];       // FERTILE members: low words of their IDs (list order)
-    uint16_t frow[kMaxCellWarp];     // ... their rows in the cell; females from 0 up, males from n-1 down
-    uint16_t sidx[kMaxCellWarp];     // list positions in ID order: females [0, nF), males [n - nM, n)
+    uint32_t fk[kMaxCellWarp];       // FERTILE members: low words of their IDs, in each cell's rows
+                                     // (females from the cell's first row up, males from its last row down)
+    uint16_t frow[kMaxCellWarp];     // ... their rows
+    uint16_t sidx[kMaxCellWarp];     // list positions in ID order, in the same places as the lists
     int16_t mate[kMaxCellWarp];      // mate's row of each row, -1 none
-    uint16_t pick[kMaxCellWarp / 2]; // pick value of each member of the smaller side (ID order)
+    uint16_t pick[kMaxCellWarp];     // pick values of a cell's smaller side (ID order), from the cell's first row
     uint16_t st[kMaxCellWarp];       // per row: state before the pairing (agent_state), then the outcome byte
     uint32_t odie[kMaxCellWarp / 32];  // OldAgeDeath decided in advance: bit per row, set = dies
     uint32_t oinw[kMaxCellWarp / 32];  // rows inside the OldAgeDeath age window, bit per row
-    uint32_t cnt[8];             // class counts: [0] stay, [1..6] movers per neighbour slot
-    uint64_t wt[6];              // WeightedMove thresholds of the cell
+    uint32_t cnt[kGroupCells][8];    // class counts: [0] stay, [1..6] movers per neighbour slot
+    uint64_t wt[kGroupCells][6];     // WeightedMove thresholds of each cell
+    CellView cv[kGroupCells];        // Verhulst thresholds and move word of each cell
+    uint32_t run[kGroupCells];       // batches: run of each cell
 };
-
-// ID ranks of the FERTILE list entries among their own sex: females are the
-// entries [0, nF), males [n - nM, n); entry k goes to sidx[region + rank].
-// One pass over both lists.  IDs are compared by their low words while all
-// high words are zero (wide == false), else in full (read from the table).
-__device__ __forceinline__ void rank_lists(CellWarpSmem &W, int n, int nF, int nM, bool wide,
-                                           const int64_t *__restrict__ id, uint32_t s) {
-    const int lane = threadIdx.x & 31;
-    for (int t0 = 0; t0 < nF + nM; t0 += 32) {
-        const int t = t0 + lane;
-        if (t < nF + nM) {
-            const bool male = t >= nF;
-            const int b = male ? n - nM : 0;
-            const int m = male ? nM : nF;
-            const int k = b + (male ? t - nF : t);
-            int r = 0;
-            if (!wide) {
-                const uint32_t x = W.fk[k];
-                int j = 0;
-                for (; j + 4 <= m; j += 4) {
-                    r += (W.fk[b + j] < x ? 1 : 0) + (W.fk[b + j + 1] < x ? 1 : 0) +
-                         (W.fk[b + j + 2] < x ? 1 : 0) + (W.fk[b + j + 3] < x ? 1 : 0);
-                }
-                for (; j < m; j++) r += (W.fk[b + j] < x) ? 1 : 0;
-            } else {
-                const int64_t x = id[s + W.frow[k]];
-                for (int j = 0; j < m; j++) r += (id[s + W.frow[b + j]] < x) ? 1 : 0;
-            }
-            W.sidx[b + r] = (uint16_t)k;
-        }
-    }
-}
 
 template <int PROG, bool BATCH>
 __global__ void __launch_bounds__(kCellThreads, 4)
@@ -1566,122 +1540,145 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
     const int32_t step = rs->step;
     const float fT = (float)step;
     const uint32_t nne = rs->n_nonempty;
-    const uint32_t G = gridDim.x * kCellWarps;
     uint32_t cnt_births = 0, cnt_deaths = 0, cnt_moves = 0;
-    // the bounds of the warp's next cell are loaded one cell ahead
-    uint32_t r = blockIdx.x * kCellWarps + (threadIdx.x >> 5);
-    uint32_t nb0 = 0, nb1 = 0;
-    if (r < nne) {
-        nb0 = ne_start[r];
-        nb1 = ne_start[r + 1];
+    // units of work: pairs of adjacent non-empty cells (2u, 2u + 1), taken by
+    // the warps in turn; their bounds are loaded one unit ahead
+    const uint32_t units = (nne + 1u) / 2u;
+    const uint32_t U = gridDim.x * kCellWarps;
+    uint32_t u = blockIdx.x * kCellWarps + (threadIdx.x >> 5);
+    uint32_t e0 = 0, e1 = 0, e2 = 0;
+    if (u < units) {
+        e0 = ne_start[2u * u];
+        e1 = ne_start[min(2u * u + 1u, nne)];
+        e2 = ne_start[min(2u * u + 2u, nne)];
     }
-    for (; r < nne; r += G) {
-        const uint32_t s = nb0;
-        const int n = (int)(nb1 - nb0);
-        const uint32_t rn = r + G;
-        if (rn < nne) {
-            nb0 = ne_start[rn];
-            nb1 = ne_start[rn + 1];
+    for (; u < units; u += U) {
+        const uint32_t b0 = e0, b1 = e1, b2 = e2;
+        const uint32_t un = u + U;
+        if (un < units) {
+            e0 = ne_start[2u * un];
+            e1 = ne_start[min(2u * un + 1u, nne)];
+            e2 = ne_start[min(2u * un + 2u, nne)];
         }
-        // the cell: index, Verhulst thresholds (LinearBirth / LinearDeath
-        // ::initialize, actions/LinearBirth.cpp:90-112, actions/LinearDeath.cpp:92-122,
-        // computed by the previous step's cell scan) and move word
-        const uint32_t c = nonempty[r];
-        ulonglong2 v = make_ulonglong2(0ull, 0ull);
-        uint32_t cm = 0u;
-        if (P.n_verhulst > 0) v = vthr[r];
-        if (P.has_move) cm = necm[r];
-        const uint64_t wl = (P.has_wmove && lane < 6) ? wthr[(size_t)c * 6 + lane] : 0ull;
-        if (n > kMaxCellWarp) {   // cannot happen: such steps run a tile form
-            if (lane == 0) set_error(rs, kErrCellTooLarge, c);
-            continue;
-        }
-        const BatchRun *R = BATCH ? BB.runs + BB.crun[c] : nullptr;
-        const bool keep = !BATCH || R->active;   // a run that leaves the batch drops its agents
-        const uint64_t sd = BATCH ? R->seed : P.seed;
-        const int32_t stR = BATCH ? step - R->step0 : step;
-        const float fTR = BATCH ? (float)stR : fT;
-        CellView cv;
-        cv.tk = (uint32_t)(v.x >> 62);
-        cv.tb = v.x & ((1ull << 62) - 1ull);
-        cv.td = v.y;
-        cv.nn = cm & 7u;
-        cv.vm = (cm >> 8) & 63u;
-        cv.wf = (cm >> 16) & 1u;
-        cv.c = 0u;   // the WeightedMove thresholds of this cell are W.wt
-        if (lane < 6) W.wt[lane] = wl;
-        __syncwarp();
-        // ---- RandomPair::findMates (actions/RandomPair.cpp:146-270): FERTILE
-        // lists, ranked by ID; the members of the smaller side pick, in ID
-        // order, each pick drawn from the pairing stream of the picking member.
-        // With an early OldAgeDeath, the agents inside its age window are
-        // marked.
-        int nF = 0, nM = 0, nq = 0;
-        bool wide = false;
-        if (keep && (kOnePass || P.has_pair || kEarlyOad)) {
-            // groups of kGroupA chunks of 32 rows: a group's loads are issued
-            // together (one chunk: larger groups cost registers that the later
-            // passes need)
-            constexpr int kGroupA = 1;
-            for (int b0 = 0; b0 < n; b0 += 32 * kGroupA) {
-                uint8_t m8s[kGroupA];
-                int64_t xs[kGroupA];
-                float fbs[kGroupA], fas[kGroupA], fls[kGroupA];
-#pragma unroll
-                for (int q = 0; q < kGroupA; q++) {
-                    const int row = b0 + q * 32 + lane;
-                    m8s[q] = 0;
-                    xs[q] = 0;
-                    fbs[q] = fas[q] = fls[q] = 0.0f;
-                    if (row < n) {
-                        const uint32_t g = s + (uint32_t)row;
-                        if (kOnePass || P.has_pair) {
-                            m8s[q] = meta[g];
-                            xs[q] = id[g];
-                        }
-                        if (kOnePass || kEarlyOad) fbs[q] = birth[g];
-                        if (kOnePass) {
-                            if (P.reads_age) fas[q] = age[g];
-                            fls[q] = lastb[g];
-                        }
+        const int ncu = (2u * u + 1u < nne) ? 2 : 1;   // cells of the unit
+        // both cells in one group when their rows fit, else one after the other
+        const bool together = ncu == 2 && (b2 - b0) <= (uint32_t)kMaxCellWarp;
+        const int ngroups = together ? 1 : ncu;
+        for (int gi = 0; gi < ngroups; gi++) {
+            const int nc = together ? 2 : 1;                 // cells of the group
+            const uint32_t r0 = 2u * u + (uint32_t)gi;       // its first cell's slot in the non-empty list
+            const uint32_t s = (gi == 0) ? b0 : b1;          // its first row
+            const int n = (int)(((together || ncu == 1 || gi == 1) ? b2 : b1) - s);
+            const int cs1 = (nc == 2) ? (int)(b1 - b0) : n;  // first row of the second cell
+            if (n > kMaxCellWarp) {   // cannot happen: such steps run a tile form
+                if (lane == 0) set_error(rs, kErrCellTooLarge, r0);
+                continue;
+            }
+            // ---- the cells: index, Verhulst thresholds (LinearBirth / LinearDeath
+            // ::initialize, actions/LinearBirth.cpp:90-112, actions/LinearDeath.cpp:92-122,
+            // computed by the previous step's cell scan), move word, WeightedMove
+            // thresholds (lane 8 lc + q holds slot q of cell lc)
+            {
+                const int lc = lane >> 3, q = lane & 7;
+                if (lc < nc) {
+                    const uint32_t c = nonempty[r0 + (uint32_t)lc];
+                    if (P.has_wmove && q < 6) W.wt[lc][q] = wthr[(size_t)c * 6 + q];
+                    if (q == 6) {
+                        ulonglong2 v = make_ulonglong2(0ull, 0ull);
+                        uint32_t cm = 0u;
+                        if (P.n_verhulst > 0) v = vthr[r0 + (uint32_t)lc];
+                        if (P.has_move) cm = necm[r0 + (uint32_t)lc];
+                        CellView cv;
+                        cv.tk = (uint32_t)(v.x >> 62);
+                        cv.tb = v.x & ((1ull << 62) - 1ull);
+                        cv.td = v.y;
+                        cv.nn = cm & 7u;
+                        cv.vm = (cm >> 8) & 63u;
+                        cv.wf = (cm >> 16) & 1u;
+                        cv.c = c;
+                        W.cv[lc] = cv;
+                        if (BATCH) W.run[lc] = BB.crun[c];
+                    }
+                    if (q == 7) {
+                        W.cnt[lc][0] = W.cnt[lc][1] = W.cnt[lc][2] = W.cnt[lc][3] = 0u;
+                        W.cnt[lc][4] = W.cnt[lc][5] = W.cnt[lc][6] = W.cnt[lc][7] = 0u;
                     }
                 }
-#pragma unroll
-                for (int q = 0; q < kGroupA; q++) {
-                    const int b = b0 + q * 32;
-                    if (b >= n) break;   // the same for the whole warp
+            }
+            __syncwarp();
+            // a run that leaves the batch drops its agents (they take no part in pairing)
+            bool keep0 = true, keep1 = true;
+            if (BATCH) {
+                keep0 = BB.runs[W.run[0]].active != 0u;
+                keep1 = nc == 2 && BB.runs[W.run[nc == 2 ? 1 : 0]].active != 0u;
+            }
+            // ---- RandomPair::findMates (actions/RandomPair.cpp:146-270): FERTILE
+            // lists of each cell, ranked by ID; the members of the smaller side
+            // pick, in ID order, each pick drawn from the pairing stream of the
+            // picking member.  With an early OldAgeDeath, the agents inside its
+            // age window are marked.
+            int nF0 = 0, nM0 = 0, nF1 = 0, nM1 = 0, nq = 0;
+            bool wide = false;
+            if (kOnePass || P.has_pair || kEarlyOad) {
+                for (int b = 0; b < n; b += 32) {
                     const int row = b + lane;
                     const bool valid = row < n;
-                    const bool fert = P.has_pair && (m8s[q] & kMetaFertile) != 0;
-                    const bool male = (m8s[q] & kMetaGender) != 0;
-                    const int64_t x = fert ? xs[q] : 0;
+                    const int lc = row >= cs1 ? 1 : 0;
+                    const bool kp = valid && (lc ? keep1 : keep0);
+                    uint8_t m8 = 0;
+                    int64_t xid = 0;
+                    float fb = 0.0f, fa = 0.0f, fl = 0.0f;
+                    if (kp) {
+                        const uint32_t g = s + (uint32_t)row;
+                        if (kOnePass || P.has_pair) {
+                            m8 = meta[g];
+                            xid = id[g];
+                        }
+                        if (kOnePass || kEarlyOad) fb = birth[g];
+                        if (kOnePass) {
+                            if (P.reads_age) fa = age[g];
+                            fl = lastb[g];
+                        }
+                    }
+                    const bool fert = P.has_pair && (m8 & kMetaFertile) != 0;
+                    const bool male = (m8 & kMetaGender) != 0;
+                    const int64_t x = fert ? xid : 0;
                     uint32_t stt = 0u;
-                    if (kOnePass && valid) {
-                        stt = agent_state<PROG, BATCH>(P, R, step, fT, xs[q], m8s[q], fbs[q], fas[q], fls[q], cv, W.wt);
+                    if (kOnePass && kp) {
+                        const BatchRun *R = BATCH ? BB.runs + W.run[lc] : nullptr;
+                        stt = agent_state<PROG, BATCH>(P, R, step, fT, xid, m8, fb, fa, fl, W.cv[lc], W.wt[lc]);
                         W.st[row] = (uint16_t)stt;
                     }
                     if (P.has_pair && valid) W.mate[row] = -1;
-                    const uint32_t fm = __ballot_sync(FULL_MASK, fert && !male);
-                    const uint32_t mm = __ballot_sync(FULL_MASK, fert && male);
+                    const uint32_t f0 = __ballot_sync(FULL_MASK, fert && !male && lc == 0);
+                    const uint32_t f1 = __ballot_sync(FULL_MASK, fert && !male && lc == 1);
+                    const uint32_t m0 = __ballot_sync(FULL_MASK, fert && male && lc == 0);
+                    const uint32_t m1 = __ballot_sync(FULL_MASK, fert && male && lc == 1);
                     if (fert) {
-                        const int pos = male ? n - 1 - (nM + __popc(mm & lt)) : nF + __popc(fm & lt);
+                        int pos;
+                        if (lc == 0) pos = male ? cs1 - 1 - (nM0 + __popc(m0 & lt)) : nF0 + __popc(f0 & lt);
+                        else pos = male ? n - 1 - (nM1 + __popc(m1 & lt)) : cs1 + nF1 + __popc(f1 & lt);
                         W.fk[pos] = (uint32_t)(uint64_t)x;
                         W.frow[pos] = (uint16_t)row;
                     }
                     wide |= __any_sync(FULL_MASK, ((uint64_t)x >> 32) != 0ull);
-                    nF += __popc(fm);
-                    nM += __popc(mm);
+                    nF0 += __popc(f0);
+                    nF1 += __popc(f1);
+                    nM0 += __popc(m0);
+                    nM1 += __popc(m1);
                     if (kEarlyOad) {
-                        const ActionConst &A = BATCH ? R->act[kOad] : P.act[kOad];
                         bool inw = false;
-                        if (valid) {
+                        if (kp) {
                             if (kOnePass) {
                                 // inside the window and alive after Verhulst in some case
                                 const bool may_live = !(stt & kStDeadU) || ((stt & kStMateDep) && !(stt & kStDeadM));
                                 inw = ((stt >> kStOad) & 3u) == 2u && may_live;
                             } else {
-                                const float fa = __fsub_rn(fTR, fbs[q]);
-                                inw = !(fa <= A.age_lo) && !(fa > A.age_hi);
+                                const BatchRun *R = BATCH ? BB.runs + W.run[lc] : nullptr;
+                                const ActionConst &A = BATCH ? R->act[kOad] : P.act[kOad];
+                                const float fTR = BATCH ? (float)(step - R->step0) : fT;
+                                const float fa2 = __fsub_rn(fTR, fb);
+                                inw = !(fa2 <= A.age_lo) && !(fa2 > A.age_hi);
                             }
                         }
                         const uint32_t qm = __ballot_sync(FULL_MASK, inw);
@@ -1692,131 +1689,143 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                         }
                     }
                 }
+                __syncwarp();
             }
-            __syncwarp();
-        }
-        const bool pairs = nF > 0 && nM > 0;
-        if (pairs) {
-            rank_lists(W, n, nF, nM, wide, id, s);
-            __syncwarp();
-        }
-        const bool femSmall = nF <= nM;
-        const int m = pairs ? (femSmall ? nF : nM) : 0;
-        const uint32_t nL = (uint32_t)(femSmall ? nM : nF);
-        const int sb = femSmall ? 0 : n - nM;   // smaller side in sidx
-        const int lb = femSmall ? n - nM : 0;   // larger side
-        // ---- one dense pass of draws: pick j (j < m) takes the pick[j]-th
-        // still unpaired member of the larger side, pick[j] = (int)wrandr(0,
-        // nL - j); then the OldAgeDeath draws of the agents in its window:
-        // age > M + wrandr(1 - U*M, 1 + U*M) (actions/OldAgeDeath.cpp:57-60)
-        for (int t0 = 0; t0 < m + nq; t0 += 32) {
-            const int t = t0 + lane;
-            if (t < m + nq) {
-                // one Philox block per lane, from the picking member's pairing
-                // stream or the old agent's action stream
-                int64_t x;
-                uint32_t blk, wd = 0u;
-                int row = 0;
-                if (t < m) {
-                    const int pos = W.sidx[sb + t];
-                    x = wide ? id[s + W.frow[pos]] : (int64_t)W.fk[pos];
-                    blk = kStreamPair;
-                } else {
-                    // the (t - m)-th marked row: find its chunk, then its bit
-                    int k = t - m, ch = 0;
-                    uint32_t cmsk = W.oinw[0];
-                    while (k >= __popc(cmsk)) {
-                        k -= __popc(cmsk);
-                        cmsk = W.oinw[++ch];
+            // per cell: the list regions, the smaller (picking) side and the larger one
+            const bool pairs0 = nF0 > 0 && nM0 > 0, pairs1 = nF1 > 0 && nM1 > 0;
+            const bool fs0 = nF0 <= nM0, fs1 = nF1 <= nM1;
+            const int m0 = pairs0 ? (fs0 ? nF0 : nM0) : 0, m1 = pairs1 ? (fs1 ? nF1 : nM1) : 0;
+            const uint32_t nL0 = (uint32_t)(fs0 ? nM0 : nF0), nL1 = (uint32_t)(fs1 ? nM1 : nF1);
+            const int sb0 = fs0 ? 0 : cs1 - nM0, sb1 = fs1 ? cs1 : n - nM1;     // smaller side in sidx
+            const int lb0 = fs0 ? cs1 - nM0 : 0, lb1 = fs1 ? n - nM1 : cs1;     // larger side
+            // ---- ID ranks of every list entry within its own list, one pass over
+            // both cells: entry k goes to sidx[region + rank].  IDs are compared by
+            // their low words while all high words are zero, else in full.
+            const int nr0 = pairs0 ? nF0 + nM0 : 0;
+            const int nr = nr0 + (pairs1 ? nF1 + nM1 : 0);
+            for (int t0 = 0; t0 < nr; t0 += 32) {
+                const int t = t0 + lane;
+                if (t < nr) {
+                    const int lc = t >= nr0 ? 1 : 0;
+                    const int tt = t - (lc ? nr0 : 0);
+                    const int nFl = lc ? nF1 : nF0, nMl = lc ? nM1 : nM0;
+                    const bool male = tt >= nFl;
+                    const int bse = male ? (lc ? n : cs1) - nMl : (lc ? cs1 : 0);
+                    const int cnt = male ? nMl : nFl;
+                    const int k = bse + (male ? tt - nFl : tt);
+                    int r = 0;
+                    if (!wide) {
+                        const uint32_t x = W.fk[k];
+                        int j = 0;
+                        for (; j + 4 <= cnt; j += 4) {
+                            r += (W.fk[bse + j] < x ? 1 : 0) + (W.fk[bse + j + 1] < x ? 1 : 0) +
+                                 (W.fk[bse + j + 2] < x ? 1 : 0) + (W.fk[bse + j + 3] < x ? 1 : 0);
+                        }
+                        for (; j < cnt; j++) r += (W.fk[bse + j] < x) ? 1 : 0;
+                    } else {
+                        const int64_t x = id[s + W.frow[k]];
+                        for (int j = 0; j < cnt; j++) r += (id[s + W.frow[bse + j]] < x) ? 1 : 0;
                     }
-                    row = (ch << 5) + (int)__fns(cmsk, 0, k + 1);
-                    x = id[s + row];
-                    constexpr uint32_t w = prog_window(PROG, kOad > 0 ? kOad : 0);
-                    blk = kStreamActions + (w >> 2);
-                    wd = w & 3u;
-                }
-                const Draw4 d4 = run_block<BATCH>(P, sd, (uint32_t)stR, x, blk);
-                if (t < m) {
-                    W.pick[t] = (uint16_t)(((uint64_t)(nL - (uint32_t)t) * (uint64_t)d4.v[0]) >> 32);
-                } else if (kEarlyOad) {
-                    const ActionConst &A = BATCH ? R->act[kOad > 0 ? kOad : 0] : P.act[kOad > 0 ? kOad : 0];
-                    const float fa = __fsub_rn(fTR, birth[s + row]);
-                    const uint32_t u = pick4(d4, wd);
-                    const double th = __dmul_rn(__dmul_rn(A.oad_w, (double)u), 2.3283064365386962890625e-10);
-                    const double thr = __dadd_rn(A.oad_M, __dadd_rn(A.oad_a, th));
-                    if ((double)fa > thr) atomicOr(&W.odie[row >> 5], 1u << (row & 31));
+                    W.sidx[bse + r] = (uint16_t)k;
                 }
             }
-        }
-        __syncwarp();
-        if (pairs) {
-            // the member taken by pick j, decoded on its own: start from pick[j]
-            // and for i = j-1 down to 0 step over the member pick i took when it
-            // lies at or below (the lanes walk i down together)
-            for (int j0 = 0; j0 < m; j0 += 32) {
-                const int j = j0 + lane;
-                uint32_t p = (j < m) ? W.pick[j] : 0u;
-                const int top = min(m, j0 + 32) - 1;
-                for (int k = top - 1; k >= 0; k--) {
-                    const uint32_t pk = W.pick[k];
-                    if (k < j) p += (p >= pk) ? 1u : 0u;
+            __syncwarp();
+            // ---- one dense pass of draws: pick j of a cell (j < m) takes the
+            // pick[j]-th still unpaired member of its larger side, pick[j] =
+            // (int)wrandr(0, nL - j); then the OldAgeDeath draws of the agents in
+            // its window: age > M + wrandr(1 - U*M, 1 + U*M) (actions/OldAgeDeath.cpp:57-60)
+            const int np = m0 + m1;
+            for (int t0 = 0; t0 < np + nq; t0 += 32) {
+                const int t = t0 + lane;
+                if (t < np + nq) {
+                    // one Philox block per lane, from the picking member's pairing
+                    // stream or the old agent's action stream
+                    int64_t x;
+                    uint32_t blk, wd = 0u;
+                    int row = 0, lc, j = 0;
+                    if (t < np) {
+                        lc = t >= m0 ? 1 : 0;
+                        j = t - (lc ? m0 : 0);
+                        const int pos = W.sidx[(lc ? sb1 : sb0) + j];
+                        x = wide ? id[s + W.frow[pos]] : (int64_t)W.fk[pos];
+                        blk = kStreamPair;
+                    } else {
+                        // the (t - np)-th marked row: find its chunk, then its bit
+                        int k = t - np, ch = 0;
+                        uint32_t cmsk = W.oinw[0];
+                        while (k >= __popc(cmsk)) {
+                            k -= __popc(cmsk);
+                            cmsk = W.oinw[++ch];
+                        }
+                        row = (ch << 5) + (int)__fns(cmsk, 0, k + 1);
+                        lc = row >= cs1 ? 1 : 0;
+                        x = id[s + row];
+                        constexpr uint32_t w = prog_window(PROG, kOad > 0 ? kOad : 0);
+                        blk = kStreamActions + (w >> 2);
+                        wd = w & 3u;
+                    }
+                    const BatchRun *R = BATCH ? BB.runs + W.run[lc] : nullptr;
+                    const uint64_t sd = BATCH ? R->seed : P.seed;
+                    const int32_t stR = BATCH ? step - R->step0 : step;
+                    const Draw4 d4 = run_block<BATCH>(P, sd, (uint32_t)stR, x, blk);
+                    if (t < np) {
+                        W.pick[(lc ? cs1 : 0) + j] =
+                            (uint16_t)(((uint64_t)((lc ? nL1 : nL0) - (uint32_t)j) * (uint64_t)d4.v[0]) >> 32);
+                    } else if (kEarlyOad) {
+                        const ActionConst &A = BATCH ? R->act[kOad > 0 ? kOad : 0] : P.act[kOad > 0 ? kOad : 0];
+                        const float fa = __fsub_rn(BATCH ? (float)stR : fT, birth[s + row]);
+                        const uint32_t uu = pick4(d4, wd);
+                        const double th = __dmul_rn(__dmul_rn(A.oad_w, (double)uu), 2.3283064365386962890625e-10);
+                        const double thr = __dadd_rn(A.oad_M, __dadd_rn(A.oad_a, th));
+                        if ((double)fa > thr) atomicOr(&W.odie[row >> 5], 1u << (row & 31));
+                    }
                 }
-                if (j < m) {
-                    if (p >= nL) {   // cannot happen: every pick finds a free member
+            }
+            __syncwarp();
+            // ---- the member taken by pick j, decoded on its own: start from pick[j]
+            // and for i = j-1 down to 0 step over the member pick i took when it
+            // lies at or below (the lanes of a pass walk i down together)
+            for (int t0 = 0; t0 < np; t0 += 32) {
+                const int t = t0 + lane;
+                const bool act = t < np;
+                const int lc = (act && t >= m0) ? 1 : 0;
+                const int j = act ? t - (lc ? m0 : 0) : 0;
+                const uint16_t *pk = W.pick + (lc ? cs1 : 0);
+                uint32_t p = act ? pk[j] : 0u;
+                const int top = __reduce_max_sync(FULL_MASK, (uint32_t)j);
+                for (int k = top - 1; k >= 0; k--) {
+                    if (k < j) p += (p >= pk[k]) ? 1u : 0u;
+                }
+                if (act) {
+                    if (p >= (lc ? nL1 : nL0)) {   // cannot happen: every pick finds a free member
                         set_error(rs, kErrInternal, 1u);
                     } else {
-                        const int a = W.frow[W.sidx[sb + j]];
-                        const int b = W.frow[W.sidx[lb + (int)p]];
-                        W.mate[a] = (int16_t)b;
-                        W.mate[b] = (int16_t)a;
+                        const int a = W.frow[W.sidx[(lc ? sb1 : sb0) + j]];
+                        const int bb = W.frow[W.sidx[(lc ? lb1 : lb0) + (int)p]];
+                        W.mate[a] = (int16_t)bb;
+                        W.mate[bb] = (int16_t)a;
                     }
                 }
             }
             __syncwarp();
-        }
-        // ---- every agent's outcome (a specialised program: settled from its
-        // state and its mate; otherwise every action in execution order), then
-        // the outcome word with the agent's rank in its cell's class
-        if (lane < 8) W.cnt[lane] = 0u;
-        uint32_t births = 0, dead = 0, moved = 0;
-        __syncwarp();
-        // groups of kGroupD chunks of 32 rows (one chunk: see kGroupA)
-        constexpr int kGroupD = 1;
-        for (int b0 = 0; b0 < n; b0 += 32 * kGroupD) {
-            uint8_t m8s[kGroupD];
-            int64_t xs[kGroupD];
-            float fbs[kGroupD], fas[kGroupD], fls[kGroupD];
-#pragma unroll
-            for (int q = 0; q < kGroupD; q++) {
-                const int row = b0 + q * 32 + lane;
-                m8s[q] = 0;
-                xs[q] = 0;
-                fbs[q] = fas[q] = fls[q] = 0.0f;
-                if (!kOnePass && row < n) {
-                    const uint32_t g = s + (uint32_t)row;
-                    m8s[q] = meta[g];
-                    xs[q] = id[g];
-                    fbs[q] = birth[g];
-                    if (P.reads_age) fas[q] = age[g];
-                    fls[q] = lastb[g];
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < kGroupD; q++) {
-                const int b = b0 + q * 32;
-                if (b >= n) break;   // the same for the whole warp
+            // ---- every agent's outcome (a specialised program: settled from its
+            // state and its mate; otherwise every action in execution order), then
+            // the outcome word with the agent's rank in its cell's class
+            uint32_t births0 = 0, births1 = 0, dm0 = 0, dm1 = 0;
+            for (int b = 0; b < n; b += 32) {
                 const int row = b + lane;
                 const bool valid = row < n;
+                const int lc = row >= cs1 ? 1 : 0;
                 uint8_t oc = 0;
                 if (valid) {
                     const uint32_t g = s + (uint32_t)row;
-                    if (!keep) {
+                    if (!(lc ? keep1 : keep0)) {
                         oc = kOutDropped;
                     } else if (kOnePass) {
                         // LinearBirth / LinearDeath with or without a mate, the move
                         // and OldAgeDeath of an agent still alive
                         const uint32_t stt = W.st[row];
-                        const int mate = pairs ? W.mate[row] : -1;
+                        const int mate = P.has_pair ? W.mate[row] : -1;
                         const bool mated = (stt & kStMateDep) && mate >= 0;
                         const bool bflag = mated && (stt & kStBirthM);
                         bool alive = !(stt & (mated ? kStDeadM : kStDeadU));
@@ -1838,13 +1847,14 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                             cnt_births++;
                         }
                     } else {
-                        const int mate = pairs ? W.mate[row] : -1;
+                        const BatchRun *R = BATCH ? BB.runs + W.run[lc] : nullptr;
+                        const int mate = P.has_pair ? W.mate[row] : -1;
                         const bool odie = kEarlyOad && ((W.odie[b >> 5] >> lane) & 1u);
                         float fa;
                         bool queued = false;
                         oc = agent_outcome<PROG, BATCH, kEarlyOad ? kOadGiven : kOadDraw>(
-                            P, R, step, fT, xs[q], m8s[q], fbs[q], fas[q], fls[q], mate >= 0, cv, W.wt, odie, fa,
-                            queued, cnt_deaths, cnt_moves);
+                            P, R, step, fT, id[g], meta[g], birth[g], P.reads_age ? age[g] : 0.0f, lastb[g],
+                            mate >= 0, W.cv[lc], wthr, odie, fa, queued, cnt_deaths, cnt_moves);
                         if (oc & kOutBirth) {
                             father[g] = (int32_t)(s + (uint32_t)mate);
                             cnt_births++;
@@ -1855,41 +1865,56 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                 const int cls = oc & 7;
                 const bool counted = valid && cls > 0;
                 const uint32_t slot = counted ? (uint32_t)(cls - 1) : 0u;
-                const uint32_t peers = __match_any_sync(FULL_MASK, counted ? slot : 0xffu);
-                const uint32_t base = counted ? W.cnt[slot] : 0u;
+                const uint32_t peers = __match_any_sync(FULL_MASK, counted ? ((uint32_t)lc << 3) | slot : 0xffu);
+                const uint32_t base = counted ? W.cnt[lc][slot] : 0u;
                 __syncwarp();
-                if (counted && (peers & lt) == 0u) W.cnt[slot] = base + (uint32_t)__popc(peers);
+                if (counted && (peers & lt) == 0u) W.cnt[lc][slot] = base + (uint32_t)__popc(peers);
                 // outcome byte | rank in the cell's class << 17
                 if (valid) outc[s + (uint32_t)row] = (uint32_t)oc | ((base + (uint32_t)__popc(peers & lt)) << 17);
-                births += __popc(__ballot_sync(FULL_MASK, valid && (oc & kOutBirth)));
+                const bool bo = valid && (oc & kOutBirth);
+                births0 += __popc(__ballot_sync(FULL_MASK, bo && lc == 0));
+                births1 += __popc(__ballot_sync(FULL_MASK, bo && lc == 1));
                 if (BATCH) {
-                    dead += __popc(__ballot_sync(FULL_MASK, valid && cls == 0 && !(oc & kOutDropped)));
-                    moved += __popc(__ballot_sync(FULL_MASK, valid && (oc & kOutMoved)));
+                    const bool dd = valid && cls == 0 && !(oc & kOutDropped);
+                    const bool mv = valid && (oc & kOutMoved);
+                    dm0 += __popc(__ballot_sync(FULL_MASK, dd && lc == 0)) +
+                           ((uint32_t)__popc(__ballot_sync(FULL_MASK, mv && lc == 0)) << 16);
+                    dm1 += __popc(__ballot_sync(FULL_MASK, dd && lc == 1)) +
+                           ((uint32_t)__popc(__ballot_sync(FULL_MASK, mv && lc == 1)) << 16);
                 }
                 __syncwarp();
             }
-        }
-        // ---- mothers' birth ranks: births are numbered in (cell, mother ID)
-        // order; mothers are FERTILE females, walked in ID order
-        if (births > 0u) {
-            uint32_t run = 0;
-            for (int q0 = 0; q0 < nF; q0 += 32) {
-                const int q = q0 + lane;
-                bool mo = false;
-                int row = 0;
-                if (q < nF) {
-                    row = W.frow[W.sidx[q]];
-                    mo = (W.st[row] & kOutBirth) != 0;
+            // ---- mothers' birth ranks: births are numbered in (cell, mother ID)
+            // order; mothers are FERTILE females, walked in ID order
+#pragma unroll
+            for (int lc = 0; lc < 2; lc++) {
+                if ((lc ? births1 : births0) == 0u) continue;
+                const int nFl = lc ? nF1 : nF0, cs = lc ? cs1 : 0;
+                uint32_t run = 0;
+                for (int q0 = 0; q0 < nFl; q0 += 32) {
+                    const int q = q0 + lane;
+                    bool mo = false;
+                    int row = 0;
+                    if (q < nFl) {
+                        row = W.frow[W.sidx[cs + q]];
+                        mo = (W.st[row] & kOutBirth) != 0;
+                    }
+                    const uint32_t mb = __ballot_sync(FULL_MASK, mo);
+                    if (mo) brank[s + (uint32_t)row] = (uint16_t)(run + (uint32_t)__popc(mb & lt));
+                    run += (uint32_t)__popc(mb);
                 }
-                const uint32_t mb = __ballot_sync(FULL_MASK, mo);
-                if (mo) brank[s + (uint32_t)row] = (uint16_t)(run + (uint32_t)__popc(mb & lt));
-                run += (uint32_t)__popc(mb);
             }
+            // class counts of each cell: stay, movers per neighbour slot, births
+            {
+                const int lc = lane >> 3, q = lane & 7;
+                if (lc < nc) {
+                    const uint32_t c = W.cv[lc].c;
+                    clsc[(size_t)c * kCls + q] = (q < 7) ? W.cnt[lc][q] : (lc ? births1 : births0);
+                    if (BATCH && q == 0) BB.cstat[c] = lc ? dm1 : dm0;   // deaths | registered moves << 16
+                }
+            }
+            __syncwarp();
         }
-        // class counts of the cell: stay, movers per neighbour slot, births
-        if (lane < 8) clsc[(size_t)c * kCls + lane] = (lane < 7) ? W.cnt[lane] : births;
-        if (BATCH && lane == 0) BB.cstat[c] = dead | (moved << 16);   // deaths | registered moves << 16
-        __syncwarp();
     }
     // statistics of the step (batches: per run, by the cell scan)
     if (BATCH) return;
