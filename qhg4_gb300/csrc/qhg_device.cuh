@@ -44,8 +44,13 @@ __host__ __device__ inline uint32_t step_form(uint32_t max_cell, uint32_t n_agen
 // whole 16-byte units around a row range
 constexpr size_t kColumnPad = 64;
 constexpr int kScanThreads = 256;
-constexpr int kScanItems = 1;            // cells per thread in the cell scan
+// cells per thread in the cell scan: one for grids of up to kScanWideCells
+// cells, two above (fewer look-back steps pay off on the larger grids);
+// tile-status arrays are sized for one cell per thread
+constexpr int kScanItems = 1;
 constexpr int kScanTile = kScanThreads * kScanItems;
+constexpr int kScanWideCells = 4 << 20;
+__host__ __device__ inline int scan_items(int num_cells) { return num_cells > kScanWideCells ? 2 : 1; }
 constexpr int kStatsRing = 1024;
 constexpr int kBatchRing = 64;           // per-run statistics ring of a batch (steps)
 constexpr uint32_t kNoRun = 0xffffffffu; // run index of a batch cell that belongs to no run

@@ -900,7 +900,7 @@ __device__ __forceinline__ void batch_run_stats(uint32_t *rstat, uint32_t slot, 
     }
 }
 
-template <bool BATCH>
+template <bool BATCH, int ITEMS>
 __global__ void __launch_bounds__(kScanThreads)
 k_cell_scan(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             const int32_t *__restrict__ nbr, const uint8_t *__restrict__ nnbr,
@@ -917,7 +917,8 @@ k_cell_scan(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
     __shared__ ScanVal s_prefix;
     if (rs->error != 0u) return;
     const int C = P.num_cells;
-    const uint32_t ntiles = (uint32_t)((C + kScanTile - 1) / kScanTile);
+    constexpr int kTile = kScanThreads * ITEMS;
+    const uint32_t ntiles = (uint32_t)((C + kTile - 1) / kTile);
     const uint32_t epoch = ((uint32_t)rs->step + 1u) & 0x3fffffffu;
     if (threadIdx.x == 0) {
         const uint32_t t = atomicAdd(&rs->scan_tiles_started, 1u);
@@ -932,18 +933,18 @@ k_cell_scan(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
     if (tile >= ntiles) return;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    const int base = (int)tile * kScanTile + threadIdx.x * kScanItems;
+    const int base = (int)tile * kTile + threadIdx.x * ITEMS;
     // a test of the bounded waits withholds this tile's status once: its
     // successor's look-back runs out, the step fails with kErrTimeout
     const bool withhold = (rs->stall_tile == tile + 1u);
     if (withhold && threadIdx.x == 0) rs->stall_tile = 0u;
 
-    uint32_t nnew[kScanItems], stay[kScanItems], bth[kScanItems];
-    uint32_t crn[kScanItems];
+    uint32_t nnew[ITEMS], stay[ITEMS], bth[ITEMS];
+    uint32_t crn[ITEMS];
     uint32_t rsum_n = 0u, rsum_b = 0u, rsum_d = 0u, rsum_m = 0u, rcur = kNoRun;
     ScanVal loc = {0u, 0u, 0u};
 #pragma unroll
-    for (int j = 0; j < kScanItems; j++) {
+    for (int j = 0; j < ITEMS; j++) {
         const int d = base + j;
         nnew[j] = stay[j] = bth[j] = 0u;
         crn[j] = kNoRun;
@@ -1087,7 +1088,7 @@ k_cell_scan(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
         if (lane >= 1) pre = sv_add(pre, y);
     }
 #pragma unroll
-    for (int j = 0; j < kScanItems; j++) {
+    for (int j = 0; j < ITEMS; j++) {
         const int d = base + j;
         if (d < C) {
             sbase[d] = pre.n;
@@ -2611,16 +2612,23 @@ extern "C" int qhg_launch_upload(const qhg::StepConst *P, qhg::RunState *rs, con
                                  const float *sbirth, const float *sage, const float *slastb, int64_t n,
                                  int32_t *gslot_out, cudaStream_t stream) {
     using namespace qhg;
-    const int ntiles = (P->num_cells + kScanTile - 1) / kScanTile;
+    const int sitems = scan_items(P->num_cells);
+    const int ntiles = (P->num_cells + kScanThreads * sitems - 1) / (kScanThreads * sitems);
     const int64_t blk = std::min<int64_t>((n + 255) / 256, 65535);
     if (n > 0) {
         k_upload_count<<<(unsigned)blk, 256, 0, stream>>>(rs, cell, state, sid, n, P->num_cells, B->clsc);
     }
     BatchBuffers BB;
     memset(&BB, 0, sizeof(BB));
-    k_cell_scan<false><<<ntiles, kScanThreads, 0, stream>>>(
-        *P, BB, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr2, B->cmove, B->necm2, B->sbase, B->bbase, B->bidbase,
-        B->obase, B->nonempty2, B->ne_start2, B->tile_first2, B->tile_flag, B->tile_agg, B->tile_incl);
+    if (sitems == 2) {
+        k_cell_scan<false, 2><<<ntiles, kScanThreads, 0, stream>>>(
+            *P, BB, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr2, B->cmove, B->necm2, B->sbase, B->bbase,
+            B->bidbase, B->obase, B->nonempty2, B->ne_start2, B->tile_first2, B->tile_flag, B->tile_agg, B->tile_incl);
+    } else {
+        k_cell_scan<false, 1><<<ntiles, kScanThreads, 0, stream>>>(
+            *P, BB, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr2, B->cmove, B->necm2, B->sbase, B->bbase,
+            B->bidbase, B->obase, B->nonempty2, B->ne_start2, B->tile_first2, B->tile_flag, B->tile_agg, B->tile_incl);
+    }
     if (n > 0) {
         k_upload_place<<<(unsigned)blk, 256, 0, stream>>>(rs, cell, gender, state, sid, sbirth, sage, slastb, n,
                                                         P->capacity, B->sbase, B->clsc, B->id2, B->birth2,
@@ -2707,7 +2715,8 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
                            cudaEvent_t *ev) {
     using namespace qhg;
     set_tile_attributes();
-    const int ntiles = (P->num_cells + kScanTile - 1) / kScanTile;
+    const int sitems = scan_items(P->num_cells);
+    const int ntiles = (P->num_cells + kScanThreads * sitems - 1) / (kScanThreads * sitems);
     const bool batch = BBp != nullptr;
     BatchBuffers BB;
     if (batch) BB = *BBp;
@@ -2750,12 +2759,17 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
 #undef QHG_LAUNCH_CELL
 #undef QHG_LAUNCH_ACTIONS
     if (ev) cudaEventRecord(ev[1], stream);
-#define QHG_LAUNCH_SCAN(BT)                                                                                 \
-    k_cell_scan<BT><<<ntiles, kScanThreads, 0, stream>>>(                                                   \
+#define QHG_LAUNCH_SCAN(BT, IT)                                                                             \
+    k_cell_scan<BT, IT><<<ntiles, kScanThreads, 0, stream>>>(                                               \
         *P, BB, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr2, B->cmove, B->necm2, B->sbase, B->bbase, B->bidbase,       \
         B->obase, B->nonempty2, B->ne_start2, B->tile_first2, B->tile_flag, B->tile_agg, B->tile_incl)
-    if (batch) QHG_LAUNCH_SCAN(true);
-    else QHG_LAUNCH_SCAN(false);
+    if (batch) {
+        if (sitems == 2) QHG_LAUNCH_SCAN(true, 2);
+        else QHG_LAUNCH_SCAN(true, 1);
+    } else {
+        if (sitems == 2) QHG_LAUNCH_SCAN(false, 2);
+        else QHG_LAUNCH_SCAN(false, 1);
+    }
 #undef QHG_LAUNCH_SCAN
     if (ev) cudaEventRecord(ev[2], stream);
 #define QHG_LAUNCH_SCATTER(BT, BG, GRID, SM)                                                                \
