@@ -2,25 +2,33 @@
 //
 // Agents live in device memory as a structure of arrays sorted by cell.
 // The non-empty cells are listed in index order (nonempty[r]) together with
-// their first row (ne_start[r]).  One step is three kernels (plus the genome
-// kernel with genetics):
+// their first row (ne_start[r]).  One step is an action kernel, the cell
+// scan and a scatter (plus the genome kernel with genetics).  The action
+// kernel and the scatter come in three forms, chosen per step from the table
+// the step reads (step_form): warp-per-cell kernels for tables of dense
+// cells, cell-aligned tiles for tables of small cells, big-cell tiles when a
+// cell holds more than kMaxCell agents.  Every form is launched; the others
+// return at once.
 //
-//   k_actions   cell-aligned tiles of ~kTileAgents agents, one CTA at a time
-//               per tile, everything staged in shared memory.  Per cell
-//               (one thread each): the Verhulst thresholds.  Per cell, agent
-//               parallel: RandomPair (fertile members ranked by ID, picks
-//               drawn per picking member and decoded independently).  Per
-//               agent: every action in execution order, one outcome byte
-//               (dead / stays / moves to neighbour slot k, gives birth, new
-//               fertility), the father's row of each mother.  Per cell: the
-//               class counts and the mothers' birth ranks by ID.
-//   k_cell_scan one pass over all cells with a decoupled look-back scan:
-//               new per-cell counts (stayers + movers in + births), output
-//               bases of every (cell, class), birth numbering, and the next
-//               step's non-empty list with first rows.
-//   k_scatter   the same tiles: stable ranks per (cell, class), every
-//               survivor and newborn written to its row of the next table,
-//               the consumed class counts cleared.  The last CTA commits.
+//   k_actions_cell  one warp per pair of adjacent non-empty cells: the
+//                   agents' actions (for a specialised program before the
+//                   pairing, both outcomes kept where a mate decides them),
+//                   RandomPair (FERTILE members ranked by ID, picks drawn per
+//                   picking member and decoded independently), the outcome
+//                   word with each agent's rank in its cell's class, the
+//                   father's row of each mother, the mothers' birth ranks by
+//                   ID and the cells' class counts.
+//   k_actions       the same on cell-aligned tiles of ~kTileAgents agents,
+//                   one CTA per tile, everything staged in shared memory.
+//   k_cell_scan     one pass over all cells with a decoupled look-back scan:
+//                   new per-cell counts (stayers + movers in + births), output
+//                   bases of every (cell, class), birth numbering, the next
+//                   step's non-empty list with first rows, Verhulst
+//                   thresholds and move words.
+//   k_scatter_cell  one warp per cell, its rows staged in shared memory by
+//                   bulk copies: every survivor and newborn written to its
+//                   row of the next table, the consumed class counts
+//                   cleared.  The last CTA commits.  k_scatter: the tile forms.
 //
 // The reference runs these as SPopulation::initializeStep / doActions /
 // finalizeStep (core/SPopulation.cpp:394-577, 596-724, 1058-1092, 509-536).
@@ -1485,10 +1493,12 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
 }
 
 // ------------------------------------------------------ warp-per-cell kernels
-// The normal form of a step (no cell above kMaxCell agents): one warp works
-// on one non-empty cell at a time, with warp-level synchronisation only.
-// The warps of the grid take the cells of the non-empty list in turn
-// (warp g: cells g, g + G, g + 2G, ...; G the warps of the grid).
+// The cell form of a step (non-empty cells of kDenseCell agents or more on
+// average, none above kMaxCellWarp): each warp works on its own cells with
+// warp-level synchronisation only.  The action kernel takes pairs of
+// adjacent cells (2u, 2u + 1) as units, the scatter single cells; the warps
+// of the grid take the units in turn (warp g: g, g + G, ...; G the warps of
+// the grid).
 constexpr int kCellThreads = 256;
 constexpr int kCellWarps = kCellThreads / 32;
 
