@@ -113,3 +113,23 @@ def test_batch_with_a_dense_run(gpu_lib):
     b.step(12)
     for k, r in enumerate(ids):
         same_as_alone(b, r, cases[k], 11)
+
+
+def test_batch_dense_cells_cell_form(gpu_lib):
+    """Runs whose cells hold ~60 agents: the batch steps in the warp-per-cell
+    form with the specialised program; a run leaves and another joins."""
+    cases = []
+    for k in range(3):
+        g = uniform_grid(6 + k, 80.0)
+        acts = config1_actions(K=80.0, b0=0.3 + 0.1 * k)
+        cases.append((g, make_agents(g, 60 * g.num_cells, seed=400 + k, age_max=50.0), acts, 70 + k))
+    b = GpuBatch(config1_actions(K=80.0), agent_capacity=600_000, cell_capacity=6_000, max_runs=3)
+    ids = {k: b.add_run(g, acts, seed, a) for k, (g, a, acts, seed) in enumerate(cases[:2])}
+    b.step(6)
+    b.remove_run(ids[1])
+    b.step(2)
+    g, a, acts, seed = cases[2]
+    ids[2] = b.add_run(g, acts, seed, a)
+    b.step(8)
+    same_as_alone(b, ids[0], cases[0], 15)
+    same_as_alone(b, ids[2], cases[2], 7)
