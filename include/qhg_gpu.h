@@ -75,6 +75,7 @@ extern "C" {
 
 /* flags of qhg_run_desc */
 #define QHG_FLAG_LOG_BIRTHS   1u   /* keep a (baby, mother, father) ID log */
+#define QHG_FLAG_TRACK_OCCUPANCY 2u /* record when each cell is first occupied (qhg_gpu_occupancy) */
 
 typedef struct qhg_run qhg_run;
 
@@ -142,6 +143,13 @@ int qhg_gpu_download(qhg_run *run, qhg_agents_soa *out, int64_t cap, int64_t *n)
 int qhg_gpu_counts(qhg_run *run, uint32_t *cell_counts);
 /* statistics of the last `nsteps` steps (nsteps <= 1024) */
 int qhg_gpu_stats(qhg_run *run, int32_t nsteps, qhg_step_stats *out);
+/* Occupation history of the cells (QHG_FLAG_TRACK_OCCUPANCY): per cell the
+ * first step whose table holds an agent there (the uploaded table counts as
+ * its step), -1 if none yet; C entries.  Replaces OccTracker::updateCounts
+ * with OccHistory::addEntry (core/OccTracker.cpp, core/OccHistory.cpp) for
+ * one population: occupation masks that change to non-zero are recorded,
+ * masks of zero are ignored. */
+int qhg_gpu_occupancy(qhg_run *run, int32_t *first_step);
 /* birth log (QHG_FLAG_LOG_BIRTHS): rows (baby, mother, father) */
 int qhg_gpu_birth_log(qhg_run *run, int64_t *baby, int64_t *mother, int64_t *father, int64_t cap,
                       int64_t *n);

@@ -21,6 +21,8 @@ extern "C" int qhg_launch_step(const qhg::StepConst *P, qhg::RunState *rs, const
                                const qhg::BatchBuffers *BB, const qhg::LaunchShape *L, cudaStream_t stream);
 extern "C" void qhg_tile_ctas_per_sm(int *actions, int *scatter);
 extern "C" int qhg_match_program(const int32_t *types, int n);
+extern "C" int qhg_launch_occupancy(const qhg::RunState *rs, const uint32_t *nonempty, int32_t *occ, int grid,
+                                    cudaStream_t stream);
 extern "C" uint32_t qhg_program_window(int p, int a);
 extern "C" int qhg_launch_gather_genomes(const int32_t *gslot, const uint64_t *genome, uint32_t n, int words,
                                          uint32_t slots, uint64_t *out, cudaStream_t stream);
@@ -64,6 +66,7 @@ struct qhg_run {
     std::vector<double> h_K;
     uint64_t *d_wthr = nullptr;
     uint32_t *d_cmove = nullptr;
+    int32_t *d_occ = nullptr;       // first step of each cell's occupation (QHG_FLAG_TRACK_OCCUPANCY)
     std::vector<int32_t> h_nbr;
     // agents (ping-pong)
     uint32_t cap = 0;
@@ -465,10 +468,11 @@ extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_
         }
     }
     cudaFree(r->d_nbr); cudaFree(r->d_nnbr); cudaFree(r->d_rev); cudaFree(r->d_K); cudaFree(r->d_vthr[0]); cudaFree(r->d_vthr[1]);
-    cudaFree(r->d_wthr); cudaFree(r->d_cmove);
+    cudaFree(r->d_wthr); cudaFree(r->d_cmove); cudaFree(r->d_occ);
     cudaFree(r->d_clsc); cudaFree(r->d_sbase); cudaFree(r->d_bbase); cudaFree(r->d_bidb);
     cudaFree(r->d_obase); cudaFree(r->d_tflag); cudaFree(r->d_tagg); cudaFree(r->d_tincl);
     r->d_vthr[0] = r->d_vthr[1] = nullptr;
+    r->d_occ = nullptr;
     r->grid_ok = false;
     r->agents_ok = false;
     drop_graphs(r);
@@ -481,6 +485,10 @@ extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_
     CUDA_TRY(cudaMalloc(&r->d_vthr[1], (size_t)C * sizeof(ulonglong2)));
     CUDA_TRY(cudaMalloc(&r->d_wthr, (size_t)C * 6 * sizeof(uint64_t)));
     CUDA_TRY(cudaMalloc(&r->d_cmove, (size_t)C * sizeof(uint32_t)));
+    if (r->desc.flags & QHG_FLAG_TRACK_OCCUPANCY) {
+        CUDA_TRY(cudaMalloc(&r->d_occ, (size_t)C * sizeof(int32_t)));
+        CUDA_TRY(cudaMemsetAsync(r->d_occ, 0xff, (size_t)C * sizeof(int32_t), r->stream));
+    }
     CUDA_TRY(cudaMalloc(&r->d_clsc, (size_t)C * kCls * sizeof(uint32_t)));
     CUDA_TRY(cudaMalloc(&r->d_sbase, (size_t)C * sizeof(uint32_t)));
     CUDA_TRY(cudaMalloc(&r->d_bbase, (size_t)C * sizeof(uint32_t)));
@@ -635,6 +643,13 @@ extern "C" int qhg_gpu_upload_agents(qhg_run *r, const qhg_agents_soa *a, int64_
     CUDA_TRY(cudaMemcpyAsync(r->d_rs, h, sizeof(RunState), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemsetAsync(r->d_tflag, 0, (size_t)ntiles * sizeof(uint32_t), st));
     CUDA_TRY(cudaStreamSynchronize(st));
+    if (r->d_occ != nullptr) {
+        // the uploaded table's cells are occupied at its step
+        CUDA_TRY(cudaMemsetAsync(r->d_occ, 0xff, (size_t)C * sizeof(int32_t), st));
+        int le2 = qhg_launch_occupancy(r->d_rs, r->d_ne[0], r->d_occ, r->shape.scatter_grid, st);
+        if (le2 != 0) return fail(QHG_ERR_CUDA, std::string("occupancy: ") + cudaGetErrorString((cudaError_t)le2));
+        CUDA_TRY(cudaStreamSynchronize(st));
+    }
     r->cur = 0;
     r->upload_step = first_step;
     r->upload_max_id = maxid;
@@ -655,6 +670,7 @@ static StepBuffers make_buffers(qhg_run *r, int cur) {
     B.meta2 = r->d_meta[nx];
     B.nbr = r->d_nbr; B.nnbr = r->d_nnbr; B.rev = r->d_rev; B.K = r->d_K; B.vthr = r->d_vthr[cur]; B.vthr2 = r->d_vthr[nx]; B.wthr = r->d_wthr;
     B.cmove = r->d_cmove; B.necm = r->d_necm[cur]; B.necm2 = r->d_necm[nx];
+    B.occ = r->d_occ;
     B.outc = r->d_outc; B.father = r->d_father; B.brank = r->d_brank; B.clsc = r->d_clsc;
     B.sbase = r->d_sbase; B.bbase = r->d_bbase; B.bidbase = r->d_bidb; B.obase = r->d_obase;
     B.tile_flag = r->d_tflag; B.tile_agg = r->d_tagg; B.tile_incl = r->d_tincl;
@@ -857,6 +873,15 @@ extern "C" int qhg_gpu_counts(qhg_run *r, uint32_t *counts) {
     return QHG_OK;
 }
 
+extern "C" int qhg_gpu_occupancy(qhg_run *r, int32_t *first_step) {
+    if (r == nullptr || first_step == nullptr) return fail(QHG_ERR_ARG, "null argument");
+    if (r->d_occ == nullptr) return fail(QHG_ERR_STATE, "run was created without QHG_FLAG_TRACK_OCCUPANCY");
+    int rc = qhg_gpu_sync(r);
+    if (rc != QHG_OK) return rc;
+    CUDA_TRY(cudaMemcpy(first_step, r->d_occ, (size_t)r->C * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    return QHG_OK;
+}
+
 extern "C" int qhg_gpu_stats(qhg_run *r, int32_t nsteps, qhg_step_stats *out) {
     if (r == nullptr || out == nullptr || nsteps < 0 || nsteps > kStatsRing) return fail(QHG_ERR_ARG, "bad stats arguments");
     int rc = qhg_gpu_sync(r);
@@ -936,7 +961,7 @@ extern "C" int qhg_gpu_destroy(qhg_run *r) {
     drop_graphs(r);
     free_agents(r);
     cudaFree(r->d_nbr); cudaFree(r->d_nnbr); cudaFree(r->d_rev); cudaFree(r->d_K); cudaFree(r->d_vthr[0]); cudaFree(r->d_vthr[1]);
-    cudaFree(r->d_wthr); cudaFree(r->d_cmove);
+    cudaFree(r->d_wthr); cudaFree(r->d_cmove); cudaFree(r->d_occ);
     cudaFree(r->d_clsc); cudaFree(r->d_sbase); cudaFree(r->d_bbase); cudaFree(r->d_bidb);
     cudaFree(r->d_obase); cudaFree(r->d_tflag); cudaFree(r->d_tagg); cudaFree(r->d_tincl);
     cudaFree(r->d_rs);

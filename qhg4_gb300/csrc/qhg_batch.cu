@@ -145,6 +145,7 @@ StepBuffers make_buffers(qhg_batch *b, int cur) {
     B.meta2 = b->d_meta[nx];
     B.nbr = b->d_nbr; B.nnbr = b->d_nnbr; B.rev = b->d_rev; B.K = b->d_K; B.vthr = b->d_vthr[cur]; B.vthr2 = b->d_vthr[nx];
     B.wthr = b->d_wthr; B.cmove = b->d_cmove; B.necm = b->d_necm[cur]; B.necm2 = b->d_necm[nx];
+    B.occ = nullptr;   // occupancy tracking is a single-run option
     B.outc = b->d_outc; B.father = b->d_father; B.brank = b->d_brank; B.clsc = b->d_clsc;
     B.sbase = b->d_sbase; B.bbase = b->d_bbase; B.bidbase = b->d_bidb; B.obase = b->d_obase;
     B.tile_flag = b->d_tflag; B.tile_agg = b->d_tagg; B.tile_incl = b->d_tincl;

@@ -196,6 +196,9 @@ struct StepBuffers {
     // list (current table, next table), copied from cmove by the cell scan;
     // the Verhulst thresholds above are stored by the same positions
     const uint32_t *necm; uint32_t *necm2;
+    // occupancy tracking (single runs with QHG_FLAG_TRACK_OCCUPANCY, else
+    // null): per cell, the first step whose table holds an agent there, -1 none
+    int32_t *occ;
     // outcome word per agent: outcome byte | local cell << 8 | rank in its
     // cell's class << 17
     uint32_t *outc; int32_t *father; uint16_t *brank; uint32_t *clsc;

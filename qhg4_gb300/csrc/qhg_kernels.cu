@@ -2295,6 +2295,24 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
     commit_step<BATCH, false>(P, BB, rs, &s_flag);
 }
 
+// ------------------------------------------------------------- occupancy
+// OccTracker::updateCounts / OccHistory::addEntry (core/OccTracker.cpp,
+// core/OccHistory.cpp) for one population: a cell's occupation is recorded
+// when it first holds an agent (a cell emptied later keeps its entry, as
+// OccHistory ignores masks of zero).  Run after a step's commit on the table
+// it made (and after an upload on the uploaded one): every non-empty cell
+// without an entry gets the step of that table.
+__global__ void __launch_bounds__(256)
+k_occupancy(const RunState *__restrict__ rs, const uint32_t *__restrict__ nonempty, int32_t *__restrict__ occ) {
+    if (rs->error != 0u) return;   // the step failed: its table was not committed
+    const uint32_t n = rs->n_nonempty;
+    const int32_t st = rs->step;
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        const uint32_t c = nonempty[r];
+        if (occ[c] < 0) occ[c] = st;
+    }
+}
+
 // ----------------------------------------------------------------- genomes
 // Poisson(1) inverse-CDF thresholds floor(P(K <= k) * 2^32), k = 0..15, exact
 __constant__ uint32_t kPoisson1Cdf32[16] = {
@@ -2647,6 +2665,12 @@ extern "C" int qhg_launch_upload(const qhg::StepConst *P, qhg::RunState *rs, con
     return (int)cudaGetLastError();
 }
 
+extern "C" int qhg_launch_occupancy(const qhg::RunState *rs, const uint32_t *nonempty, int32_t *occ, int grid,
+                                    cudaStream_t stream) {
+    qhg::k_occupancy<<<std::max(1, grid), 256, 0, stream>>>(rs, nonempty, occ);
+    return (int)cudaGetLastError();
+}
+
 extern "C" int qhg_launch_gather_genomes(const int32_t *gslot, const uint64_t *genome, uint32_t n, int words,
                                          uint32_t slots, uint64_t *out, cudaStream_t stream) {
     const uint64_t total = (uint64_t)n * (uint64_t)words;
@@ -2805,6 +2829,9 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
 #undef QHG_LAUNCH_SCATTER_CELL
 #undef QHG_LAUNCH_SCATTER
     if (ev) cudaEventRecord(ev[3], stream);
+    if (!batch && B->occ != nullptr) {
+        k_occupancy<<<std::max(1, L.scatter_grid), 256, 0, stream>>>(rs, B->nonempty2, B->occ);
+    }
     if (batch) {
         k_inject<<<L.scatter_grid, 256, 0, stream>>>(rs, BB, B->id2, B->birth2, B->age2, B->lastb2, B->meta2,
                                                      P->capacity);

@@ -19,6 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libqhg_gpu.so")
 
 QHG_FLAG_LOG_BIRTHS = 1
+QHG_FLAG_TRACK_OCCUPANCY = 2
 
 ERRORS = {
     -1: "QHG_ERR_ARG", -2: "QHG_ERR_CUDA", -3: "QHG_ERR_NOMEM", -4: "QHG_ERR_STATE",
@@ -38,7 +39,7 @@ EXPORTS = [
     "qhg_batch_set_shape", "qhg_batch_get_shape", "qhg_batch_stream", "qhg_batch_destroy",
     "qhg_batch_live_history", "qhg_batch_snapshot_async", "qhg_batch_snapshot_wait",
     "qhg_host_buffer_alloc", "qhg_host_buffer_free", "qhg_gpu_next_id", "qhg_gpu_set_next_id",
-    "qhg_gpu_test_stall_scan",
+    "qhg_gpu_test_stall_scan", "qhg_gpu_occupancy",
 ]
 
 
@@ -131,6 +132,7 @@ def load_library(path: str = LIB_PATH):
         "qhg_gpu_next_id": (I, [P, P]),
         "qhg_gpu_set_next_id": (I, [P, ct.c_int64]),
         "qhg_gpu_test_stall_scan": (I, [P, ct.c_int32]),
+        "qhg_gpu_occupancy": (I, [P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -174,9 +176,9 @@ class GpuRun:
     """One simulation held by libqhg_gpu.so on a CUDA device."""
 
     def __init__(self, grid: Grid, actions: Sequence[Action], seed: int, genetics: Genetics = Genetics(),
-                 log_births: bool = False, capacity: int = 0, device: int = 0):
+                 log_births: bool = False, capacity: int = 0, device: int = 0, track_occupancy: bool = False):
         lib = load_library()
-        flags = QHG_FLAG_LOG_BIRTHS if log_births else 0
+        flags = (QHG_FLAG_LOG_BIRTHS if log_births else 0) | (QHG_FLAG_TRACK_OCCUPANCY if track_occupancy else 0)
         self._desc = make_desc(actions, seed, genetics, capacity, flags, device)
         h = ct.c_void_p()
         _check(lib.qhg_gpu_create(ct.byref(self._desc), ct.byref(h)))
@@ -237,6 +239,13 @@ class GpuRun:
         c = np.zeros(self.C, dtype=np.uint32)
         _check(_lib.qhg_gpu_counts(self.h, _p(c)))
         return c
+
+    def occupancy(self) -> np.ndarray:
+        """Per cell, the first step whose table holds an agent there (-1 none);
+        needs track_occupancy=True."""
+        o = np.zeros(self.C, dtype=np.int32)
+        _check(_lib.qhg_gpu_occupancy(self.h, _p(o)))
+        return o
 
     def stats(self, nsteps: int) -> np.ndarray:
         buf = (StepStats * max(1, nsteps))()
