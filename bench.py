@@ -353,7 +353,10 @@ def run_ours(args, world, rank, local, dist):
                        "l2": "inputs larger than L2 (hot table ~21 B x agents > 129 MB)"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "batched": batched,
             "served": served,
-            "gpu_launches": 3 * args.steps * world,
+            # per step: the action kernel and the scatter in each of the three
+            # forms (two of each return at once) and the cell scan
+            "gpu_launches": 7 * args.steps * world,
+            "gpu_launches_per_step": {"working": 3, "idle_forms": 4},
         }
         print(json.dumps(line), flush=True)
     return 0
