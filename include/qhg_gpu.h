@@ -64,6 +64,7 @@ extern "C" {
 #define QHG_ACT_OLDAGEDEATH   5  /* OldAgeDeath   actions/OldAgeDeath.cpp:48-67 */
 #define QHG_ACT_RANDOMMOVE    6  /* RandomMove    actions/RandomMove.cpp:65-100 */
 #define QHG_ACT_WEIGHTEDMOVE  7  /* WeightedMove  actions/WeightedMove.cpp:45-106 */
+#define QHG_ACT_ATANDEATH     8  /* ATanDeath     actions/ATanDeath.cpp:41, 57-77 */
 
 #define QHG_MAX_ACTIONS       16
 #define QHG_MAX_CELL_AGENTS   4608   /* agents one cell may hold */
@@ -87,6 +88,7 @@ typedef struct qhg_run qhg_run;
  *   VERHULST      {b0, d0, theta, K}
  *   VERHULSTVARK  {b0, d0, theta}            (K per cell from the grid)
  *   OLDAGEDEATH   {max_age, uncertainty}
+ *   ATANDEATH     {max_age, range, slope}
  *   RANDOMMOVE    {prob}
  *   WEIGHTEDMOVE  {prob}                     (weights: the grid's K, cumulated)
  */

@@ -41,7 +41,8 @@
 
 enum {
     ACT_GETOLD = 0, ACT_FERTILITY = 1, ACT_RANDOMPAIR = 2, ACT_VERHULST = 3,
-    ACT_VERHULSTVARK = 4, ACT_OLDAGEDEATH = 5, ACT_RANDOMMOVE = 6, ACT_WEIGHTEDMOVE = 7
+    ACT_VERHULSTVARK = 4, ACT_OLDAGEDEATH = 5, ACT_RANDOMMOVE = 6, ACT_WEIGHTEDMOVE = 7,
+    ACT_ATANDEATH = 8
 };
 #define MAX_ACTIONS 16
 #define CROSSOVER_POISSON1 (-100)
@@ -49,6 +50,8 @@ enum {
 #define LS_ALIVE 1u
 #define LS_FERTILE 5u
 #define TWO32 4294967296.0
+/* Q_PI (utils/qhg_consts.h): std::numbers::pi, the double nearest pi */
+#define QO_PI 3.141592653589793
 
 /* Poisson(1) inverse-CDF thresholds floor(P(K<=k) * 2^32), exact */
 static const uint32_t POISSON1_CDF32[16] = {
@@ -64,6 +67,7 @@ typedef struct {
     int n_act;
     int act_type[MAX_ACTIONS];
     double act_p[MAX_ACTIONS][4];
+    double act_scale[MAX_ACTIONS];   /* ATanDeath: m_dScale of preLoop */
     uint32_t act_window[MAX_ACTIONS];
     int has_pair;
     int genome_size, num_blocks, num_crossover;
@@ -294,6 +298,13 @@ qo_run *qo_create(uint64_t seed, int n_act, const int32_t *types, const double *
         switch (types[a]) {
         case ACT_VERHULST: case ACT_VERHULSTVARK: case ACT_RANDOMMOVE: case ACT_WEIGHTEDMOVE: w += 2; break;
         case ACT_OLDAGEDEATH: w += 1; break;
+        case ACT_ATANDEATH:
+            /* ATanDeath::preLoop (actions/ATanDeath.cpp:41):
+             * scale = (pi/2 - EPS) / atan(slope * range), EPS = 0.001
+             * (actions/ATanDeath.h) */
+            r->act_scale[a] = (QO_PI / 2 - 0.001) / atan(r->act_p[a][2] * r->act_p[a][1]);
+            w += 1;
+            break;
         case ACT_RANDOMPAIR: r->has_pair = 1; break;
         default: break;
         }
@@ -546,6 +557,13 @@ int qo_step(qo_run *r, int nsteps, uint64_t *stats_out) {
                     double lo = 1 - U * M, hi = 1 + U * M;
                     double dR = lo + ((hi - lo) * next_draw(&s)) / TWO32;
                     if (age > M + dR) { alive = 0; nDeaths++; }
+                    break;
+                }
+                case ACT_ATANDEATH: { /* actions/ATanDeath.cpp:57-77 */
+                    double M = p[0], slope = p[2];
+                    age = fT - r->birth[i];
+                    double dProb = 0.5 + r->act_scale[a] * atan(slope * (age - M)) / QO_PI;
+                    if (u2d(next_draw(&s)) < dProb) { alive = 0; nDeaths++; }
                     break;
                 }
                 case ACT_RANDOMMOVE: { /* actions/RandomMove.cpp:65-100 */

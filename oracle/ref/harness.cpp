@@ -43,6 +43,7 @@
 #include "Fertility.cpp"
 #include "VerhulstVarK.cpp"
 #include "OldAgeDeath.cpp"
+#include "ATanDeath.cpp"
 #include "RandomMove.cpp"
 #include "WeightedMove.cpp"
 #include "SingleEvaluator.cpp"
@@ -61,7 +62,8 @@ unsigned long g_qhgDrawErrors = 0;
 /* action type codes shared with oracle/refsim_io.py and include/qhg_gpu.h */
 enum {
     ACT_GETOLD = 0, ACT_FERTILITY = 1, ACT_RANDOMPAIR = 2, ACT_VERHULST = 3,
-    ACT_VERHULSTVARK = 4, ACT_OLDAGEDEATH = 5, ACT_RANDOMMOVE = 6, ACT_WEIGHTEDMOVE = 7
+    ACT_VERHULSTVARK = 4, ACT_OLDAGEDEATH = 5, ACT_RANDOMMOVE = 6, ACT_WEIGHTEDMOVE = 7,
+    ACT_ATANDEATH = 8
 };
 /* the crossover mode that draws a Poisson(1) number of breakpoints per parent */
 static const int CROSSOVER_POISSON1 = -100;
@@ -265,6 +267,12 @@ public:
                 snprintf(buf, 64, "%.17g", s.p[0]); mc.addParam(ATTR_OLDAGEDEATH_MAXAGE_NAME, buf);
                 snprintf(buf, 64, "%.17g", s.p[1]); mc.addParam(ATTR_OLDAGEDEATH_UNCERTAINTY_NAME, buf);
                 break;
+            case ACT_ATANDEATH:
+                pA = new ATanDeath<RefAgent>(this, m_pCG, "", m_apWELL);
+                snprintf(buf, 64, "%.17g", s.p[0]); mc.addParam(ATTR_ATANDEATH_MAXAGE_NAME, buf);
+                snprintf(buf, 64, "%.17g", s.p[1]); mc.addParam(ATTR_ATANDEATH_RANGE_NAME, buf);
+                snprintf(buf, 64, "%.17g", s.p[2]); mc.addParam(ATTR_ATANDEATH_SLOPE_NAME, buf);
+                break;
             case ACT_RANDOMMOVE:
                 pA = new RandomMove<RefAgent>(this, m_pCG, "", m_apWELL);
                 snprintf(buf, 64, "%.17g", s.p[0]); mc.addParam(ATTR_RANDOMMOVE_PROB_NAME, buf);
@@ -347,7 +355,7 @@ public:
                         uint32_t t = m_vSpecs[k].type;
                         if ((t == ACT_VERHULST) || (t == ACT_VERHULSTVARK) || (t == ACT_RANDOMMOVE) || (t == ACT_WEIGHTEDMOVE)) {
                             n = 2;
-                        } else if (t == ACT_OLDAGEDEATH) {
+                        } else if ((t == ACT_OLDAGEDEATH) || (t == ACT_ATANDEATH)) {
                             n = 1;
                         }
                     }

@@ -8,6 +8,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <string>
 #include <vector>
 
@@ -151,6 +152,63 @@ static float float_floor_of(double x) {
     return f;
 }
 
+// ATanDeath's death probability (actions/ATanDeath.cpp:62):
+// 0.5 + scale * atan(slope * (age - M)) / Q_PI, age promoted from float
+static double atan_death_prob(const ActionConst &A, float fa) {
+    return 0.5 + A.at_scale * std::atan(A.at_slope * ((double)fa - A.at_M)) / kQPi;
+}
+
+// float <-> a key that orders floats like integers (finite and infinite)
+static int64_t float_key(float f) {
+    int32_t b;
+    std::memcpy(&b, &f, 4);
+    return b >= 0 ? (int64_t)b : -(int64_t)(b & 0x7fffffff);
+}
+static float key_float(int64_t k) {
+    const int32_t b = k >= 0 ? (int32_t)k : (int32_t)((uint32_t)(-k) | 0x80000000u);
+    float f;
+    std::memcpy(&f, &b, 4);
+    return f;
+}
+
+// Ages at which ATanDeath's decision does not depend on the draw.  The
+// draw is u / 2^32 with u < 2^32: an agent survives every draw where the
+// probability is <= 0 and dies on every draw where it exceeds 1 - 2^-32.
+// The probability rises with age when scale * slope > 0; bisection over the
+// floats finds age_lo, the oldest age with p <= -delta, and age_hi, the
+// oldest age with p < 1 + delta.  The margin delta = 2^-30 is many orders
+// above the few ulps by which the device's atan may differ from the host's,
+// so ages <= age_lo survive and ages > age_hi die whatever the atan; the
+// device evaluates the probability in between.  Without a rising curve, or
+// where a bound does not exist, the bound is NaN and the device evaluates
+// every age.
+static void atan_death_window(ActionConst &A) {
+    const float nanf = std::numeric_limits<float>::quiet_NaN();
+    A.age_lo = nanf;
+    A.age_hi = nanf;
+    if (!(std::isfinite(A.at_scale) && std::isfinite(A.at_slope) && std::isfinite(A.at_M) &&
+          A.at_scale * A.at_slope > 0))
+        return;
+    const double delta = 1.0 / 1073741824.0;
+    const int64_t kmin = float_key(-INFINITY), kmax = float_key(INFINITY);
+    // largest key in [kmin, kmax] whose probability satisfies below(p), given
+    // that below holds at kmin and not at kmax
+    auto last_key = [&](auto below) {
+        int64_t a = kmin, b = kmax;
+        while (b - a > 1) {
+            const int64_t m = a + (b - a) / 2;
+            if (below(atan_death_prob(A, key_float(m)))) a = m; else b = m;
+        }
+        return a;
+    };
+    auto never = [&](double p) { return p <= -delta; };
+    auto maybe = [&](double p) { return p < 1.0 + delta; };
+    if (never(atan_death_prob(A, -INFINITY)) && !never(atan_death_prob(A, INFINITY)))
+        A.age_lo = key_float(last_key(never));
+    if (maybe(atan_death_prob(A, -INFINITY)) && !maybe(atan_death_prob(A, INFINITY)))
+        A.age_hi = key_float(last_key(maybe));
+}
+
 // Numerical Recipes' log-gamma, continued fraction and regularised incomplete
 // beta function I_x(a, b) (Press et al., Numerical Recipes in C, 2nd ed.,
 // 6.1 and 6.4), the functions the reference's utils/bino_tools.cpp uses.
@@ -284,6 +342,16 @@ int qhg_host_actions(StepConst &P, int n, const int32_t *types, const double (*p
             w += 1;
             break;
         }
+        case kATanDeath:
+            // ATanDeath::preLoop (actions/ATanDeath.cpp:41):
+            // scale = (pi/2 - EPS) / atan(slope * range)
+            A.at_M = p[0];
+            A.at_slope = p[2];
+            A.at_scale = (kQPi / 2 - kATanEps) / std::atan(p[2] * p[1]);
+            atan_death_window(A);
+            P.age_from_birth = 1;
+            w += 1;
+            break;
         case kRandomMove:
         case kWeightedMove:
             A.pthr = host_prob_threshold(p[0]);

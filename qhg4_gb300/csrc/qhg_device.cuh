@@ -88,8 +88,13 @@ constexpr int kCls = 8;
 
 enum ActionType : int32_t {
     kGetOld = 0, kFertility = 1, kRandomPair = 2, kVerhulst = 3, kVerhulstVarK = 4,
-    kOldAgeDeath = 5, kRandomMove = 6, kWeightedMove = 7
+    kOldAgeDeath = 5, kRandomMove = 6, kWeightedMove = 7, kATanDeath = 8
 };
+
+// ATanDeath (actions/ATanDeath.h, utils/qhg_consts.h): EPS of its scale and
+// Q_PI = std::numbers::pi, the double nearest pi
+constexpr double kATanEps = 0.001;
+constexpr double kQPi = 3.141592653589793;
 
 enum ErrorCode : uint32_t {
     kErrNone = 0, kErrCellTooLarge = 1, kErrTimeout = 2, kErrCapacity = 3, kErrInternal = 4, kErrBadCell = 5
@@ -101,11 +106,12 @@ struct ActionConst {
     uint32_t window;        // first draw of the action in the per-agent stream
     int32_t vslot;          // Verhulst: index among the population's Verhulst actions
     float f0, f1, f2;       // Fertility: min age, max age, interbirth
-    float age_lo, age_hi;   // OldAgeDeath: float bounds of the uncertain age window
+    float age_lo, age_hi;   // OldAgeDeath, ATanDeath: float bounds of the uncertain age window
     double b0, d0, th;      // Verhulst
     double th_b0, th_d0;    // theta - b0, theta - d0
     double K;               // Verhulst constant K
     double oad_M, oad_a, oad_w;  // OldAgeDeath: max age, 1 - U*M, (1+U*M) - (1-U*M)
+    double at_M, at_slope, at_scale;  // ATanDeath: max age, slope, (pi/2 - EPS) / atan(slope * range)
     uint64_t pthr;          // RandomMove / WeightedMove: u < pthr  <=>  u/2^32 < p
 };
 

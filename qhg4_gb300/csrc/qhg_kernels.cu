@@ -222,7 +222,7 @@ __host__ __device__ constexpr int prog_index(int p, int t0, int t1) {
 // order, as the host hands them out
 __host__ __device__ constexpr uint32_t action_draws(int t) {
     return (t == kVerhulst || t == kVerhulstVarK || t == kRandomMove || t == kWeightedMove) ? 2u
-           : (t == kOldAgeDeath ? 1u : 0u);
+           : (t == kOldAgeDeath || t == kATanDeath ? 1u : 0u);
 }
 __host__ __device__ constexpr uint32_t prog_window(int p, int a) {
     return a <= 0 ? 0u : prog_window(p, a - 1) + action_draws(prog_act(p, a - 1));
@@ -321,6 +321,25 @@ __device__ __forceinline__ uint8_t agent_outcome(const StepConst &P, const Batch
                 const double t = __dmul_rn(__dmul_rn(A.oad_w, (double)u), 2.3283064365386962890625e-10);
                 const double thr = __dadd_rn(A.oad_M, __dadd_rn(A.oad_a, t));
                 die = (double)fa > thr;
+            }
+            if (die) { alive = false; cnt_deaths++; }
+            break;
+        }
+        case kATanDeath: {
+            // actions/ATanDeath.cpp:57-77: dies if wrandd() < 0.5 + scale *
+            // atan(slope * (age - M)) / Q_PI; ages outside the window
+            // [age_lo, age_hi] decide without the draw (NaN bounds: none)
+            fa = __fsub_rn(fTR, fb);
+            bool die;
+            if (fa <= A.age_lo) {
+                die = false;
+            } else if (fa > A.age_hi) {
+                die = true;
+            } else {
+                const double x = __dmul_rn(A.at_slope, __dsub_rn((double)fa, A.at_M));
+                const double p = __dadd_rn(0.5, __ddiv_rn(__dmul_rn(A.at_scale, atan(x)), kQPi));
+                const uint32_t u = dr.get(P, A.window);
+                die = __dmul_rn((double)u, 2.3283064365386962890625e-10) < p;
             }
             if (die) { alive = false; cnt_deaths++; }
             break;

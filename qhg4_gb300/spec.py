@@ -12,7 +12,7 @@ the per-agent Philox stream of a step: windows are handed out in execution
 order, Verhulst/VerhulstVarK 2 draws (LinearBirth then LinearDeath,
 actions/Verhulst.cpp:101-115), RandomMove 2 (actions/RandomMove.cpp:73-84),
 WeightedMove 2 (actions/WeightedMove.cpp:57-71), OldAgeDeath 1
-(actions/OldAgeDeath.cpp:57).
+(actions/OldAgeDeath.cpp:57), ATanDeath 1 (actions/ATanDeath.cpp:66).
 """
 from __future__ import annotations
 
@@ -27,6 +27,7 @@ ACT_VERHULSTVARK = 4
 ACT_OLDAGEDEATH = 5
 ACT_RANDOMMOVE = 6
 ACT_WEIGHTEDMOVE = 7
+ACT_ATANDEATH = 8
 
 #: reference class names (actions/*.h ATTR_*_NAME); Verhulst with a constant K
 #: runs through VerhulstVarK in the reference oracle build, and no action name
@@ -40,6 +41,7 @@ ACTION_NAMES = {
     ACT_OLDAGEDEATH: "OldAgeDeath",
     ACT_RANDOMMOVE: "RandomMove",
     ACT_WEIGHTEDMOVE: "WeightedMove",
+    ACT_ATANDEATH: "ATanDeath",
 }
 
 #: draws per agent per step an action may take
@@ -49,6 +51,7 @@ ACTION_DRAWS = {
     ACT_RANDOMMOVE: 2,
     ACT_WEIGHTEDMOVE: 2,
     ACT_OLDAGEDEATH: 1,
+    ACT_ATANDEATH: 1,
 }
 
 #: number of crossovers per parent drawn from Poisson(1) (an extension; the
@@ -67,6 +70,7 @@ class Action:
       Verhulst       (b0, d0, theta, K)
       VerhulstVarK   (b0, d0, theta)           K per cell from the grid
       OldAgeDeath    (max_age, uncertainty)
+      ATanDeath      (max_age, range, slope)
       RandomMove     (prob)
       WeightedMove   (prob)                    weights from the grid's K
     """

@@ -3,7 +3,7 @@
 action code.
 
 Each case runs oracle/_ref/qhg_ref_philox -- the reference's GetOld,
-Fertility, VerhulstVarK/LinearBirth/LinearDeath, OldAgeDeath, RandomMove,
+Fertility, VerhulstVarK/LinearBirth/LinearDeath, OldAgeDeath, ATanDeath, RandomMove,
 WeightedMove/SingleEvaluator, Genetics/BitGeneUtils/BinomialDist and
 SPopulation code, compiled from the reference sources by oracle/ref/Makefile,
 with Philox draws keyed by (seed, step, agent ID, action) -- on a small seeded
@@ -29,7 +29,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 from oracle.refsim_io import run_reference  # noqa: E402
-from qhg4_gb300.spec import (ACT_FERTILITY, ACT_GETOLD, ACT_OLDAGEDEATH, ACT_RANDOMMOVE,  # noqa: E402
+from qhg4_gb300.spec import (ACT_ATANDEATH, ACT_FERTILITY, ACT_GETOLD, ACT_OLDAGEDEATH, ACT_RANDOMMOVE,  # noqa: E402
                              ACT_RANDOMPAIR, ACT_VERHULSTVARK, ACT_WEIGHTEDMOVE, CROSSOVER_POISSON1,
                              Action, Genetics, config1_actions, config2_actions, config3_actions)
 from qhg4_gb300.workload import make_agents, terrain_grid, uniform_grid  # noqa: E402
@@ -54,6 +54,14 @@ def cases():
              Action(ACT_RANDOMMOVE, 7, (0.05,)), Action(ACT_WEIGHTEDMOVE, 8, (0.15,))]
     yield ("mixed_order", g5, make_agents(g5, 8000, seed=15, age_max=70.0, proportional_to_K=True), acts5,
            Genetics(), 25, 123)
+    # ATanDeath in place of OldAgeDeath: the arctangent death curve around
+    # age 55 (range 12, slope 0.35), ages up to 80
+    g7 = terrain_grid(8, seed=8)
+    acts7 = [Action(ACT_GETOLD, 1), Action(ACT_FERTILITY, 2, (15.0, 45.0, 2.0)), Action(ACT_RANDOMPAIR, 3),
+             Action(ACT_ATANDEATH, 4, (55.0, 12.0, 0.35)), Action(ACT_VERHULSTVARK, 6, (0.25, 0.04, 0.01)),
+             Action(ACT_WEIGHTEDMOVE, 8, (0.15,))]
+    yield ("atan_death", g7, make_agents(g7, 8000, seed=17, age_max=80.0, proportional_to_K=True), acts7,
+           Genetics(), 25, 77)
     # cells of more than 512 agents (the big-cell kernels), thinning out below it
     g6 = uniform_grid(3, 400.0)
     yield ("dense_cells", g6, make_agents(g6, 60000, seed=16, age_max=50.0), config1_actions(K=400.0),

@@ -133,3 +133,27 @@ def test_batch_dense_cells_cell_form(gpu_lib):
     b.step(8)
     same_as_alone(b, ids[0], cases[0], 15)
     same_as_alone(b, ids[2], cases[2], 7)
+
+
+def test_batch_atan_death(gpu_lib):
+    """ATanDeath through the batch's interpreted action program, with each
+    run's own curve (per-run max age, range and slope)."""
+    from qhg4_gb300.spec import (ACT_ATANDEATH, ACT_FERTILITY, ACT_GETOLD, ACT_RANDOMPAIR, ACT_VERHULSTVARK,
+                                 ACT_WEIGHTEDMOVE, Action)
+
+    def acts(params):
+        return [Action(ACT_GETOLD, 1), Action(ACT_FERTILITY, 2, (15.0, 45.0, 2.0)), Action(ACT_RANDOMPAIR, 3),
+                Action(ACT_ATANDEATH, 4, params), Action(ACT_VERHULSTVARK, 6, (0.25, 0.04, 0.01)),
+                Action(ACT_WEIGHTEDMOVE, 8, (0.15,))]
+
+    curves = [(55.0, 12.0, 0.35), (50.0, 8.0, -0.4), (60.0, 300.0, 5.0)]
+    cases = []
+    for k, prm in enumerate(curves):
+        g = terrain_grid(8 + k, seed=60 + k)
+        a = make_agents(g, 10_000 + 4_000 * k, seed=600 + k, age_max=80.0, proportional_to_K=True)
+        cases.append((g, a, acts(prm), 90 + k))
+    b = GpuBatch(acts(curves[0]), agent_capacity=300_000, cell_capacity=6_000, max_runs=3)
+    ids = [b.add_run(g, ac, seed, a) for g, a, ac, seed in cases]
+    b.step(16)
+    for k, r in enumerate(ids):
+        same_as_alone(b, r, cases[k], 15)

@@ -10,7 +10,7 @@ import pytest
 
 from oracle import port
 from qhg4_gb300.gpu import GpuRun
-from qhg4_gb300.spec import (ACT_FERTILITY, ACT_GETOLD, ACT_OLDAGEDEATH, ACT_RANDOMMOVE, ACT_RANDOMPAIR,
+from qhg4_gb300.spec import (ACT_ATANDEATH, ACT_FERTILITY, ACT_GETOLD, ACT_OLDAGEDEATH, ACT_RANDOMMOVE, ACT_RANDOMPAIR,
                              ACT_VERHULST, ACT_VERHULSTVARK, ACT_WEIGHTEDMOVE, CROSSOVER_POISSON1, Action,
                              Genetics, config1_actions, config3_actions)
 from qhg4_gb300.workload import make_agents, terrain_grid, uniform_grid
@@ -73,6 +73,47 @@ def test_interpreted_program_order(gpu_lib):
             Action(ACT_RANDOMMOVE, 7, (0.05,)), Action(ACT_WEIGHTEDMOVE, 8, (0.15,))]
     o, g, st = run_both(grid, agents, acts, 30, 123)
     assert_same(o, g, st, 30)
+
+
+def atan_actions(params):
+    """GetOld, Fertility, RandomPair, ATanDeath, VerhulstVarK, WeightedMove."""
+    return [Action(ACT_GETOLD, 1), Action(ACT_FERTILITY, 2, (15.0, 45.0, 2.0)), Action(ACT_RANDOMPAIR, 3),
+            Action(ACT_ATANDEATH, 4, params), Action(ACT_VERHULSTVARK, 6, (0.25, 0.04, 0.01)),
+            Action(ACT_WEIGHTEDMOVE, 8, (0.15,))]
+
+
+def atan_case(form):
+    if form == "sparse":      # mostly empty cells: cell-aligned tiles
+        grid = terrain_grid(10, seed=5)
+        return grid, make_agents(grid, 15000, seed=51, age_max=80.0, proportional_to_K=True)
+    if form == "dense":       # ~35 agents per cell: one warp per pair of cells
+        grid = uniform_grid(5, 40.0)
+        return grid, make_agents(grid, 35 * grid.num_cells, seed=52, age_max=80.0)
+    grid = uniform_grid(3, 700.0)  # ~600 agents per cell: the big-cell kernels
+    return grid, make_agents(grid, 600 * grid.num_cells, seed=53, age_max=80.0)
+
+
+@pytest.mark.parametrize("form", ["sparse", "dense", "big"])
+def test_atan_death(gpu_lib, form):
+    """ATanDeath (actions/ATanDeath.cpp): the death probability 0.5 + scale *
+    atan(slope * (age - M)) / pi against each draw, in all three kernel
+    forms; ages far from M decide without evaluating the arctangent."""
+    grid, agents = atan_case(form)
+    o, g, st = run_both(grid, agents, atan_actions((55.0, 12.0, 0.35)), 20, 61, chunks=(1, 19))
+    assert_same(o, g, st, 20)
+    assert st[:, 2].sum() > 0
+
+
+@pytest.mark.parametrize("params", [(50.0, 8.0, -0.4), (60.0, 300.0, 5.0), (45.0, 20.0, 0.1)],
+                         ids=["negative_slope", "steep_no_window", "shallow"])
+def test_atan_death_curves(gpu_lib, params):
+    """A negative slope (the curve still rises: scale changes sign with it),
+    a slope so steep that the probability never reaches 0 or 1 (every age
+    evaluates the arctangent), and a shallow curve."""
+    grid, agents = atan_case("dense")
+    o, g, st = run_both(grid, agents, atan_actions(params), 15, 62)
+    assert_same(o, g, st, 15)
+    assert st[:, 2].sum() > 0
 
 
 def test_no_pairing_no_moves(gpu_lib):

@@ -45,3 +45,26 @@ def test_port_oracle_random_case_against_reference_build(tmp_path):
     d = table_diff(r.agents(), ref.agents)
     assert d is None, d
     assert np.array_equal(st, ref.stats)
+
+
+@pytest.mark.skipif(not os.path.exists(ref_program("philox")), reason="reference build not present")
+@pytest.mark.parametrize("atan_params", [(50.0, 8.0, -0.4), (60.0, 300.0, 5.0), (45.0, 20.0, 0.1)])
+def test_port_oracle_atan_death_against_reference_build(tmp_path, atan_params):
+    """ATanDeath (actions/ATanDeath.cpp) with a negative slope, a slope so
+    steep that the death probability never reaches 0 or 1 (scale < 1), and a
+    shallow one, against the reference's own class."""
+    from qhg4_gb300.spec import (ACT_ATANDEATH, ACT_FERTILITY, ACT_GETOLD, ACT_RANDOMMOVE, ACT_RANDOMPAIR,
+                                 ACT_VERHULSTVARK, Action)
+    from qhg4_gb300.workload import make_agents, terrain_grid
+    grid = terrain_grid(8, seed=81)
+    agents = make_agents(grid, 6000, seed=82, age_max=80.0, proportional_to_K=True)
+    acts = [Action(ACT_FERTILITY, 2, (15.0, 45.0, 2.0)), Action(ACT_RANDOMPAIR, 3),
+            Action(ACT_ATANDEATH, 5, atan_params), Action(ACT_VERHULSTVARK, 6, (0.3, 0.03, 0.01)),
+            Action(ACT_RANDOMMOVE, 7, (0.1,)), Action(ACT_GETOLD, 8)]
+    ref = run_reference("philox", str(tmp_path), grid, agents, acts, 15, 4242, threads=2)
+    r, st = port.run(grid, agents, acts, 15, 4242)
+    assert ref.draw_errors == 0
+    assert st[:, 2].sum() > 0
+    d = table_diff(r.agents(), ref.agents)
+    assert d is None, d
+    assert np.array_equal(st, ref.stats)
