@@ -132,6 +132,24 @@ const char *qhg_gpu_version(void);
 int qhg_gpu_create(const qhg_run_desc *desc, qhg_run **out);
 int qhg_gpu_upload_grid(qhg_run *run, const int32_t *nbr6, const uint8_t *nnbr, const double *K,
                         int32_t num_cells);
+/* Environment updates between steps, for populations whose K and move
+ * weights come from environment evaluators (populations/FlatExpPop.cpp:43-56):
+ * qhg_gpu_set_capacity takes a new K per cell (C entries), what NPPCapacity
+ * writes into the capacity array (actions/NPPCapacity.cpp) and VerhulstVarK
+ * reads at each step's initialize (actions/LinearBirth.cpp:90-112,
+ * actions/LinearDeath.cpp:92-122); unless weights were given, WeightedMove's
+ * weights follow K as after qhg_gpu_upload_grid.  qhg_gpu_set_move_weights
+ * takes WeightedMove's cumulative weights (C x 7: W[c][0] the cell's own
+ * weight, W[c][i+1] = W[c][i] + neighbour i's), what MultiEvaluator /
+ * SingleEvaluator leave in the weight array (actions/MultiEvaluator.cpp:221-255,
+ * actions/SingleEvaluator.cpp:174-241) and WeightedMove reads
+ * (actions/WeightedMove.cpp:57-80); from then on they no longer follow K.
+ * A row whose W[c][0] differs from W[c][n] (n neighbours) must have finite
+ * entries and W[c][n] > 0 (QHG_ERR_ARG otherwise).  Both wait for the run's
+ * stream, report a device-side error of an earlier step like qhg_gpu_sync
+ * (and then change nothing), and take effect from the next step on. */
+int qhg_gpu_set_capacity(qhg_run *run, const double *K);
+int qhg_gpu_set_move_weights(qhg_run *run, const double *cumw7);
 /* agents in any order; dead rows (state 0) are dropped */
 int qhg_gpu_upload_agents(qhg_run *run, const qhg_agents_soa *agents, int64_t n, int32_t first_step);
 /* runs nsteps steps asynchronously on the run's stream */

@@ -57,6 +57,10 @@ def _load():
     lib.qo_binomial_table.restype = ct.c_int
     lib.qo_binomial_table.argtypes = [P, P, ct.c_int]
     lib.qo_set_log_births.argtypes = [P, ct.c_int]
+    lib.qo_set_capacity.restype = ct.c_int
+    lib.qo_set_capacity.argtypes = [P, P]
+    lib.qo_set_move_weights.restype = ct.c_int
+    lib.qo_set_move_weights.argtypes = [P, P]
     lib.qo_set_threads.argtypes = [ct.c_int]
     lib.qo_max_threads.restype = ct.c_int
     lib.qo_destroy.argtypes = [P]
@@ -120,6 +124,19 @@ class OracleRun:
         st = st[:n * 4].reshape(n, 4)
         self.stats.append(st)
         return st
+
+    def set_capacity(self, K: np.ndarray) -> None:
+        """VerhulstVarK's K per cell from the next step on (and the move
+        weights, unless weights were given)."""
+        k = np.ascontiguousarray(K, dtype=np.float64)
+        assert k.shape == (self.C,)
+        _load().qo_set_capacity(self.h, _p(k))
+
+    def set_move_weights(self, W: np.ndarray) -> None:
+        """WeightedMove's cumulative weights (C x 7) from the next step on."""
+        w = np.ascontiguousarray(W, dtype=np.float64)
+        assert w.shape == (self.C, 7)
+        _load().qo_set_move_weights(self.h, _p(w))
 
     def num_agents(self) -> int:
         return int(_load().qo_num_agents(self.h))

@@ -80,6 +80,7 @@ typedef struct {
     uint8_t *nnbr;
     double *K;
     double *W;          /* cumulated WeightedMove weights [C*7] */
+    int w_given;        /* W was given (qo_set_move_weights), not derived from K */
     /* agents, sorted by ID */
     int64_t n, cap;
     int64_t *id;
@@ -282,6 +283,27 @@ static void make_genome(const qo_run *r, uint64_t *baby, const uint64_t *gm, con
     }
 }
 
+/* WeightedMove's weights from K: a SingleEvaluator with direct values,
+ * cumulated over the neighbours (actions/SingleEvaluator.cpp:174-241) */
+static void weights_from_K(qo_run *r) {
+    const int C = r->C;
+    for (int c = 0; c < C; c++) {
+        double dV = r->K[c];
+        r->W[(size_t)c * 7] = (dV > 0) ? dV : 0;
+    }
+    for (int c = 0; c < C; c++) {
+        double dW = r->W[(size_t)c * 7];
+        for (int i = 0; i < 6; i++) {
+            double dCW = 0;
+            int ni = r->nbr[(size_t)c * 6 + i];
+            if (ni >= 0) dCW = r->W[(size_t)ni * 7];
+            dCW = (dCW > 0) ? dCW : 0;
+            dW = dW + dCW;
+            r->W[(size_t)c * 7 + i + 1] = dW;
+        }
+    }
+}
+
 /* ------------------------------------------------------------ create */
 qo_run *qo_create(uint64_t seed, int n_act, const int32_t *types, const double *params,
                   int genome_size, int num_crossover, double mutation_rate,
@@ -324,23 +346,8 @@ qo_run *qo_create(uint64_t seed, int n_act, const int32_t *types, const double *
     memcpy(r->nnbr, nnbr, C);
     r->K = (double *)malloc(C * sizeof(double));
     memcpy(r->K, K, C * sizeof(double));
-    /* SingleEvaluator with direct values, cumulated (actions/SingleEvaluator.cpp:174-241) */
     r->W = (double *)calloc((size_t)C * 7, sizeof(double));
-    for (int c = 0; c < C; c++) {
-        double dV = K[c];
-        r->W[(size_t)c * 7] = (dV > 0) ? dV : 0;
-    }
-    for (int c = 0; c < C; c++) {
-        double dW = r->W[(size_t)c * 7];
-        for (int i = 0; i < 6; i++) {
-            double dCW = 0;
-            int ni = nbr[(size_t)c * 6 + i];
-            if (ni >= 0) dCW = r->W[(size_t)ni * 7];
-            dCW = (dCW > 0) ? dCW : 0;
-            dW = dW + dCW;
-            r->W[(size_t)c * 7 + i + 1] = dW;
-        }
-    }
+    weights_from_K(r);
     r->count = (uint32_t *)calloc(C, sizeof(uint32_t));
     r->B = (double *)calloc(C, sizeof(double));
     r->D = (double *)calloc(C, sizeof(double));
@@ -737,6 +744,25 @@ int qo_binomial_table(const qo_run *r, double *out, int cap) {
 }
 
 void qo_set_log_births(qo_run *r, int on) { r->log_births = on; }
+
+/* A new K per cell from the next step on: VerhulstVarK's rates are computed
+ * from K at each step's initialize (actions/LinearBirth.cpp:90-112,
+ * actions/LinearDeath.cpp:92-122).  Unless weights were given, WeightedMove's
+ * weights follow K (an always-updating SingleEvaluator). */
+int qo_set_capacity(qo_run *r, const double *K) {
+    memcpy(r->K, K, (size_t)r->C * sizeof(double));
+    if (!r->w_given) weights_from_K(r);
+    return 0;
+}
+
+/* WeightedMove's cumulative weights as a MultiEvaluator or SingleEvaluator
+ * leaves them (C x 7, actions/MultiEvaluator.cpp:221-255), from the next
+ * step on; they no longer follow K. */
+int qo_set_move_weights(qo_run *r, const double *W) {
+    memcpy(r->W, W, (size_t)r->C * 7 * sizeof(double));
+    r->w_given = 1;
+    return 0;
+}
 
 void qo_set_threads(int n) {
 #ifdef _OPENMP

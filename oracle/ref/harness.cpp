@@ -214,13 +214,19 @@ public:
         }
     }
 
+    /* adGivenW: WeightedMove's cumulative weights as given (C x 7, what a
+     * MultiEvaluator leaves, actions/MultiEvaluator.cpp:221-255), or NULL for
+     * weights from K through an always-updating SingleEvaluator */
     int setup(const std::vector<ActionSpec> &vSpecs, const double *adK,
-              int iGenomeSize, int iNumCrossOvers, double dMutRate) {
+              int iGenomeSize, int iNumCrossOvers, double dMutRate, const double *adGivenW) {
         int C = (int)m_pCG->m_iNumCells;
         m_adK = new double[C];
         memcpy(m_adK, adK, C*sizeof(double));
         m_adWeights = new double[(size_t)C*(m_pCG->m_iConnectivity+1)];
         memset(m_adWeights, 0, (size_t)C*(m_pCG->m_iConnectivity+1)*sizeof(double));
+        if (adGivenW != NULL) {
+            memcpy(m_adWeights, adGivenW, (size_t)C*(m_pCG->m_iConnectivity+1)*sizeof(double));
+        }
 
         int iResult = 0;
         for (size_t i = 0; (iResult == 0) && (i < vSpecs.size()); i++) {
@@ -280,11 +286,13 @@ public:
             case ACT_WEIGHTEDMOVE: {
                 /* weights: direct cell values K, cumulated over the
                  * neighbours (actions/SingleEvaluator.cpp:174-241) */
-                SingleEvaluator<RefAgent> *pSE = new SingleEvaluator<RefAgent>(
-                    this, m_pCG, "", m_adWeights, m_adK, "", true, EVENT_ID_NONE, true);
-                m_vOwned.push_back(pSE);
-                m_prio.addAction(pSE);
-                m_mPrioInfo[pSE->getActionName()] = (int)s.prio;
+                if (adGivenW == NULL) {
+                    SingleEvaluator<RefAgent> *pSE = new SingleEvaluator<RefAgent>(
+                        this, m_pCG, "", m_adWeights, m_adK, "", true, EVENT_ID_NONE, true);
+                    m_vOwned.push_back(pSE);
+                    m_prio.addAction(pSE);
+                    m_mPrioInfo[pSE->getActionName()] = (int)s.prio;
+                }
                 pA = new WeightedMove<RefAgent>(this, m_pCG, "", m_apWELL, m_adWeights);
                 snprintf(buf, 64, "%.17g", s.p[0]); mc.addParam(ATTR_WEIGHTEDMOVE_PROB_NAME, buf);
                 break;
@@ -365,6 +373,12 @@ public:
                 w += n;
             }
         }
+    }
+
+    /* a new K per cell, read by VerhulstVarK (and the SingleEvaluator) at
+     * the next initializeStep, as when an environment event changes it */
+    void setK(const double *adK) {
+        memcpy(m_adK, adK, m_pCG->m_iNumCells*sizeof(double));
     }
 
     int loadAgents(uint32_t N, const int64_t *aiID, const int32_t *aiCell, const float *afBirth,
@@ -623,6 +637,24 @@ int main(int argc, char *argv[]) {
     size_t nWords = (iGenomeSize > 0) ? (size_t)N * 2 * ((iGenomeSize + 63) / 64) : 0;
     std::vector<uint64_t> vGen(ok ? nWords : 0);
     ok = ok && rd(fIn, vGen.data(), 8, nWords);
+    /* optional: u32 has_weights, f64 W[C*7] if 1; u32 n_k_changes,
+     * n_k_changes x (u32 step, f64 K[C]) */
+    uint32_t iHasW = 0, nKC = 0;
+    std::vector<double> vW;
+    std::vector<uint32_t> vKCStep;
+    std::vector<double> vKC;
+    if (ok && rd(fIn, &iHasW, 4, 1)) {
+        if (iHasW == 1) {
+            vW.resize((size_t)C*7);
+            ok = rd(fIn, vW.data(), 8, vW.size());
+        }
+        ok = ok && rd(fIn, &nKC, 4, 1);
+        vKCStep.resize(ok ? nKC : 0);
+        vKC.resize(ok ? (size_t)nKC*C : 0);
+        for (uint32_t k = 0; ok && (k < nKC); k++) {
+            ok = rd(fIn, &vKCStep[k], 4, 1) && rd(fIn, vKC.data() + (size_t)k*C, 8, C);
+        }
+    }
     fclose(fIn);
     if (!ok) { fprintf(stderr, "malformed input %s\n", argv[1]); return 2; }
 
@@ -648,7 +680,7 @@ int main(int argc, char *argv[]) {
     uint aiSeeds[NUM_SEEDS] = {0};
 
     OraclePop *pPop = new OraclePop(pCG, (iLayer > 0) ? (int)iLayer : 65536, apIDG, aulState, aiSeeds);
-    if (pPop->setup(vSpecs, vK.data(), (int)iGenomeSize, iCross, dMut) != 0) {
+    if (pPop->setup(vSpecs, vK.data(), (int)iGenomeSize, iCross, dMut, (iHasW == 1) ? vW.data() : NULL) != 0) {
         fprintf(stderr, "population setup failed\n");
         return 3;
     }
@@ -665,6 +697,9 @@ int main(int argc, char *argv[]) {
         g_curStep = (int)s;
         float fT = (float)s;
         iAgentSteps += pPop->countLive();
+        for (uint32_t k = 0; k < nKC; k++) {
+            if (vKCStep[k] == s) pPop->setK(vKC.data() + (size_t)k*C);
+        }
         /* PopLooper::doStep (core/PopLooper.cpp:166-200) */
         int iRes = pPop->initializeStep(fT);
         sPrios.clear();

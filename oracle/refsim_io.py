@@ -10,6 +10,9 @@ Input (little endian):
   i32 nbr[C*6], u8 nnbr[C], f64 K[C],
   i64 id[N], i32 cell[N], f32 birth[N], f32 age[N], f32 lastb[N], u8 gender[N],
   u8 state[N], u64 genome[N*2*blocks]
+  optional: u32 has_weights, f64 W[C*7] if has_weights == 1 (WeightedMove's
+  cumulative weights as given, in place of the SingleEvaluator over K),
+  u32 n_k_changes, n_k_changes x (u32 step, f64 K[C]) (K from that step on)
 Output:
   "QHGOUT01", u32 steps, u32 C, u64 stats[steps*4] (live, births, deaths, moves),
   u32 n_dumps, u32 dump_step[n_dumps], u32 counts[n_dumps*C],
@@ -39,7 +42,7 @@ def ref_program(kind: str) -> str:
 
 def write_input(path: str, grid: Grid, agents: Agents, actions: Sequence[Action], steps: int,
                 seed: int, genetics: Genetics = Genetics(), dump_every: int = 0,
-                layer_size: int = 65536) -> None:
+                layer_size: int = 65536, weights=None, k_changes=()) -> None:
     C = grid.num_cells
     N = len(agents)
     with open(path, "wb") as f:
@@ -62,6 +65,18 @@ def write_input(path: str, grid: Grid, agents: Agents, actions: Sequence[Action]
         f.write(np.ascontiguousarray(agents.state, dtype="u1").tobytes())
         if genetics.genome_size > 0:
             f.write(np.ascontiguousarray(agents.genome, dtype="<u8").tobytes())
+        if weights is not None or len(k_changes) > 0:
+            f.write(struct.pack("<I", 1 if weights is not None else 0))
+            if weights is not None:
+                w = np.ascontiguousarray(weights, dtype="<f8")
+                assert w.shape == (C, 7)
+                f.write(w.tobytes())
+            f.write(struct.pack("<I", len(k_changes)))
+            for step, K in k_changes:
+                k = np.ascontiguousarray(K, dtype="<f8")
+                assert k.shape == (C,)
+                f.write(struct.pack("<I", int(step)))
+                f.write(k.tobytes())
 
 
 class RefOutput:
@@ -105,15 +120,18 @@ def read_output(path: str, genome_blocks: int = 0) -> RefOutput:
 
 def run_reference(kind: str, workdir: str, grid: Grid, agents: Agents, actions: Sequence[Action],
                   steps: int, seed: int, genetics: Genetics = Genetics(), dump_every: int = 0,
-                  threads: int = 0, timeout: float = 3600.0) -> RefOutput:
-    """Run qhg_ref_well or qhg_ref_philox on the given input."""
+                  threads: int = 0, timeout: float = 3600.0, weights=None, k_changes=()) -> RefOutput:
+    """Run qhg_ref_well or qhg_ref_philox on the given input; `weights`
+    (C x 7 cumulative) replace the weights from K, `k_changes` holds
+    (step, K) pairs: K from that step on."""
     exe = ref_program(kind)
     if not os.path.exists(exe):
         raise FileNotFoundError(exe)
     os.makedirs(workdir, exist_ok=True)
     pin = os.path.join(workdir, f"in_{kind}_{seed}.bin")
     pout = os.path.join(workdir, f"out_{kind}_{seed}.bin")
-    write_input(pin, grid, agents, actions, steps, seed, genetics, dump_every)
+    write_input(pin, grid, agents, actions, steps, seed, genetics, dump_every, weights=weights,
+                k_changes=k_changes)
     env = dict(os.environ)
     if threads > 0:
         env["OMP_NUM_THREADS"] = str(threads)

@@ -69,6 +69,8 @@ struct qhg_run {
     uint32_t *d_cmove = nullptr;
     int32_t *d_occ = nullptr;       // first step of each cell's occupation (QHG_FLAG_TRACK_OCCUPANCY)
     std::vector<int32_t> h_nbr;
+    std::vector<uint8_t> h_nnbr;
+    bool w_given = false;        // move weights given (qhg_gpu_set_move_weights), not from K
     // agents (ping-pong)
     uint32_t cap = 0;
     int64_t *d_id[2] = {nullptr, nullptr};
@@ -419,23 +421,53 @@ int qhg_host_grid_tables(int C, const int32_t *nbr6, const uint8_t *nnbr, const 
             W[(size_t)c * 7 + i + 1] = dW;
         }
     }
+    return qhg_host_move_tables(C, nnbr, W.data(), wthr, cmove, err);
+}
+
+// WeightedMove's thresholds from cumulative weights W (C x 7, W[c][0] the
+// cell's own, W[c][i+1] = W[c][i] + neighbour i's; WeightedMove::execute,
+// actions/WeightedMove.cpp:57-80).  A cell with W[c][0] == W[c][n] draws its
+// direction with wrandi (bit 16 of its move word).  Otherwise the agent goes
+// to the first j with dR2 = wrandd() * W[c][n] < W[c][j]; dR2 rises with the
+// draw u, so "dR2 < W[c][j]" holds exactly for u below T_j, the smallest u
+// with dR2 >= W[c][j].  The first j with u < T_j is the number of j whose
+// running maximum max(T_0..T_j) is <= u, which is what the device counts
+// (j = n always qualifies: dR2 < W[c][n]).  The running maximum makes this
+// exact for rows that are not monotone too; it needs W[c][n] > 0 and finite
+// weights, which the rows of any cell that is not all-equal must have.
+// wthr gets T per cell and slot; cmove's bit 16 is set here, its other bits
+// are left as they are.
+int qhg_host_move_tables(int C, const uint8_t *nnbr, const double *W, std::vector<uint64_t> &wthr,
+                         std::vector<uint32_t> &cmove, std::string &err) {
+    wthr.assign((size_t)C * 6, 0);
     for (int c = 0; c < C; c++) {
         const int nn = nnbr[c];
         const double *Wc = &W[(size_t)c * 7];
         const double Wn = Wc[nn];
+        cmove[c] &= ~(1u << 16);
         if (Wc[0] == Wn) {
             cmove[c] |= 1u << 16;
             continue;
         }
+        if (!(Wn > 0.0) || !std::isfinite(Wn)) {
+            err = "cell " + std::to_string(c) + ": total move weight not positive and finite";
+            return -1;
+        }
         auto f = [&](uint64_t u) { return ((1.0 * (double)u) / 4294967296.0) * Wn; };
+        uint64_t run = 0;
         for (int j = 0; j < nn; j++) {
             const double x = Wc[j];
+            if (!std::isfinite(x)) {
+                err = "cell " + std::to_string(c) + ": move weight not finite";
+                return -1;
+            }
             // smallest u in [0, 2^32] with f(u) >= x  (f(2^32) counts as +inf)
             double g = std::floor(x / Wn * 4294967296.0);
             uint64_t u = (g <= 0) ? 0ull : (g >= 4294967296.0 ? 4294967296ull : (uint64_t)g);
             while (u > 0 && f(u - 1) >= x) u--;
             while (u < 4294967296ull && f(u) < x) u++;
-            wthr[(size_t)c * 6 + j] = u;
+            run = std::max(run, u);
+            wthr[(size_t)c * 6 + j] = run;
         }
     }
     return 0;
@@ -575,7 +607,9 @@ extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_
     CUDA_TRY(cudaMemsetAsync(r->d_tflag, 0, (size_t)ntiles * sizeof(uint32_t), r->stream));
     CUDA_TRY(cudaStreamSynchronize(r->stream));
     r->h_nbr.assign(nbr6, nbr6 + (size_t)C * 6);
+    r->h_nnbr.assign(nnbr, nnbr + C);
     r->h_K.assign(K, K + C);
+    r->w_given = false;
     r->C = C;
     r->P.num_cells = C;
     r->grid_ok = true;
@@ -867,6 +901,77 @@ extern "C" int qhg_gpu_sync(qhg_run *r) {
     if (r == nullptr) return fail(QHG_ERR_ARG, "null run");
     CUDA_TRY(cudaSetDevice(r->desc.device));
     return pull_state(r);
+}
+
+// The current table's per-cell constants after K or the move weights changed
+// (nothing to do before agents are uploaded: the upload derives them).
+static int refresh_cells(qhg_run *r) {
+    if (!r->agents_ok || r->h_rs->n_nonempty == 0u) {
+        CUDA_TRY(cudaStreamSynchronize(r->stream));
+        return QHG_OK;
+    }
+    const int cur = r->cur;
+    const int grid = (int)std::min<uint32_t>((r->h_rs->n_nonempty + 255u) / 256u, 4096u);
+    const int le = qhg_launch_refresh_cells(&r->P, r->d_rs, r->d_ne[cur], r->d_nes[cur], r->d_K, r->d_cmove,
+                                            r->d_vthr[cur], r->d_necm[cur], grid, r->stream);
+    if (le != 0) return fail(QHG_ERR_CUDA, std::string("launch: ") + cudaGetErrorString((cudaError_t)le));
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    return QHG_OK;
+}
+
+extern "C" int qhg_gpu_set_capacity(qhg_run *r, const double *K) {
+    if (r == nullptr || K == nullptr) return fail(QHG_ERR_ARG, "null argument");
+    if (!r->grid_ok) return fail(QHG_ERR_STATE, "upload the grid first");
+    CUDA_TRY(cudaSetDevice(r->desc.device));
+    const int C = r->C;
+    // weights that follow K are derived again, as an always-updating
+    // SingleEvaluator over K does at the next initialize
+    const bool tables = r->P.has_wmove && !r->w_given;
+    std::vector<uint32_t> rev, cmove;
+    std::vector<uint64_t> wthr;
+    if (tables) {
+        std::string err;
+        if (qhg_host_grid_tables(C, r->h_nbr.data(), r->h_nnbr.data(), K, true, rev, wthr, cmove, err) != 0) {
+            return fail(QHG_ERR_ARG, err);
+        }
+    }
+    int rc = pull_state(r);   // the run's steps so far are done (or their error is reported)
+    if (rc != QHG_OK) return rc;
+    CUDA_TRY(cudaMemcpyAsync(r->d_K, K, (size_t)C * sizeof(double), cudaMemcpyHostToDevice, r->stream));
+    if (tables) {
+        CUDA_TRY(cudaMemcpyAsync(r->d_wthr, wthr.data(), (size_t)C * 6 * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                                 r->stream));
+        CUDA_TRY(cudaMemcpyAsync(r->d_cmove, cmove.data(), (size_t)C * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                 r->stream));
+    }
+    r->h_K.assign(K, K + C);
+    return refresh_cells(r);
+}
+
+extern "C" int qhg_gpu_set_move_weights(qhg_run *r, const double *cumw7) {
+    if (r == nullptr || cumw7 == nullptr) return fail(QHG_ERR_ARG, "null argument");
+    if (!r->grid_ok) return fail(QHG_ERR_STATE, "upload the grid first");
+    CUDA_TRY(cudaSetDevice(r->desc.device));
+    const int C = r->C;
+    std::vector<uint32_t> rev, cmove;
+    std::vector<uint64_t> wthr;
+    {
+        std::string err;
+        // the neighbour bits of the move words, then the weights' thresholds
+        if (qhg_host_grid_tables(C, r->h_nbr.data(), r->h_nnbr.data(), r->h_K.data(), false, rev, wthr, cmove,
+                                 err) != 0 ||
+            qhg_host_move_tables(C, r->h_nnbr.data(), cumw7, wthr, cmove, err) != 0) {
+            return fail(QHG_ERR_ARG, err);
+        }
+    }
+    int rc = pull_state(r);
+    if (rc != QHG_OK) return rc;
+    CUDA_TRY(cudaMemcpyAsync(r->d_wthr, wthr.data(), (size_t)C * 6 * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                             r->stream));
+    CUDA_TRY(cudaMemcpyAsync(r->d_cmove, cmove.data(), (size_t)C * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                             r->stream));
+    r->w_given = true;
+    return refresh_cells(r);
 }
 
 extern "C" int qhg_gpu_num_agents(qhg_run *r, int64_t *n) {

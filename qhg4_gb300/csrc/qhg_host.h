@@ -14,7 +14,12 @@ int qhg_host_actions(qhg::StepConst &P, int n, const int32_t *types, const doubl
 int qhg_host_grid_tables(int C, const int32_t *nbr6, const uint8_t *nnbr, const double *K, bool wm,
                          std::vector<uint32_t> &rev, std::vector<uint64_t> &wthr, std::vector<uint32_t> &cmove,
                          std::string &err);
+int qhg_host_move_tables(int C, const uint8_t *nnbr, const double *W, std::vector<uint64_t> &wthr,
+                         std::vector<uint32_t> &cmove, std::string &err);
 
+extern "C" int qhg_launch_refresh_cells(const qhg::StepConst *P, const qhg::RunState *rs, const uint32_t *nonempty,
+                                        const uint32_t *ne_start, const double *K, const uint32_t *cmove,
+                                        ulonglong2 *vthr, uint32_t *necm, int grid, cudaStream_t stream);
 extern "C" int qhg_launch_step(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
                                const qhg::BatchBuffers *BB, const qhg::LaunchShape *L, cudaStream_t stream);
 extern "C" int qhg_launch_step_timed(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,

@@ -2545,6 +2545,24 @@ __global__ void k_batch_stage(uint32_t s0, uint32_t n, uint32_t cell0, uint32_t 
     if ((threadIdx.x & 31) == 0 && mx >= 0) atomicMax(reinterpret_cast<long long *>(&err[2]), mx);
 }
 
+// ------------------------------------------------------------------ refresh
+// After K or the move weights changed between steps (qhg_gpu_set_capacity,
+// qhg_gpu_set_move_weights): the current table's per-cell constants, which
+// the previous step's cell scan derived from the old values, are derived
+// again -- the Verhulst thresholds from the new K and the cell's count, the
+// move word from the new cmove -- by the cell's position in the non-empty list.
+__global__ void __launch_bounds__(256)
+k_refresh_cells(const StepConst P, const RunState *__restrict__ rs, const uint32_t *__restrict__ nonempty,
+                const uint32_t *__restrict__ ne_start, const double *__restrict__ K,
+                const uint32_t *__restrict__ cmove, ulonglong2 *__restrict__ vthr, uint32_t *__restrict__ necm) {
+    const uint32_t nne = rs->n_nonempty;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nne; i += gridDim.x * blockDim.x) {
+        const uint32_t c = nonempty[i];
+        if (P.n_verhulst > 0) vthr[i] = verhulst_thresholds(P.act[P.verhulst_act[0]], K[c], ne_start[i + 1] - ne_start[i]);
+        if (P.has_move) necm[i] = cmove[c];
+    }
+}
+
 // ------------------------------------------------------------------ upload
 // An upload on the device: the caller's columns are copied as they are into
 // staging buffers; k_upload_count counts the live agents of each cell (into
@@ -2632,6 +2650,14 @@ __global__ void k_run_cells(const uint32_t *__restrict__ nonempty, const uint32_
 }
 
 }  // namespace qhg
+
+extern "C" int qhg_launch_refresh_cells(const qhg::StepConst *P, const qhg::RunState *rs, const uint32_t *nonempty,
+                                        const uint32_t *ne_start, const double *K, const uint32_t *cmove,
+                                        ulonglong2 *vthr, uint32_t *necm, int grid, cudaStream_t stream) {
+    qhg::k_refresh_cells<<<std::max(1, grid), 256, 0, stream>>>(*P, rs, nonempty, ne_start, K, cmove, vthr, necm);
+    return (int)cudaGetLastError();
+}
+
 
 extern "C" int qhg_launch_run_cells(const uint32_t *nonempty, const uint32_t *ne_start, uint32_t n_nonempty,
                                     uint32_t cell0, uint32_t cell1, uint32_t row0, uint32_t nrows,

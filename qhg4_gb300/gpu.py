@@ -39,7 +39,7 @@ EXPORTS = [
     "qhg_batch_set_shape", "qhg_batch_get_shape", "qhg_batch_stream", "qhg_batch_destroy",
     "qhg_batch_live_history", "qhg_batch_snapshot_async", "qhg_batch_snapshot_wait",
     "qhg_host_buffer_alloc", "qhg_host_buffer_free", "qhg_gpu_next_id", "qhg_gpu_set_next_id",
-    "qhg_gpu_test_stall_scan", "qhg_gpu_occupancy",
+    "qhg_gpu_test_stall_scan", "qhg_gpu_occupancy", "qhg_gpu_set_capacity", "qhg_gpu_set_move_weights",
 ]
 
 
@@ -133,6 +133,8 @@ def load_library(path: str = LIB_PATH):
         "qhg_gpu_set_next_id": (I, [P, ct.c_int64]),
         "qhg_gpu_test_stall_scan": (I, [P, ct.c_int32]),
         "qhg_gpu_occupancy": (I, [P, P]),
+        "qhg_gpu_set_capacity": (I, [P, P]),
+        "qhg_gpu_set_move_weights": (I, [P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -239,6 +241,21 @@ class GpuRun:
         c = np.zeros(self.C, dtype=np.uint32)
         _check(_lib.qhg_gpu_counts(self.h, _p(c)))
         return c
+
+    def set_capacity(self, K: np.ndarray) -> None:
+        """A new K per cell from the next step on (VerhulstVarK; the move
+        weights follow unless weights were given)."""
+        k = np.ascontiguousarray(K, dtype=np.float64)
+        if k.shape != (self.C,):
+            raise ValueError("K needs one entry per cell")
+        _check(_lib.qhg_gpu_set_capacity(self.h, _p(k)))
+
+    def set_move_weights(self, W: np.ndarray) -> None:
+        """WeightedMove's cumulative weights (C x 7) from the next step on."""
+        w = np.ascontiguousarray(W, dtype=np.float64)
+        if w.shape != (self.C, 7):
+            raise ValueError("weights need shape (cells, 7)")
+        _check(_lib.qhg_gpu_set_move_weights(self.h, _p(w)))
 
     def occupancy(self) -> np.ndarray:
         """Per cell, the first step whose table holds an agent there (-1 none);

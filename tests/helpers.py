@@ -37,3 +37,26 @@ def case_config1(n=8, N=15000, seed=1):
 def case_config2(n=16, N=40000, seed=3, grid_seed=7):
     g = terrain_grid(n, seed=grid_seed)
     return g, make_agents(g, N, seed=seed, age_max=60.0, proportional_to_K=True), config2_actions()
+
+
+def move_weights(grid, seed, nonmonotone=0.1, equal=0.05):
+    """Cumulative WeightedMove weights (C x 7) like a MultiEvaluator leaves
+    them: W[c][0] the cell's own weight, W[c][i+1] = W[c][i] + the weight of
+    neighbour i.  A fraction of the cells has a negative contribution (the
+    cumulated row is not monotone; a combination weight can be negative),
+    another fraction all contributions zero (all weights equal); the total
+    W[c][n] stays positive elsewhere."""
+    rng = np.random.default_rng(seed)
+    C = grid.num_cells
+    inc = rng.uniform(0.0, 1.0, size=(C, 7))
+    inc[rng.random((C, 7)) < 0.15] = 0.0
+    neg = rng.random(C) < nonmonotone
+    inc[neg, 1 + rng.integers(0, 5, size=int(neg.sum()))] = -rng.uniform(0.1, 0.6, size=int(neg.sum()))
+    W = np.cumsum(inc, axis=1)
+    eq = rng.random(C) < equal
+    W[eq] = W[eq, :1]
+    nn = grid.nnbr.astype(np.int64)
+    tot = W[np.arange(C), nn]
+    low = (~eq) & (tot <= 0.05)
+    W[low] += 1.0
+    return W

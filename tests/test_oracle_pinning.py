@@ -68,3 +68,44 @@ def test_port_oracle_atan_death_against_reference_build(tmp_path, atan_params):
     d = table_diff(r.agents(), ref.agents)
     assert d is None, d
     assert np.array_equal(st, ref.stats)
+
+
+@pytest.mark.skipif(not os.path.exists(ref_program("philox")), reason="reference build not present")
+@pytest.mark.parametrize("given_weights,k_changes", [(True, False), (False, True), (True, True)],
+                         ids=["weights", "capacity", "both"])
+def test_port_oracle_environment_updates_against_reference_build(tmp_path, given_weights, k_changes):
+    """WeightedMove on cumulative weights given from outside (what
+    FlatExpPop's MultiEvaluator leaves, populations/FlatExpPop.cpp:43-56),
+    including rows that are not monotone and rows of equal weights, and K
+    changed between steps (NPPCapacity's output after an environment event),
+    against the reference's classes."""
+    from qhg4_gb300.spec import config2_actions
+    from qhg4_gb300.workload import make_agents, terrain_grid
+    from helpers import move_weights
+    grid = terrain_grid(9, seed=91)
+    agents = make_agents(grid, 9000, seed=92, age_max=70.0, proportional_to_K=True)
+    acts = config2_actions(b0=0.3, d0=0.03, move_p=0.3)
+    W = move_weights(grid, 93) if given_weights else None
+    rng = np.random.default_rng(94)
+    changes = []
+    if k_changes:
+        changes = [(5, grid.K * rng.uniform(0.3, 1.5, grid.num_cells)),
+                   (12, np.where(rng.random(grid.num_cells) < 0.2, 0.0, grid.K * 1.2))]
+    ref = run_reference("philox", str(tmp_path), grid, agents, acts, 18, 2718, threads=2, weights=W,
+                        k_changes=changes)
+    r = port.OracleRun(grid, acts, 2718)
+    r.load(agents)
+    if W is not None:
+        r.set_move_weights(W)
+    done, st = 0, []
+    for step, K in changes + [(18, None)]:
+        st.append(r.step(step - done))
+        done = step
+        if K is not None:
+            r.set_capacity(K)
+    st = np.concatenate(st)
+    assert ref.draw_errors == 0
+    d = table_diff(r.agents(), ref.agents)
+    assert d is None, d
+    assert np.array_equal(st, ref.stats)
+    assert st[:, 3].sum() > 0
