@@ -14,9 +14,15 @@
  *                  QHG_ACT_* slots), uploads the cell grid (SCellGrid
  *                  neighbours), the capacity array and the live agents of the
  *                  LayerBuf
- *   initializeStep, doActions
- *                  nothing: the GPU step does pairing, rates, every action's
- *                  execute, births, deaths, moves and counts
+ *   initializeStep runs the initialize of the environment evaluators that
+ *                  stay on the host (addHostEvaluator: the reference's own
+ *                  NPPCapacity, SingleEvaluator, MultiEvaluator objects) and,
+ *                  after an environment event, hands the arrays they fill
+ *                  (setGpuEnvironment: K per cell, cumulative move weights)
+ *                  to the GPU run; nothing else: the GPU step does pairing,
+ *                  rates, every action's execute, births, deaths, moves and
+ *                  counts
+ *   doActions      nothing
  *   finalizeStep   one qhg_gpu_step; counts are read back when asked for
  *   updateNumAgentsPerCell, updateTotal
  *                  per-cell counts and total from the GPU
@@ -50,7 +56,7 @@ public:
     GpuPop(SCellGrid *pCG, PopFinder *pPopFinder, int iLayerSize, IDGen **apIDG, uint32_t *aulState,
            uint *aiSeeds)
         : SPopulation<T>(pCG, pPopFinder, iLayerSize, apIDG, aulState, aiSeeds),
-          m_pRun(NULL), m_bStale(false), m_iDevice(0) {
+          m_pRun(NULL), m_bStale(false), m_iDevice(0), m_adEnvK(NULL), m_adEnvW(NULL), m_bEnvDirty(true) {
         // the GPU run's seed from the population's generator state
         m_ulSeed = (aulState != NULL) ? ((uint64_t)aulState[0] | ((uint64_t)aulState[1] << 32)) : 0;
     }
@@ -73,6 +79,18 @@ public:
     // capacity per cell (VerhulstVarK's K, WeightedMove's weights)
     void setGpuCapacity(const double *adK, int iNumCells) { m_vK.assign(adK, adK + iNumCells); }
     void setGpuDevice(int iDevice) { m_iDevice = iDevice; }
+    // an environment evaluator kept on the host (not owned): its initialize
+    // runs at each initializeStep, as SPopulation's does for every action
+    void addHostEvaluator(Action<T> *pA) { m_vHostEvals.push_back(pA); }
+    // the arrays the host evaluators fill (not owned): K per cell (NULL:
+    // none) and WeightedMove's cumulative weights, cells x 7 (NULL: the
+    // weights follow K); handed to the GPU run before the first step and
+    // after every environment event
+    void setGpuEnvironment(const double *adK, const double *adCumW) {
+        m_adEnvK = adK;
+        m_adEnvW = adCumW;
+        m_bEnvDirty = true;
+    }
 
     virtual int preLoop() {
         int iResult = SPopulation<T>::preLoop();
@@ -80,7 +98,27 @@ public:
         return iResult;
     }
 
-    virtual int initializeStep(float fTime) { return (m_pRun != NULL) ? 0 : -1; }
+    virtual int initializeStep(float fTime) {
+        if (m_pRun == NULL) return -1;
+        int iResult = 0;
+        for (size_t i = 0; i < m_vHostEvals.size(); i++) {
+            iResult += m_vHostEvals[i]->initialize(fTime);
+        }
+        if ((iResult == 0) && m_bEnvDirty) {
+            if ((m_adEnvW != NULL) && (qhg_gpu_set_move_weights(m_pRun, m_adEnvW) != QHG_OK)) iResult = -1;
+            if ((m_adEnvK != NULL) && (qhg_gpu_set_capacity(m_pRun, m_adEnvK) != QHG_OK)) iResult = -1;
+            m_bEnvDirty = false;
+        }
+        return iResult;
+    }
+
+    // an environment event (climate, vegetation, geography) makes the host
+    // evaluators recompute their arrays at the next initialize; they are
+    // handed to the GPU run then
+    virtual int updateEvent(int iEventID, char *pData, float fT) {
+        m_bEnvDirty = true;
+        return SPopulation<T>::updateEvent(iEventID, pData, fT);
+    }
     virtual int doActions(uint iPrio, float fTime) { return 0; }
 
     virtual int finalizeStep() {
@@ -238,6 +276,10 @@ protected:
     uint64_t m_ulSeed;
     std::vector<GpuAction> m_vActions;
     std::vector<double> m_vK;
+    std::vector<Action<T> *> m_vHostEvals;
+    const double *m_adEnvK;
+    const double *m_adEnvW;
+    bool m_bEnvDirty;
 };
 
 #endif
