@@ -170,6 +170,31 @@ int qhg_gpu_stats(qhg_run *run, int32_t nsteps, qhg_step_stats *out);
  * one population: occupation masks that change to non-zero are recorded,
  * masks of zero are ignored. */
 int qhg_gpu_occupancy(qhg_run *run, int32_t *first_step);
+/* MoveStats (actions/MoveStats.cpp, actions/MoveStats.h): per cell the hops,
+ * the distance travelled and the time of arrival of the agents that reached
+ * it, with the reference's modes MODE_STAT_FIRST / MIN / LAST:
+ *   QHG_MOVESTATS_FIRST  the first arrival (lowest mover ID of the first
+ *                        step that reaches the cell)
+ *   QHG_MOVESTATS_MIN    fewest hops, shortest distance, time of the first
+ *                        arrival
+ *   QHG_MOVESTATS_LAST   the latest arrival (highest mover ID of the last
+ *                        step with arrivals)
+ * A move from f to t offers hops[f] + 1 and dist[f] + d(f, t), as
+ * MoveStats::finalize does on one thread (its per-thread merge makes more
+ * threads order-dependent), with moves in agent-ID order instead of slot
+ * order; every registered move counts, also one whose agent a later action
+ * of the step killed.  Distances: spherdistDeg over the cells' lon/lat in
+ * degrees on a sphere of `radius`, or cartdist over x = lon, y = lat when
+ * `cartesian` (utils/geomutils.cpp:311-386).  Enabling (re)starts the
+ * statistics from the current table (MoveStats::initializeOccupied: its
+ * cells 0, the others -1) and so does each later qhg_gpu_upload_agents.
+ * qhg_gpu_move_stats copies C entries each.  Single runs only. */
+#define QHG_MOVESTATS_FIRST   0
+#define QHG_MOVESTATS_MIN     1
+#define QHG_MOVESTATS_LAST    2
+int qhg_gpu_move_stats_enable(qhg_run *run, int32_t mode, const double *lon, const double *lat, double radius,
+                              int32_t cartesian);
+int qhg_gpu_move_stats(qhg_run *run, int32_t *hops, double *dist, double *time);
 /* birth log (QHG_FLAG_LOG_BIRTHS): rows (baby, mother, father) */
 int qhg_gpu_birth_log(qhg_run *run, int64_t *baby, int64_t *mother, int64_t *father, int64_t cap,
                       int64_t *n);

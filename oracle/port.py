@@ -61,6 +61,10 @@ def _load():
     lib.qo_set_capacity.argtypes = [P, P]
     lib.qo_set_move_weights.restype = ct.c_int
     lib.qo_set_move_weights.argtypes = [P, P]
+    lib.qo_move_stats_enable.restype = ct.c_int
+    lib.qo_move_stats_enable.argtypes = [P, ct.c_int, P, P, ct.c_double, ct.c_int]
+    lib.qo_move_stats.restype = ct.c_int
+    lib.qo_move_stats.argtypes = [P, P, P, P]
     lib.qo_set_threads.argtypes = [ct.c_int]
     lib.qo_max_threads.restype = ct.c_int
     lib.qo_destroy.argtypes = [P]
@@ -137,6 +141,24 @@ class OracleRun:
         w = np.ascontiguousarray(W, dtype=np.float64)
         assert w.shape == (self.C, 7)
         _load().qo_set_move_weights(self.h, _p(w))
+
+    def move_stats_enable(self, mode: int, lon: np.ndarray, lat: np.ndarray, radius: float = 1.0,
+                          cartesian: bool = False) -> None:
+        """MoveStats (0 first, 1 min, 2 last) over the given cell coordinates."""
+        self._ms = (np.ascontiguousarray(lon, dtype=np.float64), np.ascontiguousarray(lat, dtype=np.float64))
+        rc = _load().qo_move_stats_enable(self.h, int(mode), _p(self._ms[0]), _p(self._ms[1]),
+                                          ct.c_double(radius), 1 if cartesian else 0)
+        if rc != 0:
+            raise ValueError("bad MoveStats mode")
+
+    def move_stats(self):
+        """Per cell: hops, distance and time of MoveStats."""
+        h = np.zeros(self.C, np.int32)
+        d = np.zeros(self.C, np.float64)
+        t = np.zeros(self.C, np.float64)
+        if _load().qo_move_stats(self.h, _p(h), _p(d), _p(t)) != 0:
+            raise ValueError("MoveStats not enabled")
+        return h, d, t
 
     def num_agents(self) -> int:
         return int(_load().qo_num_agents(self.h))

@@ -99,6 +99,16 @@ typedef struct {
     int64_t *blog;      /* birth log: baby, mother, father */
     int64_t blog_n, blog_cap;
     int log_births;
+    /* MoveStats (actions/MoveStats.h): mode -1 none, 0 first, 1 min, 2 last;
+     * cell coordinates (degrees, or plane x/y), the definitive per-cell hops,
+     * distance and time, and the temporaries that persist between steps */
+    int ms_mode;
+    int ms_cart;
+    double ms_R;
+    double *ms_lon, *ms_lat;
+    int32_t *ms_hops, *ms_thops;
+    double *ms_dist, *ms_time, *ms_tdist, *ms_ttime;
+    uint8_t *ms_changed;
 } qo_run;
 
 /* ---------------------------------------------------------------- draws */
@@ -304,6 +314,47 @@ static void weights_from_K(qo_run *r) {
     }
 }
 
+/* ------------------------------------------------------------ MoveStats */
+/* spherdist / spherdistDeg and cartdist (utils/geomutils.cpp:311-386),
+ * restated in the same operation order */
+static double ms_spherdist(double dLon1, double dLat1, double dLon2, double dLat2, double dR) {
+    double dX1 = cos(dLon1) * cos(dLat1);
+    double dY1 = sin(dLon1) * cos(dLat1);
+    double dZ1 = sin(dLat1);
+    double dX2 = cos(dLon2) * cos(dLat2);
+    double dY2 = sin(dLon2) * cos(dLat2);
+    double dZ2 = sin(dLat2);
+    double dProd = dX1 * dX2 + dY1 * dY2 + dZ1 * dZ2;
+    if (dProd > 1) {
+        dProd = 1;
+    } else if (dProd < -1) {
+        dProd = -1;
+    }
+    return dR * acos(dProd);
+}
+
+static double ms_distance(const qo_run *r, int a, int b) {
+    if (r->ms_cart) {
+        double dX = r->ms_lon[b] - r->ms_lon[a], dY = r->ms_lat[b] - r->ms_lat[a];
+        return 1.0 * sqrt(dX * dX + dY * dY);
+    }
+    return ms_spherdist(r->ms_lon[a] * QO_PI / 180, r->ms_lat[a] * QO_PI / 180,
+                        r->ms_lon[b] * QO_PI / 180, r->ms_lat[b] * QO_PI / 180, r->ms_R);
+}
+
+/* MoveStats::preLoop / initializeOccupied (actions/MoveStats.cpp:96-175):
+ * everything -1, the cells holding agents 0 */
+static void ms_init(qo_run *r) {
+    for (int c = 0; c < r->C; c++) {
+        r->ms_hops[c] = -1; r->ms_dist[c] = -1; r->ms_time[c] = -1;
+        r->ms_thops[c] = -1; r->ms_tdist[c] = -1; r->ms_ttime[c] = -1;
+    }
+    for (int64_t i = 0; i < r->n; i++) {
+        int c = r->cell[i];
+        r->ms_hops[c] = 0; r->ms_dist[c] = 0; r->ms_time[c] = 0;
+    }
+}
+
 /* ------------------------------------------------------------ create */
 qo_run *qo_create(uint64_t seed, int n_act, const int32_t *types, const double *params,
                   int genome_size, int num_crossover, double mutation_rate,
@@ -311,6 +362,7 @@ qo_run *qo_create(uint64_t seed, int n_act, const int32_t *types, const double *
     if (n_act < 0 || n_act > MAX_ACTIONS || C <= 0) return NULL;
     qo_run *r = (qo_run *)calloc(1, sizeof(qo_run));
     r->seed = seed;
+    r->ms_mode = -1;
     r->n_act = n_act;
     uint32_t w = 0;
     for (int a = 0; a < n_act; a++) {
@@ -417,6 +469,7 @@ int qo_load(qo_run *r, int64_t N, const int64_t *id, const int32_t *cell, const 
     r->next_id = maxid + 1;
     r->step = first_step;
     recount(r);
+    if (r->ms_mode >= 0) ms_init(r);
     return 0;
 }
 
@@ -614,6 +667,44 @@ int qo_step(qo_run *r, int nsteps, uint64_t *stats_out) {
             out[i].dead = !alive;
         }
 
+        /* ---- MoveStats::finalize (actions/MoveStats.cpp:183-256) as one
+         * thread runs it, moves in agent-ID order; every registered move
+         * counts, also that of an agent a later action killed */
+        if (r->ms_mode >= 0) {
+            const int mode = r->ms_mode;
+            memset(r->ms_changed, 0, (size_t)C);
+            for (int64_t i = 0; i < n; i++) {
+                if (out[i].move_to < 0) continue;
+                const int from = r->cell[i], to = out[i].move_to;
+                int32_t iNewHops = r->ms_hops[from] + 1;
+                double dNewDist = r->ms_dist[from] + ms_distance(r, from, to);
+                double dNewTime = fT;
+                if ((r->ms_thops[to] < 0) || (mode == 2)) {
+                    r->ms_thops[to] = iNewHops;
+                    r->ms_tdist[to] = dNewDist;
+                    r->ms_ttime[to] = dNewTime;
+                    r->ms_changed[to] = 1;
+                } else if (mode == 1) {
+                    if (iNewHops < r->ms_thops[to]) r->ms_thops[to] = iNewHops;
+                    if (dNewDist < r->ms_tdist[to]) r->ms_tdist[to] = dNewDist;
+                    r->ms_ttime[to] = dNewTime;
+                    r->ms_changed[to] = 1;
+                }
+            }
+            for (int c = 0; c < C; c++) {
+                if (!r->ms_changed[c]) continue;
+                if ((r->ms_hops[c] < 0) || (mode == 2)) {
+                    r->ms_hops[c] = r->ms_thops[c];
+                    r->ms_dist[c] = r->ms_tdist[c];
+                    r->ms_time[c] = r->ms_ttime[c];
+                } else if (mode == 1) {
+                    if (r->ms_thops[c] < r->ms_hops[c]) r->ms_hops[c] = r->ms_thops[c];
+                    if (r->ms_tdist[c] < r->ms_dist[c]) r->ms_dist[c] = r->ms_tdist[c];
+                    if (r->ms_ttime[c] < r->ms_time[c]) r->ms_time[c] = r->ms_ttime[c];
+                }
+            }
+        }
+
         /* ---- finalizeStep: births in (cell, mother ID) order */
         uint32_t *bs = (uint32_t *)calloc((size_t)C + 1, sizeof(uint32_t));
         int64_t nb = 0;
@@ -745,6 +836,36 @@ int qo_binomial_table(const qo_run *r, double *out, int cap) {
 
 void qo_set_log_births(qo_run *r, int on) { r->log_births = on; }
 
+/* MoveStats with the given mode (0 first, 1 min, 2 last) and cell
+ * coordinates (lon/lat in degrees on a sphere of radius R, or x/y on a plane
+ * when cartesian); initialised from the loaded agents, if any */
+int qo_move_stats_enable(qo_run *r, int mode, const double *lon, const double *lat, double R, int cartesian) {
+    if (mode < 0 || mode > 2) return -1;
+    const size_t C = (size_t)r->C;
+    if (r->ms_lon == NULL) {
+        r->ms_lon = (double *)malloc(C * sizeof(double)); r->ms_lat = (double *)malloc(C * sizeof(double));
+        r->ms_hops = (int32_t *)malloc(C * sizeof(int32_t)); r->ms_thops = (int32_t *)malloc(C * sizeof(int32_t));
+        r->ms_dist = (double *)malloc(C * sizeof(double)); r->ms_time = (double *)malloc(C * sizeof(double));
+        r->ms_tdist = (double *)malloc(C * sizeof(double)); r->ms_ttime = (double *)malloc(C * sizeof(double));
+        r->ms_changed = (uint8_t *)malloc(C);
+    }
+    memcpy(r->ms_lon, lon, C * sizeof(double));
+    memcpy(r->ms_lat, lat, C * sizeof(double));
+    r->ms_R = R;
+    r->ms_cart = cartesian;
+    r->ms_mode = mode;
+    ms_init(r);
+    return 0;
+}
+
+int qo_move_stats(const qo_run *r, int32_t *hops, double *dist, double *time) {
+    if (r->ms_mode < 0) return -1;
+    memcpy(hops, r->ms_hops, (size_t)r->C * sizeof(int32_t));
+    memcpy(dist, r->ms_dist, (size_t)r->C * sizeof(double));
+    memcpy(time, r->ms_time, (size_t)r->C * sizeof(double));
+    return 0;
+}
+
 /* A new K per cell from the next step on: VerhulstVarK's rates are computed
  * from K at each step's initialize (actions/LinearBirth.cpp:90-112,
  * actions/LinearDeath.cpp:92-122).  Unless weights were given, WeightedMove's
@@ -783,6 +904,8 @@ int qo_max_threads(void) {
 void qo_destroy(qo_run *r) {
     if (r == NULL) return;
     free(r->nbr); free(r->nnbr); free(r->K); free(r->W); free(r->count); free(r->B); free(r->D);
+    free(r->ms_lon); free(r->ms_lat); free(r->ms_hops); free(r->ms_thops); free(r->ms_dist);
+    free(r->ms_time); free(r->ms_tdist); free(r->ms_ttime); free(r->ms_changed);
     free(r->id); free(r->cell); free(r->birth); free(r->age); free(r->lastb); free(r->gender);
     free(r->state); free(r->genome); free(r->bino); free(r->blog); free(r->stats);
     free(r);

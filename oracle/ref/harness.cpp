@@ -48,6 +48,7 @@
 #include "WeightedMove.cpp"
 #include "SingleEvaluator.cpp"
 #include "RandomPair.cpp"
+#include "MoveStats.cpp"
 #include "BitGeneUtils.h"
 #include "BinomialDist.h"
 #include "Genetics.cpp"
@@ -175,6 +176,15 @@ protected:
 
 /* ---------------------------------------------------------------------- */
 /* Genetics with access to init() (protected in actions/Genetics.h) */
+/* the reference's MoveStats with its per-cell results readable */
+class HarnessMoveStats : public MoveStats<RefAgent> {
+public:
+    HarnessMoveStats(SPopulation<RefAgent> *pPop, SCellGrid *pCG) : MoveStats<RefAgent>(pPop, pCG, "") {}
+    const int *hops() const { return this->m_aiHops; }
+    const double *dist() const { return this->m_adDist; }
+    const double *time() const { return this->m_adTime; }
+};
+
 class HarnessGenetics : public Genetics<RefAgent, BitGeneUtils> {
 public:
     HarnessGenetics(SPopulation<RefAgent> *pPop, SCellGrid *pCG, LBController *pAC,
@@ -217,8 +227,11 @@ public:
     /* adGivenW: WeightedMove's cumulative weights as given (C x 7, what a
      * MultiEvaluator leaves, actions/MultiEvaluator.cpp:221-255), or NULL for
      * weights from K through an always-updating SingleEvaluator */
+    /* iMoveStatsMode >= 0: a MoveStats action with that mode (the grid must
+     * carry a Geography) */
     int setup(const std::vector<ActionSpec> &vSpecs, const double *adK,
-              int iGenomeSize, int iNumCrossOvers, double dMutRate, const double *adGivenW) {
+              int iGenomeSize, int iNumCrossOvers, double dMutRate, const double *adGivenW,
+              int iMoveStatsMode) {
         int C = (int)m_pCG->m_iNumCells;
         m_adK = new double[C];
         memcpy(m_adK, adK, C*sizeof(double));
@@ -314,6 +327,19 @@ public:
                 m_vSpecs.push_back(s);
                 m_vSpecActions.push_back(pA);
             }
+        }
+        if ((iResult == 0) && (iMoveStatsMode >= 0)) {
+            m_pMoveStats = new HarnessMoveStats(this, m_pCG);
+            ModuleComplex mc;
+            char buf[64];
+            snprintf(buf, 64, "%d", iMoveStatsMode); mc.addParam(ATTR_MOVESTATS_MODE_NAME, buf);
+            if (m_pMoveStats->tryGetAttributes(&mc) != 0) {
+                fprintf(stderr, "MoveStats tryGetAttributes failed\n");
+                iResult = -1;
+            }
+            m_vOwned.push_back(m_pMoveStats);
+            m_prio.addAction(m_pMoveStats);
+            m_mPrioInfo[m_pMoveStats->getActionName()] = 0;
         }
         if (iResult == 0) {
             iResult = setPrioList();
@@ -568,6 +594,7 @@ public:
     }
 
     HarnessGenetics *m_pGenetics;
+    HarnessMoveStats *m_pMoveStats = NULL;
     double *m_adK;
     double *m_adWeights;
     idtype m_iNextID;
@@ -655,6 +682,15 @@ int main(int argc, char *argv[]) {
             ok = rd(fIn, &vKCStep[k], 4, 1) && rd(fIn, vKC.data() + (size_t)k*C, 8, C);
         }
     }
+    /* optional: u32 movestats_mode + 1 (0 none), f64 radius, f64 lon[C], f64 lat[C] */
+    uint32_t iMSMode1 = 0;
+    double dMSRadius = 1.0;
+    std::vector<double> vLon, vLat;
+    if (ok && rd(fIn, &iMSMode1, 4, 1) && (iMSMode1 > 0)) {
+        vLon.resize(C);
+        vLat.resize(C);
+        ok = rd(fIn, &dMSRadius, 8, 1) && rd(fIn, vLon.data(), 8, C) && rd(fIn, vLat.data(), 8, C);
+    }
     fclose(fIn);
     if (!ok) { fprintf(stderr, "malformed input %s\n", argv[1]); return 2; }
 
@@ -671,6 +707,18 @@ int main(int argc, char *argv[]) {
         pCG->m_mIDIndexes[c] = c;
     }
 
+    /* MoveStats reads cell coordinates from the grid's Geography; no cell is ice */
+    Geography *pGeo = NULL;
+    if (iMSMode1 > 0) {
+        pGeo = new Geography(pCG, C, 6, dMSRadius);
+        for (uint32_t c = 0; c < C; c++) {
+            pGeo->m_adLongitude[c] = vLon[c];
+            pGeo->m_adLatitude[c] = vLat[c];
+            pGeo->m_abIce[c] = false;
+        }
+        pCG->setGeography(pGeo);
+    }
+
     int nThreads = omp_get_max_threads();
     IDGen **apIDG = new IDGen*[nThreads];
     for (int t = 0; t < nThreads; t++) apIDG[t] = new IDGen(0, t, nThreads);
@@ -680,7 +728,8 @@ int main(int argc, char *argv[]) {
     uint aiSeeds[NUM_SEEDS] = {0};
 
     OraclePop *pPop = new OraclePop(pCG, (iLayer > 0) ? (int)iLayer : 65536, apIDG, aulState, aiSeeds);
-    if (pPop->setup(vSpecs, vK.data(), (int)iGenomeSize, iCross, dMut, (iHasW == 1) ? vW.data() : NULL) != 0) {
+    if (pPop->setup(vSpecs, vK.data(), (int)iGenomeSize, iCross, dMut, (iHasW == 1) ? vW.data() : NULL,
+                    (int)iMSMode1 - 1) != 0) {
         fprintf(stderr, "population setup failed\n");
         return 3;
     }
@@ -778,6 +827,14 @@ int main(int argc, char *argv[]) {
     wr(fOut, &uAS, 8, 1);
     uint32_t uThr = (uint32_t)nThreads;
     wr(fOut, &uThr, 4, 1);
+    /* MoveStats: u32 present, i32 hops[C], f64 dist[C], f64 time[C] */
+    uint32_t uMS = (pPop->m_pMoveStats != NULL) ? 1 : 0;
+    wr(fOut, &uMS, 4, 1);
+    if (uMS) {
+        wr(fOut, pPop->m_pMoveStats->hops(), 4, C);
+        wr(fOut, pPop->m_pMoveStats->dist(), 8, C);
+        wr(fOut, pPop->m_pMoveStats->time(), 8, C);
+    }
     fclose(fOut);
     fprintf(stderr, "done: %u steps, %lu live, %.3f s, %.3g agent-steps/s, %d threads, draw errors %lu\n",
             nSteps, (unsigned long)nLive, dSec, dSec > 0 ? iAgentSteps / dSec : 0.0, nThreads, (unsigned long)nErr);

@@ -69,6 +69,14 @@ int qdf_writePolyLine(hid_t hSpeciesGroup, PolyLine *pPL, const std::string sPLP
 }
 int qdf_compareDataTypes(hid_t t1, hid_t t2) { (void)t1; (void)t2; return -1; }
 void qdf_closeDataSet(hid_t hDataSet) { (void)hDataSet; }
+int qdf_readArray(hid_t hGroup, const std::string sName, const uint iNum, void *vData, const hid_t hType) {
+    (void)hGroup; (void)sName; (void)iNum; (void)vData; (void)hType;
+    return -1;
+}
+int qdf_writeArray(hid_t hGroup, const std::string sName, const uint iNum, void *vData, const hid_t hType) {
+    (void)hGroup; (void)sName; (void)iNum; (void)vData; (void)hType;
+    return -1;
+}
 
 #ifdef QHG_PHILOX_TEST_BUILD
 /* the Philox test build has no WELL state to manage; these two helpers of

@@ -12,14 +12,17 @@ Input (little endian):
   u8 state[N], u64 genome[N*2*blocks]
   optional: u32 has_weights, f64 W[C*7] if has_weights == 1 (WeightedMove's
   cumulative weights as given, in place of the SingleEvaluator over K),
-  u32 n_k_changes, n_k_changes x (u32 step, f64 K[C]) (K from that step on)
+  u32 n_k_changes, n_k_changes x (u32 step, f64 K[C]) (K from that step on),
+  u32 movestats_mode + 1 (0 none), f64 radius, f64 lon[C], f64 lat[C]
+  (a MoveStats action over a Geography with these cell coordinates, degrees)
 Output:
   "QHGOUT01", u32 steps, u32 C, u64 stats[steps*4] (live, births, deaths, moves),
   u32 n_dumps, u32 dump_step[n_dumps], u32 counts[n_dumps*C],
   u64 n, i64 id[n], i32 cell[n], f32 birth[n], f32 age[n], f32 lastb[n],
   u8 gender[n], u8 state[n], u64 genome[n*2*blocks],
   u64 nb, i64 baby[nb], i64 mother[nb], i64 father[nb],
-  u64 draw_errors, f64 seconds, u64 agent_steps, u32 threads
+  u64 draw_errors, f64 seconds, u64 agent_steps, u32 threads,
+  u32 has_movestats, i32 hops[C], f64 dist[C], f64 time[C] if has_movestats
 """
 from __future__ import annotations
 
@@ -42,7 +45,7 @@ def ref_program(kind: str) -> str:
 
 def write_input(path: str, grid: Grid, agents: Agents, actions: Sequence[Action], steps: int,
                 seed: int, genetics: Genetics = Genetics(), dump_every: int = 0,
-                layer_size: int = 65536, weights=None, k_changes=()) -> None:
+                layer_size: int = 65536, weights=None, k_changes=(), move_stats=None) -> None:
     C = grid.num_cells
     N = len(agents)
     with open(path, "wb") as f:
@@ -65,7 +68,7 @@ def write_input(path: str, grid: Grid, agents: Agents, actions: Sequence[Action]
         f.write(np.ascontiguousarray(agents.state, dtype="u1").tobytes())
         if genetics.genome_size > 0:
             f.write(np.ascontiguousarray(agents.genome, dtype="<u8").tobytes())
-        if weights is not None or len(k_changes) > 0:
+        if weights is not None or len(k_changes) > 0 or move_stats is not None:
             f.write(struct.pack("<I", 1 if weights is not None else 0))
             if weights is not None:
                 w = np.ascontiguousarray(weights, dtype="<f8")
@@ -77,6 +80,11 @@ def write_input(path: str, grid: Grid, agents: Agents, actions: Sequence[Action]
                 assert k.shape == (C,)
                 f.write(struct.pack("<I", int(step)))
                 f.write(k.tobytes())
+            if move_stats is not None:
+                mode, lon, lat, radius = move_stats
+                f.write(struct.pack("<Id", int(mode) + 1, float(radius)))
+                f.write(np.ascontiguousarray(lon, dtype="<f8").tobytes())
+                f.write(np.ascontiguousarray(lat, dtype="<f8").tobytes())
 
 
 class RefOutput:
@@ -115,15 +123,20 @@ def read_output(path: str, genome_blocks: int = 0) -> RefOutput:
     o.seconds = float(take("<f8", 1)[0])
     o.agent_steps = int(take("<u8", 1)[0])
     o.threads = int(take("<u4", 1)[0])
+    o.move_stats = None
+    if pos < len(b) and int(take("<u4", 1)[0]) == 1:
+        o.move_stats = (take("<i4", int(C)), take("<f8", int(C)), take("<f8", int(C)))
     return o
 
 
 def run_reference(kind: str, workdir: str, grid: Grid, agents: Agents, actions: Sequence[Action],
                   steps: int, seed: int, genetics: Genetics = Genetics(), dump_every: int = 0,
-                  threads: int = 0, timeout: float = 3600.0, weights=None, k_changes=()) -> RefOutput:
+                  threads: int = 0, timeout: float = 3600.0, weights=None, k_changes=(),
+                  move_stats=None) -> RefOutput:
     """Run qhg_ref_well or qhg_ref_philox on the given input; `weights`
     (C x 7 cumulative) replace the weights from K, `k_changes` holds
-    (step, K) pairs: K from that step on."""
+    (step, K) pairs: K from that step on; `move_stats` = (mode, lon, lat,
+    radius) adds a MoveStats action."""
     exe = ref_program(kind)
     if not os.path.exists(exe):
         raise FileNotFoundError(exe)
@@ -131,7 +144,7 @@ def run_reference(kind: str, workdir: str, grid: Grid, agents: Agents, actions: 
     pin = os.path.join(workdir, f"in_{kind}_{seed}.bin")
     pout = os.path.join(workdir, f"out_{kind}_{seed}.bin")
     write_input(pin, grid, agents, actions, steps, seed, genetics, dump_every, weights=weights,
-                k_changes=k_changes)
+                k_changes=k_changes, move_stats=move_stats)
     env = dict(os.environ)
     if threads > 0:
         env["OMP_NUM_THREADS"] = str(threads)

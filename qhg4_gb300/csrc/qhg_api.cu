@@ -68,6 +68,12 @@ struct qhg_run {
     uint64_t *d_wthr = nullptr;
     uint32_t *d_cmove = nullptr;
     int32_t *d_occ = nullptr;       // first step of each cell's occupation (QHG_FLAG_TRACK_OCCUPANCY)
+    // MoveStats (qhg_gpu_move_stats_enable): mode (-1 off), state, candidates,
+    // distances per cell and neighbour slot
+    int32_t ms_mode = -1;
+    int32_t *d_ms_hops = nullptr, *d_ms_chops = nullptr;
+    double *d_ms_dist = nullptr, *d_ms_time = nullptr, *d_ms_D = nullptr;
+    unsigned long long *d_ms_cdist = nullptr, *d_ms_ckey = nullptr;
     std::vector<int32_t> h_nbr;
     std::vector<uint8_t> h_nnbr;
     bool w_given = false;        // move weights given (qhg_gpu_set_move_weights), not from K
@@ -551,6 +557,9 @@ extern "C" int qhg_gpu_create(const qhg_run_desc *desc, qhg_run **out) {
     return QHG_OK;
 }
 
+static int ms_reset(qhg_run *r);
+static void ms_free(qhg_run *r);
+
 extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_t *nnbr, const double *K,
                                    int32_t num_cells) {
     if (r == nullptr || nbr6 == nullptr || nnbr == nullptr || K == nullptr || num_cells <= 0) {
@@ -571,6 +580,7 @@ extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_
     cudaFree(r->d_wthr); cudaFree(r->d_cmove); cudaFree(r->d_occ);
     cudaFree(r->d_clsc); cudaFree(r->d_sbase); cudaFree(r->d_bbase); cudaFree(r->d_bidb);
     cudaFree(r->d_obase); cudaFree(r->d_tflag); cudaFree(r->d_tagg); cudaFree(r->d_tincl);
+    ms_free(r);
     r->d_vthr[0] = r->d_vthr[1] = nullptr;
     r->d_occ = nullptr;
     r->grid_ok = false;
@@ -756,6 +766,7 @@ extern "C" int qhg_gpu_upload_agents(qhg_run *r, const qhg_agents_soa *a, int64_
     r->upload_step = first_step;
     r->upload_max_id = maxid;
     r->agents_ok = true;
+    if (r->ms_mode >= 0) return ms_reset(r);
     return QHG_OK;
 }
 
@@ -773,6 +784,9 @@ static StepBuffers make_buffers(qhg_run *r, int cur) {
     B.nbr = r->d_nbr; B.nnbr = r->d_nnbr; B.rev = r->d_rev; B.K = r->d_K; B.vthr = r->d_vthr[cur]; B.vthr2 = r->d_vthr[nx]; B.wthr = r->d_wthr;
     B.cmove = r->d_cmove; B.necm = r->d_necm[cur]; B.necm2 = r->d_necm[nx];
     B.occ = r->d_occ;
+    B.ms_mode = r->ms_mode;
+    B.ms_hops = r->d_ms_hops; B.ms_dist = r->d_ms_dist; B.ms_time = r->d_ms_time;
+    B.ms_chops = r->d_ms_chops; B.ms_cdist = r->d_ms_cdist; B.ms_ckey = r->d_ms_ckey; B.ms_D = r->d_ms_D;
     B.outc = r->d_outc; B.father = r->d_father; B.brank = r->d_brank; B.clsc = r->d_clsc;
     B.sbase = r->d_sbase; B.bbase = r->d_bbase; B.bidbase = r->d_bidb; B.obase = r->d_obase;
     B.tile_flag = r->d_tflag; B.tile_agg = r->d_tagg; B.tile_incl = r->d_tincl;
@@ -974,6 +988,118 @@ extern "C" int qhg_gpu_set_move_weights(qhg_run *r, const double *cumw7) {
     return refresh_cells(r);
 }
 
+// ------------------------------------------------------------ MoveStats
+// spherdist / spherdistDeg and cartdist (utils/geomutils.cpp:311-386), in
+// the same operation order, for the distance from each cell to each of its
+// neighbours (MoveStats::finalize adds them up, actions/MoveStats.cpp:196-203)
+static double ms_spherdist(double dLon1, double dLat1, double dLon2, double dLat2, double dR) {
+    const double dX1 = std::cos(dLon1) * std::cos(dLat1);
+    const double dY1 = std::sin(dLon1) * std::cos(dLat1);
+    const double dZ1 = std::sin(dLat1);
+    const double dX2 = std::cos(dLon2) * std::cos(dLat2);
+    const double dY2 = std::sin(dLon2) * std::cos(dLat2);
+    const double dZ2 = std::sin(dLat2);
+    double dProd = dX1 * dX2 + dY1 * dY2 + dZ1 * dZ2;
+    if (dProd > 1) {
+        dProd = 1;
+    } else if (dProd < -1) {
+        dProd = -1;
+    }
+    return dR * std::acos(dProd);
+}
+
+static double ms_distance(const double *lon, const double *lat, double R, bool cart, int a, int b) {
+    if (cart) {
+        const double dX = lon[b] - lon[a], dY = lat[b] - lat[a];
+        return 1.0 * std::sqrt(dX * dX + dY * dY);
+    }
+    return ms_spherdist(lon[a] * kQPi / 180, lat[a] * kQPi / 180, lon[b] * kQPi / 180, lat[b] * kQPi / 180, R);
+}
+
+static void ms_free(qhg_run *r) {
+    cudaFree(r->d_ms_hops); cudaFree(r->d_ms_chops); cudaFree(r->d_ms_dist); cudaFree(r->d_ms_time);
+    cudaFree(r->d_ms_D); cudaFree(r->d_ms_cdist); cudaFree(r->d_ms_ckey);
+    r->d_ms_hops = r->d_ms_chops = nullptr;
+    r->d_ms_dist = r->d_ms_time = r->d_ms_D = nullptr;
+    r->d_ms_cdist = r->d_ms_ckey = nullptr;
+    r->ms_mode = -1;
+}
+
+// MoveStats::preLoop / initializeOccupied (actions/MoveStats.cpp:96-175):
+// hops, distance and time -1, the cells of the current table 0; no candidates
+static int ms_reset(qhg_run *r) {
+    const int C = r->C;
+    std::vector<int32_t> hops((size_t)C, -1), chops((size_t)C, INT32_MAX);
+    std::vector<double> dt((size_t)C, -1.0);
+    std::vector<unsigned long long> cdist((size_t)C, 0x7ff0000000000000ull);
+    std::vector<unsigned long long> ckey((size_t)C, r->ms_mode == 0 ? ~0ull : 0ull);
+    std::vector<double> dist(dt);
+    if (r->agents_ok) {
+        CUDA_TRY(cudaStreamSynchronize(r->stream));
+        const uint32_t nne = r->h_rs->n_nonempty;
+        std::vector<uint32_t> ne(nne);
+        if (nne > 0) CUDA_TRY(cudaMemcpy(ne.data(), r->d_ne[r->cur], nne * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        for (uint32_t c : ne) {
+            hops[c] = 0;
+            dist[c] = 0.0;
+            dt[c] = 0.0;
+        }
+    }
+    cudaStream_t st = r->stream;
+    CUDA_TRY(cudaMemcpyAsync(r->d_ms_hops, hops.data(), (size_t)C * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(r->d_ms_dist, dist.data(), (size_t)C * sizeof(double), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(r->d_ms_time, dt.data(), (size_t)C * sizeof(double), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(r->d_ms_chops, chops.data(), (size_t)C * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(r->d_ms_cdist, cdist.data(), (size_t)C * 8, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(r->d_ms_ckey, ckey.data(), (size_t)C * 8, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return QHG_OK;
+}
+
+extern "C" int qhg_gpu_move_stats_enable(qhg_run *r, int32_t mode, const double *lon, const double *lat,
+                                         double radius, int32_t cartesian) {
+    if (r == nullptr || lon == nullptr || lat == nullptr) return fail(QHG_ERR_ARG, "null argument");
+    if (mode < QHG_MOVESTATS_FIRST || mode > QHG_MOVESTATS_LAST) return fail(QHG_ERR_ARG, "bad MoveStats mode");
+    if (!r->grid_ok) return fail(QHG_ERR_STATE, "upload the grid first");
+    CUDA_TRY(cudaSetDevice(r->desc.device));
+    int rc = pull_state(r);
+    if (rc != QHG_OK) return rc;
+    const int C = r->C;
+    std::vector<double> D((size_t)C * 6, 0.0);
+    for (int c = 0; c < C; c++) {
+        for (int k = 0; k < (int)r->h_nnbr[c]; k++) {
+            const int d = r->h_nbr[(size_t)c * 6 + k];
+            if (d >= 0) D[(size_t)c * 6 + k] = ms_distance(lon, lat, radius, cartesian != 0, c, d);
+        }
+    }
+    drop_graphs(r);   // the step graph gains the MoveStats kernels
+    if (r->d_ms_hops == nullptr) {
+        CUDA_TRY(cudaMalloc(&r->d_ms_hops, (size_t)C * sizeof(int32_t)));
+        CUDA_TRY(cudaMalloc(&r->d_ms_chops, (size_t)C * sizeof(int32_t)));
+        CUDA_TRY(cudaMalloc(&r->d_ms_dist, (size_t)C * sizeof(double)));
+        CUDA_TRY(cudaMalloc(&r->d_ms_time, (size_t)C * sizeof(double)));
+        CUDA_TRY(cudaMalloc(&r->d_ms_D, (size_t)C * 6 * sizeof(double)));
+        CUDA_TRY(cudaMalloc(&r->d_ms_cdist, (size_t)C * 8));
+        CUDA_TRY(cudaMalloc(&r->d_ms_ckey, (size_t)C * 8));
+    }
+    CUDA_TRY(cudaMemcpyAsync(r->d_ms_D, D.data(), D.size() * sizeof(double), cudaMemcpyHostToDevice, r->stream));
+    r->ms_mode = mode;
+    return ms_reset(r);
+}
+
+extern "C" int qhg_gpu_move_stats(qhg_run *r, int32_t *hops, double *dist, double *time) {
+    if (r == nullptr || hops == nullptr || dist == nullptr || time == nullptr) return fail(QHG_ERR_ARG, "null argument");
+    if (r->ms_mode < 0) return fail(QHG_ERR_STATE, "MoveStats is not enabled");
+    CUDA_TRY(cudaSetDevice(r->desc.device));
+    int rc = pull_state(r);
+    if (rc != QHG_OK) return rc;
+    const size_t C = (size_t)r->C;
+    CUDA_TRY(cudaMemcpy(hops, r->d_ms_hops, C * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(dist, r->d_ms_dist, C * sizeof(double), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(time, r->d_ms_time, C * sizeof(double), cudaMemcpyDeviceToHost));
+    return QHG_OK;
+}
+
 extern "C" int qhg_gpu_num_agents(qhg_run *r, int64_t *n) {
     if (r == nullptr || n == nullptr) return fail(QHG_ERR_ARG, "null argument");
     int rc = qhg_gpu_sync(r);
@@ -1137,6 +1263,7 @@ extern "C" int qhg_gpu_destroy(qhg_run *r) {
     cudaFree(r->d_wthr); cudaFree(r->d_cmove); cudaFree(r->d_occ);
     cudaFree(r->d_clsc); cudaFree(r->d_sbase); cudaFree(r->d_bbase); cudaFree(r->d_bidb);
     cudaFree(r->d_obase); cudaFree(r->d_tflag); cudaFree(r->d_tagg); cudaFree(r->d_tincl);
+    ms_free(r);
     cudaFree(r->d_rs);
     cudaFreeHost(r->h_rs);
     for (int i = 0; i < 5; i++) {

@@ -205,6 +205,14 @@ struct StepBuffers {
     // occupancy tracking (single runs with QHG_FLAG_TRACK_OCCUPANCY, else
     // null): per cell, the first step whose table holds an agent there, -1 none
     int32_t *occ;
+    // MoveStats (single runs, ms_mode >= 0: 0 first, 1 min, 2 last): per cell
+    // the definitive hops, distance and time; this step's candidates (hops,
+    // distance as the bits of a non-negative double, mover ID key) per
+    // destination cell; the distance to each neighbour slot (cells x 6)
+    int32_t ms_mode;
+    int32_t *ms_hops; double *ms_dist; double *ms_time;
+    int32_t *ms_chops; unsigned long long *ms_cdist; unsigned long long *ms_ckey;
+    const double *ms_D;
     // outcome word per agent: outcome byte | local cell << 8 | rank in its
     // cell's class << 17
     uint32_t *outc; int32_t *father; uint16_t *brank; uint32_t *clsc;

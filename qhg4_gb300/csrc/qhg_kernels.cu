@@ -33,6 +33,7 @@
 // The reference runs these as SPopulation::initializeStep / doActions /
 // finalizeStep (core/SPopulation.cpp:394-577, 596-724, 1058-1092, 509-536).
 #include <algorithm>
+#include <climits>
 #include <cstring>
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -258,13 +259,15 @@ struct CellView {
 // Returns the outcome byte.  An agent inside the OldAgeDeath window draws
 // (OAD == kOadDraw), is left alive with `queued` set for the caller to draw
 // (kOadQueue), or dies as `oad_die` says (kOadGiven).
-// `fa` is the agent's age after the actions (the input age on entry).
+// `fa` is the agent's age after the actions (the input age on entry);
+// `mdir` the direction of the move it registered (neighbour slot + 1, 0
+// none), also when a later action killed it.
 template <int PROG, bool BATCH, int OAD>
 __device__ __forceinline__ uint8_t agent_outcome(const StepConst &P, const BatchRun *R, int32_t step, float fT,
                                                  int64_t id, uint8_t m8, float fb, float fa_in, float fl,
                                                  bool mated, const CellView &cv, const uint64_t *__restrict__ wthr,
                                                  bool oad_die, float &fa, bool &queued, uint32_t &cnt_deaths,
-                                                 uint32_t &cnt_moves) {
+                                                 uint32_t &cnt_moves, uint32_t &mdir) {
     const uint64_t seed = BATCH ? R->seed : P.seed;
     const int32_t stepR = BATCH ? step - R->step0 : step;
     const float fTR = BATCH ? (float)stepR : fT;
@@ -372,6 +375,7 @@ __device__ __forceinline__ uint8_t agent_outcome(const StepConst &P, const Batch
         }
     }
     const int cls = alive ? (1 + dir) : 0;
+    mdir = (uint32_t)dir;
     return (uint8_t)(cls | (bflag ? kOutBirth : 0) | (fert ? kOutFertile : 0) |
                      ((m8 & kMetaGender) ? kOutGender : 0) | (dir > 0 ? kOutMoved : 0));
 }
@@ -731,6 +735,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             if (__all_sync(FULL_MASK, i >= na)) break;
             const bool in_tile = i < na;
             uint8_t oc = 0;
+            uint32_t mdir = 0u;
             bool queued = false;
             float fa = 0.0f;
             int lc = 0;
@@ -754,7 +759,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                     const int mate = S.mate[i];
                     oc = agent_outcome<PROG, BATCH, kDeferOad ? kOadQueue : kOadDraw>(
                         P, R, step, fT, pid[j], m8, pb[j], pa[j], pl[j], mate >= 0, cv, wthr, false, fa, queued,
-                        cnt_deaths, cnt_moves);
+                        cnt_deaths, cnt_moves, mdir);
                     if (oc & kOutBirth) {
                         father[row] = (int32_t)(a0 + (uint32_t)mate);
                         cnt_births++;
@@ -777,10 +782,12 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                     }
                 }
             }
-            // outcome word: outcome byte | local cell << 8 | rank in the cell's class << 17
+            // outcome word: outcome byte | local cell << 8 | rank in the cell's
+            // class << 17; for the dead, the direction of a move they registered
             const int cls = oc & 7;
             const uint32_t rank = class_rank(in_tile && !queued && cls > 0, lc, cls, S.cls);
-            if (in_tile && !queued) outc[a0 + (uint32_t)i] = (uint32_t)oc | ((uint32_t)lc << 8) | (rank << 17);
+            if (in_tile && !queued)
+                outc[a0 + (uint32_t)i] = (uint32_t)oc | ((uint32_t)lc << 8) | ((cls > 0 ? rank : mdir) << 17);
             // mothers: a list per cell of their ID ranks (births are rare: most
             // warps have none and skip the aggregation)
             const bool mother = (mothers >> j) & 1u;
@@ -806,6 +813,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                 const bool valid = q < nq;
                 int i = 0, lc = 0;
                 uint8_t oc = 0;
+                uint32_t mdir = 0u;
                 if (valid) {
                     i = S.oadq[q];
                     lc = S.cell[i];
@@ -819,13 +827,15 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                     const double th = __dmul_rn(__dmul_rn(A.oad_w, (double)u), 2.3283064365386962890625e-10);
                     const double thr = __dadd_rn(A.oad_M, __dadd_rn(A.oad_a, th));
                     if ((double)S.ofa[q] > thr) {
+                        const uint32_t c0 = oc & 7u;   // alive until now: 1 + its move direction
+                        mdir = c0 >= 2u ? c0 - 1u : 0u;
                         oc = (uint8_t)(oc & ~7u);
                         cnt_deaths++;
                     }
                 }
                 const int cls = oc & 7;
                 const uint32_t rank = class_rank(valid && cls > 0, lc, cls, S.cls);
-                if (valid) outc[a0 + (uint32_t)i] = (uint32_t)oc | ((uint32_t)lc << 8) | (rank << 17);
+                if (valid) outc[a0 + (uint32_t)i] = (uint32_t)oc | ((uint32_t)lc << 8) | ((cls > 0 ? rank : mdir) << 17);
                 if (BATCH) {
                     const bool died = valid && cls == 0;
                     const bool moved = valid && (oc & kOutMoved);
@@ -1847,6 +1857,7 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                 const bool valid = row < n;
                 const int lc = row >= cs1 ? 1 : 0;
                 uint8_t oc = 0;
+                uint32_t mdir = 0u;   // direction of a registered move, kept for the dead
                 if (valid) {
                     const uint32_t g = s + (uint32_t)row;
                     if (!(lc ? keep1 : keep0)) {
@@ -1862,6 +1873,7 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                         if (!alive) cnt_deaths++;
                         const uint32_t dir = alive ? (stt & kStDir) : 0u;
                         if (dir) cnt_moves++;
+                        mdir = dir;
                         if (kEarlyOad && alive) {
                             const uint32_t o = (stt >> kStOad) & 3u;
                             if (o == 1u || (o == 2u && ((W.odie[b >> 5] >> lane) & 1u))) {
@@ -1884,7 +1896,7 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                         bool queued = false;
                         oc = agent_outcome<PROG, BATCH, kEarlyOad ? kOadGiven : kOadDraw>(
                             P, R, step, fT, id[g], meta[g], birth[g], P.reads_age ? age[g] : 0.0f, lastb[g],
-                            mate >= 0, W.cv[lc], wthr, odie, fa, queued, cnt_deaths, cnt_moves);
+                            mate >= 0, W.cv[lc], wthr, odie, fa, queued, cnt_deaths, cnt_moves, mdir);
                         if (oc & kOutBirth) {
                             father[g] = (int32_t)(s + (uint32_t)mate);
                             cnt_births++;
@@ -1899,8 +1911,11 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                 const uint32_t base = counted ? W.cnt[lc][slot] : 0u;
                 __syncwarp();
                 if (counted && (peers & lt) == 0u) W.cnt[lc][slot] = base + (uint32_t)__popc(peers);
-                // outcome byte | rank in the cell's class << 17
-                if (valid) outc[s + (uint32_t)row] = (uint32_t)oc | ((base + (uint32_t)__popc(peers & lt)) << 17);
+                // outcome byte | rank in the cell's class << 17 (for the dead, the
+                // direction of a move they registered)
+                if (valid)
+                    outc[s + (uint32_t)row] =
+                        (uint32_t)oc | ((counted ? base + (uint32_t)__popc(peers & lt) : mdir) << 17);
                 const bool bo = valid && (oc & kOutBirth);
                 births0 += __popc(__ballot_sync(FULL_MASK, bo && lc == 0));
                 births1 += __popc(__ballot_sync(FULL_MASK, bo && lc == 1));
@@ -2329,6 +2344,100 @@ k_occupancy(const RunState *__restrict__ rs, const uint32_t *__restrict__ nonemp
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         const uint32_t c = nonempty[r];
         if (occ[c] < 0) occ[c] = st;
+    }
+}
+
+// --------------------------------------------------------------- MoveStats
+// MoveStats::finalize (actions/MoveStats.cpp:183-256) as one thread runs it,
+// with the moves in agent-ID order: a move from cell f to cell t offers t the
+// values hops[f] + 1 and dist[f] + the f-t distance, taken from the state
+// before the step.  MIN keeps per cell the smallest hops and distance and the
+// time of the first arrival; FIRST the values of the first arrival (the
+// lowest mover ID of the first step that reaches the cell); LAST those of the
+// latest arrival (the highest mover ID of the last step with arrivals).
+// Every registered move counts, also that of an agent a later action of the
+// step killed (its direction is kept in its outcome word).
+constexpr int kMsFirst = 0, kMsMin = 1, kMsLast = 2;
+constexpr unsigned long long kMsNoDist = 0x7ff0000000000000ull;   // +inf
+
+// the destination slot of a registered move in an outcome word, -1 none
+__device__ __forceinline__ int ms_move_slot(uint32_t code) {
+    const int cls = (int)(code & 7u);
+    if (cls >= 2) return cls - 2;
+    if (cls == 0 && (code & kOutMoved)) return (int)((code >> 17) & 7u) - 1;
+    return -1;
+}
+
+// pass 0: MIN reduces the candidates, FIRST/LAST elect the mover per
+// destination; pass 1 (FIRST/LAST): the elected movers write their values.
+// One warp per non-empty cell of the step's table; runs after the actions.
+template <int MODE, int PASS>
+__global__ void __launch_bounds__(256)
+k_ms_pick(const RunState *__restrict__ rs, const uint32_t *__restrict__ nonempty,
+          const uint32_t *__restrict__ ne_start, const int64_t *__restrict__ id, const uint32_t *__restrict__ outc,
+          const int32_t *__restrict__ nbr, const double *__restrict__ D, const int32_t *__restrict__ hops,
+          const double *__restrict__ dist, int32_t *__restrict__ chops, unsigned long long *__restrict__ cdist,
+          unsigned long long *__restrict__ ckey) {
+    if (rs->error != 0u) return;
+    const uint32_t n = rs->n_nonempty;
+    const int lane = threadIdx.x & 31;
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < n; w += warps) {
+        const uint32_t f = nonempty[w];
+        const uint32_t r0 = ne_start[w], r1 = ne_start[w + 1];
+        for (uint32_t r = r0 + (uint32_t)lane; r < r1; r += 32) {
+            const int k = ms_move_slot(outc[r]);
+            if (k < 0) continue;
+            const int32_t t = nbr[(size_t)f * 6 + (size_t)k];
+            if (t < 0) continue;
+            if (MODE == kMsMin || PASS == 1) {
+                const int32_t h = hops[f] + 1;
+                const double d = __dadd_rn(dist[f], D[(size_t)f * 6 + (size_t)k]);
+                const unsigned long long db = (unsigned long long)__double_as_longlong(d);
+                if (MODE == kMsMin) {
+                    atomicMin(&chops[t], h);
+                    atomicMin(&cdist[t], db);
+                } else {
+                    const unsigned long long key = (unsigned long long)id[r] + (MODE == kMsLast ? 1ull : 0ull);
+                    if (ckey[t] == key) {
+                        chops[t] = h;
+                        cdist[t] = db;
+                    }
+                }
+            } else if (MODE == kMsFirst) {
+                atomicMin(&ckey[t], (unsigned long long)id[r]);
+            } else {
+                atomicMax(&ckey[t], (unsigned long long)id[r] + 1ull);
+            }
+        }
+    }
+}
+
+// After the commit: the candidates into the state, then cleared.  A failed
+// step leaves both untouched (its retry offers the same candidates).
+template <int MODE>
+__global__ void __launch_bounds__(256)
+k_ms_merge(const RunState *__restrict__ rs, int C, int32_t *__restrict__ hops, double *__restrict__ dist,
+           double *__restrict__ time, int32_t *__restrict__ chops, unsigned long long *__restrict__ cdist,
+           unsigned long long *__restrict__ ckey) {
+    if (rs->error != 0u) return;
+    const double t = (double)(float)(rs->step - 1);   // the step that made the moves
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) {
+        const int32_t ch = chops[c];
+        if (ch == INT_MAX) continue;
+        const double cd = __longlong_as_double((long long)cdist[c]);
+        const int32_t h = hops[c];
+        if (MODE == kMsLast || h < 0) {
+            hops[c] = ch;
+            dist[c] = cd;
+            time[c] = t;
+        } else if (MODE == kMsMin) {
+            if (ch < h) hops[c] = ch;
+            if (cd < dist[c]) dist[c] = cd;
+        }
+        chops[c] = INT_MAX;
+        cdist[c] = kMsNoDist;
+        ckey[c] = MODE == kMsFirst ? ~0ull : 0ull;
     }
 }
 
@@ -2838,6 +2947,18 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
 #undef QHG_LAUNCH_CELL
 #undef QHG_LAUNCH_ACTIONS
     if (ev) cudaEventRecord(ev[1], stream);
+    const int ms_grid = std::max(1, std::min((P->num_cells + 7) / 8, 152 * 16));
+    if (!batch && B->ms_mode >= 0) {
+#define QHG_LAUNCH_MS_PICK(MD, PS)                                                                          \
+    k_ms_pick<MD, PS><<<ms_grid, 256, 0, stream>>>(rs, B->nonempty, B->ne_start, B->id, B->outc, B->nbr, B->ms_D, \
+                                                  B->ms_hops, B->ms_dist, B->ms_chops, B->ms_cdist, B->ms_ckey)
+        switch (B->ms_mode) {
+        case kMsFirst: QHG_LAUNCH_MS_PICK(kMsFirst, 0); QHG_LAUNCH_MS_PICK(kMsFirst, 1); break;
+        case kMsMin: QHG_LAUNCH_MS_PICK(kMsMin, 0); break;
+        default: QHG_LAUNCH_MS_PICK(kMsLast, 0); QHG_LAUNCH_MS_PICK(kMsLast, 1); break;
+        }
+#undef QHG_LAUNCH_MS_PICK
+    }
 #define QHG_LAUNCH_SCAN(BT, IT)                                                                             \
     k_cell_scan<BT, IT><<<ntiles, kScanThreads, 0, stream>>>(                                               \
         *P, BB, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr2, B->cmove, B->necm2, B->sbase, B->bbase, B->bidbase,       \
@@ -2876,6 +2997,18 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
     if (ev) cudaEventRecord(ev[3], stream);
     if (!batch && B->occ != nullptr) {
         k_occupancy<<<std::max(1, L.scatter_grid), 256, 0, stream>>>(rs, B->nonempty2, B->occ);
+    }
+    if (!batch && B->ms_mode >= 0) {
+        const int mg = std::max(1, std::min((P->num_cells + 255) / 256, 152 * 8));
+#define QHG_LAUNCH_MS_MERGE(MD)                                                                             \
+    k_ms_merge<MD><<<mg, 256, 0, stream>>>(rs, P->num_cells, B->ms_hops, B->ms_dist, B->ms_time, B->ms_chops, \
+                                           B->ms_cdist, B->ms_ckey)
+        switch (B->ms_mode) {
+        case kMsFirst: QHG_LAUNCH_MS_MERGE(kMsFirst); break;
+        case kMsMin: QHG_LAUNCH_MS_MERGE(kMsMin); break;
+        default: QHG_LAUNCH_MS_MERGE(kMsLast); break;
+        }
+#undef QHG_LAUNCH_MS_MERGE
     }
     if (batch) {
         k_inject<<<L.scatter_grid, 256, 0, stream>>>(rs, BB, B->id2, B->birth2, B->age2, B->lastb2, B->meta2,

@@ -40,6 +40,7 @@ EXPORTS = [
     "qhg_batch_live_history", "qhg_batch_snapshot_async", "qhg_batch_snapshot_wait",
     "qhg_host_buffer_alloc", "qhg_host_buffer_free", "qhg_gpu_next_id", "qhg_gpu_set_next_id",
     "qhg_gpu_test_stall_scan", "qhg_gpu_occupancy", "qhg_gpu_set_capacity", "qhg_gpu_set_move_weights",
+    "qhg_gpu_move_stats_enable", "qhg_gpu_move_stats",
 ]
 
 
@@ -135,6 +136,8 @@ def load_library(path: str = LIB_PATH):
         "qhg_gpu_occupancy": (I, [P, P]),
         "qhg_gpu_set_capacity": (I, [P, P]),
         "qhg_gpu_set_move_weights": (I, [P, P]),
+        "qhg_gpu_move_stats_enable": (I, [P, ct.c_int32, P, P, ct.c_double, ct.c_int32]),
+        "qhg_gpu_move_stats": (I, [P, P, P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -256,6 +259,25 @@ class GpuRun:
         if w.shape != (self.C, 7):
             raise ValueError("weights need shape (cells, 7)")
         _check(_lib.qhg_gpu_set_move_weights(self.h, _p(w)))
+
+    def move_stats_enable(self, mode: int, lon: np.ndarray, lat: np.ndarray, radius: float = 1.0,
+                          cartesian: bool = False) -> None:
+        """MoveStats (QHG_MOVESTATS_FIRST / MIN / LAST = 0 / 1 / 2) over the
+        cells' coordinates (lon/lat in degrees, or x/y when cartesian)."""
+        lo = np.ascontiguousarray(lon, dtype=np.float64)
+        la = np.ascontiguousarray(lat, dtype=np.float64)
+        if lo.shape != (self.C,) or la.shape != (self.C,):
+            raise ValueError("coordinates need one entry per cell")
+        _check(_lib.qhg_gpu_move_stats_enable(self.h, int(mode), _p(lo), _p(la), float(radius),
+                                              1 if cartesian else 0))
+
+    def move_stats(self):
+        """Per cell: hops (int32), distance and time (float64) of MoveStats."""
+        h = np.zeros(self.C, np.int32)
+        d = np.zeros(self.C, np.float64)
+        t = np.zeros(self.C, np.float64)
+        _check(_lib.qhg_gpu_move_stats(self.h, _p(h), _p(d), _p(t)))
+        return h, d, t
 
     def occupancy(self) -> np.ndarray:
         """Per cell, the first step whose table holds an agent there (-1 none);

@@ -60,3 +60,9 @@ def move_weights(grid, seed, nonmonotone=0.1, equal=0.05):
     low = (~eq) & (tot <= 0.05)
     W[low] += 1.0
     return W
+
+
+def cell_lonlat(grid):
+    """Longitude and latitude (degrees) of the grid's cell centres."""
+    x, y, z = grid.xyz[:, 0], grid.xyz[:, 1], grid.xyz[:, 2]
+    return np.degrees(np.arctan2(y, x)), np.degrees(np.arcsin(np.clip(z, -1.0, 1.0)))

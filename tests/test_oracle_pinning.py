@@ -109,3 +109,43 @@ def test_port_oracle_environment_updates_against_reference_build(tmp_path, given
     assert d is None, d
     assert np.array_equal(st, ref.stats)
     assert st[:, 3].sum() > 0
+
+
+@pytest.mark.skipif(not os.path.exists(ref_program("philox")), reason="reference build not present")
+@pytest.mark.parametrize("moves", ["random", "weighted"])
+def test_port_oracle_move_stats_against_reference_build(tmp_path, moves):
+    """MoveStats in its MIN mode (actions/MoveStats.cpp): per cell the
+    fewest hops, the shortest distance and the first time agents reached
+    it, against the reference's class on one thread (its per-thread merge
+    makes more threads order-dependent); distances on a sphere of radius
+    6371 from the cell centres' longitudes and latitudes."""
+    from qhg4_gb300.spec import config1_actions, config2_actions
+    from qhg4_gb300.workload import make_agents, terrain_grid, uniform_grid
+    from helpers import cell_lonlat
+    if moves == "random":
+        grid = uniform_grid(10, 30.0)
+        agents = make_agents(grid, 400, seed=101, age_max=50.0)
+        agents.cell[:] = grid.nbr[0, agents.id % 5]   # start around one cell and spread out
+        acts = config1_actions(b0=0.4, d0=0.02, move_p=0.4)
+    else:
+        grid = terrain_grid(10, seed=102)
+        agents = make_agents(grid, 2000, seed=103, age_max=60.0, proportional_to_K=True)
+        top = np.argsort(-grid.K)[:40]
+        agents.cell[:] = top[agents.id % 40]      # start in the 40 best cells and spread out
+        acts = config2_actions(b0=0.3, d0=0.03, move_p=0.3)
+    lon, lat = cell_lonlat(grid)
+    ref = run_reference("philox", str(tmp_path), grid, agents, acts, 30, 777, threads=1,
+                        move_stats=(1, lon, lat, 6371.0))
+    r = port.OracleRun(grid, acts, 777)
+    r.load(agents)
+    r.move_stats_enable(1, lon, lat, 6371.0)
+    st = r.step(30)
+    assert ref.draw_errors == 0
+    assert table_diff(r.agents(), ref.agents) is None
+    assert np.array_equal(st, ref.stats)
+    h, d, t = r.move_stats()
+    rh, rd, rt = ref.move_stats
+    assert (h > 0).sum() > 20
+    assert np.array_equal(h, rh)
+    assert np.array_equal(d.view(np.uint64), rd.view(np.uint64))
+    assert np.array_equal(t.view(np.uint64), rt.view(np.uint64))
