@@ -170,6 +170,9 @@ int qhg_gpu_stats(qhg_run *run, int32_t nsteps, qhg_step_stats *out);
  * one population: occupation masks that change to non-zero are recorded,
  * masks of zero are ignored. */
 int qhg_gpu_occupancy(qhg_run *run, int32_t *first_step);
+/* Restores the occupation history (C entries as qhg_gpu_occupancy gives
+ * them) after a checkpoint's table was uploaded. */
+int qhg_gpu_set_occupancy(qhg_run *run, const int32_t *first_step);
 /* MoveStats (actions/MoveStats.cpp, actions/MoveStats.h): per cell the hops,
  * the distance travelled and the time of arrival of the agents that reached
  * it, with the reference's modes MODE_STAT_FIRST / MIN / LAST:
@@ -195,6 +198,10 @@ int qhg_gpu_occupancy(qhg_run *run, int32_t *first_step);
 int qhg_gpu_move_stats_enable(qhg_run *run, int32_t mode, const double *lon, const double *lat, double radius,
                               int32_t cartesian);
 int qhg_gpu_move_stats(qhg_run *run, int32_t *hops, double *dist, double *time);
+/* Restores the statistics (as qhg_gpu_move_stats gives them) after a
+ * checkpoint's table was uploaded and MoveStats enabled: the reference's
+ * MoveStats::readAdditionalDataQDF (actions/MoveStats.cpp) on --resume. */
+int qhg_gpu_set_move_stats(qhg_run *run, const int32_t *hops, const double *dist, const double *time);
 /* birth log (QHG_FLAG_LOG_BIRTHS): rows (baby, mother, father) */
 int qhg_gpu_birth_log(qhg_run *run, int64_t *baby, int64_t *mother, int64_t *father, int64_t cap,
                       int64_t *n);

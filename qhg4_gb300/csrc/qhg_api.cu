@@ -1087,6 +1087,20 @@ extern "C" int qhg_gpu_move_stats_enable(qhg_run *r, int32_t mode, const double 
     return ms_reset(r);
 }
 
+extern "C" int qhg_gpu_set_move_stats(qhg_run *r, const int32_t *hops, const double *dist, const double *time) {
+    if (r == nullptr || hops == nullptr || dist == nullptr || time == nullptr) return fail(QHG_ERR_ARG, "null argument");
+    if (r->ms_mode < 0) return fail(QHG_ERR_STATE, "MoveStats is not enabled");
+    CUDA_TRY(cudaSetDevice(r->desc.device));
+    int rc = pull_state(r);
+    if (rc != QHG_OK) return rc;
+    const size_t C = (size_t)r->C;
+    CUDA_TRY(cudaMemcpyAsync(r->d_ms_hops, hops, C * sizeof(int32_t), cudaMemcpyHostToDevice, r->stream));
+    CUDA_TRY(cudaMemcpyAsync(r->d_ms_dist, dist, C * sizeof(double), cudaMemcpyHostToDevice, r->stream));
+    CUDA_TRY(cudaMemcpyAsync(r->d_ms_time, time, C * sizeof(double), cudaMemcpyHostToDevice, r->stream));
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    return QHG_OK;
+}
+
 extern "C" int qhg_gpu_move_stats(qhg_run *r, int32_t *hops, double *dist, double *time) {
     if (r == nullptr || hops == nullptr || dist == nullptr || time == nullptr) return fail(QHG_ERR_ARG, "null argument");
     if (r->ms_mode < 0) return fail(QHG_ERR_STATE, "MoveStats is not enabled");
@@ -1178,6 +1192,15 @@ extern "C" int qhg_gpu_occupancy(qhg_run *r, int32_t *first_step) {
     int rc = qhg_gpu_sync(r);
     if (rc != QHG_OK) return rc;
     CUDA_TRY(cudaMemcpy(first_step, r->d_occ, (size_t)r->C * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    return QHG_OK;
+}
+
+extern "C" int qhg_gpu_set_occupancy(qhg_run *r, const int32_t *first_step) {
+    if (r == nullptr || first_step == nullptr) return fail(QHG_ERR_ARG, "null argument");
+    if (r->d_occ == nullptr) return fail(QHG_ERR_STATE, "run was created without QHG_FLAG_TRACK_OCCUPANCY");
+    int rc = qhg_gpu_sync(r);
+    if (rc != QHG_OK) return rc;
+    CUDA_TRY(cudaMemcpy(r->d_occ, first_step, (size_t)r->C * sizeof(int32_t), cudaMemcpyHostToDevice));
     return QHG_OK;
 }
 

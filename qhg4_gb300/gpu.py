@@ -40,7 +40,7 @@ EXPORTS = [
     "qhg_batch_live_history", "qhg_batch_snapshot_async", "qhg_batch_snapshot_wait",
     "qhg_host_buffer_alloc", "qhg_host_buffer_free", "qhg_gpu_next_id", "qhg_gpu_set_next_id",
     "qhg_gpu_test_stall_scan", "qhg_gpu_occupancy", "qhg_gpu_set_capacity", "qhg_gpu_set_move_weights",
-    "qhg_gpu_move_stats_enable", "qhg_gpu_move_stats",
+    "qhg_gpu_move_stats_enable", "qhg_gpu_move_stats", "qhg_gpu_set_move_stats", "qhg_gpu_set_occupancy",
 ]
 
 
@@ -138,6 +138,8 @@ def load_library(path: str = LIB_PATH):
         "qhg_gpu_set_move_weights": (I, [P, P]),
         "qhg_gpu_move_stats_enable": (I, [P, ct.c_int32, P, P, ct.c_double, ct.c_int32]),
         "qhg_gpu_move_stats": (I, [P, P, P, P]),
+        "qhg_gpu_set_move_stats": (I, [P, P, P, P]),
+        "qhg_gpu_set_occupancy": (I, [P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -191,6 +193,12 @@ class GpuRun:
         self.C = grid.num_cells
         self.genetics = genetics
         self.grid = grid
+        self.track_occupancy = track_occupancy
+        # what the run was given beyond its grid (for checkpoints): K and
+        # move weights set between steps, the MoveStats configuration
+        self.capacity_K = None
+        self.move_weights = None
+        self.move_stats_config = None
         nbr = np.ascontiguousarray(grid.nbr, dtype=np.int32)
         nnbr = np.ascontiguousarray(grid.nnbr, dtype=np.uint8)
         K = np.ascontiguousarray(grid.K, dtype=np.float64)
@@ -252,6 +260,7 @@ class GpuRun:
         if k.shape != (self.C,):
             raise ValueError("K needs one entry per cell")
         _check(_lib.qhg_gpu_set_capacity(self.h, _p(k)))
+        self.capacity_K = k.copy()
 
     def set_move_weights(self, W: np.ndarray) -> None:
         """WeightedMove's cumulative weights (C x 7) from the next step on."""
@@ -259,6 +268,7 @@ class GpuRun:
         if w.shape != (self.C, 7):
             raise ValueError("weights need shape (cells, 7)")
         _check(_lib.qhg_gpu_set_move_weights(self.h, _p(w)))
+        self.move_weights = w.copy()
 
     def move_stats_enable(self, mode: int, lon: np.ndarray, lat: np.ndarray, radius: float = 1.0,
                           cartesian: bool = False) -> None:
@@ -270,6 +280,16 @@ class GpuRun:
             raise ValueError("coordinates need one entry per cell")
         _check(_lib.qhg_gpu_move_stats_enable(self.h, int(mode), _p(lo), _p(la), float(radius),
                                               1 if cartesian else 0))
+        self.move_stats_config = (int(mode), lo.copy(), la.copy(), float(radius), bool(cartesian))
+
+    def set_move_stats(self, hops: np.ndarray, dist: np.ndarray, time: np.ndarray) -> None:
+        """Restores MoveStats' per-cell arrays (after enabling it)."""
+        h = np.ascontiguousarray(hops, dtype=np.int32)
+        d = np.ascontiguousarray(dist, dtype=np.float64)
+        t = np.ascontiguousarray(time, dtype=np.float64)
+        if h.shape != (self.C,) or d.shape != (self.C,) or t.shape != (self.C,):
+            raise ValueError("one entry per cell")
+        _check(_lib.qhg_gpu_set_move_stats(self.h, _p(h), _p(d), _p(t)))
 
     def move_stats(self):
         """Per cell: hops (int32), distance and time (float64) of MoveStats."""
@@ -278,6 +298,13 @@ class GpuRun:
         t = np.zeros(self.C, np.float64)
         _check(_lib.qhg_gpu_move_stats(self.h, _p(h), _p(d), _p(t)))
         return h, d, t
+
+    def set_occupancy(self, first_step: np.ndarray) -> None:
+        """Restores the occupation history (needs track_occupancy=True)."""
+        o = np.ascontiguousarray(first_step, dtype=np.int32)
+        if o.shape != (self.C,):
+            raise ValueError("one entry per cell")
+        _check(_lib.qhg_gpu_set_occupancy(self.h, _p(o)))
 
     def occupancy(self) -> np.ndarray:
         """Per cell, the first step whose table holds an agent there (-1 none);

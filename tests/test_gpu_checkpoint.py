@@ -45,3 +45,46 @@ def test_resume_equals_uninterrupted(gpu_lib, tmp_path, kind):
     assert np.array_equal(np.concatenate([part_log, res.birth_log()]), whole.birth_log())
     res.close()
     whole.close()
+
+
+def test_resume_with_environment_and_statistics(gpu_lib, tmp_path):
+    """A run with K and move weights changed between steps, its occupation
+    history and MoveStats: the checkpoint carries all of it, and the resumed
+    run continues exactly as the uninterrupted one."""
+    from helpers import cell_lonlat, move_weights
+    grid = terrain_grid(12, seed=14)
+    agents = make_agents(grid, 8000, seed=15, age_max=60.0, proportional_to_K=True)
+    top = np.argsort(-grid.K)[:80]
+    agents.cell[:] = top[agents.id % 80]
+    acts = config2_actions(b0=0.3, d0=0.03, move_p=0.3)
+    lon, lat = cell_lonlat(grid)
+    K1 = grid.K * np.random.default_rng(16).uniform(0.5, 1.5, grid.num_cells)
+    W = move_weights(grid, 17)
+
+    def started():
+        r = GpuRun(grid, acts, 55, track_occupancy=True)
+        r.set_move_weights(W)
+        r.load(agents)
+        r.move_stats_enable(1, lon, lat, 6371.0)
+        r.step(5)
+        r.set_capacity(K1)
+        r.step(5)
+        return r
+
+    whole = started()
+    whole.step(15)
+    part = started()
+    path = str(tmp_path / "ck_env.npz")
+    checkpoint.save(part, path)
+    part.close()
+    res = checkpoint.resume(grid, acts, 55, path)
+    assert res.current_step() == 10
+    res.step(15)
+    d = table_diff(res.agents(), whole.agents())
+    assert d is None, d
+    assert np.array_equal(res.occupancy(), whole.occupancy())
+    for x, y in zip(res.move_stats(), whole.move_stats()):
+        assert np.array_equal(x.view(np.uint8), y.view(np.uint8))
+    assert (whole.move_stats()[0] > 0).sum() > 10
+    res.close()
+    whole.close()
