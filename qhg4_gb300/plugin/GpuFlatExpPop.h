@@ -1,0 +1,52 @@
+/*
+ * GpuFlatExpPop: the FlatExpPop population (populations/FlatExpPop.cpp:32-91)
+ * with its step on the GPU (GpuPop.h).
+ *
+ * Its environment evaluators stay on the host as the reference's own
+ * objects: NPPCapacity turns the vegetation's NPP into capacities, two
+ * SingleEvaluators (altitude, NPP) feed a MultiEvaluator that leaves
+ * WeightedMove's cumulative weights.  They read their attributes from the
+ * configuration under their own names, run in initializeStep, and their
+ * weights go to the GPU run before the first step and after each
+ * environment event (qhg_gpu_set_move_weights).  The agent actions --
+ * Fertility, RandomPair, Verhulst, GetOld, OldAgeDeath, WeightedMove -- are
+ * GpuParamActions: their attributes and priorities come from the same
+ * configuration modules the reference's actions read.
+ *
+ * Not carried over: the genomes of FlatExpPop's Genetics (the GPU library
+ * steps genomes, but this plugin uploads none), and updateEvent's drowning
+ * of agents in water or ice cells after a geography event.
+ */
+#ifndef QHG_GPUFLATEXPPOP_H
+#define QHG_GPUFLATEXPPOP_H
+
+#include "GpuPop.h"
+#include "Geography.h"
+#include "MultiEvaluator.h"
+#include "NPPCapacity.h"
+#include "SingleEvaluator.h"
+
+struct GpuFlatExpAgent : Agent {
+    float m_fAge;
+    float m_fLastBirth;
+    int m_iMateIndex;
+    int m_iNumBabies;
+};
+
+class GpuFlatExpPop : public GpuPop<GpuFlatExpAgent> {
+public:
+    GpuFlatExpPop(SCellGrid *pCG, PopFinder *pPopFinder, int iLayerSize, IDGen **apIDG, uint32_t *aulState,
+                  uint *aiSeeds);
+    virtual ~GpuFlatExpPop();
+
+    int addPopSpecificAgentData(int iAgentIndex, char **ppData);
+    int makePopSpecificOffspring(int iAgent, int iMother, int iFather);
+
+protected:
+    double *m_adCapacities;    // NPPCapacity's output, the NPP evaluator's input
+    double *m_adEnvWeights;    // the MultiEvaluator's cumulative weights, cells x (connectivity + 1)
+    NPPCapacity<GpuFlatExpAgent> *m_pNPPCap;
+    MultiEvaluator<GpuFlatExpAgent> *m_pME;
+};
+
+#endif

@@ -40,15 +40,99 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
+#include <set>
 #include <string>
 #include <vector>
 
 #include "Action.h"
+#include "ParamProvider2.h"
 #include "SPopulation.h"
+#include "Fertility.h"
+#include "GetOld.h"
+#include "OldAgeDeath.h"
+#include "RandomMove.h"
+#include "RandomPair.h"
+#include "Verhulst.h"
+#include "VerhulstVarK.h"
+#include "WeightedMove.h"
 #include "LBController.h"
 #include "SCellGrid.h"
 #include "qhg_gpu.h"
+
+// An action of a GPU population as the configuration sees it: it carries the
+// reference action's name and attribute names, so that the population's
+// Prioritizer hands it that action's module (Prioritizer::getActionAttributes,
+// core/Prioritizer.cpp:440-462) and its priority (SPopulation::setPrioList);
+// tryGetAttributes reads the attributes into the QHG_ACT_* parameter slots.
+// Its execute is never called: the GPU step runs the action.
+template<typename T>
+class GpuParamAction : public Action<T> {
+public:
+    GpuParamAction(SPopulation<T> *pPop, SCellGrid *pCG, int32_t iType, const std::string &sName,
+                   const std::vector<std::string> &vSlots)
+        : Action<T>(pPop, pCG, sName, ""), m_iType(iType), m_vSlots(vSlots) {
+        this->m_vNames.insert(this->m_vNames.end(), vSlots.begin(), vSlots.end());
+        for (int k = 0; k < 4; k++) m_adP[k] = 0;
+    }
+
+    virtual int tryGetAttributes(const ModuleComplex *pMC) {
+        const stringmap &mParams = pMC->getAttributes();
+        int iResult = 0;
+        for (size_t k = 0; (k < m_vSlots.size()) && (k < 4); k++) {
+            stringmap::const_iterator it = mParams.find(m_vSlots[k]);
+            if (it == mParams.end()) {
+                iResult = -1;
+                continue;
+            }
+            char *pEnd = NULL;
+            m_adP[k] = strtod(it->second.c_str(), &pEnd);
+            if (pEnd == it->second.c_str()) iResult = -1;
+        }
+        return iResult;
+    }
+
+    // the parameter action of a QHG_ACT_* type, with the reference's names
+    // (actions/*.h ATTR_*), NULL for an unknown type
+    static GpuParamAction<T> *create(SPopulation<T> *pPop, SCellGrid *pCG, int32_t iType) {
+        switch (iType) {
+        case QHG_ACT_GETOLD:
+            return new GpuParamAction<T>(pPop, pCG, iType, ATTR_GETOLD_NAME, {});
+        case QHG_ACT_FERTILITY:
+            return new GpuParamAction<T>(pPop, pCG, iType, ATTR_FERTILITY_NAME,
+                                         {ATTR_FERTILITY_MIN_AGE_NAME, ATTR_FERTILITY_MAX_AGE_NAME,
+                                          ATTR_FERTILITY_INTERBIRTH_NAME});
+        case QHG_ACT_RANDOMPAIR:
+            return new GpuParamAction<T>(pPop, pCG, iType, ATTR_RANDPAIR_NAME, {});
+        case QHG_ACT_VERHULST:
+            return new GpuParamAction<T>(pPop, pCG, iType, ATTR_VERHULST_NAME,
+                                         {ATTR_VERHULST_B0_NAME, ATTR_VERHULST_D0_NAME, ATTR_VERHULST_TURNOVER_NAME,
+                                          ATTR_VERHULST_CAPACITY_NAME});
+        case QHG_ACT_VERHULSTVARK:
+            return new GpuParamAction<T>(pPop, pCG, iType, ATTR_VERHULSTVARK_NAME,
+                                         {ATTR_VERHULSTVARK_B0_NAME, ATTR_VERHULSTVARK_D0_NAME,
+                                          ATTR_VERHULSTVARK_TURNOVER_NAME});
+        case QHG_ACT_OLDAGEDEATH:
+            return new GpuParamAction<T>(pPop, pCG, iType, ATTR_OLDAGEDEATH_NAME,
+                                         {ATTR_OLDAGEDEATH_MAXAGE_NAME, ATTR_OLDAGEDEATH_UNCERTAINTY_NAME});
+        case QHG_ACT_RANDOMMOVE:
+            return new GpuParamAction<T>(pPop, pCG, iType, ATTR_RANDOMMOVE_NAME, {ATTR_RANDOMMOVE_PROB_NAME});
+        case QHG_ACT_WEIGHTEDMOVE:
+            return new GpuParamAction<T>(pPop, pCG, iType, ATTR_WEIGHTEDMOVE_NAME, {ATTR_WEIGHTEDMOVE_PROB_NAME});
+        case QHG_ACT_ATANDEATH:
+            // actions/ATanDeath.h's names (that header's EPS would clash here)
+            return new GpuParamAction<T>(pPop, pCG, iType, "ATanDeath",
+                                         {"ATanDeath_max_age", "ATanDeath_range", "ATanDeath_slope"});
+        default:
+            return NULL;
+        }
+    }
+
+    int32_t m_iType;
+    std::vector<std::string> m_vSlots;
+    double m_adP[4];
+};
 
 template<typename T>
 class GpuPop : public SPopulation<T> {
@@ -63,6 +147,19 @@ public:
 
     virtual ~GpuPop() {
         if (m_pRun != NULL) qhg_gpu_destroy(m_pRun);
+        for (size_t i = 0; i < m_vParamActions.size(); i++) delete m_vParamActions[i];
+    }
+
+    // an action of the GPU step configured like the reference's: added to
+    // the population's Prioritizer under the reference action's name, so that
+    // its attributes and priority come from the configuration; preLoop hands
+    // it to the GPU run
+    int addGpuParamAction(int32_t iType) {
+        GpuParamAction<T> *pA = GpuParamAction<T>::create(this, this->m_pCG, iType);
+        if (pA == NULL) return -1;
+        m_vParamActions.push_back(pA);
+        this->m_prio.addAction(pA);
+        return 0;
     }
 
     // one action: its QHG_ACT_* type, its priority and class name (the
@@ -79,9 +176,14 @@ public:
     // capacity per cell (VerhulstVarK's K, WeightedMove's weights)
     void setGpuCapacity(const double *adK, int iNumCells) { m_vK.assign(adK, adK + iNumCells); }
     void setGpuDevice(int iDevice) { m_iDevice = iDevice; }
-    // an environment evaluator kept on the host (not owned): its initialize
-    // runs at each initializeStep, as SPopulation's does for every action
-    void addHostEvaluator(Action<T> *pA) { m_vHostEvals.push_back(pA); }
+    // an environment evaluator kept on the host (not owned; also added to the
+    // Prioritizer, which gives it its attributes and priority): its
+    // initialize runs at each initializeStep and its finalize at each
+    // finalizeStep, in priority order, as SPopulation's do for every action
+    void addHostEvaluator(Action<T> *pA) {
+        m_vHostEvals.push_back(pA);
+        this->m_prio.addAction(pA);
+    }
     // the arrays the host evaluators fill (not owned): K per cell (NULL:
     // none) and WeightedMove's cumulative weights, cells x 7 (NULL: the
     // weights follow K); handed to the GPU run before the first step and
@@ -94,6 +196,7 @@ public:
 
     virtual int preLoop() {
         int iResult = SPopulation<T>::preLoop();
+        if (iResult == 0) collectParamActions();
         if (iResult == 0) iResult = startGpu();
         return iResult;
     }
@@ -101,8 +204,8 @@ public:
     virtual int initializeStep(float fTime) {
         if (m_pRun == NULL) return -1;
         int iResult = 0;
-        for (size_t i = 0; i < m_vHostEvals.size(); i++) {
-            iResult += m_vHostEvals[i]->initialize(fTime);
+        for (size_t i = 0; i < m_vHostOrder.size(); i++) {
+            iResult += m_vHostOrder[i]->initialize(fTime);
         }
         if ((iResult == 0) && m_bEnvDirty) {
             if ((m_adEnvW != NULL) && (qhg_gpu_set_move_weights(m_pRun, m_adEnvW) != QHG_OK)) iResult = -1;
@@ -124,7 +227,12 @@ public:
     virtual int finalizeStep() {
         if ((m_pRun == NULL) || (qhg_gpu_step(m_pRun, 1) != QHG_OK)) return -1;
         m_bStale = true;
-        return 0;
+        // the host evaluators' finalize (an evaluator clears its update flag there)
+        int iResult = 0;
+        for (size_t i = 0; i < m_vHostOrder.size(); i++) {
+            iResult += m_vHostOrder[i]->finalize(this->m_fCurTime);
+        }
+        return iResult;
     }
 
     virtual void updateNumAgentsPerCell() {
@@ -169,6 +277,27 @@ protected:
         std::string sName;
         double adP[4];
     };
+
+    // the parameter actions, in the Prioritizer's levels, into the action
+    // list; the host evaluators in the same order
+    void collectParamActions() {
+        m_vHostOrder.clear();
+        std::set<uint> sPrios;
+        this->m_prio.getPrios(sPrios);
+        for (std::set<uint>::const_iterator it = sPrios.begin(); it != sPrios.end(); ++it) {
+            for (uint j = 0; j < this->m_prio.getNumActionsForPrio(*it); j++) {
+                Action<T> *pA = this->m_prio.getAction(*it, j);
+                for (size_t k = 0; k < m_vParamActions.size(); k++) {
+                    if (m_vParamActions[k] == pA) {
+                        addGpuAction(m_vParamActions[k]->m_iType, *it, pA->getActionName(), m_vParamActions[k]->m_adP);
+                    }
+                }
+                if (std::find(m_vHostEvals.begin(), m_vHostEvals.end(), pA) != m_vHostEvals.end()) {
+                    m_vHostOrder.push_back(pA);
+                }
+            }
+        }
+    }
 
     int startGpu() {
         std::vector<GpuAction> v(m_vActions);
@@ -277,6 +406,8 @@ protected:
     std::vector<GpuAction> m_vActions;
     std::vector<double> m_vK;
     std::vector<Action<T> *> m_vHostEvals;
+    std::vector<GpuParamAction<T> *> m_vParamActions;
+    std::vector<Action<T> *> m_vHostOrder;   // the host evaluators in priority order
     const double *m_adEnvK;
     const double *m_adEnvW;
     bool m_bEnvDirty;
