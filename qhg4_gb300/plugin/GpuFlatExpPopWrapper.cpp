@@ -16,7 +16,10 @@ PopBase *createPop(ArrayShare *pAS, SCellGrid *pCG, PopFinder *pPopFinder, int i
                    uint32_t *aulState, uint *aiSeeds) {
     ArrayShare::setInstance(pAS);
     // the loader calls createPop with six arguments (populations/DynPopFactory.cpp:18,150):
-    // aiSeeds is not valid and is not passed on
-    return new GpuFlatExpPop(pCG, pPopFinder, iLayerSize, apIDG, aulState, NULL);
+    // aiSeeds is not valid; SPopulation's constructor copies NUM_SEEDS values
+    // from the pointer it gets (core/SPopulation.cpp:82), so it gets zeros
+    static uint s_aiNoSeeds[NUM_SEEDS] = {0};
+    (void)aiSeeds;
+    return new GpuFlatExpPop(pCG, pPopFinder, iLayerSize, apIDG, aulState, s_aiNoSeeds);
 }
 }
