@@ -1,0 +1,188 @@
+/*
+ * TEST INFRASTRUCTURE ONLY.  Runs the population plugin's GpuSexualPop the
+ * way QHG4 runs a population: agents in its LayerBuf, SPopulation::preLoop,
+ * then per step initializeStep / doActions per priority / finalizeStep
+ * (PopLooper::doStep, core/PopLooper.cpp:166-200), and preWrite, which
+ * copies the run's table back into the LayerBuf.  Linked against the
+ * oracle-backed stand-in for libqhg_gpu.so (qhg_gpu_fake.c), so it runs
+ * without a GPU; tests/test_plugin_host.py compares what it writes with the
+ * reference's own tut_Sexual actions (the Philox test build).
+ *
+ *   plugin_drive <input> <output>
+ * input: the oracle harness's input format (oracle/refsim_io.py) with the
+ * tutorial action set; output: u64 n, i64 id[n], i32 cell[n], f32 birth[n],
+ * f32 age[n], f32 lastb[n], u8 gender[n], u8 state[n], u32 C, u32 counts[C].
+ */
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "GpuSexualPop.cpp"
+
+class DrivePop : public GpuSexualPop {
+public:
+    DrivePop(SCellGrid *pCG, IDGen **apIDG, uint32_t *aulState, uint *aiSeeds)
+        : GpuSexualPop(pCG, NULL, 65536, apIDG, aulState, aiSeeds) {}
+
+    void prios(std::set<uint> &sPrios) { getPrios(sPrios); }
+
+    void load(uint32_t N, const int64_t *id, const int32_t *cell, const float *birth, const float *age,
+              const float *lastb, const uint8_t *gender, const uint8_t *state) {
+        if (N == 0) return;
+        const int iStart = (int)m_pAgentController->reserveSpace2(N);
+        for (uint32_t i = 0; i < N; i++) {
+            GpuSexualAgent &a = m_aAgents[iStart + (int)i];
+            a.m_iLifeState = state[i];
+            a.m_iCellIndex = cell[i];
+            a.m_ulID = (idtype)id[i];
+            a.m_ulCellID = m_pCG->m_aCells[cell[i]].m_iGlobalID;
+            a.m_fBirthTime = birth[i];
+            a.m_iGender = gender[i];
+            a.m_fAge = age[i];
+            a.m_fLastBirth = lastb[i];
+            a.m_iMateIndex = -3;
+        }
+    }
+
+    void write(FILE *f) {
+        std::vector<int64_t> id;
+        std::vector<int32_t> cell;
+        std::vector<float> birth, age, lastb;
+        std::vector<uint8_t> gender, state;
+        const int iFirst = getFirstAgentIndex();
+        if (iFirst != LBController::NIL) {
+            for (int iA = iFirst; iA <= getLastAgentIndex(); iA++) {
+                const GpuSexualAgent &a = m_aAgents[iA];
+                if (a.m_iLifeState <= 0) continue;
+                id.push_back((int64_t)a.m_ulID);
+                cell.push_back(a.m_iCellIndex);
+                birth.push_back(a.m_fBirthTime);
+                age.push_back(a.m_fAge);
+                lastb.push_back(a.m_fLastBirth);
+                gender.push_back(a.m_iGender);
+                state.push_back((uint8_t)a.m_iLifeState);
+            }
+        }
+        const uint64_t n = id.size();
+        fwrite(&n, 8, 1, f);
+        fwrite(id.data(), 8, n, f);
+        fwrite(cell.data(), 4, n, f);
+        fwrite(birth.data(), 4, n, f);
+        fwrite(age.data(), 4, n, f);
+        fwrite(lastb.data(), 4, n, f);
+        fwrite(gender.data(), 1, n, f);
+        fwrite(state.data(), 1, n, f);
+        updateNumAgentsPerCell();
+        const uint32_t C = (uint32_t)m_pCG->m_iNumCells;
+        fwrite(&C, 4, 1, f);
+        for (uint32_t c = 0; c < C; c++) {
+            const uint32_t k = (uint32_t)m_aiNumAgentsPerCell[c];
+            fwrite(&k, 4, 1, f);
+        }
+    }
+};
+
+static bool rd(FILE *f, void *p, size_t sz, size_t n) { return (n == 0) || (fread(p, sz, n, f) == n); }
+
+int main(int argc, char *argv[]) {
+    if (argc < 3) return 2;
+    FILE *fIn = fopen(argv[1], "rb");
+    if (fIn == NULL) return 2;
+    char magic[8];
+    uint32_t C, N, nSteps, iLayer, nAct;
+    uint64_t seed;
+    bool ok = rd(fIn, magic, 1, 8) && (memcmp(magic, "QHGREF01", 8) == 0);
+    ok = ok && rd(fIn, &C, 4, 1) && rd(fIn, &N, 4, 1) && rd(fIn, &nSteps, 4, 1) && rd(fIn, &iLayer, 4, 1);
+    ok = ok && rd(fIn, &seed, 8, 1) && rd(fIn, &nAct, 4, 1);
+    // the tutorial action set, parameters by type
+    std::string sParams;
+    char buf[256];
+    for (uint32_t i = 0; ok && (i < nAct); i++) {
+        uint32_t type, prio;
+        double p[4];
+        ok = rd(fIn, &type, 4, 1) && rd(fIn, &prio, 4, 1) && rd(fIn, p, 8, 4);
+        if (type == QHG_ACT_FERTILITY) {
+            snprintf(buf, sizeof(buf), "Fertility_min_age=%.17g;Fertility_max_age=%.17g;Fertility_interbirth=%.17g;",
+                     p[0], p[1], p[2]);
+        } else if (type == QHG_ACT_VERHULST) {
+            snprintf(buf, sizeof(buf), "Verhulst_b0=%.17g;Verhulst_d0=%.17g;Verhulst_theta=%.17g;Verhulst_K=%.17g;",
+                     p[0], p[1], p[2], p[3]);
+        } else if (type == QHG_ACT_RANDOMMOVE) {
+            snprintf(buf, sizeof(buf), "RandomMove_prob=%.17g;", p[0]);
+        } else {
+            buf[0] = '\0';
+        }
+        sParams += buf;
+    }
+    uint32_t iGenome = 0, iDump = 0;
+    int32_t iCross = 0;
+    double dMut = 0;
+    ok = ok && rd(fIn, &iGenome, 4, 1) && rd(fIn, &iCross, 4, 1) && rd(fIn, &dMut, 8, 1) && rd(fIn, &iDump, 4, 1);
+    std::vector<int32_t> vNbr(ok ? (size_t)C * 6 : 0);
+    std::vector<uint8_t> vNN(ok ? C : 0);
+    std::vector<double> vK(ok ? C : 0);
+    ok = ok && rd(fIn, vNbr.data(), 4, vNbr.size()) && rd(fIn, vNN.data(), 1, C) && rd(fIn, vK.data(), 8, C);
+    std::vector<int64_t> vID(ok ? N : 0);
+    std::vector<int32_t> vCell(ok ? N : 0);
+    std::vector<float> vB(ok ? N : 0), vA(ok ? N : 0), vL(ok ? N : 0);
+    std::vector<uint8_t> vG(ok ? N : 0), vS(ok ? N : 0);
+    ok = ok && rd(fIn, vID.data(), 8, N) && rd(fIn, vCell.data(), 4, N) && rd(fIn, vB.data(), 4, N) &&
+         rd(fIn, vA.data(), 4, N) && rd(fIn, vL.data(), 4, N) && rd(fIn, vG.data(), 1, N) && rd(fIn, vS.data(), 1, N);
+    fclose(fIn);
+    if (!ok || iGenome != 0) {
+        fprintf(stderr, "malformed input or genomes (not driven here)\n");
+        return 2;
+    }
+
+    stringmap smSurf;
+    smSurf[SURF_TYPE] = SURF_EQSAHEDRON;
+    SCellGrid *pCG = new SCellGrid(0, C, smSurf);
+    pCG->m_aCells = new SCell[C];
+    for (uint32_t c = 0; c < C; c++) {
+        pCG->m_aCells[c].m_iGlobalID = (gridtype)c;
+        pCG->m_aCells[c].m_iNumNeighbors = vNN[c];
+        for (int j = 0; j < 6; j++) pCG->m_aCells[c].m_aNeighbors[j] = vNbr[(size_t)c * 6 + j];
+        pCG->m_mIDIndexes[c] = c;
+    }
+    int nThreads = omp_get_max_threads();
+    IDGen **apIDG = new IDGen*[nThreads];
+    for (int t = 0; t < nThreads; t++) apIDG[t] = new IDGen(0, t, nThreads);
+    // GpuPop takes the run's seed from the first two state words
+    uint32_t aulState[16] = {0};
+    aulState[0] = (uint32_t)(seed & 0xffffffffu);
+    aulState[1] = (uint32_t)(seed >> 32);
+    static uint aiSeeds[NUM_SEEDS] = {0};
+
+    DrivePop *pPop = new DrivePop(pCG, apIDG, aulState, aiSeeds);
+    if (pPop->setParams(sParams) != 0) {
+        fprintf(stderr, "setParams refused [%s]\n", sParams.c_str());
+        return 3;
+    }
+    pPop->load(N, vID.data(), vCell.data(), vB.data(), vA.data(), vL.data(), vG.data(), vS.data());
+    if (pPop->preLoop() != 0) {
+        fprintf(stderr, "preLoop failed: %s\n", pPop->gpuError());
+        return 3;
+    }
+    std::set<uint> sPrios;
+    for (uint32_t s = 0; s < nSteps; s++) {
+        const float fT = (float)s;
+        int iRes = pPop->initializeStep(fT);
+        sPrios.clear();
+        pPop->prios(sPrios);
+        for (std::set<uint>::const_iterator it = sPrios.begin(); it != sPrios.end(); ++it) {
+            iRes += pPop->doActions(*it, fT);
+        }
+        iRes += pPop->finalizeStep();
+        if (iRes != 0) {
+            fprintf(stderr, "step %u failed\n", s);
+            return 4;
+        }
+    }
+    if (pPop->preWrite((float)nSteps) != 0) return 5;
+    FILE *fOut = fopen(argv[2], "wb");
+    if (fOut == NULL) return 2;
+    pPop->write(fOut);
+    fclose(fOut);
+    return 0;
+}

@@ -1,0 +1,88 @@
+"""The population plugin's host code under QHG4's step loop, without a GPU.
+
+tests/plugin_host/plugin_drive.cpp runs GpuSexualPop (qhg4_gb300/plugin) as
+QHG4 runs a population -- agents in its LayerBuf, preLoop, initializeStep /
+doActions / finalizeStep per step, preWrite -- linked against
+tests/plugin_host/qhg_gpu_fake.c, a stand-in for libqhg_gpu.so that runs
+the C ABI on the oracle.  What it copies back into its LayerBuf must equal
+the reference's own tutorial actions run by the Philox test build: this
+checks the plugin's glue (seed, parameters and priorities, the upload from
+the LayerBuf, the copy back), the part no machine here can run against the
+real library.  Needs the reference tree (headers, template code and the
+support objects built by oracle/ref/Makefile).
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle.refsim_io import ref_program, run_reference, write_input
+from qhg4_gb300.spec import config1_actions
+from qhg4_gb300.workload import Agents, make_agents, uniform_grid
+
+from helpers import table_diff
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REF = "/root/reference/QHG4"
+HERE = os.path.join(ROOT, "tests", "plugin_host")
+
+
+def build_driver(out: str) -> str:
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref")], check=True, capture_output=True,
+                   timeout=1200)
+    fake = os.path.join(out, "libqhg_gpu.so")
+    subprocess.run(["gcc", "-O2", "-fPIC", "-fopenmp", "-ffp-contract=off", "-std=c11", "-shared",
+                    "-I" + os.path.join(ROOT, "include"), os.path.join(HERE, "qhg_gpu_fake.c"),
+                    os.path.join(ROOT, "oracle", "qhg_oracle.c"), "-lm", "-o", fake], check=True, timeout=300)
+    refobj = os.path.join(ROOT, "oracle", "_ref", "well")
+    objs = [os.path.join(refobj, f) for f in sorted(os.listdir(refobj)) if f.endswith(".o") and f != "harness.o"]
+    inc = ["-I" + os.path.join(REF, d) for d in ("core", "actions", "utils", "io", "genes", "utils_qhg", "icosa",
+                                                   "populations", "geoinfo")]
+    exe = os.path.join(out, "plugin_drive")
+    r = subprocess.run(["g++", "-std=c++20", "-O1", "-fopenmp", "-w", "-I" + os.path.join(ROOT, "oracle", "ref", "shim")]
+                       + inc + ["-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(ROOT, "qhg4_gb300", "plugin"),
+                                os.path.join(HERE, "plugin_drive.cpp")] + objs
+                       + ["-L" + out, "-Wl,-rpath," + out, "-lqhg_gpu", "-lz", "-o", exe],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-3000:]
+    return exe
+
+
+def read_drive_output(path: str):
+    b = open(path, "rb").read()
+    pos = 0
+
+    def take(dt, n):
+        nonlocal pos
+        a = np.frombuffer(b, dtype=dt, count=n, offset=pos).copy()
+        pos += np.dtype(dt).itemsize * n
+        return a
+
+    n = int(take("<u8", 1)[0])
+    a = Agents(take("<i8", n), take("<i4", n), take("<f4", n), take("<f4", n), take("<f4", n), take("u1", n),
+               take("u1", n))
+    C = int(take("<u4", 1)[0])
+    return a, take("<u4", C)
+
+
+@pytest.mark.skipif(not os.path.isdir(REF), reason="the reference tree is not present")
+def test_plugin_population_equals_reference_actions(tmp_path):
+    out = str(tmp_path)
+    exe = build_driver(out)
+    grid = uniform_grid(8, 30.0)
+    agents = make_agents(grid, 15000, seed=71, age_max=50.0)
+    acts = config1_actions(b0=0.3, d0=0.03, move_p=0.2)
+    pin, pout = os.path.join(out, "in.bin"), os.path.join(out, "drive.bin")
+    write_input(pin, grid, agents, acts, 25, 4711)
+    r = subprocess.run([exe, pin, pout], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    got, counts = read_drive_output(pout)
+    ref = run_reference("philox", out, grid, agents, acts, 25, 4711, threads=2)
+    assert ref.draw_errors == 0
+    order = np.argsort(got.id, kind="stable")
+    got = Agents(*(getattr(got, k)[order] for k in ("id", "cell", "birth", "age", "lastb", "gender", "state")))
+    d = table_diff(got, ref.agents)
+    assert d is None, d
+    assert np.array_equal(counts, np.bincount(ref.agents.cell, minlength=grid.num_cells).astype(np.uint32))
+    assert len(got) > 5000
