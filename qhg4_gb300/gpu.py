@@ -20,6 +20,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libqhg_gpu.so")
 
 QHG_FLAG_LOG_BIRTHS = 1
 QHG_FLAG_TRACK_OCCUPANCY = 2
+QHG_MOVESTATS_FIRST, QHG_MOVESTATS_MIN, QHG_MOVESTATS_LAST = 0, 1, 2   # MoveStats modes
 
 ERRORS = {
     -1: "QHG_ERR_ARG", -2: "QHG_ERR_CUDA", -3: "QHG_ERR_NOMEM", -4: "QHG_ERR_STATE",
