@@ -149,3 +149,48 @@ def test_port_oracle_move_stats_against_reference_build(tmp_path, moves):
     assert np.array_equal(h, rh)
     assert np.array_equal(d.view(np.uint64), rd.view(np.uint64))
     assert np.array_equal(t.view(np.uint64), rt.view(np.uint64))
+
+
+@pytest.mark.skipif(not os.path.exists(ref_program("philox")), reason="reference build not present")
+@pytest.mark.parametrize("case", range(int(os.environ.get("QHG_PIN_CASES", "8"))))
+def test_port_oracle_random_programs_against_reference_build(tmp_path, case):
+    """Random action lists -- which actions, their priorities (ties broken by
+    name), their parameters -- through the oracle and the reference's own
+    classes: the oracle's action chain, draw windows and ordering rules hold
+    for any program, not only the ones the other cases fix."""
+    from qhg4_gb300.spec import (ACT_ATANDEATH, ACT_FERTILITY, ACT_GETOLD, ACT_OLDAGEDEATH, ACT_RANDOMMOVE,
+                                 ACT_RANDOMPAIR, ACT_VERHULST, ACT_VERHULSTVARK, ACT_WEIGHTEDMOVE, Action)
+    from qhg4_gb300.workload import make_agents, terrain_grid
+    rng = np.random.default_rng(500 + case)
+
+    def prio():
+        return int(rng.integers(1, 6))
+
+    acts = [Action(ACT_FERTILITY, prio(), (float(rng.uniform(10, 20)), float(rng.uniform(35, 50)),
+                                           float(rng.uniform(0, 3)))),
+            Action(ACT_RANDOMPAIR, prio())]
+    if rng.random() < 0.5:
+        acts.append(Action(ACT_VERHULST, prio(), (float(rng.uniform(0.1, 0.5)), float(rng.uniform(0.01, 0.08)),
+                                                  0.01, float(rng.uniform(20, 80)))))
+    else:
+        acts.append(Action(ACT_VERHULSTVARK, prio(), (float(rng.uniform(0.1, 0.5)), float(rng.uniform(0.01, 0.08)),
+                                                      0.01)))
+    if rng.random() < 0.6:
+        acts.append(Action(ACT_RANDOMMOVE, prio(), (float(rng.uniform(0.05, 0.5)),)))
+    if rng.random() < 0.6:
+        acts.append(Action(ACT_WEIGHTEDMOVE, prio(), (float(rng.uniform(0.05, 0.5)),)))
+    if rng.random() < 0.6:
+        acts.append(Action(ACT_OLDAGEDEATH, prio(), (float(rng.uniform(50, 70)), float(rng.uniform(0.01, 0.15)))))
+    if rng.random() < 0.5:
+        acts.append(Action(ACT_ATANDEATH, prio(), (float(rng.uniform(45, 65)), float(rng.uniform(5, 20)),
+                                                   float(rng.uniform(-0.6, 0.6)))))
+    if rng.random() < 0.8:
+        acts.append(Action(ACT_GETOLD, prio()))
+    grid = terrain_grid(8, seed=600 + case)
+    agents = make_agents(grid, 5000, seed=700 + case, age_max=75.0, proportional_to_K=True)
+    ref = run_reference("philox", str(tmp_path), grid, agents, acts, 15, 800 + case, threads=2)
+    r, st = port.run(grid, agents, acts, 15, 800 + case)
+    assert ref.draw_errors == 0
+    d = table_diff(r.agents(), ref.agents)
+    assert d is None, (d, [(a.type, a.prio) for a in acts])
+    assert np.array_equal(st, ref.stats)
