@@ -8,12 +8,15 @@
  * without a GPU; tests/test_plugin_host.py compares what it writes with the
  * reference's own tut_Sexual actions (the Philox test build).
  *
- *   plugin_drive <input> <output>
+ *   plugin_drive <input> <output> [write_every]
+ * write_every > 0: preWrite every that many steps as well (QHG4 writes a
+ * snapshot that way), the LayerBuf rewritten while the run goes on.
  * input: the oracle harness's input format (oracle/refsim_io.py) with the
  * tutorial action set; output: u64 n, i64 id[n], i32 cell[n], f32 birth[n],
  * f32 age[n], f32 lastb[n], u8 gender[n], u8 state[n], u32 C, u32 counts[C].
  */
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -87,6 +90,7 @@ static bool rd(FILE *f, void *p, size_t sz, size_t n) { return (n == 0) || (frea
 
 int main(int argc, char *argv[]) {
     if (argc < 3) return 2;
+    const int iWriteEvery = (argc > 3) ? atoi(argv[3]) : 0;
     FILE *fIn = fopen(argv[1], "rb");
     if (fIn == NULL) return 2;
     char magic[8];
@@ -174,6 +178,7 @@ int main(int argc, char *argv[]) {
             iRes += pPop->doActions(*it, fT);
         }
         iRes += pPop->finalizeStep();
+        if ((iWriteEvery > 0) && (((s + 1) % (uint32_t)iWriteEvery) == 0)) iRes += pPop->preWrite(fT);
         if (iRes != 0) {
             fprintf(stderr, "step %u failed\n", s);
             return 4;

@@ -67,7 +67,8 @@ def read_drive_output(path: str):
 
 
 @pytest.mark.skipif(not os.path.isdir(REF), reason="the reference tree is not present")
-def test_plugin_population_equals_reference_actions(tmp_path):
+@pytest.mark.parametrize("write_every", [0, 4], ids=["no_snapshots", "snapshot_every_4"])
+def test_plugin_population_equals_reference_actions(tmp_path, write_every):
     out = str(tmp_path)
     exe = build_driver(out)
     grid = uniform_grid(8, 30.0)
@@ -75,7 +76,7 @@ def test_plugin_population_equals_reference_actions(tmp_path):
     acts = config1_actions(b0=0.3, d0=0.03, move_p=0.2)
     pin, pout = os.path.join(out, "in.bin"), os.path.join(out, "drive.bin")
     write_input(pin, grid, agents, acts, 25, 4711)
-    r = subprocess.run([exe, pin, pout], capture_output=True, text=True, timeout=600)
+    r = subprocess.run([exe, pin, pout, str(write_every)], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     got, counts = read_drive_output(pout)
     ref = run_reference("philox", out, grid, agents, acts, 25, 4711, threads=2)
