@@ -10,10 +10,11 @@
  *
  * What changes against SPopulation<T>:
  *   preLoop        after SPopulation's preLoop: creates the GPU run from the
- *                  action list given by addGpuAction (types and parameters in
- *                  QHG_ACT_* slots), uploads the cell grid (SCellGrid
- *                  neighbours), the capacity array and the live agents of the
- *                  LayerBuf
+ *                  action list given by addGpuAction / addGpuParamAction
+ *                  (types and parameters in QHG_ACT_* slots), uploads the
+ *                  cell grid (SCellGrid neighbours), the capacity array and
+ *                  the live agents of the LayerBuf (with their genomes, when
+ *                  setGpuGenetics names the genome buffer)
  *   initializeStep runs the initialize of the environment evaluators that
  *                  stay on the host (addHostEvaluator: the reference's own
  *                  NPPCapacity, SingleEvaluator, MultiEvaluator objects) and,
@@ -58,6 +59,7 @@
 #include "VerhulstVarK.h"
 #include "WeightedMove.h"
 #include "LBController.h"
+#include "LayerArrBuf.h"
 #include "SCellGrid.h"
 #include "qhg_gpu.h"
 
@@ -140,7 +142,8 @@ public:
     GpuPop(SCellGrid *pCG, PopFinder *pPopFinder, int iLayerSize, IDGen **apIDG, uint32_t *aulState,
            uint *aiSeeds)
         : SPopulation<T>(pCG, pPopFinder, iLayerSize, apIDG, aulState, aiSeeds),
-          m_pRun(NULL), m_bStale(false), m_iDevice(0), m_adEnvK(NULL), m_adEnvW(NULL), m_bEnvDirty(true) {
+          m_pRun(NULL), m_bStale(false), m_iDevice(0), m_adEnvK(NULL), m_adEnvW(NULL), m_bEnvDirty(true),
+          m_iGenomeSize(0), m_iNumCrossover(0), m_dMutationRate(0), m_pGenome(NULL) {
         // the GPU run's seed from the population's generator state
         m_ulSeed = (aulState != NULL) ? ((uint64_t)aulState[0] | ((uint64_t)aulState[1] << 32)) : 0;
     }
@@ -176,6 +179,18 @@ public:
     // capacity per cell (VerhulstVarK's K, WeightedMove's weights)
     void setGpuCapacity(const double *adK, int iNumCells) { m_vK.assign(adK, adK + iNumCells); }
     void setGpuDevice(int iDevice) { m_iDevice = iDevice; }
+    // genetics of the run (Genetics_genome_size, Genetics_num_crossover or
+    // QHG_CROSSOVER_POISSON1, Genetics_mutation_rate) and the genome buffer
+    // the population keeps beside its agents (a LayerArrBuf of
+    // 2 x ceil(size / 64) words per agent slot, strand 0 then strand 1, as
+    // Genetics::m_aGenome, actions/Genetics.cpp:205-213, registered with the
+    // agent controller): uploaded with the agents, written back by preWrite
+    void setGpuGenetics(int iGenomeSize, int iNumCrossover, double dMutationRate, LayerArrBuf<ulong> *pGenome) {
+        m_iGenomeSize = iGenomeSize;
+        m_iNumCrossover = iNumCrossover;
+        m_dMutationRate = dMutationRate;
+        m_pGenome = pGenome;
+    }
     // an environment evaluator kept on the host (not owned; also added to the
     // Prioritizer, which gives it its attributes and priority): its
     // initialize runs at each initializeStep and its finalize at each
@@ -314,6 +329,11 @@ protected:
             for (int k = 0; k < 4; k++) d.action_param[i][k] = v[i].adP[k];
         }
         d.device = m_iDevice;
+        if (m_pGenome != NULL) {
+            d.genome_size = m_iGenomeSize;
+            d.num_crossover = m_iNumCrossover;
+            d.mutation_rate = m_dMutationRate;
+        }
         if (qhg_gpu_create(&d, &m_pRun) != QHG_OK) return -1;
         // grid: neighbours of each cell, -1 padded to 6
         const int C = (int)this->m_pCG->m_iNumCells;
@@ -332,12 +352,18 @@ protected:
         std::vector<int32_t> vCell;
         std::vector<float> vBirth, vAge, vLast;
         std::vector<uint8_t> vGender, vState;
+        std::vector<uint64_t> vGenome;
+        const size_t nW = genomeWords();
         const int iFirst = this->getFirstAgentIndex();
         if (iFirst != LBController::NIL) {
             const int iLast = this->getLastAgentIndex();
             for (int iA = iFirst; iA <= iLast; iA++) {
                 const T &a = this->m_aAgents[iA];
                 if (a.m_iLifeState <= 0) continue;
+                if (nW > 0) {
+                    const ulong *g = &(*m_pGenome)[(uint)iA];
+                    vGenome.insert(vGenome.end(), g, g + nW);
+                }
                 vID.push_back((int64_t)a.m_ulID);
                 vCell.push_back((int32_t)a.m_iCellIndex);
                 vBirth.push_back(a.m_fBirthTime);
@@ -348,10 +374,15 @@ protected:
             }
         }
         qhg_agents_soa s = {vID.data(), vCell.data(), vBirth.data(), vAge.data(), vLast.data(),
-                            vGender.data(), vState.data(), NULL};
+                            vGender.data(), vState.data(), (nW > 0) ? vGenome.data() : NULL};
         if (qhg_gpu_upload_agents(m_pRun, &s, (int64_t)vID.size(), 0) != QHG_OK) return -1;
         m_bStale = false;
         return 0;
+    }
+
+    // genome words per agent (0 without genetics)
+    size_t genomeWords() const {
+        return ((m_pGenome != NULL) && (m_iGenomeSize > 0)) ? 2 * (size_t)((m_iGenomeSize + 63) / 64) : 0;
     }
 
     void pullCounts() {
@@ -375,8 +406,10 @@ protected:
         std::vector<int32_t> vCell((size_t)n);
         std::vector<float> vBirth((size_t)n), vAge((size_t)n), vLast((size_t)n);
         std::vector<uint8_t> vGender((size_t)n), vState((size_t)n);
+        const size_t nW = genomeWords();
+        std::vector<uint64_t> vGenome((size_t)n * nW);
         qhg_agents_soa s = {vID.data(), vCell.data(), vBirth.data(), vAge.data(), vLast.data(),
-                            vGender.data(), vState.data(), NULL};
+                            vGender.data(), vState.data(), (nW > 0) ? vGenome.data() : NULL};
         int64_t got = 0;
         if (qhg_gpu_download(m_pRun, &s, n, &got) != QHG_OK) return -1;
         this->m_pAgentController->clear();
@@ -392,6 +425,10 @@ protected:
                 a.m_iGender = vGender[(size_t)i];
                 a.m_fAge = vAge[(size_t)i];
                 a.m_fLastBirth = vLast[(size_t)i];
+                if (nW > 0) {
+                    memcpy(&(*m_pGenome)[(uint)(iStart + (int)i)], vGenome.data() + (size_t)i * nW,
+                           nW * sizeof(uint64_t));
+                }
             }
         }
         pullCounts();
@@ -411,6 +448,10 @@ protected:
     const double *m_adEnvK;
     const double *m_adEnvW;
     bool m_bEnvDirty;
+    int m_iGenomeSize;
+    int m_iNumCrossover;
+    double m_dMutationRate;
+    LayerArrBuf<ulong> *m_pGenome;
 };
 
 #endif

@@ -12,8 +12,10 @@
  * write_every > 0: preWrite every that many steps as well (QHG4 writes a
  * snapshot that way), the LayerBuf rewritten while the run goes on.
  * input: the oracle harness's input format (oracle/refsim_io.py) with the
- * tutorial action set; output: u64 n, i64 id[n], i32 cell[n], f32 birth[n],
- * f32 age[n], f32 lastb[n], u8 gender[n], u8 state[n], u32 C, u32 counts[C].
+ * tutorial action set (and genomes, kept in a LayerArrBuf registered with the
+ * agent controller as Genetics keeps them); output: u64 n, i64 id[n],
+ * i32 cell[n], f32 birth[n], f32 age[n], f32 lastb[n], u8 gender[n],
+ * u8 state[n], u32 C, u32 counts[C], u32 words, u64 genome[n * words].
  */
 #include <cstdio>
 #include <cstdlib>
@@ -22,6 +24,7 @@
 #include <vector>
 
 #include "GpuSexualPop.cpp"
+#include "LayerArrBuf.cpp"
 
 class DrivePop : public GpuSexualPop {
 public:
@@ -30,8 +33,17 @@ public:
 
     void prios(std::set<uint> &sPrios) { getPrios(sPrios); }
 
+    // genomes beside the agents, as Genetics::init sets them up
+    // (actions/Genetics.cpp:205-213)
+    void enableGenomes(int iGenomeSize, int iNumCrossover, double dMutationRate) {
+        m_iWords = 2 * (uint)((iGenomeSize + 63) / 64);
+        m_aGenomes.init(m_pAgentController->getLayerSize(), m_iWords);
+        m_pAgentController->addBuffer(static_cast<LBBase *>(&m_aGenomes));
+        setGpuGenetics(iGenomeSize, iNumCrossover, dMutationRate, &m_aGenomes);
+    }
+
     void load(uint32_t N, const int64_t *id, const int32_t *cell, const float *birth, const float *age,
-              const float *lastb, const uint8_t *gender, const uint8_t *state) {
+              const float *lastb, const uint8_t *gender, const uint8_t *state, const uint64_t *genome) {
         if (N == 0) return;
         const int iStart = (int)m_pAgentController->reserveSpace2(N);
         for (uint32_t i = 0; i < N; i++) {
@@ -45,6 +57,8 @@ public:
             a.m_fAge = age[i];
             a.m_fLastBirth = lastb[i];
             a.m_iMateIndex = -3;
+            if (m_iWords > 0) memcpy(&m_aGenomes[(uint)(iStart + (int)i)], genome + (size_t)i * m_iWords,
+                                     m_iWords * sizeof(uint64_t));
         }
     }
 
@@ -53,6 +67,7 @@ public:
         std::vector<int32_t> cell;
         std::vector<float> birth, age, lastb;
         std::vector<uint8_t> gender, state;
+        std::vector<uint64_t> genome;
         const int iFirst = getFirstAgentIndex();
         if (iFirst != LBController::NIL) {
             for (int iA = iFirst; iA <= getLastAgentIndex(); iA++) {
@@ -65,6 +80,10 @@ public:
                 lastb.push_back(a.m_fLastBirth);
                 gender.push_back(a.m_iGender);
                 state.push_back((uint8_t)a.m_iLifeState);
+                if (m_iWords > 0) {
+                    const ulong *g = &m_aGenomes[(uint)iA];
+                    genome.insert(genome.end(), g, g + m_iWords);
+                }
             }
         }
         const uint64_t n = id.size();
@@ -83,7 +102,12 @@ public:
             const uint32_t k = (uint32_t)m_aiNumAgentsPerCell[c];
             fwrite(&k, 4, 1, f);
         }
+        fwrite(&m_iWords, 4, 1, f);
+        fwrite(genome.data(), 8, genome.size(), f);
     }
+
+    uint m_iWords = 0;
+    LayerArrBuf<ulong> m_aGenomes;
 };
 
 static bool rd(FILE *f, void *p, size_t sz, size_t n) { return (n == 0) || (fread(p, sz, n, f) == n); }
@@ -133,9 +157,12 @@ int main(int argc, char *argv[]) {
     std::vector<uint8_t> vG(ok ? N : 0), vS(ok ? N : 0);
     ok = ok && rd(fIn, vID.data(), 8, N) && rd(fIn, vCell.data(), 4, N) && rd(fIn, vB.data(), 4, N) &&
          rd(fIn, vA.data(), 4, N) && rd(fIn, vL.data(), 4, N) && rd(fIn, vG.data(), 1, N) && rd(fIn, vS.data(), 1, N);
+    const size_t nWords = (iGenome > 0) ? (size_t)N * 2 * ((iGenome + 63) / 64) : 0;
+    std::vector<uint64_t> vGen(ok ? nWords : 0);
+    ok = ok && rd(fIn, vGen.data(), 8, nWords);
     fclose(fIn);
-    if (!ok || iGenome != 0) {
-        fprintf(stderr, "malformed input or genomes (not driven here)\n");
+    if (!ok) {
+        fprintf(stderr, "malformed input\n");
         return 2;
     }
 
@@ -163,7 +190,8 @@ int main(int argc, char *argv[]) {
         fprintf(stderr, "setParams refused [%s]\n", sParams.c_str());
         return 3;
     }
-    pPop->load(N, vID.data(), vCell.data(), vB.data(), vA.data(), vL.data(), vG.data(), vS.data());
+    if (iGenome > 0) pPop->enableGenomes((int)iGenome, iCross, dMut);
+    pPop->load(N, vID.data(), vCell.data(), vB.data(), vA.data(), vL.data(), vG.data(), vS.data(), vGen.data());
     if (pPop->preLoop() != 0) {
         fprintf(stderr, "preLoop failed: %s\n", pPop->gpuError());
         return 3;

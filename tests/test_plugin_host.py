@@ -18,7 +18,7 @@ import numpy as np
 import pytest
 
 from oracle.refsim_io import ref_program, run_reference, write_input
-from qhg4_gb300.spec import config1_actions
+from qhg4_gb300.spec import CROSSOVER_POISSON1, Genetics, config1_actions, config3_actions
 from qhg4_gb300.workload import Agents, make_agents, uniform_grid
 
 from helpers import table_diff
@@ -49,6 +49,13 @@ def build_driver(out: str) -> str:
     return exe
 
 
+@pytest.fixture(scope="module")
+def driver(tmp_path_factory):
+    if not os.path.isdir(REF):
+        pytest.skip("the reference tree is not present")
+    return build_driver(str(tmp_path_factory.mktemp("plugin_drive")))
+
+
 def read_drive_output(path: str):
     b = open(path, "rb").read()
     pos = 0
@@ -63,14 +70,18 @@ def read_drive_output(path: str):
     a = Agents(take("<i8", n), take("<i4", n), take("<f4", n), take("<f4", n), take("<f4", n), take("u1", n),
                take("u1", n))
     C = int(take("<u4", 1)[0])
-    return a, take("<u4", C)
+    counts = take("<u4", C)
+    words = int(take("<u4", 1)[0])
+    if words > 0:
+        a.genome = take("<u8", n * words).reshape(n, words)
+    return a, counts
 
 
 @pytest.mark.skipif(not os.path.isdir(REF), reason="the reference tree is not present")
 @pytest.mark.parametrize("write_every", [0, 4], ids=["no_snapshots", "snapshot_every_4"])
-def test_plugin_population_equals_reference_actions(tmp_path, write_every):
+def test_plugin_population_equals_reference_actions(tmp_path, driver, write_every):
     out = str(tmp_path)
-    exe = build_driver(out)
+    exe = driver
     grid = uniform_grid(8, 30.0)
     agents = make_agents(grid, 15000, seed=71, age_max=50.0)
     acts = config1_actions(b0=0.3, d0=0.03, move_p=0.2)
@@ -81,9 +92,32 @@ def test_plugin_population_equals_reference_actions(tmp_path, write_every):
     got, counts = read_drive_output(pout)
     ref = run_reference("philox", out, grid, agents, acts, 25, 4711, threads=2)
     assert ref.draw_errors == 0
-    order = np.argsort(got.id, kind="stable")
-    got = Agents(*(getattr(got, k)[order] for k in ("id", "cell", "birth", "age", "lastb", "gender", "state")))
+    got = got.sorted_by_id()
     d = table_diff(got, ref.agents)
     assert d is None, d
     assert np.array_equal(counts, np.bincount(ref.agents.cell, minlength=grid.num_cells).astype(np.uint32))
     assert len(got) > 5000
+
+
+@pytest.mark.skipif(not os.path.isdir(REF), reason="the reference tree is not present")
+@pytest.mark.parametrize("genetics", [Genetics(512, CROSSOVER_POISSON1, 1e-3), Genetics(200, 2, 5e-3)],
+                         ids=["poisson_512", "fixed2_200"])
+def test_plugin_population_with_genomes(tmp_path, driver, genetics):
+    """With genomes kept beside the agents (setGpuGenetics): uploaded with the
+    LayerBuf, crossed and mutated by the run, written back by preWrite --
+    against the reference's Genetics / BitGeneUtils in the Philox test build."""
+    out = str(tmp_path)
+    exe = driver
+    grid = uniform_grid(5, 40.0)
+    agents = make_agents(grid, 3000, seed=72, age_max=50.0, genome_blocks=genetics.num_blocks)
+    acts = config3_actions()
+    pin, pout = os.path.join(out, "in.bin"), os.path.join(out, "drive.bin")
+    write_input(pin, grid, agents, acts, 15, 4712, genetics)
+    r = subprocess.run([exe, pin, pout, "5"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    got, counts = read_drive_output(pout)
+    ref = run_reference("philox", out, grid, agents, acts, 15, 4712, genetics, threads=2)
+    assert ref.draw_errors == 0
+    d = table_diff(got.sorted_by_id(), ref.agents)
+    assert d is None, d
+    assert len(ref.births) > 0
