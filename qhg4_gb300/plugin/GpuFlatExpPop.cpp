@@ -8,6 +8,9 @@
 #include "SingleEvaluator.cpp"
 #include "MultiEvaluator.cpp"
 #include "NPPCapacity.cpp"
+#include "LayerArrBuf.cpp"
+#include "Genetics.cpp"
+#include "GenomeCreator.cpp"
 
 #include <cstring>
 
@@ -16,7 +19,7 @@
 GpuFlatExpPop::GpuFlatExpPop(SCellGrid *pCG, PopFinder *pPopFinder, int iLayerSize, IDGen **apIDG,
                              uint32_t *aulState, uint *aiSeeds)
     : GpuPop<GpuFlatExpAgent>(pCG, pPopFinder, iLayerSize, apIDG, aulState, aiSeeds),
-      m_adCapacities(NULL), m_adEnvWeights(NULL), m_pNPPCap(NULL), m_pME(NULL) {
+      m_adCapacities(NULL), m_adEnvWeights(NULL), m_pNPPCap(NULL), m_pME(NULL), m_pGenetics(NULL) {
     m_sSpeciesName = "GpuFlatExp";
     m_sClassName = "GpuFlatExpPop";
     const size_t C = (size_t)m_pCG->m_iNumCells;
@@ -51,15 +54,34 @@ GpuFlatExpPop::GpuFlatExpPop(SCellGrid *pCG, PopFinder *pPopFinder, int iLayerSi
     addGpuParamAction(QHG_ACT_OLDAGEDEATH);
     addGpuParamAction(QHG_ACT_FERTILITY);
 
+    // the genomes: the reference's Genetics for attributes, initial genomes
+    // and the buffer beside the agents (its own step work is the GPU's)
+    m_pGenetics = new GpuFlatExpGenetics(this, m_pCG, m_pAgentController, &m_vMergedDeadList, m_apWELL);
+    m_prio.addAction(m_pGenetics);
+
     // the GPU run takes the weights as cells x 7 (connectivity 6)
     if (m_pCG->m_iConnectivity == 6) setGpuEnvironment(NULL, m_adEnvWeights);
 }
 
 GpuFlatExpPop::~GpuFlatExpPop() {
+    delete m_pGenetics;
     delete m_pME;
     delete m_pNPPCap;
     delete[] m_adEnvWeights;
     delete[] m_adCapacities;
+}
+
+// after SPopulation's preLoop, as FlatExpPop::preLoop does: the initial
+// genomes; the GPU run then gets the genetics the Genetics object read from
+// the configuration and its genome buffer
+int GpuFlatExpPop::prepareGpu() {
+    int iResult = 0;
+    if (m_pGenetics->getGenomeSize() > 0) {
+        iResult = m_pGenetics->createInitialGenomes(getNumAgentsEffective());
+        setGpuGenetics(m_pGenetics->getGenomeSize(), m_pGenetics->numCrossOvers(), m_pGenetics->mutationRate(),
+                       m_pGenetics->getGenome());
+    }
+    return iResult;
 }
 
 // age and last birth time follow the basic agent data in the species' agent lines

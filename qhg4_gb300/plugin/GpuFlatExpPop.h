@@ -13,14 +13,21 @@
  * GpuParamActions: their attributes and priorities come from the same
  * configuration modules the reference's actions read.
  *
- * Not carried over: the genomes of FlatExpPop's Genetics (the GPU library
- * steps genomes, but this plugin uploads none), and updateEvent's drowning
- * of agents in water or ice cells after a geography event.
+ * Genomes: the reference's Genetics object stays on the host for what it
+ * does there -- its attributes, the initial genomes (createInitialGenomes in
+ * preLoop, as FlatExpPop::preLoop calls it) and the genome buffer beside the
+ * agents that QDF writing reads; crossover and mutation of the newborns run
+ * on the GPU (setGpuGenetics), and preWrite brings the genomes back.
+ *
+ * Not carried over: updateEvent's drowning of agents in water or ice cells
+ * after a geography event.
  */
 #ifndef QHG_GPUFLATEXPPOP_H
 #define QHG_GPUFLATEXPPOP_H
 
 #include "GpuPop.h"
+#include "BitGeneUtils.h"
+#include "Genetics.h"
 #include "Geography.h"
 #include "MultiEvaluator.h"
 #include "NPPCapacity.h"
@@ -33,12 +40,27 @@ struct GpuFlatExpAgent : Agent {
     int m_iNumBabies;
 };
 
+// the reference's Genetics with the parameters it read readable
+class GpuFlatExpGenetics : public Genetics<GpuFlatExpAgent, BitGeneUtils> {
+public:
+    GpuFlatExpGenetics(SPopulation<GpuFlatExpAgent> *pPop, SCellGrid *pCG, LBController *pAgentController,
+                       std::vector<int> *pvDeadList, WELL512 **apWELL)
+        : Genetics<GpuFlatExpAgent, BitGeneUtils>(pPop, pCG, "", pAgentController, pvDeadList, apWELL) {}
+    int numCrossOvers() const { return m_iNumCrossOvers; }
+    double mutationRate() const { return m_dMutationRate; }
+    // newborns' genomes are made by the GPU run
+    virtual int initialize(float fT) { return 0; }
+    virtual int execute(int iA, float fT) { return 0; }
+    virtual int finalize(float fT) { return 0; }
+};
+
 class GpuFlatExpPop : public GpuPop<GpuFlatExpAgent> {
 public:
     GpuFlatExpPop(SCellGrid *pCG, PopFinder *pPopFinder, int iLayerSize, IDGen **apIDG, uint32_t *aulState,
                   uint *aiSeeds);
     virtual ~GpuFlatExpPop();
 
+    virtual int prepareGpu();
     int addPopSpecificAgentData(int iAgentIndex, char **ppData);
     int makePopSpecificOffspring(int iAgent, int iMother, int iFather);
 
@@ -47,6 +69,7 @@ protected:
     double *m_adEnvWeights;    // the MultiEvaluator's cumulative weights, cells x (connectivity + 1)
     NPPCapacity<GpuFlatExpAgent> *m_pNPPCap;
     MultiEvaluator<GpuFlatExpAgent> *m_pME;
+    GpuFlatExpGenetics *m_pGenetics;
 };
 
 #endif

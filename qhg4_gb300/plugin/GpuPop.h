@@ -211,10 +211,15 @@ public:
 
     virtual int preLoop() {
         int iResult = SPopulation<T>::preLoop();
+        if (iResult == 0) iResult = prepareGpu();
         if (iResult == 0) collectParamActions();
         if (iResult == 0) iResult = startGpu();
         return iResult;
     }
+
+    // between SPopulation's preLoop and the creation of the GPU run: what a
+    // population's own preLoop does with its agents first (initial genomes)
+    virtual int prepareGpu() { return 0; }
 
     virtual int initializeStep(float fTime) {
         if (m_pRun == NULL) return -1;
