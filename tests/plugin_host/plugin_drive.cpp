@@ -8,9 +8,14 @@
  * without a GPU; tests/test_plugin_host.py compares what it writes with the
  * reference's own tut_Sexual actions (the Philox test build).
  *
- *   plugin_drive <input> <output> [write_every]
+ *   plugin_drive <input> <output> [write_every] [param]
  * write_every > 0: preWrite every that many steps as well (QHG4 writes a
  * snapshot that way), the LayerBuf rewritten while the run goes on.
+ * "param": the population's actions are the input's action list as
+ * GpuParamActions, configured the way QHG4 configures a population --
+ * priorities through SPopulation::setPrioList, attributes through
+ * Prioritizer::getActionAttributes from one module per action -- with K per
+ * cell from the input (VerhulstVarK, WeightedMove's weights).
  * input: the oracle harness's input format (oracle/refsim_io.py) with the
  * tutorial action set (and genomes, kept in a LayerArrBuf registered with the
  * agent controller as Genetics keeps them); output: u64 n, i64 id[n],
@@ -32,6 +37,35 @@ public:
         : GpuSexualPop(pCG, NULL, 65536, apIDG, aulState, aiSeeds) {}
 
     void prios(std::set<uint> &sPrios) { getPrios(sPrios); }
+
+    // the input's actions as parameter actions, configured from modules
+    int configureActions(const std::vector<uint32_t> &vType, const std::vector<uint32_t> &vPrio,
+                         const std::vector<double> &vP, const double *adK) {
+        m_bParamMode = true;
+        modulemap mModules;
+        for (size_t i = 0; i < vType.size(); i++) {
+            if (addGpuParamAction((int32_t)vType[i]) != 0) return -1;
+            GpuParamAction<GpuSexualAgent> *pA = m_vParamActions.back();
+            m_mPrioInfo[pA->getActionName()] = (int)vPrio[i];
+            ModuleComplex *pMC = new ModuleComplex();
+            char buf[64];
+            for (size_t k = 0; k < pA->m_vSlots.size(); k++) {
+                snprintf(buf, sizeof(buf), "%.17g", vP[i * 4 + k]);
+                pMC->addParam(pA->m_vSlots[k], buf);
+            }
+            mModules[pA->getActionName()] = pMC;
+        }
+        int iResult = setPrioList();
+        if (iResult == 0) iResult = m_prio.getActionAttributes(mModules);
+        for (modulemap::iterator it = mModules.begin(); it != mModules.end(); ++it) delete it->second;
+        setGpuCapacity(adK, (int)m_pCG->m_iNumCells);
+        return iResult;
+    }
+
+    // the tutorial actions of GpuSexualPop, or the configured ones
+    virtual int preLoop() {
+        return m_bParamMode ? GpuPop<GpuSexualAgent>::preLoop() : GpuSexualPop::preLoop();
+    }
 
     // genomes beside the agents, as Genetics::init sets them up
     // (actions/Genetics.cpp:205-213)
@@ -108,6 +142,7 @@ public:
 
     uint m_iWords = 0;
     LayerArrBuf<ulong> m_aGenomes;
+    bool m_bParamMode = false;
 };
 
 static bool rd(FILE *f, void *p, size_t sz, size_t n) { return (n == 0) || (fread(p, sz, n, f) == n); }
@@ -115,6 +150,7 @@ static bool rd(FILE *f, void *p, size_t sz, size_t n) { return (n == 0) || (frea
 int main(int argc, char *argv[]) {
     if (argc < 3) return 2;
     const int iWriteEvery = (argc > 3) ? atoi(argv[3]) : 0;
+    const bool bParam = (argc > 4) && (strcmp(argv[4], "param") == 0);
     FILE *fIn = fopen(argv[1], "rb");
     if (fIn == NULL) return 2;
     char magic[8];
@@ -126,10 +162,15 @@ int main(int argc, char *argv[]) {
     // the tutorial action set, parameters by type
     std::string sParams;
     char buf[256];
+    std::vector<uint32_t> vType, vPrio;
+    std::vector<double> vP;
     for (uint32_t i = 0; ok && (i < nAct); i++) {
         uint32_t type, prio;
         double p[4];
         ok = rd(fIn, &type, 4, 1) && rd(fIn, &prio, 4, 1) && rd(fIn, p, 8, 4);
+        vType.push_back(type);
+        vPrio.push_back(prio);
+        vP.insert(vP.end(), p, p + 4);
         if (type == QHG_ACT_FERTILITY) {
             snprintf(buf, sizeof(buf), "Fertility_min_age=%.17g;Fertility_max_age=%.17g;Fertility_interbirth=%.17g;",
                      p[0], p[1], p[2]);
@@ -186,7 +227,12 @@ int main(int argc, char *argv[]) {
     static uint aiSeeds[NUM_SEEDS] = {0};
 
     DrivePop *pPop = new DrivePop(pCG, apIDG, aulState, aiSeeds);
-    if (pPop->setParams(sParams) != 0) {
+    if (bParam) {
+        if (pPop->configureActions(vType, vPrio, vP, vK.data()) != 0) {
+            fprintf(stderr, "configuration refused\n");
+            return 3;
+        }
+    } else if (pPop->setParams(sParams) != 0) {
         fprintf(stderr, "setParams refused [%s]\n", sParams.c_str());
         return 3;
     }

@@ -121,3 +121,41 @@ def test_plugin_population_with_genomes(tmp_path, driver, genetics):
     d = table_diff(got.sorted_by_id(), ref.agents)
     assert d is None, d
     assert len(ref.births) > 0
+
+
+@pytest.mark.skipif(not os.path.isdir(REF), reason="the reference tree is not present")
+@pytest.mark.parametrize("case", range(4))
+def test_plugin_population_configured_like_the_reference(tmp_path, driver, case):
+    """A plugin population whose actions are GpuParamActions, configured from
+    one module per action and the priorities (random action lists, ties
+    included), equals the reference's population configured the same way."""
+    from qhg4_gb300.spec import (ACT_ATANDEATH, ACT_FERTILITY, ACT_GETOLD, ACT_OLDAGEDEATH, ACT_RANDOMMOVE,
+                                 ACT_RANDOMPAIR, ACT_VERHULST, ACT_VERHULSTVARK, ACT_WEIGHTEDMOVE, Action)
+    from qhg4_gb300.workload import terrain_grid
+    rng = np.random.default_rng(900 + case)
+
+    def prio():
+        return int(rng.integers(1, 6))
+
+    acts = [Action(ACT_FERTILITY, prio(), (15.0, 45.0, float(rng.uniform(0, 3)))), Action(ACT_RANDOMPAIR, prio())]
+    if case % 2 == 0:
+        acts.append(Action(ACT_VERHULST, prio(), (float(rng.uniform(0.2, 0.5)), 0.03, 0.01, 50.0)))
+    else:
+        acts.append(Action(ACT_VERHULSTVARK, prio(), (float(rng.uniform(0.2, 0.5)), 0.03, 0.01)))
+    acts.append(Action(ACT_WEIGHTEDMOVE if case < 2 else ACT_RANDOMMOVE, prio(), (float(rng.uniform(0.1, 0.4)),)))
+    acts.append(Action(ACT_OLDAGEDEATH, prio(), (62.0, 0.08)))
+    if case >= 2:
+        acts.append(Action(ACT_ATANDEATH, prio(), (55.0, 12.0, 0.3)))
+    acts.append(Action(ACT_GETOLD, prio()))
+    grid = terrain_grid(8, seed=910 + case)
+    agents = make_agents(grid, 6000, seed=920 + case, age_max=75.0, proportional_to_K=True)
+    out = str(tmp_path)
+    pin, pout = os.path.join(out, "in.bin"), os.path.join(out, "drive.bin")
+    write_input(pin, grid, agents, acts, 15, 930 + case)
+    r = subprocess.run([driver, pin, pout, "6", "param"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    got, counts = read_drive_output(pout)
+    ref = run_reference("philox", out, grid, agents, acts, 15, 930 + case, threads=2)
+    assert ref.draw_errors == 0
+    d = table_diff(got.sorted_by_id(), ref.agents)
+    assert d is None, (d, [(a.type, a.prio) for a in acts])
