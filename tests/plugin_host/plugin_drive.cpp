@@ -15,7 +15,11 @@
  * GpuParamActions, configured the way QHG4 configures a population --
  * priorities through SPopulation::setPrioList, attributes through
  * Prioritizer::getActionAttributes from one module per action -- with K per
- * cell from the input (VerhulstVarK, WeightedMove's weights).
+ * cell from the input (VerhulstVarK, WeightedMove's weights).  The input's
+ * optional environment -- given move weights, K changes at given steps --
+ * is handed over as GpuPop's environment arrays: a K change rewrites the
+ * array and raises an environment event before that step, as QHG4's event
+ * manager does.
  * input: the oracle harness's input format (oracle/refsim_io.py) with the
  * tutorial action set (and genomes, kept in a LayerArrBuf registered with the
  * agent controller as Genetics keeps them); output: u64 n, i64 id[n],
@@ -28,6 +32,7 @@
 #include <string>
 #include <vector>
 
+#include "EventConsts.h"
 #include "GpuSexualPop.cpp"
 #include "LayerArrBuf.cpp"
 
@@ -201,6 +206,22 @@ int main(int argc, char *argv[]) {
     const size_t nWords = (iGenome > 0) ? (size_t)N * 2 * ((iGenome + 63) / 64) : 0;
     std::vector<uint64_t> vGen(ok ? nWords : 0);
     ok = ok && rd(fIn, vGen.data(), 8, nWords);
+    // optional: u32 has_weights, f64 W[C*7]; u32 n_k_changes, (u32 step, f64 K[C])...
+    uint32_t iHasW = 0, nKC = 0;
+    std::vector<double> vW, vKC;
+    std::vector<uint32_t> vKCStep;
+    if (ok && rd(fIn, &iHasW, 4, 1)) {
+        if (iHasW == 1) {
+            vW.resize((size_t)C * 7);
+            ok = rd(fIn, vW.data(), 8, vW.size());
+        }
+        ok = ok && rd(fIn, &nKC, 4, 1);
+        vKCStep.resize(ok ? nKC : 0);
+        vKC.resize(ok ? (size_t)nKC * C : 0);
+        for (uint32_t k = 0; ok && (k < nKC); k++) {
+            ok = rd(fIn, &vKCStep[k], 4, 1) && rd(fIn, vKC.data() + (size_t)k * C, 8, C);
+        }
+    }
     fclose(fIn);
     if (!ok) {
         fprintf(stderr, "malformed input\n");
@@ -227,10 +248,14 @@ int main(int argc, char *argv[]) {
     static uint aiSeeds[NUM_SEEDS] = {0};
 
     DrivePop *pPop = new DrivePop(pCG, apIDG, aulState, aiSeeds);
+    std::vector<double> vEnvK(vK);   // the environment's K array, rewritten by K changes
     if (bParam) {
         if (pPop->configureActions(vType, vPrio, vP, vK.data()) != 0) {
             fprintf(stderr, "configuration refused\n");
             return 3;
+        }
+        if ((iHasW == 1) || (nKC > 0)) {
+            pPop->setGpuEnvironment((nKC > 0) ? vEnvK.data() : NULL, (iHasW == 1) ? vW.data() : NULL);
         }
     } else if (pPop->setParams(sParams) != 0) {
         fprintf(stderr, "setParams refused [%s]\n", sParams.c_str());
@@ -245,6 +270,12 @@ int main(int argc, char *argv[]) {
     std::set<uint> sPrios;
     for (uint32_t s = 0; s < nSteps; s++) {
         const float fT = (float)s;
+        for (uint32_t k = 0; k < nKC; k++) {
+            if (vKCStep[k] == s) {
+                memcpy(vEnvK.data(), vKC.data() + (size_t)k * C, (size_t)C * sizeof(double));
+                pPop->updateEvent(EVENT_ID_VEG, NULL, fT);
+            }
+        }
         int iRes = pPop->initializeStep(fT);
         sPrios.clear();
         pPop->prios(sPrios);

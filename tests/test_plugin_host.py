@@ -159,3 +159,32 @@ def test_plugin_population_configured_like_the_reference(tmp_path, driver, case)
     assert ref.draw_errors == 0
     d = table_diff(got.sorted_by_id(), ref.agents)
     assert d is None, (d, [(a.type, a.prio) for a in acts])
+
+
+@pytest.mark.skipif(not os.path.isdir(REF), reason="the reference tree is not present")
+@pytest.mark.parametrize("given_weights", [False, True], ids=["weights_from_K", "given_weights"])
+def test_plugin_population_environment_events(tmp_path, driver, given_weights):
+    """GpuPop's environment arrays: given move weights, and K rewritten with
+    an environment event before steps 4 and 9, handed to the run by the next
+    initializeStep -- against the reference's classes with the same weights
+    and K changes."""
+    from qhg4_gb300.spec import config2_actions
+    from qhg4_gb300.workload import terrain_grid
+    from helpers import move_weights
+    grid = terrain_grid(9, seed=940)
+    agents = make_agents(grid, 8000, seed=941, age_max=70.0, proportional_to_K=True)
+    acts = config2_actions(b0=0.3, d0=0.03, move_p=0.3)
+    rng = np.random.default_rng(942)
+    changes = [(4, grid.K * rng.uniform(0.3, 1.5, grid.num_cells)),
+               (9, np.where(rng.random(grid.num_cells) < 0.2, 0.0, grid.K * 1.2))]
+    W = move_weights(grid, 943) if given_weights else None
+    out = str(tmp_path)
+    pin, pout = os.path.join(out, "in.bin"), os.path.join(out, "drive.bin")
+    write_input(pin, grid, agents, acts, 14, 944, weights=W, k_changes=changes)
+    r = subprocess.run([driver, pin, pout, "0", "param"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    got, counts = read_drive_output(pout)
+    ref = run_reference("philox", out, grid, agents, acts, 14, 944, threads=2, weights=W, k_changes=changes)
+    assert ref.draw_errors == 0
+    d = table_diff(got.sorted_by_id(), ref.agents)
+    assert d is None, d
