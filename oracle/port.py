@@ -44,6 +44,7 @@ def _load():
     lib.qo_num_agents.argtypes = [P]
     lib.qo_next_id.restype = ct.c_int64
     lib.qo_next_id.argtypes = [P]
+    lib.qo_set_next_id.argtypes = [P, ct.c_int64]
     lib.qo_current_step.restype = ct.c_int32
     lib.qo_current_step.argtypes = [P]
     lib.qo_get_agents.restype = ct.c_int
@@ -195,6 +196,12 @@ class OracleRun:
 
     def next_id(self) -> int:
         return int(_load().qo_next_id(self.h))
+
+    def set_next_id(self, next_id: int) -> None:
+        _load().qo_set_next_id(self.h, int(next_id))
+
+    def current_step(self) -> int:
+        return int(_load().qo_current_step(self.h))
 
     def close(self) -> None:
         if getattr(self, "h", None):

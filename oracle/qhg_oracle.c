@@ -795,6 +795,7 @@ int qo_step(qo_run *r, int nsteps, uint64_t *stats_out) {
 int64_t qo_num_agents(const qo_run *r) { return r->n; }
 int32_t qo_current_step(const qo_run *r) { return r->step; }
 int64_t qo_next_id(const qo_run *r) { return r->next_id; }
+void qo_set_next_id(qo_run *r, int64_t next_id) { r->next_id = next_id; }
 
 int qo_get_agents(const qo_run *r, int64_t *id, int32_t *cell, float *birth, float *age, float *lastb,
                   uint8_t *gender, uint8_t *state, uint64_t *genome) {

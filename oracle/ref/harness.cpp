@@ -401,6 +401,25 @@ public:
         }
     }
 
+    /* the deaths of FlatExpPop::updateEvent after a geography event
+     * (populations/FlatExpPop.cpp:187-214): registerDeath for every live
+     * agent in a flagged cell, the dead removed before the next step */
+    void killInCells(const uint8_t *aucKill) {
+        int iFirst = getFirstAgentIndex();
+        if (iFirst != LBController::NIL) {
+            int iLast = getLastAgentIndex();
+            for (int iA = iFirst; iA <= iLast; iA++) {
+                if ((m_aAgents[iA].m_iLifeState > LIFE_STATE_DEAD) && aucKill[m_aAgents[iA].m_iCellIndex]) {
+                    registerDeath(m_aAgents[iA].m_iCellIndex, iA);
+                }
+            }
+        }
+        recycleDeadSpaceNew();
+        updateTotal();
+        updateNumAgentsPerCell();
+        initListIdx();
+    }
+
     /* a new K per cell, read by VerhulstVarK (and the SingleEvaluator) at
      * the next initializeStep, as when an environment event changes it */
     void setK(const double *adK) {
@@ -686,10 +705,24 @@ int main(int argc, char *argv[]) {
     uint32_t iMSMode1 = 0;
     double dMSRadius = 1.0;
     std::vector<double> vLon, vLat;
-    if (ok && rd(fIn, &iMSMode1, 4, 1) && (iMSMode1 > 0)) {
+    bool bMS = ok && rd(fIn, &iMSMode1, 4, 1);
+    if (bMS && (iMSMode1 > 0)) {
         vLon.resize(C);
         vLat.resize(C);
         ok = rd(fIn, &dMSRadius, 8, 1) && rd(fIn, vLon.data(), 8, C) && rd(fIn, vLat.data(), 8, C);
+    }
+    /* optional: u32 n_kill_events, (u32 step, u8 flags[C])...: before that
+     * step every agent in a flagged cell dies, as FlatExpPop::updateEvent
+     * kills agents in water or ice after a geography event */
+    uint32_t nKill = 0;
+    std::vector<uint32_t> vKillStep;
+    std::vector<uint8_t> vKill;
+    if (bMS && ok && rd(fIn, &nKill, 4, 1)) {
+        vKillStep.resize(nKill);
+        vKill.resize((size_t)nKill * C);
+        for (uint32_t k = 0; ok && (k < nKill); k++) {
+            ok = rd(fIn, &vKillStep[k], 4, 1) && rd(fIn, vKill.data() + (size_t)k * C, 1, C);
+        }
     }
     fclose(fIn);
     if (!ok) { fprintf(stderr, "malformed input %s\n", argv[1]); return 2; }
@@ -748,6 +781,9 @@ int main(int argc, char *argv[]) {
         iAgentSteps += pPop->countLive();
         for (uint32_t k = 0; k < nKC; k++) {
             if (vKCStep[k] == s) pPop->setK(vKC.data() + (size_t)k*C);
+        }
+        for (uint32_t k = 0; k < nKill; k++) {
+            if (vKillStep[k] == s) pPop->killInCells(vKill.data() + (size_t)k*C);
         }
         /* PopLooper::doStep (core/PopLooper.cpp:166-200) */
         int iRes = pPop->initializeStep(fT);

@@ -14,7 +14,9 @@ Input (little endian):
   cumulative weights as given, in place of the SingleEvaluator over K),
   u32 n_k_changes, n_k_changes x (u32 step, f64 K[C]) (K from that step on),
   u32 movestats_mode + 1 (0 none), f64 radius, f64 lon[C], f64 lat[C]
-  (a MoveStats action over a Geography with these cell coordinates, degrees)
+  (a MoveStats action over a Geography with these cell coordinates, degrees),
+  u32 n_kill_events, n_kill_events x (u32 step, u8 flags[C]) (before that
+  step every agent in a flagged cell dies, as after a geography event)
 Output:
   "QHGOUT01", u32 steps, u32 C, u64 stats[steps*4] (live, births, deaths, moves),
   u32 n_dumps, u32 dump_step[n_dumps], u32 counts[n_dumps*C],
@@ -45,7 +47,7 @@ def ref_program(kind: str) -> str:
 
 def write_input(path: str, grid: Grid, agents: Agents, actions: Sequence[Action], steps: int,
                 seed: int, genetics: Genetics = Genetics(), dump_every: int = 0,
-                layer_size: int = 65536, weights=None, k_changes=(), move_stats=None) -> None:
+                layer_size: int = 65536, weights=None, k_changes=(), move_stats=None, kills=()) -> None:
     C = grid.num_cells
     N = len(agents)
     with open(path, "wb") as f:
@@ -68,7 +70,7 @@ def write_input(path: str, grid: Grid, agents: Agents, actions: Sequence[Action]
         f.write(np.ascontiguousarray(agents.state, dtype="u1").tobytes())
         if genetics.genome_size > 0:
             f.write(np.ascontiguousarray(agents.genome, dtype="<u8").tobytes())
-        if weights is not None or len(k_changes) > 0 or move_stats is not None:
+        if weights is not None or len(k_changes) > 0 or move_stats is not None or len(kills) > 0:
             f.write(struct.pack("<I", 1 if weights is not None else 0))
             if weights is not None:
                 w = np.ascontiguousarray(weights, dtype="<f8")
@@ -85,6 +87,14 @@ def write_input(path: str, grid: Grid, agents: Agents, actions: Sequence[Action]
                 f.write(struct.pack("<Id", int(mode) + 1, float(radius)))
                 f.write(np.ascontiguousarray(lon, dtype="<f8").tobytes())
                 f.write(np.ascontiguousarray(lat, dtype="<f8").tobytes())
+            else:
+                f.write(struct.pack("<I", 0))
+            f.write(struct.pack("<I", len(kills)))
+            for step, flags in kills:
+                fl = np.ascontiguousarray(flags, dtype="u1")
+                assert fl.shape == (C,)
+                f.write(struct.pack("<I", int(step)))
+                f.write(fl.tobytes())
 
 
 class RefOutput:
@@ -132,11 +142,12 @@ def read_output(path: str, genome_blocks: int = 0) -> RefOutput:
 def run_reference(kind: str, workdir: str, grid: Grid, agents: Agents, actions: Sequence[Action],
                   steps: int, seed: int, genetics: Genetics = Genetics(), dump_every: int = 0,
                   threads: int = 0, timeout: float = 3600.0, weights=None, k_changes=(),
-                  move_stats=None) -> RefOutput:
+                  move_stats=None, kills=()) -> RefOutput:
     """Run qhg_ref_well or qhg_ref_philox on the given input; `weights`
     (C x 7 cumulative) replace the weights from K, `k_changes` holds
     (step, K) pairs: K from that step on; `move_stats` = (mode, lon, lat,
-    radius) adds a MoveStats action."""
+    radius) adds a MoveStats action; `kills` holds (step, cell flags) pairs:
+    before that step every agent in a flagged cell dies."""
     exe = ref_program(kind)
     if not os.path.exists(exe):
         raise FileNotFoundError(exe)
@@ -144,7 +155,7 @@ def run_reference(kind: str, workdir: str, grid: Grid, agents: Agents, actions: 
     pin = os.path.join(workdir, f"in_{kind}_{seed}.bin")
     pout = os.path.join(workdir, f"out_{kind}_{seed}.bin")
     write_input(pin, grid, agents, actions, steps, seed, genetics, dump_every, weights=weights,
-                k_changes=k_changes, move_stats=move_stats)
+                k_changes=k_changes, move_stats=move_stats, kills=kills)
     env = dict(os.environ)
     if threads > 0:
         env["OMP_NUM_THREADS"] = str(threads)

@@ -84,6 +84,30 @@ int GpuFlatExpPop::prepareGpu() {
     return iResult;
 }
 
+// FlatExpPop::updateEvent (populations/FlatExpPop.cpp:187-219): a geography
+// event drowns the agents in water or ice; every event goes on to the
+// evaluators and marks the environment for the next step
+int GpuFlatExpPop::updateEvent(int iEventID, char *pData, float fT) {
+    int iResult = 0;
+    Geography *pGeo = m_pCG->m_pGeography;
+    if ((iEventID == EVENT_ID_GEO) && (pGeo != NULL)) {
+        const size_t C = (size_t)m_pCG->m_iNumCells;
+        std::vector<uint8_t> vRemove(C, 0);
+        for (size_t c = 0; c < C; c++) {
+            vRemove[c] = ((pGeo->m_adAltitude[c] < 0) || (pGeo->m_abIce[c] > 0)) ? 1 : 0;
+        }
+        iResult = removeAgentsInCells(vRemove.data());
+    }
+    if (iResult == 0) iResult = GpuPop<GpuFlatExpAgent>::updateEvent(iEventID, pData, fT);
+    notifyObservers(iEventID, pData);
+    return iResult;
+}
+
+// FlatExpPop::flushEvents
+void GpuFlatExpPop::flushEvents(float fT) {
+    notifyObservers(EVENT_ID_FLUSH, NULL);
+}
+
 // age and last birth time follow the basic agent data in the species' agent lines
 int GpuFlatExpPop::addPopSpecificAgentData(int iAgentIndex, char **ppData) {
     int iResult = addAgentDataSingle(ppData, &m_aAgents[iAgentIndex].m_fAge);

@@ -19,8 +19,10 @@
  * agents that QDF writing reads; crossover and mutation of the newborns run
  * on the GPU (setGpuGenetics), and preWrite brings the genomes back.
  *
- * Not carried over: updateEvent's drowning of agents in water or ice cells
- * after a geography event.
+ * Events: after a geography event the agents in water or ice cells die
+ * before the next step (GpuPop::removeAgentsInCells), as in
+ * FlatExpPop::updateEvent; every event is passed on to the evaluators
+ * (notifyObservers) and marks the environment arrays for the next step.
  */
 #ifndef QHG_GPUFLATEXPPOP_H
 #define QHG_GPUFLATEXPPOP_H
@@ -61,6 +63,8 @@ public:
     virtual ~GpuFlatExpPop();
 
     virtual int prepareGpu();
+    virtual int updateEvent(int iEventID, char *pData, float fT);
+    virtual void flushEvents(float fT);
     int addPopSpecificAgentData(int iAgentIndex, char **ppData);
     int makePopSpecificOffspring(int iAgent, int iMother, int iFather);
 

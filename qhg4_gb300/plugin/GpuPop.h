@@ -290,6 +290,62 @@ public:
     // the last error of the GPU library
     const char *gpuError() const { return qhg_gpu_last_error(); }
 
+    // Every agent in a flagged cell dies now, before the next step -- what
+    // FlatExpPop::updateEvent does after a geography event to agents in water
+    // or ice (populations/FlatExpPop.cpp:187-214).  Such events are rare: the
+    // run's table goes through the host (download, the flagged cells' agents
+    // left out, upload at the run's step with its next ID kept).  The run's
+    // occupation history and move statistics restart from that table.
+    // Before the run exists the LayerBuf's agents are marked dead.
+    int removeAgentsInCells(const uint8_t *aucRemove) {
+        if (m_pRun == NULL) {
+            const int iFirst = this->getFirstAgentIndex();
+            if (iFirst != LBController::NIL) {
+                for (int iA = iFirst; iA <= this->getLastAgentIndex(); iA++) {
+                    T &a = this->m_aAgents[iA];
+                    if ((a.m_iLifeState > 0) && aucRemove[a.m_iCellIndex]) a.m_iLifeState = 0;
+                }
+            }
+            return 0;
+        }
+        int64_t n = 0, iNextID = 0;
+        int32_t iStep = 0;
+        if ((qhg_gpu_num_agents(m_pRun, &n) != QHG_OK) || (qhg_gpu_next_id(m_pRun, &iNextID) != QHG_OK) ||
+            (qhg_gpu_current_step(m_pRun, &iStep) != QHG_OK)) {
+            return -1;
+        }
+        const size_t nW = genomeWords();
+        std::vector<int64_t> vID((size_t)n);
+        std::vector<int32_t> vCell((size_t)n);
+        std::vector<float> vBirth((size_t)n), vAge((size_t)n), vLast((size_t)n);
+        std::vector<uint8_t> vGender((size_t)n), vState((size_t)n);
+        std::vector<uint64_t> vGenome((size_t)n * nW);
+        qhg_agents_soa s = {vID.data(), vCell.data(), vBirth.data(), vAge.data(), vLast.data(),
+                            vGender.data(), vState.data(), (nW > 0) ? vGenome.data() : NULL};
+        int64_t got = 0;
+        if (qhg_gpu_download(m_pRun, &s, n, &got) != QHG_OK) return -1;
+        int64_t k = 0;
+        for (int64_t i = 0; i < got; i++) {
+            if (aucRemove[vCell[(size_t)i]]) continue;
+            vID[(size_t)k] = vID[(size_t)i];
+            vCell[(size_t)k] = vCell[(size_t)i];
+            vBirth[(size_t)k] = vBirth[(size_t)i];
+            vAge[(size_t)k] = vAge[(size_t)i];
+            vLast[(size_t)k] = vLast[(size_t)i];
+            vGender[(size_t)k] = vGender[(size_t)i];
+            vState[(size_t)k] = vState[(size_t)i];
+            if (nW > 0) memmove(&vGenome[(size_t)k * nW], &vGenome[(size_t)i * nW], nW * sizeof(uint64_t));
+            k++;
+        }
+        if ((qhg_gpu_upload_agents(m_pRun, &s, k, iStep) != QHG_OK) ||
+            (qhg_gpu_set_next_id(m_pRun, iNextID) != QHG_OK)) {
+            return -1;
+        }
+        m_bStale = true;
+        pullCounts();
+        return 0;
+    }
+
 protected:
     struct GpuAction {
         int32_t iType;

@@ -19,7 +19,8 @@
  * optional environment -- given move weights, K changes at given steps --
  * is handed over as GpuPop's environment arrays: a K change rewrites the
  * array and raises an environment event before that step, as QHG4's event
- * manager does.
+ * manager does.  Kill events remove every agent of the flagged cells before
+ * their step (GpuPop::removeAgentsInCells, a geography event's drowning).
  * input: the oracle harness's input format (oracle/refsim_io.py) with the
  * tutorial action set (and genomes, kept in a LayerArrBuf registered with the
  * agent controller as Genetics keeps them); output: u64 n, i64 id[n],
@@ -222,6 +223,21 @@ int main(int argc, char *argv[]) {
             ok = rd(fIn, &vKCStep[k], 4, 1) && rd(fIn, vKC.data() + (size_t)k * C, 8, C);
         }
     }
+    // optional: u32 movestats_mode + 1 (must be 0 here); u32 n_kill_events,
+    // (u32 step, u8 flags[C])...: agents in flagged cells die before that step
+    uint32_t iMS1 = 0, nKill = 0;
+    std::vector<uint32_t> vKillStep;
+    std::vector<uint8_t> vKill;
+    if (ok && rd(fIn, &iMS1, 4, 1)) {
+        if (iMS1 != 0) ok = false;
+        if (ok && rd(fIn, &nKill, 4, 1)) {
+            vKillStep.resize(nKill);
+            vKill.resize((size_t)nKill * C);
+            for (uint32_t k = 0; ok && (k < nKill); k++) {
+                ok = rd(fIn, &vKillStep[k], 4, 1) && rd(fIn, vKill.data() + (size_t)k * C, 1, C);
+            }
+        }
+    }
     fclose(fIn);
     if (!ok) {
         fprintf(stderr, "malformed input\n");
@@ -274,6 +290,12 @@ int main(int argc, char *argv[]) {
             if (vKCStep[k] == s) {
                 memcpy(vEnvK.data(), vKC.data() + (size_t)k * C, (size_t)C * sizeof(double));
                 pPop->updateEvent(EVENT_ID_VEG, NULL, fT);
+            }
+        }
+        for (uint32_t k = 0; k < nKill; k++) {
+            if ((vKillStep[k] == s) && (pPop->removeAgentsInCells(vKill.data() + (size_t)k * C) != 0)) {
+                fprintf(stderr, "removal failed\n");
+                return 4;
             }
         }
         int iRes = pPop->initializeStep(fT);

@@ -22,6 +22,9 @@ int qo_load(qo_run *r, int64_t N, const int64_t *id, const int32_t *cell, const 
             int32_t first_step);
 int qo_step(qo_run *r, int nsteps, uint64_t *stats_out);
 int64_t qo_num_agents(const qo_run *r);
+int64_t qo_next_id(const qo_run *r);
+void qo_set_next_id(qo_run *r, int64_t next_id);
+int32_t qo_current_step(const qo_run *r);
 int qo_get_agents(const qo_run *r, int64_t *id, int32_t *cell, float *birth, float *age, float *lastb,
                   uint8_t *gender, uint8_t *state, uint64_t *genome);
 int qo_get_counts(const qo_run *r, uint32_t *counts);
@@ -102,6 +105,24 @@ int qhg_gpu_set_capacity(qhg_run *r, const double *K) {
 int qhg_gpu_set_move_weights(qhg_run *r, const double *W) {
     if (r == NULL || r->o == NULL) return QHG_ERR_STATE;
     return qo_set_move_weights(r->o, W) == 0 ? QHG_OK : QHG_ERR_ARG;
+}
+
+int qhg_gpu_next_id(qhg_run *r, int64_t *next_id) {
+    if (r == NULL || r->o == NULL) return QHG_ERR_STATE;
+    *next_id = qo_next_id(r->o);
+    return QHG_OK;
+}
+
+int qhg_gpu_set_next_id(qhg_run *r, int64_t next_id) {
+    if (r == NULL || r->o == NULL) return QHG_ERR_STATE;
+    qo_set_next_id(r->o, next_id);
+    return QHG_OK;
+}
+
+int qhg_gpu_current_step(qhg_run *r, int32_t *step) {
+    if (r == NULL || r->o == NULL) return QHG_ERR_STATE;
+    *step = qo_current_step(r->o);
+    return QHG_OK;
 }
 
 int qhg_gpu_destroy(qhg_run *r) {

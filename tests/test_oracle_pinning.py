@@ -194,3 +194,37 @@ def test_port_oracle_random_programs_against_reference_build(tmp_path, case):
     d = table_diff(r.agents(), ref.agents)
     assert d is None, (d, [(a.type, a.prio) for a in acts])
     assert np.array_equal(st, ref.stats)
+
+
+@pytest.mark.skipif(not os.path.exists(ref_program("philox")), reason="reference build not present")
+def test_port_oracle_geography_kills_against_reference_build(tmp_path):
+    """After a geography event FlatExpPop kills every agent in water or ice
+    (populations/FlatExpPop.cpp:187-214); the plugin does it by taking the
+    table out, leaving those cells' agents out and loading it back at the
+    run's step with its next ID.  The oracle run that way equals the
+    reference's registerDeath / recycleDeadSpaceNew path."""
+    from qhg4_gb300.spec import config2_actions
+    from qhg4_gb300.workload import Agents, make_agents, terrain_grid
+    grid = terrain_grid(9, seed=950)
+    agents = make_agents(grid, 9000, seed=951, age_max=70.0, proportional_to_K=True)
+    acts = config2_actions(b0=0.3, d0=0.03, move_p=0.3)
+    rng = np.random.default_rng(952)
+    kills = [(5, (rng.random(grid.num_cells) < 0.15).astype(np.uint8)),
+             (11, (rng.random(grid.num_cells) < 0.3).astype(np.uint8))]
+    ref = run_reference("philox", str(tmp_path), grid, agents, acts, 16, 953, threads=2, kills=kills)
+    r = port.OracleRun(grid, acts, 953)
+    r.load(agents)
+    done = 0
+    for step, flags in kills + [(16, None)]:
+        r.step(step - done)
+        done = step
+        if flags is None:
+            continue
+        a, nid, st = r.agents(), r.next_id(), r.current_step()
+        keep = flags[a.cell] == 0
+        r.load(Agents(*(getattr(a, k)[keep] for k in ("id", "cell", "birth", "age", "lastb", "gender", "state"))),
+               first_step=st)
+        r.set_next_id(nid)
+    assert ref.draw_errors == 0
+    d = table_diff(r.agents(), ref.agents)
+    assert d is None, d

@@ -188,3 +188,28 @@ def test_plugin_population_environment_events(tmp_path, driver, given_weights):
     assert ref.draw_errors == 0
     d = table_diff(got.sorted_by_id(), ref.agents)
     assert d is None, d
+
+
+@pytest.mark.skipif(not os.path.isdir(REF), reason="the reference tree is not present")
+def test_plugin_population_removes_agents_in_cells(tmp_path, driver):
+    """GpuPop::removeAgentsInCells (a geography event's drowning, as
+    FlatExpPop::updateEvent does it) before steps 5 and 11, with genomes,
+    against the reference's registerDeath / recycleDeadSpaceNew path."""
+    from qhg4_gb300.workload import uniform_grid as ug
+    gen = Genetics(256, CROSSOVER_POISSON1, 2e-3)
+    grid = ug(6, 40.0)
+    agents = make_agents(grid, 9000, seed=961, age_max=50.0, genome_blocks=gen.num_blocks)
+    acts = config3_actions()
+    rng = np.random.default_rng(962)
+    kills = [(5, (rng.random(grid.num_cells) < 0.2).astype(np.uint8)),
+             (11, (rng.random(grid.num_cells) < 0.3).astype(np.uint8))]
+    out = str(tmp_path)
+    pin, pout = os.path.join(out, "in.bin"), os.path.join(out, "drive.bin")
+    write_input(pin, grid, agents, acts, 16, 963, gen, kills=kills)
+    r = subprocess.run([driver, pin, pout, "7"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    got, counts = read_drive_output(pout)
+    ref = run_reference("philox", out, grid, agents, acts, 16, 963, gen, threads=2, kills=kills)
+    assert ref.draw_errors == 0
+    d = table_diff(got.sorted_by_id(), ref.agents)
+    assert d is None, d
