@@ -401,6 +401,11 @@ public:
         }
     }
 
+    /* a runtime edit, as QHG4 applies one (Prioritizer::modifyAttributes) */
+    int modify(const std::string &sName, double dValue) {
+        return m_prio.modifyAttributes(sName, dValue);
+    }
+
     /* the deaths of FlatExpPop::updateEvent after a geography event
      * (populations/FlatExpPop.cpp:187-214): registerDeath for every live
      * agent in a flagged cell, the dead removed before the next step */
@@ -717,11 +722,31 @@ int main(int argc, char *argv[]) {
     uint32_t nKill = 0;
     std::vector<uint32_t> vKillStep;
     std::vector<uint8_t> vKill;
-    if (bMS && ok && rd(fIn, &nKill, 4, 1)) {
+    bool bKill = bMS && ok && rd(fIn, &nKill, 4, 1);
+    if (bKill) {
         vKillStep.resize(nKill);
         vKill.resize((size_t)nKill * C);
         for (uint32_t k = 0; ok && (k < nKill); k++) {
             ok = rd(fIn, &vKillStep[k], 4, 1) && rd(fIn, vKill.data() + (size_t)k * C, 1, C);
+        }
+    }
+    /* optional: u32 n_mods, (u32 step, u32 name_len, char name[name_len],
+     * f64 value)...: runtime edits through Prioritizer::modifyAttributes
+     * before that step */
+    uint32_t nMods = 0;
+    std::vector<uint32_t> vModStep;
+    std::vector<std::string> vModName;
+    std::vector<double> vModValue;
+    if (bKill && ok && rd(fIn, &nMods, 4, 1)) {
+        for (uint32_t k = 0; ok && (k < nMods); k++) {
+            uint32_t iStepM = 0, iLen = 0;
+            double dV = 0;
+            ok = rd(fIn, &iStepM, 4, 1) && rd(fIn, &iLen, 4, 1) && (iLen < 256);
+            std::string sName(ok ? iLen : 0, ' ');
+            ok = ok && rd(fIn, &sName[0], 1, iLen) && rd(fIn, &dV, 8, 1);
+            vModStep.push_back(iStepM);
+            vModName.push_back(sName);
+            vModValue.push_back(dV);
         }
     }
     fclose(fIn);
@@ -784,6 +809,9 @@ int main(int argc, char *argv[]) {
         }
         for (uint32_t k = 0; k < nKill; k++) {
             if (vKillStep[k] == s) pPop->killInCells(vKill.data() + (size_t)k*C);
+        }
+        for (uint32_t k = 0; k < nMods; k++) {
+            if (vModStep[k] == s) pPop->modify(vModName[k], vModValue[k]);
         }
         /* PopLooper::doStep (core/PopLooper.cpp:166-200) */
         int iRes = pPop->initializeStep(fT);

@@ -95,6 +95,28 @@ public:
         return iResult;
     }
 
+    // Runtime edits (Prioritizer::modifyAttributes, core/Prioritizer.cpp:420-434),
+    // with the reference actions' effect: RandomMove and WeightedMove take a
+    // new probability (actions/RandomMove.cpp:144-154,
+    // actions/WeightedMove.cpp:153-163), which the GPU run gets before the
+    // next step.  Verhulst / VerhulstVarK change their own fields but pass
+    // the name to LinearBirth / LinearDeath, which know other names
+    // (actions/Verhulst.cpp:235-255, actions/LinearBirth.cpp:235-248), so
+    // their rates stay as they were and the call reports an error: the same
+    // here.  The other actions have no runtime attributes.
+    virtual int modifyAttributes(const std::string sAttrName, double dValue) {
+        for (size_t k = 0; (k < m_vSlots.size()) && (k < 4); k++) {
+            if (m_vSlots[k] != sAttrName) continue;
+            if ((m_iType == QHG_ACT_RANDOMMOVE) || (m_iType == QHG_ACT_WEIGHTEDMOVE)) {
+                m_adP[k] = dValue;
+                m_bModified = true;
+                return 0;
+            }
+            if ((m_iType == QHG_ACT_VERHULST) || (m_iType == QHG_ACT_VERHULSTVARK)) return -2;
+        }
+        return -1;
+    }
+
     // the parameter action of a QHG_ACT_* type, with the reference's names
     // (actions/*.h ATTR_*), NULL for an unknown type
     static GpuParamAction<T> *create(SPopulation<T> *pPop, SCellGrid *pCG, int32_t iType) {
@@ -134,6 +156,7 @@ public:
     int32_t m_iType;
     std::vector<std::string> m_vSlots;
     double m_adP[4];
+    bool m_bModified = false;   // a runtime edit the GPU run has not seen
 };
 
 template<typename T>
@@ -224,6 +247,7 @@ public:
     virtual int initializeStep(float fTime) {
         if (m_pRun == NULL) return -1;
         int iResult = 0;
+        if (paramsModified()) iResult = rebuildRun();
         for (size_t i = 0; i < m_vHostOrder.size(); i++) {
             iResult += m_vHostOrder[i]->initialize(fTime);
         }
@@ -358,6 +382,7 @@ protected:
     // list; the host evaluators in the same order
     void collectParamActions() {
         m_vHostOrder.clear();
+        m_vParamGpu.clear();
         std::set<uint> sPrios;
         this->m_prio.getPrios(sPrios);
         for (std::set<uint>::const_iterator it = sPrios.begin(); it != sPrios.end(); ++it) {
@@ -365,7 +390,13 @@ protected:
                 Action<T> *pA = this->m_prio.getAction(*it, j);
                 for (size_t k = 0; k < m_vParamActions.size(); k++) {
                     if (m_vParamActions[k] == pA) {
-                        addGpuAction(m_vParamActions[k]->m_iType, *it, pA->getActionName(), m_vParamActions[k]->m_adP);
+                        GpuAction a;
+                        a.iType = m_vParamActions[k]->m_iType;
+                        a.iPrio = *it;
+                        a.sName = pA->getActionName();
+                        for (int q = 0; q < 4; q++) a.adP[q] = m_vParamActions[k]->m_adP[q];
+                        m_vParamGpu.push_back(a);
+                        m_vParamActions[k]->m_bModified = false;
                     }
                 }
                 if (std::find(m_vHostEvals.begin(), m_vHostEvals.end(), pA) != m_vHostEvals.end()) {
@@ -375,11 +406,59 @@ protected:
         }
     }
 
-    int startGpu() {
+    // the run's action list: the explicit actions and the parameter
+    // actions, in execution order (priority, then name)
+    std::vector<GpuAction> actionList() const {
         std::vector<GpuAction> v(m_vActions);
+        v.insert(v.end(), m_vParamGpu.begin(), m_vParamGpu.end());
         std::stable_sort(v.begin(), v.end(), [](const GpuAction &a, const GpuAction &b) {
             return (a.iPrio != b.iPrio) ? (a.iPrio < b.iPrio) : (a.sName < b.sName);
         });
+        return v;
+    }
+
+    bool paramsModified() const {
+        for (size_t k = 0; k < m_vParamActions.size(); k++) {
+            if (m_vParamActions[k]->m_bModified) return true;
+        }
+        return false;
+    }
+
+    // a new run with the edited parameters, holding the current one's table
+    // (with genomes) at its step and with its next ID; the environment
+    // arrays are handed over again at once
+    int rebuildRun() {
+        int64_t n = 0, iNextID = 0;
+        int32_t iStep = 0;
+        if ((qhg_gpu_num_agents(m_pRun, &n) != QHG_OK) || (qhg_gpu_next_id(m_pRun, &iNextID) != QHG_OK) ||
+            (qhg_gpu_current_step(m_pRun, &iStep) != QHG_OK)) {
+            return -1;
+        }
+        const size_t nW = genomeWords();
+        std::vector<int64_t> vID((size_t)n);
+        std::vector<int32_t> vCell((size_t)n);
+        std::vector<float> vBirth((size_t)n), vAge((size_t)n), vLast((size_t)n);
+        std::vector<uint8_t> vGender((size_t)n), vState((size_t)n);
+        std::vector<uint64_t> vGenome((size_t)n * nW);
+        qhg_agents_soa s = {vID.data(), vCell.data(), vBirth.data(), vAge.data(), vLast.data(),
+                            vGender.data(), vState.data(), (nW > 0) ? vGenome.data() : NULL};
+        int64_t got = 0;
+        if (qhg_gpu_download(m_pRun, &s, n, &got) != QHG_OK) return -1;
+        qhg_gpu_destroy(m_pRun);
+        m_pRun = NULL;
+        collectParamActions();
+        if (createRun() != 0) return -1;
+        if ((qhg_gpu_upload_agents(m_pRun, &s, got, iStep) != QHG_OK) ||
+            (qhg_gpu_set_next_id(m_pRun, iNextID) != QHG_OK)) {
+            return -1;
+        }
+        m_bEnvDirty = true;
+        return 0;
+    }
+
+    // the GPU run with the action list, genetics and cell grid
+    int createRun() {
+        std::vector<GpuAction> v = actionList();
         if (v.size() > QHG_MAX_ACTIONS) return -1;
         qhg_run_desc d;
         memset(&d, 0, sizeof(d));
@@ -408,6 +487,11 @@ protected:
         }
         if (m_vK.size() != (size_t)C) m_vK.assign((size_t)C, 0.0);
         if (qhg_gpu_upload_grid(m_pRun, vNbr.data(), vN.data(), m_vK.data(), C) != QHG_OK) return -1;
+        return 0;
+    }
+
+    int startGpu() {
+        if (createRun() != 0) return -1;
         // live agents of the LayerBuf
         std::vector<int64_t> vID;
         std::vector<int32_t> vCell;
@@ -502,6 +586,7 @@ protected:
     int m_iDevice;
     uint64_t m_ulSeed;
     std::vector<GpuAction> m_vActions;
+    std::vector<GpuAction> m_vParamGpu;   // the parameter actions' entries (collectParamActions)
     std::vector<double> m_vK;
     std::vector<Action<T> *> m_vHostEvals;
     std::vector<GpuParamAction<T> *> m_vParamActions;

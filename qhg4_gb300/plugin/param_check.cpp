@@ -31,10 +31,10 @@ public:
     }
 
     void show() {
-        m_vActions.clear();
         collectParamActions();
-        for (size_t i = 0; i < m_vActions.size(); i++) {
-            const GpuAction &a = m_vActions[i];
+        const std::vector<GpuAction> v = actionList();
+        for (size_t i = 0; i < v.size(); i++) {
+            const GpuAction &a = v[i];
             printf("%d %u %s %.17g %.17g %.17g %.17g\n", a.iType, a.iPrio, a.sName.c_str(), a.adP[0], a.adP[1],
                    a.adP[2], a.adP[3]);
         }

@@ -20,7 +20,8 @@
  * is handed over as GpuPop's environment arrays: a K change rewrites the
  * array and raises an environment event before that step, as QHG4's event
  * manager does.  Kill events remove every agent of the flagged cells before
- * their step (GpuPop::removeAgentsInCells, a geography event's drowning).
+ * their step (GpuPop::removeAgentsInCells, a geography event's drowning);
+ * runtime edits go through the Prioritizer's modifyAttributes before theirs.
  * input: the oracle harness's input format (oracle/refsim_io.py) with the
  * tutorial action set (and genomes, kept in a LayerArrBuf registered with the
  * agent controller as Genetics keeps them); output: u64 n, i64 id[n],
@@ -43,6 +44,9 @@ public:
         : GpuSexualPop(pCG, NULL, 65536, apIDG, aulState, aiSeeds) {}
 
     void prios(std::set<uint> &sPrios) { getPrios(sPrios); }
+
+    // a runtime edit, as QHG4 applies one (Prioritizer::modifyAttributes)
+    int modify(const std::string &sName, double dValue) { return m_prio.modifyAttributes(sName, dValue); }
 
     // the input's actions as parameter actions, configured from modules
     int configureActions(const std::vector<uint32_t> &vType, const std::vector<uint32_t> &vPrio,
@@ -225,9 +229,13 @@ int main(int argc, char *argv[]) {
     }
     // optional: u32 movestats_mode + 1 (must be 0 here); u32 n_kill_events,
     // (u32 step, u8 flags[C])...: agents in flagged cells die before that step
-    uint32_t iMS1 = 0, nKill = 0;
-    std::vector<uint32_t> vKillStep;
+    // u32 n_mods, (u32 step, u32 name_len, char name[], f64 value)...: runtime
+    // edits through the Prioritizer before that step
+    uint32_t iMS1 = 0, nKill = 0, nMods = 0;
+    std::vector<uint32_t> vKillStep, vModStep;
     std::vector<uint8_t> vKill;
+    std::vector<std::string> vModName;
+    std::vector<double> vModValue;
     if (ok && rd(fIn, &iMS1, 4, 1)) {
         if (iMS1 != 0) ok = false;
         if (ok && rd(fIn, &nKill, 4, 1)) {
@@ -235,6 +243,18 @@ int main(int argc, char *argv[]) {
             vKill.resize((size_t)nKill * C);
             for (uint32_t k = 0; ok && (k < nKill); k++) {
                 ok = rd(fIn, &vKillStep[k], 4, 1) && rd(fIn, vKill.data() + (size_t)k * C, 1, C);
+            }
+            if (ok && rd(fIn, &nMods, 4, 1)) {
+                for (uint32_t k = 0; ok && (k < nMods); k++) {
+                    uint32_t iStepM = 0, iLen = 0;
+                    double dV = 0;
+                    ok = rd(fIn, &iStepM, 4, 1) && rd(fIn, &iLen, 4, 1) && (iLen < 256);
+                    std::string sName(ok ? iLen : 0, ' ');
+                    ok = ok && rd(fIn, &sName[0], 1, iLen) && rd(fIn, &dV, 8, 1);
+                    vModStep.push_back(iStepM);
+                    vModName.push_back(sName);
+                    vModValue.push_back(dV);
+                }
             }
         }
     }
@@ -291,6 +311,9 @@ int main(int argc, char *argv[]) {
                 memcpy(vEnvK.data(), vKC.data() + (size_t)k * C, (size_t)C * sizeof(double));
                 pPop->updateEvent(EVENT_ID_VEG, NULL, fT);
             }
+        }
+        for (uint32_t k = 0; k < nMods; k++) {
+            if (vModStep[k] == s) pPop->modify(vModName[k], vModValue[k]);
         }
         for (uint32_t k = 0; k < nKill; k++) {
             if ((vKillStep[k] == s) && (pPop->removeAgentsInCells(vKill.data() + (size_t)k * C) != 0)) {

@@ -213,3 +213,29 @@ def test_plugin_population_removes_agents_in_cells(tmp_path, driver):
     assert ref.draw_errors == 0
     d = table_diff(got.sorted_by_id(), ref.agents)
     assert d is None, d
+
+
+@pytest.mark.skipif(not os.path.isdir(REF), reason="the reference tree is not present")
+def test_plugin_population_runtime_edits(tmp_path, driver):
+    """Runtime edits through Prioritizer::modifyAttributes: WeightedMove's
+    probability changes from step 4 (the plugin rebuilds its run with the
+    table, step and next ID kept), and a Verhulst edit changes nothing, as in
+    the reference (its LinearBirth / LinearDeath know other names)."""
+    from qhg4_gb300.spec import config2_actions
+    from qhg4_gb300.workload import terrain_grid
+    grid = terrain_grid(9, seed=970)
+    agents = make_agents(grid, 8000, seed=971, age_max=70.0, proportional_to_K=True)
+    acts = config2_actions(b0=0.3, d0=0.03, move_p=0.1)
+    mods = [(4, "WeightedMove_prob", 0.6), (7, "Verhulst_b0", 0.9), (9, "WeightedMove_prob", 0.02)]
+    out = str(tmp_path)
+    pin, pout = os.path.join(out, "in.bin"), os.path.join(out, "drive.bin")
+    write_input(pin, grid, agents, acts, 14, 972, mods=mods)
+    r = subprocess.run([driver, pin, pout, "5", "param"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    got, counts = read_drive_output(pout)
+    ref = run_reference("philox", out, grid, agents, acts, 14, 972, threads=2, mods=mods)
+    assert ref.draw_errors == 0
+    d = table_diff(got.sorted_by_id(), ref.agents)
+    assert d is None, d
+    plain = run_reference("philox", out, grid, agents, acts, 14, 972, threads=2)
+    assert table_diff(plain.agents, ref.agents) is not None   # the edits matter
