@@ -271,6 +271,7 @@ public:
     virtual int finalizeStep() {
         if ((m_pRun == NULL) || (qhg_gpu_step(m_pRun, 1) != QHG_OK)) return -1;
         m_bStale = true;
+        if (syncIDGens() != 0) return -1;
         // the host evaluators' finalize (an evaluator clears its update flag there)
         int iResult = 0;
         for (size_t i = 0; i < m_vHostOrder.size(); i++) {
@@ -521,8 +522,37 @@ protected:
         qhg_agents_soa s = {vID.data(), vCell.data(), vBirth.data(), vAge.data(), vLast.data(),
                             vGender.data(), vState.data(), (nW > 0) ? vGenome.data() : NULL};
         if (qhg_gpu_upload_agents(m_pRun, &s, (int64_t)vID.size(), 0) != QHG_OK) return -1;
+        if (claimIDs() != 0) return -1;
         m_bStale = false;
         return 0;
+    }
+
+    // The ID generators are the application's, shared by all populations
+    // (app/SimParams.cpp:138-141): the run's newborns took IDs from its own
+    // counter, so every generator is moved past it (never back), and QHG4's
+    // dumps record it (IDGen::getCur, core/IDGen.h).
+    int syncIDGens() {
+        int64_t iNextID = 0;
+        if (qhg_gpu_next_id(m_pRun, &iNextID) != QHG_OK) return -1;
+        for (int t = 0; t < this->m_iNumThreads; t++) {
+            IDGen *pG = this->m_apIDGen[t];
+            const idtype iCur = pG->getCur();
+            pG->setBase((idtype)iNextID);
+            if (pG->getCur() < iCur) pG->setCur(iCur);
+        }
+        return 0;
+    }
+
+    // the run's first ID for newborns: above every ID in the table (the
+    // upload's own choice) and every ID the generators have handed out
+    int claimIDs() {
+        int64_t iNextID = 0;
+        if (qhg_gpu_next_id(m_pRun, &iNextID) != QHG_OK) return -1;
+        for (int t = 0; t < this->m_iNumThreads; t++) {
+            const int64_t iUsed = (int64_t)this->m_apIDGen[t]->getCur() + 1;
+            if (iUsed > iNextID) iNextID = iUsed;
+        }
+        return (qhg_gpu_set_next_id(m_pRun, iNextID) == QHG_OK) ? 0 : -1;
     }
 
     // genome words per agent (0 without genetics)

@@ -26,7 +26,8 @@
  * tutorial action set (and genomes, kept in a LayerArrBuf registered with the
  * agent controller as Genetics keeps them); output: u64 n, i64 id[n],
  * i32 cell[n], f32 birth[n], f32 age[n], f32 lastb[n], u8 gender[n],
- * u8 state[n], u32 C, u32 counts[C], u32 words, u64 genome[n * words].
+ * u8 state[n], u32 C, u32 counts[C], u32 words, u64 genome[n * words],
+ * i64 the smallest next ID of the population's ID generators.
  */
 #include <cstdio>
 #include <cstdlib>
@@ -148,6 +149,13 @@ public:
         }
         fwrite(&m_iWords, 4, 1, f);
         fwrite(genome.data(), 8, genome.size(), f);
+        int64_t iMinNext = -1;
+        for (int t = 0; t < m_iNumThreads; t++) {
+            IDGen g = *m_apIDGen[t];
+            const int64_t iNext = (int64_t)g.getID();
+            if ((iMinNext < 0) || (iNext < iMinNext)) iMinNext = iNext;
+        }
+        fwrite(&iMinNext, 8, 1, f);
     }
 
     uint m_iWords = 0;

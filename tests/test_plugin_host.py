@@ -74,6 +74,7 @@ def read_drive_output(path: str):
     words = int(take("<u4", 1)[0])
     if words > 0:
         a.genome = take("<u8", n * words).reshape(n, words)
+    read_drive_output.generators_next = int(take("<i8", 1)[0])
     return a, counts
 
 
@@ -97,6 +98,8 @@ def test_plugin_population_equals_reference_actions(tmp_path, driver, write_ever
     assert d is None, d
     assert np.array_equal(counts, np.bincount(ref.agents.cell, minlength=grid.num_cells).astype(np.uint32))
     assert len(got) > 5000
+    # the application's ID generators were moved past the run's newborn IDs
+    assert read_drive_output.generators_next > int(ref.births[:, 0].max())
 
 
 @pytest.mark.skipif(not os.path.isdir(REF), reason="the reference tree is not present")
