@@ -49,6 +49,8 @@
 
 #include "Action.h"
 #include "ParamProvider2.h"
+#include "QDFUtils.h"
+#include "QDFUtilsT.h"
 #include "SPopulation.h"
 #include "Fertility.h"
 #include "GetOld.h"
@@ -93,6 +95,34 @@ public:
             if (pEnd == it->second.c_str()) iResult = -1;
         }
         return iResult;
+    }
+
+    // QDF attributes under the reference action's names, so that a QDF file
+    // of a GPU population and one of the reference's population read alike
+    // (e.g. RandomMove::writeAttributesQDF, actions/RandomMove.cpp:130-137)
+    virtual int writeAttributesQDF(hid_t hSpeciesGroup) {
+        int iResult = 0;
+        for (size_t k = 0; (k < m_vSlots.size()) && (k < 4); k++) {
+            iResult += qdf_insertAttribute(hSpeciesGroup, m_vSlots[k], 1, &m_adP[k]);
+        }
+        return iResult;
+    }
+
+    virtual int extractAttributesQDF(hid_t hSpeciesGroup) {
+        for (size_t k = 0; (k < m_vSlots.size()) && (k < 4); k++) {
+            if (qdf_extractAttribute(hSpeciesGroup, m_vSlots[k], 1, &m_adP[k]) != 0) return -1;
+        }
+        return 0;
+    }
+
+    // the same action with the same parameters (Prioritizer::isEqual)
+    virtual bool isEqual(Action<T> *pAction, bool bStrict) {
+        GpuParamAction<T> *pA = dynamic_cast<GpuParamAction<T> *>(pAction);
+        if ((pA == NULL) || (pA->m_iType != m_iType)) return false;
+        for (int k = 0; k < 4; k++) {
+            if (pA->m_adP[k] != m_adP[k]) return false;
+        }
+        return true;
     }
 
     // Runtime edits (Prioritizer::modifyAttributes, core/Prioritizer.cpp:420-434),

@@ -4,7 +4,9 @@
 // Prioritizer::getActionAttributes, as QHG4 configures a population from its
 // XML/QDF modules, and prints the action list the GPU run would be created
 // with, one line per action: "type prio name p0 p1 p2 p3".  Then a module
-// without one of its attributes must be refused ("missing <rc>").
+// without one of its attributes must be refused ("missing <rc>"); equal
+// configurations compare equal (Action::isEqual, "equal 1") until a runtime
+// edit changes one ("edited <rc> <equal>").
 //
 // Built by `make -C qhg4_gb300/plugin param_check` against the reference tree
 // and the reference's support objects (tests/test_plugin_build.py).
@@ -29,6 +31,15 @@ public:
         if (iResult == 0) iResult = m_prio.getActionAttributes(mModules);
         return iResult;
     }
+
+    bool sameActions(ParamCheckPop *pOther) {
+        for (size_t k = 0; k < m_vParamActions.size(); k++) {
+            if (!m_vParamActions[k]->isEqual(pOther->m_vParamActions[k], true)) return false;
+        }
+        return true;
+    }
+
+    int edit(const std::string &sName, double dValue) { return m_prio.modifyAttributes(sName, dValue); }
 
     void show() {
         collectParamActions();
@@ -90,6 +101,12 @@ int main() {
         return 1;
     }
     pPop->show();
+
+    ParamCheckPop *pSame = new ParamCheckPop(pCG, apIDG, aulState);
+    pSame->configure(mPrios, mModules);
+    printf("equal %d\n", pPop->sameActions(pSame) ? 1 : 0);
+    const int iEdit = pSame->edit("RandomMove_prob", 0.3);
+    printf("edited %d %d\n", iEdit, pPop->sameActions(pSame) ? 1 : 0);
 
     // a module that lacks an attribute is refused
     ParamCheckPop *pPop2 = new ParamCheckPop(pCG, apIDG, aulState);

@@ -62,3 +62,5 @@ def test_plugin_reads_actions_from_configuration(tmp_path):
     assert got == want
     missing = [ln for ln in run.stdout.splitlines() if ln.startswith("missing ")]
     assert missing and int(missing[0].split()[1]) != 0
+    assert "equal 1" in run.stdout.splitlines()
+    assert "edited 0 0" in run.stdout.splitlines()
