@@ -36,35 +36,39 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-from qhg4_gb300.spec import config1_actions, config2_actions  # noqa: E402
-from qhg4_gb300.workload import make_agents, terrain_grid, uniform_grid  # noqa: E402
+from qhg4_gb300 import configs  # noqa: E402
+from qhg4_gb300.spec import config1_actions  # noqa: E402
 
 METRIC = "agent-steps/s"
 
+# name: workload factory (seed -> configs.Workload)
 WORKLOADS = {
-    # name: grid n, agents, age max, K-proportional placement, actions, bytes per cell-step
-    "large": dict(n=256, agents=20_000_000, age_max=60.0, prop=True, actions=config2_actions,
-                  cell_bytes=53 + 56, desc="single large run: grid n=256 (655,362 cells), altitude K, 20M agents, "
-                  "GetOld+Fertility+RandomPair+VerhulstVarK+OldAgeDeath+WeightedMove(p=0.2)", job_steps=200),
+    "large": lambda seed: configs.single_large_run(seed),
     # a smaller case of the same actions for profiler captures (hot table > L2)
-    "medium": dict(n=192, agents=8_000_000, age_max=60.0, prop=True, actions=config2_actions,
-                   cell_bytes=53 + 56, desc="grid n=192 (368,642 cells), altitude K, 8M agents, "
-                   "actions of the large run", job_steps=200),
-    "plain": dict(n=32, agents=100_000, age_max=50.0, prop=False, actions=config1_actions,
-                  cell_bytes=53, desc="plain method: grid n=32 (10,242 cells), K=30, 100k agents, "
-                  "GetOld+Fertility+RandomPair+Verhulst+RandomMove(p=0.1)", job_steps=1000),
+    "medium": lambda seed: configs.single_large_run(seed, n=192, agents=8_000_000),
+    "plain": lambda seed: configs.plain_method(seed),
+    "genetics": lambda seed: configs.genetics_run(seed),
 }
 AGENT_BYTES = 60   # one read and one write of the 30-byte hot record per agent-step
+BIRTH_BYTES = 3 * 1024   # genetics: two parent genomes read, one child genome written (2 x 4,096 loci)
+# kernels launched per step: the action kernel and the scatter in each of the
+# three forms (two of each return at once) and the cell scan
+LAUNCHES_PER_STEP = 7
+# speed of the C port relative to the reference's own OpenMP code, measured
+# where the reference sources are (both on 8 cores of the build container,
+# the plain method and the large run's actions at 2M agents)
+PORT_VS_REFERENCE = "(not yet compared with)"
 
 
-def build_workload(name: str, seed: int = 42, grid_seed: int = 2024):
-    w = WORKLOADS[name]
-    if w["prop"]:
-        grid = terrain_grid(w["n"], seed=grid_seed)
-    else:
-        grid = uniform_grid(w["n"], 30.0)
-    agents = make_agents(grid, w["agents"], seed=seed, age_max=w["age_max"], proportional_to_K=w["prop"])
-    return grid, agents, w["actions"]()
+def build_workload(name: str, seed: int = 42):
+    return WORKLOADS[name](seed)
+
+
+def workload_config(w, world: int):
+    """The line's `config` (identical for this implementation and the CPU reference arm)."""
+    return {"workload": w.name, "detail": w.desc, "agents": len(w.agents), "cells": w.grid.num_cells,
+            "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 (hot table ~21 B x agents > 129 MB)"}
 
 
 class ClockSampler:
@@ -168,13 +172,13 @@ def read_traffic(workload: str):
     return None
 
 
-def cpu_leg(grid, agents, actions, seed, steps, warmup):
+def cpu_leg(w, steps, warmup):
     """The C port of the reference algorithm on all host threads (OpenMP)."""
     from oracle import port
     threads = os.cpu_count() or 1
     port.set_threads(threads)
-    r = port.OracleRun(grid, actions, seed, log_births=False)
-    r.load(agents)
+    r = port.OracleRun(w.grid, w.actions, w.seed, w.genetics, log_births=False)
+    r.load(w.agents)
     if warmup > 0:
         r.step(warmup)
     n0 = r.num_agents()
@@ -216,21 +220,25 @@ def gather_sum(dist, x: float) -> float:
 
 
 def run_reference(args, world, rank, dist):
+    """The reference arm: the CPU implementation of the path on this host's
+    cores (the C port, OpenMP on every core), on the same workload, config,
+    warm-up and timed steps as this implementation's line."""
     if rank != 0:
         return 0
-    grid, agents, actions = build_workload(args.workload, args.seed)
-    steps = max(1, min(args.steps, args.cpu_steps))
-    warm = min(args.warmup, 1)
-    n_as, dt, thr = cpu_leg(grid, agents, actions, args.seed, steps, warm)
+    w = build_workload(args.workload, args.seed)
+    steps = max(1, args.steps)
+    warm = args.warmup
+    n_as, dt, thr = cpu_leg(w, steps, warm)
     v = n_as / dt
-    sample = (f"{steps} step(s) after {warm} warm-up step(s) of the full {args.workload} workload "
-              f"({WORKLOADS[args.workload]['agents']} initial agents)")
+    sample = (f"all {steps} timed step(s) after {warm} warm-up step(s) of the full {w.name} workload "
+              f"({len(w.agents)} initial agents) on the C port of the reference algorithm "
+              f"(oracle/qhg_oracle.c, OpenMP, {thr} threads)")
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "agent-steps/s", "n_gpus": args.gpus,
         "steps": steps, "warmup": warm, "ms_per_step": 1000.0 * dt / steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "int32/f32/f64", "data": "synthetic",
-        "config": {"workload": args.workload, "detail": WORKLOADS[args.workload]["desc"],
-                   "cpu": "C port of the reference algorithm (oracle/qhg_oracle.c), OpenMP"},
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32/f32/f64",
+        "data": "synthetic (seeded; shapes and distributions of the configuration)",
+        "config": workload_config(w, world),
         "cpu_baseline": {"value": v, "unit": "agent-steps/s", "cores": thr, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": "agent-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -238,14 +246,79 @@ def run_reference(args, world, rank, dist):
     return 0
 
 
+def step_roofline(w, kms, prof_agents, births_per_step):
+    """Roofline of one step: its algorithmic bytes over the summed event
+    time of its kernels; the same for the genome kernel alone."""
+    kmean = kms.mean(axis=0)
+    names = ["k_actions", "k_cell_scan", "k_scatter", "k_genomes"]
+    nk = 4 if w.genetics.genome_size > 0 else 3
+    step_ms = float(kmean[:nk].sum())
+    kshare = {names[i]: {"ms": float(kmean[i]), "share": float(kmean[i] / step_ms) if step_ms > 0 else 0.0}
+              for i in range(nk)}
+    dominant = max(range(nk), key=lambda i: kmean[i])
+    C = w.grid.num_cells
+    alg_bytes = AGENT_BYTES * prof_agents + w.cell_bytes * C + BIRTH_BYTES * births_per_step
+    peak, peak_kind = read_peaks()
+    achieved = alg_bytes / (step_ms / 1000.0) / 1e9 if step_ms > 0 else 0.0
+    tpa = read_traffic(w.name)
+    roof = {"bound": "hbm", "kernel": "one step: " + " + ".join(names[:nk]) + f" (dominant: {names[dominant]})",
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
+            "traffic": (tpa * prof_agents) if tpa is not None else None,
+            "algorithmic_bytes": alg_bytes,
+            "algorithmic_formula": f"{AGENT_BYTES} B x agents + {w.cell_bytes} B x cells"
+                                   + (f" + {BIRTH_BYTES} B x births" if nk == 4 else ""),
+            "per_kernel": kshare}
+    if nk == 4:
+        gb = BIRTH_BYTES * births_per_step
+        gms = float(kmean[3])
+        ga = gb / (gms / 1000.0) / 1e9 if gms > 0 else 0.0
+        roof["k_genomes"] = {"achieved": ga, "frac": ga / peak, "ms": gms, "births_per_step": births_per_step,
+                             "algorithmic_bytes": gb, "unit": "GB/s"}
+    return roof, step_ms
+
+
+def profile_steps(run, n_prof_start, prof_steps):
+    """Per-kernel device times of prof_steps steps (each kernel launched alone
+    between CUDA events on the run's stream), the mean agents at their start
+    and the mean births per step."""
+    kms = run.step_profiled(prof_steps)
+    pst = run.stats(prof_steps)
+    prof_agents = (n_prof_start + int(pst[:-1, 0].sum())) / prof_steps
+    births = float(pst[:, 1].mean())
+    return kms, prof_agents, births
+
+
+def measure_genetics(seed: int, device: int, steps: int, warmup: int, prof_steps: int):
+    """The genetics run beside the default workload: agent-steps/s of the
+    step with genomes and the genome kernel's roofline (3 x 1 KiB per birth)."""
+    from qhg4_gb300.gpu import GpuRun
+    w = build_workload("genetics", seed)
+    run = GpuRun(w.grid, w.actions, w.seed, w.genetics, capacity=int(len(w.agents) * 1.6) + 65536, device=device)
+    run.load(w.agents)
+    run.step(warmup)
+    run.sync()
+    n_start = run.num_agents()
+    ms = run.step_timed(steps)
+    st = run.stats(steps)
+    agent_steps = n_start + int(st[:-1, 0].sum())
+    kms, prof_agents, births = profile_steps(run, int(st[-1, 0]), prof_steps)
+    roof, step_ms = step_roofline(w, kms, prof_agents, births)
+    run.close()
+    return {"value": agent_steps / (ms / 1000.0), "unit": "agent-steps/s", "steps": steps, "warmup": warmup,
+            "ms_per_step": ms / steps, "agents_at_timed_start": n_start, "config": workload_config(w, 1),
+            "births_per_step": births, "roofline": roof}
+
+
 def run_ours(args, world, rank, local, dist):
     from qhg4_gb300.gpu import GpuRun
     device = local if world > 1 else args.device
-    grid, agents, actions = build_workload(args.workload, args.seed + rank)
+    w = build_workload(args.workload, args.seed + rank)
+    grid, agents, actions = w.grid, w.agents, w.actions
     N0 = len(agents)
     C = grid.num_cells
-    wl = WORKLOADS[args.workload]
-    run = GpuRun(grid, actions, args.seed + rank, capacity=int(N0 * 2.5) + 65536, device=device)
+    cap = int(N0 * (1.6 if w.genetics.genome_size > 0 else 2.5)) + 65536
+    run = GpuRun(grid, actions, w.seed, w.genetics, capacity=cap, device=device)
     run.load(agents)
     if args.warmup > 0:
         run.step(args.warmup)
@@ -265,40 +338,22 @@ def run_ours(args, world, rank, local, dist):
     agent_steps = n_start + int(st[:-1, 0].sum()) if args.steps > 0 else 0
     # per-kernel device times (each kernel launched alone between events)
     prof_steps = max(1, args.profile_steps)
-    kms = run.step_profiled(prof_steps)
-    n_prof_start = int(st[-1, 0]) if args.steps > 0 else n_start
-    pst = run.stats(prof_steps)
-    prof_agents = (n_prof_start + int(pst[:-1, 0].sum())) / prof_steps
+    kms, prof_agents, births = profile_steps(run, int(st[-1, 0]) if args.steps > 0 else n_start, prof_steps)
     if os.environ.get("QHG_BENCH_DEBUG"):
-        sys.stderr.write(f"timed stats tail {st[-3:].tolist()} profiled stats {pst.tolist()} kms {kms.tolist()}\n")
+        sys.stderr.write(f"timed stats tail {st[-3:].tolist()} kms {kms.tolist()}\n")
     clocks = sampler.stop(t_on, t_off)
     t_max = gather_max(dist, ms / 1000.0)
     total = gather_sum(dist, float(agent_steps))
     value = total / t_max if t_max > 0 else 0.0
-
-    kmean = kms.mean(axis=0)
-    step_ms = float(kmean[:3].sum())
-    names = ["k_actions", "k_cell_scan", "k_scatter", "k_genomes"]
-    kshare = {names[i]: {"ms": float(kmean[i]), "share": float(kmean[i] / step_ms) if step_ms > 0 else 0.0}
-              for i in range(3)}
-    dominant = max(range(3), key=lambda i: kmean[i])
-    alg_bytes = AGENT_BYTES * prof_agents + wl["cell_bytes"] * C
-    peak, peak_kind = read_peaks()
-    achieved = alg_bytes / (step_ms / 1000.0) / 1e9 if step_ms > 0 else 0.0
-    tpa = read_traffic(args.workload)
-    roofline = {"bound": "hbm", "kernel": "one step: k_actions + k_cell_scan + k_scatter "
-                f"(dominant: {names[dominant]})",
-                "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
-                "traffic": (tpa * prof_agents) if tpa is not None else None,
-                "algorithmic_bytes": alg_bytes, "per_kernel": kshare}
+    roofline, step_ms = step_roofline(w, kms, prof_agents, births)
+    run.close()
 
     # end to end through the public API: upload from host, the configured job
     # length with per-step statistics read back, download of the final table
     e2e = None
     if not args.skip_e2e:
-        job_steps = wl["job_steps"] if args.e2e_steps <= 0 else args.e2e_steps
-        run2 = GpuRun(grid, actions, args.seed + rank, capacity=int(N0 * 2.5) + 65536, device=device)
+        job_steps = w.steps if args.e2e_steps <= 0 else args.e2e_steps
+        run2 = GpuRun(grid, actions, w.seed, w.genetics, capacity=cap, device=device)
         run2.sync()
         t0 = time.perf_counter()
         run2.load(agents)
@@ -312,7 +367,7 @@ def run_ours(args, world, rank, local, dist):
         final = run2.agents(sort_by_id=False)
         dt = time.perf_counter() - t0
         run2.close()
-        rec = 8 + 4 + 4 + 4 + 4 + 1 + 1
+        rec = 8 + 4 + 4 + 4 + 4 + 1 + 1 + (16 * w.genetics.num_blocks if w.genetics.genome_size > 0 else 0)
         e2e_t = gather_max(dist, dt)
         e2e_as = gather_sum(dist, float(e_as))
         e2e = {"value": e2e_as / e2e_t, "unit": "agent-steps/s",
@@ -321,10 +376,12 @@ def run_ours(args, world, rank, local, dist):
                "steps": job_steps, "detail": "qhg_gpu_upload_agents from host arrays + per-step "
                "qhg_gpu_step(1) and qhg_gpu_stats(1) + final qhg_gpu_download, wall clock"}
 
+    genetics = None
+    if not args.skip_genetics and w.genetics.genome_size == 0:
+        genetics = measure_genetics(args.seed + rank, device, args.genetics_steps, 3, prof_steps)
     # the batched ensemble beside the single large run (256 runs, 500 steps each)
     batched = None
     if not args.skip_batched:
-        run.close()
         batched = measure_ensemble(args.ensemble_runs, args.ensemble_steps, device, args.plain_runs,
                                    seed=2024 + rank)
         batched["workload"] = ("batched ensemble: runs with grid n in {32,64,128}, agents log-uniform "
@@ -337,26 +394,24 @@ def run_ours(args, world, rank, local, dist):
     cpu = None
     if rank == 0 and not args.skip_cpu:
         cs = max(1, args.cpu_steps)
-        n_as, dt, thr = cpu_leg(grid, agents, actions, args.seed, cs, 0)
+        n_as, dt, thr = cpu_leg(w, cs, 0)
         cpu = {"value": n_as / dt, "unit": "agent-steps/s", "cores": thr, "kind": "port",
                "sample": f"first {cs} step(s) of the same workload on the C port of the reference algorithm "
-                         f"(oracle/qhg_oracle.c, OpenMP, {thr} threads)"}
-    run.close()
+                         f"(oracle/qhg_oracle.c, OpenMP, {thr} threads); the port runs "
+                         f"{PORT_VS_REFERENCE} the reference's own OpenMP code built from its sources"}
     if rank == 0:
+        cfg = workload_config(w, world)
+        cfg["agents_at_timed_start"] = n_start
         line = {
             "metric": METRIC, "value": value, "unit": "agent-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / max(1, args.steps),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32/f32/f64",
             "data": "synthetic (seeded; shapes and distributions of the configuration)",
-            "config": {"workload": args.workload, "detail": wl["desc"], "agents": N0, "cells": C,
-                       "agents_at_timed_start": n_start, "parallelism": f"replicas x{world}",
-                       "l2": "inputs larger than L2 (hot table ~21 B x agents > 129 MB)"},
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "batched": batched,
-            "served": served,
-            # per step: the action kernel and the scatter in each of the three
-            # forms (two of each return at once) and the cell scan
-            "gpu_launches": 7 * args.steps * world,
-            "gpu_launches_per_step": {"working": 3, "idle_forms": 4},
+            "config": cfg,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "genetics": genetics,
+            "batched": batched, "served": served,
+            "gpu_launches": LAUNCHES_PER_STEP * args.steps * world,
+            "gpu_launches_per_step": LAUNCHES_PER_STEP,
         }
         print(json.dumps(line), flush=True)
     return 0
@@ -522,12 +577,14 @@ def main():
     ap.add_argument("--seed", type=int, default=42)
     ap.add_argument("--device", type=int, default=0)
     ap.add_argument("--profile-steps", type=int, default=3)
-    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--cpu-steps", type=int, default=10)
     ap.add_argument("--e2e-steps", type=int, default=0)
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-batched", action="store_true")
     ap.add_argument("--skip-served", action="store_true")
+    ap.add_argument("--skip-genetics", action="store_true")
+    ap.add_argument("--genetics-steps", type=int, default=20)
     args = ap.parse_args()
     if args.warmup < 0 or args.steps < 0:
         ap.error("steps and warmup must be >= 0")

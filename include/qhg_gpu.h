@@ -329,15 +329,18 @@ int qhg_batch_destroy(qhg_batch *batch);
  * d_counts (num_cells) receives the live agents per cell and d_first_row
  * (num_cells + 1) the exclusive prefix of the counts, i.e. the first row of
  * each cell in a table sorted by cell, with the agent count last.  Runs on
- * `stream` (a cudaStream_t, NULL for the default stream) and waits for it.
+ * `stream` (a cudaStream_t, NULL for the default stream) on the current
+ * device and is synchronous: it reads its error word back to the host and
+ * waits for the stream before it returns, so it cannot be called on a
+ * stream that is being captured.
  *
  * It allocates nothing: its scratch (the look-back status words) is a
  * file-scope __device__ array sized for QHG_CENSUS_MAX_CELLS cells, held by
  * every GPU that loads the library until the process exits.  Larger grids
- * are rejected with QHG_ERR_ARG.  The first call on a device looks up the
- * array's device address with that device current, so make it before any
- * stream capture.  All calls on a device share the array: calls that
- * overlap on the GPU race and must be serialised by the caller.
+ * are rejected with QHG_ERR_ARG.  Every call looks up the array's device
+ * address on the current device (cudaGetSymbolAddress, no allocation).  All
+ * calls on a device share the array and each leaves its contents behind:
+ * calls that overlap on the GPU race and must be serialised by the caller.
  */
 #define QHG_CENSUS_MAX_CELLS  4194304
 int qhg_gpu_cell_census_noalloc(const int32_t *d_agent_cell, int64_t n_agents, int32_t num_cells,

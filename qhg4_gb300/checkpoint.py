@@ -8,6 +8,10 @@ given or accumulated beside the table: K and move weights set between steps
 (OccTracker) and MoveStats' per-cell arrays (what the reference's
 writeAdditionalDataQDF / readAdditionalDataQDF carry, actions/MoveStats.cpp).
 A run resumed from a checkpoint continues exactly as the uninterrupted one.
+The checkpoint also records the seed and a digest of the action list and
+genetics (spec_digest): the draws are keyed by the seed and the actions'
+windows, so a resume with a different seed or action set would continue
+differently, and resume() refuses it.
 Checkpoints are .npz files (HDF5, which QDF files need, is not available
 here).
 """
@@ -18,14 +22,15 @@ from typing import Sequence
 import numpy as np
 
 from .gpu import GpuRun
-from .spec import Action, Genetics
+from .spec import Action, Genetics, spec_digest
 from .workload import Agents, Grid
 
 
 def save(run: GpuRun, path: str) -> None:
     a = run.agents(sort_by_id=True)
     cols = dict(id=a.id, cell=a.cell, birth=a.birth, age=a.age, lastb=a.lastb, gender=a.gender, state=a.state,
-                step=np.array([run.current_step()], np.int64), next_id=np.array([run.next_id()], np.int64))
+                step=np.array([run.current_step()], np.int64), next_id=np.array([run.next_id()], np.int64),
+                seed=np.array([run.seed], np.uint64), spec=np.array(run.spec_digest))
     if a.genome is not None:
         cols["genome"] = a.genome
     if run.capacity_K is not None:
@@ -46,6 +51,10 @@ def save(run: GpuRun, path: str) -> None:
 def resume(grid: Grid, actions: Sequence[Action], seed: int, path: str, genetics: Genetics = Genetics(),
            **kw) -> GpuRun:
     d = np.load(path)
+    if "seed" in d and int(d["seed"][0]) != int(seed):
+        raise ValueError(f"checkpoint {path} was written by a run with seed {int(d['seed'][0])}, not {int(seed)}")
+    if "spec" in d and str(d["spec"]) != spec_digest(actions, genetics):
+        raise ValueError(f"checkpoint {path} was written by a run with other actions, parameters or genetics")
     a = Agents(d["id"], d["cell"], d["birth"], d["age"], d["lastb"], d["gender"], d["state"],
                d["genome"] if "genome" in d else None)
     if "occupancy" in d:

@@ -16,7 +16,6 @@
 // the tile status words in the static array instead of the run's buffers.
 #include <cstdint>
 #include <cstring>
-#include <mutex>
 #include <string>
 
 #include <cuda_runtime.h>
@@ -30,7 +29,6 @@ constexpr int kItems = 8;
 constexpr int kTileCells = kThreads * kItems;
 constexpr uint32_t kMaxTiles = (uint32_t)QHG_CENSUS_MAX_CELLS / kTileCells;
 constexpr uint32_t kSpinLimit = 1u << 24;
-constexpr int kMaxDevices = 64;
 
 // The scratch shared by every call on a device.  Calls that overlap on the
 // GPU race on it; each call leaves its contents behind, and the next call
@@ -49,8 +47,6 @@ struct CensusScratch {
 static __device__ __align__(256) CensusScratch g_census_scratch;
 
 thread_local std::string g_census_error;
-std::mutex g_census_mutex;
-CensusScratch *g_census_ptr[kMaxDevices] = {nullptr};
 
 __global__ void k_census_reset(CensusScratch *sc, uint32_t *counts, int C) {
     const int stride = gridDim.x * blockDim.x;
@@ -182,26 +178,17 @@ extern "C" int qhg_gpu_cell_census_noalloc(const int32_t *d_agent_cell, int64_t 
     if (n_agents > 0x7fffffffLL) {
         return census_fail(QHG_ERR_ARG, "n_agents exceeds 2^31-1");
     }
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return census_fail(QHG_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
-    if (dev < 0 || dev >= kMaxDevices) return census_fail(QHG_ERR_ARG, "device ordinal above 63");
-    CensusScratch *sc = nullptr;
-    {
-        // first call on a device: look up the device address of the scratch
-        // array with the device current (the symbol's host-side name is not
-        // a device address)
-        std::lock_guard<std::mutex> lk(g_census_mutex);
-        if (g_census_ptr[dev] == nullptr) {
-            void *p = nullptr;
-            e = cudaGetSymbolAddress(&p, g_census_scratch);
-            if (e != cudaSuccess) {
-                return census_fail(QHG_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-            }
-            g_census_ptr[dev] = static_cast<CensusScratch *>(p);
-        }
-        sc = g_census_ptr[dev];
+    // The device address of the scratch array on the current device.  The
+    // array's name in host code is only a host-side stand-in, so the address
+    // is looked up with the device current, on every call: a cached address
+    // would go stale when the device's context is torn down and rebuilt
+    // (cudaDeviceReset), and the lookup allocates nothing.
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_census_scratch);
+    if (e != cudaSuccess) {
+        return census_fail(QHG_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
     }
+    CensusScratch *sc = static_cast<CensusScratch *>(p);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int C = num_cells;
     k_census_reset<<<(C + 255) / 256 < 1024 ? (C + 255) / 256 : 1024, 256, 0, st>>>(sc, d_counts, C);

@@ -12,7 +12,7 @@ from typing import Sequence
 
 import numpy as np
 
-from .spec import Action, Genetics, MAX_ACTIONS, execution_order
+from .spec import Action, Genetics, MAX_ACTIONS, execution_order, spec_digest
 from .workload import Agents, Grid
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -193,6 +193,8 @@ class GpuRun:
         self.h = h
         self.C = grid.num_cells
         self.genetics = genetics
+        self.seed = int(seed)
+        self.spec_digest = spec_digest(actions, genetics)
         self.grid = grid
         self.track_occupancy = track_occupancy
         # what the run was given beyond its grid (for checkpoints): K and

@@ -104,6 +104,18 @@ def execution_order(actions: Sequence[Action]) -> List[Action]:
     return sorted(actions, key=lambda a: (int(a.prio), ACTION_NAMES[a.type]))
 
 
+def spec_digest(actions: Sequence[Action], genetics: Genetics = Genetics()) -> str:
+    """A digest of what a run's draws and decisions depend on besides its
+    seed: the actions in execution order with their parameters, and the
+    genetics.  Checkpoints carry it, so that a resume with other settings is
+    refused instead of silently diverging."""
+    import hashlib
+    parts = [f"{a.type}:{ACTION_NAMES[a.type]}:" + ",".join(repr(x) for x in a.params4())
+             for a in execution_order(actions)]
+    parts.append(f"genetics:{genetics.genome_size}:{genetics.num_crossover}:{genetics.mutation_rate!r}")
+    return hashlib.sha256(";".join(parts).encode()).hexdigest()
+
+
 def draw_windows(ordered: Sequence[Action]) -> List[int]:
     """First draw index of each action's window in the per-agent stream."""
     out, w = [], 0

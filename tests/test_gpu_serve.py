@@ -58,6 +58,7 @@ def test_served_jobs_equal_alone(gpu_lib, tmp_path):
                 assert np.array_equal(cols["m_ulCellID"][o], ref.cell)
                 assert np.array_equal(cols["m_fBirthTime"][o].view(np.uint32), ref.birth.view(np.uint32))
                 assert np.array_equal(cols["m_fAge"][o].view(np.uint32), ref.age.view(np.uint32))
+                assert np.array_equal(cols["m_fLastBirth"][o].view(np.uint32), ref.lastb.view(np.uint32))
                 assert np.array_equal(cols["m_iGender"][o], ref.gender)
                 assert np.array_equal(cols["m_iLifeState"][o], ref.state)
         d = table_diff(j.result.sorted_by_id(), r.agents())

@@ -9,8 +9,10 @@ import subprocess
 
 import pytest
 
+from oracle.refpath import REFERENCE_DIR
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference/QHG4"
+REF = REFERENCE_DIR
 
 
 @pytest.mark.skipif(not os.path.isdir(REF), reason="the reference tree is not present")

@@ -17,6 +17,8 @@ import subprocess
 import numpy as np
 import pytest
 
+from oracle.refpath import REFERENCE_DIR
+
 from oracle.refsim_io import ref_program, run_reference, write_input
 from qhg4_gb300.spec import CROSSOVER_POISSON1, Genetics, config1_actions, config3_actions
 from qhg4_gb300.workload import Agents, make_agents, uniform_grid
@@ -24,7 +26,7 @@ from qhg4_gb300.workload import Agents, make_agents, uniform_grid
 from helpers import table_diff
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference/QHG4"
+REF = REFERENCE_DIR
 HERE = os.path.join(ROOT, "tests", "plugin_host")
 
 

@@ -60,3 +60,43 @@ def test_census_noalloc_rejects_oversized_grid(gpu_lib):
     rc = gpu_lib.qhg_gpu_cell_census_noalloc(None, 0, 4194305, ct.c_void_p(8), ct.c_void_p(8), None)
     assert rc == -1
     assert b"QHG_CENSUS_MAX_CELLS" in gpu_lib.qhg_gpu_census_last_error()
+
+
+def test_census_noalloc_many_tiles_then_fewer_then_maximum(gpu_lib):
+    """Synthetic cell arrays without a run, checked against np.bincount:
+    about 1M cells (hundreds of scan tiles, so that tiles combine the
+    aggregates of tiles still waiting for their prefix), then a grid of a
+    few tiles on the next call (the status words the first call left behind
+    must count as stale), then exactly QHG_CENSUS_MAX_CELLS cells (every
+    status word of the static array in use), and the small grid again."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(11)
+    for C, n in ((1_000_003, 3_000_000), (5_000, 40_000), (4_194_304, 6_000_000), (5_000, 1)):
+        cells = rng.integers(0, C, size=n, dtype=np.int64).astype(np.int32)
+        # a dense stretch of cells holding many agents each, and empty ones
+        cells[: n // 4] = (cells[: n // 4] % max(1, C // 64)).astype(np.int32)
+        counts, first = _census(gpu_lib, torch, cells, C)
+        expect = np.bincount(cells, minlength=C).astype(np.uint64)
+        assert np.array_equal(counts.astype(np.uint64), expect), f"C={C}: counts differ"
+        assert first[0] == 0 and int(first[-1]) == n
+        assert np.array_equal(first[1:].astype(np.uint64), np.cumsum(expect)), f"C={C}: first rows differ"
+
+
+def test_census_noalloc_reports_a_bad_cell(gpu_lib):
+    """A cell index outside the grid is reported (never counted) and the
+    next call is unaffected."""
+    torch = pytest.importorskip("torch")
+    C = 3000
+    cells = np.arange(10_000, dtype=np.int32) % C
+    cells[1234] = C + 5
+    d_cell = torch.from_numpy(cells).cuda()
+    d_counts = torch.zeros(C, dtype=torch.int32, device="cuda")
+    d_first = torch.zeros(C + 1, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    rc = gpu_lib.qhg_gpu_cell_census_noalloc(ct.c_void_p(d_cell.data_ptr()), len(cells), C,
+                                             ct.c_void_p(d_counts.data_ptr()), ct.c_void_p(d_first.data_ptr()), None)
+    assert rc == -1
+    assert b"1234" in gpu_lib.qhg_gpu_census_last_error()
+    cells[1234] = 0
+    counts, first = _census(gpu_lib, torch, cells, C)
+    assert np.array_equal(counts.astype(np.int64), np.bincount(cells, minlength=C))
