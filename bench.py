@@ -71,6 +71,91 @@ def workload_config(w, world: int):
             "l2": "inputs larger than L2 (hot table ~21 B x agents > 129 MB)"}
 
 
+class NvmlSampler:
+    """Samples the SM clock, power and clock-event reasons through NVML
+    (read-only queries, ctypes into libnvidia-ml) every ~2 ms from a thread,
+    so that even a timed region of a few milliseconds holds samples.  The
+    GPU is found by the PCI bus ID the CUDA runtime gives for `device`."""
+
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, device: int):
+        import ctypes as ct
+        self.ct = ct
+        self.nv = ct.CDLL("libnvidia-ml.so.1")
+        if self.nv.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        bus = ct.create_string_buffer(64)
+        rt = None
+        for name in ("libcudart.so", "libcudart.so.13", "libcudart.so.12"):
+            try:
+                rt = ct.CDLL(name)
+                break
+            except OSError:
+                continue
+        self.h = ct.c_void_p()
+        rc = -1
+        if rt is not None and rt.cudaDeviceGetPCIBusId(bus, 64, int(device)) == 0:
+            rc = self.nv.nvmlDeviceGetHandleByPciBusId_v2(bus, ct.byref(self.h))
+        if rc != 0:
+            rc = self.nv.nvmlDeviceGetHandleByIndex_v2(int(device), ct.byref(self.h))
+        if rc != 0:
+            raise OSError("no NVML handle for the device")
+        fn = getattr(self.nv, "nvmlDeviceGetCurrentClocksEventReasons", None)
+        self.reasons_fn = fn if fn is not None else self.nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx = ct.c_uint()
+        self.max_mhz = float(mx.value) if self.nv.nvmlDeviceGetMaxClockInfo(self.h, 1, ct.byref(mx)) == 0 else None
+        self.samples = []
+        self.stop_flag = False
+        self.thread = None
+
+    def _sample(self):
+        ct = self.ct
+        mhz, rs, mw = ct.c_uint(), ct.c_ulonglong(), ct.c_uint()
+        while not self.stop_flag:
+            t = time.perf_counter()
+            if self.nv.nvmlDeviceGetClockInfo(self.h, 1, ct.byref(mhz)) == 0 and \
+                    self.reasons_fn(self.h, ct.byref(rs)) == 0:
+                self.nv.nvmlDeviceGetPowerUsage(self.h, ct.byref(mw))
+                self.samples.append((t, float(mhz.value), int(rs.value), mw.value / 1000.0))
+            time.sleep(0.002)
+
+    def start(self):
+        self.thread = threading.Thread(target=self._sample, daemon=True)
+        self.thread.start()
+
+    def wait_first(self, timeout: float = 5.0) -> None:
+        t0 = time.perf_counter()
+        while not self.samples and time.perf_counter() - t0 < timeout:
+            time.sleep(0.005)
+
+    def mark(self) -> float:
+        return time.perf_counter()
+
+    def stop(self, t_from: float = None, t_to: float = None):
+        self.stop_flag = True
+        if self.thread:
+            self.thread.join(timeout=2)
+        inside = [x for x in self.samples if t_from is not None and t_from <= x[0] <= t_to]
+        window = bool(inside)
+        use = inside if inside else self.samples
+        reasons = sorted({nm for _, _, r, _ in use for bit, nm in self.REASONS.items() if r & bit})
+        sm = [m for _, m, _, _ in use]
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": self.max_mhz, "reasons": reasons,
+                "samples": len(use), "power_w_max": max((p for *_, p in use), default=None),
+                "source": "NVML every ~2 ms",
+                "window": "timed region" if window else "whole measurement (no sample inside the timed region)"}
+
+
+def clock_sampler(device: int):
+    """NVML sampler where NVML loads, else nvidia-smi."""
+    try:
+        return NvmlSampler(device)
+    except (OSError, AttributeError):
+        return ClockSampler(device)
+
+
 class ClockSampler:
     """Samples SM clocks and throttle reasons with nvidia-smi while running."""
 
@@ -257,7 +342,7 @@ def step_roofline(w, kms, prof_agents, births_per_step):
               for i in range(nk)}
     dominant = max(range(nk), key=lambda i: kmean[i])
     C = w.grid.num_cells
-    alg_bytes = AGENT_BYTES * prof_agents + w.cell_bytes * C + BIRTH_BYTES * births_per_step
+    alg_bytes = AGENT_BYTES * prof_agents + w.cell_bytes * C + (BIRTH_BYTES * births_per_step if nk == 4 else 0.0)
     peak, peak_kind = read_peaks()
     achieved = alg_bytes / (step_ms / 1000.0) / 1e9 if step_ms > 0 else 0.0
     tpa = read_traffic(w.name)
@@ -324,7 +409,7 @@ def run_ours(args, world, rank, local, dist):
         run.step(args.warmup)
     run.sync()
     n_start = run.num_agents()
-    sampler = ClockSampler(device)
+    sampler = clock_sampler(device)
     sampler.start()
     sampler.wait_first()
     if dist is not None:

@@ -150,6 +150,14 @@ int qhg_gpu_upload_grid(qhg_run *run, const int32_t *nbr6, const uint8_t *nnbr, 
  * (and then change nothing), and take effect from the next step on. */
 int qhg_gpu_set_capacity(qhg_run *run, const double *K);
 int qhg_gpu_set_move_weights(qhg_run *run, const double *cumw7);
+/* The ice flags of the grid's Geography (Geography::m_abIce, C entries,
+ * nonzero = ice; NULL = no ice), from the next step on: WeightedMove
+ * registers no move into an ice cell (actions/WeightedMove.cpp:91; its draws
+ * are taken all the same), and weights that follow K give ice cells weight
+ * 0, as the SingleEvaluator does (actions/SingleEvaluator.cpp:183-202).
+ * RandomMove ignores ice, as in the reference.  qhg_gpu_upload_grid clears
+ * the flags.  Waits for the run's stream like qhg_gpu_set_capacity. */
+int qhg_gpu_set_ice(qhg_run *run, const uint8_t *ice);
 /* agents in any order; dead rows (state 0) are dropped */
 int qhg_gpu_upload_agents(qhg_run *run, const qhg_agents_soa *agents, int64_t n, int32_t first_step);
 /* runs nsteps steps asynchronously on the run's stream */

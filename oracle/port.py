@@ -66,6 +66,8 @@ def _load():
     lib.qo_move_stats_enable.argtypes = [P, ct.c_int, P, P, ct.c_double, ct.c_int]
     lib.qo_move_stats.restype = ct.c_int
     lib.qo_move_stats.argtypes = [P, P, P, P]
+    lib.qo_set_ice.restype = ct.c_int
+    lib.qo_set_ice.argtypes = [P, P]
     lib.qo_set_threads.argtypes = [ct.c_int]
     lib.qo_max_threads.restype = ct.c_int
     lib.qo_destroy.argtypes = [P]
@@ -142,6 +144,17 @@ class OracleRun:
         w = np.ascontiguousarray(W, dtype=np.float64)
         assert w.shape == (self.C, 7)
         _load().qo_set_move_weights(self.h, _p(w))
+
+    def set_ice(self, ice) -> None:
+        """Geography::m_abIce per cell from the next step on (None: no ice);
+        WeightedMove refuses moves into ice cells."""
+        if ice is None:
+            _load().qo_set_ice(self.h, None)
+            return
+        f = np.ascontiguousarray(np.asarray(ice) != 0, dtype=np.uint8)
+        assert f.shape == (self.C,)
+        self._ice = f
+        _load().qo_set_ice(self.h, _p(f))
 
     def move_stats_enable(self, mode: int, lon: np.ndarray, lat: np.ndarray, radius: float = 1.0,
                           cartesian: bool = False) -> None:

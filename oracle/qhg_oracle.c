@@ -81,6 +81,7 @@ typedef struct {
     double *K;
     double *W;          /* cumulated WeightedMove weights [C*7] */
     int w_given;        /* W was given (qo_set_move_weights), not derived from K */
+    uint8_t *ice;       /* Geography::m_abIce per cell (NULL: no Geography, no ice) */
     /* agents, sorted by ID */
     int64_t n, cap;
     int64_t *id;
@@ -294,12 +295,13 @@ static void make_genome(const qo_run *r, uint64_t *baby, const uint64_t *gm, con
 }
 
 /* WeightedMove's weights from K: a SingleEvaluator with direct values,
- * cumulated over the neighbours (actions/SingleEvaluator.cpp:174-241) */
+ * cumulated over the neighbours (actions/SingleEvaluator.cpp:174-241); an
+ * ice cell of the Geography weighs 0 (:183-202) */
 static void weights_from_K(qo_run *r) {
     const int C = r->C;
     for (int c = 0; c < C; c++) {
         double dV = r->K[c];
-        r->W[(size_t)c * 7] = (dV > 0) ? dV : 0;
+        r->W[(size_t)c * 7] = (r->ice != NULL && r->ice[c]) ? 0 : ((dV > 0) ? dV : 0);
     }
     for (int c = 0; c < C; c++) {
         double dW = r->W[(size_t)c * 7];
@@ -653,7 +655,8 @@ int qo_step(qo_run *r, int nsteps, uint64_t *stats_out) {
                         }
                         if (dir > 0) {
                             int to = r->nbr[(size_t)c * 6 + dir - 1];
-                            if (to >= 0) { out[i].move_to = to; nMoves++; }
+                            /* a move into an ice cell is not registered (actions/WeightedMove.cpp:91) */
+                            if (to >= 0 && (r->ice == NULL || !r->ice[to])) { out[i].move_to = to; nMoves++; }
                         }
                     }
                     break;
@@ -886,6 +889,24 @@ int qo_set_move_weights(qo_run *r, const double *W) {
     return 0;
 }
 
+/* Geography::m_abIce per cell (nonzero: ice), from the next step on;
+ * WeightedMove refuses moves into ice cells (actions/WeightedMove.cpp:91)
+ * and the SingleEvaluator over K gives them weight 0
+ * (actions/SingleEvaluator.cpp:183-202).  NULL removes the Geography's ice. */
+int qo_set_ice(qo_run *r, const uint8_t *ice) {
+    if (ice == NULL) {
+        free(r->ice);
+        r->ice = NULL;
+    } else {
+        if (r->ice == NULL) r->ice = (uint8_t *)malloc((size_t)r->C);
+        if (r->ice == NULL) return -1;
+        memcpy(r->ice, ice, (size_t)r->C);
+    }
+    /* weights that follow K give ice cells weight 0 */
+    if (!r->w_given) weights_from_K(r);
+    return 0;
+}
+
 void qo_set_threads(int n) {
 #ifdef _OPENMP
     if (n > 0) omp_set_num_threads(n);
@@ -904,7 +925,7 @@ int qo_max_threads(void) {
 
 void qo_destroy(qo_run *r) {
     if (r == NULL) return;
-    free(r->nbr); free(r->nnbr); free(r->K); free(r->W); free(r->count); free(r->B); free(r->D);
+    free(r->nbr); free(r->nnbr); free(r->K); free(r->W); free(r->count); free(r->B); free(r->D); free(r->ice);
     free(r->ms_lon); free(r->ms_lat); free(r->ms_hops); free(r->ms_thops); free(r->ms_dist);
     free(r->ms_time); free(r->ms_tdist); free(r->ms_ttime); free(r->ms_changed);
     free(r->id); free(r->cell); free(r->birth); free(r->age); free(r->lastb); free(r->gender);

@@ -749,6 +749,14 @@ int main(int argc, char *argv[]) {
             vModValue.push_back(dV);
         }
     }
+    /* optional: u32 has_ice, u8 ice[C] if has_ice == 1: the Geography's
+     * m_abIce, which WeightedMove reads (actions/WeightedMove.cpp:91) */
+    uint32_t iHasIce = 0;
+    std::vector<uint8_t> vIce;
+    if (bKill && ok && rd(fIn, &iHasIce, 4, 1) && (iHasIce == 1)) {
+        vIce.resize(C);
+        ok = rd(fIn, vIce.data(), 1, C);
+    }
     fclose(fIn);
     if (!ok) { fprintf(stderr, "malformed input %s\n", argv[1]); return 2; }
 
@@ -765,14 +773,16 @@ int main(int argc, char *argv[]) {
         pCG->m_mIDIndexes[c] = c;
     }
 
-    /* MoveStats reads cell coordinates from the grid's Geography; no cell is ice */
+    /* MoveStats reads cell coordinates from the grid's Geography, WeightedMove
+     * its ice flags; the Geography exists before the actions are made, as
+     * WeightedMove keeps the pointer it finds at construction */
     Geography *pGeo = NULL;
-    if (iMSMode1 > 0) {
+    if ((iMSMode1 > 0) || !vIce.empty()) {
         pGeo = new Geography(pCG, C, 6, dMSRadius);
         for (uint32_t c = 0; c < C; c++) {
-            pGeo->m_adLongitude[c] = vLon[c];
-            pGeo->m_adLatitude[c] = vLat[c];
-            pGeo->m_abIce[c] = false;
+            pGeo->m_adLongitude[c] = (iMSMode1 > 0) ? vLon[c] : 0.0;
+            pGeo->m_adLatitude[c] = (iMSMode1 > 0) ? vLat[c] : 0.0;
+            pGeo->m_abIce[c] = vIce.empty() ? false : (vIce[c] != 0);
         }
         pCG->setGeography(pGeo);
     }

@@ -18,7 +18,9 @@ Input (little endian):
   u32 n_kill_events, n_kill_events x (u32 step, u8 flags[C]) (before that
   step every agent in a flagged cell dies, as after a geography event),
   u32 n_mods, n_mods x (u32 step, u32 name_len, char name[name_len], f64 value)
-  (runtime edits through Prioritizer::modifyAttributes before that step)
+  (runtime edits through Prioritizer::modifyAttributes before that step),
+  u32 has_ice, u8 ice[C] if has_ice == 1 (the Geography's m_abIce, which
+  WeightedMove reads)
 Output:
   "QHGOUT01", u32 steps, u32 C, u64 stats[steps*4] (live, births, deaths, moves),
   u32 n_dumps, u32 dump_step[n_dumps], u32 counts[n_dumps*C],
@@ -49,7 +51,7 @@ def ref_program(kind: str) -> str:
 
 def write_input(path: str, grid: Grid, agents: Agents, actions: Sequence[Action], steps: int,
                 seed: int, genetics: Genetics = Genetics(), dump_every: int = 0,
-                layer_size: int = 65536, weights=None, k_changes=(), move_stats=None, kills=(),
+                layer_size: int = 65536, weights=None, k_changes=(), move_stats=None, kills=(), ice=None,
                 mods=()) -> None:
     C = grid.num_cells
     N = len(agents)
@@ -73,7 +75,8 @@ def write_input(path: str, grid: Grid, agents: Agents, actions: Sequence[Action]
         f.write(np.ascontiguousarray(agents.state, dtype="u1").tobytes())
         if genetics.genome_size > 0:
             f.write(np.ascontiguousarray(agents.genome, dtype="<u8").tobytes())
-        if weights is not None or len(k_changes) > 0 or move_stats is not None or len(kills) > 0 or len(mods) > 0:
+        if (weights is not None or len(k_changes) > 0 or move_stats is not None or len(kills) > 0 or len(mods) > 0
+                or ice is not None):
             f.write(struct.pack("<I", 1 if weights is not None else 0))
             if weights is not None:
                 w = np.ascontiguousarray(weights, dtype="<f8")
@@ -104,6 +107,13 @@ def write_input(path: str, grid: Grid, agents: Agents, actions: Sequence[Action]
                 f.write(struct.pack("<II", int(step), len(nb)))
                 f.write(nb)
                 f.write(struct.pack("<d", float(value)))
+            if ice is not None:
+                fi = np.ascontiguousarray(np.asarray(ice) != 0, dtype="u1")
+                assert fi.shape == (C,)
+                f.write(struct.pack("<I", 1))
+                f.write(fi.tobytes())
+            else:
+                f.write(struct.pack("<I", 0))
 
 
 class RefOutput:
@@ -151,7 +161,7 @@ def read_output(path: str, genome_blocks: int = 0) -> RefOutput:
 def run_reference(kind: str, workdir: str, grid: Grid, agents: Agents, actions: Sequence[Action],
                   steps: int, seed: int, genetics: Genetics = Genetics(), dump_every: int = 0,
                   threads: int = 0, timeout: float = 3600.0, weights=None, k_changes=(),
-                  move_stats=None, kills=(), mods=()) -> RefOutput:
+                  move_stats=None, kills=(), mods=(), ice=None) -> RefOutput:
     """Run qhg_ref_well or qhg_ref_philox on the given input; `weights`
     (C x 7 cumulative) replace the weights from K, `k_changes` holds
     (step, K) pairs: K from that step on; `move_stats` = (mode, lon, lat,
@@ -165,7 +175,7 @@ def run_reference(kind: str, workdir: str, grid: Grid, agents: Agents, actions: 
     pin = os.path.join(workdir, f"in_{kind}_{seed}.bin")
     pout = os.path.join(workdir, f"out_{kind}_{seed}.bin")
     write_input(pin, grid, agents, actions, steps, seed, genetics, dump_every, weights=weights,
-                k_changes=k_changes, move_stats=move_stats, kills=kills, mods=mods)
+                k_changes=k_changes, move_stats=move_stats, kills=kills, mods=mods, ice=ice)
     env = dict(os.environ)
     if threads > 0:
         env["OMP_NUM_THREADS"] = str(threads)

@@ -3,8 +3,8 @@
 
 With draws keyed by (seed, step, agent ID, action) the state of a run is its
 agent table (+ genomes), its step and its next agent ID, plus what it was
-given or accumulated beside the table: K and move weights set between steps
-(qhg_gpu_set_capacity / qhg_gpu_set_move_weights), the occupation history
+given or accumulated beside the table: K, move weights and ice set between
+steps (qhg_gpu_set_capacity / qhg_gpu_set_move_weights / qhg_gpu_set_ice), the occupation history
 (OccTracker) and MoveStats' per-cell arrays (what the reference's
 writeAdditionalDataQDF / readAdditionalDataQDF carry, actions/MoveStats.cpp).
 A run resumed from a checkpoint continues exactly as the uninterrupted one.
@@ -37,6 +37,8 @@ def save(run: GpuRun, path: str) -> None:
         cols["env_K"] = run.capacity_K
     if run.move_weights is not None:
         cols["env_W"] = run.move_weights
+    if run.ice is not None:
+        cols["env_ice"] = run.ice
     if run.track_occupancy:
         cols["occupancy"] = run.occupancy()
     if run.move_stats_config is not None:
@@ -60,6 +62,8 @@ def resume(grid: Grid, actions: Sequence[Action], seed: int, path: str, genetics
     if "occupancy" in d:
         kw = dict(kw, track_occupancy=True)
     run = GpuRun(grid, actions, seed, genetics, **kw)
+    if "env_ice" in d:
+        run.set_ice(d["env_ice"])
     if "env_K" in d:
         run.set_capacity(d["env_K"])
     if "env_W" in d:

@@ -77,6 +77,7 @@ struct qhg_run {
     std::vector<int32_t> h_nbr;
     std::vector<uint8_t> h_nnbr;
     bool w_given = false;        // move weights given (qhg_gpu_set_move_weights), not from K
+    std::vector<uint8_t> h_ice;  // the Geography's ice flags per cell (qhg_gpu_set_ice), empty: none
     // agents (ping-pong)
     uint32_t cap = 0;
     int64_t *d_id[2] = {nullptr, nullptr};
@@ -379,15 +380,32 @@ int qhg_host_actions(StepConst &P, int n, const int32_t *types, const double (*p
     return 0;
 }
 
+// The slots of each cell's move word that WeightedMove may move to (bits
+// 24-29): those holding a neighbour that is not ice.  WeightedMove::execute
+// registers no move into a cell the grid's Geography marks as ice
+// (actions/WeightedMove.cpp:91); ice == nullptr: no Geography, no ice.
+void qhg_host_ice_bits(int C, const int32_t *nbr6, const uint8_t *ice, std::vector<uint32_t> &cmove) {
+    for (int c = 0; c < C; c++) {
+        uint32_t wv = 0;
+        for (int j = 0; j < 6; j++) {
+            const int d = nbr6[(size_t)c * 6 + j];
+            if (d >= 0 && (ice == nullptr || ice[d] == 0)) wv |= 1u << j;
+        }
+        cmove[c] = (cmove[c] & ~(63u << 24)) | (wv << 24);
+    }
+}
+
 // Grid tables of one run: rev packs, 3 bits per neighbour slot q, the slot
 // of the cell in the neighbour's own list; wthr holds the WeightedMove
 // thresholds (SingleEvaluator's cumulated weights, actions/SingleEvaluator.cpp:174-241,
 // as integers: dR2 = wrandd()*W[n] < W[j]  <=>  u < T_j); cmove packs per cell
-// the neighbour count (bits 0-2), the slots that hold a neighbour (bits 8-13)
-// and whether all weights are equal (bit 16).
+// the neighbour count (bits 0-2), the slots that hold a neighbour (bits 8-13),
+// whether all weights are equal (bit 16) and the slots WeightedMove may move
+// to (bits 24-29, not ice).  The SingleEvaluator gives an ice cell weight 0
+// (actions/SingleEvaluator.cpp:183-202).
 int qhg_host_grid_tables(int C, const int32_t *nbr6, const uint8_t *nnbr, const double *K, bool wm,
-                         std::vector<uint32_t> &rev, std::vector<uint64_t> &wthr, std::vector<uint32_t> &cmove,
-                         std::string &err) {
+                         const uint8_t *ice, std::vector<uint32_t> &rev, std::vector<uint64_t> &wthr,
+                         std::vector<uint32_t> &cmove, std::string &err) {
     rev.assign((size_t)C, 0u);
     for (int c = 0; c < C; c++) {
         if (nnbr[c] > 6) { err = "more than 6 neighbours"; return -1; }
@@ -410,11 +428,12 @@ int qhg_host_grid_tables(int C, const int32_t *nbr6, const uint8_t *nnbr, const 
         for (int j = 0; j < 6; j++) vm |= (nbr6[(size_t)c * 6 + j] >= 0 ? 1u : 0u) << j;
         cmove[c] = (uint32_t)nnbr[c] | (vm << 8);
     }
+    qhg_host_ice_bits(C, nbr6, ice, cmove);
     if (!wm) return 0;
     std::vector<double> W((size_t)C * 7);
     for (int c = 0; c < C; c++) {
         const double dV = K[c];
-        W[(size_t)c * 7] = (dV > 0) ? dV : 0;
+        W[(size_t)c * 7] = (ice != nullptr && ice[c] != 0) ? 0 : ((dV > 0) ? dV : 0);
     }
     for (int c = 0; c < C; c++) {
         double dW = W[(size_t)c * 7];
@@ -560,6 +579,8 @@ extern "C" int qhg_gpu_create(const qhg_run_desc *desc, qhg_run **out) {
 static int ms_reset(qhg_run *r);
 static void ms_free(qhg_run *r);
 
+static const uint8_t *ice_ptr(const qhg_run *r) { return r->h_ice.empty() ? nullptr : r->h_ice.data(); }
+
 extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_t *nnbr, const double *K,
                                    int32_t num_cells) {
     if (r == nullptr || nbr6 == nullptr || nnbr == nullptr || K == nullptr || num_cells <= 0) {
@@ -572,7 +593,7 @@ extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_
     std::vector<uint32_t> cmove;
     {
         std::string err;
-        if (qhg_host_grid_tables(C, nbr6, nnbr, K, r->P.has_wmove != 0, rev, wthr, cmove, err) != 0) {
+        if (qhg_host_grid_tables(C, nbr6, nnbr, K, r->P.has_wmove != 0, nullptr, rev, wthr, cmove, err) != 0) {
             return fail(QHG_ERR_ARG, err);
         }
     }
@@ -620,6 +641,7 @@ extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_
     r->h_nnbr.assign(nnbr, nnbr + C);
     r->h_K.assign(K, K + C);
     r->w_given = false;
+    r->h_ice.clear();
     r->C = C;
     r->P.num_cells = C;
     r->grid_ok = true;
@@ -945,7 +967,7 @@ extern "C" int qhg_gpu_set_capacity(qhg_run *r, const double *K) {
     std::vector<uint64_t> wthr;
     if (tables) {
         std::string err;
-        if (qhg_host_grid_tables(C, r->h_nbr.data(), r->h_nnbr.data(), K, true, rev, wthr, cmove, err) != 0) {
+        if (qhg_host_grid_tables(C, r->h_nbr.data(), r->h_nnbr.data(), K, true, ice_ptr(r), rev, wthr, cmove, err) != 0) {
             return fail(QHG_ERR_ARG, err);
         }
     }
@@ -972,7 +994,7 @@ extern "C" int qhg_gpu_set_move_weights(qhg_run *r, const double *cumw7) {
     {
         std::string err;
         // the neighbour bits of the move words, then the weights' thresholds
-        if (qhg_host_grid_tables(C, r->h_nbr.data(), r->h_nnbr.data(), r->h_K.data(), false, rev, wthr, cmove,
+        if (qhg_host_grid_tables(C, r->h_nbr.data(), r->h_nnbr.data(), r->h_K.data(), false, ice_ptr(r), rev, wthr, cmove,
                                  err) != 0 ||
             qhg_host_move_tables(C, r->h_nnbr.data(), cumw7, wthr, cmove, err) != 0) {
             return fail(QHG_ERR_ARG, err);
@@ -985,6 +1007,50 @@ extern "C" int qhg_gpu_set_move_weights(qhg_run *r, const double *cumw7) {
     CUDA_TRY(cudaMemcpyAsync(r->d_cmove, cmove.data(), (size_t)C * sizeof(uint32_t), cudaMemcpyHostToDevice,
                              r->stream));
     r->w_given = true;
+    return refresh_cells(r);
+}
+
+extern "C" int qhg_gpu_set_ice(qhg_run *r, const uint8_t *ice) {
+    if (r == nullptr) return fail(QHG_ERR_ARG, "null run");
+    if (!r->grid_ok) return fail(QHG_ERR_STATE, "upload the grid first");
+    CUDA_TRY(cudaSetDevice(r->desc.device));
+    const int C = r->C;
+    std::vector<uint8_t> flags;
+    if (ice != nullptr) {
+        flags.resize((size_t)C);
+        for (int c = 0; c < C; c++) flags[(size_t)c] = ice[c] != 0 ? 1u : 0u;
+    }
+    const uint8_t *fp = flags.empty() ? nullptr : flags.data();
+    // the move words' WeightedMove slots, and the weights when they follow K
+    // (the SingleEvaluator gives ice cells weight 0); given weights stay
+    std::vector<uint32_t> rev, cmove;
+    std::vector<uint64_t> wthr;
+    const bool tables = r->P.has_wmove && !r->w_given;
+    {
+        std::string err;
+        if (qhg_host_grid_tables(C, r->h_nbr.data(), r->h_nnbr.data(), r->h_K.data(), tables, fp, rev, wthr, cmove,
+                                 err) != 0) {
+            return fail(QHG_ERR_ARG, err);
+        }
+    }
+    int rc = pull_state(r);
+    if (rc != QHG_OK) return rc;
+    if (tables) {
+        CUDA_TRY(cudaMemcpyAsync(r->d_wthr, wthr.data(), (size_t)C * 6 * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                                 r->stream));
+        CUDA_TRY(cudaMemcpyAsync(r->d_cmove, cmove.data(), (size_t)C * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                 r->stream));
+    } else {
+        // keep the words' other bits (the given weights' all-equal flags)
+        std::vector<uint32_t> cur((size_t)C);
+        CUDA_TRY(cudaMemcpyAsync(cur.data(), r->d_cmove, (size_t)C * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                 r->stream));
+        CUDA_TRY(cudaStreamSynchronize(r->stream));
+        qhg_host_ice_bits(C, r->h_nbr.data(), fp, cur);
+        CUDA_TRY(cudaMemcpyAsync(r->d_cmove, cur.data(), (size_t)C * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                 r->stream));
+    }
+    r->h_ice.swap(flags);
     return refresh_cells(r);
 }
 

@@ -396,7 +396,7 @@ extern "C" int qhg_batch_add_run(qhg_batch *b, const qhg_batch_run_desc *rd, con
     std::vector<uint64_t> wthr;
     std::vector<uint32_t> cmove;
     std::string err;
-    if (qhg_host_grid_tables(num_cells, nbr6, nnbr, K, b->P.has_wmove != 0, rev, wthr, cmove, err) != 0) {
+    if (qhg_host_grid_tables(num_cells, nbr6, nnbr, K, b->P.has_wmove != 0, nullptr, rev, wthr, cmove, err) != 0) {
         return bfail(QHG_ERR_ARG, err);
     }
     std::vector<int32_t> gnbr((size_t)C * 6);

@@ -12,8 +12,9 @@
 
 int qhg_host_actions(qhg::StepConst &P, int n, const int32_t *types, const double (*params)[4], std::string &err);
 int qhg_host_grid_tables(int C, const int32_t *nbr6, const uint8_t *nnbr, const double *K, bool wm,
-                         std::vector<uint32_t> &rev, std::vector<uint64_t> &wthr, std::vector<uint32_t> &cmove,
-                         std::string &err);
+                         const uint8_t *ice, std::vector<uint32_t> &rev, std::vector<uint64_t> &wthr,
+                         std::vector<uint32_t> &cmove, std::string &err);
+void qhg_host_ice_bits(int C, const int32_t *nbr6, const uint8_t *ice, std::vector<uint32_t> &cmove);
 int qhg_host_move_tables(int C, const uint8_t *nnbr, const double *W, std::vector<uint64_t> &wthr,
                          std::vector<uint32_t> &cmove, std::string &err);
 

@@ -192,6 +192,7 @@ struct ActionsSmemT {
     uint8_t tk[kTileCells];
     uint8_t nn[kTileCells];        // moves: neighbours of each cell
     uint8_t vm[kTileCells];        // moves: bit q set when neighbour slot q holds a cell
+    uint8_t wv[kTileCells];        // WeightedMove: bit q set when neighbour slot q holds a cell that is not ice
     uint8_t wf[kTileCells];        // WeightedMove: all weights of the cell equal
     uint32_t cls[kTileCells][4];   // class counts, two 16-bit counters per word
     uint32_t red[TT / 32];
@@ -248,6 +249,7 @@ struct CellView {
     uint64_t tb, td;      // Verhulst: birth (kind 1) or birth-rate death (kind 2) threshold, death threshold
     uint32_t tk;          // Verhulst kind (0 none)
     uint32_t nn, vm, wf;  // moves: neighbour count, valid neighbour slots, all weights equal
+    uint32_t wv;          // WeightedMove: valid neighbour slots that are not ice
     uint32_t c;           // cell index (WeightedMove thresholds)
 };
 
@@ -366,7 +368,8 @@ __device__ __forceinline__ uint8_t agent_outcome(const StepConst &P, const Batch
                     const uint64_t *w = wthr + (size_t)cv.c * 6;
                     for (int q = 0; q < (int)cv.nn; q++) d += (w[q] <= (uint64_t)u2) ? 1 : 0;
                 }
-                if (d > 0 && ((cv.vm >> (d - 1)) & 1u)) { dir = d; cnt_moves++; }
+                // no move into an ice cell (actions/WeightedMove.cpp:91)
+                if (d > 0 && ((cv.wv >> (d - 1)) & 1u)) { dir = d; cnt_moves++; }
             }
             break;
         }
@@ -448,7 +451,8 @@ __device__ __forceinline__ uint32_t agent_state(const StepConst &P, const BatchR
                 d = 0;
                 for (int q = 0; q < (int)cv.nn; q++) d += (wt[q] <= (uint64_t)u2) ? 1 : 0;
             }
-            if (d > 0 && ((cv.vm >> (d - 1)) & 1u)) st |= (uint32_t)d;
+            // WeightedMove registers no move into an ice cell (actions/WeightedMove.cpp:91)
+            if (d > 0 && (((kWeighted ? cv.wv : cv.vm) >> (d - 1)) & 1u)) st |= (uint32_t)d;
         }
     }
     if (iO >= 0) {   // OldAgeDeath::execute (actions/OldAgeDeath.cpp:48-67): the window test
@@ -556,6 +560,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             // so that moving agents read no neighbour data from memory
             S.nn[lc] = (uint8_t)(cm & 7u);
             S.vm[lc] = (uint8_t)((cm >> 8) & 63u);
+            S.wv[lc] = (uint8_t)((cm >> 24) & 63u);
             S.wf[lc] = (uint8_t)((cm >> 16) & 1u);
             S.tk[lc] = (uint8_t)(v.x >> 62);
             S.tb[lc] = v.x & ((1ull << 62) - 1ull);
@@ -754,6 +759,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                     cv.td = S.td[lc];
                     cv.nn = S.nn[lc];
                     cv.vm = S.vm[lc];
+                    cv.wv = S.wv[lc];
                     cv.wf = S.wf[lc];
                     cv.c = (uint32_t)c;
                     const int mate = S.mate[i];
@@ -1634,6 +1640,7 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                         cv.td = v.y;
                         cv.nn = cm & 7u;
                         cv.vm = (cm >> 8) & 63u;
+                        cv.wv = (cm >> 24) & 63u;
                         cv.wf = (cm >> 16) & 1u;
                         cv.c = c;
                         W.cv[lc] = cv;
@@ -2455,60 +2462,50 @@ __device__ __forceinline__ int poisson1(uint32_t u) {
     return k;
 }
 
-// BitGeneUtils::makeMultiMask (genes/BitGeneUtils.cpp:90-109), including its
-// behaviour for breaks that are not in ascending order
-__device__ uint64_t multi_mask(const uint32_t *br, int nb) {
-    uint32_t k = 1u - (uint32_t)(nb % 2);
-    uint64_t out = 0;
-    int i = nb - 1;
-    for (uint32_t j = 0; j < 64; j++) {
-        if ((i >= 0) && (j == 64u - br[i])) {
-            i--;
-            k = 1u - k;
-        }
-        out = (out << 1) + k;
+// BitGeneUtils::makeMultiMask (genes/BitGeneUtils.cpp:90-109) for the
+// breaks of one 64-bit block, fed one at a time in draw order.  The
+// reference emits the mask's 64 bits from the top, starting with
+// 1 - (breaks % 2), and flips the emitted value when the bit index reaches
+// 64 - break, taking the breaks from the last one backwards; a break whose
+// flip position lies at or before the previous flip (breaks given out of
+// ascending order) is never reached, and neither is any break after it.  So
+// the flips that happen are those of the longest run at the end of the draw
+// order whose values strictly increase (a break at 0 never flips), each
+// toggling the low `break` bits: `mask` is the XOR of those toggles, reset
+// whenever a break does not exceed the one before it.
+struct BlockMask {
+    uint64_t mask = 0ull;
+    int last = -1;
+    int nb = 0;
+    __device__ __forceinline__ void add(uint32_t br) {
+        const uint64_t m = (1ull << br) - 1ull;   // br in 0..63
+        mask = ((int)br > last) ? (mask ^ m) : m;
+        last = (int)br;
+        nb++;
     }
-    return out;
-}
+    // the mask makeMultiMask returns (all ones without breaks)
+    __device__ __forceinline__ uint64_t value() const { return ((nb & 1) ? 0ull : ~0ull) ^ mask; }
+};
 
-// draw k of the newborn's birth stream, lane L holding block L
+// draw k (the same for every lane) of the newborn's birth stream, lane L
+// holding block L
 __device__ __forceinline__ uint32_t birth_draw(const Draw4 &d, int k) {
-    const int src = k >> 2;
-    const uint32_t w0 = __shfl_sync(FULL_MASK, d.v[0], src);
-    const uint32_t w1 = __shfl_sync(FULL_MASK, d.v[1], src);
-    const uint32_t w2 = __shfl_sync(FULL_MASK, d.v[2], src);
-    const uint32_t w3 = __shfl_sync(FULL_MASK, d.v[3], src);
     const int q = k & 3;
-    return q == 0 ? w0 : (q == 1 ? w1 : (q == 2 ? w2 : w3));
-}
-
-// one strand word of a crossed parent genome (BitGeneUtils::crossOver,
-// genes/BitGeneUtils.cpp:116-188): strand `sel` of the parent genome after
-// nbk breaks drawn from draws kb.. of the stream, at block b
-__device__ __forceinline__ uint64_t crossed_word(const Draw4 &d, int kb, int nbk, uint32_t nbits, int b,
-                                                 const uint64_t *g, int nblk, int sel) {
-    // every lane walks all breaks (the shuffles need the whole warp) and keeps
-    // those in its own block, in draw order
-    uint32_t br[32];
-    int before = 0, nb = 0;
-    for (int t = 0; t < nbk; t++) {
-        const uint32_t pos = (uint32_t)(((uint64_t)nbits * (uint64_t)birth_draw(d, kb + t)) >> 32);
-        const int blk = (int)(pos >> 6);
-        before += (blk < b) ? 1 : 0;
-        if (blk == b && nb < 32) br[nb++] = pos & 63u;
-    }
-    const uint64_t m = nb > 0 ? multi_mask(br, nb) : ~0ull;
-    const int cur = (before & 1) ^ sel;
-    const uint64_t A = g[cur * nblk + b];
-    const uint64_t B = g[(1 - cur) * nblk + b];
-    return (m & A) | (~m & B);
+    const uint32_t mine = q == 0 ? d.v[0] : (q == 1 ? d.v[1] : (q == 2 ? d.v[2] : d.v[3]));
+    return __shfl_sync(FULL_MASK, mine, k >> 2);
 }
 
 // Genetics::makeOffspring (actions/Genetics.cpp:285-337), one warp per
 // newborn.  Birth stream of the mother: draw 0 gender (k_scatter), 1 and 2
 // the strands taken from mother and father, then (Poisson mode) the two
 // crossover counts, the mother's and the father's breakpoints, the mutation
-// count and the mutation positions.
+// count and the mutation positions.  Lane L builds blocks L and L + 32 of
+// both strands of the newborn: strand 0 is strand i1 of the mother crossed
+// over at her breaks (BitGeneUtils::crossOver, genes/BitGeneUtils.cpp:116-188:
+// before a block, the parity of the breaks in earlier blocks picks the
+// strand, inside it the makeMultiMask mask mixes the two), strand 1 the same
+// for the father with i2, then the mutation flips.  The parents' words are
+// loaded first, so that their latency overlaps the draws.
 __global__ void __launch_bounds__(256)
 k_genomes(const StepConst P, RunState *__restrict__ rs, uint64_t *__restrict__ genome,
           const uint32_t *__restrict__ brec) {
@@ -2521,11 +2518,27 @@ k_genomes(const StepConst P, RunState *__restrict__ rs, uint64_t *__restrict__ g
     const uint32_t nbits = (uint32_t)nblk * 64u;
     for (uint32_t g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < nbirths;
          g += (gridDim.x * blockDim.x) >> 5) {
-        const uint32_t ms = __ldg(&brec[(size_t)g * 5 + 0]);
-        const uint32_t fs = __ldg(&brec[(size_t)g * 5 + 1]);
-        const uint32_t bs = __ldg(&brec[(size_t)g * 5 + 2]);
-        const uint64_t mid = (uint64_t)__ldg(&brec[(size_t)g * 5 + 3]) |
-                             ((uint64_t)__ldg(&brec[(size_t)g * 5 + 4]) << 32);
+        // the record {mother slot, father slot, baby slot, mother ID low, high}
+        const uint32_t rv = (lane < 5) ? __ldg(&brec[(size_t)g * 5 + (uint32_t)lane]) : 0u;
+        const uint32_t ms = __shfl_sync(FULL_MASK, rv, 0);
+        const uint32_t fs = __shfl_sync(FULL_MASK, rv, 1);
+        const uint32_t bs = __shfl_sync(FULL_MASK, rv, 2);
+        const uint64_t mid = (uint64_t)__shfl_sync(FULL_MASK, rv, 3) | ((uint64_t)__shfl_sync(FULL_MASK, rv, 4) << 32);
+        const uint64_t *gm = genome + (size_t)ms * gw;
+        const uint64_t *gf = genome + (size_t)fs * gw;
+        uint64_t *gb = genome + (size_t)bs * gw;
+        // both strands of both parents at the lane's blocks
+        uint64_t m0[2] = {0ull, 0ull}, m1[2] = {0ull, 0ull}, f0[2] = {0ull, 0ull}, f1[2] = {0ull, 0ull};
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int b = lane + 32 * h;
+            if (b < nblk) {
+                m0[h] = gm[b];
+                m1[h] = gm[nblk + b];
+                f0[h] = gf[b];
+                f1[h] = gf[nblk + b];
+            }
+        }
         const Draw4 d = run_block<false>(P, P.seed, step, (int64_t)mid, kStreamBirth + (uint32_t)lane);
         const int i1 = (int)(birth_draw(d, 1) >> 31);
         const int i2 = (int)(birth_draw(d, 2) >> 31);
@@ -2549,27 +2562,57 @@ k_genomes(const StepConst P, RunState *__restrict__ rs, uint64_t *__restrict__ g
             if (lane == 0) set_error(rs, kErrInternal, 6u);
             continue;
         }
-        const uint64_t *gm = genome + (size_t)ms * gw;
-        const uint64_t *gf = genome + (size_t)fs * gw;
-        uint64_t *gb = genome + (size_t)bs * gw;
-        for (int b0 = 0; b0 < nblk; b0 += 32) {
-            const int b = b0 + lane;
-            const int bb = b < nblk ? b : 0;
-            uint64_t w0 = crossed_word(d, kMom, nM, nbits, bb, gm, nblk, i1);
-            uint64_t w1 = crossed_word(d, kDad, nF, nbits, bb, gf, nblk, i2);
-            // BitGeneUtils::mutateNucs (genes/BitGeneUtils.cpp:57-75): flips at
-            // wrandi(0, 2 * genome size) over both strands of the newborn
-            for (int t = 0; t < nmut; t++) {
-                const uint32_t pos = (uint32_t)(((uint64_t)(2u * (uint32_t)P.genome_size) *
-                                                 (uint64_t)birth_draw(d, k + t)) >> 32);
-                const int w = (int)(pos >> 6);
-                const uint64_t bit = 1ull << (pos & 63u);
-                if (w == b) w0 ^= bit;
-                if (w == nblk + b) w1 ^= bit;
+        // the breaks of each parent: those in earlier blocks (their parity
+        // picks the strand) and those in the lane's own blocks (the mask)
+        BlockMask bmM[2], bmF[2];
+        int befM[2] = {0, 0}, befF[2] = {0, 0};
+        for (int t = 0; t < nM + nF; t++) {
+            const uint32_t pos = (uint32_t)(((uint64_t)nbits * (uint64_t)birth_draw(d, kMom + t)) >> 32);
+            const int blk = (int)(pos >> 6);
+            const bool mom = t < nM;
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int b = lane + 32 * h;
+                if (mom) {
+                    befM[h] += (blk < b) ? 1 : 0;
+                    if (blk == b) bmM[h].add(pos & 63u);
+                } else {
+                    befF[h] += (blk < b) ? 1 : 0;
+                    if (blk == b) bmF[h].add(pos & 63u);
+                }
             }
+        }
+        uint64_t w0[2], w1[2];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const uint64_t mm = bmM[h].value(), mf = bmF[h].value();
+            const bool cm = ((befM[h] & 1) ^ i1) != 0;   // mother: strand taken at the block's start
+            const bool cf = ((befF[h] & 1) ^ i2) != 0;
+            const uint64_t am = cm ? m1[h] : m0[h], bm = cm ? m0[h] : m1[h];
+            const uint64_t af = cf ? f1[h] : f0[h], bf = cf ? f0[h] : f1[h];
+            w0[h] = (mm & am) | (~mm & bm);
+            w1[h] = (mf & af) | (~mf & bf);
+        }
+        // BitGeneUtils::mutateNucs (genes/BitGeneUtils.cpp:57-75): flips at
+        // wrandi(0, 2 * genome size) over both strands of the newborn
+        for (int t = 0; t < nmut; t++) {
+            const uint32_t pos = (uint32_t)(((uint64_t)(2u * (uint32_t)P.genome_size) *
+                                             (uint64_t)birth_draw(d, k + t)) >> 32);
+            const int w = (int)(pos >> 6);
+            const uint64_t bit = 1ull << (pos & 63u);
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int b = lane + 32 * h;
+                if (w == b) w0[h] ^= bit;
+                if (w == nblk + b) w1[h] ^= bit;
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int b = lane + 32 * h;
             if (b < nblk) {
-                gb[b] = w0;
-                gb[nblk + b] = w1;
+                gb[b] = w0[h];
+                gb[nblk + b] = w1[h];
             }
         }
     }

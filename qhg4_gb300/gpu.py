@@ -40,7 +40,7 @@ EXPORTS = [
     "qhg_batch_set_shape", "qhg_batch_get_shape", "qhg_batch_stream", "qhg_batch_destroy",
     "qhg_batch_live_history", "qhg_batch_snapshot_async", "qhg_batch_snapshot_wait",
     "qhg_host_buffer_alloc", "qhg_host_buffer_free", "qhg_gpu_next_id", "qhg_gpu_set_next_id",
-    "qhg_gpu_test_stall_scan", "qhg_gpu_occupancy", "qhg_gpu_set_capacity", "qhg_gpu_set_move_weights",
+    "qhg_gpu_test_stall_scan", "qhg_gpu_occupancy", "qhg_gpu_set_capacity", "qhg_gpu_set_move_weights", "qhg_gpu_set_ice",
     "qhg_gpu_move_stats_enable", "qhg_gpu_move_stats", "qhg_gpu_set_move_stats", "qhg_gpu_set_occupancy",
 ]
 
@@ -137,6 +137,7 @@ def load_library(path: str = LIB_PATH):
         "qhg_gpu_occupancy": (I, [P, P]),
         "qhg_gpu_set_capacity": (I, [P, P]),
         "qhg_gpu_set_move_weights": (I, [P, P]),
+        "qhg_gpu_set_ice": (I, [P, P]),
         "qhg_gpu_move_stats_enable": (I, [P, ct.c_int32, P, P, ct.c_double, ct.c_int32]),
         "qhg_gpu_move_stats": (I, [P, P, P, P]),
         "qhg_gpu_set_move_stats": (I, [P, P, P, P]),
@@ -201,6 +202,7 @@ class GpuRun:
         # move weights set between steps, the MoveStats configuration
         self.capacity_K = None
         self.move_weights = None
+        self.ice = None
         self.move_stats_config = None
         nbr = np.ascontiguousarray(grid.nbr, dtype=np.int32)
         nnbr = np.ascontiguousarray(grid.nnbr, dtype=np.uint8)
@@ -272,6 +274,20 @@ class GpuRun:
             raise ValueError("weights need shape (cells, 7)")
         _check(_lib.qhg_gpu_set_move_weights(self.h, _p(w)))
         self.move_weights = w.copy()
+
+    def set_ice(self, ice) -> None:
+        """The Geography's ice flags per cell (None: no ice) from the next step
+        on: WeightedMove registers no move into an ice cell, and weights that
+        follow K give ice cells weight 0."""
+        if ice is None:
+            _check(_lib.qhg_gpu_set_ice(self.h, None))
+            self.ice = None
+            return
+        f = np.ascontiguousarray(np.asarray(ice) != 0, dtype=np.uint8)
+        if f.shape != (self.C,):
+            raise ValueError("one flag per cell")
+        _check(_lib.qhg_gpu_set_ice(self.h, _p(f)))
+        self.ice = f.copy()
 
     def move_stats_enable(self, mode: int, lon: np.ndarray, lat: np.ndarray, radius: float = 1.0,
                           cartesian: bool = False) -> None:

@@ -63,6 +63,7 @@
 #include "LBController.h"
 #include "LayerArrBuf.h"
 #include "SCellGrid.h"
+#include "Geography.h"
 #include "qhg_gpu.h"
 
 // An action of a GPU population as the configuration sees it: it carries the
@@ -282,6 +283,14 @@ public:
             iResult += m_vHostOrder[i]->initialize(fTime);
         }
         if ((iResult == 0) && m_bEnvDirty) {
+            // the Geography's ice: WeightedMove registers no move into an ice
+            // cell (actions/WeightedMove.cpp:91)
+            const Geography *pGeo = this->m_pCG->m_pGeography;
+            if ((pGeo != NULL) && (pGeo->m_abIce != NULL)) {
+                std::vector<uint8_t> vIce((size_t)this->m_pCG->m_iNumCells);
+                for (size_t c = 0; c < vIce.size(); c++) vIce[c] = pGeo->m_abIce[c] ? 1 : 0;
+                if (qhg_gpu_set_ice(m_pRun, vIce.data()) != QHG_OK) iResult = -1;
+            }
             if ((m_adEnvW != NULL) && (qhg_gpu_set_move_weights(m_pRun, m_adEnvW) != QHG_OK)) iResult = -1;
             if ((m_adEnvK != NULL) && (qhg_gpu_set_capacity(m_pRun, m_adEnvK) != QHG_OK)) iResult = -1;
             m_bEnvDirty = false;

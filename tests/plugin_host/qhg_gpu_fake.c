@@ -29,6 +29,7 @@ int qo_get_agents(const qo_run *r, int64_t *id, int32_t *cell, float *birth, flo
                   uint8_t *gender, uint8_t *state, uint64_t *genome);
 int qo_get_counts(const qo_run *r, uint32_t *counts);
 int qo_set_capacity(qo_run *r, const double *K);
+int qo_set_ice(qo_run *r, const uint8_t *ice);
 int qo_set_move_weights(qo_run *r, const double *W);
 void qo_destroy(qo_run *r);
 
@@ -105,6 +106,12 @@ int qhg_gpu_set_capacity(qhg_run *r, const double *K) {
 int qhg_gpu_set_move_weights(qhg_run *r, const double *W) {
     if (r == NULL || r->o == NULL) return QHG_ERR_STATE;
     return qo_set_move_weights(r->o, W) == 0 ? QHG_OK : QHG_ERR_ARG;
+}
+
+
+int qhg_gpu_set_ice(qhg_run *r, const uint8_t *ice) {
+    if (r == NULL || r->o == NULL) return QHG_ERR_STATE;
+    return qo_set_ice(r->o, ice) == 0 ? QHG_OK : QHG_ERR_ARG;
 }
 
 int qhg_gpu_next_id(qhg_run *r, int64_t *next_id) {

@@ -1,5 +1,5 @@
 """Environment updates between steps (qhg_gpu_set_capacity,
-qhg_gpu_set_move_weights) against the oracle, bit for bit.
+qhg_gpu_set_move_weights, qhg_gpu_set_ice) against the oracle, bit for bit.
 
 FlatExpPop (populations/FlatExpPop.cpp:43-56) takes VerhulstVarK's K from
 NPPCapacity and WeightedMove's cumulative weights from a MultiEvaluator;
@@ -27,11 +27,14 @@ def env_case(form):
     return grid, make_agents(grid, 35 * grid.num_cells, seed=23, age_max=70.0)
 
 
-def run_with_updates(grid, agents, acts, steps, seed, weights=None, updates=()):
-    """updates: (step, kind, array) with kind "K" or "W", applied before that step."""
+def run_with_updates(grid, agents, acts, steps, seed, weights=None, updates=(), ice=None):
+    """updates: (step, kind, array) with kind "K", "W" or "ice", applied before that step."""
     o = port.OracleRun(grid, acts, seed)
     g = GpuRun(grid, acts, seed, log_births=True)
-    if weights is not None:       # before the upload
+    if ice is not None:           # before the upload
+        o.set_ice(ice)
+        g.set_ice(ice)
+    if weights is not None:
         o.set_move_weights(weights)
         g.set_move_weights(weights)
     o.load(agents)
@@ -48,6 +51,9 @@ def run_with_updates(grid, agents, acts, steps, seed, weights=None, updates=()):
         elif kind == "W":
             o.set_move_weights(arr)
             g.set_move_weights(arr)
+        elif kind == "ice":
+            o.set_ice(arr)
+            g.set_ice(arr)
     ost = np.concatenate(ost)
     d = table_diff(o.agents(), g.agents())
     assert d is None, d
@@ -106,3 +112,23 @@ def test_bad_move_weights_rejected(gpu_lib):
         g.set_move_weights(W)
     g.step(2)               # the run is unaffected
     assert g.num_agents() > 0
+
+
+@pytest.mark.parametrize("form", ["sparse", "dense"])
+@pytest.mark.parametrize("weights", [False, True])
+def test_ice_refuses_weighted_moves(gpu_lib, form, weights):
+    """The Geography's ice (actions/WeightedMove.cpp:91): no move into an ice
+    cell, weights from K give ice cells weight 0; ice set before the upload,
+    changed after 5 steps and removed after 10 (then K changes, and weights
+    that follow K follow the ice as well)."""
+    grid, agents = env_case(form)
+    rng = np.random.default_rng(341)
+    acts = config2_actions(b0=0.3, d0=0.03, move_p=0.4)
+    C = grid.num_cells
+    ice0 = (rng.random(C) < 0.3).astype(np.uint8)
+    ice1 = (rng.random(C) < 0.15).astype(np.uint8)
+    W = move_weights(grid, 342) if weights else None
+    st = run_with_updates(grid, agents, acts, 18, 343, weights=W, ice=ice0,
+                          updates=[(5, "ice", ice1), (10, "ice", None), (13, "ice", ice0),
+                                   (15, "K", grid.K * rng.uniform(0.5, 1.5, C))])
+    assert st[:, 3].sum() > 0

@@ -228,3 +228,38 @@ def test_port_oracle_geography_kills_against_reference_build(tmp_path):
     assert ref.draw_errors == 0
     d = table_diff(r.agents(), ref.agents)
     assert d is None, d
+
+
+@pytest.mark.skipif(not os.path.exists(ref_program("philox")), reason="reference build not present")
+@pytest.mark.parametrize("weights", [False, True])
+def test_port_oracle_ice_refusal_against_reference_build(tmp_path, weights):
+    """WeightedMove does not register a move into an ice cell of the grid's
+    Geography (actions/WeightedMove.cpp:91); its draws are taken all the
+    same.  A quarter of the cells is ice, with the weights from K and with
+    given weights (rows of equal weights draw with wrandi)."""
+    from helpers import move_weights
+    from qhg4_gb300.spec import config2_actions
+    from qhg4_gb300.workload import make_agents, terrain_grid
+    grid = terrain_grid(8, seed=960)
+    agents = make_agents(grid, 8000, seed=961, age_max=70.0, proportional_to_K=True)
+    acts = config2_actions(b0=0.35, d0=0.03, move_p=0.4)
+    ice = (np.random.default_rng(962).random(grid.num_cells) < 0.25).astype(np.uint8)
+    W = move_weights(grid, 963) if weights else None
+    ref = run_reference("philox", str(tmp_path), grid, agents, acts, 14, 964, threads=2, ice=ice, weights=W)
+    r = port.OracleRun(grid, acts, 964)
+    r.set_ice(ice)
+    if W is not None:
+        r.set_move_weights(W)
+    r.load(agents)
+    st = r.step(14)
+    assert ref.draw_errors == 0
+    d = table_diff(r.agents(), ref.agents)
+    assert d is None, d
+    assert np.array_equal(st, ref.stats)
+    # the ice made a difference: without it the oracle registers more moves
+    r2 = port.OracleRun(grid, acts, 964)
+    if W is not None:
+        r2.set_move_weights(W)
+    r2.load(agents)
+    st2 = r2.step(14)
+    assert st2[:, 3].sum() > st[:, 3].sum()
