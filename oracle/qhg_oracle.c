@@ -88,7 +88,12 @@ typedef struct {
     int32_t *cell;
     float *birth, *age, *lastb;
     uint8_t *gender, *state;
-    uint64_t *genome;   /* [cap * 2 * num_blocks] */
+    int32_t *gslot;     /* genome slot of each agent row */
+    uint64_t *genome;   /* genome slab [gcap slots * 2 * num_blocks]; slots, not rows, hold genomes,
+                         * as the reference's LayerArrBuf does, so rows move without their genomes */
+    int64_t gcap, ghwm; /* slots allocated, slots ever used */
+    int32_t *gfree;     /* free slots (of agents that died in earlier steps) */
+    int64_t nfree;
     int64_t next_id;
     /* per cell */
     uint32_t *count;
@@ -420,10 +425,18 @@ static void reserve_agents(qo_run *r, int64_t need) {
     r->lastb = (float *)realloc(r->lastb, cap * sizeof(float));
     r->gender = (uint8_t *)realloc(r->gender, cap);
     r->state = (uint8_t *)realloc(r->state, cap);
-    if (r->num_blocks > 0) {
-        r->genome = (uint64_t *)realloc(r->genome, (size_t)cap * 2 * r->num_blocks * sizeof(uint64_t));
-    }
+    if (r->num_blocks > 0) r->gslot = (int32_t *)realloc(r->gslot, cap * sizeof(int32_t));
     r->cap = cap;
+}
+
+/* room for `need` genome slots in the slab */
+static void reserve_slots(qo_run *r, int64_t need) {
+    if (need <= r->gcap) return;
+    int64_t cap = r->gcap ? r->gcap : 1024;
+    while (cap < need) cap *= 2;
+    r->genome = (uint64_t *)realloc(r->genome, (size_t)cap * 2 * r->num_blocks * sizeof(uint64_t));
+    r->gfree = (int32_t *)realloc(r->gfree, cap * sizeof(int32_t));
+    r->gcap = cap;
 }
 
 static void recount(qo_run *r) {
@@ -452,6 +465,9 @@ int qo_load(qo_run *r, int64_t N, const int64_t *id, const int32_t *cell, const 
     }
     free(tmp);
     reserve_agents(r, N);
+    if (r->num_blocks > 0) reserve_slots(r, N);
+    r->ghwm = 0;
+    r->nfree = 0;
     r->n = 0;
     int64_t maxid = -1;
     for (int64_t j = 0; j < N; j++) {
@@ -462,12 +478,14 @@ int qo_load(qo_run *r, int64_t N, const int64_t *id, const int32_t *cell, const 
         r->id[k] = id[i]; r->cell[k] = cell[i]; r->birth[k] = birth[i]; r->age[k] = age[i];
         r->lastb[k] = lastb[i]; r->gender[k] = gender[i]; r->state[k] = state[i];
         if (r->num_blocks > 0) {
+            r->gslot[k] = (int32_t)k;
             memcpy(r->genome + (size_t)k * 2 * r->num_blocks, genome + (size_t)i * 2 * r->num_blocks,
                    2 * r->num_blocks * sizeof(uint64_t));
         }
         if (id[i] > maxid) maxid = id[i];
     }
     free(ord);
+    r->ghwm = r->n;
     r->next_id = maxid + 1;
     r->step = first_step;
     recount(r);
@@ -727,9 +745,9 @@ int qo_step(qo_run *r, int nsteps, uint64_t *stats_out) {
         float *lastb2 = (float *)malloc((nnew > 0 ? nnew : 1) * sizeof(float));
         uint8_t *gender2 = (uint8_t *)malloc(nnew > 0 ? nnew : 1);
         uint8_t *state2 = (uint8_t *)malloc(nnew > 0 ? nnew : 1);
-        uint64_t *gen2 = NULL;
+        int32_t *gslot2 = NULL;
         int gw = 2 * r->num_blocks;
-        if (gw > 0) gen2 = (uint64_t *)malloc((size_t)(nnew > 0 ? nnew : 1) * gw * sizeof(uint64_t));
+        if (gw > 0) gslot2 = (int32_t *)malloc((size_t)(nnew > 0 ? nnew : 1) * sizeof(int32_t));
         int64_t k = 0;
         for (int64_t i = 0; i < n; i++) {
             if (out[i].dead) continue;
@@ -737,8 +755,23 @@ int qo_step(qo_run *r, int nsteps, uint64_t *stats_out) {
             cell2[k] = (out[i].move_to >= 0) ? out[i].move_to : r->cell[i];
             birth2[k] = r->birth[i]; age2[k] = r->age[i]; lastb2[k] = r->lastb[i];
             gender2[k] = r->gender[i]; state2[k] = r->state[i];
-            if (gw > 0) memcpy(gen2 + (size_t)k * gw, r->genome + (size_t)i * gw, gw * sizeof(uint64_t));
+            if (gw > 0) gslot2[k] = r->gslot[i];
             k++;
+        }
+        /* newborns' genome slots: slots freed by earlier steps' deaths, then
+         * unused ones; this step's deaths free theirs after the births, so a
+         * newborn never takes a parent's slot of the same step */
+        if (gw > 0) {
+            reserve_slots(r, r->ghwm + nb);
+            for (int64_t b = 0; b < nb; b++) {
+                gslot2[nsurv + b] = (b < r->nfree) ? r->gfree[r->nfree - 1 - b] : (int32_t)(r->ghwm + (b - r->nfree));
+            }
+            if (nb > r->nfree) {
+                r->ghwm += nb - r->nfree;
+                r->nfree = 0;
+            } else {
+                r->nfree -= nb;
+            }
         }
         if (r->log_births) {
             if (r->blog_n + nb > r->blog_cap) {
@@ -764,7 +797,8 @@ int qo_step(qo_run *r, int nsteps, uint64_t *stats_out) {
             gender2[kk] = g;
             state2[kk] = (g == 0) ? LS_FERTILE : LS_ALIVE;
             if (gw > 0) {
-                make_genome(r, gen2 + (size_t)kk * gw, r->genome + (size_t)m * gw, r->genome + (size_t)f * gw, &s);
+                make_genome(r, r->genome + (size_t)gslot2[kk] * gw, r->genome + (size_t)r->gslot[m] * gw,
+                            r->genome + (size_t)r->gslot[f] * gw, &s);
             }
             if (r->log_births) {
                 r->blog[(r->blog_n + b) * 3 + 0] = r->next_id + b;
@@ -774,12 +808,17 @@ int qo_step(qo_run *r, int nsteps, uint64_t *stats_out) {
         }
         if (r->log_births) r->blog_n += nb;
         r->next_id += nb;
+        if (gw > 0) {
+            for (int64_t i = 0; i < n; i++) {
+                if (out[i].dead) r->gfree[r->nfree++] = r->gslot[i];
+            }
+        }
         free(mom);
         free(out);
         free(r->id); free(r->cell); free(r->birth); free(r->age); free(r->lastb);
-        free(r->gender); free(r->state); free(r->genome);
+        free(r->gender); free(r->state); free(r->gslot);
         r->id = id2; r->cell = cell2; r->birth = birth2; r->age = age2; r->lastb = lastb2;
-        r->gender = gender2; r->state = state2; r->genome = gen2;
+        r->gender = gender2; r->state = state2; r->gslot = gslot2;
         r->n = nnew;
         r->cap = nnew > 0 ? nnew : 1;
         recount(r);
@@ -811,7 +850,11 @@ int qo_get_agents(const qo_run *r, int64_t *id, int32_t *cell, float *birth, flo
     memcpy(gender, r->gender, n);
     memcpy(state, r->state, n);
     if (genome != NULL && r->num_blocks > 0) {
-        memcpy(genome, r->genome, (size_t)n * 2 * r->num_blocks * sizeof(uint64_t));
+        const int gw = 2 * r->num_blocks;
+#pragma omp parallel for schedule(static)
+        for (int64_t k = 0; k < n; k++) {
+            memcpy(genome + (size_t)k * gw, r->genome + (size_t)r->gslot[k] * gw, gw * sizeof(uint64_t));
+        }
     }
     return 0;
 }
@@ -929,6 +972,6 @@ void qo_destroy(qo_run *r) {
     free(r->ms_lon); free(r->ms_lat); free(r->ms_hops); free(r->ms_thops); free(r->ms_dist);
     free(r->ms_time); free(r->ms_tdist); free(r->ms_ttime); free(r->ms_changed);
     free(r->id); free(r->cell); free(r->birth); free(r->age); free(r->lastb); free(r->gender);
-    free(r->state); free(r->genome); free(r->bino); free(r->blog); free(r->stats);
+    free(r->state); free(r->genome); free(r->gslot); free(r->gfree); free(r->bino); free(r->blog); free(r->stats);
     free(r);
 }
