@@ -171,6 +171,14 @@ int qhg_gpu_download(qhg_run *run, qhg_agents_soa *out, int64_t cap, int64_t *n)
 int qhg_gpu_counts(qhg_run *run, uint32_t *cell_counts);
 /* statistics of the last `nsteps` steps (nsteps <= 1024) */
 int qhg_gpu_stats(qhg_run *run, int32_t nsteps, qhg_step_stats *out);
+/* Queues on the run's stream a copy of the statistics of the step launched
+ * last into *out and returns without waiting (the per-step counts that
+ * PopLooper reads from the population after each step,
+ * core/PopLooper.cpp:166-200; *out should be page-locked host memory, see
+ * qhg_host_buffer_alloc).  The values are there once qhg_gpu_sync (or any
+ * call that waits for the run) has returned; a step that failed leaves
+ * undefined values and its error is reported by that call. */
+int qhg_gpu_stats_async(qhg_run *run, qhg_step_stats *out);
 /* Occupation history of the cells (QHG_FLAG_TRACK_OCCUPANCY): per cell the
  * first step whose table holds an agent there (the uploaded table counts as
  * its step), -1 if none yet; C entries.  Replaces OccTracker::updateCounts

@@ -25,6 +25,10 @@ extern "C" int qhg_match_program(const int32_t *types, int n);
 extern "C" int qhg_launch_occupancy(const qhg::RunState *rs, const uint32_t *nonempty, int32_t *occ, int grid,
                                     cudaStream_t stream);
 extern "C" uint32_t qhg_program_window(int p, int a);
+extern "C" int qhg_launch_download_cols(const uint32_t *nonempty, const uint32_t *ne_start, uint32_t nne, uint32_t n,
+                                        const uint8_t *meta, const float *birth, float t_prev, int derived,
+                                        int32_t *cell_out, uint8_t *gender_out, uint8_t *state_out, float *age,
+                                        cudaStream_t stream);
 extern "C" int qhg_launch_gather_genomes(const int32_t *gslot, const uint64_t *genome, uint32_t n, int words,
                                          uint32_t slots, uint64_t *out, cudaStream_t stream);
 extern "C" int qhg_launch_upload(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
@@ -78,6 +82,7 @@ struct qhg_run {
     std::vector<uint8_t> h_nnbr;
     bool w_given = false;        // move weights given (qhg_gpu_set_move_weights), not from K
     std::vector<uint8_t> h_ice;  // the Geography's ice flags per cell (qhg_gpu_set_ice), empty: none
+    int64_t launched = 0;        // steps launched since the run state was last read back
     // agents (ping-pong)
     uint32_t cap = 0;
     int64_t *d_id[2] = {nullptr, nullptr};
@@ -494,6 +499,9 @@ int qhg_host_move_tables(int C, const uint8_t *nnbr, const double *W, std::vecto
             run = std::max(run, u);
             wthr[(size_t)c * 6 + j] = run;
         }
+        // slots without a neighbour: 2^32, a threshold no draw reaches (the
+        // device may count over all six slots)
+        for (int j = nn; j < 6; j++) wthr[(size_t)c * 6 + j] = 4294967296ull;
     }
     return 0;
 }
@@ -749,6 +757,7 @@ extern "C" int qhg_gpu_upload_agents(qhg_run *r, const qhg_agents_soa *a, int64_
     if (le != 0) return fail(QHG_ERR_CUDA, std::string("upload: ") + cudaGetErrorString((cudaError_t)le));
     CUDA_TRY(cudaMemcpyAsync(r->h_rs, r->d_rs, sizeof(RunState), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
+    r->launched = 0;
     RunState *h = r->h_rs;
     if (h->error != 0u) {
         const uint32_t code = h->error;
@@ -847,6 +856,7 @@ extern "C" int qhg_gpu_step(qhg_run *r, int32_t nsteps) {
         }
         CUDA_TRY(cudaGraphLaunch(r->graph[r->cur], r->stream));
         r->cur ^= 1;
+        r->launched++;
     }
     return QHG_OK;
 }
@@ -885,6 +895,7 @@ extern "C" int qhg_gpu_step_profiled(qhg_run *r, int32_t nsteps, float *kernel_m
             kernel_ms[s * 4 + k] = ms;
         }
         r->cur ^= 1;
+        r->launched++;
     }
     return QHG_OK;
 }
@@ -894,6 +905,7 @@ extern "C" int qhg_gpu_step_profiled(qhg_run *r, int32_t nsteps, float *kernel_m
 static int pull_state(qhg_run *r) {
     CUDA_TRY(cudaMemcpyAsync(r->h_rs, r->d_rs, sizeof(RunState), cudaMemcpyDeviceToHost, r->stream));
     CUDA_TRY(cudaStreamSynchronize(r->stream));
+    r->launched = 0;
     r->cur = (int)((uint32_t)(r->h_rs->step - r->upload_step) & 1u);
     if (r->h_rs->error != 0u) {
         const uint32_t code = r->h_rs->error, info = r->h_rs->error_info;
@@ -1206,23 +1218,30 @@ extern "C" int qhg_gpu_download(qhg_run *r, qhg_agents_soa *o, int64_t cap, int6
     if (cap < N) return fail(QHG_ERR_ARG, "output arrays too small");
     const int cur = r->cur;
     const uint32_t nne = r->h_rs->n_nonempty;
-    std::vector<uint32_t> ne(nne), nes((size_t)nne + 1);
-    std::vector<uint8_t> meta((size_t)N);
-    if (nne > 0) CUDA_TRY(cudaMemcpy(ne.data(), r->d_ne[cur], nne * sizeof(uint32_t), cudaMemcpyDeviceToHost));
-    CUDA_TRY(cudaMemcpy(nes.data(), r->d_nes[cur], (nne + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost));
     if (N > 0) {
-        CUDA_TRY(cudaMemcpy(o->id, r->d_id[cur], N * sizeof(int64_t), cudaMemcpyDeviceToHost));
-        CUDA_TRY(cudaMemcpy(o->birth, r->d_birth[cur], N * sizeof(float), cudaMemcpyDeviceToHost));
-        CUDA_TRY(cudaMemcpy(o->age, r->d_age[cur], N * sizeof(float), cudaMemcpyDeviceToHost));
-        CUDA_TRY(cudaMemcpy(o->last_birth, r->d_lastb[cur], N * sizeof(float), cudaMemcpyDeviceToHost));
-        CUDA_TRY(cudaMemcpy(meta.data(), r->d_meta[cur], N, cudaMemcpyDeviceToHost));
-    }
-    for (uint32_t k = 0; k < nne; k++) {
-        for (uint32_t i = nes[k]; i < nes[(size_t)k + 1]; i++) o->cell[i] = (int32_t)ne[k];
-    }
-    for (int64_t i = 0; i < N; i++) {
-        o->gender[i] = meta[(size_t)i] & kMetaGender;
-        o->state[i] = (meta[(size_t)i] & kMetaFertile) ? QHG_LS_FERTILE : QHG_LS_ALIVE;
+        // per-row columns built on the device, in the step's scratch arrays
+        // (the outcome words hold the cells, the father rows gender and state;
+        // the next step's action kernel writes both before reading them); the
+        // table's ages, where derived (t - birth of the step that made the
+        // table, GetOld's fp32 arithmetic, actions/GetOld.cpp:44), into its
+        // own age column
+        int32_t *d_cell = reinterpret_cast<int32_t *>(r->d_outc);
+        uint8_t *d_gender = reinterpret_cast<uint8_t *>(r->d_father);
+        uint8_t *d_state = d_gender + r->cap;
+        const int le = qhg_launch_download_cols(r->d_ne[cur], r->d_nes[cur], nne, (uint32_t)N, r->d_meta[cur],
+                                                r->d_birth[cur], (float)(r->h_rs->step - 1),
+                                                r->h_rs->age_derived ? 1 : 0, d_cell, d_gender, d_state,
+                                                r->d_age[cur], r->stream);
+        if (le != 0) return fail(QHG_ERR_CUDA, std::string("launch: ") + cudaGetErrorString((cudaError_t)le));
+        cudaStream_t st = r->stream;
+        CUDA_TRY(cudaMemcpyAsync(o->id, r->d_id[cur], N * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(o->cell, d_cell, N * sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(o->birth, r->d_birth[cur], N * sizeof(float), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(o->age, r->d_age[cur], N * sizeof(float), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(o->last_birth, r->d_lastb[cur], N * sizeof(float), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(o->gender, d_gender, N, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaMemcpyAsync(o->state, d_state, N, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
     }
     if (r->P.genome_words > 0 && o->genome != nullptr && N > 0) {
         const size_t gw = (size_t)r->P.genome_words;
@@ -1280,6 +1299,18 @@ extern "C" int qhg_gpu_stats(qhg_run *r, int32_t nsteps, qhg_step_stats *out) {
         const unsigned long long *v = r->h_rs->stats[s % kStatsRing];
         out[k].live = v[0]; out[k].births = v[1]; out[k].deaths = v[2]; out[k].moves = v[3];
     }
+    return QHG_OK;
+}
+
+extern "C" int qhg_gpu_stats_async(qhg_run *r, qhg_step_stats *out) {
+    if (r == nullptr || out == nullptr) return fail(QHG_ERR_ARG, "null argument");
+    if (!r->agents_ok || r->launched == 0) return fail(QHG_ERR_STATE, "no step launched since the last sync");
+    CUDA_TRY(cudaSetDevice(r->desc.device));
+    const uint32_t s = (uint32_t)(r->h_rs->step + r->launched - 1);
+    const char *src = reinterpret_cast<const char *>(r->d_rs) + offsetof(RunState, stats) +
+                      (size_t)(s % kStatsRing) * 4 * sizeof(unsigned long long);
+    static_assert(sizeof(qhg_step_stats) == 4 * sizeof(unsigned long long), "stats layout");
+    CUDA_TRY(cudaMemcpyAsync(out, src, sizeof(qhg_step_stats), cudaMemcpyDeviceToHost, r->stream));
     return QHG_OK;
 }
 

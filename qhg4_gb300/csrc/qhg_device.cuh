@@ -71,6 +71,9 @@ constexpr int kBirthDraws = 128;
 constexpr int kMaxFixedCrossover = 30;   // 3 + 2*30 + 1 + 64 draws fit kBirthDraws
 constexpr int kCrossoverPoisson1 = -100;
 
+// life states of the downloaded table (QHG_LS_ALIVE, QHG_LS_FERTILE)
+constexpr uint8_t QHG_LS_ALIVE_DEV = 1u, QHG_LS_FERTILE_DEV = 5u;
+
 // agent meta byte: bit 0 gender, bit 1 fertile (life state 5, else 1)
 constexpr uint8_t kMetaGender = 1u;
 constexpr uint8_t kMetaFertile = 2u;
@@ -172,6 +175,10 @@ struct RunState {
     uint32_t form_next;      // the same for the table the step writes (set by its commit)
     uint32_t max_cell;       // largest cell of the next table when above kMaxCellWarp (cell scan)
     uint32_t stall_tile;     // tests of the bounded waits: tile + 1 whose scan status is withheld once
+    // single runs whose actions set every survivor's age to t - birth
+    // (GetOld or OldAgeDeath): once a step has run, the table's age column is
+    // not kept up to date; its ages are (float)(step - 1) - birth
+    uint32_t age_derived;
     // statistics ring: [step % kStatsRing][live, births, deaths, moves]
     unsigned long long stats[kStatsRing][4];
 };

@@ -400,7 +400,7 @@ constexpr int kStOad = 9;              // bits 9-10, OldAgeDeath: 0 survives, 1 
 template <int PROG, bool BATCH>
 __device__ __forceinline__ uint32_t agent_state(const StepConst &P, const BatchRun *R, int32_t step, float fT,
                                                 int64_t id, uint8_t m8, float fb, float fa, float fl,
-                                                const CellView &cv, const uint64_t *wt) {
+                                                const CellView &cv, const uint32_t *wt32, uint32_t wnever) {
     constexpr int iF = prog_index(PROG, kFertility, kFertility);
     constexpr int iV = prog_index(PROG, kVerhulst, kVerhulstVarK);
     constexpr int iM = prog_index(PROG, kRandomMove, kWeightedMove);
@@ -448,8 +448,15 @@ __device__ __forceinline__ uint32_t agent_state(const StepConst &P, const BatchR
             if (!kWeighted || (cv.wf & 1u)) {
                 d = (int)(((uint64_t)(cv.nn + 1u) * (uint64_t)u2) >> 32);
             } else {
-                d = 0;
-                for (int q = 0; q < (int)cv.nn; q++) d += (wt[q] <= (uint64_t)u2) ? 1 : 0;
+                // the number of slots whose threshold (a running maximum, 2^32
+                // past the neighbours) is <= u2: in 32 bits every slot counts
+                // correctly except a 2^32 threshold against u2 = 0xffffffff,
+                // which the never mask takes back out
+                const uint4 wa = *reinterpret_cast<const uint4 *>(wt32);
+                const uint2 wb = *reinterpret_cast<const uint2 *>(wt32 + 4);
+                d = (wa.x <= u2 ? 1 : 0) + (wa.y <= u2 ? 1 : 0) + (wa.z <= u2 ? 1 : 0) + (wa.w <= u2 ? 1 : 0) +
+                    (wb.x <= u2 ? 1 : 0) + (wb.y <= u2 ? 1 : 0);
+                if (u2 == 0xffffffffu) d -= __popc(wnever);
             }
             // WeightedMove registers no move into an ice cell (actions/WeightedMove.cpp:91)
             if (d > 0 && (((kWeighted ? cv.wv : cv.vm) >> (d - 1)) & 1u)) st |= (uint32_t)d;
@@ -487,6 +494,9 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
     const int lane = tid & 31;
     const int32_t step = rs->step;
     const float fT = (float)step;
+    // the table's ages: derived from birth times once a step of a single run has run
+    const bool derived = !BATCH && rs->age_derived != 0u;
+    const float fTprev = (float)(step - 1);
     const uint32_t N = rs->n_agents;
     const uint32_t ntiles = (N + kTileAgents - 1) / kTileAgents;
     uint32_t cnt_births = 0, cnt_deaths = 0, cnt_moves = 0;
@@ -531,7 +541,7 @@ k_actions(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                 pid[j] = id[a0 + i];
                 pm[j] = meta[a0 + i];
                 pb[j] = birth[a0 + i];
-                pa[j] = P.reads_age ? age[a0 + i] : 0.0f;
+                pa[j] = P.reads_age ? (derived ? __fsub_rn(fTprev, pb[j]) : age[a0 + i]) : 0.0f;
                 pl[j] = lastb[a0 + i];
             }
         }
@@ -1241,6 +1251,7 @@ __device__ __forceinline__ void commit_step(const StepConst &P, const BatchBuffe
             rs->dead_count = 0u;
             rs->genome_step = (int32_t)step;
         }
+        if (!BATCH && P.age_from_birth) rs->age_derived = 1u;
         rs->step = (int32_t)(step + 1u);
         __threadfence();
     }
@@ -1455,7 +1466,7 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                 id2[dst] = pid[j];
                 birth2[dst] = fb;
                 lastb2[dst] = pl[j];
-                age2[dst] = P.age_from_birth ? __fsub_rn(BATCH ? S.cft[lc] : fT, fb) : pa[j];
+                if (BATCH || !P.age_from_birth) age2[dst] = P.age_from_birth ? __fsub_rn(S.cft[lc], fb) : pa[j];
                 meta2[dst] = (uint8_t)(((code & kOutGender) ? kMetaGender : 0) |
                                        ((code & kOutFertile) ? kMetaFertile : 0));
                 if (genetics) gslot2[dst] = pg[j];
@@ -1496,7 +1507,7 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             id2[dst] = baby;
             birth2[dst] = ft;
             lastb2[dst] = 0.0f;
-            age2[dst] = 0.0f;
+            if (BATCH || !P.age_from_birth) age2[dst] = 0.0f;
             meta2[dst] = (uint8_t)(g ? kMetaGender : kMetaFertile);
             if (genetics) {
                 const uint32_t gr = S.bid[lc] + rk;   // birth rank of the step
@@ -1550,9 +1561,13 @@ struct CellWarpSmem {
     uint16_t pick[kMaxCellWarp];     // pick values of a cell's smaller side (ID order), from the cell's first row
     uint16_t st[kMaxCellWarp];       // per row: state before the pairing (agent_state), then the outcome byte
     uint32_t odie[kMaxCellWarp / 32];  // OldAgeDeath decided in advance: bit per row, set = dies
-    uint32_t oinw[kMaxCellWarp / 32];  // rows inside the OldAgeDeath age window, bit per row
+    uint16_t oq[kMaxCellWarp];       // rows inside the OldAgeDeath age window, in a dense queue
     uint32_t cnt[kGroupCells][8];    // class counts: [0] stay, [1..6] movers per neighbour slot
-    uint64_t wt[kGroupCells][6];     // WeightedMove thresholds of each cell
+    // WeightedMove thresholds of each cell (slots 0-5) as 32-bit values: a
+    // threshold of 2^32 (no draw reaches it) is kept as 0xffffffff and its
+    // slot marked in wnever (see agent_state)
+    __align__(16) uint32_t wt32[kGroupCells][8];
+    uint32_t wnever[kGroupCells];
     CellView cv[kGroupCells];        // Verhulst thresholds and move word of each cell
     uint32_t run[kGroupCells];       // batches: run of each cell
 };
@@ -1585,6 +1600,9 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
     const uint32_t lt = lanemask_lt();
     const int32_t step = rs->step;
     const float fT = (float)step;
+    // the table's ages: derived from birth times once a step of a single run has run
+    const bool derived = !BATCH && rs->age_derived != 0u;
+    const float fTprev = (float)(step - 1);
     const uint32_t nne = rs->n_nonempty;
     uint32_t cnt_births = 0, cnt_deaths = 0, cnt_moves = 0;
     // units of work: pairs of adjacent non-empty cells (2u, 2u + 1), taken by
@@ -1626,9 +1644,14 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
             // thresholds (lane 8 lc + q holds slot q of cell lc)
             {
                 const int lc = lane >> 3, q = lane & 7;
+                bool never = false;
                 if (lc < nc) {
                     const uint32_t c = nonempty[r0 + (uint32_t)lc];
-                    if (P.has_wmove && q < 6) W.wt[lc][q] = wthr[(size_t)c * 6 + q];
+                    if (P.has_wmove) {
+                        const uint64_t w = (q < 6) ? wthr[(size_t)c * 6 + q] : (1ull << 32);
+                        never = (w >> 32) != 0ull;
+                        W.wt32[lc][q] = never ? 0xffffffffu : (uint32_t)w;
+                    }
                     if (q == 6) {
                         ulonglong2 v = make_ulonglong2(0ull, 0ull);
                         uint32_t cm = 0u;
@@ -1651,6 +1674,8 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                         W.cnt[lc][4] = W.cnt[lc][5] = W.cnt[lc][6] = W.cnt[lc][7] = 0u;
                     }
                 }
+                const uint32_t nv = __ballot_sync(FULL_MASK, never && q < 6);
+                if (lane < kGroupCells) W.wnever[lane] = (nv >> (8 * lane)) & 63u;
             }
             __syncwarp();
             // a run that leaves the batch drops its agents (they take no part in pairing)
@@ -1683,7 +1708,7 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                         }
                         if (kOnePass || kEarlyOad) fb = birth[g];
                         if (kOnePass) {
-                            if (P.reads_age) fa = age[g];
+                            if (P.reads_age) fa = derived ? __fsub_rn(fTprev, fb) : age[g];
                             fl = lastb[g];
                         }
                     }
@@ -1693,7 +1718,8 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                     uint32_t stt = 0u;
                     if (kOnePass && kp) {
                         const BatchRun *R = BATCH ? BB.runs + W.run[lc] : nullptr;
-                        stt = agent_state<PROG, BATCH>(P, R, step, fT, xid, m8, fb, fa, fl, W.cv[lc], W.wt[lc]);
+                        stt = agent_state<PROG, BATCH>(P, R, step, fT, xid, m8, fb, fa, fl, W.cv[lc], W.wt32[lc],
+                                                       W.wnever[lc]);
                         W.st[row] = (uint16_t)stt;
                     }
                     if (P.has_pair && valid) W.mate[row] = -1;
@@ -1729,11 +1755,9 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                             }
                         }
                         const uint32_t qm = __ballot_sync(FULL_MASK, inw);
+                        if (inw) W.oq[nq + __popc(qm & lt)] = (uint16_t)row;
                         nq += __popc(qm);
-                        if (lane == 0) {
-                            W.oinw[b >> 5] = qm;
-                            W.odie[b >> 5] = 0u;
-                        }
+                        if (lane == 0) W.odie[b >> 5] = 0u;
                     }
                 }
                 __syncwarp();
@@ -1797,14 +1821,8 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                         x = wide ? id[s + W.frow[pos]] : (int64_t)W.fk[pos];
                         blk = kStreamPair;
                     } else {
-                        // the (t - np)-th marked row: find its chunk, then its bit
-                        int k = t - np, ch = 0;
-                        uint32_t cmsk = W.oinw[0];
-                        while (k >= __popc(cmsk)) {
-                            k -= __popc(cmsk);
-                            cmsk = W.oinw[++ch];
-                        }
-                        row = (ch << 5) + (int)__fns(cmsk, 0, k + 1);
+                        // the (t - np)-th marked row
+                        row = W.oq[t - np];
                         lc = row >= cs1 ? 1 : 0;
                         x = id[s + row];
                         constexpr uint32_t w = prog_window(PROG, kOad > 0 ? kOad : 0);
@@ -1902,7 +1920,8 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                         float fa;
                         bool queued = false;
                         oc = agent_outcome<PROG, BATCH, kEarlyOad ? kOadGiven : kOadDraw>(
-                            P, R, step, fT, id[g], meta[g], birth[g], P.reads_age ? age[g] : 0.0f, lastb[g],
+                            P, R, step, fT, id[g], meta[g], birth[g],
+                            P.reads_age ? (derived ? __fsub_rn(fTprev, birth[g]) : age[g]) : 0.0f, lastb[g],
                             mate >= 0, W.cv[lc], wthr, odie, fa, queued, cnt_deaths, cnt_moves, mdir);
                         if (oc & kOutBirth) {
                             father[g] = (int32_t)(s + (uint32_t)mate);
@@ -2263,7 +2282,7 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                     id2[dst] = x;
                     birth2[dst] = fb;
                     lastb2[dst] = fl;
-                    age2[dst] = P.age_from_birth ? __fsub_rn(ft, fb) : fa;
+                    if (BATCH || !P.age_from_birth) age2[dst] = P.age_from_birth ? __fsub_rn(ft, fb) : fa;
                     meta2[dst] = (uint8_t)(((code & kOutGender) ? kMetaGender : 0) |
                                            ((code & kOutFertile) ? kMetaFertile : 0));
                     if (genetics) gslot2[dst] = gs;
@@ -2284,7 +2303,7 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                     id2[dst] = baby;
                     birth2[dst] = ft;
                     lastb2[dst] = 0.0f;
-                    age2[dst] = 0.0f;
+                    if (BATCH || !P.age_from_birth) age2[dst] = 0.0f;
                     meta2[dst] = (uint8_t)((u >> 31) ? kMetaGender : kMetaFertile);
                     if (genetics) {
                         const uint32_t gr = bid + rk;   // birth rank of the step
@@ -2783,6 +2802,31 @@ __global__ void k_gather_genomes(const int32_t *__restrict__ gslot, const uint64
     }
 }
 
+// the download's per-row columns of a single run's table, built on the
+// device: the cell of each row (one warp per non-empty cell), the gender and
+// the life state from the meta byte, and -- where the table's ages are
+// derived -- the ages (float)(step - 1) - birth, written into the table's
+// own age column
+__global__ void k_download_cols(const uint32_t *__restrict__ nonempty, const uint32_t *__restrict__ ne_start,
+                                uint32_t nne, uint32_t n, const uint8_t *__restrict__ meta,
+                                const float *__restrict__ birth, float t_prev, int derived,
+                                int32_t *__restrict__ cell_out, uint8_t *__restrict__ gender_out,
+                                uint8_t *__restrict__ state_out, float *__restrict__ age) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < nne; k += warps) {
+        const int32_t c = (int32_t)nonempty[k];
+        const uint32_t a = ne_start[k], b = ne_start[k + 1];
+        for (uint32_t i = a + lane; i < b && i < n; i += 32u) cell_out[i] = c;
+    }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint8_t m = meta[i];
+        gender_out[i] = m & kMetaGender;
+        state_out[i] = (m & kMetaFertile) ? QHG_LS_FERTILE_DEV : QHG_LS_ALIVE_DEV;
+        if (derived) age[i] = __fsub_rn(t_prev, birth[i]);
+    }
+}
+
 // rows of one batch run in the current table: the cell of each row and the
 // agents per cell (either output may be null)
 __global__ void k_run_cells(const uint32_t *__restrict__ nonempty, const uint32_t *__restrict__ ne_start,
@@ -2865,6 +2909,17 @@ extern "C" int qhg_launch_upload(const qhg::StepConst *P, qhg::RunState *rs, con
 extern "C" int qhg_launch_occupancy(const qhg::RunState *rs, const uint32_t *nonempty, int32_t *occ, int grid,
                                     cudaStream_t stream) {
     qhg::k_occupancy<<<std::max(1, grid), 256, 0, stream>>>(rs, nonempty, occ);
+    return (int)cudaGetLastError();
+}
+
+extern "C" int qhg_launch_download_cols(const uint32_t *nonempty, const uint32_t *ne_start, uint32_t nne, uint32_t n,
+                                        const uint8_t *meta, const float *birth, float t_prev, int derived,
+                                        int32_t *cell_out, uint8_t *gender_out, uint8_t *state_out, float *age,
+                                        cudaStream_t stream) {
+    const uint32_t work = std::max(nne * 32u, n);
+    const unsigned blocks = (unsigned)std::max<uint32_t>(1u, std::min<uint32_t>((work + 255u) / 256u, 152u * 16u));
+    qhg::k_download_cols<<<blocks, 256, 0, stream>>>(nonempty, ne_start, nne, n, meta, birth, t_prev, derived,
+                                                      cell_out, gender_out, state_out, age);
     return (int)cudaGetLastError();
 }
 

@@ -40,7 +40,7 @@ EXPORTS = [
     "qhg_batch_set_shape", "qhg_batch_get_shape", "qhg_batch_stream", "qhg_batch_destroy",
     "qhg_batch_live_history", "qhg_batch_snapshot_async", "qhg_batch_snapshot_wait",
     "qhg_host_buffer_alloc", "qhg_host_buffer_free", "qhg_gpu_next_id", "qhg_gpu_set_next_id",
-    "qhg_gpu_test_stall_scan", "qhg_gpu_occupancy", "qhg_gpu_set_capacity", "qhg_gpu_set_move_weights", "qhg_gpu_set_ice",
+    "qhg_gpu_test_stall_scan", "qhg_gpu_occupancy", "qhg_gpu_set_capacity", "qhg_gpu_set_move_weights", "qhg_gpu_set_ice", "qhg_gpu_stats_async",
     "qhg_gpu_move_stats_enable", "qhg_gpu_move_stats", "qhg_gpu_set_move_stats", "qhg_gpu_set_occupancy",
 ]
 
@@ -138,6 +138,7 @@ def load_library(path: str = LIB_PATH):
         "qhg_gpu_set_capacity": (I, [P, P]),
         "qhg_gpu_set_move_weights": (I, [P, P]),
         "qhg_gpu_set_ice": (I, [P, P]),
+        "qhg_gpu_stats_async": (I, [P, P]),
         "qhg_gpu_move_stats_enable": (I, [P, ct.c_int32, P, P, ct.c_double, ct.c_int32]),
         "qhg_gpu_move_stats": (I, [P, P, P, P]),
         "qhg_gpu_set_move_stats": (I, [P, P, P, P]),
@@ -179,6 +180,50 @@ def make_desc(actions: Sequence[Action], seed: int, genetics: Genetics = Genetic
     d.flags = int(flags)
     d.device = int(device)
     return d
+
+
+class HostBuffer:
+    """Page-locked host memory (qhg_host_buffer_alloc) seen as a numpy array:
+    copies between it and the device run at the interconnect's speed, and
+    qhg_gpu_stats_async can write into it without a wait."""
+
+    def __init__(self, shape, dtype):
+        lib = load_library()
+        dt = np.dtype(dtype)
+        count = int(np.prod(shape))
+        nbytes = max(1, count * dt.itemsize)
+        p = ct.c_void_p()
+        if lib.qhg_host_buffer_alloc(nbytes, ct.byref(p)) != 0:
+            raise QhgError(-3, lib.qhg_batch_last_error().decode())
+        self.ptr = p.value
+        raw = (ct.c_uint8 * nbytes).from_address(self.ptr)
+        self.array = np.frombuffer(raw, dtype=np.uint8, count=count * dt.itemsize).view(dt).reshape(shape)
+
+    def free(self) -> None:
+        if self.ptr:
+            self.array = None
+            _lib.qhg_host_buffer_free(ct.c_void_p(self.ptr))
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def pinned_agents(n: int, genome_words: int = 0):
+    """An agent table of n rows in page-locked host memory, and the buffers
+    that hold it (keep them alive while the table is used)."""
+    bufs = [HostBuffer((n,), np.int64), HostBuffer((n,), np.int32), HostBuffer((n,), np.float32),
+            HostBuffer((n,), np.float32), HostBuffer((n,), np.float32), HostBuffer((n,), np.uint8),
+            HostBuffer((n,), np.uint8)]
+    a = Agents(*(b.array for b in bufs))
+    if genome_words > 0:
+        g = HostBuffer((n, genome_words), np.uint64)
+        bufs.append(g)
+        a.genome = g.array
+    return a, bufs
 
 
 class GpuRun:
@@ -239,15 +284,25 @@ class GpuRun:
         _check(_lib.qhg_gpu_current_step(self.h, ct.byref(s)))
         return int(s.value)
 
-    def agents(self, sort_by_id: bool = True) -> Agents:
+    def agents(self, sort_by_id: bool = True, out: Agents = None) -> Agents:
+        """The current table (rows by cell, or by ID).  `out`: arrays to fill
+        (e.g. pinned_agents), at least as long as the table; the result is
+        then their first rows."""
         n = self.num_agents()
-        out = Agents(np.zeros(n, np.int64), np.zeros(n, np.int32), np.zeros(n, np.float32),
-                     np.zeros(n, np.float32), np.zeros(n, np.float32), np.zeros(n, np.uint8),
-                     np.zeros(n, np.uint8))
+        if out is not None:
+            if len(out) < n:
+                raise ValueError("output table too small")
+            out = Agents(out.id[:n], out.cell[:n], out.birth[:n], out.age[:n], out.lastb[:n], out.gender[:n],
+                         out.state[:n], None if out.genome is None else out.genome[:n])
+        else:
+            out = Agents(np.zeros(n, np.int64), np.zeros(n, np.int32), np.zeros(n, np.float32),
+                         np.zeros(n, np.float32), np.zeros(n, np.float32), np.zeros(n, np.uint8),
+                         np.zeros(n, np.uint8))
         soa = AgentsSoA(out.id.ctypes.data, out.cell.ctypes.data, out.birth.ctypes.data, out.age.ctypes.data,
                         out.lastb.ctypes.data, out.gender.ctypes.data, out.state.ctypes.data, None)
         if self.genetics.genome_size > 0:
-            out.genome = np.zeros((n, 2 * self.genetics.num_blocks), dtype=np.uint64)
+            if out.genome is None:
+                out.genome = np.zeros((n, 2 * self.genetics.num_blocks), dtype=np.uint64)
             soa.genome = out.genome.ctypes.data
         got = ct.c_int64()
         _check(_lib.qhg_gpu_download(self.h, ct.byref(soa), n, ct.byref(got)))
@@ -336,6 +391,13 @@ class GpuRun:
         buf = (StepStats * max(1, nsteps))()
         _check(_lib.qhg_gpu_stats(self.h, int(nsteps), ct.byref(buf)))
         return np.array([[s.live, s.births, s.deaths, s.moves] for s in buf[:nsteps]], dtype=np.uint64)
+
+    def stats_async(self, out: np.ndarray) -> None:
+        """Queues a copy of the last launched step's statistics (live,
+        births, deaths, moves) into `out` (4 uint64, page-locked memory such
+        as a HostBuffer row) without waiting; valid after sync()."""
+        assert out.dtype == np.uint64 and out.size == 4 and out.flags["C_CONTIGUOUS"]
+        _check(_lib.qhg_gpu_stats_async(self.h, ct.c_void_p(out.ctypes.data)))
 
     def birth_log(self) -> np.ndarray:
         n = ct.c_int64()
