@@ -51,8 +51,9 @@ WORKLOADS = {
 }
 AGENT_BYTES = 60   # one read and one write of the 30-byte hot record per agent-step
 BIRTH_BYTES = 3 * 1024   # genetics: two parent genomes read, one child genome written (2 x 4,096 loci)
-# kernels launched per step: the action kernel and the scatter in each of the
-# three forms (two of each return at once) and the cell scan
+# kernels launched per step of a single run: the action kernel and the
+# scatter in each of the three forms (two of each return at once) and the
+# cell scan; the genome kernel with genetics
 LAUNCHES_PER_STEP = 7
 # speed of the C port relative to the reference's own OpenMP code, measured
 # where the reference sources are (both on 8 cores of the build container,
@@ -516,8 +517,8 @@ def run_ours(args, world, rank, local, dist):
             "config": cfg,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks, "genetics": genetics,
             "batched": batched, "served": served,
-            "gpu_launches": LAUNCHES_PER_STEP * args.steps * world,
-            "gpu_launches_per_step": LAUNCHES_PER_STEP,
+            "gpu_launches": (LAUNCHES_PER_STEP + (1 if w.genetics.genome_size > 0 else 0)) * args.steps * world,
+            "gpu_launches_per_step": LAUNCHES_PER_STEP + (1 if w.genetics.genome_size > 0 else 0),
         }
         print(json.dumps(line), flush=True)
     return 0

@@ -10,6 +10,7 @@
 #include <cstring>
 #include <limits>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -400,6 +401,29 @@ void qhg_host_ice_bits(int C, const int32_t *nbr6, const uint8_t *ice, std::vect
     }
 }
 
+// Runs f(c0, c1) over [0, n) in contiguous chunks on the host's cores (the
+// grid tables of large grids: every cell independent); returns the smallest
+// cell at which some chunk reported an error (f returns the failing cell, or
+// n when its chunk went through), n if none.
+template <class F>
+static int parallel_cells(int n, F f) {
+    unsigned hw = std::thread::hardware_concurrency();
+    const int nt = (int)std::max(1u, std::min(hw == 0u ? 1u : hw, 32u));
+    if (n < 65536 || nt == 1) return f(0, n);
+    std::vector<int> bad((size_t)nt, n);
+    std::vector<std::thread> th;
+    const int per = (n + nt - 1) / nt;
+    for (int t = 0; t < nt; t++) {
+        const int c0 = t * per, c1 = std::min(n, c0 + per);
+        if (c0 >= c1) break;
+        th.emplace_back([&, t, c0, c1]() { bad[(size_t)t] = f(c0, c1); });
+    }
+    for (auto &x : th) x.join();
+    int b = n;
+    for (int v : bad) b = std::min(b, v);
+    return b;
+}
+
 // Grid tables of one run: rev packs, 3 bits per neighbour slot q, the slot
 // of the cell in the neighbour's own list; wthr holds the WeightedMove
 // thresholds (SingleEvaluator's cumulated weights, actions/SingleEvaluator.cpp:174-241,
@@ -412,19 +436,31 @@ int qhg_host_grid_tables(int C, const int32_t *nbr6, const uint8_t *nnbr, const 
                          const uint8_t *ice, std::vector<uint32_t> &rev, std::vector<uint64_t> &wthr,
                          std::vector<uint32_t> &cmove, std::string &err) {
     rev.assign((size_t)C, 0u);
-    for (int c = 0; c < C; c++) {
-        if (nnbr[c] > 6) { err = "more than 6 neighbours"; return -1; }
-        for (int j = 0; j < 6; j++) {
-            const int d = nbr6[(size_t)c * 6 + j];
-            if (d >= C || d < -1) { err = "neighbour index out of range"; return -1; }
-            if (j >= nnbr[c] || d < 0) continue;
-            int k = -1;
-            for (int q = 0; q < nnbr[d]; q++) {
-                if (nbr6[(size_t)d * 6 + q] == c) { k = q; break; }
+    // the first failing cell's problem: 1 too many neighbours, 2 index out of
+    // range, 3 not symmetric
+    std::vector<uint8_t> why((size_t)C, 0u);
+    const int bad = parallel_cells(C, [&](int c0, int c1) {
+        for (int c = c0; c < c1; c++) {
+            if (nnbr[c] > 6) { why[(size_t)c] = 1u; return c; }
+            for (int j = 0; j < 6; j++) {
+                const int d = nbr6[(size_t)c * 6 + j];
+                if (d >= C || d < -1) { why[(size_t)c] = 2u; return c; }
+                if (j >= nnbr[c] || d < 0) continue;
+                int k = -1;
+                for (int q = 0; q < nnbr[d] && q < 6; q++) {
+                    if (nbr6[(size_t)d * 6 + q] == c) { k = q; break; }
+                }
+                if (k < 0) { why[(size_t)c] = 3u; return c; }
+                rev[(size_t)c] |= (uint32_t)k << (3 * j);
             }
-            if (k < 0) { err = "neighbour table is not symmetric"; return -1; }
-            rev[(size_t)c] |= (uint32_t)k << (3 * j);
         }
+        return C;
+    });
+    if (bad < C) {
+        const uint8_t w = why[(size_t)bad];
+        err = w == 1u ? "more than 6 neighbours" : (w == 2u ? "neighbour index out of range"
+                                                            : "neighbour table is not symmetric");
+        return -1;
     }
     wthr.assign((size_t)C * 6, 0);
     cmove.assign((size_t)C, 0u);
@@ -440,17 +476,20 @@ int qhg_host_grid_tables(int C, const int32_t *nbr6, const uint8_t *nnbr, const 
         const double dV = K[c];
         W[(size_t)c * 7] = (ice != nullptr && ice[c] != 0) ? 0 : ((dV > 0) ? dV : 0);
     }
-    for (int c = 0; c < C; c++) {
-        double dW = W[(size_t)c * 7];
-        for (int i = 0; i < 6; i++) {
-            double dCW = 0;
-            const int ni = nbr6[(size_t)c * 6 + i];
-            if (ni >= 0) dCW = W[(size_t)ni * 7];
-            dCW = (dCW > 0) ? dCW : 0;
-            dW = dW + dCW;
-            W[(size_t)c * 7 + i + 1] = dW;
+    parallel_cells(C, [&](int c0, int c1) {
+        for (int c = c0; c < c1; c++) {
+            double dW = W[(size_t)c * 7];
+            for (int i = 0; i < 6; i++) {
+                double dCW = 0;
+                const int ni = nbr6[(size_t)c * 6 + i];
+                if (ni >= 0) dCW = W[(size_t)ni * 7];
+                dCW = (dCW > 0) ? dCW : 0;
+                dW = dW + dCW;
+                W[(size_t)c * 7 + i + 1] = dW;
+            }
         }
-    }
+        return C;
+    });
     return qhg_host_move_tables(C, nnbr, W.data(), wthr, cmove, err);
 }
 
@@ -470,38 +509,42 @@ int qhg_host_grid_tables(int C, const int32_t *nbr6, const uint8_t *nnbr, const 
 int qhg_host_move_tables(int C, const uint8_t *nnbr, const double *W, std::vector<uint64_t> &wthr,
                          std::vector<uint32_t> &cmove, std::string &err) {
     wthr.assign((size_t)C * 6, 0);
-    for (int c = 0; c < C; c++) {
-        const int nn = nnbr[c];
-        const double *Wc = &W[(size_t)c * 7];
-        const double Wn = Wc[nn];
-        cmove[c] &= ~(1u << 16);
-        if (Wc[0] == Wn) {
-            cmove[c] |= 1u << 16;
-            continue;
-        }
-        if (!(Wn > 0.0) || !std::isfinite(Wn)) {
-            err = "cell " + std::to_string(c) + ": total move weight not positive and finite";
-            return -1;
-        }
-        auto f = [&](uint64_t u) { return ((1.0 * (double)u) / 4294967296.0) * Wn; };
-        uint64_t run = 0;
-        for (int j = 0; j < nn; j++) {
-            const double x = Wc[j];
-            if (!std::isfinite(x)) {
-                err = "cell " + std::to_string(c) + ": move weight not finite";
-                return -1;
+    // per failing cell: 1 total weight not positive and finite, 2 a weight not finite
+    std::vector<uint8_t> why((size_t)C, 0u);
+    const int bad = parallel_cells(C, [&](int c0, int c1) {
+        for (int c = c0; c < c1; c++) {
+            const int nn = nnbr[c];
+            const double *Wc = &W[(size_t)c * 7];
+            const double Wn = Wc[nn];
+            cmove[c] &= ~(1u << 16);
+            if (Wc[0] == Wn) {
+                cmove[c] |= 1u << 16;
+                continue;
             }
-            // smallest u in [0, 2^32] with f(u) >= x  (f(2^32) counts as +inf)
-            double g = std::floor(x / Wn * 4294967296.0);
-            uint64_t u = (g <= 0) ? 0ull : (g >= 4294967296.0 ? 4294967296ull : (uint64_t)g);
-            while (u > 0 && f(u - 1) >= x) u--;
-            while (u < 4294967296ull && f(u) < x) u++;
-            run = std::max(run, u);
-            wthr[(size_t)c * 6 + j] = run;
+            if (!(Wn > 0.0) || !std::isfinite(Wn)) { why[(size_t)c] = 1u; return c; }
+            auto f = [&](uint64_t u) { return ((1.0 * (double)u) / 4294967296.0) * Wn; };
+            uint64_t run = 0;
+            for (int j = 0; j < nn; j++) {
+                const double x = Wc[j];
+                if (!std::isfinite(x)) { why[(size_t)c] = 2u; return c; }
+                // smallest u in [0, 2^32] with f(u) >= x  (f(2^32) counts as +inf)
+                double g = std::floor(x / Wn * 4294967296.0);
+                uint64_t u = (g <= 0) ? 0ull : (g >= 4294967296.0 ? 4294967296ull : (uint64_t)g);
+                while (u > 0 && f(u - 1) >= x) u--;
+                while (u < 4294967296ull && f(u) < x) u++;
+                run = std::max(run, u);
+                wthr[(size_t)c * 6 + j] = run;
+            }
+            // slots without a neighbour: 2^32, a threshold no draw reaches (the
+            // device may count over all six slots)
+            for (int j = nn; j < 6; j++) wthr[(size_t)c * 6 + j] = 4294967296ull;
         }
-        // slots without a neighbour: 2^32, a threshold no draw reaches (the
-        // device may count over all six slots)
-        for (int j = nn; j < 6; j++) wthr[(size_t)c * 6 + j] = 4294967296ull;
+        return C;
+    });
+    if (bad < C) {
+        err = "cell " + std::to_string(bad) +
+              (why[(size_t)bad] == 1u ? ": total move weight not positive and finite" : ": move weight not finite");
+        return -1;
     }
     return 0;
 }

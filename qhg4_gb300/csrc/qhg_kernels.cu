@@ -2569,7 +2569,7 @@ k_genomes(const StepConst P, RunState *__restrict__ rs, uint64_t *__restrict__ g
         } else if (P.num_crossover > 0) {
             nM = nF = P.num_crossover;
         }
-        const int kMom = k, kDad = k + nM;
+        const int kMom = k;   // the father's breaks follow the mother's
         k += nM + nF;
         int nmut = 0;
         if (P.has_mutation) {
@@ -2996,29 +2996,51 @@ static CellGrids cell_grids() {
     return g[dev];
 }
 
-static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
-                           const qhg::BatchBuffers *BBp, const qhg::LaunchShape &L, cudaStream_t stream,
-                           cudaEvent_t *ev) {
+// One step's launches come in four phases: the action kernels, the
+// MoveStats candidates and the cell scan, the scatters, the work after the
+// commit.  The action kernel and the scatter exist in three forms; `form`
+// selects one (kFormTile, kFormBig, kFormCell) or, with -1, launches all of
+// them, and those that do not match the step's table (RunState::form, set by
+// the previous step) return at once.  Steps launch all forms: graphs whose
+// switch nodes launch only the step's form measured slower on GB300 (the
+// large run's step +3 %, steps of small runs markedly slower) than the three
+// early-returning launches they save.
+struct StepLaunch {
+    const qhg::StepConst *P;
+    qhg::RunState *rs;
+    const qhg::StepBuffers *B;
+    qhg::BatchBuffers BB;
+    bool batch;
+    qhg::LaunchShape L;
+    cudaStream_t stream;
+};
+
+static StepLaunch step_launch(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
+                              const qhg::BatchBuffers *BBp, const qhg::LaunchShape &L, cudaStream_t stream) {
+    StepLaunch S;
+    S.P = P; S.rs = rs; S.B = B; S.batch = BBp != nullptr; S.L = L; S.stream = stream;
+    if (S.batch) S.BB = *BBp;
+    else memset(&S.BB, 0, sizeof(S.BB));
+    return S;
+}
+
+static void launch_actions(const StepLaunch &S, int form) {
     using namespace qhg;
-    set_tile_attributes();
-    const int sitems = scan_items(P->num_cells);
-    const int ntiles = (P->num_cells + kScanThreads * sitems - 1) / (kScanThreads * sitems);
-    const bool batch = BBp != nullptr;
-    BatchBuffers BB;
-    if (batch) BB = *BBp;
-    else memset(&BB, 0, sizeof(BB));
+    const StepConst *P = S.P;
+    RunState *rs = S.rs;
+    const StepBuffers *B = S.B;
+    const BatchBuffers &BB = S.BB;
+    const LaunchShape &L = S.L;
+    cudaStream_t stream = S.stream;
+    const bool batch = S.batch;
     constexpr size_t kSmC = sizeof(CellWarpSmem) * kCellWarps;
     const CellGrids CG = cell_grids();
-    const size_t kSmSC = (size_t)2 * kCellWarps * scatter_stage_bytes(!P->age_from_birth, P->genome_words > 0);
     const size_t kSmA = batch ? sizeof(ActionsSmemT<Tile<false>::kMax, Tile<false>::kThreads, true>)
                               : sizeof(ActionsSmemT<Tile<false>::kMax, Tile<false>::kThreads, false>);
-    constexpr size_t kSmS = sizeof(ScatterSmemT<Tile<false>::kMax, Tile<false>::kThreads>);
     const size_t kSmAB = batch ? sizeof(ActionsSmemT<Tile<true>::kMax, Tile<true>::kThreads, true>)
                                : sizeof(ActionsSmemT<Tile<true>::kMax, Tile<true>::kThreads, false>);
-    constexpr size_t kSmSB = sizeof(ScatterSmemT<Tile<true>::kMax, Tile<true>::kThreads>);
-    if (ev) cudaEventRecord(ev[0], stream);
-    // every form is launched; those that do not match the step's table
-    // (RunState::form, set by the previous step) return at once
+    const bool tile = form < 0 || form == (int)kFormTile, cell = form < 0 || form == (int)kFormCell;
+    const bool big = form < 0 || form == (int)kFormBig;
 #define QHG_LAUNCH_ACTIONS(PR, BT, BG, GRID, SM)                                                          \
     k_actions<PR, BT, BG><<<GRID, Tile<BG>::kThreads, SM, stream>>>(                                      \
         *P, BB, rs, B->nonempty, B->ne_start, B->tile_first, B->id, B->birth, B->age, B->lastb, B->meta, \
@@ -3027,24 +3049,41 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
     k_actions_cell<PR, BT><<<CG.actions, kCellThreads, kSmC, stream>>>(                                    \
         *P, BB, rs, B->nonempty, B->ne_start, B->id, B->birth, B->age, B->lastb, B->meta, B->vthr, B->wthr, \
         B->necm, B->outc, B->father, B->brank, B->clsc)
+#define QHG_FORMS(PR, BT)                                                      \
+    do {                                                                       \
+        if (tile) QHG_LAUNCH_ACTIONS(PR, BT, false, L.actions_grid, kSmA);     \
+        if (cell) QHG_LAUNCH_CELL(PR, BT);                                     \
+    } while (0)
     if (batch) {
         switch (P->program) {
-        case 1: QHG_LAUNCH_ACTIONS(1, true, false, L.actions_grid, kSmA); QHG_LAUNCH_CELL(1, true); break;
-        default: QHG_LAUNCH_ACTIONS(0, true, false, L.actions_grid, kSmA); QHG_LAUNCH_CELL(0, true); break;
+        case 1: QHG_FORMS(1, true); break;
+        default: QHG_FORMS(0, true); break;
         }
-        QHG_LAUNCH_ACTIONS(0, true, true, L.big_grid, kSmAB);
+        if (big) QHG_LAUNCH_ACTIONS(0, true, true, L.big_grid, kSmAB);
     } else {
         switch (P->program) {
-        case 1: QHG_LAUNCH_ACTIONS(1, false, false, L.actions_grid, kSmA); QHG_LAUNCH_CELL(1, false); break;
-        case 2: QHG_LAUNCH_ACTIONS(2, false, false, L.actions_grid, kSmA); QHG_LAUNCH_CELL(2, false); break;
-        case 3: QHG_LAUNCH_ACTIONS(3, false, false, L.actions_grid, kSmA); QHG_LAUNCH_CELL(3, false); break;
-        default: QHG_LAUNCH_ACTIONS(0, false, false, L.actions_grid, kSmA); QHG_LAUNCH_CELL(0, false); break;
+        case 1: QHG_FORMS(1, false); break;
+        case 2: QHG_FORMS(2, false); break;
+        case 3: QHG_FORMS(3, false); break;
+        default: QHG_FORMS(0, false); break;
         }
-        QHG_LAUNCH_ACTIONS(0, false, true, L.big_grid, kSmAB);
+        if (big) QHG_LAUNCH_ACTIONS(0, false, true, L.big_grid, kSmAB);
     }
+#undef QHG_FORMS
 #undef QHG_LAUNCH_CELL
 #undef QHG_LAUNCH_ACTIONS
-    if (ev) cudaEventRecord(ev[1], stream);
+}
+
+static void launch_scan(const StepLaunch &S) {
+    using namespace qhg;
+    const StepConst *P = S.P;
+    RunState *rs = S.rs;
+    const StepBuffers *B = S.B;
+    const BatchBuffers &BB = S.BB;
+    cudaStream_t stream = S.stream;
+    const bool batch = S.batch;
+    const int sitems = scan_items(P->num_cells);
+    const int ntiles = (P->num_cells + kScanThreads * sitems - 1) / (kScanThreads * sitems);
     const int ms_grid = std::max(1, std::min((P->num_cells + 7) / 8, 152 * 16));
     if (!batch && B->ms_mode >= 0) {
 #define QHG_LAUNCH_MS_PICK(MD, PS)                                                                          \
@@ -3069,7 +3108,23 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
         else QHG_LAUNCH_SCAN(false, 1);
     }
 #undef QHG_LAUNCH_SCAN
-    if (ev) cudaEventRecord(ev[2], stream);
+}
+
+static void launch_scatter(const StepLaunch &S, int form) {
+    using namespace qhg;
+    const StepConst *P = S.P;
+    RunState *rs = S.rs;
+    const StepBuffers *B = S.B;
+    const BatchBuffers &BB = S.BB;
+    const LaunchShape &L = S.L;
+    cudaStream_t stream = S.stream;
+    const bool batch = S.batch;
+    const CellGrids CG = cell_grids();
+    const size_t kSmSC = (size_t)2 * kCellWarps * scatter_stage_bytes(!P->age_from_birth, P->genome_words > 0);
+    constexpr size_t kSmS = sizeof(ScatterSmemT<Tile<false>::kMax, Tile<false>::kThreads>);
+    constexpr size_t kSmSB = sizeof(ScatterSmemT<Tile<true>::kMax, Tile<true>::kThreads>);
+    const bool tile = form < 0 || form == (int)kFormTile, cell = form < 0 || form == (int)kFormCell;
+    const bool big = form < 0 || form == (int)kFormBig;
 #define QHG_LAUNCH_SCATTER(BT, BG, GRID, SM)                                                                \
     k_scatter<BT, BG><<<GRID, Tile<BG>::kThreads, SM, stream>>>(                                            \
         *P, BB, rs, B->nonempty, B->ne_start, B->tile_first, B->id, B->birth, B->age, B->lastb, B->outc,   \
@@ -3082,17 +3137,27 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
         B->brank, B->sbase, B->bbase, B->bidbase, B->obase, B->clsc, B->id2, B->birth2, B->age2, B->lastb2, \
         B->meta2, B->blog, B->blog_cap, B->gslot, B->gslot2, B->freelist, B->freelist2, B->brec)
     if (batch) {
-        QHG_LAUNCH_SCATTER(true, false, L.scatter_grid, kSmS);
-        QHG_LAUNCH_SCATTER_CELL(true);
-        QHG_LAUNCH_SCATTER(true, true, L.big_grid, kSmSB);
+        if (tile) QHG_LAUNCH_SCATTER(true, false, L.scatter_grid, kSmS);
+        if (cell) QHG_LAUNCH_SCATTER_CELL(true);
+        if (big) QHG_LAUNCH_SCATTER(true, true, L.big_grid, kSmSB);
     } else {
-        QHG_LAUNCH_SCATTER(false, false, L.scatter_grid, kSmS);
-        QHG_LAUNCH_SCATTER_CELL(false);
-        QHG_LAUNCH_SCATTER(false, true, L.big_grid, kSmSB);
+        if (tile) QHG_LAUNCH_SCATTER(false, false, L.scatter_grid, kSmS);
+        if (cell) QHG_LAUNCH_SCATTER_CELL(false);
+        if (big) QHG_LAUNCH_SCATTER(false, true, L.big_grid, kSmSB);
     }
 #undef QHG_LAUNCH_SCATTER_CELL
 #undef QHG_LAUNCH_SCATTER
-    if (ev) cudaEventRecord(ev[3], stream);
+}
+
+static void launch_post(const StepLaunch &S, cudaEvent_t *ev) {
+    using namespace qhg;
+    const StepConst *P = S.P;
+    RunState *rs = S.rs;
+    const StepBuffers *B = S.B;
+    const BatchBuffers &BB = S.BB;
+    const LaunchShape &L = S.L;
+    cudaStream_t stream = S.stream;
+    const bool batch = S.batch;
     if (!batch && B->occ != nullptr) {
         k_occupancy<<<std::max(1, L.scatter_grid), 256, 0, stream>>>(rs, B->nonempty2, B->occ);
     }
@@ -3116,6 +3181,21 @@ static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg
         k_genomes<<<L.scatter_grid, 256, 0, stream>>>(*P, rs, B->genome, B->brec);
         if (ev) cudaEventRecord(ev[4], stream);
     }
+}
+
+static void launch_kernels(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
+                           const qhg::BatchBuffers *BBp, const qhg::LaunchShape &L, cudaStream_t stream,
+                           cudaEvent_t *ev) {
+    set_tile_attributes();
+    const StepLaunch S = step_launch(P, rs, B, BBp, L, stream);
+    if (ev) cudaEventRecord(ev[0], stream);
+    launch_actions(S, -1);
+    if (ev) cudaEventRecord(ev[1], stream);
+    launch_scan(S);
+    if (ev) cudaEventRecord(ev[2], stream);
+    launch_scatter(S, -1);
+    if (ev) cudaEventRecord(ev[3], stream);
+    launch_post(S, ev);
 }
 
 extern "C" int qhg_launch_step(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
