@@ -32,6 +32,10 @@ CASES = {
     # the plain method's action set with rates at which the population persists
     "plain_stationary": (lambda: uniform_grid(32, 30.0), 100_000, 50.0, False,
                          lambda: config1_actions(b0=0.5, d0=0.02), 200),
+    # the plain method exactly as configured (b0 0.2, d0 0.05): the population
+    # shrinks to a few dozen agents by step 200 and dies out soon after, so
+    # its summaries cover the decline (running on to step 1,000 adds nothing)
+    "plain_configured": (lambda: uniform_grid(32, 30.0), 100_000, 50.0, False, config1_actions, 200),
     # the large run's action set (VerhulstVarK, OldAgeDeath, WeightedMove) on a
     # smaller altitude grid
     "large_actions": (lambda: terrain_grid(32, seed=5), 100_000, 60.0, True, config2_actions, 200),

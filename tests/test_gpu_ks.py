@@ -36,7 +36,7 @@ class _GpuRunner:
         self.r.close()
 
 
-@pytest.mark.parametrize("case", ["plain_stationary", "large_actions"])
+@pytest.mark.parametrize("case", ["plain_stationary", "plain_configured", "large_actions"])
 def test_gpu_matches_unmodified_reference_in_distribution(gpu_lib, case):
     ref = np.load(os.path.join(HERE, "golden", f"ks_{case}.npz"))["summaries"]
     ours = run_summaries(_GpuRunner, case, range(5000, 5000 + N_SEEDS))

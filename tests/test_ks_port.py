@@ -35,9 +35,10 @@ class _PortRunner:
         self.r.close()
 
 
-def test_port_matches_unmodified_reference_in_distribution():
-    ref = np.load(os.path.join(HERE, "golden", "ks_small.npz"))["summaries"]
-    ours = run_summaries(_PortRunner, "small", range(5000, 5000 + N_SEEDS))
+@pytest.mark.parametrize("case", ["small", "plain_configured"])
+def test_port_matches_unmodified_reference_in_distribution(case):
+    ref = np.load(os.path.join(HERE, "golden", f"ks_{case}.npz"))["summaries"]
+    ours = run_summaries(_PortRunner, case, range(5000, 5000 + N_SEEDS))
     p = ks_pvalues(ref, ours)
     report = ", ".join(f"{n} p={v:.3f}" for n, v in zip(SUMMARY_NAMES, p))
     print(report)
