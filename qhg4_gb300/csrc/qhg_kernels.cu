@@ -396,11 +396,18 @@ constexpr uint32_t kStDeadU = 64u;     // Verhulst kills it (without a mate)
 constexpr uint32_t kStDeadM = 128u;    // Verhulst kills it (with a mate)
 constexpr uint32_t kStBirthM = 256u;   // gives birth (with a mate)
 constexpr int kStOad = 9;              // bits 9-10, OldAgeDeath: 0 survives, 1 dies, 2 inside the window
+constexpr uint32_t kStMoveDraw = 2048u; // the move draw passed: the direction is decided later (deferred move)
 
-template <int PROG, bool BATCH>
+// With DEFER the move's direction is left out: an agent whose move draw
+// passes gets kStMoveDraw and its direction draw in u2out, and move_direction
+// decides the direction later, in a dense pass over such agents only (a
+// warp's rows rarely all move, so this saves the direction work in most
+// lanes).
+template <int PROG, bool BATCH, bool DEFER = false>
 __device__ __forceinline__ uint32_t agent_state(const StepConst &P, const BatchRun *R, int32_t step, float fT,
                                                 int64_t id, uint8_t m8, float fb, float fa, float fl,
-                                                const CellView &cv, const uint32_t *wt32, uint32_t wnever) {
+                                                const CellView &cv, const uint32_t *wt32, uint32_t wnever,
+                                                uint32_t *u2out = nullptr) {
     constexpr int iF = prog_index(PROG, kFertility, kFertility);
     constexpr int iV = prog_index(PROG, kVerhulst, kVerhulstVarK);
     constexpr int iM = prog_index(PROG, kRandomMove, kWeightedMove);
@@ -442,7 +449,10 @@ __device__ __forceinline__ uint32_t agent_state(const StepConst &P, const BatchR
     {   // RandomMove / WeightedMove ::execute (actions/RandomMove.cpp:65-100,
         // actions/WeightedMove.cpp:45-106), for an agent still alive
         const ActionConst &A = BATCH ? R->act[iM] : P.act[iM];
-        if ((uint64_t)d.v[kWM] < A.pthr) {
+        if (DEFER) {
+            if ((uint64_t)d.v[kWM] < A.pthr) st |= kStMoveDraw;
+            *u2out = d.v[kWM + 1u];
+        } else if ((uint64_t)d.v[kWM] < A.pthr) {
             const uint32_t u2 = d.v[kWM + 1u];
             int d;
             if (!kWeighted || (cv.wf & 1u)) {
@@ -470,6 +480,29 @@ __device__ __forceinline__ uint32_t agent_state(const StepConst &P, const BatchR
     }
     return st;
     }
+}
+
+// The direction of an agent whose move draw passed (RandomMove::execute,
+// actions/RandomMove.cpp:65-100; WeightedMove::execute,
+// actions/WeightedMove.cpp:45-106): neighbour slot + 1, 0 when it stays or
+// the slot holds no cell (for WeightedMove also when the cell is ice,
+// actions/WeightedMove.cpp:91)
+template <bool kWeighted>
+__device__ __forceinline__ uint32_t move_direction(const CellView &cv, const uint32_t *wt32, uint32_t wnever,
+                                                   uint32_t u2) {
+    int d;
+    if (!kWeighted || (cv.wf & 1u)) {
+        d = (int)(((uint64_t)(cv.nn + 1u) * (uint64_t)u2) >> 32);
+    } else {
+        // see agent_state: slots whose threshold is <= u2, in 32 bits with
+        // the unreachable thresholds taken back out for u2 = 0xffffffff
+        const uint4 wa = *reinterpret_cast<const uint4 *>(wt32);
+        const uint2 wb = *reinterpret_cast<const uint2 *>(wt32 + 4);
+        d = (wa.x <= u2 ? 1 : 0) + (wa.y <= u2 ? 1 : 0) + (wa.z <= u2 ? 1 : 0) + (wa.w <= u2 ? 1 : 0) +
+            (wb.x <= u2 ? 1 : 0) + (wb.y <= u2 ? 1 : 0);
+        if (u2 == 0xffffffffu) d -= __popc(wnever);
+    }
+    return (d > 0 && (((kWeighted ? cv.wv : cv.vm) >> (d - 1)) & 1u)) ? (uint32_t)d : 0u;
 }
 
 template <int PROG, bool BATCH, bool BIG>
@@ -1562,6 +1595,8 @@ struct CellWarpSmem {
     uint16_t st[kMaxCellWarp];       // per row: state before the pairing (agent_state), then the outcome byte
     uint32_t odie[kMaxCellWarp / 32];  // OldAgeDeath decided in advance: bit per row, set = dies
     uint16_t oq[kMaxCellWarp];       // rows inside the OldAgeDeath age window, in a dense queue
+    uint16_t mq[kMaxCellWarp];       // rows whose move draw passed (deferred moves), in a dense queue
+    uint32_t mu2[kMaxCellWarp];      // ... and their direction draws
     uint32_t cnt[kGroupCells][8];    // class counts: [0] stay, [1..6] movers per neighbour slot
     // WeightedMove thresholds of each cell (slots 0-5) as 32-bit values: a
     // threshold of 2^32 (no draw reaches it) is kept as 0xffffffff and its
@@ -1689,10 +1724,11 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
             // pick, in ID order, each pick drawn from the pairing stream of the
             // picking member.  With an early OldAgeDeath, the agents inside its
             // age window are marked.
-            int nF0 = 0, nM0 = 0, nF1 = 0, nM1 = 0, nq = 0;
+            int nF0 = 0, nM0 = 0, nF1 = 0, nM1 = 0, nq = 0, nmv = 0;
             bool wide = false;
             if (kOnePass || P.has_pair || kEarlyOad) {
                 for (int b = 0; b < n; b += 32) {
+                    uint32_t mu2 = 0u;
                     const int row = b + lane;
                     const bool valid = row < n;
                     const int lc = row >= cs1 ? 1 : 0;
@@ -1718,9 +1754,20 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                     uint32_t stt = 0u;
                     if (kOnePass && kp) {
                         const BatchRun *R = BATCH ? BB.runs + W.run[lc] : nullptr;
-                        stt = agent_state<PROG, BATCH>(P, R, step, fT, xid, m8, fb, fa, fl, W.cv[lc], W.wt32[lc],
-                                                       W.wnever[lc]);
+                        stt = agent_state<PROG, BATCH, !BATCH>(P, R, step, fT, xid, m8, fb, fa, fl, W.cv[lc],
+                                                               W.wt32[lc], W.wnever[lc], &mu2);
                         W.st[row] = (uint16_t)stt;
+                    }
+                    if (kOnePass && !BATCH) {
+                        // deferred moves: queue the rows whose move draw passed
+                        const bool mv = (stt & kStMoveDraw) != 0u;
+                        const uint32_t mm = __ballot_sync(FULL_MASK, mv);
+                        if (mv) {
+                            const int qp = nmv + __popc(mm & lt);
+                            W.mq[qp] = (uint16_t)row;
+                            W.mu2[qp] = mu2;
+                        }
+                        nmv += __popc(mm);
                     }
                     if (P.has_pair && valid) W.mate[row] = -1;
                     const uint32_t f0 = __ballot_sync(FULL_MASK, fert && !male && lc == 0);
@@ -1769,6 +1816,18 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
             const uint32_t nL0 = (uint32_t)(fs0 ? nM0 : nF0), nL1 = (uint32_t)(fs1 ? nM1 : nF1);
             const int sb0 = fs0 ? 0 : cs1 - nM0, sb1 = fs1 ? cs1 : n - nM1;     // smaller side in sidx
             const int lb0 = fs0 ? cs1 - nM0 : 0, lb1 = fs1 ? n - nM1 : cs1;     // larger side
+            // ---- the directions of the deferred moves, one lane per queued row
+            if (kOnePass && !BATCH) {
+                constexpr int iMv = prog_index(PROG, kRandomMove, kWeightedMove);
+                constexpr bool kWeightedMv = PROG > 0 && prog_act(PROG, iMv > 0 ? iMv : 0) == kWeightedMove;
+                for (int t = lane; t < nmv; t += 32) {
+                    const int row = W.mq[t];
+                    const int lc = row >= cs1 ? 1 : 0;
+                    W.st[row] = (uint16_t)(W.st[row] | move_direction<kWeightedMv>(W.cv[lc], W.wt32[lc], W.wnever[lc],
+                                                                                   W.mu2[t]));
+                }
+                __syncwarp();
+            }
             // ---- ID ranks of every list entry within its own list, one pass over
             // both cells: entry k goes to sidx[region + rank].  IDs are compared by
             // their low words while all high words are zero, else in full.
