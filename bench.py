@@ -48,6 +48,8 @@ WORKLOADS = {
     "medium": lambda seed: configs.single_large_run(seed, n=192, agents=8_000_000),
     "plain": lambda seed: configs.plain_method(seed),
     "genetics": lambda seed: configs.genetics_run(seed),
+    # a smaller case of the genetics run's actions for profiler captures
+    "genetics_small": lambda seed: configs.genetics_run(seed, agents=1_000_000, n=64),
 }
 AGENT_BYTES = 60   # one read and one write of the 30-byte hot record per agent-step
 BIRTH_BYTES = 3 * 1024   # genetics: two parent genomes read, one child genome written (2 x 4,096 loci)
@@ -546,21 +548,29 @@ def measure_ensemble(n_runs: int, steps: int, device: int, plain_runs: int, seed
                  stage_capacity=n0, device=device)
     ids = [b.add_run(s.grid, s.actions, s.seed, s.agents) for s in specs]
     b.step(1)   # the runs' agents enter the table
+    # the autotuner (re)tunes whenever the batch enters another size bucket
+    # (the ensemble shrinks); its trial steps are simulation steps, timed
+    # apart from the measured chunks, and the first steps after a change of
+    # launch (graph capture) are not timed either
     tuner = Autotuner(trial_steps=2, span=2)
-    shape = tuner.tune(b)
-    done = b.steps_done(ids[0])
-    left = steps - done
-    b.step(1)   # graph of the other table parity
-    left -= 1
-    ms_b, as_b = 0.0, 0
-    n_start = b.num_agents()
-    while left > 0:
-        k = min(left, 200)
+    ms_b, as_b, timed_steps = 0.0, 0, 0
+    last = None
+    while True:
+        left = steps - b.steps_done(ids[0])
+        if left <= 0:
+            break
+        launch = tuner.tune(b)
+        left = steps - b.steps_done(ids[0])
+        if launch != last:
+            b.step(min(2, left))   # graphs of both table parities
+            last = launch
+            continue
+        k = min(left, 50)
+        n_start = b.num_agents()
         ms_b += b.step_timed(k)
         live = b.live_history(k)
         as_b += n_start + int(live[:-1].sum())
-        n_start = int(live[-1])
-        left -= k
+        timed_steps += k
     finals = [len(b.agents(r, sort_by_id=False)) for r in ids]
     hist = b.live_history(steps + 1)
     b.close()
@@ -590,9 +600,13 @@ def measure_ensemble(n_runs: int, steps: int, device: int, plain_runs: int, seed
         "value": bat, "unit": "agent-steps/s", "plain_value": pla,
         "speedup_vs_plain": bat / pla if pla > 0 else None,
         "runs": n_runs, "steps_per_run": steps, "initial_agents": n0, "cells": cells,
-        "timed_steps": steps - done - 1, "batched_ms": ms_b, "plain_runs": np_runs, "plain_ms": ms_p,
-        "shape": {"actions_ctas_per_sm": shape[0], "scatter_ctas_per_sm": shape[1],
-                  "trials": [[list(c), t] for c, t in tuner.trials.get(Autotuner.bucket(n0), [])]},
+        "timed_steps": timed_steps, "batched_ms": ms_b, "plain_runs": np_runs, "plain_ms": ms_p,
+        "launch_tuning": {
+            "knobs": "actions CTAs/SM, scatter CTAs/SM, scan cells per thread (0: by grid size), "
+                     "warp-per-cell form from this mean occupancy (0: default 24)",
+            "bucket": "(log2 agents, log2 mean agents per non-empty cell)",
+            "table": {str(list(k)): list(v) for k, v in tuner.table.items()},
+            "trials_ms_per_agent_step": {str(list(k)): [[list(c), t] for c, t in v] for k, v in tuner.trials.items()}},
         "final_agents": int(sum(finals)),
         "e2e": {"value": as_job / t_job, "unit": "agent-steps/s", "job_s": t_job,
                 "plain_value": as_p_all / wall_p if wall_p > 0 else None, "plain_job_s": wall_p,

@@ -332,6 +332,23 @@ int qhg_host_buffer_free(void *p);
 int qhg_batch_set_shape(qhg_batch *batch, int32_t actions_ctas_per_sm, int32_t scatter_ctas_per_sm);
 int qhg_batch_get_shape(qhg_batch *batch, int32_t *actions_ctas_per_sm, int32_t *scatter_ctas_per_sm,
                         int32_t *max_actions, int32_t *max_scatter);
+/* The batch's launch tuning (what its autotuner searches; results do not
+ * depend on it): CTAs per SM of the action kernel and of the scatter, cells
+ * per thread of the cell scan (1 or 2; 0: chosen from the grid size), and
+ * the mean occupancy of the non-empty cells from which a step runs the
+ * warp-per-cell form instead of cell-aligned tiles (0: the default, 24).
+ * Waits for the batch; the form threshold applies from the next step's
+ * commit on. */
+typedef struct {
+    int32_t actions_ctas_per_sm;
+    int32_t scatter_ctas_per_sm;
+    int32_t scan_cells_per_thread;
+    int32_t dense_cell;
+} qhg_batch_launch;
+int qhg_batch_set_launch(qhg_batch *batch, const qhg_batch_launch *launch);
+int qhg_batch_get_launch(qhg_batch *batch, qhg_batch_launch *launch);
+/* agents and non-empty cells of the batch's table (waits for the batch) */
+int qhg_batch_table_info(qhg_batch *batch, int64_t *n_agents, int64_t *n_nonempty_cells);
 int qhg_batch_stream(qhg_batch *batch, void **stream);
 int qhg_batch_destroy(qhg_batch *batch);
 

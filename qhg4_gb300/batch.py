@@ -6,10 +6,11 @@ populations per run) are admitted into one batch, stepped together by one
 launch of each step kernel over all runs, and removed when done. Every run's
 results equal those of the same run alone through ``GpuRun``.
 
-``Autotuner`` picks the launch shape of the persistent kernels (CTAs per SM
-of the action and scatter kernels) per size bucket of the batch, by timing
-real steps of the batch with each candidate; because results do not depend
-on the shape, tuning costs no simulation work.
+``Autotuner`` picks the batch's launch tuning (CTAs per SM of the action and
+scatter kernels, cells per scan thread, the occupancy from which steps run
+the warp-per-cell form) per size bucket of the batch, by timing real steps
+of the batch with each candidate; because results do not depend on the
+launch, tuning costs no simulation work.
 """
 from __future__ import annotations
 
@@ -39,6 +40,11 @@ class BatchDesc(ct.Structure):
 
 class BatchRunDesc(ct.Structure):
     _fields_ = [("seed", ct.c_uint64), ("action_param", (ct.c_double * 4) * MAX_ACTIONS)]
+
+
+class BatchLaunch(ct.Structure):
+    _fields_ = [("actions_ctas_per_sm", ct.c_int32), ("scatter_ctas_per_sm", ct.c_int32),
+                ("scan_cells_per_thread", ct.c_int32), ("dense_cell", ct.c_int32)]
 
 
 class BatchRunStatus(ct.Structure):
@@ -176,6 +182,26 @@ class GpuBatch:
         _bcheck(load_library().qhg_batch_get_shape(self.h, ct.byref(a), ct.byref(s), ct.byref(ma), ct.byref(ms)))
         return int(a.value), int(s.value), int(ma.value), int(ms.value)
 
+    def set_launch(self, actions_ctas: int, scatter_ctas: int, scan_cells_per_thread: int = 0,
+                   dense_cell: int = 0) -> None:
+        """The launch tuning: CTAs per SM of the action kernel and scatter,
+        cells per scan thread (0: by grid size), the mean occupancy from
+        which steps run the warp-per-cell form (0: default)."""
+        lb = BatchLaunch(int(actions_ctas), int(scatter_ctas), int(scan_cells_per_thread), int(dense_cell))
+        _bcheck(load_library().qhg_batch_set_launch(self.h, ct.byref(lb)))
+
+    def launch(self) -> Tuple[int, int, int, int]:
+        lb = BatchLaunch()
+        _bcheck(load_library().qhg_batch_get_launch(self.h, ct.byref(lb)))
+        return (int(lb.actions_ctas_per_sm), int(lb.scatter_ctas_per_sm), int(lb.scan_cells_per_thread),
+                int(lb.dense_cell))
+
+    def table_info(self) -> Tuple[int, int]:
+        """Agents and non-empty cells of the batch's table."""
+        n, ne = ct.c_int64(), ct.c_int64()
+        _bcheck(load_library().qhg_batch_table_info(self.h, ct.byref(n), ct.byref(ne)))
+        return int(n.value), int(ne.value)
+
     def close(self) -> None:
         if getattr(self, "h", None):
             load_library().qhg_batch_destroy(self.h)
@@ -190,35 +216,63 @@ class GpuBatch:
 
 @dataclass
 class Autotuner:
-    """Launch shape per size bucket (log2 of the batch's agents), chosen by
-    timing ``trial_steps`` real steps of the batch with every candidate."""
+    """Launch tuning of a batch per size bucket, chosen by timing real steps.
+
+    The bucket is (log2 of the batch's agents, log2 of its mean agents per
+    non-empty cell).  On a bucket's first visit the tuner searches one knob
+    at a time, keeping the best value of each before it moves to the next:
+    CTAs per SM of the action kernel and the scatter (the top ``span``
+    values of each that fit), then cells per thread of the cell scan (1, 2),
+    then the mean occupancy from which steps run the warp-per-cell form
+    (``dense_choices``; below it, cell-aligned tiles of 512 agents in
+    256-thread blocks).  Each candidate is set, stepped once untimed (graph
+    capture, form change) and timed over ``trial_steps`` steps; candidates
+    compare by time per agent-step.  The steps are the batch's own (results
+    do not depend on the launch), so tuning costs no simulation work.  A
+    later visit of a known bucket just sets its entry."""
 
     trial_steps: int = 2
-    span: int = 3          # candidates: the top `span` CTAs-per-SM values of each kernel
-    table: Dict[int, Tuple[int, int]] = field(default_factory=dict)
-    trials: Dict[int, List[Tuple[Tuple[int, int], float]]] = field(default_factory=dict)
+    span: int = 3
+    dense_choices: Tuple[int, ...] = (12, 24, 48)
+    table: Dict[Tuple[int, int], Tuple[int, int, int, int]] = field(default_factory=dict)
+    trials: Dict[Tuple[int, int], List[Tuple[Tuple[int, int, int, int], float]]] = field(default_factory=dict)
+    current: Optional[Tuple[int, int, int, int]] = None
 
     @staticmethod
-    def bucket(n_agents: int) -> int:
-        return int(math.log2(max(1, n_agents)))
+    def bucket(n_agents: int, n_nonempty: int = 1) -> Tuple[int, int]:
+        occ = max(1.0, n_agents / max(1, n_nonempty))
+        return int(math.log2(max(1, n_agents))), int(math.log2(occ))
 
-    def candidates(self, batch: GpuBatch) -> List[Tuple[int, int]]:
-        _, _, ma, ms = batch.shape()
-        return [(a, s) for a in range(max(1, ma - self.span + 1), ma + 1)
-                for s in range(max(1, ms - self.span + 1), ms + 1)]
+    def _time(self, batch: GpuBatch, cand: Tuple[int, int, int, int]) -> float:
+        batch.set_launch(*cand)
+        self.current = cand
+        batch.step(1)
+        n0, _ = batch.table_info()
+        return batch.step_timed(self.trial_steps) / (self.trial_steps * max(1, n0))
 
-    def tune(self, batch: GpuBatch) -> Tuple[int, int]:
-        """Sets the batch's shape for its current size, measuring once per
-        bucket; steps the batch len(candidates) * trial_steps times on a
-        bucket's first visit."""
-        b = self.bucket(batch.num_agents())
+    def tune(self, batch: GpuBatch) -> Tuple[int, int, int, int]:
+        """Sets the batch's launch for its current bucket (searching on the
+        bucket's first visit) and returns it."""
+        n, ne = batch.table_info()
+        b = self.bucket(n, ne)
         if b not in self.table:
+            _, _, ma, ms = batch.shape()
+            best = (ma, ms, 0, 0)
             results = []
-            for cand in self.candidates(batch):
-                batch.set_shape(*cand)
-                batch.step(1)   # graph capture outside the timed steps
-                results.append((cand, batch.step_timed(self.trial_steps) / self.trial_steps))
+
+            def consider(cands):
+                nonlocal best
+                scored = [(c, self._time(batch, c)) for c in cands]
+                results.extend(scored)
+                best = min(scored, key=lambda x: x[1])[0]
+
+            consider([(a, s_, 0, 0) for a in range(max(1, ma - self.span + 1), ma + 1)
+                      for s_ in range(max(1, ms - self.span + 1), ms + 1)])
+            consider([(best[0], best[1], items, 0) for items in (1, 2)])
+            consider([(best[0], best[1], best[2], d) for d in self.dense_choices])
             self.trials[b] = results
-            self.table[b] = min(results, key=lambda x: x[1])[0]
-        batch.set_shape(*self.table[b])
+            self.table[b] = best
+        if self.current != self.table[b]:   # setting it drops the batch's captured step graphs
+            batch.set_launch(*self.table[b])
+            self.current = self.table[b]
         return self.table[b]

@@ -118,7 +118,7 @@ struct qhg_run {
     int32_t upload_step = 0;
     int64_t upload_max_id = -1;
     bool grid_ok = false, agents_ok = false;
-    LaunchShape shape = {1, 1, 1};
+    LaunchShape shape = {1, 1, 1, 0};
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     std::vector<int64_t> stage;  // host staging for uploads
@@ -311,6 +311,7 @@ static int64_t bino_threshold(double L) {
 // execution order; draw windows are handed out in that order.
 int qhg_host_actions(StepConst &P, int n, const int32_t *types, const double (*params)[4], std::string &err) {
     uint32_t w = 0;
+    if (P.dense_cell == 0u) P.dense_cell = kDenseCell;
     for (int a = 0; a < n; a++) {
         ActionConst &A = P.act[a];
         const double *p = params[a];
@@ -817,7 +818,7 @@ extern "C" int qhg_gpu_upload_agents(qhg_run *r, const qhg_agents_soa *a, int64_
     const int64_t maxid = h->next_id;
     const uint32_t live = h->new_n_agents;
     const uint32_t nne = h->new_n_nonempty;
-    const uint32_t form = step_form(h->max_cell, live, nne);
+    const uint32_t form = step_form(h->max_cell, live, nne, r->P.dense_cell);
     memset(h, 0, sizeof(RunState));
     h->step = first_step;
     h->n_agents = live;

@@ -62,7 +62,7 @@ struct qhg_batch {
     qhg_batch_desc desc;
     cudaStream_t stream = nullptr;
     StepConst P;
-    LaunchShape shape = {1, 1, 1};
+    LaunchShape shape = {1, 1, 1, 0};
     int nsm = 1, max_ctas_actions = 1, max_ctas_scatter = 1;
     uint32_t cell_cap = 0, agent_cap = 0, stage_cap = 0;
     int max_runs = 0;
@@ -584,6 +584,44 @@ extern "C" int qhg_batch_get_shape(qhg_batch *b, int32_t *actions_ctas_per_sm, i
     if (scatter_ctas_per_sm) *scatter_ctas_per_sm = b->shape.scatter_grid / b->nsm;
     if (max_actions) *max_actions = b->max_ctas_actions;
     if (max_scatter) *max_scatter = b->max_ctas_scatter;
+    return QHG_OK;
+}
+
+extern "C" int qhg_batch_set_launch(qhg_batch *b, const qhg_batch_launch *l) {
+    if (b == nullptr || l == nullptr) return bfail(QHG_ERR_ARG, "null argument");
+    if (l->actions_ctas_per_sm < 1 || l->actions_ctas_per_sm > b->max_ctas_actions || l->scatter_ctas_per_sm < 1 ||
+        l->scatter_ctas_per_sm > b->max_ctas_scatter) {
+        return bfail(QHG_ERR_ARG, "CTAs per SM outside what fits");
+    }
+    if (l->scan_cells_per_thread < 0 || l->scan_cells_per_thread > 2) {
+        return bfail(QHG_ERR_ARG, "scan cells per thread must be 0 (by grid size), 1 or 2");
+    }
+    if (l->dense_cell < 0 || l->dense_cell > 256) return bfail(QHG_ERR_ARG, "dense_cell must be 0 (default) .. 256");
+    int rc = qhg_batch_sync(b);   // the form threshold takes effect at the next commit
+    if (rc != QHG_OK) return rc;
+    b->shape.actions_grid = b->nsm * l->actions_ctas_per_sm;
+    b->shape.scatter_grid = b->nsm * l->scatter_ctas_per_sm;
+    b->shape.scan_items = l->scan_cells_per_thread;
+    b->P.dense_cell = l->dense_cell > 0 ? (uint32_t)l->dense_cell : kDenseCell;
+    drop_graphs(b);
+    return QHG_OK;
+}
+
+extern "C" int qhg_batch_get_launch(qhg_batch *b, qhg_batch_launch *l) {
+    if (b == nullptr || l == nullptr) return bfail(QHG_ERR_ARG, "null argument");
+    l->actions_ctas_per_sm = b->shape.actions_grid / b->nsm;
+    l->scatter_ctas_per_sm = b->shape.scatter_grid / b->nsm;
+    l->scan_cells_per_thread = b->shape.scan_items;
+    l->dense_cell = (int32_t)b->P.dense_cell;
+    return QHG_OK;
+}
+
+extern "C" int qhg_batch_table_info(qhg_batch *b, int64_t *n_agents, int64_t *n_nonempty_cells) {
+    if (b == nullptr) return bfail(QHG_ERR_ARG, "null batch");
+    int rc = qhg_batch_sync(b);
+    if (rc != QHG_OK) return rc;
+    if (n_agents) *n_agents = b->h_rs->n_agents;
+    if (n_nonempty_cells) *n_nonempty_cells = b->h_rs->n_nonempty;
     return QHG_OK;
 }
 

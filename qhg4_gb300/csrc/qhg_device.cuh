@@ -35,10 +35,13 @@ struct Tile {
 constexpr uint32_t kFormTile = 0u, kFormBig = 1u, kFormCell = 2u;
 constexpr uint32_t kDenseCell = 24u;
 constexpr int kMaxCellWarp = 256;        // agents per cell of the warp-per-cell kernels
-__host__ __device__ inline uint32_t step_form(uint32_t max_cell, uint32_t n_agents, uint32_t n_nonempty) {
+// dense: the mean occupancy of the non-empty cells from which the
+// warp-per-cell form runs (kDenseCell unless a batch's launch tuning sets it)
+__host__ __device__ inline uint32_t step_form(uint32_t max_cell, uint32_t n_agents, uint32_t n_nonempty,
+                                              uint32_t dense = kDenseCell) {
     if (max_cell > (uint32_t)kMaxCell) return kFormBig;
     if (max_cell > (uint32_t)kMaxCellWarp) return kFormTile;
-    return ((uint64_t)n_agents >= (uint64_t)kDenseCell * n_nonempty) ? kFormCell : kFormTile;
+    return ((uint64_t)n_agents >= (uint64_t)dense * n_nonempty) ? kFormCell : kFormTile;
 }
 // bytes every agent column is allocated beyond its rows: bulk copies read
 // whole 16-byte units around a row range
@@ -143,6 +146,7 @@ struct StepConst {
     int32_t program;         // specialised action program (0: interpreted)
     int32_t has_move;        // RandomMove or WeightedMove present
     int32_t has_wmove;       // WeightedMove present
+    uint32_t dense_cell;     // mean occupancy from which a step runs the warp-per-cell form (step_form)
     ActionConst act[kMaxActions];
 };
 
@@ -272,6 +276,7 @@ struct LaunchShape {
     int actions_grid;
     int scatter_grid;
     int big_grid;      // CTAs of the big-cell forms (one per SM)
+    int scan_items;    // cells per thread of the cell scan (1 or 2; 0: chosen from the grid size)
 };
 
 // ------------------------------------------------------------- Philox

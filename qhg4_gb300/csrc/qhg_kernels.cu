@@ -1270,7 +1270,7 @@ __device__ __forceinline__ void commit_step(const StepConst &P, const BatchBuffe
         nx[0] = 0ull; nx[1] = 0ull; nx[2] = 0ull; nx[3] = 0ull;
         rs->n_agents = rs->new_n_agents;
         rs->n_nonempty = rs->new_n_nonempty;
-        rs->form_next = step_form(rs->max_cell, rs->new_n_agents, rs->new_n_nonempty);
+        rs->form_next = step_form(rs->max_cell, rs->new_n_agents, rs->new_n_nonempty, P.dense_cell);
         if (BIG) rs->form = rs->form_next;
         rs->max_cell = 0u;
         rs->next_id += (int64_t)rs->births;
@@ -3141,7 +3141,7 @@ static void launch_scan(const StepLaunch &S) {
     const BatchBuffers &BB = S.BB;
     cudaStream_t stream = S.stream;
     const bool batch = S.batch;
-    const int sitems = scan_items(P->num_cells);
+    const int sitems = S.L.scan_items > 0 ? std::min(S.L.scan_items, 2) : scan_items(P->num_cells);
     const int ntiles = (P->num_cells + kScanThreads * sitems - 1) / (kScanThreads * sitems);
     const int ms_grid = std::max(1, std::min((P->num_cells + 7) / 8, 152 * 16));
     if (!batch && B->ms_mode >= 0) {

@@ -40,7 +40,8 @@ EXPORTS = [
     "qhg_batch_set_shape", "qhg_batch_get_shape", "qhg_batch_stream", "qhg_batch_destroy",
     "qhg_batch_live_history", "qhg_batch_snapshot_async", "qhg_batch_snapshot_wait",
     "qhg_host_buffer_alloc", "qhg_host_buffer_free", "qhg_gpu_next_id", "qhg_gpu_set_next_id",
-    "qhg_gpu_test_stall_scan", "qhg_gpu_occupancy", "qhg_gpu_set_capacity", "qhg_gpu_set_move_weights", "qhg_gpu_set_ice", "qhg_gpu_stats_async",
+    "qhg_gpu_test_stall_scan", "qhg_gpu_occupancy", "qhg_gpu_set_capacity", "qhg_gpu_set_move_weights", "qhg_gpu_set_ice", "qhg_gpu_stats_async", "qhg_batch_set_launch", "qhg_batch_get_launch",
+    "qhg_batch_table_info",
     "qhg_gpu_move_stats_enable", "qhg_gpu_move_stats", "qhg_gpu_set_move_stats", "qhg_gpu_set_occupancy",
 ]
 
@@ -139,6 +140,9 @@ def load_library(path: str = LIB_PATH):
         "qhg_gpu_set_move_weights": (I, [P, P]),
         "qhg_gpu_set_ice": (I, [P, P]),
         "qhg_gpu_stats_async": (I, [P, P]),
+        "qhg_batch_set_launch": (I, [P, P]),
+        "qhg_batch_get_launch": (I, [P, P]),
+        "qhg_batch_table_info": (I, [P, P, P]),
         "qhg_gpu_move_stats_enable": (I, [P, ct.c_int32, P, P, ct.c_double, ct.c_int32]),
         "qhg_gpu_move_stats": (I, [P, P, P, P]),
         "qhg_gpu_set_move_stats": (I, [P, P, P, P]),

@@ -80,8 +80,13 @@ def test_batch_shape_does_not_change_results(gpu_lib):
     for k, (sa, ss) in enumerate(((1, 1), (ma, 1), (1, ms), (ma, ms))):
         b.set_shape(sa, ss)
         b.step(3)
-    tuner = Autotuner(trial_steps=1)
+    b.set_launch(ma, ms, 2, 200)   # wide scan tiles; warp-per-cell form only above 200 per cell
+    b.step(3)
+    b.set_launch(1, 1, 1, 2)       # narrow scan tiles; warp-per-cell form from 2 per cell
+    b.step(3)
+    tuner = Autotuner(trial_steps=1, span=2)
     tuner.tune(b)
+    assert tuner.table and len(tuner.trials[next(iter(tuner.trials))]) == 4 + 2 + 3
     b.step(2)
     for k, r in enumerate(ids):
         same_as_alone(b, r, cases[k], b.steps_done(r))
