@@ -225,9 +225,10 @@ class Autotuner:
     values of each that fit), then cells per thread of the cell scan (1, 2),
     then the mean occupancy from which steps run the warp-per-cell form
     (``dense_choices``; below it, cell-aligned tiles of 512 agents in
-    256-thread blocks).  Each candidate is set, stepped once untimed (graph
-    capture, form change) and timed over ``trial_steps`` steps; candidates
-    compare by time per agent-step.  The steps are the batch's own (results
+    256-thread blocks).  Each candidate is set, stepped twice untimed (the
+    step graphs of both table parities captured, the form changed) and
+    timed over ``trial_steps`` steps; candidates compare by time per
+    agent-step.  The steps are the batch's own (results
     do not depend on the launch), so tuning costs no simulation work.  A
     later visit of a known bucket just sets its entry."""
 
@@ -246,7 +247,7 @@ class Autotuner:
     def _time(self, batch: GpuBatch, cand: Tuple[int, int, int, int]) -> float:
         batch.set_launch(*cand)
         self.current = cand
-        batch.step(1)
+        batch.step(2)   # step graphs of both table parities captured (and the form applied) untimed
         n0, _ = batch.table_info()
         return batch.step_timed(self.trial_steps) / (self.trial_steps * max(1, n0))
 
