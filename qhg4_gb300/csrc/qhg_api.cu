@@ -91,8 +91,6 @@ struct qhg_run {
     float *d_age[2] = {nullptr, nullptr};
     float *d_lastb[2] = {nullptr, nullptr};
     uint8_t *d_meta[2] = {nullptr, nullptr};
-    uint16_t *d_st[2] = {nullptr, nullptr};   // next-step action states per table (single runs, cell form)
-    ulonglong2 *d_vthr_cell = nullptr;         // the next step's Verhulst thresholds by cell
     uint32_t *d_ne[2] = {nullptr, nullptr};    // non-empty cells in index order
     uint32_t *d_necm[2] = {nullptr, nullptr};  // their move words, by position in that list
     uint32_t *d_nes[2] = {nullptr, nullptr};   // their first rows (+ agent count)
@@ -130,8 +128,6 @@ static void free_agents(qhg_run *r) {
     for (int p = 0; p < 2; p++) {
         cudaFree(r->d_id[p]); cudaFree(r->d_birth[p]); cudaFree(r->d_age[p]); cudaFree(r->d_lastb[p]);
         cudaFree(r->d_meta[p]); cudaFree(r->d_ne[p]); cudaFree(r->d_nes[p]); cudaFree(r->d_tf[p]);
-        cudaFree(r->d_st[p]);
-        r->d_st[p] = nullptr;
         cudaFree(r->d_necm[p]);
         r->d_tf[p] = nullptr; r->d_necm[p] = nullptr;
         r->d_id[p] = nullptr; r->d_birth[p] = r->d_age[p] = r->d_lastb[p] = nullptr;
@@ -654,8 +650,7 @@ extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_
         }
     }
     cudaFree(r->d_nbr); cudaFree(r->d_nnbr); cudaFree(r->d_rev); cudaFree(r->d_K); cudaFree(r->d_vthr[0]); cudaFree(r->d_vthr[1]);
-    cudaFree(r->d_wthr); cudaFree(r->d_cmove); cudaFree(r->d_occ); cudaFree(r->d_vthr_cell);
-    r->d_vthr_cell = nullptr;
+    cudaFree(r->d_wthr); cudaFree(r->d_cmove); cudaFree(r->d_occ);
     cudaFree(r->d_clsc); cudaFree(r->d_sbase); cudaFree(r->d_bbase); cudaFree(r->d_bidb);
     cudaFree(r->d_obase); cudaFree(r->d_tflag); cudaFree(r->d_tagg); cudaFree(r->d_tincl);
     ms_free(r);
@@ -670,7 +665,6 @@ extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_
     CUDA_TRY(cudaMalloc(&r->d_rev, (size_t)C * sizeof(uint32_t)));
     CUDA_TRY(cudaMalloc(&r->d_K, (size_t)C * sizeof(double)));
     CUDA_TRY(cudaMalloc(&r->d_vthr[0], (size_t)C * sizeof(ulonglong2)));
-    CUDA_TRY(cudaMalloc(&r->d_vthr_cell, (size_t)C * sizeof(ulonglong2)));
     CUDA_TRY(cudaMalloc(&r->d_vthr[1], (size_t)C * sizeof(ulonglong2)));
     CUDA_TRY(cudaMalloc(&r->d_wthr, (size_t)C * 6 * sizeof(uint64_t)));
     CUDA_TRY(cudaMalloc(&r->d_cmove, (size_t)C * sizeof(uint32_t)));
@@ -715,7 +709,6 @@ static int alloc_agents(qhg_run *r, uint32_t cap) {
         CUDA_TRY(cudaMalloc(&r->d_age[p], (size_t)cap * sizeof(float) + kColumnPad));
         CUDA_TRY(cudaMalloc(&r->d_lastb[p], (size_t)cap * sizeof(float) + kColumnPad));
         CUDA_TRY(cudaMalloc(&r->d_meta[p], (size_t)cap + kColumnPad));
-        CUDA_TRY(cudaMalloc(&r->d_st[p], (size_t)cap * sizeof(uint16_t) + kColumnPad));
         CUDA_TRY(cudaMalloc(&r->d_ne[p], (size_t)C * sizeof(uint32_t)));
         CUDA_TRY(cudaMalloc(&r->d_necm[p], (size_t)C * sizeof(uint32_t)));
         CUDA_TRY(cudaMalloc(&r->d_nes[p], (size_t)(C + 1) * sizeof(uint32_t)));
@@ -860,7 +853,6 @@ static StepBuffers make_buffers(qhg_run *r, int cur) {
     B.nonempty = r->d_ne[cur]; B.ne_start = r->d_nes[cur]; B.tile_first = r->d_tf[cur];
     B.id = r->d_id[cur]; B.birth = r->d_birth[cur]; B.age = r->d_age[cur]; B.lastb = r->d_lastb[cur];
     B.meta = r->d_meta[cur];
-    B.st = r->d_st[cur]; B.st2 = r->d_st[nx]; B.vthr_cell = r->d_vthr_cell;
     B.nonempty2 = r->d_ne[nx]; B.ne_start2 = r->d_nes[nx]; B.tile_first2 = r->d_tf[nx];
     B.id2 = r->d_id[nx]; B.birth2 = r->d_birth[nx]; B.age2 = r->d_age[nx]; B.lastb2 = r->d_lastb[nx];
     B.meta2 = r->d_meta[nx];
@@ -1006,10 +998,6 @@ extern "C" int qhg_gpu_sync(qhg_run *r) {
 // The current table's per-cell constants after K or the move weights changed
 // (nothing to do before agents are uploaded: the upload derives them).
 static int refresh_cells(qhg_run *r) {
-    // the action states the last step stored used the old constants
-    r->h_rs->st_valid = 0u;
-    CUDA_TRY(cudaMemsetAsync(reinterpret_cast<char *>(r->d_rs) + offsetof(RunState, st_valid), 0, sizeof(uint32_t),
-                             r->stream));
     if (!r->agents_ok || r->h_rs->n_nonempty == 0u) {
         CUDA_TRY(cudaStreamSynchronize(r->stream));
         return QHG_OK;
@@ -1436,7 +1424,7 @@ extern "C" int qhg_gpu_destroy(qhg_run *r) {
     drop_graphs(r);
     free_agents(r);
     cudaFree(r->d_nbr); cudaFree(r->d_nnbr); cudaFree(r->d_rev); cudaFree(r->d_K); cudaFree(r->d_vthr[0]); cudaFree(r->d_vthr[1]);
-    cudaFree(r->d_wthr); cudaFree(r->d_cmove); cudaFree(r->d_occ); cudaFree(r->d_vthr_cell);
+    cudaFree(r->d_wthr); cudaFree(r->d_cmove); cudaFree(r->d_occ);
     cudaFree(r->d_clsc); cudaFree(r->d_sbase); cudaFree(r->d_bbase); cudaFree(r->d_bidb);
     cudaFree(r->d_obase); cudaFree(r->d_tflag); cudaFree(r->d_tagg); cudaFree(r->d_tincl);
     ms_free(r);

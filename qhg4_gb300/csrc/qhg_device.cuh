@@ -183,10 +183,6 @@ struct RunState {
     // (GetOld or OldAgeDeath): once a step has run, the table's age column is
     // not kept up to date; its ages are (float)(step - 1) - birth
     uint32_t age_derived;
-    // the table's action-state column holds every row's state for the step
-    // (written by the previous step's warp-per-cell scatter; cleared by an
-    // upload and by changes of K, move weights or ice)
-    uint32_t st_valid;
     // statistics ring: [step % kStatsRing][live, births, deaths, moves]
     unsigned long long stats[kStatsRing][4];
 };
@@ -199,10 +195,6 @@ struct StepBuffers {
     // tile_first[t]: index of the first non-empty cell of tile t (ceil(N/kTileAgents)+1 entries)
     const uint32_t *nonempty; const uint32_t *ne_start; const uint32_t *tile_first;
     const int64_t *id; const float *birth; const float *age; const float *lastb; const uint8_t *meta;
-    // single runs: each agent's action state for the step (cell_state_word),
-    // written by the previous step's warp-per-cell scatter, and the same for
-    // the next table; the next step's Verhulst thresholds by cell (null: none)
-    const uint16_t *st; uint16_t *st2; ulonglong2 *vthr_cell;
     uint32_t *nonempty2; uint32_t *ne_start2; uint32_t *tile_first2;
     int64_t *id2; float *birth2; float *age2; float *lastb2; uint8_t *meta2;
     // rev packs, 3 bits per neighbour slot q, the slot of this cell in the

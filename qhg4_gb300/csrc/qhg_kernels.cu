@@ -397,9 +397,6 @@ constexpr uint32_t kStDeadM = 128u;    // Verhulst kills it (with a mate)
 constexpr uint32_t kStBirthM = 256u;   // gives birth (with a mate)
 constexpr int kStOad = 9;              // bits 9-10, OldAgeDeath: 0 survives, 1 dies, 2 inside the window
 constexpr uint32_t kStMoveDraw = 2048u; // the move draw passed: the direction is decided later (deferred move)
-// bits of the states the warp-per-cell scatter stores for the next step
-constexpr uint32_t kStPairFert = 4096u; // the table's FERTILE flag (what RandomPair pairs by)
-constexpr uint32_t kStNone = 8192u;     // no state stored (a mover): the action kernel computes it
 
 // With DEFER the move's direction is left out: an agent whose move draw
 // passes gets kStMoveDraw and its direction draw in u2out, and move_direction
@@ -994,7 +991,7 @@ __global__ void __launch_bounds__(kScanThreads)
 k_cell_scan(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
             const int32_t *__restrict__ nbr, const uint8_t *__restrict__ nnbr,
             const uint32_t *__restrict__ rev, const uint32_t *__restrict__ clsc,
-            const double *__restrict__ Kc, ulonglong2 *__restrict__ vthr, ulonglong2 *__restrict__ vthr_cell,
+            const double *__restrict__ Kc, ulonglong2 *__restrict__ vthr,
             const uint32_t *__restrict__ cmove, uint32_t *__restrict__ necm,
             uint32_t *__restrict__ sbase, uint32_t *__restrict__ bbase,
             uint32_t *__restrict__ bidbase, uint32_t *__restrict__ obase,
@@ -1203,9 +1200,7 @@ k_cell_scan(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                 // its position in the next table's non-empty list
                 if (P.n_verhulst > 0) {
                     if (!BATCH) {
-                        const ulonglong2 vt = verhulst_thresholds(P.act[P.verhulst_act[0]], Kc[d], nnew[j]);
-                        vthr[pre.ne] = vt;
-                        if (vthr_cell != nullptr) vthr_cell[d] = vt;   // for the scatter's next-step states
+                        vthr[pre.ne] = verhulst_thresholds(P.act[P.verhulst_act[0]], Kc[d], nnew[j]);
                     } else if (crn[j] != kNoRun) {
                         vthr[pre.ne] = verhulst_thresholds(BB.runs[crn[j]].act[P.verhulst_act[0]], Kc[d], nnew[j]);
                     }
@@ -1239,7 +1234,7 @@ k_cell_scan(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
 // form applies it).  Every thread of the CTA calls it; `flag` is a shared word.
 template <bool BATCH, bool BIG>
 __device__ __forceinline__ void commit_step(const StepConst &P, const BatchBuffers &BB, RunState *__restrict__ rs,
-                                            uint32_t *flag, uint32_t st_valid) {
+                                            uint32_t *flag) {
     const int tid = threadIdx.x;
     __syncthreads();
     if (tid == 0) {
@@ -1290,7 +1285,6 @@ __device__ __forceinline__ void commit_step(const StepConst &P, const BatchBuffe
             rs->genome_step = (int32_t)step;
         }
         if (!BATCH && P.age_from_birth) rs->age_derived = 1u;
-        if (!BATCH) rs->st_valid = st_valid;   // the next table's action states are stored
         rs->step = (int32_t)(step + 1u);
         __threadfence();
     }
@@ -1574,7 +1568,7 @@ k_scatter(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
         }
         par ^= 1u;
     }
-    commit_step<BATCH, BIG>(P, BB, rs, &S.last, 0u);
+    commit_step<BATCH, BIG>(P, BB, rs, &S.last);
 }
 
 // ------------------------------------------------------ warp-per-cell kernels
@@ -1623,7 +1617,7 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                const ulonglong2 *__restrict__ vthr, const uint64_t *__restrict__ wthr,
                const uint32_t *__restrict__ necm,
                uint32_t *__restrict__ outc, int32_t *__restrict__ father, uint16_t *__restrict__ brank,
-               uint32_t *__restrict__ clsc, const uint16_t *__restrict__ stin) {
+               uint32_t *__restrict__ clsc) {
     extern __shared__ __align__(16) unsigned char qhg_smem[];
     __shared__ uint32_t red[kCellWarps];
     CellWarpSmem &W = reinterpret_cast<CellWarpSmem *>(qhg_smem)[threadIdx.x >> 5];
@@ -1637,9 +1631,6 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
     // FERTILE lists (keeping both outcomes where the outcome depends on a
     // mate), the outcome is settled after the pairing
     constexpr bool kOnePass = PROG > 0;
-    // the previous step's scatter stored every row's action state (kStNone
-    // for movers, whose states a dense pass computes here)
-    const bool pre = !BATCH && kOnePass && stin != nullptr && rs->st_valid != 0u;
     const int lane = threadIdx.x & 31;
     const uint32_t lt = lanemask_lt();
     const int32_t step = rs->step;
@@ -1745,23 +1736,16 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                     uint8_t m8 = 0;
                     int64_t xid = 0;
                     float fb = 0.0f, fa = 0.0f, fl = 0.0f;
-                    uint32_t s16 = 0u;
                     if (kp) {
                         const uint32_t g = s + (uint32_t)row;
-                        if (pre) {
-                            s16 = stin[g];
-                            m8 = (uint8_t)(((s16 & kStGender) ? kMetaGender : 0) | ((s16 & kStPairFert) ? kMetaFertile : 0));
+                        if (kOnePass || P.has_pair) {
+                            m8 = meta[g];
                             xid = id[g];
-                        } else {
-                            if (kOnePass || P.has_pair) {
-                                m8 = meta[g];
-                                xid = id[g];
-                            }
-                            if (kOnePass || kEarlyOad) fb = birth[g];
-                            if (kOnePass) {
-                                if (P.reads_age) fa = derived ? __fsub_rn(fTprev, fb) : age[g];
-                                fl = lastb[g];
-                            }
+                        }
+                        if (kOnePass || kEarlyOad) fb = birth[g];
+                        if (kOnePass) {
+                            if (P.reads_age) fa = derived ? __fsub_rn(fTprev, fb) : age[g];
+                            fl = lastb[g];
                         }
                     }
                     const bool fert = P.has_pair && (m8 & kMetaFertile) != 0;
@@ -1769,19 +1753,14 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                     const int64_t x = fert ? xid : 0;
                     uint32_t stt = 0u;
                     if (kOnePass && kp) {
-                        if (pre) {
-                            stt = s16;
-                        } else {
-                            const BatchRun *R = BATCH ? BB.runs + W.run[lc] : nullptr;
-                            stt = agent_state<PROG, BATCH, !BATCH>(P, R, step, fT, xid, m8, fb, fa, fl, W.cv[lc],
-                                                                   W.wt32[lc], W.wnever[lc], &mu2);
-                        }
+                        const BatchRun *R = BATCH ? BB.runs + W.run[lc] : nullptr;
+                        stt = agent_state<PROG, BATCH, !BATCH>(P, R, step, fT, xid, m8, fb, fa, fl, W.cv[lc],
+                                                               W.wt32[lc], W.wnever[lc], &mu2);
                         W.st[row] = (uint16_t)stt;
                     }
                     if (kOnePass && !BATCH) {
-                        // deferred moves (rows whose move draw passed), or with stored
-                        // states the rows that have none: queued for a dense pass
-                        const bool mv = (stt & (pre ? kStNone : kStMoveDraw)) != 0u;
+                        // deferred moves: queue the rows whose move draw passed
+                        const bool mv = (stt & kStMoveDraw) != 0u;
                         const uint32_t mm = __ballot_sync(FULL_MASK, mv);
                         if (mv) {
                             const int qp = nmv + __popc(mm & lt);
@@ -1837,41 +1816,8 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
             const uint32_t nL0 = (uint32_t)(fs0 ? nM0 : nF0), nL1 = (uint32_t)(fs1 ? nM1 : nF1);
             const int sb0 = fs0 ? 0 : cs1 - nM0, sb1 = fs1 ? cs1 : n - nM1;     // smaller side in sidx
             const int lb0 = fs0 ? cs1 - nM0 : 0, lb1 = fs1 ? n - nM1 : cs1;     // larger side
-            // ---- with stored states: the states of the rows without one (movers
-            // of the previous step), one lane per queued row; OldAgeDeath marks
-            if (pre) {
-                for (int t0 = 0; t0 < nmv; t0 += 32) {
-                    const int t = t0 + lane;
-                    bool inw = false;
-                    int row = 0;
-                    if (t < nmv) {
-                        row = W.mq[t];
-                        const int lc = row >= cs1 ? 1 : 0;
-                        const uint32_t g = s + (uint32_t)row;
-                        const uint32_t s16 = W.st[row];
-                        const uint8_t m8 = (uint8_t)(((s16 & kStGender) ? kMetaGender : 0) |
-                                                     ((s16 & kStPairFert) ? kMetaFertile : 0));
-                        const float fb = birth[g];
-                        const float fa = P.reads_age ? (derived ? __fsub_rn(fTprev, fb) : age[g]) : 0.0f;
-                        const uint32_t stt = agent_state<PROG, false, false>(P, nullptr, step, fT, id[g], m8, fb, fa,
-                                                                             lastb[g], W.cv[lc], W.wt32[lc],
-                                                                             W.wnever[lc]);
-                        W.st[row] = (uint16_t)stt;
-                        if (kEarlyOad) {
-                            const bool may_live = !(stt & kStDeadU) || ((stt & kStMateDep) && !(stt & kStDeadM));
-                            inw = ((stt >> kStOad) & 3u) == 2u && may_live;
-                        }
-                    }
-                    if (kEarlyOad) {
-                        const uint32_t qm = __ballot_sync(FULL_MASK, inw);
-                        if (inw) W.oq[nq + __popc(qm & lt)] = (uint16_t)row;
-                        nq += __popc(qm);
-                    }
-                }
-                __syncwarp();
-            }
             // ---- the directions of the deferred moves, one lane per queued row
-            if (kOnePass && !BATCH && !pre) {
+            if (kOnePass && !BATCH) {
                 constexpr int iMv = prog_index(PROG, kRandomMove, kWeightedMove);
                 constexpr bool kWeightedMv = PROG > 0 && prog_act(PROG, iMv > 0 ? iMv : 0) == kWeightedMove;
                 for (int t = lane; t < nmv; t += 32) {
@@ -2185,14 +2131,7 @@ __device__ __forceinline__ void stage_range(uint32_t a, uint32_t n, uint32_t ele
     head = (uint32_t)(lo - off);
 }
 
-// With PROG > 0 (a single run's specialised program, ages derived from
-// birth times) the scatter also stores every stayer's and newborn's action
-// state for the next step (agent_state with the cell's next-step constants:
-// the agent's Philox block, Fertility, Verhulst, the move, the OldAgeDeath
-// window), so that the next step's action kernel reads two bytes in place
-// of the agent's birth and last birth times and runs no Philox for it;
-// movers, whose next cell is another one, get kStNone.
-template <bool BATCH, int PROG>
+template <bool BATCH>
 __global__ void __launch_bounds__(kCellThreads, 4)
 k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
                const uint32_t *__restrict__ nonempty, const uint32_t *__restrict__ ne_start,
@@ -2208,15 +2147,10 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                int64_t *__restrict__ blog, uint64_t blog_cap,
                const int32_t *__restrict__ gslot, int32_t *__restrict__ gslot2,
                const uint32_t *__restrict__ freelist, uint32_t *__restrict__ freelist2,
-               uint32_t *__restrict__ brec, const uint64_t *__restrict__ wthr, const uint32_t *__restrict__ cmove,
-               const ulonglong2 *__restrict__ vthr_cell, uint16_t *__restrict__ st2) {
+               uint32_t *__restrict__ brec) {
     extern __shared__ __align__(16) unsigned char qhg_smem[];
     __shared__ uint32_t s_flag;
     __shared__ __align__(8) uint64_t s_bar[kCellWarps][2];
-    // the next-step constants of each warp's cell (next-step states)
-    __shared__ CellView s_cv[kCellWarps];
-    __shared__ __align__(16) uint32_t s_wt[kCellWarps][8];
-    __shared__ uint32_t s_wn[kCellWarps];
     if (rs->error != 0u) return;   // the state stays as before the step
     // the form of the step is read once per CTA (the big form, launched
     // last, applies the next step's form)
@@ -2240,9 +2174,6 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
     // next step, so a newborn never overwrites a parent of the same step
     const bool genetics = P.genome_words > 0;
     const bool age_col = !P.age_from_birth;
-    // next-step states (see above); fT1 is the next step's time
-    const bool states = !BATCH && PROG > 0 && st2 != nullptr && vthr_cell != nullptr && P.age_from_birth;
-    const float fT1 = (float)(rs->step + 1);
     const uint32_t births = rs->births;
     const uint32_t nfree = rs->nfree;
     const uint32_t hwm = rs->hwm;
@@ -2354,37 +2285,6 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
             }
             // the class counts are consumed: clear them for the next step
             if (lane < 2) reinterpret_cast<uint4 *>(clsc + (size_t)c * kCls)[lane] = make_uint4(0u, 0u, 0u, 0u);
-            if (states) {
-                // the cell's constants for the next step, as its action kernel
-                // sets them up: the Verhulst thresholds the cell scan derived
-                // from its new count, the move word, the WeightedMove
-                // thresholds in 32 bits with the unreachable ones marked
-                bool never = false;
-                if (P.has_wmove) {
-                    const uint64_t w = (lane < 6) ? wthr[(size_t)c * 6 + lane] : (1ull << 32);
-                    never = (w >> 32) != 0ull;
-                    if (lane < 8) s_wt[warp][lane] = never ? 0xffffffffu : (uint32_t)w;
-                }
-                const uint32_t nv = __ballot_sync(FULL_MASK, never && lane < 6);
-                if (lane == 8) {
-                    ulonglong2 v = make_ulonglong2(0ull, 0ull);
-                    uint32_t cm = 0u;
-                    if (P.n_verhulst > 0) v = vthr_cell[c];
-                    if (P.has_move) cm = cmove[c];
-                    CellView cv;
-                    cv.tk = (uint32_t)(v.x >> 62);
-                    cv.tb = v.x & ((1ull << 62) - 1ull);
-                    cv.td = v.y;
-                    cv.nn = cm & 7u;
-                    cv.vm = (cm >> 8) & 63u;
-                    cv.wf = (cm >> 16) & 1u;
-                    cv.wv = (cm >> 24) & 63u;
-                    cv.c = c;
-                    s_cv[warp] = cv;
-                    s_wn[warp] = nv & 63u;
-                }
-                __syncwarp();
-            }
         }
         // the rows of the piece, staged
         if (!mbar_wait_bounded(&bar[buf], (parity >> buf) & 1u)) {
@@ -2442,21 +2342,9 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                     birth2[dst] = fb;
                     lastb2[dst] = fl;
                     if (BATCH || !P.age_from_birth) age2[dst] = P.age_from_birth ? __fsub_rn(ft, fb) : fa;
-                    const uint8_t m8n = (uint8_t)(((code & kOutGender) ? kMetaGender : 0) |
-                                                  ((code & kOutFertile) ? kMetaFertile : 0));
-                    meta2[dst] = m8n;
+                    meta2[dst] = (uint8_t)(((code & kOutGender) ? kMetaGender : 0) |
+                                           ((code & kOutFertile) ? kMetaFertile : 0));
                     if (genetics) gslot2[dst] = gs;
-                    if (states) {
-                        uint32_t sw = ((m8n & kMetaGender) ? kStGender : 0u) | ((m8n & kMetaFertile) ? kStPairFert : 0u);
-                        if (k == 1) {
-                            sw |= agent_state<PROG, false, false>(P, nullptr, step + 1, fT1, x, m8n, fb,
-                                                                  P.reads_age ? __fsub_rn(ft, fb) : 0.0f, fl,
-                                                                  s_cv[warp], s_wt[warp], s_wn[warp]);
-                        } else {
-                            sw |= kStNone;
-                        }
-                        st2[dst] = (uint16_t)sw;
-                    }
                 }
             }
             // newborns (SPopulation::createAgentAtIndex, core/SPopulation.cpp:880-900):
@@ -2475,16 +2363,7 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                     birth2[dst] = ft;
                     lastb2[dst] = 0.0f;
                     if (BATCH || !P.age_from_birth) age2[dst] = 0.0f;
-                    const uint8_t m8b = (uint8_t)((u >> 31) ? kMetaGender : kMetaFertile);
-                    meta2[dst] = m8b;
-                    if (states) {
-                        const uint32_t sw = ((m8b & kMetaGender) ? kStGender : 0u) |
-                                            ((m8b & kMetaFertile) ? kStPairFert : 0u) |
-                                            agent_state<PROG, false, false>(P, nullptr, step + 1, fT1, baby, m8b, ft,
-                                                                            0.0f, 0.0f, s_cv[warp], s_wt[warp],
-                                                                            s_wn[warp]);
-                        st2[dst] = (uint16_t)sw;
-                    }
+                    meta2[dst] = (uint8_t)((u >> 31) ? kMetaGender : kMetaFertile);
                     if (genetics) {
                         const uint32_t gr = bid + rk;   // birth rank of the step
                         const uint32_t bs = gr < nfree ? freelist[gr] : hwm + (gr - nfree);
@@ -2532,7 +2411,7 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
             if ((fl >> b) & 1u) mbar_wait_bounded(&bar[b], (parity >> b) & 1u);
         }
     }
-    commit_step<BATCH, false>(P, BB, rs, &s_flag, states ? 1u : 0u);
+    commit_step<BATCH, false>(P, BB, rs, &s_flag);
 }
 
 // ------------------------------------------------------------- occupancy
@@ -3071,11 +2950,11 @@ extern "C" int qhg_launch_upload(const qhg::StepConst *P, qhg::RunState *rs, con
     memset(&BB, 0, sizeof(BB));
     if (sitems == 2) {
         k_cell_scan<false, 2><<<ntiles, kScanThreads, 0, stream>>>(
-            *P, BB, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr2, B->vthr_cell, B->cmove, B->necm2, B->sbase, B->bbase,
+            *P, BB, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr2, B->cmove, B->necm2, B->sbase, B->bbase,
             B->bidbase, B->obase, B->nonempty2, B->ne_start2, B->tile_first2, B->tile_flag, B->tile_agg, B->tile_incl);
     } else {
         k_cell_scan<false, 1><<<ntiles, kScanThreads, 0, stream>>>(
-            *P, BB, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr2, B->vthr_cell, B->cmove, B->necm2, B->sbase, B->bbase,
+            *P, BB, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr2, B->cmove, B->necm2, B->sbase, B->bbase,
             B->bidbase, B->obase, B->nonempty2, B->ne_start2, B->tile_first2, B->tile_flag, B->tile_agg, B->tile_incl);
     }
     if (n > 0) {
@@ -3124,9 +3003,9 @@ static void set_scatter_attr() {
                          (int)sizeof(qhg::ScatterSmemT<qhg::Tile<BIG>::kMax, qhg::Tile<BIG>::kThreads>));
 }
 
-template <bool BATCH, int PR>
+template <bool BATCH>
 static void set_scatter_cell_attr() {
-    cudaFuncSetAttribute(qhg::k_scatter_cell<BATCH, PR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(qhg::k_scatter_cell<BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)(2 * qhg::kCellWarps * qhg::scatter_stage_bytes(true, true)));
 }
 
@@ -3143,8 +3022,7 @@ static void set_tile_attributes() {
     if (dev < 0 || dev >= 64 || done[dev]) return;
     set_cell_attr<0, false>(); set_cell_attr<1, false>(); set_cell_attr<2, false>(); set_cell_attr<3, false>();
     set_cell_attr<0, true>(); set_cell_attr<1, true>();
-    set_scatter_cell_attr<false, 0>(); set_scatter_cell_attr<false, 1>(); set_scatter_cell_attr<false, 2>();
-    set_scatter_cell_attr<false, 3>(); set_scatter_cell_attr<true, 0>();
+    set_scatter_cell_attr<false>(); set_scatter_cell_attr<true>();
     set_actions_attr<0, false, false>(); set_actions_attr<1, false, false>();
     set_actions_attr<2, false, false>(); set_actions_attr<3, false, false>();
     set_actions_attr<0, true, false>(); set_actions_attr<1, true, false>();
@@ -3169,7 +3047,7 @@ static CellGrids cell_grids() {
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, qhg::k_actions_cell<2, false>, qhg::kCellThreads,
                                                       sizeof(qhg::CellWarpSmem) * qhg::kCellWarps);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, qhg::k_scatter_cell<false, 2>, qhg::kCellThreads,
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, qhg::k_scatter_cell<false>, qhg::kCellThreads,
                                                       2 * qhg::kCellWarps * qhg::scatter_stage_bytes(true, true));
         g[dev].actions = std::max(1, nsm) * std::max(1, a);
         g[dev].scatter = std::max(1, nsm) * std::max(1, b);
@@ -3229,7 +3107,7 @@ static void launch_actions(const StepLaunch &S, int form) {
 #define QHG_LAUNCH_CELL(PR, BT)                                                                            \
     k_actions_cell<PR, BT><<<CG.actions, kCellThreads, kSmC, stream>>>(                                    \
         *P, BB, rs, B->nonempty, B->ne_start, B->id, B->birth, B->age, B->lastb, B->meta, B->vthr, B->wthr, \
-        B->necm, B->outc, B->father, B->brank, B->clsc, B->st)
+        B->necm, B->outc, B->father, B->brank, B->clsc)
 #define QHG_FORMS(PR, BT)                                                      \
     do {                                                                       \
         if (tile) QHG_LAUNCH_ACTIONS(PR, BT, false, L.actions_grid, kSmA);     \
@@ -3279,7 +3157,7 @@ static void launch_scan(const StepLaunch &S) {
     }
 #define QHG_LAUNCH_SCAN(BT, IT)                                                                             \
     k_cell_scan<BT, IT><<<ntiles, kScanThreads, 0, stream>>>(                                               \
-        *P, BB, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr2, B->vthr_cell, B->cmove, B->necm2, B->sbase, B->bbase, B->bidbase,       \
+        *P, BB, rs, B->nbr, B->nnbr, B->rev, B->clsc, B->K, B->vthr2, B->cmove, B->necm2, B->sbase, B->bbase, B->bidbase,       \
         B->obase, B->nonempty2, B->ne_start2, B->tile_first2, B->tile_flag, B->tile_agg, B->tile_incl)
     if (batch) {
         if (sitems == 2) QHG_LAUNCH_SCAN(true, 2);
@@ -3312,27 +3190,18 @@ static void launch_scatter(const StepLaunch &S, int form) {
         B->father, B->brank, B->nnbr, B->sbase, B->bbase, B->bidbase, B->obase, B->clsc, B->id2, B->birth2, \
         B->age2, B->lastb2, B->meta2, B->blog, B->blog_cap, B->gslot, B->gslot2, B->freelist,              \
         B->freelist2, B->brec)
-#define QHG_LAUNCH_SCATTER_CELL(BT, PR)                                                                    \
-    k_scatter_cell<BT, PR><<<CG.scatter, kCellThreads, kSmSC, stream>>>(                                   \
+#define QHG_LAUNCH_SCATTER_CELL(BT)                                                                        \
+    k_scatter_cell<BT><<<CG.scatter, kCellThreads, kSmSC, stream>>>(                                       \
         *P, BB, rs, B->nonempty, B->ne_start, B->id, B->birth, B->age, B->lastb, B->outc, B->father,       \
         B->brank, B->sbase, B->bbase, B->bidbase, B->obase, B->clsc, B->id2, B->birth2, B->age2, B->lastb2, \
-        B->meta2, B->blog, B->blog_cap, B->gslot, B->gslot2, B->freelist, B->freelist2, B->brec, B->wthr,   \
-        B->cmove, B->vthr_cell, B->st2)
+        B->meta2, B->blog, B->blog_cap, B->gslot, B->gslot2, B->freelist, B->freelist2, B->brec)
     if (batch) {
         if (tile) QHG_LAUNCH_SCATTER(true, false, L.scatter_grid, kSmS);
-        if (cell) QHG_LAUNCH_SCATTER_CELL(true, 0);
+        if (cell) QHG_LAUNCH_SCATTER_CELL(true);
         if (big) QHG_LAUNCH_SCATTER(true, true, L.big_grid, kSmSB);
     } else {
         if (tile) QHG_LAUNCH_SCATTER(false, false, L.scatter_grid, kSmS);
-        if (cell) {
-            // the scatter of a specialised program stores the next step's action states
-            switch (P->program) {
-            case 1: QHG_LAUNCH_SCATTER_CELL(false, 1); break;
-            case 2: QHG_LAUNCH_SCATTER_CELL(false, 2); break;
-            case 3: QHG_LAUNCH_SCATTER_CELL(false, 3); break;
-            default: QHG_LAUNCH_SCATTER_CELL(false, 0); break;
-            }
-        }
+        if (cell) QHG_LAUNCH_SCATTER_CELL(false);
         if (big) QHG_LAUNCH_SCATTER(false, true, L.big_grid, kSmSB);
     }
 #undef QHG_LAUNCH_SCATTER_CELL
