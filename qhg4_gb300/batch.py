@@ -228,9 +228,11 @@ class Autotuner:
     256-thread blocks).  Each candidate is set, stepped twice untimed (the
     step graphs of both table parities captured, the form changed) and
     timed over ``trial_steps`` steps; candidates compare by time per
-    agent-step.  The steps are the batch's own (results
-    do not depend on the launch), so tuning costs no simulation work.  A
-    later visit of a known bucket just sets its entry."""
+    agent-step.  Every stage times the incumbent first and again last and
+    removes the linear drift between the two (``drift_corrected``).  The
+    steps are the batch's own (results do not depend on the launch), so
+    tuning costs no simulation work.  A later visit of a known bucket just
+    sets its entry."""
 
     trial_steps: int = 2
     span: int = 3
@@ -243,6 +245,19 @@ class Autotuner:
     def bucket(n_agents: int, n_nonempty: int = 1) -> Tuple[int, int]:
         occ = max(1.0, n_agents / max(1, n_nonempty))
         return int(math.log2(max(1, n_agents))), int(math.log2(occ))
+
+    @staticmethod
+    def drift_corrected(times: List[float]) -> List[float]:
+        """Times of a stage's trials, timed in order between two trials of
+        the incumbent (first and last), with the linear drift between those
+        two removed: the batch's runs change while it is tuned (populations
+        grow or shrink, so the cost per agent-step moves), and without the
+        correction a stage would favour whichever candidates came first."""
+        n = len(times) - 1
+        if n <= 0:
+            return list(times)
+        drift = times[-1] - times[0]
+        return [t - drift * i / n for i, t in enumerate(times)]
 
     def _time(self, batch: GpuBatch, cand: Tuple[int, int, int, int]) -> float:
         batch.set_launch(*cand)
@@ -263,13 +278,17 @@ class Autotuner:
 
             def consider(cands):
                 nonlocal best
-                scored = [(c, self._time(batch, c)) for c in cands]
+                cands = [c for c in cands if c != best]
+                seq = [best] + cands + [best]
+                times = [self._time(batch, c) for c in seq]
+                corrected = self.drift_corrected(times)
+                scored = list(zip(seq[:-1], corrected[:-1]))
                 results.extend(scored)
                 best = min(scored, key=lambda x: x[1])[0]
 
             consider([(a, s_, 0, 0) for a in range(max(1, ma - self.span + 1), ma + 1)
                       for s_ in range(max(1, ms - self.span + 1), ms + 1)])
-            consider([(best[0], best[1], items, 0) for items in (1, 2)])
+            consider([(best[0], best[1], items, best[3]) for items in (1, 2)])
             consider([(best[0], best[1], best[2], d) for d in self.dense_choices])
             self.trials[b] = results
             self.table[b] = best
