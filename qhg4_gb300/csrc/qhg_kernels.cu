@@ -2231,24 +2231,37 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
 
     // pieces of work: the warp's cells in turn (cells r, r + G, ...), each in
     // parts of at most kStageRows rows.  The piece being written (cur) and the
-    // one being copied (nxt); the bounds of the cell after nxt's are loaded ahead.
+    // one being copied (nxt).  Every cell-level load is issued one piece before
+    // its use: when cur is its cell's last piece, the next cell's bases and
+    // the index and bounds of the cell after it are loaded while cur's rows
+    // are written.
     uint32_t r = blockIdx.x * kCellWarps + (uint32_t)warp;
     uint32_t cs = 0, cn = 0;           // cur: cell start row and rows
     int coff = 0;                      // cur: first row of the piece within the cell
     uint32_t ns_ = 0, nn_ = 0;         // bounds of the cell r + G
+    uint32_t nc_ = 0;                  // index of the cell r + G
+    // cell data of cur's cell
+    uint32_t c = 0, sb = 0, bb = 0, bid = 0, ob = 0;
     if (r < nne) {
         cs = ne_start[r];
         cn = ne_start[r + 1] - cs;
+        c = nonempty[r];
         if (r + G < nne) {
             ns_ = ne_start[r + G];
             nn_ = ne_start[r + G + 1] - ns_;
+            nc_ = nonempty[r + G];
         }
         issue(0, cs, min(cn, (uint32_t)kStageRows));
+        sb = sbase[c];
+        bb = bbase[c];
+        bid = bidbase[c];
+        ob = (lane < 6) ? obase[(size_t)c * 6 + lane] : 0u;
     }
     int buf = 0;
     bool failed = false;
-    // cell data of cur's cell, loaded when its first piece starts
-    uint32_t c = 0, sb = 0, bb = 0, bid = 0, ob = 0;
+    // the next cell's bases, and the index and bounds of the cell after it
+    uint32_t nsb = 0, nbb = 0, nbid = 0, nob = 0;
+    uint32_t nns = 0, nnn = 0, nnc = 0;
     float ft = fT;
     uint64_t sd = P.seed;
     int32_t st = step;
@@ -2264,15 +2277,24 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
             xs = ns_;
             xn = nn_;
         }
-        if (xr < nne) issue(buf ^ 1, xs + (uint32_t)xoff, min(xn - (uint32_t)xoff, (uint32_t)kStageRows));
+        if (xr < nne) {
+            issue(buf ^ 1, xs + (uint32_t)xoff, min(xn - (uint32_t)xoff, (uint32_t)kStageRows));
+            if (xr != r) {
+                // the next cell's bases in the next table: stayers, newborns
+                // (and their birth numbers), movers per neighbour slot (lane
+                // k holds slot k); the cell after it
+                nsb = sbase[nc_];
+                nbb = bbase[nc_];
+                nbid = bidbase[nc_];
+                nob = (lane < 6) ? obase[(size_t)nc_ * 6 + lane] : 0u;
+                if (xr + G < nne) {
+                    nns = ne_start[xr + G];
+                    nnn = ne_start[xr + G + 1];
+                    nnc = nonempty[xr + G];
+                }
+            }
+        }
         if (coff == 0) {
-            // the cell's bases in the next table: stayers, newborns (and their
-            // birth numbers), movers per neighbour slot (lane k holds slot k)
-            c = nonempty[r];
-            sb = sbase[c];
-            bb = bbase[c];
-            bid = bidbase[c];
-            ob = (lane < 6) ? obase[(size_t)c * 6 + lane] : 0u;
             if (BATCH) {
                 // birth ranks and IDs count within the run
                 const uint32_t rr = BB.crun[c];
@@ -2395,10 +2417,14 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
         if (xr != r) {
             cs = ns_;
             cn = nn_;
-            if (xr + G < nne) {
-                ns_ = ne_start[xr + G];
-                nn_ = ne_start[xr + G + 1] - ns_;
-            }
+            c = nc_;
+            sb = nsb;
+            bb = nbb;
+            bid = nbid;
+            ob = nob;
+            ns_ = nns;
+            nn_ = nnn - nns;
+            nc_ = nnc;
         }
         r = xr;
         coff = xoff;
