@@ -349,6 +349,24 @@ int qhg_batch_set_launch(qhg_batch *batch, const qhg_batch_launch *launch);
 int qhg_batch_get_launch(qhg_batch *batch, qhg_batch_launch *launch);
 /* agents and non-empty cells of the batch's table (waits for the batch) */
 int qhg_batch_table_info(qhg_batch *batch, int64_t *n_agents, int64_t *n_nonempty_cells);
+/* Environment updates of one run between steps, with the effect the
+ * single-run calls have on a run alone (qhg_gpu_set_capacity,
+ * qhg_gpu_set_move_weights, qhg_gpu_set_ice: NPPCapacity's K,
+ * MultiEvaluator's move weights, the Geography's ice, handed over after an
+ * environment event, populations/FlatExpPop.cpp:43-56,
+ * actions/WeightedMove.cpp:91); arrays cover the run's own grid.  Wait for
+ * the batch; QHG_ERR_STATE for a run that has left. */
+int qhg_batch_set_capacity(qhg_batch *batch, int32_t run, const double *K);
+int qhg_batch_set_move_weights(qhg_batch *batch, int32_t run, const double *cumw7);
+int qhg_batch_set_ice(qhg_batch *batch, int32_t run, const uint8_t *ice);
+/* Occupation history of every run (as qhg_gpu_occupancy for a run alone,
+ * OccTracker::updateCounts, core/OccTracker.cpp): per cell of the run's
+ * grid the first of the run's steps whose table holds an agent there (0:
+ * the agents it was admitted with), -1 never.  Enable before the first run
+ * is added (QHG_ERR_STATE after); it adds one kernel per step over the
+ * non-empty cells.  qhg_batch_occupancy waits for the batch. */
+int qhg_batch_enable_occupancy(qhg_batch *batch);
+int qhg_batch_occupancy(qhg_batch *batch, int32_t run, int32_t *first_step);
 int qhg_batch_stream(qhg_batch *batch, void **stream);
 int qhg_batch_destroy(qhg_batch *batch);
 

@@ -202,6 +202,44 @@ class GpuBatch:
         _bcheck(load_library().qhg_batch_table_info(self.h, ct.byref(n), ct.byref(ne)))
         return int(n.value), int(ne.value)
 
+    def set_capacity(self, run: int, K: np.ndarray) -> None:
+        """A new K per cell of the run's grid from its next step on (as
+        GpuRun.set_capacity for the run alone)."""
+        k = np.ascontiguousarray(K, dtype=np.float64)
+        if k.shape != (self.grids[run].num_cells,):
+            raise ValueError("K needs one entry per cell of the run's grid")
+        _bcheck(load_library().qhg_batch_set_capacity(self.h, int(run), _p(k)))
+
+    def set_move_weights(self, run: int, W: np.ndarray) -> None:
+        """WeightedMove's cumulative weights (cells x 7) of the run from its
+        next step on (as GpuRun.set_move_weights)."""
+        w = np.ascontiguousarray(W, dtype=np.float64)
+        if w.shape != (self.grids[run].num_cells, 7):
+            raise ValueError("weights need shape (cells of the run's grid, 7)")
+        _bcheck(load_library().qhg_batch_set_move_weights(self.h, int(run), _p(w)))
+
+    def set_ice(self, run: int, ice) -> None:
+        """The run's ice flags per cell (None: no ice) from its next step on
+        (as GpuRun.set_ice)."""
+        if ice is None:
+            _bcheck(load_library().qhg_batch_set_ice(self.h, int(run), None))
+            return
+        f = np.ascontiguousarray(np.asarray(ice) != 0, dtype=np.uint8)
+        if f.shape != (self.grids[run].num_cells,):
+            raise ValueError("one flag per cell of the run's grid")
+        _bcheck(load_library().qhg_batch_set_ice(self.h, int(run), _p(f)))
+
+    def enable_occupancy(self) -> None:
+        """Tracks every run's occupation history (before the first run)."""
+        _bcheck(load_library().qhg_batch_enable_occupancy(self.h))
+
+    def occupancy(self, run: int) -> np.ndarray:
+        """Per cell of the run's grid, the first of its steps whose table
+        holds an agent there (-1 none), as GpuRun.occupancy for the run alone."""
+        o = np.zeros(self.grids[run].num_cells, dtype=np.int32)
+        _bcheck(load_library().qhg_batch_occupancy(self.h, int(run), _p(o)))
+        return o
+
     def close(self) -> None:
         if getattr(self, "h", None):
             load_library().qhg_batch_destroy(self.h)

@@ -54,6 +54,8 @@ struct RunSlot {
     uint32_t cell0 = 0, cell1 = 0;
     int32_t step0 = 0;      // batch step of the run's step 0
     int32_t left_at = -1;   // batch step at which its agents leave (-1: still in)
+    bool w_given = false;   // WeightedMove weights given (qhg_batch_set_move_weights), else they follow K
+    std::vector<uint8_t> ice;   // the run's ice flags (qhg_batch_set_ice), empty: none
 };
 
 }  // namespace
@@ -116,6 +118,7 @@ struct qhg_batch {
     int32_t copy_table_step = -1;   // batch step after which the copied table is overwritten
     RunState *d_rs = nullptr;
     RunState *h_rs = nullptr;
+    int32_t *d_occ = nullptr;   // first occupied step per cell, in each run's steps (when enabled)
     std::vector<RunSlot> slots;
     std::vector<BatchRun> h_runs;
     int32_t gstep = 0;              // batch steps launched
@@ -145,7 +148,7 @@ StepBuffers make_buffers(qhg_batch *b, int cur) {
     B.meta2 = b->d_meta[nx];
     B.nbr = b->d_nbr; B.nnbr = b->d_nnbr; B.rev = b->d_rev; B.K = b->d_K; B.vthr = b->d_vthr[cur]; B.vthr2 = b->d_vthr[nx];
     B.wthr = b->d_wthr; B.cmove = b->d_cmove; B.necm = b->d_necm[cur]; B.necm2 = b->d_necm[nx];
-    B.occ = nullptr;   // occupancy tracking is a single-run option
+    B.occ = b->d_occ;   // occupation history (qhg_batch_enable_occupancy), else null
     B.outc = b->d_outc; B.father = b->d_father; B.brank = b->d_brank; B.clsc = b->d_clsc;
     B.sbase = b->d_sbase; B.bbase = b->d_bbase; B.bidbase = b->d_bidb; B.obase = b->d_obase;
     B.tile_flag = b->d_tflag; B.tile_agg = b->d_tagg; B.tile_incl = b->d_tincl;
@@ -467,9 +470,15 @@ extern "C" int qhg_batch_add_run(qhg_batch *b, const qhg_batch_run_desc *rd, con
     // the host buffers above are freed on return: wait for the copies
     BCUDA(cudaStreamSynchronize(st));
     b->staged = s0 + (uint32_t)n;
+    if (b->d_occ != nullptr) {
+        // the run's cells have no entries yet (a leaving run's cells are reused)
+        BCUDA(cudaMemsetAsync(b->d_occ + c0, 0xff, C * sizeof(int32_t), st));
+    }
     RunSlot &s = b->slots[(size_t)r];
     s.used = true;
     s.active = true;
+    s.w_given = false;
+    s.ice.clear();
     s.cell0 = c0;
     s.cell1 = c0 + C;
     s.step0 = R.step0;
@@ -826,6 +835,198 @@ extern "C" int qhg_batch_counts(qhg_batch *b, int32_t run, uint32_t *counts) {
     return QHG_OK;
 }
 
+// ------------------------------------------------- environment of one run
+namespace {
+
+// an active run's slot, after the batch's steps so far
+int env_slot(qhg_batch *b, int32_t run, RunSlot **out) {
+    int rc = check_slot(b, run);
+    if (rc != QHG_OK) return rc;
+    RunSlot &s = b->slots[(size_t)run];
+    if (!s.active) return bfail(QHG_ERR_STATE, "the run has left the batch");
+    BCUDA(cudaSetDevice(b->desc.device));
+    rc = pull_state(b);
+    if (rc != QHG_OK) return rc;
+    *out = &s;
+    return QHG_OK;
+}
+
+// the run's grid as it was admitted: neighbours in its own cell indices,
+// neighbour counts, K
+int run_grid(qhg_batch *b, const RunSlot &s, std::vector<int32_t> &nbr6, std::vector<uint8_t> &nnbr,
+             std::vector<double> &K) {
+    const uint32_t C = s.cell1 - s.cell0;
+    nbr6.resize((size_t)C * 6);
+    nnbr.resize(C);
+    K.resize(C);
+    BCUDA(cudaMemcpyAsync(nbr6.data(), b->d_nbr + (size_t)s.cell0 * 6, nbr6.size() * sizeof(int32_t),
+                          cudaMemcpyDeviceToHost, b->stream));
+    BCUDA(cudaMemcpyAsync(nnbr.data(), b->d_nnbr + s.cell0, C, cudaMemcpyDeviceToHost, b->stream));
+    BCUDA(cudaMemcpyAsync(K.data(), b->d_K + s.cell0, C * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    BCUDA(cudaStreamSynchronize(b->stream));
+    for (int32_t &x : nbr6) x = x >= 0 ? x - (int32_t)s.cell0 : -1;
+    return QHG_OK;
+}
+
+// the Verhulst thresholds and move words of the run's cells in the current
+// table, derived again from K and the move tables (the previous step's cell
+// scan derived them from the old ones)
+int refresh_run(qhg_batch *b, const RunSlot &s) {
+    const int cur = b->cur;
+    const uint32_t nne = b->h_rs->n_nonempty;
+    if (nne > 0u) {
+        const int grid = (int)std::min<uint32_t>((nne + 255u) / 256u, 4096u);
+        const int le = qhg_launch_refresh_cells_batch(&b->P, b->d_runs, b->d_crun, b->d_rs, b->d_ne[cur],
+                                                      b->d_nes[cur], b->d_K, b->d_cmove, b->d_vthr[cur],
+                                                      b->d_necm[cur], s.cell0, s.cell1, grid, b->stream);
+        if (le != 0) return bfail(QHG_ERR_CUDA, std::string("launch: ") + cudaGetErrorString((cudaError_t)le));
+    }
+    BCUDA(cudaStreamSynchronize(b->stream));
+    return QHG_OK;
+}
+
+int upload_move_tables(qhg_batch *b, const RunSlot &s, const std::vector<uint64_t> &wthr,
+                       const std::vector<uint32_t> &cmove) {
+    const uint32_t C = s.cell1 - s.cell0;
+    BCUDA(cudaMemcpyAsync(b->d_wthr + (size_t)s.cell0 * 6, wthr.data(), (size_t)C * 6 * sizeof(uint64_t),
+                          cudaMemcpyHostToDevice, b->stream));
+    BCUDA(cudaMemcpyAsync(b->d_cmove + s.cell0, cmove.data(), C * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                          b->stream));
+    return QHG_OK;
+}
+
+}  // namespace
+
+extern "C" int qhg_batch_set_capacity(qhg_batch *b, int32_t run, const double *K) {
+    if (b == nullptr || K == nullptr) return bfail(QHG_ERR_ARG, "null argument");
+    RunSlot *s = nullptr;
+    int rc = env_slot(b, run, &s);
+    if (rc != QHG_OK) return rc;
+    const uint32_t C = s->cell1 - s->cell0;
+    // weights that follow K are derived again (SingleEvaluator over K)
+    const bool tables = b->P.has_wmove && !s->w_given;
+    std::vector<uint32_t> rev, cmove;
+    std::vector<uint64_t> wthr;
+    if (tables) {
+        std::vector<int32_t> nbr6;
+        std::vector<uint8_t> nnbr;
+        std::vector<double> oldK;
+        rc = run_grid(b, *s, nbr6, nnbr, oldK);
+        if (rc != QHG_OK) return rc;
+        std::string err;
+        if (qhg_host_grid_tables((int)C, nbr6.data(), nnbr.data(), K, true, s->ice.empty() ? nullptr : s->ice.data(),
+                                 rev, wthr, cmove, err) != 0) {
+            return bfail(QHG_ERR_ARG, err);
+        }
+    }
+    BCUDA(cudaMemcpyAsync(b->d_K + s->cell0, K, C * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+    if (tables) {
+        rc = upload_move_tables(b, *s, wthr, cmove);
+        if (rc != QHG_OK) return rc;
+    }
+    return refresh_run(b, *s);
+}
+
+extern "C" int qhg_batch_set_move_weights(qhg_batch *b, int32_t run, const double *cumw7) {
+    if (b == nullptr || cumw7 == nullptr) return bfail(QHG_ERR_ARG, "null argument");
+    RunSlot *s = nullptr;
+    int rc = env_slot(b, run, &s);
+    if (rc != QHG_OK) return rc;
+    const uint32_t C = s->cell1 - s->cell0;
+    std::vector<int32_t> nbr6;
+    std::vector<uint8_t> nnbr;
+    std::vector<double> K;
+    rc = run_grid(b, *s, nbr6, nnbr, K);
+    if (rc != QHG_OK) return rc;
+    std::vector<uint32_t> rev, cmove;
+    std::vector<uint64_t> wthr;
+    {
+        std::string err;
+        // the neighbour and ice bits of the move words, then the weights' thresholds
+        if (qhg_host_grid_tables((int)C, nbr6.data(), nnbr.data(), K.data(), false,
+                                 s->ice.empty() ? nullptr : s->ice.data(), rev, wthr, cmove, err) != 0 ||
+            qhg_host_move_tables((int)C, nnbr.data(), cumw7, wthr, cmove, err) != 0) {
+            return bfail(QHG_ERR_ARG, err);
+        }
+    }
+    rc = upload_move_tables(b, *s, wthr, cmove);
+    if (rc != QHG_OK) return rc;
+    s->w_given = true;
+    return refresh_run(b, *s);
+}
+
+extern "C" int qhg_batch_set_ice(qhg_batch *b, int32_t run, const uint8_t *ice) {
+    if (b == nullptr) return bfail(QHG_ERR_ARG, "null batch");
+    RunSlot *s = nullptr;
+    int rc = env_slot(b, run, &s);
+    if (rc != QHG_OK) return rc;
+    const uint32_t C = s->cell1 - s->cell0;
+    std::vector<uint8_t> flags;
+    if (ice != nullptr) {
+        flags.resize(C);
+        for (uint32_t c = 0; c < C; c++) flags[c] = ice[c] != 0 ? 1u : 0u;
+    }
+    const uint8_t *fp = flags.empty() ? nullptr : flags.data();
+    std::vector<int32_t> nbr6;
+    std::vector<uint8_t> nnbr;
+    std::vector<double> K;
+    rc = run_grid(b, *s, nbr6, nnbr, K);
+    if (rc != QHG_OK) return rc;
+    const bool tables = b->P.has_wmove && !s->w_given;
+    if (tables) {
+        // weights that follow K give ice cells weight 0
+        std::vector<uint32_t> rev, cmove;
+        std::vector<uint64_t> wthr;
+        std::string err;
+        if (qhg_host_grid_tables((int)C, nbr6.data(), nnbr.data(), K.data(), true, fp, rev, wthr, cmove, err) != 0) {
+            return bfail(QHG_ERR_ARG, err);
+        }
+        rc = upload_move_tables(b, *s, wthr, cmove);
+        if (rc != QHG_OK) return rc;
+    } else {
+        // keep the words' other bits (the given weights' all-equal flags)
+        std::vector<uint32_t> cur(C);
+        BCUDA(cudaMemcpyAsync(cur.data(), b->d_cmove + s->cell0, C * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                              b->stream));
+        BCUDA(cudaStreamSynchronize(b->stream));
+        qhg_host_ice_bits((int)C, nbr6.data(), fp, cur);
+        BCUDA(cudaMemcpyAsync(b->d_cmove + s->cell0, cur.data(), C * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                              b->stream));
+    }
+    s->ice.swap(flags);
+    return refresh_run(b, *s);
+}
+
+// ------------------------------------------------------ occupation history
+extern "C" int qhg_batch_enable_occupancy(qhg_batch *b) {
+    if (b == nullptr) return bfail(QHG_ERR_ARG, "null batch");
+    if (b->d_occ != nullptr) return QHG_OK;
+    for (const RunSlot &s : b->slots) {
+        if (s.used) return bfail(QHG_ERR_STATE, "enable occupancy tracking before the first run is added");
+    }
+    BCUDA(cudaSetDevice(b->desc.device));
+    BCUDA(cudaMalloc((void **)&b->d_occ, (size_t)b->cell_cap * sizeof(int32_t)));
+    BCUDA(cudaMemsetAsync(b->d_occ, 0xff, (size_t)b->cell_cap * sizeof(int32_t), b->stream));
+    BCUDA(cudaStreamSynchronize(b->stream));
+    drop_graphs(b);   // the step graphs gain the occupancy kernel
+    return QHG_OK;
+}
+
+extern "C" int qhg_batch_occupancy(qhg_batch *b, int32_t run, int32_t *first_step) {
+    if (b == nullptr || first_step == nullptr) return bfail(QHG_ERR_ARG, "null argument");
+    if (b->d_occ == nullptr) return bfail(QHG_ERR_STATE, "occupancy tracking is not enabled");
+    int rc = check_slot(b, run);
+    if (rc != QHG_OK) return rc;
+    BCUDA(cudaSetDevice(b->desc.device));
+    rc = pull_state(b);
+    if (rc != QHG_OK) return rc;
+    const RunSlot &s = b->slots[(size_t)run];
+    BCUDA(cudaMemcpyAsync(first_step, b->d_occ + s.cell0, (size_t)(s.cell1 - s.cell0) * sizeof(int32_t),
+                          cudaMemcpyDeviceToHost, b->stream));
+    BCUDA(cudaStreamSynchronize(b->stream));
+    return QHG_OK;
+}
+
 extern "C" int qhg_batch_stream(qhg_batch *b, void **stream) {
     if (b == nullptr || stream == nullptr) return bfail(QHG_ERR_ARG, "null argument");
     *stream = (void *)b->stream;
@@ -842,7 +1043,7 @@ extern "C" int qhg_batch_destroy(qhg_batch *b) {
                     b->d_outc, b->d_father, b->d_brank, b->d_clsc, b->d_sbase, b->d_bbase, b->d_bidb,
                     b->d_obase, b->d_tflag, b->d_tagg, b->d_tincl, b->d_runs, b->d_rnext, b->d_rstat,
                     b->d_inj, b->d_sgender, b->d_stage_err, b->d_ibase, b->d_injdone, b->d_cstat, b->d_sid, b->d_sbirth, b->d_sage,
-                    b->d_slastb, b->d_smeta, b->d_scell, b->d_rowcell, b->d_rs};
+                    b->d_slastb, b->d_smeta, b->d_scell, b->d_rowcell, b->d_rs, b->d_occ};
     for (void *p : ptrs) cudaFree(p);
     for (int p = 0; p < 2; p++) {
         cudaFree(b->d_id[p]); cudaFree(b->d_birth[p]); cudaFree(b->d_age[p]); cudaFree(b->d_lastb[p]);

@@ -21,6 +21,11 @@ int qhg_host_move_tables(int C, const uint8_t *nnbr, const double *W, std::vecto
 extern "C" int qhg_launch_refresh_cells(const qhg::StepConst *P, const qhg::RunState *rs, const uint32_t *nonempty,
                                         const uint32_t *ne_start, const double *K, const uint32_t *cmove,
                                         ulonglong2 *vthr, uint32_t *necm, int grid, cudaStream_t stream);
+extern "C" int qhg_launch_refresh_cells_batch(const qhg::StepConst *P, const qhg::BatchRun *runs, const uint32_t *crun,
+                                              const qhg::RunState *rs, const uint32_t *nonempty,
+                                              const uint32_t *ne_start, const double *K, const uint32_t *cmove,
+                                              ulonglong2 *vthr, uint32_t *necm, uint32_t cell0, uint32_t cell1,
+                                              int grid, cudaStream_t stream);
 extern "C" int qhg_launch_step(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,
                                const qhg::BatchBuffers *BB, const qhg::LaunchShape *L, cudaStream_t stream);
 extern "C" int qhg_launch_step_timed(const qhg::StepConst *P, qhg::RunState *rs, const qhg::StepBuffers *B,

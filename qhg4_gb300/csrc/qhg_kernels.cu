@@ -1589,14 +1589,22 @@ struct CellWarpSmem {
     uint32_t fk[kMaxCellWarp];       // FERTILE members: low words of their IDs, in each cell's rows
                                      // (females from the cell's first row up, males from its last row down)
     uint16_t frow[kMaxCellWarp];     // ... their rows
-    uint16_t sidx[kMaxCellWarp];     // list positions in ID order, in the same places as the lists
+    // the deferred moves' direction draws live from the first pass to the
+    // deferred-move pass, the ID-ordered positions and the picks from the ID
+    // ranks on: they share their room
+    union {
+        uint32_t mu2[kMaxCellWarp];  // direction draws of the queued moves (mq)
+        struct {
+            uint16_t sidx[kMaxCellWarp];  // list positions in ID order, in the same places as the lists
+            uint16_t pick[kMaxCellWarp];  // pick values of a cell's smaller side (ID order), from the cell's first row
+        } lp;
+    };
     int16_t mate[kMaxCellWarp];      // mate's row of each row, -1 none
-    uint16_t pick[kMaxCellWarp];     // pick values of a cell's smaller side (ID order), from the cell's first row
     uint16_t st[kMaxCellWarp];       // per row: state before the pairing (agent_state), then the outcome byte
     uint32_t odie[kMaxCellWarp / 32];  // OldAgeDeath decided in advance: bit per row, set = dies
-    uint16_t oq[kMaxCellWarp];       // rows inside the OldAgeDeath age window, in a dense queue
-    uint16_t mq[kMaxCellWarp];       // rows whose move draw passed (deferred moves), in a dense queue
-    uint32_t mu2[kMaxCellWarp];      // ... and their direction draws
+    uint16_t oq[kMaxCellWarp];       // rows inside the OldAgeDeath age window, in a dense queue (then mothers)
+    uint16_t mq[kMaxCellWarp];       // rows whose move draw passed (deferred moves), in a dense queue (then
+                                     // the mothers' list positions)
     uint32_t cnt[kGroupCells][8];    // class counts: [0] stay, [1..6] movers per neighbour slot
     // WeightedMove thresholds of each cell (slots 0-5) as 32-bit values: a
     // threshold of 2^32 (no draw reaches it) is kept as 0xffffffff and its
@@ -1607,6 +1615,9 @@ struct CellWarpSmem {
     uint32_t run[kGroupCells];       // batches: run of each cell
 };
 
+// four CTAs per SM (64 registers): five fit in shared memory and a
+// specialised program fits in 48 registers without spills, but then runs
+// 10 % more instructions and measured slower
 template <int PROG, bool BATCH>
 __global__ void __launch_bounds__(kCellThreads, 4)
 k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ rs,
@@ -1856,7 +1867,7 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                         const int64_t x = id[s + W.frow[k]];
                         for (int j = 0; j < cnt; j++) r += (id[s + W.frow[bse + j]] < x) ? 1 : 0;
                     }
-                    W.sidx[bse + r] = (uint16_t)k;
+                    W.lp.sidx[bse + r] = (uint16_t)k;
                 }
             }
             __syncwarp();
@@ -1876,7 +1887,7 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                     if (t < np) {
                         lc = t >= m0 ? 1 : 0;
                         j = t - (lc ? m0 : 0);
-                        const int pos = W.sidx[(lc ? sb1 : sb0) + j];
+                        const int pos = W.lp.sidx[(lc ? sb1 : sb0) + j];
                         x = wide ? id[s + W.frow[pos]] : (int64_t)W.fk[pos];
                         blk = kStreamPair;
                     } else {
@@ -1893,7 +1904,7 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                     const int32_t stR = BATCH ? step - R->step0 : step;
                     const Draw4 d4 = run_block<BATCH>(P, sd, (uint32_t)stR, x, blk);
                     if (t < np) {
-                        W.pick[(lc ? cs1 : 0) + j] =
+                        W.lp.pick[(lc ? cs1 : 0) + j] =
                             (uint16_t)(((uint64_t)((lc ? nL1 : nL0) - (uint32_t)j) * (uint64_t)d4.v[0]) >> 32);
                     } else if (kEarlyOad) {
                         const ActionConst &A = BATCH ? R->act[kOad > 0 ? kOad : 0] : P.act[kOad > 0 ? kOad : 0];
@@ -1914,7 +1925,7 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                 const bool act = t < np;
                 const int lc = (act && t >= m0) ? 1 : 0;
                 const int j = act ? t - (lc ? m0 : 0) : 0;
-                const uint16_t *pk = W.pick + (lc ? cs1 : 0);
+                const uint16_t *pk = W.lp.pick + (lc ? cs1 : 0);
                 uint32_t p = act ? pk[j] : 0u;
                 const int top = __reduce_max_sync(FULL_MASK, (uint32_t)j);
                 for (int k = top - 1; k >= 0; k--) {
@@ -1924,8 +1935,8 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                     if (p >= (lc ? nL1 : nL0)) {   // cannot happen: every pick finds a free member
                         set_error(rs, kErrInternal, 1u);
                     } else {
-                        const int a = W.frow[W.sidx[(lc ? sb1 : sb0) + j]];
-                        const int bb = W.frow[W.sidx[(lc ? lb1 : lb0) + (int)p]];
+                        const int a = W.frow[W.lp.sidx[(lc ? sb1 : sb0) + j]];
+                        const int bb = W.frow[W.lp.sidx[(lc ? lb1 : lb0) + (int)p]];
                         W.mate[a] = (int16_t)bb;
                         W.mate[bb] = (int16_t)a;
                     }
@@ -2015,24 +2026,49 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                 __syncwarp();
             }
             // ---- mothers' birth ranks: births are numbered in (cell, mother ID)
-            // order; mothers are FERTILE females, walked in ID order
+            // order; mothers are FERTILE females, walked in ID order and queued
+            // in birth order (rows and list positions; the OldAgeDeath and move
+            // queues are free by now)
+            uint32_t nmo = 0;
 #pragma unroll
             for (int lc = 0; lc < 2; lc++) {
                 if ((lc ? births1 : births0) == 0u) continue;
                 const int nFl = lc ? nF1 : nF0, cs = lc ? cs1 : 0;
-                uint32_t run = 0;
                 for (int q0 = 0; q0 < nFl; q0 += 32) {
                     const int q = q0 + lane;
                     bool mo = false;
-                    int row = 0;
+                    int row = 0, pos = 0;
                     if (q < nFl) {
-                        row = W.frow[W.sidx[cs + q]];
+                        pos = W.lp.sidx[cs + q];
+                        row = W.frow[pos];
                         mo = (W.st[row] & kOutBirth) != 0;
                     }
                     const uint32_t mb = __ballot_sync(FULL_MASK, mo);
-                    if (mo) brank[s + (uint32_t)row] = (uint16_t)(run + (uint32_t)__popc(mb & lt));
-                    run += (uint32_t)__popc(mb);
+                    if (mo) {
+                        const uint32_t k = nmo + (uint32_t)__popc(mb & lt);
+                        W.oq[k] = (uint16_t)row;
+                        W.mq[k] = (uint16_t)pos;
+                    }
+                    nmo += (uint32_t)__popc(mb);
                 }
+            }
+            __syncwarp();
+            // ---- the newborns: one lane per mother, in a dense pass.  Gender =
+            // (uchar)(2 * wrandd()) from the mother's birth stream
+            // (SPopulation::createAgentAtIndex, core/SPopulation.cpp:880-900),
+            // the birth rank in the cell (< 128: a cell of the warp-per-cell form
+            // holds at most 256 agents) and the gender join the mother's outcome
+            // word (bits 8-15 and 16), which the cell scatter reads
+            for (int t = lane; t < (int)nmo; t += 32) {
+                const int row = W.oq[t];
+                const int lc = row >= cs1 ? 1 : 0;
+                const uint32_t rk = (uint32_t)t - (lc ? births0 : 0u);
+                const int64_t x = wide ? id[s + (uint32_t)row] : (int64_t)W.fk[W.mq[t]];
+                const BatchRun *R = BATCH ? BB.runs + W.run[lc] : nullptr;
+                const uint32_t u = run_block<BATCH>(P, BATCH ? R->seed : P.seed,
+                                                    (uint32_t)(BATCH ? step - R->step0 : step), x, kStreamBirth)
+                                       .v[0];
+                atomicOr(&outc[s + (uint32_t)row], (rk << 8) | ((u >> 31) << 16));
             }
             // class counts of each cell: stay, movers per neighbour slot, births
             {
@@ -2263,8 +2299,6 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
     uint32_t nsb = 0, nbb = 0, nbid = 0, nob = 0;
     uint32_t nns = 0, nnn = 0, nnc = 0;
     float ft = fT;
-    uint64_t sd = P.seed;
-    int32_t st = step;
     int64_t nid = next_id;
     while (r < nne) {
         // the next piece: the rest of this cell, or the next cell's first part
@@ -2301,8 +2335,6 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                 const BatchRun &R = BB.runs[rr];
                 bid -= bidbase[R.cell0];
                 ft = (float)(step - R.step0);
-                sd = R.seed;
-                st = step - R.step0;
                 nid = BB.rnext[rr];
             }
             // the class counts are consumed: clear them for the next step
@@ -2373,19 +2405,21 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
             // gender = (uchar)(2 * wrandd()) from the mother's birth stream,
             // females start FERTILE
             if (valid && (code & kOutBirth)) {
-                const uint32_t rk = brank[g];
-                const int32_t fr = father[g];
+                // birth rank and gender from the mother's outcome word; her
+                // mate's row only where his genome slot or ID is needed
+                const uint32_t rk = (code >> 8) & 255u;
+                const bool mate_read = genetics || P.log_births;
+                const int32_t fr = mate_read ? father[g] : 0;
                 const uint32_t dst = bb + rk;
                 if (dst >= cap || fr < 0 || (uint32_t)fr >= N) {
                     set_error(rs, kErrInternal, 4u);
                 } else {
-                    const uint32_t u = run_block<BATCH>(P, sd, (uint32_t)st, x, kStreamBirth).v[0];
                     const int64_t baby = nid + (int64_t)(bid + rk);
                     id2[dst] = baby;
                     birth2[dst] = ft;
                     lastb2[dst] = 0.0f;
                     if (BATCH || !P.age_from_birth) age2[dst] = 0.0f;
-                    meta2[dst] = (uint8_t)((u >> 31) ? kMetaGender : kMetaFertile);
+                    meta2[dst] = (uint8_t)(((code >> 16) & 1u) ? kMetaGender : kMetaFertile);
                     if (genetics) {
                         const uint32_t gr = bid + rk;   // birth rank of the step
                         const uint32_t bs = gr < nfree ? freelist[gr] : hwm + (gr - nfree);
@@ -2448,13 +2482,18 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
 // it made (and after an upload on the uploaded one): every non-empty cell
 // without an entry gets the step of that table.
 __global__ void __launch_bounds__(256)
-k_occupancy(const RunState *__restrict__ rs, const uint32_t *__restrict__ nonempty, int32_t *__restrict__ occ) {
+k_occupancy(const RunState *__restrict__ rs, const uint32_t *__restrict__ nonempty, int32_t *__restrict__ occ,
+            const BatchRun *__restrict__ runs, const uint32_t *__restrict__ crun) {
     if (rs->error != 0u) return;   // the step failed: its table was not committed
     const uint32_t n = rs->n_nonempty;
     const int32_t st = rs->step;
     for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         const uint32_t c = nonempty[r];
-        if (occ[c] < 0) occ[c] = st;
+        if (occ[c] < 0) {
+            // a batch's cells record the step of their run (0: the table its
+            // agents were admitted into)
+            occ[c] = runs != nullptr ? st - runs[crun[c]].step0 : st;
+        }
     }
 }
 
@@ -2808,13 +2847,20 @@ __global__ void k_batch_stage(uint32_t s0, uint32_t n, uint32_t cell0, uint32_t 
 // again -- the Verhulst thresholds from the new K and the cell's count, the
 // move word from the new cmove -- by the cell's position in the non-empty list.
 __global__ void __launch_bounds__(256)
-k_refresh_cells(const StepConst P, const RunState *__restrict__ rs, const uint32_t *__restrict__ nonempty,
+k_refresh_cells(const StepConst P, const BatchRun *__restrict__ runs, const uint32_t *__restrict__ crun,
+                const RunState *__restrict__ rs, const uint32_t *__restrict__ nonempty,
                 const uint32_t *__restrict__ ne_start, const double *__restrict__ K,
-                const uint32_t *__restrict__ cmove, ulonglong2 *__restrict__ vthr, uint32_t *__restrict__ necm) {
+                const uint32_t *__restrict__ cmove, ulonglong2 *__restrict__ vthr, uint32_t *__restrict__ necm,
+                uint32_t c0, uint32_t c1) {
     const uint32_t nne = rs->n_nonempty;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nne; i += gridDim.x * blockDim.x) {
         const uint32_t c = nonempty[i];
-        if (P.n_verhulst > 0) vthr[i] = verhulst_thresholds(P.act[P.verhulst_act[0]], K[c], ne_start[i + 1] - ne_start[i]);
+        if (c < c0 || c >= c1) continue;   // a batch refreshes one run's cells
+        if (P.n_verhulst > 0) {
+            // a batch's run has its own rates
+            const ActionConst &A = runs != nullptr ? runs[crun[c]].act[P.verhulst_act[0]] : P.act[P.verhulst_act[0]];
+            vthr[i] = verhulst_thresholds(A, K[c], ne_start[i + 1] - ne_start[i]);
+        }
         if (P.has_move) necm[i] = cmove[c];
     }
 }
@@ -2935,7 +2981,18 @@ __global__ void k_run_cells(const uint32_t *__restrict__ nonempty, const uint32_
 extern "C" int qhg_launch_refresh_cells(const qhg::StepConst *P, const qhg::RunState *rs, const uint32_t *nonempty,
                                         const uint32_t *ne_start, const double *K, const uint32_t *cmove,
                                         ulonglong2 *vthr, uint32_t *necm, int grid, cudaStream_t stream) {
-    qhg::k_refresh_cells<<<std::max(1, grid), 256, 0, stream>>>(*P, rs, nonempty, ne_start, K, cmove, vthr, necm);
+    qhg::k_refresh_cells<<<std::max(1, grid), 256, 0, stream>>>(*P, nullptr, nullptr, rs, nonempty, ne_start, K, cmove,
+                                                                 vthr, necm, 0u, 0xffffffffu);
+    return (int)cudaGetLastError();
+}
+
+extern "C" int qhg_launch_refresh_cells_batch(const qhg::StepConst *P, const qhg::BatchRun *runs, const uint32_t *crun,
+                                              const qhg::RunState *rs, const uint32_t *nonempty,
+                                              const uint32_t *ne_start, const double *K, const uint32_t *cmove,
+                                              ulonglong2 *vthr, uint32_t *necm, uint32_t cell0, uint32_t cell1,
+                                              int grid, cudaStream_t stream) {
+    qhg::k_refresh_cells<<<std::max(1, grid), 256, 0, stream>>>(*P, runs, crun, rs, nonempty, ne_start, K, cmove, vthr,
+                                                                 necm, cell0, cell1);
     return (int)cudaGetLastError();
 }
 
@@ -2993,7 +3050,7 @@ extern "C" int qhg_launch_upload(const qhg::StepConst *P, qhg::RunState *rs, con
 
 extern "C" int qhg_launch_occupancy(const qhg::RunState *rs, const uint32_t *nonempty, int32_t *occ, int grid,
                                     cudaStream_t stream) {
-    qhg::k_occupancy<<<std::max(1, grid), 256, 0, stream>>>(rs, nonempty, occ);
+    qhg::k_occupancy<<<std::max(1, grid), 256, 0, stream>>>(rs, nonempty, occ, nullptr, nullptr);
     return (int)cudaGetLastError();
 }
 
@@ -3061,7 +3118,13 @@ static void set_tile_attributes() {
 // grids of the cell form: every SM filled with as many CTAs of each cell
 // kernel as fit (once per device)
 struct CellGrids {
-    int actions, scatter;
+    int actions, actions0;   // action kernel: specialised programs, the interpreter
+    // scatter [batch]: as many CTAs as fit with the largest staging buffers
+    // (age and genome-slot columns), three per SM.  Grids sized for the
+    // run's own buffers (four or five CTAs, 64 or 48 registers) measured
+    // slower on the 20M-agent run (0.23 / 0.27 ms against 0.20 ms), though
+    // four were 5 % faster on an 8M-agent one
+    int scatter[2];
 };
 static CellGrids cell_grids() {
     static CellGrids g[64] = {};
@@ -3069,14 +3132,20 @@ static CellGrids cell_grids() {
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64) dev = 0;
     if (g[dev].actions == 0) {
-        int nsm = 1, a = 0, b = 0;
+        int nsm = 1, a = 0, a0 = 0;
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, qhg::k_actions_cell<2, false>, qhg::kCellThreads,
                                                       sizeof(qhg::CellWarpSmem) * qhg::kCellWarps);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, qhg::k_scatter_cell<false>, qhg::kCellThreads,
-                                                      2 * qhg::kCellWarps * qhg::scatter_stage_bytes(true, true));
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a0, qhg::k_actions_cell<0, false>, qhg::kCellThreads,
+                                                      sizeof(qhg::CellWarpSmem) * qhg::kCellWarps);
         g[dev].actions = std::max(1, nsm) * std::max(1, a);
-        g[dev].scatter = std::max(1, nsm) * std::max(1, b);
+        g[dev].actions0 = std::max(1, nsm) * std::max(1, a0);
+        const size_t sm = 2 * qhg::kCellWarps * qhg::scatter_stage_bytes(true, true);
+        int b = 0, bb = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, qhg::k_scatter_cell<false>, qhg::kCellThreads, sm);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bb, qhg::k_scatter_cell<true>, qhg::kCellThreads, sm);
+        g[dev].scatter[0] = std::max(1, nsm) * std::max(1, b);
+        g[dev].scatter[1] = std::max(1, nsm) * std::max(1, bb);
     }
     return g[dev];
 }
@@ -3131,7 +3200,7 @@ static void launch_actions(const StepLaunch &S, int form) {
         *P, BB, rs, B->nonempty, B->ne_start, B->tile_first, B->id, B->birth, B->age, B->lastb, B->meta, \
         B->vthr, B->wthr, B->necm, B->outc, B->father, B->brank, B->clsc)
 #define QHG_LAUNCH_CELL(PR, BT)                                                                            \
-    k_actions_cell<PR, BT><<<CG.actions, kCellThreads, kSmC, stream>>>(                                    \
+    k_actions_cell<PR, BT><<<(PR > 0 ? CG.actions : CG.actions0), kCellThreads, kSmC, stream>>>(            \
         *P, BB, rs, B->nonempty, B->ne_start, B->id, B->birth, B->age, B->lastb, B->meta, B->vthr, B->wthr, \
         B->necm, B->outc, B->father, B->brank, B->clsc)
 #define QHG_FORMS(PR, BT)                                                      \
@@ -3217,7 +3286,7 @@ static void launch_scatter(const StepLaunch &S, int form) {
         B->age2, B->lastb2, B->meta2, B->blog, B->blog_cap, B->gslot, B->gslot2, B->freelist,              \
         B->freelist2, B->brec)
 #define QHG_LAUNCH_SCATTER_CELL(BT)                                                                        \
-    k_scatter_cell<BT><<<CG.scatter, kCellThreads, kSmSC, stream>>>(                                       \
+    k_scatter_cell<BT><<<CG.scatter[BT ? 1 : 0], kCellThreads, kSmSC, stream>>>(                             \
         *P, BB, rs, B->nonempty, B->ne_start, B->id, B->birth, B->age, B->lastb, B->outc, B->father,       \
         B->brank, B->sbase, B->bbase, B->bidbase, B->obase, B->clsc, B->id2, B->birth2, B->age2, B->lastb2, \
         B->meta2, B->blog, B->blog_cap, B->gslot, B->gslot2, B->freelist, B->freelist2, B->brec)
@@ -3243,8 +3312,10 @@ static void launch_post(const StepLaunch &S, cudaEvent_t *ev) {
     const LaunchShape &L = S.L;
     cudaStream_t stream = S.stream;
     const bool batch = S.batch;
-    if (!batch && B->occ != nullptr) {
-        k_occupancy<<<std::max(1, L.scatter_grid), 256, 0, stream>>>(rs, B->nonempty2, B->occ);
+    if (B->occ != nullptr) {
+        k_occupancy<<<std::max(1, L.scatter_grid), 256, 0, stream>>>(rs, B->nonempty2, B->occ,
+                                                                      batch ? BB.runs : nullptr,
+                                                                      batch ? BB.crun : nullptr);
     }
     if (!batch && B->ms_mode >= 0) {
         const int mg = std::max(1, std::min((P->num_cells + 255) / 256, 152 * 8));

@@ -41,7 +41,8 @@ EXPORTS = [
     "qhg_batch_live_history", "qhg_batch_snapshot_async", "qhg_batch_snapshot_wait",
     "qhg_host_buffer_alloc", "qhg_host_buffer_free", "qhg_gpu_next_id", "qhg_gpu_set_next_id",
     "qhg_gpu_test_stall_scan", "qhg_gpu_occupancy", "qhg_gpu_set_capacity", "qhg_gpu_set_move_weights", "qhg_gpu_set_ice", "qhg_gpu_stats_async", "qhg_batch_set_launch", "qhg_batch_get_launch",
-    "qhg_batch_table_info",
+    "qhg_batch_table_info", "qhg_batch_set_capacity", "qhg_batch_set_move_weights", "qhg_batch_set_ice",
+    "qhg_batch_enable_occupancy", "qhg_batch_occupancy",
     "qhg_gpu_move_stats_enable", "qhg_gpu_move_stats", "qhg_gpu_set_move_stats", "qhg_gpu_set_occupancy",
 ]
 
@@ -143,6 +144,11 @@ def load_library(path: str = LIB_PATH):
         "qhg_batch_set_launch": (I, [P, P]),
         "qhg_batch_get_launch": (I, [P, P]),
         "qhg_batch_table_info": (I, [P, P, P]),
+        "qhg_batch_set_capacity": (I, [P, ct.c_int32, P]),
+        "qhg_batch_set_move_weights": (I, [P, ct.c_int32, P]),
+        "qhg_batch_set_ice": (I, [P, ct.c_int32, P]),
+        "qhg_batch_enable_occupancy": (I, [P]),
+        "qhg_batch_occupancy": (I, [P, ct.c_int32, P]),
         "qhg_gpu_move_stats_enable": (I, [P, ct.c_int32, P, P, ct.c_double, ct.c_int32]),
         "qhg_gpu_move_stats": (I, [P, P, P, P]),
         "qhg_gpu_set_move_stats": (I, [P, P, P, P]),

@@ -86,7 +86,9 @@ def test_batch_shape_does_not_change_results(gpu_lib):
     b.step(3)
     tuner = Autotuner(trial_steps=1, span=2)
     tuner.tune(b)
-    assert tuner.table and len(tuner.trials[next(iter(tuner.trials))]) == 4 + 2 + 3
+    # CTA stage: 4 shapes, the incumbent among them; scan stage: the
+    # incumbent + 2 widths; form stage: the incumbent + 3 thresholds
+    assert tuner.table and len(tuner.trials[next(iter(tuner.trials))]) == 4 + 3 + 4
     b.step(2)
     for k, r in enumerate(ids):
         same_as_alone(b, r, cases[k], b.steps_done(r))
