@@ -57,6 +57,8 @@ BIRTH_BYTES = 3 * 1024   # genetics: two parent genomes read, one child genome w
 # scatter in each of the three forms (two of each return at once) and the
 # cell scan; the genome kernel with genetics
 LAUNCHES_PER_STEP = 7
+# untimed first steps of every ensemble run, batched and plain alike
+ENSEMBLE_WARM = 5
 # speed of the C port relative to the reference's own OpenMP code, measured
 # where the reference sources are (both on 8 cores of the build container,
 # the plain method and the large run's actions at 2M agents)
@@ -547,11 +549,14 @@ def measure_ensemble(n_runs: int, steps: int, device: int, plain_runs: int, seed
     b = GpuBatch(config1_actions(), agent_capacity=cap, cell_capacity=cells, max_runs=n_runs,
                  stage_capacity=n0, device=device)
     ids = [b.add_run(s.grid, s.actions, s.seed, s.agents) for s in specs]
-    b.step(1)   # the runs' agents enter the table
+    # the runs' agents enter the table; the first steps (few births while the
+    # runs' first mothers wait out the interbirth time) run untimed before
+    # the first tuning, like the plain runs' first steps
+    b.step(1 + ENSEMBLE_WARM)
     # the autotuner (re)tunes whenever the batch enters another size bucket
-    # (the ensemble shrinks); its trial steps are simulation steps, timed
-    # apart from the measured chunks, and the first steps after a change of
-    # launch (graph capture) are not timed either
+    # (the ensemble shrinks); its timed trial steps are simulation steps and
+    # count in the batched figure; steps that capture a new launch's graphs
+    # are not timed
     tuner = Autotuner(trial_steps=2, span=2)
     ms_b, as_b, timed_steps = 0.0, 0, 0
     last = None
@@ -571,6 +576,9 @@ def measure_ensemble(n_runs: int, steps: int, device: int, plain_runs: int, seed
         live = b.live_history(k)
         as_b += n_start + int(live[:-1].sum())
         timed_steps += k
+    ms_b += tuner.trial_ms
+    as_b += tuner.trial_agent_steps
+    timed_steps += tuner.trial_steps_done
     finals = [len(b.agents(r, sort_by_id=False)) for r in ids]
     hist = b.live_history(steps + 1)
     b.close()
@@ -584,13 +592,13 @@ def measure_ensemble(n_runs: int, steps: int, device: int, plain_runs: int, seed
         r = GpuRun(s.grid, s.actions, s.seed, capacity=max(2 * len(s.agents), 40 * s.grid.num_cells) + 65536,
                    device=device)
         r.load(s.agents)
-        r.step(2)   # both graphs built outside the timed steps
-        st0 = r.stats(2)
-        k = s.steps - 2
+        r.step(1 + ENSEMBLE_WARM)   # both graphs built outside the timed steps
+        st0 = r.stats(1 + ENSEMBLE_WARM)
+        k = s.steps - 1 - ENSEMBLE_WARM
         ms_p += r.step_timed(k)
         st = r.stats(k)
         as_p += int(st0[-1, 0]) + int(st[:-1, 0].sum())
-        as_p_all += len(s.agents) + int(st0[0, 0]) + int(st0[-1, 0]) + int(st[:-1, 0].sum())
+        as_p_all += len(s.agents) + int(st0[:, 0].sum()) + int(st[:-1, 0].sum())
         r.agents(sort_by_id=False)
         r.close()
         wall_p += time.perf_counter() - t0
@@ -668,7 +676,7 @@ def run_served(args, world, rank, local, dist):
 
 def run_ensemble(args, world, rank, local, dist):
     device = local if world > 1 else args.device
-    res = measure_ensemble(args.ensemble_runs, args.ensemble_steps, device, args.plain_runs, seed=args.seed + rank)
+    res = measure_ensemble(args.ensemble_runs, args.ensemble_steps, device, args.plain_runs, seed=2024 + rank)
     if rank == 0:
         line = {"metric": METRIC, "value": res["value"], "unit": "agent-steps/s", "n_gpus": world,
                 "steps": res["timed_steps"], "warmup": res["steps_per_run"] - res["timed_steps"],

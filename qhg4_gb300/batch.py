@@ -278,6 +278,11 @@ class Autotuner:
     table: Dict[Tuple[int, int], Tuple[int, int, int, int]] = field(default_factory=dict)
     trials: Dict[Tuple[int, int], List[Tuple[Tuple[int, int, int, int], float]]] = field(default_factory=dict)
     current: Optional[Tuple[int, int, int, int]] = None
+    # the timed trial steps so far: device ms and agent-steps (they are steps
+    # of the batch's runs like any other)
+    trial_ms: float = 0.0
+    trial_agent_steps: int = 0
+    trial_steps_done: int = 0
 
     @staticmethod
     def bucket(n_agents: int, n_nonempty: int = 1) -> Tuple[int, int]:
@@ -302,7 +307,11 @@ class Autotuner:
         self.current = cand
         batch.step(2)   # step graphs of both table parities captured (and the form applied) untimed
         n0, _ = batch.table_info()
-        return batch.step_timed(self.trial_steps) / (self.trial_steps * max(1, n0))
+        ms = batch.step_timed(self.trial_steps)
+        self.trial_ms += ms
+        self.trial_agent_steps += n0 * self.trial_steps
+        self.trial_steps_done += self.trial_steps
+        return ms / (self.trial_steps * max(1, n0))
 
     def tune(self, batch: GpuBatch) -> Tuple[int, int, int, int]:
         """Sets the batch's launch for its current bucket (searching on the
