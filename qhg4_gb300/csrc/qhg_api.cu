@@ -715,7 +715,7 @@ static int alloc_agents(qhg_run *r, uint32_t cap) {
         CUDA_TRY(cudaMalloc(&r->d_tf[p], ((size_t)cap / kTileAgents + 2) * sizeof(uint32_t)));
     }
     CUDA_TRY(cudaMalloc(&r->d_outc, (size_t)cap * sizeof(uint32_t) + kColumnPad));
-    CUDA_TRY(cudaMalloc(&r->d_father, (size_t)cap * sizeof(int32_t)));
+    CUDA_TRY(cudaMalloc(&r->d_father, (size_t)cap * sizeof(int32_t) + kColumnPad));   // staged by the cell scatter
     CUDA_TRY(cudaMalloc(&r->d_brank, (size_t)cap * sizeof(uint16_t)));
     if (r->P.log_births) {
         r->blog_cap = std::max<uint64_t>(1u << 20, (uint64_t)cap * 4);

@@ -299,7 +299,7 @@ extern "C" int qhg_batch_create(const qhg_batch_desc *desc, qhg_batch **out) {
         A((void **)&b->d_tf[p], (N / kTileAgents + 2) * sizeof(uint32_t));
     }
     A((void **)&b->d_outc, N * sizeof(uint32_t) + kColumnPad);
-    A((void **)&b->d_father, N * sizeof(int32_t));
+    A((void **)&b->d_father, N * sizeof(int32_t) + kColumnPad);
     A((void **)&b->d_brank, N * sizeof(uint16_t));
     A((void **)&b->d_clsc, C * kCls * sizeof(uint32_t));
     A((void **)&b->d_sbase, C * sizeof(uint32_t));

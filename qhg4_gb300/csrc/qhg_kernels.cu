@@ -2106,10 +2106,10 @@ constexpr uint32_t kStageSpinLimit = 1u << 24;   // polls of a staging wait (wit
 __host__ __device__ constexpr uint32_t stage_col_bytes(uint32_t elem) { return (uint32_t)kStageRows * elem + 32u; }
 // one staging buffer of the scatter: outcome words, IDs, birth times, last
 // births, ages (when the table's ages are not derived from birth times),
-// genome slots (genetics)
+// genome slots and mates' rows (genetics)
 __host__ __device__ inline uint32_t scatter_stage_bytes(bool age_col, bool gslot_col) {
     return stage_col_bytes(4) + stage_col_bytes(8) + 2u * stage_col_bytes(4) + (age_col ? stage_col_bytes(4) : 0u) +
-           (gslot_col ? stage_col_bytes(4) : 0u);
+           (gslot_col ? 2u * stage_col_bytes(4) : 0u);
 }
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -2247,7 +2247,7 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
         stage_range(g, cnt, 4, off[3], by[3], hd[3]);
         stage_range(g, cnt, 4, off[4], by[4], hd[4]);
         stage_range(g, cnt, 4, off[5], by[5], hd[5]);
-        total = by[0] + by[1] + by[2] + by[3] + (age_col ? by[4] : 0u) + (genetics ? by[5] : 0u);
+        total = by[0] + by[1] + by[2] + by[3] + (age_col ? by[4] : 0u) + (genetics ? 2u * by[5] : 0u);
         mbar_arrive_expect_tx(&bar[b], total);
         unsigned char *d = buf;
         bulk_g2s(d, reinterpret_cast<const unsigned char *>(outc) + off[0], by[0], &bar[b]);
@@ -2262,7 +2262,11 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
             bulk_g2s(d, reinterpret_cast<const unsigned char *>(age) + off[4], by[4], &bar[b]);
             d += stage_col_bytes(4);
         }
-        if (genetics) bulk_g2s(d, reinterpret_cast<const unsigned char *>(gslot) + off[5], by[5], &bar[b]);
+        if (genetics) {
+            bulk_g2s(d, reinterpret_cast<const unsigned char *>(gslot) + off[5], by[5], &bar[b]);
+            d += stage_col_bytes(4);
+            bulk_g2s(d, reinterpret_cast<const unsigned char *>(father) + off[5], by[5], &bar[b]);
+        }
     };
 
     // pieces of work: the warp's cells in turn (cells r, r + G, ...), each in
@@ -2360,6 +2364,7 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
         const float *s_age = reinterpret_cast<const float *>(sp + 3u * stage_col_bytes(4) + stage_col_bytes(8) + h4);
         const int32_t *s_gslot = reinterpret_cast<const int32_t *>(
             sp + (3u + (age_col ? 1u : 0u)) * stage_col_bytes(4) + stage_col_bytes(8) + h4);
+        const int32_t *s_father = s_gslot + stage_col_bytes(4) / 4u;
         for (int b = 0; b < pn; b += 32) {
             const int i = b + lane;
             const bool valid = i < pn;
@@ -2408,8 +2413,7 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                 // birth rank and gender from the mother's outcome word; her
                 // mate's row only where his genome slot or ID is needed
                 const uint32_t rk = (code >> 8) & 255u;
-                const bool mate_read = genetics || P.log_births;
-                const int32_t fr = mate_read ? father[g] : 0;
+                const int32_t fr = genetics ? s_father[i] : (P.log_births ? father[g] : 0);
                 const uint32_t dst = bb + rk;
                 if (dst >= cap || fr < 0 || (uint32_t)fr >= N) {
                     set_error(rs, kErrInternal, 4u);
@@ -2428,8 +2432,11 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                         } else {
                             gslot2[dst] = (int32_t)bs;
                             uint32_t *br = brec + (size_t)gr * 5;
+                            // the mate lies in the same cell: in this piece
+                            // unless the cell spans several
+                            const int fi = fr - (int)g0;
                             br[0] = (uint32_t)gs;
-                            br[1] = (uint32_t)gslot[fr];
+                            br[1] = (uint32_t)((fi >= 0 && fi < pn) ? s_gslot[fi] : gslot[fr]);
                             br[2] = bs;
                             br[3] = (uint32_t)(uint64_t)x;
                             br[4] = (uint32_t)((uint64_t)x >> 32);
@@ -2649,7 +2656,7 @@ __device__ __forceinline__ uint32_t birth_draw(const Draw4 &d, int k) {
 // strand, inside it the makeMultiMask mask mixes the two), strand 1 the same
 // for the father with i2, then the mutation flips.  The parents' words are
 // loaded first, so that their latency overlaps the draws.
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)   // four CTAs per SM: the grid of four per SM in one wave
 k_genomes(const StepConst P, RunState *__restrict__ rs, uint64_t *__restrict__ genome,
           const uint32_t *__restrict__ brec) {
     if (rs->error != 0u) return;
