@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <memory>
 #include <string>
 #include <thread>
 #include <vector>
@@ -436,23 +437,40 @@ static int parallel_cells(int n, F f) {
 int qhg_host_grid_tables(int C, const int32_t *nbr6, const uint8_t *nnbr, const double *K, bool wm,
                          const uint8_t *ice, std::vector<uint32_t> &rev, std::vector<uint64_t> &wthr,
                          std::vector<uint32_t> &cmove, std::string &err) {
-    rev.assign((size_t)C, 0u);
+    // one pass over the cells on all host cores: reverse slots, move words,
+    // each cell's own SingleEvaluator weight (every element is written: the
+    // weights need no zero fill)
+    rev.resize((size_t)C);
+    cmove.resize((size_t)C);
+    std::unique_ptr<double[]> W(wm ? new double[(size_t)C * 7] : nullptr);
     // the first failing cell's problem: 1 too many neighbours, 2 index out of
     // range, 3 not symmetric
     std::vector<uint8_t> why((size_t)C, 0u);
     const int bad = parallel_cells(C, [&](int c0, int c1) {
         for (int c = c0; c < c1; c++) {
             if (nnbr[c] > 6) { why[(size_t)c] = 1u; return c; }
+            uint32_t rv = 0u, vm = 0u, wv = 0u;
             for (int j = 0; j < 6; j++) {
                 const int d = nbr6[(size_t)c * 6 + j];
                 if (d >= C || d < -1) { why[(size_t)c] = 2u; return c; }
+                if (d >= 0) {
+                    vm |= 1u << j;
+                    if (ice == nullptr || ice[d] == 0) wv |= 1u << j;
+                }
                 if (j >= nnbr[c] || d < 0) continue;
                 int k = -1;
                 for (int q = 0; q < nnbr[d] && q < 6; q++) {
                     if (nbr6[(size_t)d * 6 + q] == c) { k = q; break; }
                 }
                 if (k < 0) { why[(size_t)c] = 3u; return c; }
-                rev[(size_t)c] |= (uint32_t)k << (3 * j);
+                rv |= (uint32_t)k << (3 * j);
+            }
+            rev[(size_t)c] = rv;
+            // neighbour count, slots holding a neighbour, slots a WeightedMove may enter
+            cmove[(size_t)c] = (uint32_t)nnbr[c] | (vm << 8) | (wv << 24);
+            if (wm) {
+                const double dV = K[c];
+                W[(size_t)c * 7] = (ice != nullptr && ice[c] != 0) ? 0 : ((dV > 0) ? dV : 0);
             }
         }
         return C;
@@ -463,19 +481,9 @@ int qhg_host_grid_tables(int C, const int32_t *nbr6, const uint8_t *nnbr, const 
                                                             : "neighbour table is not symmetric");
         return -1;
     }
-    wthr.assign((size_t)C * 6, 0);
-    cmove.assign((size_t)C, 0u);
-    for (int c = 0; c < C; c++) {
-        uint32_t vm = 0;
-        for (int j = 0; j < 6; j++) vm |= (nbr6[(size_t)c * 6 + j] >= 0 ? 1u : 0u) << j;
-        cmove[c] = (uint32_t)nnbr[c] | (vm << 8);
-    }
-    qhg_host_ice_bits(C, nbr6, ice, cmove);
-    if (!wm) return 0;
-    std::vector<double> W((size_t)C * 7);
-    for (int c = 0; c < C; c++) {
-        const double dV = K[c];
-        W[(size_t)c * 7] = (ice != nullptr && ice[c] != 0) ? 0 : ((dV > 0) ? dV : 0);
+    if (!wm) {
+        wthr.assign((size_t)C * 6, 0);
+        return 0;
     }
     parallel_cells(C, [&](int c0, int c1) {
         for (int c = c0; c < c1; c++) {
@@ -491,7 +499,7 @@ int qhg_host_grid_tables(int C, const int32_t *nbr6, const uint8_t *nnbr, const 
         }
         return C;
     });
-    return qhg_host_move_tables(C, nnbr, W.data(), wthr, cmove, err);
+    return qhg_host_move_tables(C, nnbr, W.get(), wthr, cmove, err);
 }
 
 // WeightedMove's thresholds from cumulative weights W (C x 7, W[c][0] the
@@ -509,7 +517,9 @@ int qhg_host_grid_tables(int C, const int32_t *nbr6, const uint8_t *nnbr, const 
 // are left as they are.
 int qhg_host_move_tables(int C, const uint8_t *nnbr, const double *W, std::vector<uint64_t> &wthr,
                          std::vector<uint32_t> &cmove, std::string &err) {
-    wthr.assign((size_t)C * 6, 0);
+    // every slot of every cell is written below (the vector keeps its size
+    // when a caller filled it already)
+    wthr.resize((size_t)C * 6);
     // per failing cell: 1 total weight not positive and finite, 2 a weight not finite
     std::vector<uint8_t> why((size_t)C, 0u);
     const int bad = parallel_cells(C, [&](int c0, int c1) {
@@ -520,16 +530,20 @@ int qhg_host_move_tables(int C, const uint8_t *nnbr, const double *W, std::vecto
             cmove[c] &= ~(1u << 16);
             if (Wc[0] == Wn) {
                 cmove[c] |= 1u << 16;
+                for (int j = 0; j < 6; j++) wthr[(size_t)c * 6 + j] = 0;
                 continue;
             }
             if (!(Wn > 0.0) || !std::isfinite(Wn)) { why[(size_t)c] = 1u; return c; }
-            auto f = [&](uint64_t u) { return ((1.0 * (double)u) / 4294967296.0) * Wn; };
+            // wrandd() * W[n] for the draw u: u / 2^32 is exact, so it is u * 2^-32
+            auto f = [&](uint64_t u) { return ((double)u * 0x1p-32) * Wn; };
+            // where the search starts (the loops below settle u exactly)
+            const double guess = 4294967296.0 / Wn;
             uint64_t run = 0;
             for (int j = 0; j < nn; j++) {
                 const double x = Wc[j];
                 if (!std::isfinite(x)) { why[(size_t)c] = 2u; return c; }
                 // smallest u in [0, 2^32] with f(u) >= x  (f(2^32) counts as +inf)
-                double g = std::floor(x / Wn * 4294967296.0);
+                double g = std::floor(x * guess);
                 uint64_t u = (g <= 0) ? 0ull : (g >= 4294967296.0 ? 4294967296ull : (uint64_t)g);
                 while (u > 0 && f(u - 1) >= x) u--;
                 while (u < 4294967296ull && f(u) < x) u++;
