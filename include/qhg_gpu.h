@@ -367,6 +367,18 @@ int qhg_batch_set_ice(qhg_batch *batch, int32_t run, const uint8_t *ice);
  * non-empty cells.  qhg_batch_occupancy waits for the batch. */
 int qhg_batch_enable_occupancy(qhg_batch *batch);
 int qhg_batch_occupancy(qhg_batch *batch, int32_t run, int32_t *first_step);
+/* MoveStats of every run (as qhg_gpu_move_stats_enable / qhg_gpu_move_stats
+ * for a run alone, actions/MoveStats.cpp): one mode, radius and distance
+ * kind for the batch, enabled before the first run is added
+ * (QHG_ERR_STATE after).  A run's state starts at its admission (the cells
+ * its agents start in are the origins: hops, distance and time 0); its cell
+ * coordinates (lon/lat in degrees, or x/y with cartesian) are given by
+ * qhg_batch_move_stats_coords before the steps whose moves should add
+ * distances (until then they add 0).  Times are the run's own steps.  Both
+ * calls wait for the batch. */
+int qhg_batch_move_stats_enable(qhg_batch *batch, int32_t mode, double radius, int32_t cartesian);
+int qhg_batch_move_stats_coords(qhg_batch *batch, int32_t run, const double *lon, const double *lat);
+int qhg_batch_move_stats(qhg_batch *batch, int32_t run, int32_t *hops, double *dist, double *time);
 int qhg_batch_stream(qhg_batch *batch, void **stream);
 int qhg_batch_destroy(qhg_batch *batch);
 

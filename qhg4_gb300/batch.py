@@ -240,6 +240,30 @@ class GpuBatch:
         _bcheck(load_library().qhg_batch_occupancy(self.h, int(run), _p(o)))
         return o
 
+    def move_stats_enable(self, mode: int, radius: float = 1.0, cartesian: bool = False) -> None:
+        """MoveStats for every run (before the first run), in mode
+        QHG_MOVESTATS_FIRST / MIN / LAST (qhg4_gb300.gpu's constants)."""
+        _bcheck(load_library().qhg_batch_move_stats_enable(self.h, int(mode), float(radius), 1 if cartesian else 0))
+
+    def move_stats_coords(self, run: int, lon: np.ndarray, lat: np.ndarray) -> None:
+        """The run's cell coordinates (degrees, or x/y with cartesian)."""
+        C = self.grids[run].num_cells
+        lo = np.ascontiguousarray(lon, dtype=np.float64)
+        la = np.ascontiguousarray(lat, dtype=np.float64)
+        if lo.shape != (C,) or la.shape != (C,):
+            raise ValueError("one coordinate pair per cell of the run's grid")
+        _bcheck(load_library().qhg_batch_move_stats_coords(self.h, int(run), _p(lo), _p(la)))
+
+    def move_stats(self, run: int):
+        """Per cell of the run's grid: hops, distance and time of the arrivals
+        (as GpuRun.move_stats for the run alone)."""
+        C = self.grids[run].num_cells
+        h = np.zeros(C, dtype=np.int32)
+        d = np.zeros(C, dtype=np.float64)
+        t = np.zeros(C, dtype=np.float64)
+        _bcheck(load_library().qhg_batch_move_stats(self.h, int(run), _p(h), _p(d), _p(t)))
+        return h, d, t
+
     def close(self) -> None:
         if getattr(self, "h", None):
             load_library().qhg_batch_destroy(self.h)

@@ -1152,6 +1152,10 @@ static double ms_distance(const double *lon, const double *lat, double R, bool c
     return ms_spherdist(lon[a] * kQPi / 180, lat[a] * kQPi / 180, lon[b] * kQPi / 180, lat[b] * kQPi / 180, R);
 }
 
+double qhg_host_move_distance(const double *lon, const double *lat, double radius, bool cartesian, int a, int b) {
+    return ms_distance(lon, lat, radius, cartesian, a, b);
+}
+
 static void ms_free(qhg_run *r) {
     cudaFree(r->d_ms_hops); cudaFree(r->d_ms_chops); cudaFree(r->d_ms_dist); cudaFree(r->d_ms_time);
     cudaFree(r->d_ms_D); cudaFree(r->d_ms_cdist); cudaFree(r->d_ms_ckey);

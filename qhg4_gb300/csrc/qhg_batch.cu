@@ -119,6 +119,14 @@ struct qhg_batch {
     RunState *d_rs = nullptr;
     RunState *h_rs = nullptr;
     int32_t *d_occ = nullptr;   // first occupied step per cell, in each run's steps (when enabled)
+    // MoveStats of every run (qhg_batch_move_stats_enable): mode (-1 off), per-cell state,
+    // candidates of the step, distances to the neighbour slots
+    int32_t ms_mode = -1;
+    double ms_radius = 1.0;
+    bool ms_cartesian = false;
+    int32_t *d_ms_hops = nullptr, *d_ms_chops = nullptr;
+    double *d_ms_dist = nullptr, *d_ms_time = nullptr, *d_ms_D = nullptr;
+    unsigned long long *d_ms_cdist = nullptr, *d_ms_ckey = nullptr;
     std::vector<RunSlot> slots;
     std::vector<BatchRun> h_runs;
     int32_t gstep = 0;              // batch steps launched
@@ -149,6 +157,9 @@ StepBuffers make_buffers(qhg_batch *b, int cur) {
     B.nbr = b->d_nbr; B.nnbr = b->d_nnbr; B.rev = b->d_rev; B.K = b->d_K; B.vthr = b->d_vthr[cur]; B.vthr2 = b->d_vthr[nx];
     B.wthr = b->d_wthr; B.cmove = b->d_cmove; B.necm = b->d_necm[cur]; B.necm2 = b->d_necm[nx];
     B.occ = b->d_occ;   // occupation history (qhg_batch_enable_occupancy), else null
+    B.ms_mode = b->ms_mode;
+    B.ms_hops = b->d_ms_hops; B.ms_dist = b->d_ms_dist; B.ms_time = b->d_ms_time;
+    B.ms_chops = b->d_ms_chops; B.ms_cdist = b->d_ms_cdist; B.ms_ckey = b->d_ms_ckey; B.ms_D = b->d_ms_D;
     B.outc = b->d_outc; B.father = b->d_father; B.brank = b->d_brank; B.clsc = b->d_clsc;
     B.sbase = b->d_sbase; B.bbase = b->d_bbase; B.bidbase = b->d_bidb; B.obase = b->d_obase;
     B.tile_flag = b->d_tflag; B.tile_agg = b->d_tagg; B.tile_incl = b->d_tincl;
@@ -473,6 +484,31 @@ extern "C" int qhg_batch_add_run(qhg_batch *b, const qhg_batch_run_desc *rd, con
     if (b->d_occ != nullptr) {
         // the run's cells have no entries yet (a leaving run's cells are reused)
         BCUDA(cudaMemsetAsync(b->d_occ + c0, 0xff, C * sizeof(int32_t), st));
+    }
+    if (b->ms_mode >= 0) {
+        // MoveStats of the run: no arrivals yet, distances zero until its
+        // coordinates are given; the cells its agents start in are the origins
+        std::vector<uint8_t> occupied(C, 0u);
+        for (int64_t q = 0; q < n; q++) {
+            if (a->state[q] != 0 && a->cell[q] >= 0 && (uint32_t)a->cell[q] < C) occupied[(size_t)a->cell[q]] = 1u;
+        }
+        std::vector<uint32_t> origin;
+        for (uint32_t c = 0; c < C; c++) {
+            if (occupied[c]) origin.push_back(c);
+        }
+        uint32_t *d_origin = nullptr;
+        if (!origin.empty()) {
+            BCUDA(cudaMalloc(&d_origin, origin.size() * sizeof(uint32_t)));
+            BCUDA(cudaMemcpyAsync(d_origin, origin.data(), origin.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+        }
+        const int le = qhg_launch_ms_fill(c0, c0 + C, b->ms_mode, d_origin, (uint32_t)origin.size(), b->d_ms_hops,
+                                          b->d_ms_dist, b->d_ms_time, b->d_ms_chops, b->d_ms_cdist, b->d_ms_ckey,
+                                          b->d_ms_D, st);
+        if (le == 0 && d_origin != nullptr) {
+            BCUDA(cudaStreamSynchronize(st));
+        }
+        cudaFree(d_origin);
+        if (le != 0) return bfail(QHG_ERR_CUDA, std::string("launch: ") + cudaGetErrorString((cudaError_t)le));
     }
     RunSlot &s = b->slots[(size_t)r];
     s.used = true;
@@ -997,6 +1033,76 @@ extern "C" int qhg_batch_set_ice(qhg_batch *b, int32_t run, const uint8_t *ice) 
     return refresh_run(b, *s);
 }
 
+// --------------------------------------------------------------- MoveStats
+extern "C" int qhg_batch_move_stats_enable(qhg_batch *b, int32_t mode, double radius, int32_t cartesian) {
+    if (b == nullptr) return bfail(QHG_ERR_ARG, "null batch");
+    if (mode < QHG_MOVESTATS_FIRST || mode > QHG_MOVESTATS_LAST) return bfail(QHG_ERR_ARG, "bad MoveStats mode");
+    if (b->ms_mode >= 0) return bfail(QHG_ERR_STATE, "MoveStats is enabled already");
+    for (const RunSlot &s : b->slots) {
+        if (s.used) return bfail(QHG_ERR_STATE, "enable MoveStats before the first run is added");
+    }
+    BCUDA(cudaSetDevice(b->desc.device));
+    const size_t C = (size_t)b->cell_cap;
+    BCUDA(cudaMalloc((void **)&b->d_ms_hops, C * sizeof(int32_t)));
+    BCUDA(cudaMalloc((void **)&b->d_ms_chops, C * sizeof(int32_t)));
+    BCUDA(cudaMalloc((void **)&b->d_ms_dist, C * sizeof(double)));
+    BCUDA(cudaMalloc((void **)&b->d_ms_time, C * sizeof(double)));
+    BCUDA(cudaMalloc((void **)&b->d_ms_D, C * 6 * sizeof(double)));
+    BCUDA(cudaMalloc((void **)&b->d_ms_cdist, C * 8));
+    BCUDA(cudaMalloc((void **)&b->d_ms_ckey, C * 8));
+    const int le = qhg_launch_ms_fill(0u, (uint32_t)C, mode, nullptr, 0u, b->d_ms_hops, b->d_ms_dist, b->d_ms_time,
+                                      b->d_ms_chops, b->d_ms_cdist, b->d_ms_ckey, b->d_ms_D, b->stream);
+    if (le != 0) return bfail(QHG_ERR_CUDA, std::string("launch: ") + cudaGetErrorString((cudaError_t)le));
+    BCUDA(cudaStreamSynchronize(b->stream));
+    b->ms_mode = mode;
+    b->ms_radius = radius;
+    b->ms_cartesian = cartesian != 0;
+    drop_graphs(b);   // the step graphs gain the MoveStats kernels
+    return QHG_OK;
+}
+
+extern "C" int qhg_batch_move_stats_coords(qhg_batch *b, int32_t run, const double *lon, const double *lat) {
+    if (b == nullptr || lon == nullptr || lat == nullptr) return bfail(QHG_ERR_ARG, "null argument");
+    if (b->ms_mode < 0) return bfail(QHG_ERR_STATE, "MoveStats is not enabled");
+    RunSlot *s = nullptr;
+    int rc = env_slot(b, run, &s);
+    if (rc != QHG_OK) return rc;
+    std::vector<int32_t> nbr6;
+    std::vector<uint8_t> nnbr;
+    std::vector<double> K;
+    rc = run_grid(b, *s, nbr6, nnbr, K);
+    if (rc != QHG_OK) return rc;
+    const uint32_t C = s->cell1 - s->cell0;
+    std::vector<double> D((size_t)C * 6, 0.0);
+    for (uint32_t c = 0; c < C; c++) {
+        for (int k = 0; k < (int)nnbr[c]; k++) {
+            const int d = nbr6[(size_t)c * 6 + k];
+            if (d >= 0) D[(size_t)c * 6 + k] = qhg_host_move_distance(lon, lat, b->ms_radius, b->ms_cartesian, (int)c, d);
+        }
+    }
+    BCUDA(cudaMemcpyAsync(b->d_ms_D + (size_t)s->cell0 * 6, D.data(), D.size() * sizeof(double), cudaMemcpyHostToDevice,
+                          b->stream));
+    BCUDA(cudaStreamSynchronize(b->stream));
+    return QHG_OK;
+}
+
+extern "C" int qhg_batch_move_stats(qhg_batch *b, int32_t run, int32_t *hops, double *dist, double *time) {
+    if (b == nullptr || hops == nullptr || dist == nullptr || time == nullptr) return bfail(QHG_ERR_ARG, "null argument");
+    if (b->ms_mode < 0) return bfail(QHG_ERR_STATE, "MoveStats is not enabled");
+    int rc = check_slot(b, run);
+    if (rc != QHG_OK) return rc;
+    BCUDA(cudaSetDevice(b->desc.device));
+    rc = pull_state(b);
+    if (rc != QHG_OK) return rc;
+    const RunSlot &s = b->slots[(size_t)run];
+    const size_t C = (size_t)(s.cell1 - s.cell0);
+    BCUDA(cudaMemcpyAsync(hops, b->d_ms_hops + s.cell0, C * sizeof(int32_t), cudaMemcpyDeviceToHost, b->stream));
+    BCUDA(cudaMemcpyAsync(dist, b->d_ms_dist + s.cell0, C * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    BCUDA(cudaMemcpyAsync(time, b->d_ms_time + s.cell0, C * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    BCUDA(cudaStreamSynchronize(b->stream));
+    return QHG_OK;
+}
+
 // ------------------------------------------------------ occupation history
 extern "C" int qhg_batch_enable_occupancy(qhg_batch *b) {
     if (b == nullptr) return bfail(QHG_ERR_ARG, "null batch");
@@ -1043,7 +1149,8 @@ extern "C" int qhg_batch_destroy(qhg_batch *b) {
                     b->d_outc, b->d_father, b->d_brank, b->d_clsc, b->d_sbase, b->d_bbase, b->d_bidb,
                     b->d_obase, b->d_tflag, b->d_tagg, b->d_tincl, b->d_runs, b->d_rnext, b->d_rstat,
                     b->d_inj, b->d_sgender, b->d_stage_err, b->d_ibase, b->d_injdone, b->d_cstat, b->d_sid, b->d_sbirth, b->d_sage,
-                    b->d_slastb, b->d_smeta, b->d_scell, b->d_rowcell, b->d_rs, b->d_occ};
+                    b->d_slastb, b->d_smeta, b->d_scell, b->d_rowcell, b->d_rs, b->d_occ, b->d_ms_hops,
+                    b->d_ms_chops, b->d_ms_dist, b->d_ms_time, b->d_ms_D, b->d_ms_cdist, b->d_ms_ckey};
     for (void *p : ptrs) cudaFree(p);
     for (int p = 0; p < 2; p++) {
         cudaFree(b->d_id[p]); cudaFree(b->d_birth[p]); cudaFree(b->d_age[p]); cudaFree(b->d_lastb[p]);

@@ -15,12 +15,18 @@ int qhg_host_grid_tables(int C, const int32_t *nbr6, const uint8_t *nnbr, const 
                          const uint8_t *ice, std::vector<uint32_t> &rev, std::vector<uint64_t> &wthr,
                          std::vector<uint32_t> &cmove, std::string &err);
 void qhg_host_ice_bits(int C, const int32_t *nbr6, const uint8_t *ice, std::vector<uint32_t> &cmove);
+// MoveStats' distance from cell a to cell b (spherdistDeg / cartdist,
+// utils/geomutils.cpp:311-386)
+double qhg_host_move_distance(const double *lon, const double *lat, double radius, bool cartesian, int a, int b);
 int qhg_host_move_tables(int C, const uint8_t *nnbr, const double *W, std::vector<uint64_t> &wthr,
                          std::vector<uint32_t> &cmove, std::string &err);
 
 extern "C" int qhg_launch_refresh_cells(const qhg::StepConst *P, const qhg::RunState *rs, const uint32_t *nonempty,
                                         const uint32_t *ne_start, const double *K, const uint32_t *cmove,
                                         ulonglong2 *vthr, uint32_t *necm, int grid, cudaStream_t stream);
+extern "C" int qhg_launch_ms_fill(uint32_t c0, uint32_t c1, int mode, const uint32_t *origin, uint32_t norigin,
+                                  int32_t *hops, double *dist, double *time, int32_t *chops,
+                                  unsigned long long *cdist, unsigned long long *ckey, double *D, cudaStream_t stream);
 extern "C" int qhg_launch_refresh_cells_batch(const qhg::StepConst *P, const qhg::BatchRun *runs, const uint32_t *crun,
                                               const qhg::RunState *rs, const uint32_t *nonempty,
                                               const uint32_t *ne_start, const double *K, const uint32_t *cmove,

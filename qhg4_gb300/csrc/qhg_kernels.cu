@@ -2576,12 +2576,16 @@ template <int MODE>
 __global__ void __launch_bounds__(256)
 k_ms_merge(const RunState *__restrict__ rs, int C, int32_t *__restrict__ hops, double *__restrict__ dist,
            double *__restrict__ time, int32_t *__restrict__ chops, unsigned long long *__restrict__ cdist,
-           unsigned long long *__restrict__ ckey) {
+           unsigned long long *__restrict__ ckey, const BatchRun *__restrict__ runs,
+           const uint32_t *__restrict__ crun) {
     if (rs->error != 0u) return;
-    const double t = (double)(float)(rs->step - 1);   // the step that made the moves
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) {
         const int32_t ch = chops[c];
         if (ch == INT_MAX) continue;
+        const uint32_t rr = runs != nullptr ? crun[c] : 0u;
+        if (rr == kNoRun) continue;   // a batch cell of no run (never offered a move)
+        // the step that made the moves (a batch's cell: in its run's steps)
+        const double t = (double)(float)(rs->step - 1 - (runs != nullptr ? runs[rr].step0 : 0));
         const double cd = __longlong_as_double((long long)cdist[c]);
         const int32_t h = hops[c];
         if (MODE == kMsLast || h < 0) {
@@ -2595,6 +2599,38 @@ k_ms_merge(const RunState *__restrict__ rs, int C, int32_t *__restrict__ hops, d
         chops[c] = INT_MAX;
         cdist[c] = kMsNoDist;
         ckey[c] = MODE == kMsFirst ? ~0ull : 0ull;
+    }
+}
+
+// MoveStats state of the cells [c0, c1) before any move: no arrival (-1),
+// no candidates, distances zero (k_ms_origins then marks the cells where the
+// population starts: hops, distance and time 0, as the reset of a run alone
+// leaves its occupied cells)
+__global__ void __launch_bounds__(256)
+k_ms_fill(uint32_t c0, uint32_t c1, int mode, int32_t *__restrict__ hops, double *__restrict__ dist, double *__restrict__ time,
+          int32_t *__restrict__ chops, unsigned long long *__restrict__ cdist, unsigned long long *__restrict__ ckey,
+          double *__restrict__ D) {
+    for (uint32_t c = c0 + blockIdx.x * blockDim.x + threadIdx.x; c < c1; c += gridDim.x * blockDim.x) {
+        hops[c] = -1;
+        dist[c] = -1.0;
+        time[c] = -1.0;
+        chops[c] = INT_MAX;
+        cdist[c] = kMsNoDist;
+        ckey[c] = mode == kMsFirst ? ~0ull : 0ull;
+        for (int k = 0; k < 6; k++) D[(size_t)c * 6 + k] = 0.0;
+    }
+}
+
+__global__ void __launch_bounds__(256)
+k_ms_origins(uint32_t c0, uint32_t c1, const uint32_t *__restrict__ origin, uint32_t norigin,
+             int32_t *__restrict__ hops, double *__restrict__ dist, double *__restrict__ time) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < norigin; i += gridDim.x * blockDim.x) {
+        const uint32_t c = c0 + origin[i];
+        if (c < c1) {
+            hops[c] = 0;
+            dist[c] = 0.0;
+            time[c] = 0.0;
+        }
     }
 }
 
@@ -2993,6 +3029,20 @@ extern "C" int qhg_launch_refresh_cells(const qhg::StepConst *P, const qhg::RunS
     return (int)cudaGetLastError();
 }
 
+extern "C" int qhg_launch_ms_fill(uint32_t c0, uint32_t c1, int mode, const uint32_t *origin, uint32_t norigin,
+                                  int32_t *hops, double *dist, double *time, int32_t *chops,
+                                  unsigned long long *cdist, unsigned long long *ckey, double *D, cudaStream_t stream) {
+    if (c1 > c0) {
+        const uint32_t g = std::min<uint32_t>((c1 - c0 + 255u) / 256u, 4096u);
+        qhg::k_ms_fill<<<g, 256, 0, stream>>>(c0, c1, mode, hops, dist, time, chops, cdist, ckey, D);
+    }
+    if (norigin > 0u) {
+        const uint32_t g = std::min<uint32_t>((norigin + 255u) / 256u, 4096u);
+        qhg::k_ms_origins<<<g, 256, 0, stream>>>(c0, c1, origin, norigin, hops, dist, time);
+    }
+    return (int)cudaGetLastError();
+}
+
 extern "C" int qhg_launch_refresh_cells_batch(const qhg::StepConst *P, const qhg::BatchRun *runs, const uint32_t *crun,
                                               const qhg::RunState *rs, const uint32_t *nonempty,
                                               const uint32_t *ne_start, const double *K, const uint32_t *cmove,
@@ -3246,7 +3296,7 @@ static void launch_scan(const StepLaunch &S) {
     const int sitems = S.L.scan_items > 0 ? std::min(S.L.scan_items, 2) : scan_items(P->num_cells);
     const int ntiles = (P->num_cells + kScanThreads * sitems - 1) / (kScanThreads * sitems);
     const int ms_grid = std::max(1, std::min((P->num_cells + 7) / 8, 152 * 16));
-    if (!batch && B->ms_mode >= 0) {
+    if (B->ms_mode >= 0) {
 #define QHG_LAUNCH_MS_PICK(MD, PS)                                                                          \
     k_ms_pick<MD, PS><<<ms_grid, 256, 0, stream>>>(rs, B->nonempty, B->ne_start, B->id, B->outc, B->nbr, B->ms_D, \
                                                   B->ms_hops, B->ms_dist, B->ms_chops, B->ms_cdist, B->ms_ckey)
@@ -3324,11 +3374,12 @@ static void launch_post(const StepLaunch &S, cudaEvent_t *ev) {
                                                                       batch ? BB.runs : nullptr,
                                                                       batch ? BB.crun : nullptr);
     }
-    if (!batch && B->ms_mode >= 0) {
+    if (B->ms_mode >= 0) {
         const int mg = std::max(1, std::min((P->num_cells + 255) / 256, 152 * 8));
 #define QHG_LAUNCH_MS_MERGE(MD)                                                                             \
     k_ms_merge<MD><<<mg, 256, 0, stream>>>(rs, P->num_cells, B->ms_hops, B->ms_dist, B->ms_time, B->ms_chops, \
-                                           B->ms_cdist, B->ms_ckey)
+                                           B->ms_cdist, B->ms_ckey, batch ? BB.runs : nullptr,             \
+                                           batch ? BB.crun : nullptr)
         switch (B->ms_mode) {
         case kMsFirst: QHG_LAUNCH_MS_MERGE(kMsFirst); break;
         case kMsMin: QHG_LAUNCH_MS_MERGE(kMsMin); break;

@@ -42,7 +42,8 @@ EXPORTS = [
     "qhg_host_buffer_alloc", "qhg_host_buffer_free", "qhg_gpu_next_id", "qhg_gpu_set_next_id",
     "qhg_gpu_test_stall_scan", "qhg_gpu_occupancy", "qhg_gpu_set_capacity", "qhg_gpu_set_move_weights", "qhg_gpu_set_ice", "qhg_gpu_stats_async", "qhg_batch_set_launch", "qhg_batch_get_launch",
     "qhg_batch_table_info", "qhg_batch_set_capacity", "qhg_batch_set_move_weights", "qhg_batch_set_ice",
-    "qhg_batch_enable_occupancy", "qhg_batch_occupancy",
+    "qhg_batch_enable_occupancy", "qhg_batch_occupancy", "qhg_batch_move_stats_enable",
+    "qhg_batch_move_stats_coords", "qhg_batch_move_stats",
     "qhg_gpu_move_stats_enable", "qhg_gpu_move_stats", "qhg_gpu_set_move_stats", "qhg_gpu_set_occupancy",
 ]
 
@@ -149,6 +150,9 @@ def load_library(path: str = LIB_PATH):
         "qhg_batch_set_ice": (I, [P, ct.c_int32, P]),
         "qhg_batch_enable_occupancy": (I, [P]),
         "qhg_batch_occupancy": (I, [P, ct.c_int32, P]),
+        "qhg_batch_move_stats_enable": (I, [P, ct.c_int32, ct.c_double, ct.c_int32]),
+        "qhg_batch_move_stats_coords": (I, [P, ct.c_int32, P, P]),
+        "qhg_batch_move_stats": (I, [P, ct.c_int32, P, P, P]),
         "qhg_gpu_move_stats_enable": (I, [P, ct.c_int32, P, P, ct.c_double, ct.c_int32]),
         "qhg_gpu_move_stats": (I, [P, P, P, P]),
         "qhg_gpu_set_move_stats": (I, [P, P, P, P]),

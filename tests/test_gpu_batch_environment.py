@@ -154,3 +154,65 @@ def test_batch_occupancy_needs_enabling_first(gpu_lib):
     with pytest.raises(QhgError):
         b.enable_occupancy()  # a run is in the batch already
     b.close()
+
+
+def spreading_runs(form):
+    """Runs whose agents start in part of their grid and spread out (the
+    large run's actions: OldAgeDeath after WeightedMove, so some movers die
+    in the step of their move)."""
+    cases = []
+    for k in range(3):
+        if form == "sparse":
+            g = terrain_grid(8 + 2 * k, seed=70 + k)
+            a = make_agents(g, 4_000 + 1_000 * k, seed=710 + k, age_max=70.0, proportional_to_K=True)
+            top = np.argsort(-g.K)[:40]
+            a.cell[:] = top[a.id % 40]
+        else:
+            g = uniform_grid(6 + k, 60.0)
+            cap = np.nonzero(g.xyz[:, 2] > 0.6)[0]
+            a = make_agents(g, 35 * len(cap), seed=720 + k, age_max=70.0)
+            a.cell[:] = cap[a.id % len(cap)]
+        cases.append((g, a, config2_actions(b0=0.3, d0=0.03, move_p=0.25 + 0.05 * k), 95 + k))
+    return cases
+
+
+@pytest.mark.parametrize("form", ["sparse", "dense"])
+@pytest.mark.parametrize("mode", [0, 1, 2], ids=["first", "min", "last"])
+def test_batch_move_stats_equal_alone(gpu_lib, form, mode):
+    from helpers import cell_lonlat
+    cases = spreading_runs(form)
+    b = GpuBatch(config2_actions(), agent_capacity=400_000, cell_capacity=4_000, max_runs=3)
+    b.move_stats_enable(mode)
+    ids = []
+    for g, a, acts, seed in cases:
+        r = b.add_run(g, acts, seed, a)
+        b.move_stats_coords(r, *cell_lonlat(g))
+        ids.append(r)
+    b.step(13)
+    for k, r in enumerate(ids):
+        g, a, acts, seed = cases[k]
+        alone = GpuRun(g, acts, seed)
+        alone.load(a)
+        alone.move_stats_enable(mode, *cell_lonlat(g))
+        alone.step(b.steps_done(r))
+        d = table_diff(b.agents(r), alone.agents())
+        assert d is None, f"run {k}: {d}"
+        bh, bd, bt = b.move_stats(r)
+        ah, ad, at = alone.move_stats()
+        assert np.array_equal(bh, ah), f"run {k}: hops differ in {(bh != ah).sum()} cells"
+        assert np.array_equal(bd.view(np.uint64), ad.view(np.uint64)), f"run {k}: distances differ"
+        assert np.array_equal(bt.view(np.uint64), at.view(np.uint64)), f"run {k}: times differ"
+        assert (bh > 0).sum() > 0   # arrivals were recorded
+        alone.close()
+    b.close()
+
+
+def test_batch_move_stats_needs_enabling_first(gpu_lib):
+    g = uniform_grid(6, 30.0)
+    b = GpuBatch(config1_actions(), agent_capacity=100_000, cell_capacity=3_000, max_runs=2)
+    r = b.add_run(g, config1_actions(), 5, make_agents(g, 2_000, seed=5, age_max=50.0))
+    with pytest.raises(QhgError):
+        b.move_stats(r)            # not enabled
+    with pytest.raises(QhgError):
+        b.move_stats_enable(1)     # a run is in the batch already
+    b.close()
