@@ -17,7 +17,8 @@
 //                   picking member and decoded independently), the outcome
 //                   word with each agent's rank in its cell's class, the
 //                   father's row of each mother, the mothers' birth ranks by
-//                   ID and the cells' class counts.
+//                   ID with the newborns' genders (in the mothers' outcome
+//                   words) and the cells' class counts.
 //   k_actions       the same on cell-aligned tiles of ~kTileAgents agents,
 //                   one CTA per tile, everything staged in shared memory.
 //   k_cell_scan     one pass over all cells with a decoupled look-back scan:
@@ -1627,8 +1628,7 @@ k_actions_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                const uint8_t *__restrict__ meta,
                const ulonglong2 *__restrict__ vthr, const uint64_t *__restrict__ wthr,
                const uint32_t *__restrict__ necm,
-               uint32_t *__restrict__ outc, int32_t *__restrict__ father, uint16_t *__restrict__ brank,
-               uint32_t *__restrict__ clsc) {
+               uint32_t *__restrict__ outc, int32_t *__restrict__ father, uint32_t *__restrict__ clsc) {
     extern __shared__ __align__(16) unsigned char qhg_smem[];
     __shared__ uint32_t red[kCellWarps];
     CellWarpSmem &W = reinterpret_cast<CellWarpSmem *>(qhg_smem)[threadIdx.x >> 5];
@@ -2174,7 +2174,6 @@ k_scatter_cell(const StepConst P, const BatchBuffers BB, RunState *__restrict__ 
                const int64_t *__restrict__ id, const float *__restrict__ birth,
                const float *__restrict__ age, const float *__restrict__ lastb,
                const uint32_t *__restrict__ outc, const int32_t *__restrict__ father,
-               const uint16_t *__restrict__ brank,
                const uint32_t *__restrict__ sbase, const uint32_t *__restrict__ bbase,
                const uint32_t *__restrict__ bidbase, const uint32_t *__restrict__ obase,
                uint32_t *__restrict__ clsc,
@@ -3259,7 +3258,7 @@ static void launch_actions(const StepLaunch &S, int form) {
 #define QHG_LAUNCH_CELL(PR, BT)                                                                            \
     k_actions_cell<PR, BT><<<(PR > 0 ? CG.actions : CG.actions0), kCellThreads, kSmC, stream>>>(            \
         *P, BB, rs, B->nonempty, B->ne_start, B->id, B->birth, B->age, B->lastb, B->meta, B->vthr, B->wthr, \
-        B->necm, B->outc, B->father, B->brank, B->clsc)
+        B->necm, B->outc, B->father, B->clsc)
 #define QHG_FORMS(PR, BT)                                                      \
     do {                                                                       \
         if (tile) QHG_LAUNCH_ACTIONS(PR, BT, false, L.actions_grid, kSmA);     \
@@ -3345,7 +3344,7 @@ static void launch_scatter(const StepLaunch &S, int form) {
 #define QHG_LAUNCH_SCATTER_CELL(BT)                                                                        \
     k_scatter_cell<BT><<<CG.scatter[BT ? 1 : 0], kCellThreads, kSmSC, stream>>>(                             \
         *P, BB, rs, B->nonempty, B->ne_start, B->id, B->birth, B->age, B->lastb, B->outc, B->father,       \
-        B->brank, B->sbase, B->bbase, B->bidbase, B->obase, B->clsc, B->id2, B->birth2, B->age2, B->lastb2, \
+        B->sbase, B->bbase, B->bidbase, B->obase, B->clsc, B->id2, B->birth2, B->age2, B->lastb2,          \
         B->meta2, B->blog, B->blog_cap, B->gslot, B->gslot2, B->freelist, B->freelist2, B->brec)
     if (batch) {
         if (tile) QHG_LAUNCH_SCATTER(true, false, L.scatter_grid, kSmS);
