@@ -323,7 +323,8 @@ def run_reference(args, world, rank, dist):
     v = n_as / dt
     sample = (f"all {steps} timed step(s) after {warm} warm-up step(s) of the full {w.name} workload "
               f"({len(w.agents)} initial agents) on the C port of the reference algorithm "
-              f"(oracle/qhg_oracle.c, OpenMP, {thr} threads)")
+              f"(oracle/qhg_oracle.c, OpenMP, {thr} threads); the port runs {PORT_VS_REFERENCE} "
+              f"the reference's own OpenMP code built from its sources")
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "agent-steps/s", "n_gpus": args.gpus,
         "steps": steps, "warmup": warm, "ms_per_step": 1000.0 * dt / steps, "higher_is_better": True,
