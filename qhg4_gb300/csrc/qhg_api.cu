@@ -647,6 +647,22 @@ static void ms_free(qhg_run *r);
 
 static const uint8_t *ice_ptr(const qhg_run *r) { return r->h_ice.empty() ? nullptr : r->h_ice.data(); }
 
+// The grid's neighbour table, neighbour counts and K as host copies, for the
+// updates between steps that rebuild tables on the host (fetched from the
+// device on first use: the upload keeps none)
+static int host_grid(qhg_run *r) {
+    if (!r->h_nbr.empty()) return QHG_OK;
+    const size_t C = (size_t)r->C;
+    r->h_nbr.resize(C * 6);
+    r->h_nnbr.resize(C);
+    r->h_K.resize(C);
+    CUDA_TRY(cudaMemcpyAsync(r->h_nbr.data(), r->d_nbr, C * 6 * sizeof(int32_t), cudaMemcpyDeviceToHost, r->stream));
+    CUDA_TRY(cudaMemcpyAsync(r->h_nnbr.data(), r->d_nnbr, C, cudaMemcpyDeviceToHost, r->stream));
+    CUDA_TRY(cudaMemcpyAsync(r->h_K.data(), r->d_K, C * sizeof(double), cudaMemcpyDeviceToHost, r->stream));
+    CUDA_TRY(cudaStreamSynchronize(r->stream));
+    return QHG_OK;
+}
+
 extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_t *nnbr, const double *K,
                                    int32_t num_cells) {
     if (r == nullptr || nbr6 == nullptr || nnbr == nullptr || K == nullptr || num_cells <= 0) {
@@ -654,37 +670,85 @@ extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_
     }
     CUDA_TRY(cudaSetDevice(r->desc.device));
     const int C = num_cells;
-    std::vector<uint32_t> rev;
-    std::vector<uint64_t> wthr;
-    std::vector<uint32_t> cmove;
-    {
-        std::string err;
-        if (qhg_host_grid_tables(C, nbr6, nnbr, K, r->P.has_wmove != 0, nullptr, rev, wthr, cmove, err) != 0) {
-            return fail(QHG_ERR_ARG, err);
+    cudaStream_t st = r->stream;
+    // the grid tables are built on the device in new buffers; a grid that is
+    // rejected leaves the run as it was
+    int32_t *n_nbr = nullptr;
+    uint8_t *n_nnbr = nullptr;
+    double *n_K = nullptr, *tW = nullptr;
+    uint32_t *n_rev = nullptr, *n_cmove = nullptr;
+    uint64_t *n_wthr = nullptr;
+    unsigned long long *d_bad = nullptr;
+    auto release = [&]() {
+        cudaFree(n_nbr); cudaFree(n_nnbr); cudaFree(n_K); cudaFree(n_rev); cudaFree(n_cmove); cudaFree(n_wthr);
+        cudaFree(tW); cudaFree(d_bad);
+    };
+    const bool wm = r->P.has_wmove != 0;
+    cudaError_t e = cudaMalloc(&n_nbr, (size_t)C * 6 * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&n_nnbr, (size_t)C);
+    if (e == cudaSuccess) e = cudaMalloc(&n_K, (size_t)C * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&n_rev, (size_t)C * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&n_cmove, (size_t)C * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&n_wthr, (size_t)C * 6 * sizeof(uint64_t));
+    if (e == cudaSuccess && wm) e = cudaMalloc(&tW, (size_t)C * 7 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&d_bad, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(n_nbr, nbr6, (size_t)C * 6 * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(n_nnbr, nnbr, (size_t)C, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(n_K, K, (size_t)C * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_bad, 0xff, sizeof(unsigned long long), st);
+    if (e == cudaSuccess && !wm) e = cudaMemsetAsync(n_wthr, 0, (size_t)C * 6 * sizeof(uint64_t), st);
+    if (e != cudaSuccess) {
+        release();
+        return fail(e == cudaErrorMemoryAllocation ? QHG_ERR_NOMEM : QHG_ERR_CUDA, cudaGetErrorString(e));
+    }
+    unsigned long long bad = ~0ull;
+    for (int pass = 0; pass < (wm ? 2 : 1); pass++) {
+        // the weights' pass reads neighbours' rows: only over a valid table
+        int le = qhg_launch_grid_tables(C, n_nbr, n_nnbr, n_K, wm ? 1 : 0, n_rev, n_cmove, tW, n_wthr, d_bad, pass, st);
+        cudaError_t ce = le == 0 ? cudaMemcpyAsync(&bad, d_bad, sizeof(bad), cudaMemcpyDeviceToHost, st) : (cudaError_t)le;
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+        if (ce != cudaSuccess) {
+            release();
+            return fail(QHG_ERR_CUDA, std::string("grid tables: ") + cudaGetErrorString(ce));
+        }
+        if (bad != ~0ull) {
+            release();
+            const unsigned long long cell = bad >> 8;
+            switch ((int)(bad & 0xffull)) {
+            case 1: return fail(QHG_ERR_ARG, "more than 6 neighbours");
+            case 2: return fail(QHG_ERR_ARG, "neighbour index out of range");
+            case 3: return fail(QHG_ERR_ARG, "neighbour table is not symmetric");
+            case 4: return fail(QHG_ERR_ARG, "cell " + std::to_string(cell) + ": total move weight not positive and finite");
+            default: return fail(QHG_ERR_ARG, "cell " + std::to_string(cell) + ": move weight not finite");
+            }
         }
     }
+    cudaFree(tW);
+    tW = nullptr;
+    cudaFree(d_bad);
+    d_bad = nullptr;
     cudaFree(r->d_nbr); cudaFree(r->d_nnbr); cudaFree(r->d_rev); cudaFree(r->d_K); cudaFree(r->d_vthr[0]); cudaFree(r->d_vthr[1]);
     cudaFree(r->d_wthr); cudaFree(r->d_cmove); cudaFree(r->d_occ);
     cudaFree(r->d_clsc); cudaFree(r->d_sbase); cudaFree(r->d_bbase); cudaFree(r->d_bidb);
     cudaFree(r->d_obase); cudaFree(r->d_tflag); cudaFree(r->d_tagg); cudaFree(r->d_tincl);
     ms_free(r);
+    r->d_nbr = n_nbr;
+    r->d_nnbr = n_nnbr;
+    r->d_K = n_K;
+    r->d_rev = n_rev;
+    r->d_cmove = n_cmove;
+    r->d_wthr = n_wthr;
     r->d_vthr[0] = r->d_vthr[1] = nullptr;
     r->d_occ = nullptr;
     r->grid_ok = false;
     r->agents_ok = false;
     drop_graphs(r);
     const int ntiles = (C + kScanTile - 1) / kScanTile;
-    CUDA_TRY(cudaMalloc(&r->d_nbr, (size_t)C * 6 * sizeof(int32_t)));
-    CUDA_TRY(cudaMalloc(&r->d_nnbr, (size_t)C));
-    CUDA_TRY(cudaMalloc(&r->d_rev, (size_t)C * sizeof(uint32_t)));
-    CUDA_TRY(cudaMalloc(&r->d_K, (size_t)C * sizeof(double)));
     CUDA_TRY(cudaMalloc(&r->d_vthr[0], (size_t)C * sizeof(ulonglong2)));
     CUDA_TRY(cudaMalloc(&r->d_vthr[1], (size_t)C * sizeof(ulonglong2)));
-    CUDA_TRY(cudaMalloc(&r->d_wthr, (size_t)C * 6 * sizeof(uint64_t)));
-    CUDA_TRY(cudaMalloc(&r->d_cmove, (size_t)C * sizeof(uint32_t)));
     if (r->desc.flags & QHG_FLAG_TRACK_OCCUPANCY) {
         CUDA_TRY(cudaMalloc(&r->d_occ, (size_t)C * sizeof(int32_t)));
-        CUDA_TRY(cudaMemsetAsync(r->d_occ, 0xff, (size_t)C * sizeof(int32_t), r->stream));
+        CUDA_TRY(cudaMemsetAsync(r->d_occ, 0xff, (size_t)C * sizeof(int32_t), st));
     }
     CUDA_TRY(cudaMalloc(&r->d_clsc, (size_t)C * kCls * sizeof(uint32_t)));
     CUDA_TRY(cudaMalloc(&r->d_sbase, (size_t)C * sizeof(uint32_t)));
@@ -694,18 +758,13 @@ extern "C" int qhg_gpu_upload_grid(qhg_run *r, const int32_t *nbr6, const uint8_
     CUDA_TRY(cudaMalloc(&r->d_tflag, (size_t)ntiles * sizeof(uint32_t)));
     CUDA_TRY(cudaMalloc(&r->d_tagg, (size_t)ntiles * sizeof(uint4)));
     CUDA_TRY(cudaMalloc(&r->d_tincl, (size_t)ntiles * sizeof(uint4)));
-    CUDA_TRY(cudaMemcpyAsync(r->d_nbr, nbr6, (size_t)C * 6 * sizeof(int32_t), cudaMemcpyHostToDevice, r->stream));
-    CUDA_TRY(cudaMemcpyAsync(r->d_nnbr, nnbr, (size_t)C, cudaMemcpyHostToDevice, r->stream));
-    CUDA_TRY(cudaMemcpyAsync(r->d_rev, rev.data(), (size_t)C * sizeof(uint32_t), cudaMemcpyHostToDevice, r->stream));
-    CUDA_TRY(cudaMemsetAsync(r->d_clsc, 0, (size_t)C * kCls * sizeof(uint32_t), r->stream));
-    CUDA_TRY(cudaMemcpyAsync(r->d_K, K, (size_t)C * sizeof(double), cudaMemcpyHostToDevice, r->stream));
-    CUDA_TRY(cudaMemcpyAsync(r->d_wthr, wthr.data(), (size_t)C * 6 * sizeof(uint64_t), cudaMemcpyHostToDevice, r->stream));
-    CUDA_TRY(cudaMemcpyAsync(r->d_cmove, cmove.data(), (size_t)C * sizeof(uint32_t), cudaMemcpyHostToDevice, r->stream));
-    CUDA_TRY(cudaMemsetAsync(r->d_tflag, 0, (size_t)ntiles * sizeof(uint32_t), r->stream));
-    CUDA_TRY(cudaStreamSynchronize(r->stream));
-    r->h_nbr.assign(nbr6, nbr6 + (size_t)C * 6);
-    r->h_nnbr.assign(nnbr, nnbr + C);
-    r->h_K.assign(K, K + C);
+    CUDA_TRY(cudaMemsetAsync(r->d_clsc, 0, (size_t)C * kCls * sizeof(uint32_t), st));
+    CUDA_TRY(cudaMemsetAsync(r->d_tflag, 0, (size_t)ntiles * sizeof(uint32_t), st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    // host copies of the grid are fetched when an update needs them
+    r->h_nbr.clear();
+    r->h_nnbr.clear();
+    r->h_K.clear();
     r->w_given = false;
     r->h_ice.clear();
     r->C = C;
@@ -1029,6 +1088,10 @@ extern "C" int qhg_gpu_set_capacity(qhg_run *r, const double *K) {
     if (r == nullptr || K == nullptr) return fail(QHG_ERR_ARG, "null argument");
     if (!r->grid_ok) return fail(QHG_ERR_STATE, "upload the grid first");
     CUDA_TRY(cudaSetDevice(r->desc.device));
+    {
+        const int hg = host_grid(r);   // the grid's host copies (fetched once)
+        if (hg != QHG_OK) return hg;
+    }
     const int C = r->C;
     // weights that follow K are derived again, as an always-updating
     // SingleEvaluator over K does at the next initialize
@@ -1058,6 +1121,10 @@ extern "C" int qhg_gpu_set_move_weights(qhg_run *r, const double *cumw7) {
     if (r == nullptr || cumw7 == nullptr) return fail(QHG_ERR_ARG, "null argument");
     if (!r->grid_ok) return fail(QHG_ERR_STATE, "upload the grid first");
     CUDA_TRY(cudaSetDevice(r->desc.device));
+    {
+        const int hg = host_grid(r);   // the grid's host copies (fetched once)
+        if (hg != QHG_OK) return hg;
+    }
     const int C = r->C;
     std::vector<uint32_t> rev, cmove;
     std::vector<uint64_t> wthr;
@@ -1084,6 +1151,10 @@ extern "C" int qhg_gpu_set_ice(qhg_run *r, const uint8_t *ice) {
     if (r == nullptr) return fail(QHG_ERR_ARG, "null run");
     if (!r->grid_ok) return fail(QHG_ERR_STATE, "upload the grid first");
     CUDA_TRY(cudaSetDevice(r->desc.device));
+    {
+        const int hg = host_grid(r);   // the grid's host copies (fetched once)
+        if (hg != QHG_OK) return hg;
+    }
     const int C = r->C;
     std::vector<uint8_t> flags;
     if (ice != nullptr) {
@@ -1202,6 +1273,10 @@ extern "C" int qhg_gpu_move_stats_enable(qhg_run *r, int32_t mode, const double 
     if (mode < QHG_MOVESTATS_FIRST || mode > QHG_MOVESTATS_LAST) return fail(QHG_ERR_ARG, "bad MoveStats mode");
     if (!r->grid_ok) return fail(QHG_ERR_STATE, "upload the grid first");
     CUDA_TRY(cudaSetDevice(r->desc.device));
+    {
+        const int hg = host_grid(r);   // the grid's host copies (fetched once)
+        if (hg != QHG_OK) return hg;
+    }
     int rc = pull_state(r);
     if (rc != QHG_OK) return rc;
     const int C = r->C;

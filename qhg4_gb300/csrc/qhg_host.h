@@ -27,6 +27,9 @@ extern "C" int qhg_launch_refresh_cells(const qhg::StepConst *P, const qhg::RunS
 extern "C" int qhg_launch_ms_fill(uint32_t c0, uint32_t c1, int mode, const uint32_t *origin, uint32_t norigin,
                                   int32_t *hops, double *dist, double *time, int32_t *chops,
                                   unsigned long long *cdist, unsigned long long *ckey, double *D, cudaStream_t stream);
+extern "C" int qhg_launch_grid_tables(int C, const int32_t *nbr6, const uint8_t *nnbr, const double *K, int wm,
+                                      uint32_t *rev, uint32_t *cmove, double *W, uint64_t *wthr,
+                                      unsigned long long *bad, int pass, cudaStream_t stream);
 extern "C" int qhg_launch_refresh_cells_batch(const qhg::StepConst *P, const qhg::BatchRun *runs, const uint32_t *crun,
                                               const qhg::RunState *rs, const uint32_t *nonempty,
                                               const uint32_t *ne_start, const double *K, const uint32_t *cmove,

@@ -2907,6 +2907,105 @@ k_refresh_cells(const StepConst P, const BatchRun *__restrict__ runs, const uint
     }
 }
 
+// ------------------------------------------------------------ grid tables
+// The grid tables of a run built on the device at qhg_gpu_upload_grid, the
+// same as qhg_host_grid_tables / qhg_host_move_tables build on the host
+// (which serve the batch form and the updates between steps): per cell the
+// reverse slots (3 bits per neighbour slot: the cell's slot in the
+// neighbour's list), the move word (neighbour count, slots holding a
+// neighbour, slots a WeightedMove may enter) and SingleEvaluator's own
+// weight (actions/SingleEvaluator.cpp:174-241); then the cumulative weights
+// and WeightedMove's integer thresholds.  A cell that fails records
+// (cell << 8 | problem) in *bad (the smallest wins): 1 more than 6
+// neighbours, 2 a neighbour index out of range, 3 a link without its
+// reverse, 4 a total weight not positive and finite, 5 a weight not finite.
+__global__ void __launch_bounds__(256)
+k_grid_cells(int C, const int32_t *__restrict__ nbr6, const uint8_t *__restrict__ nnbr,
+             const double *__restrict__ K, int wm, uint32_t *__restrict__ rev, uint32_t *__restrict__ cmove,
+             double *__restrict__ W, unsigned long long *__restrict__ bad) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) {
+        const int nn = nnbr[c];
+        uint32_t why = nn > 6 ? 1u : 0u, rv = 0u, vm = 0u;
+        for (int j = 0; j < 6 && why == 0u; j++) {
+            const int d = nbr6[(size_t)c * 6 + j];
+            if (d >= C || d < -1) {
+                why = 2u;
+                break;
+            }
+            if (d >= 0) vm |= 1u << j;
+            if (j >= nn || d < 0) continue;
+            int k = -1;
+            for (int q = 0; q < (int)nnbr[d] && q < 6; q++) {
+                if (nbr6[(size_t)d * 6 + q] == c) {
+                    k = q;
+                    break;
+                }
+            }
+            if (k < 0) why = 3u;
+            else rv |= (uint32_t)k << (3 * j);
+        }
+        if (why != 0u) {
+            atomicMin(bad, ((unsigned long long)c << 8) | why);
+            continue;
+        }
+        rev[c] = rv;
+        // no ice at the upload: every slot holding a neighbour may be entered
+        cmove[c] = (uint32_t)nn | (vm << 8) | (vm << 24);
+        if (wm) W[(size_t)c * 7] = K[c] > 0.0 ? K[c] : 0.0;
+    }
+}
+
+__global__ void __launch_bounds__(256)
+k_grid_weights(int C, const int32_t *__restrict__ nbr6, const uint8_t *__restrict__ nnbr, double *__restrict__ W,
+               uint64_t *__restrict__ wthr, uint32_t *__restrict__ cmove, unsigned long long *__restrict__ bad) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) {
+        // cumulative weights: W[c][i+1] = W[c][i] + max(0, neighbour i's own weight)
+        double row[7];
+        row[0] = W[(size_t)c * 7];
+        double dW = row[0];
+        for (int i = 0; i < 6; i++) {
+            const int ni = nbr6[(size_t)c * 6 + i];
+            double dCW = ni >= 0 ? W[(size_t)ni * 7] : 0.0;
+            dCW = dCW > 0.0 ? dCW : 0.0;
+            dW = __dadd_rn(dW, dCW);
+            row[i + 1] = dW;
+        }
+        for (int i = 1; i < 7; i++) W[(size_t)c * 7 + i] = row[i];
+        // thresholds: the smallest draw u with wrandd() * W[n] >= W[j]
+        // (u / 2^32 is exact, so it is u * 2^-32), as a running maximum
+        const int nn = nnbr[c];
+        const double Wn = row[nn];
+        uint32_t cm = cmove[c] & ~(1u << 16);
+        uint64_t *wt = wthr + (size_t)c * 6;
+        if (row[0] == Wn) {
+            cm |= 1u << 16;
+            for (int j = 0; j < 6; j++) wt[j] = 0ull;
+        } else if (!(Wn > 0.0) || !isfinite(Wn)) {
+            atomicMin(bad, ((unsigned long long)c << 8) | 4u);
+        } else {
+            const double guess = __ddiv_rn(4294967296.0, Wn);   // where the search starts
+            uint64_t run = 0ull;
+            bool ok = true;
+            for (int j = 0; j < nn; j++) {
+                const double x = row[j];
+                if (!isfinite(x)) {
+                    ok = false;
+                    break;
+                }
+                const double g = floor(__dmul_rn(x, guess));
+                uint64_t u = (g <= 0.0) ? 0ull : (g >= 4294967296.0 ? 4294967296ull : (uint64_t)g);
+                while (u > 0ull && __dmul_rn((double)(u - 1ull) * 0x1p-32, Wn) >= x) u--;
+                while (u < 4294967296ull && __dmul_rn((double)u * 0x1p-32, Wn) < x) u++;
+                run = max(run, u);
+                wt[j] = run;
+            }
+            if (!ok) atomicMin(bad, ((unsigned long long)c << 8) | 5u);
+            for (int j = nn; j < 6; j++) wt[j] = 4294967296ull;
+        }
+        cmove[c] = cm;
+    }
+}
+
 // ------------------------------------------------------------------ upload
 // An upload on the device: the caller's columns are copied as they are into
 // staging buffers; k_upload_count counts the live agents of each cell (into
@@ -3039,6 +3138,15 @@ extern "C" int qhg_launch_ms_fill(uint32_t c0, uint32_t c1, int mode, const uint
         const uint32_t g = std::min<uint32_t>((norigin + 255u) / 256u, 4096u);
         qhg::k_ms_origins<<<g, 256, 0, stream>>>(c0, c1, origin, norigin, hops, dist, time);
     }
+    return (int)cudaGetLastError();
+}
+
+extern "C" int qhg_launch_grid_tables(int C, const int32_t *nbr6, const uint8_t *nnbr, const double *K, int wm,
+                                      uint32_t *rev, uint32_t *cmove, double *W, uint64_t *wthr,
+                                      unsigned long long *bad, int pass, cudaStream_t stream) {
+    const int g = std::max(1, std::min((C + 255) / 256, 152 * 16));
+    if (pass == 0) qhg::k_grid_cells<<<g, 256, 0, stream>>>(C, nbr6, nnbr, K, wm, rev, cmove, W, bad);
+    else qhg::k_grid_weights<<<g, 256, 0, stream>>>(C, nbr6, nnbr, W, wthr, cmove, bad);
     return (int)cudaGetLastError();
 }
 
